@@ -1,0 +1,213 @@
+"""ctypes binding of libcmgpu.so, the C ABI declared in include/cmgpu.h.
+
+The shared library is the only compute path of this package: if it cannot be
+loaded (not built, or no CUDA driver), every entry point that needs it raises
+``NativeUnavailable``.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+CM_API_VERSION = 1
+CM_OK, CM_EINVAL, CM_ENOMEM, CM_ECUDA, CM_EDEVICE, CM_ESTATE = range(6)
+CM_MODE_MDDF, CM_MODE_COORDINATION_NUMBER = 0, 1
+CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
+CM_REGIME_AUTO, CM_REGIME_PAIRS, CM_REGIME_ATOMS = 0, 1, 2
+CM_COORD_F64, CM_COORD_F32 = 0, 1
+CM_MEM_HOST, CM_MEM_DEVICE = 0, 1
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libcmgpu.so")
+
+
+class NativeUnavailable(RuntimeError):
+    """The CUDA engine library is missing or cannot be loaded."""
+
+
+class cm_system_desc(C.Structure):
+    _fields_ = [
+        ("api_version", C.c_int32),
+        ("solute_nmols", C.c_int32),
+        ("solute_natomspermol", C.c_int32),
+        ("solvent_nmols", C.c_int32),
+        ("solvent_natomspermol", C.c_int32),
+        ("autocorrelation", C.c_int32),
+        ("irefatom", C.c_int32),
+        ("cutoff", C.c_double),
+        ("binstep", C.c_double),
+        ("dbulk", C.c_double),
+        ("usecutoff", C.c_int32),
+        ("nbins", C.c_int32),
+        ("n_random_samples", C.c_int32),
+        ("lcell", C.c_int32),
+        ("mode", C.c_int32),
+        ("precision", C.c_int32),
+        ("regime", C.c_int32),
+        ("seed", C.c_uint64),
+        ("solute_ngroups", C.c_int32),
+        ("solute_group_offsets", C.POINTER(C.c_int64)),
+        ("solute_groups", C.POINTER(C.c_int32)),
+        ("solvent_ngroups", C.c_int32),
+        ("solvent_group_offsets", C.POINTER(C.c_int64)),
+        ("solvent_groups", C.POINTER(C.c_int32)),
+        ("device", C.c_int32),
+        ("max_frames_per_batch", C.c_int32),
+        ("hbm_budget_bytes", C.c_int64),
+    ]
+
+
+class cm_frames(C.Structure):
+    _fields_ = [
+        ("nframes", C.c_int32),
+        ("coord_type", C.c_int32),
+        ("memory", C.c_int32),
+        ("reserved", C.c_int32),
+        ("solute_xyz", C.c_void_p),
+        ("solvent_xyz", C.c_void_p),
+        ("cells", C.POINTER(C.c_double)),
+        ("weights", C.POINTER(C.c_double)),
+        ("frame_ids", C.POINTER(C.c_int64)),
+    ]
+
+
+_DP = C.POINTER(C.c_double)
+_LP = C.POINTER(C.c_int64)
+
+
+class cm_counts(C.Structure):
+    _fields_ = [
+        ("md_count", _DP),
+        ("md_count_random", _DP),
+        ("rdf_count", _DP),
+        ("rdf_count_random", _DP),
+        ("solute_group_count", _DP),
+        ("solute_group_count_random", _DP),
+        ("solvent_group_count", _DP),
+        ("solvent_group_count_random", _DP),
+        ("volume_total", C.c_double),
+        ("weight_total", C.c_double),
+        ("frames", C.c_int64),
+    ]
+
+
+class cm_raw_counts(C.Structure):
+    _fields_ = [
+        ("md", _LP),
+        ("md_random", _LP),
+        ("rdf", _LP),
+        ("rdf_random", _LP),
+        ("solute_group", _LP),
+        ("solute_group_random", _LP),
+        ("solvent_group", _LP),
+        ("solvent_group_random", _LP),
+    ]
+
+
+class cm_stats(C.Structure):
+    _fields_ = [
+        ("frames", C.c_int64),
+        ("molecule_pairs_evaluated", C.c_int64),
+        ("atom_pairs_evaluated", C.c_int64),
+        ("hits_real", C.c_int64),
+        ("hits_random", C.c_int64),
+        ("guard_reevaluations", C.c_int64),
+        ("guard_pair_evaluations", C.c_int64),
+        ("max_guard_error", C.c_double),
+        ("guard_band", C.c_double),
+        ("regime", C.c_int32),
+        ("kernels_per_frame", C.c_int32),
+    ]
+
+
+EXPORTED = (
+    "cm_create",
+    "cm_submit_frames",
+    "cm_synchronize",
+    "cm_read_counts",
+    "cm_read_raw_counts",
+    "cm_get_stats",
+    "cm_reset",
+    "cm_destroy",
+    "cm_last_error",
+    "cm_status_string",
+    "cm_device_bytes",
+    "cm_stream",
+)
+
+_lib: Optional[C.CDLL] = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load libcmgpu.so and declare the prototypes of include/cmgpu.h."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise NativeUnavailable(
+            f"{path} not found: build the CUDA engine first (python -c 'import __graft_entry__ as g; g.build()')"
+        )
+    try:
+        lib = C.CDLL(path)
+    except OSError as e:  # missing libcudart / driver
+        raise NativeUnavailable(f"cannot load {path}: {e}") from e
+    H = C.c_void_p
+    lib.cm_create.argtypes = [C.POINTER(cm_system_desc), C.POINTER(H)]
+    lib.cm_create.restype = C.c_int
+    lib.cm_submit_frames.argtypes = [H, C.POINTER(cm_frames)]
+    lib.cm_submit_frames.restype = C.c_int
+    lib.cm_synchronize.argtypes = [H]
+    lib.cm_synchronize.restype = C.c_int
+    lib.cm_read_counts.argtypes = [H, C.POINTER(cm_counts)]
+    lib.cm_read_counts.restype = C.c_int
+    lib.cm_read_raw_counts.argtypes = [H, C.POINTER(cm_raw_counts)]
+    lib.cm_read_raw_counts.restype = C.c_int
+    lib.cm_get_stats.argtypes = [H, C.POINTER(cm_stats)]
+    lib.cm_get_stats.restype = C.c_int
+    lib.cm_reset.argtypes = [H]
+    lib.cm_reset.restype = C.c_int
+    lib.cm_destroy.argtypes = [H]
+    lib.cm_destroy.restype = C.c_int
+    lib.cm_last_error.argtypes = [H]
+    lib.cm_last_error.restype = C.c_char_p
+    lib.cm_status_string.argtypes = [C.c_int]
+    lib.cm_status_string.restype = C.c_char_p
+    lib.cm_device_bytes.argtypes = [H]
+    lib.cm_device_bytes.restype = C.c_int64
+    lib.cm_stream.argtypes = [H]
+    lib.cm_stream.restype = C.c_void_p
+    _lib = lib
+    return lib
+
+
+def raise_for(status: int, handle) -> None:
+    """Turn a cm_status into the exception the reference raises for it."""
+    if status == CM_OK:
+        return
+    lib = load()
+    msg = lib.cm_last_error(handle).decode(errors="replace")
+    what = lib.cm_status_string(status).decode()
+    text = f"{what}: {msg}" if msg else what
+    if status == CM_EINVAL:
+        raise ValueError(text)
+    if status == CM_ENOMEM:
+        raise MemoryError(text)
+    raise RuntimeError(text)
+
+
+def csr(rows, nrows: int):
+    """(offsets int64[nrows+1], values int32[]) from a list of int sequences."""
+    off = np.zeros(nrows + 1, dtype=np.int64)
+    vals = []
+    for i in range(nrows):
+        r = rows[i]
+        off[i + 1] = off[i] + len(r)
+        vals.extend(int(g) for g in r)
+    return off, np.asarray(vals if vals else [0], dtype=np.int32)
+
+
+def as_ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))

@@ -1,0 +1,120 @@
+// cm_geom.h -- unit-cell geometry shared by the host planner and the kernels.
+//
+// Positions are binned on a grid in fractional coordinates: with f = Hinv x
+// wrapped into [0, 1), the cell along axis k is c_k = floor(f_k n_k) and the
+// position inside the cell is g_k = f_k n_k - c_k in [0, 1).  A site is then
+// stored as its cell index and q = Hn g, its offset from the cell origin
+// (Hn = H diag(1/n) holds the three cell edge vectors).  The displacement from
+// a site in cell c to a site in cell c + Delta (Delta unwrapped, so it carries
+// the periodic image) is q' - q + Hn Delta.  Hn Delta is tabulated per frame,
+// so the single-precision search never works with coordinates larger than a
+// few cells, whatever the size of the box.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#include "cm_feed.h"
+
+namespace cmgeom {
+
+// Four doubles, 32-byte aligned: one vector load per site.
+struct alignas(32) d4 {
+    double x, y, z, w;
+};
+CM_HD d4 make_d4(double x, double y, double z, double w) {
+    d4 r;
+    r.x = x; r.y = y; r.z = z; r.w = w;
+    return r;
+}
+
+// Largest stencil half-width the per-frame offset table covers.
+constexpr int kLT = 6;
+constexpr int kLTW = 2 * kLT + 1;
+constexpr int kOffEntries = kLTW * kLTW * kLTW;
+
+struct FrameGeom {
+    double H[9];      // column-major: H[0..2] = a, H[3..5] = b, H[6..8] = c
+    double Hi[9];     // row-major inverse
+    double Hn[9];     // column-major cell edge vectors: column k = H column k / n_k
+    double det;       // dot(cross(a, b), c)  (src/mddf.jl:350-351)
+    double w[3];      // perpendicular widths of the cell
+    double cw[3];     // perpendicular widths of one grid cell (w / n)
+    double weight;
+    int64_t frame_id;
+    int n[3];
+    int ncell;
+    int sample_off;   // offset of this frame's random samples
+    int nsamples;     // random samples this frame (0 in coordination-number mode)
+    int ndistinct;    // distinct sampled solute molecules
+    int pad;
+};
+
+using cmfeed::add;
+using cmfeed::mul;
+using cmfeed::sub;
+
+// v = M x for column-major M: v_k = (M[k] x0 + M[3+k] x1) + M[6+k] x2
+CM_HD void matvec_cm(const double *M, double x0, double x1, double x2, double *v) {
+    for (int k = 0; k < 3; ++k) v[k] = add(add(mul(M[k], x0), mul(M[3 + k], x1)), mul(M[6 + k], x2));
+}
+// v = M x for row-major M
+CM_HD void matvec_rm(const double *M, double x0, double x1, double x2, double *v) {
+    for (int k = 0; k < 3; ++k) v[k] = add(add(mul(M[3 * k], x0), mul(M[3 * k + 1], x1)), mul(M[3 * k + 2], x2));
+}
+
+// Bin a position: cell index per axis and FP64 offset from the cell origin.
+CM_HD void bin_position(const FrameGeom &G, double x0, double x1, double x2, int *c, double *q) {
+    double f[3], g[3];
+    matvec_rm(G.Hi, x0, x1, x2, f);
+    for (int k = 0; k < 3; ++k) {
+        double fk = sub(f[k], floor(f[k]));
+        if (!(fk < 1.0)) fk = 0.0;  // f just below an integer can round up to 1
+        if (!(fk >= 0.0)) fk = 0.0; // NaN guard
+        double fn = mul(fk, (double)G.n[k]);
+        double ck = floor(fn);
+        int ci = (int)ck;
+        if (ci >= G.n[k]) ci = G.n[k] - 1;
+        if (ci < 0) ci = 0;
+        c[k] = ci;
+        g[k] = sub(fn, (double)ci);
+    }
+    matvec_cm(G.Hn, g[0], g[1], g[2], q);
+}
+
+// Bin a fractional position already in [0, 1) (the centre of a placed molecule).
+CM_HD void bin_fractional(const FrameGeom &G, const double *f, int *c, double *q) {
+    double g[3];
+    for (int k = 0; k < 3; ++k) {
+        double fn = mul(f[k], (double)G.n[k]);
+        int ci = (int)floor(fn);
+        if (ci >= G.n[k]) ci = G.n[k] - 1;
+        if (ci < 0) ci = 0;
+        c[k] = ci;
+        g[k] = sub(fn, (double)ci);
+    }
+    matvec_cm(G.Hn, g[0], g[1], g[2], q);
+}
+
+// Minimum-image displacement d -> d - H rint(Hinv d), the unwrap used to make
+// molecules whole (CellListMap.wrap_relative_to, src/rigid_body.jl:129-131).
+CM_HD void unwrap(const FrameGeom &G, double *d) {
+    double f[3];
+    matvec_rm(G.Hi, d[0], d[1], d[2], f);
+    double n0 = rint(f[0]), n1 = rint(f[1]), n2 = rint(f[2]);
+    if (n0 != 0.0 || n1 != 0.0 || n2 != 0.0) {
+        double s[3];
+        matvec_cm(G.H, n0, n1, n2, s);
+        for (int k = 0; k < 3; ++k) d[k] = sub(d[k], s[k]);
+    }
+}
+
+CM_HD int cell_linear(const FrameGeom &G, int cx, int cy, int cz) { return (cz * G.n[1] + cy) * G.n[0] + cx; }
+
+CM_HD int off_index(int dx, int dy, int dz) { return ((dz + kLT) * kLTW + (dy + kLT)) * kLTW + (dx + kLT); }
+
+CM_HD int wrapi(int c, int n) {
+    int r = c % n;
+    return r < 0 ? r + n : r;
+}
+
+}  // namespace cmgeom

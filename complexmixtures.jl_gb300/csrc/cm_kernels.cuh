@@ -1,0 +1,1412 @@
+// cm_kernels.cuh -- device code of the GB300 MDDF engine.
+//
+// Per frame the engine answers, for every (solute molecule s, solvent molecule v)
+// pair, the question mddf_frame! asks through CellListMap (src/mddf.jl:382-396,
+// src/minimum_distances.jl:81-148): the minimum-distance atom pair within the
+// cutoff, its distance, and the shortest distance from s to v's reference atom;
+// then it bins the answer into the MDDF / RDF / group histograms
+// (src/update_counters.jl:43-87).  Only pairs that are within the cutoff touch
+// the histograms, which replaces the reference's O(nsolute * nsolvent) scan of
+// the whole list with the same counts.
+//
+// Two search layouts ("regimes"):
+//   PAIRS  molecules of both selections are small.  Molecules are binned by an
+//          anchor atom; a warp walks the stencil of one solute molecule, queues
+//          candidate solvent molecules whose anchors pass a bounding-sphere test,
+//          and each lane evaluates all atom pairs of one candidate.  In self mode
+//          each unordered pair is evaluated once and credited in both directions.
+//   ATOMS  the solute molecule is large (a protein).  Its atoms are counting-
+//          sorted into cells; one thread per solvent molecule scans the stencil
+//          of each of its atoms.
+//
+// Precision.  In FP32 mode the search runs in single precision on cell-relative
+// coordinates.  Every discrete decision -- within cutoff, which atom pair is the
+// minimum, the histogram bin, the bulk test, the reference-atom distance -- is
+// taken from the FP32 value only when the value is farther than the guard band
+// `delta` from the decision boundary; otherwise the pair is re-evaluated in FP64
+// with the same formula the FP64 mode uses, so both modes produce identical
+// integer counts.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "cm_geom.h"
+
+namespace cmk {
+
+using cmfeed::add;
+using cmfeed::div;
+using cmfeed::mul;
+using cmfeed::sub;
+using namespace cmgeom;
+
+constexpr int kMaxSmallMol = 32;  // PAIRS regime: atoms per molecule on either side
+constexpr int kWarps = 8;         // warps per CTA of the PAIRS real-pass kernel
+constexpr int kQueue = 64;        // per-warp candidate queue
+
+enum : int { ERR_STENCIL = 1, ERR_BIN = 2, ERR_QUEUE = 4, ERR_SIZE = 8 };
+enum : int {
+    ST_MOLPAIRS = 0,
+    ST_ATOMPAIRS,
+    ST_HITS_REAL,
+    ST_HITS_RAND,
+    ST_GUARD,
+    ST_GUARD_PAIRS,
+    ST_MAXERR,  // bits of a non-negative double
+    ST_N
+};
+
+struct DevSys {
+    int ms, aps, mv, apv;
+    int self;
+    int iref;       // 0-based reference atom (solvent role)
+    int nbins;
+    int nrs;
+    int fp32;
+    int usecutoff;
+    int Gs, Gv;
+    int default_s, default_v;
+    int smem_groups;
+    double cut, cut2, binstep, dbulk;
+    uint64_t seed;
+    const int64_t *gs_off;
+    const int32_t *gs_idx;
+    const int64_t *gv_off;
+    const int32_t *gv_idx;
+    unsigned long long *hist;  // class accumulators, half units
+    int64_t o_md, o_mdr, o_rdf, o_rdfr, o_gs, o_gsr, o_gv, o_gvr;
+    unsigned long long *stats;
+    int *err;
+};
+
+// Radii found by the prep kernels (max over molecules), per frame.
+struct FrameScratch {
+    float rmax_s;   // solute anchor radius
+    float rmax_v;   // solvent anchor radius
+    float rcmax;    // solvent centroid radius (placed molecules)
+    float pad;
+};
+
+struct Sample {
+    int s;     // solute molecule
+    int rep;   // repetition index of s in this frame
+    int d;     // distinct-sample index (flags / bulk list row)
+    int pad;
+};
+
+__device__ __forceinline__ void raise_err(const DevSys &S, int code) { atomicOr(S.err, code); }
+
+__device__ __forceinline__ int setbin0(double d, double step) {
+    int b = (int)ceil(div(d, step));
+    return (b < 1 ? 1 : b) - 1;
+}
+
+__device__ __forceinline__ float norm3f(float x, float y, float z) { return sqrtf(fmaf(z, z, fmaf(y, y, x * x))); }
+
+// ------------------------------------------------------------------ histograms
+struct SHist {
+    unsigned int *md, *rdf, *gs, *gv;  // shared-memory privatised counters
+};
+
+__device__ __forceinline__ int hist_words(const DevSys &S) {
+    return S.nbins * (2 + (S.smem_groups ? (S.Gs + (S.self ? 0 : S.Gv)) : 0));
+}
+
+__device__ __forceinline__ SHist shist_bind(const DevSys &S, unsigned int *base) {
+    SHist h;
+    h.md = base;
+    h.rdf = base + S.nbins;
+    h.gs = base + 2 * S.nbins;
+    h.gv = h.gs + (int64_t)S.Gs * S.nbins;
+    return h;
+}
+
+__device__ void shist_zero(const DevSys &S, unsigned int *base) {
+    int n = hist_words(S);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) base[i] = 0u;
+}
+
+__device__ void shist_flush(const DevSys &S, const SHist &h, bool rnd) {
+    unsigned long long *md = S.hist + (rnd ? S.o_mdr : S.o_md);
+    unsigned long long *rdf = S.hist + (rnd ? S.o_rdfr : S.o_rdf);
+    for (int i = threadIdx.x; i < S.nbins; i += blockDim.x) {
+        if (h.md[i]) atomicAdd(md + i, (unsigned long long)h.md[i]);
+        if (h.rdf[i]) atomicAdd(rdf + i, (unsigned long long)h.rdf[i]);
+    }
+    if (S.smem_groups) {
+        unsigned long long *gs = S.hist + (rnd ? S.o_gsr : S.o_gs);
+        int64_t n = (int64_t)S.Gs * S.nbins;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+            if (h.gs[i]) atomicAdd(gs + i, (unsigned long long)h.gs[i]);
+        if (!S.self) {
+            unsigned long long *gv = S.hist + (rnd ? S.o_gvr : S.o_gv);
+            int64_t m = (int64_t)S.Gv * S.nbins;
+            for (int64_t i = threadIdx.x; i < m; i += blockDim.x)
+                if (h.gv[i]) atomicAdd(gv + i, (unsigned long long)h.gv[i]);
+        }
+    }
+}
+
+__device__ __forceinline__ void add_group(const DevSys &S, const SHist &h, bool rnd, bool solvent_table, int g, int bin,
+                                          unsigned inc) {
+    int64_t idx = (int64_t)g * S.nbins + bin;
+    if (S.smem_groups) {
+        atomicAdd((solvent_table ? h.gv : h.gs) + idx, inc);
+    } else {
+        int64_t o = solvent_table ? (rnd ? S.o_gvr : S.o_gv) : (rnd ? S.o_gsr : S.o_gs);
+        atomicAdd(S.hist + o + idx, (unsigned long long)inc);
+    }
+}
+
+// update_group_count! (src/update_counters.jl:22-36) for the solute-side atom,
+// identified by its index inside the solute molecule.
+__device__ __forceinline__ void credit_solute(const DevSys &S, const SHist &h, bool rnd, int i_local, int bin, unsigned inc) {
+    if (S.default_s) {
+        add_group(S, h, rnd, false, i_local, bin, inc);
+    } else {
+        for (int64_t p = S.gs_off[i_local]; p < S.gs_off[i_local + 1]; ++p) add_group(S, h, rnd, false, S.gs_idx[p], bin, inc);
+    }
+}
+
+// The solvent-side atom, identified by its index in the whole selection; in
+// self mode it credits the solute table (src/update_counters.jl:272-277).
+__device__ __forceinline__ void credit_solvent(const DevSys &S, const SHist &h, bool rnd, int64_t j, int bin, unsigned inc) {
+    bool to_solvent = !S.self;
+    if (S.default_v) {
+        add_group(S, h, rnd, to_solvent, (int)(j % S.apv), bin, inc);
+    } else {
+        for (int64_t p = S.gv_off[j]; p < S.gv_off[j + 1]; ++p) add_group(S, h, rnd, to_solvent, S.gv_idx[p], bin, inc);
+    }
+}
+
+// One within-cutoff record of the reference's list, binned (update_counters!).
+__device__ __forceinline__ void apply_hit(const DevSys &S, const SHist &h, bool rnd, int bin, int i_local, int64_t j, bool ref,
+                                          int rbin) {
+    if (bin < 0 || bin >= S.nbins || (ref && (rbin < 0 || rbin >= S.nbins))) {
+        raise_err(S, ERR_BIN);
+        return;
+    }
+    atomicAdd(h.md + bin, 2u);
+    if (S.self) {
+        credit_solute(S, h, rnd, i_local, bin, 1u);
+        credit_solvent(S, h, rnd, j, bin, 1u);
+    } else {
+        credit_solute(S, h, rnd, i_local, bin, 2u);
+        credit_solvent(S, h, rnd, j, bin, 2u);
+    }
+    if (ref) atomicAdd(h.rdf + rbin, 2u);
+}
+
+// Warp-aggregated statistics counters.
+struct LocalStats {
+    unsigned long long molpairs = 0, atompairs = 0, hits = 0, guard = 0, guard_pairs = 0;
+    double maxerr = 0.0;
+};
+
+__device__ void stats_flush(const DevSys &S, LocalStats &st, bool rnd) {
+    unsigned long long v[5] = {st.molpairs, st.atompairs, st.hits, st.guard, st.guard_pairs};
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    double e = st.maxerr;
+    for (int o = 16; o > 0; o >>= 1) e = fmax(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) {
+        if (v[0]) atomicAdd(S.stats + ST_MOLPAIRS, v[0]);
+        if (v[1]) atomicAdd(S.stats + ST_ATOMPAIRS, v[1]);
+        if (v[2]) atomicAdd(S.stats + (rnd ? ST_HITS_RAND : ST_HITS_REAL), v[2]);
+        if (v[3]) atomicAdd(S.stats + ST_GUARD, v[3]);
+        if (v[4]) atomicAdd(S.stats + ST_GUARD_PAIRS, v[4]);
+        if (e > 0.0) atomicMax(S.stats + ST_MAXERR, (unsigned long long)__double_as_longlong(e));
+    }
+}
+
+// ------------------------------------------------------------------ geometry
+// Sum of the lengths of the three cell edge vectors: bounds |q| of any site.
+__device__ __forceinline__ double cell_span(const FrameGeom &G) {
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s += sqrt(G.Hn[3 * k] * G.Hn[3 * k] + G.Hn[3 * k + 1] * G.Hn[3 * k + 1] + G.Hn[3 * k + 2] * G.Hn[3 * k + 2]);
+    return s;
+}
+__device__ __forceinline__ double edge_len(const FrameGeom &G, int k) {
+    return sqrt(G.Hn[3 * k] * G.Hn[3 * k] + G.Hn[3 * k + 1] * G.Hn[3 * k + 1] + G.Hn[3 * k + 2] * G.Hn[3 * k + 2]);
+}
+
+// Stencil half-widths for a search range; false if the offset table is too small.
+__device__ __forceinline__ bool stencil(const FrameGeom &G, double range, int *L) {
+    bool ok = true;
+    for (int k = 0; k < 3; ++k) {
+        int l = (int)ceil(range * (1.0 + 1e-9) / G.cw[k]);
+        if (l < 1) l = 1;
+        if (l > kLT) { ok = false; l = kLT; }
+        L[k] = l;
+    }
+    return ok;
+}
+
+// Guard half-width (Angstrom) of the FP32 search: 2^-20 times a bound on the
+// magnitudes entering the FP32 displacement (each FP32 rounding contributes at
+// most 2^-24 of its operand; 16x covers the <= 9 roundings per component and
+// the norm).
+__device__ __forceinline__ double guard_band(const FrameGeom &G, const int *L, double radii) {
+    double span = cell_span(G);
+    double off = 0.0;
+    for (int k = 0; k < 3; ++k) off += L[k] * edge_len(G, k);
+    return 0x1.0p-20 * (2.0 * span + off + radii + 1.0);
+}
+
+
+// Images of a candidate pair: along axis k the stencil offsets
+// Delta_k = base_k + t * step_k, t < cnt_k.  A single image (cnt = 1 on every
+// axis) is the normal case; several images arise when the box is narrower
+// than the search range along an axis, and then all images are searched and
+// the minimum over them is kept, as the reference's cell list does.
+struct Images {
+    int base[3];
+    int step[3];
+    int cnt[3];
+};
+
+__device__ __forceinline__ int image_count(const Images &im) { return im.cnt[0] * im.cnt[1] * im.cnt[2]; }
+
+// All Delta == t0 (mod n) inside [-L, L].
+__device__ __forceinline__ void axis_images(int t0, int n, int L, int &base, int &cnt) {
+    int r = ((t0 + L) % n + n) % n;
+    base = -L + r;
+    cnt = base > L ? 0 : (L - base) / n + 1;
+}
+
+#define CM_FOR_IMAGES(im, DX, DY, DZ)                                       \
+    for (int _iz = 0; _iz < (im).cnt[2]; ++_iz)                            \
+        for (int _iy = 0; _iy < (im).cnt[1]; ++_iy)                        \
+            for (int _ix = 0; _ix < (im).cnt[0]; ++_ix)                    \
+                if (int DX = (im).base[0] + _ix * (im).step[0], DY = (im).base[1] + _iy * (im).step[1], \
+                    DZ = (im).base[2] + _iz * (im).step[2]; true)
+
+// One direction of a (solute molecule, solvent molecule) result: the record the
+// reference keeps in its list for the solvent molecule (src/minimum_distances.jl:12-19),
+// already binned.
+struct DirRec {
+    int within;
+    int i_local;   // solute-side atom, index inside its molecule
+    int64_t j;     // solvent-side atom, index in the whole selection
+    int bin;       // 0-based histogram bin of d
+    int ref;       // reference atom within cutoff
+    int rbin;      // 0-based bin of d_ref_atom
+    int bulk;      // inbulk(...) of the solvent molecule for this solute molecule (src/mddf.jl:55-57)
+};
+
+// ---------------------------------------------------------- PAIRS evaluation
+// FP32 first pass: smallest / second-smallest squared distance and the pair
+// (a, b) of the smallest, plus the reference-atom row / column minima.
+struct Pass32 {
+    float m1, m2;
+    int k1;        // a * apv + b
+    float r1, r2;
+};
+
+template <bool ROW>
+__device__ __forceinline__ void inner32(const float4 *__restrict__ os, int aps, int apv, int b, float tx, float ty, float tz,
+                                        Pass32 &P) {
+    float row = P.r1;
+    for (int a = 0; a < aps; ++a) {
+        float4 oa = os[a];
+        float dx = tx - oa.x, dy = ty - oa.y, dz = tz - oa.z;
+        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        P.m2 = fminf(P.m2, fmaxf(P.m1, d2));
+        P.k1 = d2 < P.m1 ? a * apv + b : P.k1;
+        P.m1 = fminf(P.m1, d2);
+        if (ROW) row = fminf(row, d2);
+    }
+    if (ROW) P.r1 = row;
+}
+
+template <bool SELF>
+__device__ __forceinline__ void pairs_pass32(const DevSys &S, const float4 *__restrict__ off32, const Images &im, float4 qs,
+                                             float4 qv, const float4 *__restrict__ os, const float4 *ov, Pass32 &P) {
+    P.m1 = P.m2 = P.r1 = P.r2 = INFINITY;
+    P.k1 = 0;
+    const int aps = S.aps, apv = S.apv, iref = S.iref;
+    CM_FOR_IMAGES(im, dx, dy, dz) {
+        float4 o = off32[off_index(dx, dy, dz)];
+        float Dx = (qv.x - qs.x) + o.x, Dy = (qv.y - qs.y) + o.y, Dz = (qv.z - qs.z) + o.z;
+        for (int b = 0; b < apv; ++b) {
+            float4 ob = ov[b];
+            float tx = Dx + ob.x, ty = Dy + ob.y, tz = Dz + ob.z;
+            if (b == iref) inner32<true>(os, aps, apv, b, tx, ty, tz, P);
+            else inner32<false>(os, aps, apv, b, tx, ty, tz, P);
+            if (SELF) {
+                float4 oa = os[iref];
+                float ex = tx - oa.x, ey = ty - oa.y, ez = tz - oa.z;
+                P.r2 = fminf(P.r2, fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
+            }
+        }
+    }
+}
+
+// Exact FP64 minimum search with the reference's tie rule: among equal
+// distances the pair visited last wins (src/minimum_distances.jl:33-37, the new
+// pair replaces the record unless the record is strictly closer), restated as
+// the largest (solute atom, solvent atom) index pair.  Distances are compared
+// as d = sqrt(d2) like the reference; d2 decides when it is far enough from the
+// current best that the square roots cannot tie.
+struct Best64 {
+    double d2, d, lo, hi;
+    int a, b;     // direction 1: key (a, b)
+    int a2, b2;   // direction 2 (self mode): key (b, a)
+};
+
+__device__ __forceinline__ void best_init(Best64 &B) {
+    B.d2 = INFINITY;
+    B.d = -1.0;
+    B.lo = INFINITY;
+    B.hi = INFINITY;
+    B.a = B.b = B.a2 = B.b2 = -1;
+}
+
+template <bool DIR2>
+__device__ __forceinline__ void best_update(Best64 &B, double d2, int a, int b) {
+    if (d2 < B.lo) {
+        B.d2 = d2;
+        B.d = -1.0;
+        B.lo = mul(d2, 1.0 - 0x1.0p-50);
+        B.hi = mul(d2, 1.0 + 0x1.0p-50);
+        B.a = a; B.b = b; B.a2 = a; B.b2 = b;
+    } else if (d2 <= B.hi) {
+        double d = sqrt(d2);
+        if (B.d < 0.0) B.d = sqrt(B.d2);
+        if (d < B.d) {
+            B.d2 = d2;
+            B.d = d;
+            B.lo = mul(d2, 1.0 - 0x1.0p-50);
+            B.hi = mul(d2, 1.0 + 0x1.0p-50);
+            B.a = a; B.b = b; B.a2 = a; B.b2 = b;
+        } else if (d == B.d) {
+            if (a > B.a || (a == B.a && b > B.b)) { B.a = a; B.b = b; }
+            if (DIR2 && (b > B.b2 || (b == B.b2 && a > B.a2))) { B.a2 = a; B.b2 = b; }
+        }
+    }
+}
+
+__device__ __forceinline__ double best_d(Best64 &B) {
+    if (B.d < 0.0) B.d = sqrt(B.d2);
+    return B.d;
+}
+
+__device__ __forceinline__ double pair_d2_64(double tx, double ty, double tz, double ax, double ay, double az) {
+    double dx = sub(tx, ax), dy = sub(ty, ay), dz = sub(tz, az);
+    return add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz));
+}
+
+struct Exact64 {
+    Best64 B;
+    double rr1, rr2;   // exact squared minima (within cutoff) of the row / column
+    long long evals;
+};
+
+// Exact scan of a molecule pair over its images.  With FILTER an atom pair is
+// evaluated in FP64 only if its FP32 squared distance is at most the threshold
+// of an accumulator it feeds (thr_arg: the minimum; thr_r1: row of v's
+// reference atom; thr_r2: column of s's reference atom); each threshold keeps
+// every pair that can hold the exact minimum of its accumulator.
+template <bool FILTER, bool SELF>
+__device__ void pairs_exact(const DevSys &S, const d4 *__restrict__ off64, const float4 *__restrict__ off32, const Images &im,
+                            d4 qs64, float4 qs32, d4 qv64, float4 qv32, const d4 *os64, const float4 *os32,
+                            const d4 *ov64, const float4 *ov32, float thr_arg, float thr_r1, float thr_r2, Exact64 &E) {
+    best_init(E.B);
+    E.rr1 = INFINITY;
+    E.rr2 = INFINITY;
+    E.evals = 0;
+    const int aps = S.aps, apv = S.apv, iref = S.iref;
+    const double cut2 = S.cut2;
+    CM_FOR_IMAGES(im, ix, iy, iz) {
+        int oi = off_index(ix, iy, iz);
+        d4 o = off64[oi];
+        double Dx = add(sub(qv64.x, qs64.x), o.x);
+        double Dy = add(sub(qv64.y, qs64.y), o.y);
+        double Dz = add(sub(qv64.z, qs64.z), o.z);
+        float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+        if (FILTER) {
+            float4 of = off32[oi];
+            Fx = (qv32.x - qs32.x) + of.x;
+            Fy = (qv32.y - qs32.y) + of.y;
+            Fz = (qv32.z - qs32.z) + of.z;
+        }
+        for (int b = 0; b < apv; ++b) {
+            d4 ob = ov64[b];
+            double tx = add(Dx, ob.x), ty = add(Dy, ob.y), tz = add(Dz, ob.z);
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+            if (FILTER) {
+                float4 of = ov32[b];
+                fx = Fx + of.x; fy = Fy + of.y; fz = Fz + of.z;
+            }
+            for (int a = 0; a < aps; ++a) {
+                if (FILTER) {
+                    float4 oa = os32[a];
+                    float ex = fx - oa.x, ey = fy - oa.y, ez = fz - oa.z;
+                    float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                    bool need = d2f <= thr_arg || (b == iref && d2f <= thr_r1) || (SELF && a == iref && d2f <= thr_r2);
+                    if (!need) continue;
+                }
+                d4 oa = os64[a];
+                double d2 = pair_d2_64(tx, ty, tz, oa.x, oa.y, oa.z);
+                E.evals++;
+                if (d2 <= cut2) {
+                    if (b == iref) E.rr1 = fmin(E.rr1, d2);
+                    if (SELF && a == iref) E.rr2 = fmin(E.rr2, d2);
+                    best_update<SELF>(E.B, d2, a, b);
+                }
+            }
+        }
+    }
+}
+
+// FP64 squared distance of one atom pair, minimum over the images.
+__device__ double pairs_one64(const d4 *__restrict__ off64, const Images &im, d4 qs64, d4 qv64, d4 oa,
+                              d4 ob) {
+    double best = INFINITY;
+    CM_FOR_IMAGES(im, ix, iy, iz) {
+        d4 o = off64[off_index(ix, iy, iz)];
+        double tx = add(add(sub(qv64.x, qs64.x), o.x), ob.x);
+        double ty = add(add(sub(qv64.y, qs64.y), o.y), ob.y);
+        double tz = add(add(sub(qv64.z, qs64.z), o.z), ob.z);
+        best = fmin(best, pair_d2_64(tx, ty, tz, oa.x, oa.y, oa.z));
+    }
+    return best;
+}
+
+// Guard-band constants of one kernel launch.
+struct Guard {
+    double delta;     // Angstrom
+    float cutp2;      // (cut + delta)^2, rounded up
+    float cutm2;      // (cut - delta)^2, rounded down
+    float two_delta;
+    float inv_bs;     // 1 / binstep in FP32
+    float bin_band;   // half-width of the bin-edge band in units of bins
+    float dbulk_lo, dbulk_hi;
+};
+
+__device__ __forceinline__ Guard make_guard(const DevSys &S, double delta) {
+    Guard g;
+    g.delta = delta;
+    double cp = S.cut + delta, cm = S.cut - delta;
+    g.cutp2 = __double2float_ru(cp * cp);
+    g.cutm2 = cm > 0.0 ? __double2float_rd(cm * cm) : 0.0f;
+    g.two_delta = __double2float_ru(2.0 * delta);
+    g.inv_bs = (float)(1.0 / S.binstep);
+    g.bin_band = __double2float_ru(delta / S.binstep + (double)S.nbins * 0x1.0p-21 + 1e-6);
+    g.dbulk_lo = __double2float_rd(S.dbulk - delta);
+    g.dbulk_hi = __double2float_ru(S.dbulk + delta);
+    return g;
+}
+
+// Bin from an FP32 distance, or -1 when it lies in the band around a bin edge.
+__device__ __forceinline__ int bin32(const Guard &g, float d) {
+    float k = d * g.inv_bs;
+    float r = rintf(k);
+    if (fabsf(k - r) <= g.bin_band) return -1;
+    int b = (int)ceilf(k);
+    return (b < 1 ? 1 : b) - 1;
+}
+
+__device__ __forceinline__ DirRec dir_none(const DevSys &S) {
+    DirRec r;
+    r.within = 0; r.i_local = -1; r.j = -1; r.bin = -1; r.ref = 0; r.rbin = -1;
+    r.bulk = S.usecutoff ? 0 : 1;
+    return r;
+}
+
+__device__ __forceinline__ int inbulk64(const DevSys &S, bool within, double d) {
+    return S.usecutoff ? (within && d > S.dbulk) : !within;
+}
+
+// Records from an exact scan.
+template <bool SELF>
+__device__ __forceinline__ void records_from_exact(const DevSys &S, Exact64 &E, int s, int64_t v, DirRec &r1, DirRec &r2) {
+    r1 = dir_none(S);
+    r2 = dir_none(S);
+    if (!(E.B.d2 <= S.cut2)) return;
+    double d = best_d(E.B);
+    int bin = setbin0(d, S.binstep);
+    r1.within = 1;
+    r1.i_local = E.B.a;
+    r1.j = v * S.apv + E.B.b;
+    r1.bin = bin;
+    r1.bulk = inbulk64(S, true, d);
+    if (E.rr1 <= S.cut2) { r1.ref = 1; r1.rbin = setbin0(sqrt(E.rr1), S.binstep); }
+    if (SELF) {
+        r2.within = 1;
+        r2.i_local = E.B.b2;
+        r2.j = (int64_t)s * S.aps + E.B.a2;
+        r2.bin = bin;
+        r2.bulk = r1.bulk;
+        if (E.rr2 <= S.cut2) { r2.ref = 1; r2.rbin = setbin0(sqrt(E.rr2), S.binstep); }
+    }
+}
+
+// Decide one molecule pair from its FP32 pass, falling back to FP64 inside the
+// guard band.  Produces exactly the records of pairs_exact<false, SELF>.
+template <bool SELF>
+__device__ void pairs_decide(const DevSys &S, const Guard &g, const Pass32 &P, const d4 *__restrict__ off64,
+                             const float4 *__restrict__ off32, const Images &im, d4 qs64, float4 qs32, d4 qv64,
+                             float4 qv32, const d4 *os64, const float4 *os32, const d4 *ov64, const float4 *ov32, int s,
+                             int64_t v, DirRec &r1, DirRec &r2, LocalStats &st) {
+    r1 = dir_none(S);
+    r2 = dir_none(S);
+    if (P.m1 > g.cutp2) return;  // every pair is beyond the cutoff
+    float d1 = sqrtf(P.m1);
+    bool amb = P.m1 >= g.cutm2 || (sqrtf(P.m2) - d1) <= g.two_delta;
+    if (amb) {
+        float t = d1 + g.two_delta;
+        float thr = __fmul_ru(t, t);
+        float thr1 = INFINITY, thr2 = INFINITY;
+        if (P.r1 <= g.cutp2) { float u = sqrtf(P.r1) + g.two_delta; thr1 = __fmul_ru(u, u); } else thr1 = -1.f;
+        if (SELF) { if (P.r2 <= g.cutp2) { float u = sqrtf(P.r2) + g.two_delta; thr2 = __fmul_ru(u, u); } else thr2 = -1.f; }
+        Exact64 E;
+        pairs_exact<true, SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, thr, thr1, thr2, E);
+        records_from_exact<SELF>(S, E, s, v, r1, r2);
+        st.guard++;
+        st.guard_pairs += E.evals;
+        if (E.B.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(E.B)));
+        return;
+    }
+    // unambiguous: the FP32 minimum pair is the exact minimum pair, within cutoff
+    int a = P.k1 / S.apv, b = P.k1 - a * S.apv;
+    int bin = bin32(g, d1);
+    double d64 = -1.0;
+    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
+        double q = pairs_one64(off64, im, qs64, qv64, os64[a], ov64[b]);
+        d64 = sqrt(q);
+        bin = setbin0(d64, S.binstep);
+        st.guard++;
+        st.guard_pairs += image_count(im);
+        st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
+    }
+    int bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
+    r1.within = 1;
+    r1.i_local = a;
+    r1.j = v * S.apv + b;
+    r1.bin = bin;
+    r1.bulk = bulk;
+    if (SELF) {
+        r2.within = 1;
+        r2.i_local = b;
+        r2.j = (int64_t)s * S.aps + a;
+        r2.bin = bin;
+        r2.bulk = bulk;
+    }
+    // reference-atom rows (and columns in self mode)
+    for (int dir = 0; dir < (SELF ? 2 : 1); ++dir) {
+        float rm = dir == 0 ? P.r1 : P.r2;
+        DirRec &r = dir == 0 ? r1 : r2;
+        if (rm > g.cutp2) continue;
+        int rb = -1;
+        if (rm < g.cutm2) rb = bin32(g, sqrtf(rm));
+        if (rb >= 0) {
+            r.ref = 1;
+            r.rbin = rb;
+            continue;
+        }
+        float u = sqrtf(rm) + g.two_delta;
+        float thr = __fmul_ru(u, u);
+        Exact64 E;
+        pairs_exact<true, SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, -1.f, dir == 0 ? thr : -1.f,
+                                dir == 1 ? thr : -1.f, E);
+        double rr = dir == 0 ? E.rr1 : E.rr2;
+        st.guard++;
+        st.guard_pairs += E.evals;
+        if (rr <= S.cut2) {
+            r.ref = 1;
+            r.rbin = setbin0(sqrt(rr), S.binstep);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned char flag_code(const DirRec &r) { return r.within ? (unsigned char)(1 + (r.bulk ? 1 : 0)) : 0; }
+
+__device__ __forceinline__ int pack_delta(int dx, int dy, int dz) { return (dx + 16) | ((dy + 16) << 5) | ((dz + 16) << 10); }
+__device__ __forceinline__ void unpack_delta(int c, int &dx, int &dy, int &dz) {
+    dx = (c & 31) - 16;
+    dy = ((c >> 5) & 31) - 16;
+    dz = ((c >> 10) & 31) - 16;
+}
+
+// ------------------------------------------------------------------- kernels
+// Per-frame offset table: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
+__global__ void k_offtable(const FrameGeom *__restrict__ Gp, d4 *__restrict__ off64, float4 *__restrict__ off32) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kOffEntries) return;
+    int dx = i % kLTW - kLT, dy = (i / kLTW) % kLTW - kLT, dz = i / (kLTW * kLTW) - kLT;
+    double v[3];
+    matvec_cm(Gp->Hn, (double)dx, (double)dy, (double)dz, v);
+    off64[i] = make_d4(v[0], v[1], v[2], 0.0);
+    off32[i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+}
+
+template <typename T>
+__device__ __forceinline__ void load_xyz(const T *p, double *x) {
+    x[0] = (double)p[0];
+    x[1] = (double)p[1];
+    x[2] = (double)p[2];
+}
+
+__device__ __forceinline__ void atomic_max_pos(float *addr, float v) { atomicMax((int *)addr, __float_as_int(v)); }
+
+// Molecule-centred data for random insertion (src/rigid_body.jl:127-134):
+// the molecule made whole around its reference atom, relative to its mean.
+template <typename T>
+__device__ void centroid_data(const FrameGeom &G, const T *x, int apm, int iref, d4 *u64, float &rc) {
+    double xr[3];
+    load_xyz(x + 3 * iref, xr);
+    double cm[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < apm; ++b) {
+        double xb[3], d[3];
+        load_xyz(x + 3 * b, xb);
+        for (int k = 0; k < 3; ++k) d[k] = sub(xb[k], xr[k]);
+        double f[3];
+        matvec_rm(G.Hi, d[0], d[1], d[2], f);
+        double n0 = rint(f[0]), n1 = rint(f[1]), n2 = rint(f[2]);
+        if (n0 != 0.0 || n1 != 0.0 || n2 != 0.0) {
+            double sh[3];
+            matvec_cm(G.H, n0, n1, n2, sh);
+            for (int k = 0; k < 3; ++k) xb[k] = sub(xb[k], sh[k]);
+        }
+        u64[b] = make_d4(xb[0], xb[1], xb[2], 0.0);
+        for (int k = 0; k < 3; ++k) cm[k] = add(cm[k], xb[k]);
+    }
+    for (int k = 0; k < 3; ++k) cm[k] = div(cm[k], (double)apm);
+    double r = 0.0;
+    for (int b = 0; b < apm; ++b) {
+        d4 w = u64[b];
+        w.x = sub(w.x, cm[0]);
+        w.y = sub(w.y, cm[1]);
+        w.z = sub(w.z, cm[2]);
+        u64[b] = w;
+        r = fmax(r, sqrt(w.x * w.x + w.y * w.y + w.z * w.z));
+    }
+    rc = __double2float_ru(r * (1.0 + 1e-12) + 1e-12);
+}
+
+// PAIRS regime: anchor (first atom) binned, atoms as offsets from the anchor
+// made whole by minimum image; radius = largest offset.
+template <typename T>
+__global__ void k_prep_pairs(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int nmol, int apm, int iref,
+                             int *__restrict__ mcell, float4 *__restrict__ mq32, d4 *__restrict__ mq64,
+                             float4 *__restrict__ mo32, d4 *__restrict__ mo64, int *__restrict__ cellcount,
+                             float *__restrict__ rmax, d4 *__restrict__ u64, float *__restrict__ rc) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    const FrameGeom &G = *Gp;
+    const T *x = xyz + (int64_t)m * apm * 3;
+    double x0[3];
+    load_xyz(x, x0);
+    int c[3];
+    double q[3];
+    bin_position(G, x0[0], x0[1], x0[2], c, q);
+    int cell = cell_linear(G, c[0], c[1], c[2]);
+    double r = 0.0;
+    for (int a = 0; a < apm; ++a) {
+        double xa[3], d[3];
+        load_xyz(x + 3 * a, xa);
+        for (int k = 0; k < 3; ++k) d[k] = sub(xa[k], x0[k]);
+        unwrap(G, d);
+        int64_t ia = (int64_t)m * apm + a;
+        mo64[ia] = make_d4(d[0], d[1], d[2], 0.0);
+        mo32[ia] = make_float4((float)d[0], (float)d[1], (float)d[2], 0.f);
+        r = fmax(r, sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+    }
+    float rf = __double2float_ru(r * (1.0 + 1e-12) + 1e-12);
+    mcell[m] = cell;
+    mq64[m] = make_d4(q[0], q[1], q[2], 0.0);
+    mq32[m] = make_float4((float)q[0], (float)q[1], (float)q[2], rf);
+    if (cellcount) atomicAdd(cellcount + cell, 1);
+    atomic_max_pos(rmax, rf);
+    if (u64) {
+        float rcm;
+        centroid_data(G, x, apm, iref, u64 + (int64_t)m * apm, rcm);
+        rc[m] = rcm;
+        atomic_max_pos(rmax + 1, rcm);
+    }
+}
+
+// Exclusive scan of n counts into start[0..n] (single CTA of 1024 threads);
+// also copies start into fill for the scatter.
+__global__ void __launch_bounds__(1024) k_scan(const int *__restrict__ count, int n, int *__restrict__ start, int *__restrict__ fill) {
+    __shared__ int wsum[32];
+    int t = threadIdx.x;
+    int per = (n + 1023) / 1024;
+    int lo = t * per, hi = min(n, lo + per);
+    int local = 0;
+    for (int i = lo; i < hi; ++i) local += count[i];
+    // block exclusive scan of `local`
+    int lane = t & 31, w = t >> 5;
+    int v = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int s = wsum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        wsum[lane] = s;
+    }
+    __syncthreads();
+    int excl = v - local + (w > 0 ? wsum[w - 1] : 0);
+    for (int i = lo; i < hi; ++i) {
+        start[i] = excl;
+        if (fill) fill[i] = excl;
+        excl += count[i];
+    }
+    if (hi == n && lo < hi) start[n] = excl;
+    if (n == 0 && t == 0) start[0] = 0;
+}
+
+__global__ void k_scatter_mols(const int *__restrict__ mcell, int nmol, int *__restrict__ fill, int *__restrict__ cmol) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    int p = atomicAdd(fill + mcell[m], 1);
+    cmol[p] = m;
+}
+
+// PAIRS regime, real pass: one warp per solute molecule.
+template <bool FP32, bool SELF>
+__global__ void __launch_bounds__(kWarps * 32)
+    k_pairs_real(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS, const d4 *__restrict__ off64,
+                 const float4 *__restrict__ off32, const int *__restrict__ scell, const float4 *__restrict__ sq32,
+                 const d4 *__restrict__ sq64, const float4 *__restrict__ so32, const d4 *__restrict__ so64,
+                 const float4 *__restrict__ vq32, const d4 *__restrict__ vq64, const float4 *__restrict__ vo32,
+                 const d4 *__restrict__ vo64, const int *__restrict__ cstart, const int *__restrict__ cmol,
+                 const int *__restrict__ slot_of_mol, unsigned char *__restrict__ flags) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    const int hw = hist_words(S);
+    float4 *os_all = (float4 *)(smem_raw + (((size_t)hw * 4 + 15) & ~(size_t)15));
+    int *q_all = (int *)(os_all + kWarps * kMaxSmallMol);
+    shist_zero(S, hbase);
+    __syncthreads();
+    SHist h = shist_bind(S, hbase);
+    const FrameGeom &G = *Gp;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4 *os = os_all + warp * kMaxSmallMol;
+    int *qv = q_all + warp * kQueue * 2;
+    int *qi = qv + kQueue;
+    LocalStats st;
+
+    const double rv = FS->rmax_v;
+    const double rs = SELF ? rv : (double)FS->rmax_s;
+    const double range = S.cut + rs + rv;
+    int L[3];
+    const bool ok = stencil(G, range + 1e-6 * (1.0 + range), L);
+    const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
+    const bool m0 = 2 * L[0] + 1 > n0, m1 = 2 * L[1] + 1 > n1, m2 = 2 * L[2] + 1 > n2;
+    const bool anymulti = m0 || m1 || m2;
+    const int e0 = m0 ? n0 : 2 * L[0] + 1, e1 = m1 ? n1 : 2 * L[1] + 1, e2 = m2 ? n2 : 2 * L[2] + 1;
+    const Guard g = make_guard(S, guard_band(G, L, 2.0 * (rs + rv)));
+    const float pre_margin = (float)(1e-3 * (1.0 + range));
+
+    if (ok) {
+        for (int s = blockIdx.x * kWarps + warp; s < S.ms; s += gridDim.x * kWarps) {
+            const int sc = scell[s];
+            const int cx = sc % n0, cy = (sc / n0) % n1, cz = sc / (n0 * n1);
+            const float4 qs32 = sq32[s];
+            const d4 qs64 = sq64[s];
+            for (int a = lane; a < S.aps; a += 32) os[a] = so32[(int64_t)s * S.aps + a];
+            __syncwarp();
+            const int sslot = slot_of_mol ? slot_of_mol[s] : -1;
+            int cnt = 0;
+            auto process = [&](int v, int code) {
+                int d0, d1, d2;
+                unpack_delta(code, d0, d1, d2);
+                Images im;
+                if (m0) { axis_images(d0, n0, L[0], im.base[0], im.cnt[0]); im.step[0] = n0; } else { im.base[0] = d0; im.cnt[0] = 1; im.step[0] = 0; }
+                if (m1) { axis_images(d1, n1, L[1], im.base[1], im.cnt[1]); im.step[1] = n1; } else { im.base[1] = d1; im.cnt[1] = 1; im.step[1] = 0; }
+                if (m2) { axis_images(d2, n2, L[2], im.base[2], im.cnt[2]); im.step[2] = n2; } else { im.base[2] = d2; im.cnt[2] = 1; im.step[2] = 0; }
+                const float4 qv32 = vq32[v];
+                const d4 qv64 = vq64[v];
+                const float4 *ov32 = vo32 + (int64_t)v * S.apv;
+                const d4 *ov64 = vo64 + (int64_t)v * S.apv;
+                const d4 *os64 = so64 + (int64_t)s * S.aps;
+                DirRec r1, r2;
+                st.molpairs++;
+                st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
+                if (FP32) {
+                    Pass32 P;
+                    pairs_pass32<SELF>(S, off32, im, qs32, qv32, os, ov32, P);
+                    pairs_decide<SELF>(S, g, P, off64, off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, s, v, r1, r2, st);
+                } else {
+                    Exact64 E;
+                    pairs_exact<false, SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, 0.f, 0.f, 0.f, E);
+                    records_from_exact<SELF>(S, E, s, v, r1, r2);
+                }
+                if (r1.within) { apply_hit(S, h, false, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
+                if (SELF && r2.within) { apply_hit(S, h, false, r2.bin, r2.i_local, r2.j, r2.ref, r2.rbin); st.hits++; }
+                if (sslot >= 0) flags[(int64_t)sslot * S.mv + v] = flag_code(r1);
+                if (SELF && slot_of_mol) {
+                    int vs = slot_of_mol[v];
+                    if (vs >= 0) flags[(int64_t)vs * S.mv + s] = flag_code(r2);
+                }
+            };
+            for (int iz = 0; iz < e2; ++iz) {
+                int dz = m2 ? iz - cz : iz - L[2];
+                int zc = m2 ? iz : wrapi(cz + dz, n2);
+                for (int iy = 0; iy < e1; ++iy) {
+                    int dy = m1 ? iy - cy : iy - L[1];
+                    int yc = m1 ? iy : wrapi(cy + dy, n1);
+                    for (int ix = 0; ix < e0; ++ix) {
+                        int dx = m0 ? ix - cx : ix - L[0];
+                        int xc = m0 ? ix : wrapi(cx + dx, n0);
+                        const int cell = (zc * n1 + yc) * n0 + xc;
+                        const int beg = cstart[cell], end = cstart[cell + 1];
+                        const int code = pack_delta(dx, dy, dz);
+                        float4 of = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (!anymulti) of = off32[off_index(dx, dy, dz)];
+                        for (int p0 = beg; p0 < end; p0 += 32) {
+                            const int p = p0 + lane;
+                            bool cand = false;
+                            int v = 0;
+                            if (p < end) {
+                                v = cmol[p];
+                                cand = !SELF || v > s;
+                                if (cand && !anymulti) {
+                                    float4 qv = vq32[v];
+                                    float Dx = (qv.x - qs32.x) + of.x, Dy = (qv.y - qs32.y) + of.y, Dz = (qv.z - qs32.z) + of.z;
+                                    float rr = S.cut + qs32.w + qv.w + pre_margin;
+                                    cand = fmaf(Dz, Dz, fmaf(Dy, Dy, Dx * Dx)) <= rr * rr;
+                                }
+                            }
+                            const unsigned mask = __ballot_sync(0xffffffffu, cand);
+                            const int pos = cnt + __popc(mask & ((1u << lane) - 1u));
+                            if (cand) { qv[pos] = v; qi[pos] = code; }
+                            cnt += __popc(mask);
+                            if (cnt >= 32) {
+                                __syncwarp();
+                                process(qv[lane], qi[lane]);
+                                __syncwarp();
+                                int rest = cnt - 32, tv = 0, ti = 0;
+                                if (lane < rest) { tv = qv[32 + lane]; ti = qi[32 + lane]; }
+                                __syncwarp();
+                                if (lane < rest) { qv[lane] = tv; qi[lane] = ti; }
+                                cnt = rest;
+                                __syncwarp();
+                            }
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane < cnt) process(qv[lane], qi[lane]);
+            __syncwarp();
+        }
+    } else if (threadIdx.x == 0) {
+        raise_err(S, ERR_STENCIL);
+    }
+    stats_flush(S, st, false);
+    __syncthreads();
+    shist_flush(S, h, false);
+}
+
+// Bulk-molecule list of each distinct sampled solute molecule, ascending
+// (src/mddf.jl:406-415); one CTA per sampled molecule.
+__global__ void __launch_bounds__(1024) k_bulk(const DevSys S, const Sample *__restrict__ samples, int nsamples,
+                                              const unsigned char *__restrict__ flags, int *__restrict__ bulk, int *__restrict__ nbulk) {
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    // find the sample that introduces distinct index blockIdx.x
+    int d = blockIdx.x;
+    int s = -1;
+    for (int i = 0; i < nsamples; ++i)
+        if (samples[i].d == d) { s = samples[i].s; break; }
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const unsigned char *f = flags + (int64_t)d * S.mv;
+    int *out = bulk + (int64_t)d * S.mv;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int base = 0; base < S.mv; base += blockDim.x) {
+        int v = base + threadIdx.x;
+        int keep = 0;
+        if (v < S.mv && !(S.self && v == s)) {
+            unsigned char c = f[v];
+            keep = S.usecutoff ? (c == 2) : (c == 0);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wsum[w] = __popc(m);
+        __syncthreads();
+        if (w == 0) {
+            int x = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            wsum[lane] = x;
+        }
+        __syncthreads();
+        int pos = carry + (w > 0 ? wsum[w - 1] : 0) + __popc(m & ((1u << lane) - 1u));
+        if (keep) out[pos] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += wsum[(blockDim.x >> 5) - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) nbulk[d] = carry;
+}
+
+// Draws of one placement slot, in stream order: bulk pick, centre, angles.
+struct Placement {
+    int jmol;
+    double fc[3];
+    uint64_t st;  // stream state after the centre (angles follow)
+};
+
+__device__ __forceinline__ Placement draw_placement(const DevSys &S, int64_t frame_id, const Sample &sm, int k, const int *bulk,
+                                                   const int *nbulk) {
+    Placement P;
+    uint64_t st = cmfeed::key(S.seed, cmfeed::kTagSlot, (uint64_t)frame_id, (uint64_t)sm.s,
+                              ((uint64_t)(uint32_t)sm.rep << 32) | (uint64_t)(uint32_t)k);
+    int nb = nbulk[sm.d];
+    if (nb > 0) P.jmol = bulk[(int64_t)sm.d * S.mv + (int64_t)cmfeed::below(st, (uint64_t)nb)];
+    else P.jmol = (int)cmfeed::below(st, (uint64_t)S.mv);
+    for (int q = 0; q < 3; ++q) P.fc[q] = cmfeed::uniform(st);
+    P.st = st;
+    return P;
+}
+
+__device__ __forceinline__ void draw_rotation(uint64_t &st, double *A) {
+    double cb, sb, cg, sg, ct, stt;
+    cmfeed::angle(st, cb, sb);
+    cmfeed::angle(st, cg, sg);
+    cmfeed::angle(st, ct, stt);
+    cmfeed::eulermat(cb, sb, cg, sg, ct, stt, A);
+}
+
+// PAIRS regime, random pass: one thread per (slot, sample).  Each slot gets a
+// copy of a bulk molecule, rotated and centred at a random point
+// (src/mddf.jl:65-88, src/rigid_body.jl:107-137); only slots whose bounding
+// sphere reaches the sampled solute molecule are rotated and evaluated.
+template <bool FP32, bool SELF>
+__global__ void __launch_bounds__(128)
+    k_pairs_random(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS, const d4 *__restrict__ off64,
+                   const float4 *__restrict__ off32, const Sample *__restrict__ samples, int sample0, const int *__restrict__ scell,
+                   const float4 *__restrict__ sq32, const d4 *__restrict__ sq64, const float4 *__restrict__ so32,
+                   const d4 *__restrict__ so64, const d4 *__restrict__ u64, const float *__restrict__ rc,
+                   const int *__restrict__ bulk, const int *__restrict__ nbulk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    const int hw = hist_words(S);
+    float4 *os32 = (float4 *)(smem_raw + (((size_t)hw * 4 + 15) & ~(size_t)15));
+    d4 *os64 = (d4 *)(os32 + kMaxSmallMol);
+    shist_zero(S, hbase);
+    const Sample sm = samples[sample0 + blockIdx.y];
+    const int s = sm.s;
+    for (int a = threadIdx.x; a < S.aps; a += blockDim.x) {
+        os32[a] = so32[(int64_t)s * S.aps + a];
+        os64[a] = so64[(int64_t)s * S.aps + a];
+    }
+    __syncthreads();
+    SHist h = shist_bind(S, hbase);
+    const FrameGeom &G = *Gp;
+    LocalStats st;
+    const double rs = SELF ? (double)FS->rmax_v : (double)FS->rmax_s;
+    const double rcm = FS->rcmax;
+    const double range = S.cut + rs + rcm;
+    int L[3];
+    const bool ok = stencil(G, range + 1e-6 * (1.0 + range), L);
+    const Guard g = make_guard(S, guard_band(G, L, 2.0 * (rs + rcm)));
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!ok) {
+        if (threadIdx.x == 0) raise_err(S, ERR_STENCIL);
+    } else if (k < S.mv && !(SELF && k == s)) {
+        Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
+        int cp[3];
+        double qp[3];
+        bin_fractional(G, P.fc, cp, qp);
+        const int sc = scell[s];
+        const int cs[3] = {sc % G.n[0], (sc / G.n[0]) % G.n[1], sc / (G.n[0] * G.n[1])};
+        Images im;
+        for (int q = 0; q < 3; ++q) {
+            axis_images(cp[q] - cs[q], G.n[q], L[q], im.base[q], im.cnt[q]);
+            im.step[q] = G.n[q];
+        }
+        const float4 qs32 = sq32[s];
+        const d4 qs64 = sq64[s];
+        const float4 qp32 = make_float4((float)qp[0], (float)qp[1], (float)qp[2], 0.f);
+        const d4 qp64 = make_d4(qp[0], qp[1], qp[2], 0.0);
+        const float rr = (float)(S.cut + rs + rc[P.jmol] + 1e-3 * (1.0 + range));
+        bool any = false;
+        CM_FOR_IMAGES(im, ix, iy, iz) {
+            float4 o = off32[off_index(ix, iy, iz)];
+            float Dx = (qp32.x - qs32.x) + o.x, Dy = (qp32.y - qs32.y) + o.y, Dz = (qp32.z - qs32.z) + o.z;
+            any |= fmaf(Dz, Dz, fmaf(Dy, Dy, Dx * Dx)) <= rr * rr;
+        }
+        if (any) {
+            double A[9];
+            draw_rotation(P.st, A);
+            d4 ov64[kMaxSmallMol];
+            float4 ov32[kMaxSmallMol];
+            const d4 *u = u64 + (int64_t)P.jmol * S.apv;
+            for (int b = 0; b < S.apv; ++b) {
+                d4 w = u[b];
+                double o[3];
+                matvec_rm(A, w.x, w.y, w.z, o);
+                ov64[b] = make_d4(o[0], o[1], o[2], 0.0);
+                ov32[b] = make_float4((float)o[0], (float)o[1], (float)o[2], 0.f);
+            }
+            DirRec r1, r2;
+            st.molpairs++;
+            st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
+            if (FP32) {
+                Pass32 Q;
+                pairs_pass32<false>(S, off32, im, qs32, qp32, os32, ov32, Q);
+                pairs_decide<false>(S, g, Q, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, s, k, r1, r2, st);
+            } else {
+                Exact64 E;
+                pairs_exact<false, false>(S, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, 0.f, 0.f, 0.f, E);
+                records_from_exact<false>(S, E, s, k, r1, r2);
+            }
+            if (r1.within) { apply_hit(S, h, true, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
+        }
+    }
+    stats_flush(S, st, true);
+    __syncthreads();
+    shist_flush(S, h, true);
+}
+
+// ----------------------------------------------------------- ATOMS regime
+__device__ __forceinline__ int pack_cell(const int *c) { return c[0] | (c[1] << 10) | (c[2] << 20); }
+
+// Solvent atoms binned individually (real frame).
+template <typename T>
+__global__ void k_prep_atoms_solvent(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int nmol, int apm, int iref,
+                                     int *__restrict__ acell, float4 *__restrict__ aq32, d4 *__restrict__ aq64,
+                                     d4 *__restrict__ u64, float *__restrict__ rc, float *__restrict__ rcmax) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    const FrameGeom &G = *Gp;
+    const T *x = xyz + (int64_t)m * apm * 3;
+    for (int b = 0; b < apm; ++b) {
+        double xb[3];
+        load_xyz(x + 3 * b, xb);
+        int c[3];
+        double q[3];
+        bin_position(G, xb[0], xb[1], xb[2], c, q);
+        int64_t i = (int64_t)m * apm + b;
+        acell[i] = pack_cell(c);
+        aq32[i] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
+        aq64[i] = make_d4(q[0], q[1], q[2], 0.0);
+    }
+    if (u64) {
+        float r;
+        centroid_data(G, x, apm, iref, u64 + (int64_t)m * apm, r);
+        rc[m] = r;
+        atomic_max_pos(rcmax, r);
+    }
+}
+
+// Solute atoms binned into per-molecule cell lists: key = s * ncell + cell.
+template <typename T>
+__global__ void k_prep_atoms_solute(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int natoms, int aps,
+                                    int *__restrict__ key, float4 *__restrict__ tq32, d4 *__restrict__ tq64,
+                                    int *__restrict__ count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= natoms) return;
+    const FrameGeom &G = *Gp;
+    double x[3];
+    load_xyz(xyz + 3 * (int64_t)i, x);
+    int c[3];
+    double q[3];
+    bin_position(G, x[0], x[1], x[2], c, q);
+    int s = i / aps, a = i - s * aps;
+    int k = s * G.ncell + cell_linear(G, c[0], c[1], c[2]);
+    key[i] = k;
+    tq32[i] = make_float4((float)q[0], (float)q[1], (float)q[2], __int_as_float(a));
+    tq64[i] = make_d4(q[0], q[1], q[2], 0.0);
+    atomicAdd(count + k, 1);
+}
+
+__global__ void k_scatter_atoms(const int *__restrict__ key, int natoms, const float4 *__restrict__ tq32,
+                                const d4 *__restrict__ tq64, int *__restrict__ fill, float4 *__restrict__ sq32,
+                                d4 *__restrict__ sq64) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= natoms) return;
+    int p = atomicAdd(fill + key[i], 1);
+    sq32[p] = tq32[i];
+    sq64[p] = tq64[i];
+}
+
+// Placed solvent for the ATOMS regime: every slot of every sample in the
+// chunk, absolute FP64 positions A u + centre, then binned per atom.
+__global__ void k_atoms_place(DevSys S, const FrameGeom *__restrict__ Gp, const Sample *__restrict__ samples, int sample0,
+                              const d4 *__restrict__ u64, const int *__restrict__ bulk, const int *__restrict__ nbulk,
+                              int *__restrict__ pcell, float4 *__restrict__ pq32, d4 *__restrict__ pq64) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= S.mv) return;
+    const FrameGeom &G = *Gp;
+    const Sample sm = samples[sample0 + blockIdx.y];
+    int64_t base = (int64_t)blockIdx.y * S.mv * S.apv + (int64_t)k * S.apv;
+    if (S.self && k == sm.s) {
+        for (int b = 0; b < S.apv; ++b) pcell[base + b] = -1;
+        return;
+    }
+    Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
+    double A[9];
+    draw_rotation(P.st, A);
+    double cm[3];
+    matvec_cm(G.H, P.fc[0], P.fc[1], P.fc[2], cm);
+    const d4 *u = u64 + (int64_t)P.jmol * S.apv;
+    for (int b = 0; b < S.apv; ++b) {
+        d4 w = u[b];
+        double o[3];
+        matvec_rm(A, w.x, w.y, w.z, o);
+        double y0 = add(o[0], cm[0]), y1 = add(o[1], cm[1]), y2 = add(o[2], cm[2]);
+        int c[3];
+        double q[3];
+        bin_position(G, y0, y1, y2, c, q);
+        pcell[base + b] = pack_cell(c);
+        pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
+        pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
+    }
+}
+
+// FP32 pass of one solvent molecule against one solute molecule's atom cells.
+struct AtomPass {
+    float m1, m2;
+    int p1, b1;   // sorted position of the solute atom, solvent atom index
+    float r1;     // row minimum of the reference atom
+};
+
+// ATOMS regime evaluation: thread per solvent molecule v; grid.y = solute
+// molecule (real pass) or sample of the chunk (random pass).
+template <bool FP32, bool RANDOM>
+__global__ void __launch_bounds__(128)
+    k_atoms_eval(DevSys S, const FrameGeom *__restrict__ Gp, const d4 *__restrict__ off64, const float4 *__restrict__ off32,
+                 const int *__restrict__ sstart, const float4 *__restrict__ sq32, const d4 *__restrict__ sq64,
+                 const int *__restrict__ vcell, const float4 *__restrict__ vq32, const d4 *__restrict__ vq64,
+                 const Sample *__restrict__ samples, int sample0, const int *__restrict__ slot_of_mol,
+                 unsigned char *__restrict__ flags) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    shist_zero(S, hbase);
+    __syncthreads();
+    SHist h = shist_bind(S, hbase);
+    const FrameGeom &G = *Gp;
+    LocalStats st;
+    int s;
+    int64_t vbase = 0;
+    if (RANDOM) {
+        s = samples[sample0 + blockIdx.y].s;
+        vbase = (int64_t)blockIdx.y * S.mv * S.apv;
+    } else {
+        s = blockIdx.y;
+    }
+    int L[3];
+    const bool ok = stencil(G, S.cut * (1.0 + 1e-7) + 1e-7, L);
+    const Guard g = make_guard(S, guard_band(G, L, 0.0));
+    const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int *cs = sstart + (int64_t)s * G.ncell;
+    if (!ok) {
+        if (threadIdx.x == 0) raise_err(S, ERR_STENCIL);
+    } else if (v < S.mv && !(S.self && v == s)) {
+        const int apv = S.apv, iref = S.iref;
+        DirRec r = dir_none(S);
+        auto cells_of = [&](int b, int &cx, int &cy, int &cz) {
+            int c = vcell[vbase + (int64_t)v * apv + b];
+            cx = c & 1023; cy = (c >> 10) & 1023; cz = (c >> 20) & 1023;
+        };
+        // exact (FP64) scan; with FILTER only pairs whose FP32 squared distance
+        // is within the thresholds are evaluated in FP64
+        auto exact = [&](bool filter, float thr_arg, float thr_r1, Best64 &B, double &rr1, long long &evals) {
+            best_init(B);
+            rr1 = INFINITY;
+            evals = 0;
+            for (int b = 0; b < apv; ++b) {
+                int cx, cy, cz;
+                cells_of(b, cx, cy, cz);
+                const d4 qb = vq64[vbase + (int64_t)v * apv + b];
+                const float4 qf = vq32[vbase + (int64_t)v * apv + b];
+                for (int dz = -L[2]; dz <= L[2]; ++dz)
+                    for (int dy = -L[1]; dy <= L[1]; ++dy)
+                        for (int dx = -L[0]; dx <= L[0]; ++dx) {
+                            int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                            int beg = cs[cell], end = cs[cell + 1];
+                            if (beg == end) continue;
+                            int oi = off_index(dx, dy, dz);
+                            d4 o = off64[oi];
+                            double tx = sub(qb.x, o.x), ty = sub(qb.y, o.y), tz = sub(qb.z, o.z);
+                            float4 of = off32[oi];
+                            float fx = qf.x - of.x, fy = qf.y - of.y, fz = qf.z - of.z;
+                            for (int p = beg; p < end; ++p) {
+                                float4 qa32 = sq32[p];
+                                if (filter) {
+                                    float ex = qa32.x - fx, ey = qa32.y - fy, ez = qa32.z - fz;
+                                    float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                                    if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1))) continue;
+                                }
+                                d4 qa = sq64[p];
+                                // displacement solute atom -> solvent atom: (q_b - off) - q_a
+                                double d2 = pair_d2_64(tx, ty, tz, qa.x, qa.y, qa.z);
+                                evals++;
+                                if (d2 <= S.cut2) {
+                                    if (b == iref) rr1 = fmin(rr1, d2);
+                                    best_update<false>(B, d2, __float_as_int(qa32.w), b);
+                                }
+                            }
+                        }
+            }
+        };
+        auto from_exact = [&](Best64 &B, double rr1) {
+            DirRec q = dir_none(S);
+            if (B.d2 <= S.cut2) {
+                double d = best_d(B);
+                q.within = 1;
+                q.i_local = B.a;
+                q.j = (int64_t)v * apv + B.b;
+                q.bin = setbin0(d, S.binstep);
+                q.bulk = inbulk64(S, true, d);
+                if (rr1 <= S.cut2) { q.ref = 1; q.rbin = setbin0(sqrt(rr1), S.binstep); }
+            }
+            return q;
+        };
+        if (!FP32) {
+            Best64 B;
+            double rr1;
+            long long ev;
+            exact(false, 0.f, 0.f, B, rr1, ev);
+            st.atompairs += ev;
+            r = from_exact(B, rr1);
+        } else {
+            AtomPass P;
+            P.m1 = P.m2 = P.r1 = INFINITY;
+            P.p1 = 0;
+            P.b1 = 0;
+            long long evals = 0;
+            for (int b = 0; b < apv; ++b) {
+                int cx, cy, cz;
+                cells_of(b, cx, cy, cz);
+                const float4 qf = vq32[vbase + (int64_t)v * apv + b];
+                const bool isref = b == iref;
+                for (int dz = -L[2]; dz <= L[2]; ++dz)
+                    for (int dy = -L[1]; dy <= L[1]; ++dy)
+                        for (int dx = -L[0]; dx <= L[0]; ++dx) {
+                            int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                            int beg = cs[cell], end = cs[cell + 1];
+                            if (beg == end) continue;
+                            float4 of = off32[off_index(dx, dy, dz)];
+                            float tx = qf.x - of.x, ty = qf.y - of.y, tz = qf.z - of.z;
+                            evals += end - beg;
+                            float row = P.r1;
+                            for (int p = beg; p < end; ++p) {
+                                float4 qa = sq32[p];
+                                float ex = qa.x - tx, ey = qa.y - ty, ez = qa.z - tz;
+                                float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                                P.m2 = fminf(P.m2, fmaxf(P.m1, d2));
+                                bool lt = d2 < P.m1;
+                                P.p1 = lt ? p : P.p1;
+                                P.b1 = lt ? b : P.b1;
+                                P.m1 = fminf(P.m1, d2);
+                                row = fminf(row, d2);
+                            }
+                            if (isref) P.r1 = row;
+                        }
+            }
+            st.atompairs += evals;
+            if (P.m1 <= g.cutp2) {
+                float d1 = sqrtf(P.m1);
+                bool amb = P.m1 >= g.cutm2 || (sqrtf(P.m2) - d1) <= g.two_delta;
+                if (amb) {
+                    float t = d1 + g.two_delta;
+                    float thr1 = -1.f;
+                    if (P.r1 <= g.cutp2) { float u = sqrtf(P.r1) + g.two_delta; thr1 = __fmul_ru(u, u); }
+                    Best64 B;
+                    double rr1;
+                    long long ev;
+                    exact(true, __fmul_ru(t, t), thr1, B, rr1, ev);
+                    r = from_exact(B, rr1);
+                    st.guard++;
+                    st.guard_pairs += ev;
+                    if (B.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(B)));
+                } else {
+                    int bin = bin32(g, d1);
+                    double d64 = -1.0;
+                    const float4 qa32 = sq32[P.p1];
+                    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
+                        // exact distance of the minimum pair: its own image is the
+                        // one of smallest FP64 distance among the stencil cells
+                        int cx, cy, cz;
+                        cells_of(P.b1, cx, cy, cz);
+                        const d4 qb = vq64[vbase + (int64_t)v * apv + P.b1];
+                        const d4 qa = sq64[P.p1];
+                        double best = INFINITY;
+                        for (int dz = -L[2]; dz <= L[2]; ++dz)
+                            for (int dy = -L[1]; dy <= L[1]; ++dy)
+                                for (int dx = -L[0]; dx <= L[0]; ++dx) {
+                                    int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                                    if (P.p1 < cs[cell] || P.p1 >= cs[cell + 1]) continue;
+                                    d4 o = off64[off_index(dx, dy, dz)];
+                                    best = fmin(best, pair_d2_64(sub(qb.x, o.x), sub(qb.y, o.y), sub(qb.z, o.z), qa.x, qa.y, qa.z));
+                                }
+                        d64 = sqrt(best);
+                        bin = setbin0(d64, S.binstep);
+                        st.guard++;
+                        st.guard_pairs++;
+                        st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
+                    }
+                    r.within = 1;
+                    r.i_local = __float_as_int(qa32.w);
+                    r.j = (int64_t)v * apv + P.b1;
+                    r.bin = bin;
+                    r.bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
+                    if (P.r1 <= g.cutp2) {
+                        int rb = P.r1 < g.cutm2 ? bin32(g, sqrtf(P.r1)) : -1;
+                        if (rb >= 0) {
+                            r.ref = 1;
+                            r.rbin = rb;
+                        } else {
+                            float u = sqrtf(P.r1) + g.two_delta;
+                            Best64 B;
+                            double rr1;
+                            long long ev;
+                            exact(true, -1.f, __fmul_ru(u, u), B, rr1, ev);
+                            st.guard++;
+                            st.guard_pairs += ev;
+                            if (rr1 <= S.cut2) { r.ref = 1; r.rbin = setbin0(sqrt(rr1), S.binstep); }
+                        }
+                    }
+                }
+            }
+        }
+        st.molpairs++;
+        if (r.within) { apply_hit(S, h, RANDOM, r.bin, r.i_local, r.j, r.ref, r.rbin); st.hits++; }
+        if (!RANDOM && slot_of_mol) {
+            int sl = slot_of_mol[s];
+            if (sl >= 0) flags[(int64_t)sl * S.mv + v] = flag_code(r);
+        }
+    }
+    stats_flush(S, st, RANDOM);
+    __syncthreads();
+    shist_flush(S, h, RANDOM);
+}
+
+// Weight change: fold the integer class accumulators into FP64 sums
+// (acc += w * count / 2) and clear them.
+__global__ void k_fold(unsigned long long *__restrict__ acc, double *__restrict__ sums, int64_t n, double w) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long c = acc[i];
+    if (c) {
+        sums[i] = add(sums[i], mul(w, div((double)c, 2.0)));
+        acc[i] = 0ull;
+    }
+}
+
+// Slot table of the sampled solute molecules (set / clear).
+__global__ void k_slots(const Sample *__restrict__ samples, int n, int *__restrict__ slot_of_mol, int set) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    slot_of_mol[samples[i].s] = set ? samples[i].d : -1;
+}
+
+}  // namespace cmk

@@ -1,0 +1,967 @@
+// cmgpu.cu -- C ABI and host orchestration of the GB300 MDDF engine.
+//
+// One handle = one system (solute and solvent selections, options) on one
+// device.  Frames are staged into HBM in chunks (double-buffered against the
+// compute stream when they come from host memory) and each frame runs a fixed
+// chain of kernels on the handle's stream.  Counts accumulate in int64 half
+// units per frame-weight class; a change of weight folds the class into FP64
+// sums (sum += w * count / 2), so runs with one weight are exact integers.
+//
+// Replaces (ComplexMixtures.jl): the frame loop of mddf (src/mddf.jl:287-338),
+// mddf_frame! (src/mddf.jl:361-429), coordination_number_frame!
+// (src/mddf.jl:438-471) and sum! (src/results.jl:629-649).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cmgpu.h"
+#include "cm_kernels.cuh"
+
+using namespace cmk;
+using cmgeom::FrameGeom;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct cm_error : std::exception {
+    int code;
+    std::string msg;
+    cm_error(int c, std::string m) : code(c), msg(std::move(m)) {}
+};
+
+#define CM_CUDA(call)                                                                                  \
+    do {                                                                                               \
+        cudaError_t _e = (call);                                                                       \
+        if (_e != cudaSuccess)                                                                         \
+            throw cm_error(CM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e));              \
+    } while (0)
+
+constexpr int kChunkSamples = 32;  // random samples placed per launch in the ATOMS regime
+
+}  // namespace
+
+struct cm_handle {
+    // configuration
+    cm_system_desc d{};
+    std::vector<int64_t> gs_off, gv_off;
+    std::vector<int32_t> gs_idx, gv_idx;
+    int regime = CM_REGIME_PAIRS;
+    int Gs = 0, Gv = 0;
+    int64_t Ns = 0, Nv = 0;
+    int ndist_max = 0;
+    bool mddf = true;
+    int device = 0;
+    cudaStream_t stream = nullptr, copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
+    std::string err;
+
+    // plan
+    bool planned = false;
+    double pair_cell = 0.0;
+    int64_t ncell_cap = 0;
+    int max_frames = 64;
+    int coord_elem = 0;  // bytes per coordinate of the staging buffers
+
+    // device memory
+    std::vector<DevBuf *> owned;
+    int64_t device_bytes = 0;
+    DevBuf geoms, samples, fscratch, off64, off32, hist, sums, stats, errflag, slot_of_mol, flags, bulk, nbulk;
+    DevBuf stage_s[2], stage_v[2];
+    // PAIRS
+    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, u64, rc, ccount, cstart, cfill, cmol;
+    // group tables
+    DevBuf g_soff, g_sidx, g_voff, g_vidx;
+    // ATOMS
+    DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, pcell, pq32, pq64;
+    // pinned host staging
+    FrameGeom *h_geoms[2] = {nullptr, nullptr};
+    Sample *h_samples[2] = {nullptr, nullptr};
+    int64_t h_samples_cap = 0;
+
+    // accumulation state
+    bool class_open = false;
+    double class_w = 1.0;
+    int64_t folds = 0;
+    double volume_total = 0.0, weight_total = 0.0;
+    int64_t frames = 0;
+    int64_t hist_n = 0;
+    int64_t o_md, o_mdr, o_rdf, o_rdfr, o_gs, o_gsr, o_gv, o_gvr;
+    int smem_groups = 0;
+    double last_guard = 0.0;
+    int kernels_per_frame = 0;
+    int chunk_parity = 0;
+};
+
+namespace {
+
+void dev_alloc(cm_handle *h, DevBuf &b, size_t bytes) {
+    if (b.bytes >= bytes && b.p) return;
+    if (b.p) {
+        cudaFree(b.p);
+        h->device_bytes -= (int64_t)b.bytes;
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    if (bytes == 0) bytes = 16;
+    if (h->d.hbm_budget_bytes > 0 && h->device_bytes + (int64_t)bytes > h->d.hbm_budget_bytes)
+        throw cm_error(CM_ENOMEM, "device memory budget exceeded (" + std::to_string(h->device_bytes + (int64_t)bytes) +
+                                      " > " + std::to_string(h->d.hbm_budget_bytes) + " bytes)");
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        throw cm_error(CM_ENOMEM, std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    h->device_bytes += (int64_t)bytes;
+}
+
+template <typename T>
+T *P(DevBuf &b) {
+    return reinterpret_cast<T *>(b.p);
+}
+
+// ----------------------------------------------------------------- geometry
+void cross3(const double *a, const double *b, double *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+double dot3(const double *a, const double *b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+// Geometry of one frame with a grid of target cell side `cs`.
+void frame_geometry(const double *H, double cs, int ncap_axis, FrameGeom &G) {
+    memcpy(G.H, H, 9 * sizeof(double));
+    const double *a = H, *b = H + 3, *c = H + 6;
+    double ab[3], bc[3], ca[3];
+    cross3(a, b, ab);
+    cross3(b, c, bc);
+    cross3(c, a, ca);
+    G.det = dot3(ab, c);
+    if (!(std::fabs(G.det) > 0.0) || !std::isfinite(G.det)) throw cm_error(CM_EINVAL, "degenerate unit cell (zero volume)");
+    for (int m = 0; m < 3; ++m) {
+        G.Hi[0 + m] = bc[m] / G.det;
+        G.Hi[3 + m] = ca[m] / G.det;
+        G.Hi[6 + m] = ab[m] / G.det;
+    }
+    double V = std::fabs(G.det);
+    G.w[0] = V / std::sqrt(dot3(bc, bc));
+    G.w[1] = V / std::sqrt(dot3(ca, ca));
+    G.w[2] = V / std::sqrt(dot3(ab, ab));
+    for (int k = 0; k < 3; ++k) {
+        int n = (int)std::floor(G.w[k] / cs);
+        if (n < 1) n = 1;
+        if (n > ncap_axis) n = ncap_axis;
+        G.n[k] = n;
+        G.cw[k] = G.w[k] / n;
+        for (int m = 0; m < 3; ++m) G.Hn[3 * k + m] = H[3 * k + m] / (double)n;
+    }
+    G.ncell = G.n[0] * G.n[1] * G.n[2];
+}
+
+// Host restatement of the anchor radius of a selection (largest distance of an
+// atom to its molecule's first atom, minimum image), used to size PAIRS cells.
+double anchor_radius(const double *xyz, int nmol, int apm, const double *H) {
+    FrameGeom G;
+    frame_geometry(H, 1e30, 1, G);
+    double r = 0.0;
+    for (int m = 0; m < nmol; ++m) {
+        const double *x0 = xyz + (int64_t)m * apm * 3;
+        for (int a = 1; a < apm; ++a) {
+            double d[3] = {x0[3 * a] - x0[0], x0[3 * a + 1] - x0[1], x0[3 * a + 2] - x0[2]};
+            cmgeom::unwrap(G, d);
+            r = std::max(r, std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+        }
+    }
+    return r;
+}
+
+void check_desc(const cm_system_desc *d) {
+    auto bad = [](const std::string &m) { throw cm_error(CM_EINVAL, m); };
+    if (!d) bad("NULL system description");
+    if (d->api_version != CM_API_VERSION) bad("api_version mismatch");
+    if (d->solute_nmols < 1 || d->solute_natomspermol < 1 || d->solvent_nmols < 1 || d->solvent_natomspermol < 1)
+        bad("selections must have at least one molecule of at least one atom");
+    if (d->autocorrelation && (d->solute_nmols != d->solvent_nmols || d->solute_natomspermol != d->solvent_natomspermol))
+        bad("autocorrelation requires identical solute and solvent selections");
+    if (d->irefatom < 1 || d->irefatom > d->solvent_natomspermol)
+        bad("Reference atom index " + std::to_string(d->irefatom) + " is greater than number of atoms of the solvent molecule.");
+    if (!(d->binstep > 0.0) || !(d->cutoff > 0.0) || !(d->dbulk > 0.0)) bad("cutoff, dbulk and binstep must be positive");
+    if (d->usecutoff && d->dbulk >= d->cutoff) bad("The bulk volume is zero (dbulk must be smaller than cutoff).");
+    double cut = d->usecutoff ? d->cutoff : d->dbulk;
+    int need = std::max(1, (int)std::ceil(cut / d->binstep));
+    if (d->nbins < need) bad("nbins is smaller than setbin(cutoff, binstep)");
+    if (d->n_random_samples < 0) bad("n_random_samples must be >= 0");
+    if (d->mode == CM_MODE_MDDF && d->n_random_samples < 1) bad("n_random_samples must be greater than 0.");
+    if (d->mode != CM_MODE_MDDF && d->mode != CM_MODE_COORDINATION_NUMBER) bad("unknown mode");
+    if (d->precision != CM_PRECISION_FP64 && d->precision != CM_PRECISION_FP32_GUARD) bad("unknown precision");
+    if (d->regime < CM_REGIME_AUTO || d->regime > CM_REGIME_ATOMS) bad("unknown regime");
+    if (d->lcell < 1) bad("lcell must be >= 1");
+    int64_t Nv = (int64_t)d->solvent_nmols * d->solvent_natomspermol;
+    int64_t Ns = (int64_t)d->solute_nmols * d->solute_natomspermol;
+    if (Ns >= (1LL << 31) || Nv >= (1LL << 31)) bad("selections above 2^31 atoms are not supported");
+    if ((d->solute_group_offsets == nullptr) != (d->solute_groups == nullptr) ||
+        (d->solvent_group_offsets == nullptr) != (d->solvent_groups == nullptr))
+        bad("group CSR needs both offsets and indices");
+    if (d->solute_group_offsets && d->solute_ngroups < 1) bad("solute_ngroups must be >= 1 with custom groups");
+    if (d->solvent_group_offsets && d->solvent_ngroups < 1) bad("solvent_ngroups must be >= 1 with custom groups");
+}
+
+void copy_csr(int64_t natoms, int ngroups, const int64_t *off, const int32_t *idx, std::vector<int64_t> &o,
+              std::vector<int32_t> &ix, const char *what) {
+    o.assign(off, off + natoms + 1);
+    if (o[0] != 0) throw cm_error(CM_EINVAL, std::string(what) + " group offsets must start at 0");
+    for (int64_t i = 0; i < natoms; ++i)
+        if (o[i + 1] < o[i]) throw cm_error(CM_EINVAL, std::string(what) + " group offsets must be non-decreasing");
+    ix.assign(idx, idx + o[natoms]);
+    for (int32_t g : ix)
+        if (g < 0 || g >= ngroups) throw cm_error(CM_EINVAL, std::string(what) + " group index out of range");
+}
+
+DevSys make_devsys(cm_handle *h) {
+    DevSys S{};
+    const cm_system_desc &d = h->d;
+    S.ms = d.solute_nmols;
+    S.aps = d.solute_natomspermol;
+    S.mv = d.solvent_nmols;
+    S.apv = d.solvent_natomspermol;
+    S.self = d.autocorrelation ? 1 : 0;
+    S.iref = d.irefatom - 1;
+    S.nbins = d.nbins;
+    S.nrs = h->mddf ? d.n_random_samples : 0;
+    S.fp32 = d.precision == CM_PRECISION_FP32_GUARD;
+    S.usecutoff = d.usecutoff ? 1 : 0;
+    S.Gs = h->Gs;
+    S.Gv = h->Gv;
+    S.default_s = h->gs_off.empty() ? 1 : 0;
+    S.default_v = h->gv_off.empty() ? 1 : 0;
+    S.smem_groups = h->smem_groups;
+    S.cut = d.usecutoff ? d.cutoff : d.dbulk;  // src/minimum_distances.jl:166
+    S.cut2 = S.cut * S.cut;
+    S.binstep = d.binstep;
+    S.dbulk = d.dbulk;
+    S.seed = d.seed;
+    S.gs_off = nullptr;
+    S.gs_idx = nullptr;
+    S.gv_off = nullptr;
+    S.gv_idx = nullptr;
+    S.hist = P<unsigned long long>(h->hist);
+    S.o_md = h->o_md; S.o_mdr = h->o_mdr; S.o_rdf = h->o_rdf; S.o_rdfr = h->o_rdfr;
+    S.o_gs = h->o_gs; S.o_gsr = h->o_gsr; S.o_gv = h->o_gv; S.o_gvr = h->o_gvr;
+    S.stats = P<unsigned long long>(h->stats);
+    S.err = P<int>(h->errflag);
+    return S;
+}
+
+size_t hist_smem_bytes(const cm_handle *h, int smem_groups) {
+    int words = h->d.nbins * (2 + (smem_groups ? (h->Gs + (h->d.autocorrelation ? 0 : h->Gv)) : 0));
+    return ((size_t)words * 4 + 15) & ~(size_t)15;
+}
+
+}  // namespace
+
+namespace {
+
+DevSys devsys_full(cm_handle *h) {
+    DevSys S = make_devsys(h);
+    if (!h->gs_off.empty()) {
+        S.gs_off = P<int64_t>(h->g_soff);
+        S.gs_idx = P<int32_t>(h->g_sidx);
+    }
+    if (!h->gv_off.empty()) {
+        S.gv_off = P<int64_t>(h->g_voff);
+        S.gv_idx = P<int32_t>(h->g_vidx);
+    }
+    return S;
+}
+
+void upload_groups(cm_handle *h) {
+    auto up = [&](DevBuf &b, const void *src, size_t bytes) {
+        dev_alloc(h, b, bytes);
+        if (bytes) CM_CUDA(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
+    };
+    if (!h->gs_off.empty()) {
+        up(h->g_soff, h->gs_off.data(), h->gs_off.size() * 8);
+        up(h->g_sidx, h->gs_idx.data(), std::max<size_t>(h->gs_idx.size() * 4, 4));
+    }
+    if (!h->gv_off.empty()) {
+        up(h->g_voff, h->gv_off.data(), h->gv_off.size() * 8);
+        up(h->g_vidx, h->gv_idx.data(), std::max<size_t>(h->gv_idx.size() * 4, 4));
+    }
+}
+
+double target_cell(const cm_handle *h) {
+    double cut = h->d.usecutoff ? h->d.cutoff : h->d.dbulk;
+    if (h->regime == CM_REGIME_ATOMS) return cut / h->d.lcell * (1.0 + 1e-6);
+    return h->pair_cell;
+}
+
+// Reallocate the cell arrays if a frame needs more cells than planned.
+void ensure_cells(cm_handle *h, int64_t ncell) {
+    if (ncell <= h->ncell_cap) return;
+    h->ncell_cap = ncell;
+    if (h->regime == CM_REGIME_PAIRS) {
+        dev_alloc(h, h->ccount, (ncell + 1) * 4);
+        dev_alloc(h, h->cstart, (ncell + 1) * 4);
+        dev_alloc(h, h->cfill, (ncell + 1) * 4);
+    } else {
+        int64_t n = (int64_t)h->d.solute_nmols * ncell + 1;
+        dev_alloc(h, h->acount, n * 4);
+        dev_alloc(h, h->astart, n * 4);
+        dev_alloc(h, h->afill, n * 4);
+    }
+}
+
+void plan(cm_handle *h, const cm_frames *f) {
+    const cm_system_desc &d = h->d;
+    h->coord_elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
+    // radii of the first frame for the PAIRS cell size
+    if (h->regime == CM_REGIME_PAIRS) {
+        std::vector<double> xs(h->Ns * 3), xv;
+        auto fetch = [&](const void *src, int64_t n, std::vector<double> &out) {
+            out.resize(n * 3);
+            std::vector<char> raw(n * 3 * h->coord_elem);
+            if (f->memory == CM_MEM_DEVICE) CM_CUDA(cudaMemcpy(raw.data(), src, raw.size(), cudaMemcpyDeviceToHost));
+            else memcpy(raw.data(), src, raw.size());
+            for (int64_t i = 0; i < n * 3; ++i)
+                out[i] = h->coord_elem == 4 ? (double)reinterpret_cast<float *>(raw.data())[i] : reinterpret_cast<double *>(raw.data())[i];
+        };
+        fetch(f->solute_xyz, h->Ns, xs);
+        double rs = anchor_radius(xs.data(), d.solute_nmols, d.solute_natomspermol, f->cells);
+        double rv = rs;
+        if (!d.autocorrelation) {
+            fetch(f->solvent_xyz, h->Nv, xv);
+            rv = anchor_radius(xv.data(), d.solvent_nmols, d.solvent_natomspermol, f->cells);
+        }
+        double cut = d.usecutoff ? d.cutoff : d.dbulk;
+        h->pair_cell = (cut + rs + rv) * 1.05 + 0.25;
+    }
+    h->max_frames = d.max_frames_per_batch > 0 ? d.max_frames_per_batch : 64;
+
+    // common buffers
+    dev_alloc(h, h->geoms, sizeof(FrameGeom) * h->max_frames * 2);
+    dev_alloc(h, h->fscratch, sizeof(FrameScratch));
+    dev_alloc(h, h->off64, sizeof(d4) * cmgeom::kOffEntries);
+    dev_alloc(h, h->off32, sizeof(float4) * cmgeom::kOffEntries);
+    for (int i = 0; i < 2; ++i) {
+        CM_CUDA(cudaMallocHost((void **)&h->h_geoms[i], sizeof(FrameGeom) * h->max_frames));
+    }
+    if (h->mddf) {
+        int nd = h->ndist_max;
+        dev_alloc(h, h->slot_of_mol, (size_t)d.solute_nmols * 4);
+        CM_CUDA(cudaMemset(h->slot_of_mol.p, 0xff, (size_t)d.solute_nmols * 4));
+        dev_alloc(h, h->flags, (size_t)nd * d.solvent_nmols);
+        dev_alloc(h, h->bulk, (size_t)nd * d.solvent_nmols * 4);
+        dev_alloc(h, h->nbulk, (size_t)nd * 4);
+        h->h_samples_cap = (int64_t)h->max_frames * d.n_random_samples;
+        dev_alloc(h, h->samples, sizeof(Sample) * h->h_samples_cap * 2);
+        for (int i = 0; i < 2; ++i) CM_CUDA(cudaMallocHost((void **)&h->h_samples[i], sizeof(Sample) * h->h_samples_cap));
+    }
+    // staging for host coordinates
+    if (f->memory == CM_MEM_HOST) {
+        for (int i = 0; i < 2; ++i) {
+            dev_alloc(h, h->stage_s[i], (size_t)h->max_frames * h->Ns * 3 * h->coord_elem);
+            if (!d.autocorrelation) dev_alloc(h, h->stage_v[i], (size_t)h->max_frames * h->Nv * 3 * h->coord_elem);
+        }
+    }
+    int64_t ms = d.solute_nmols, mv = d.solvent_nmols;
+    if (h->regime == CM_REGIME_PAIRS) {
+        dev_alloc(h, h->scell, ms * 4);
+        dev_alloc(h, h->sq32, ms * 16);
+        dev_alloc(h, h->sq64, ms * 32);
+        dev_alloc(h, h->so32, h->Ns * 16);
+        dev_alloc(h, h->so64, h->Ns * 32);
+        if (!d.autocorrelation) {
+            dev_alloc(h, h->vcell, mv * 4);
+            dev_alloc(h, h->vq32, mv * 16);
+            dev_alloc(h, h->vq64, mv * 32);
+            dev_alloc(h, h->vo32, h->Nv * 16);
+            dev_alloc(h, h->vo64, h->Nv * 32);
+        }
+        dev_alloc(h, h->cmol, mv * 4);
+    } else {
+        dev_alloc(h, h->akey, h->Ns * 4);
+        dev_alloc(h, h->atq32, h->Ns * 16);
+        dev_alloc(h, h->atq64, h->Ns * 32);
+        dev_alloc(h, h->asq32, h->Ns * 16);
+        dev_alloc(h, h->asq64, h->Ns * 32);
+        dev_alloc(h, h->avcell, h->Nv * 4);
+        dev_alloc(h, h->avq32, h->Nv * 16);
+        dev_alloc(h, h->avq64, h->Nv * 32);
+        if (h->mddf) {
+            int chunk = std::min(kChunkSamples, std::max(1, d.n_random_samples));
+            dev_alloc(h, h->pcell, (size_t)chunk * h->Nv * 4);
+            dev_alloc(h, h->pq32, (size_t)chunk * h->Nv * 16);
+            dev_alloc(h, h->pq64, (size_t)chunk * h->Nv * 32);
+        }
+    }
+    if (h->mddf) {
+        dev_alloc(h, h->u64, h->Nv * 32);
+        dev_alloc(h, h->rc, mv * 4);
+    }
+    // histogram shared-memory plan
+    size_t extra = h->regime == CM_REGIME_PAIRS ? (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8 : 0;
+    h->smem_groups = hist_smem_bytes(h, 1) + extra + 2048 <= 160 * 1024 ? 1 : 0;
+    size_t smem_real = hist_smem_bytes(h, h->smem_groups) + extra;
+    size_t smem_rand = hist_smem_bytes(h, h->smem_groups) + kMaxSmallMol * 48;
+    size_t smem_max = std::max(smem_real, smem_rand);
+    if (smem_max > 48 * 1024) {
+        int a = (int)smem_max;
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+    }
+    h->planned = true;
+}
+
+// Reference solute molecules of one frame (src/mddf.jl:374-376), sorted, with
+// their repetition number and distinct index.
+int draw_samples(const cm_handle *h, int64_t frame_id, Sample *out, int &ndistinct) {
+    const cm_system_desc &d = h->d;
+    int nrs = d.n_random_samples;
+    uint64_t st = cmfeed::key(d.seed, cmfeed::kTagRef, (uint64_t)frame_id, 0, 0);
+    std::vector<int> s(nrs);
+    for (int i = 0; i < nrs; ++i) s[i] = (int)cmfeed::below(st, (uint64_t)d.solute_nmols);
+    std::sort(s.begin(), s.end());
+    ndistinct = 0;
+    for (int i = 0; i < nrs; ++i) {
+        if (i == 0 || s[i] != s[i - 1]) {
+            out[i].rep = 0;
+            out[i].d = ndistinct++;
+        } else {
+            out[i].rep = out[i - 1].rep + 1;
+            out[i].d = out[i - 1].d;
+        }
+        out[i].s = s[i];
+        out[i].pad = 0;
+    }
+    return nrs;
+}
+
+int grid_for(int64_t n, int block) { return (int)std::max<int64_t>(1, (n + block - 1) / block); }
+
+template <typename T>
+void run_frame(cm_handle *h, const FrameGeom *dG, const FrameGeom &G, const Sample *dS, int nsamp, int ndist, const T *xs,
+               const T *xv) {
+    const cm_system_desc &d = h->d;
+    cudaStream_t st = h->stream;
+    DevSys S = devsys_full(h);
+    const bool self = d.autocorrelation;
+    const bool fp32 = d.precision == CM_PRECISION_FP32_GUARD;
+    const int ms = d.solute_nmols, mv = d.solvent_nmols, aps = d.solute_natomspermol, apv = d.solvent_natomspermol;
+    const int iref = d.irefatom - 1;
+    FrameScratch *FS = P<FrameScratch>(h->fscratch);
+    int launches = 0;
+    CM_CUDA(cudaMemsetAsync(FS, 0, sizeof(FrameScratch), st));
+    k_offtable<<<grid_for(cmgeom::kOffEntries, 256), 256, 0, st>>>(dG, P<d4>(h->off64), P<float4>(h->off32));
+    launches++;
+    const bool rnd = h->mddf && nsamp > 0;
+    if (rnd) {
+        k_slots<<<grid_for(nsamp, 256), 256, 0, st>>>(dS, nsamp, P<int>(h->slot_of_mol), 1);
+        launches++;
+    }
+    const size_t hsm = hist_smem_bytes(h, h->smem_groups);
+    if (h->regime == CM_REGIME_PAIRS) {
+        ensure_cells(h, G.ncell);
+        if (rnd) CM_CUDA(cudaMemsetAsync(h->flags.p, 0, (size_t)ndist * mv, st));
+        CM_CUDA(cudaMemsetAsync(h->ccount.p, 0, (size_t)(G.ncell + 1) * 4, st));
+        // solute molecules (and, in self mode, the solvent cell list)
+        float *rmax_s = self ? &FS->rmax_v : &FS->rmax_s;
+        k_prep_pairs<T><<<grid_for(ms, 128), 128, 0, st>>>(dG, xs, ms, aps, iref, P<int>(h->scell), P<float4>(h->sq32), P<d4>(h->sq64),
+                                                          P<float4>(h->so32), P<d4>(h->so64), self ? P<int>(h->ccount) : nullptr,
+                                                          rmax_s, (self && h->mddf) ? P<d4>(h->u64) : nullptr, P<float>(h->rc));
+        launches++;
+        if (!self) {
+            k_prep_pairs<T><<<grid_for(mv, 128), 128, 0, st>>>(dG, xv, mv, apv, iref, P<int>(h->vcell), P<float4>(h->vq32),
+                                                              P<d4>(h->vq64), P<float4>(h->vo32), P<d4>(h->vo64),
+                                                              P<int>(h->ccount), &FS->rmax_v, h->mddf ? P<d4>(h->u64) : nullptr,
+                                                              P<float>(h->rc));
+            launches++;
+        }
+        k_scan<<<1, 1024, 0, st>>>(P<int>(h->ccount), G.ncell, P<int>(h->cstart), P<int>(h->cfill));
+        k_scatter_mols<<<grid_for(mv, 256), 256, 0, st>>>(self ? P<int>(h->scell) : P<int>(h->vcell), mv, P<int>(h->cfill), P<int>(h->cmol));
+        launches += 2;
+        const int *vcell = self ? P<int>(h->scell) : P<int>(h->vcell);
+        (void)vcell;
+        const float4 *vq32 = self ? P<float4>(h->sq32) : P<float4>(h->vq32);
+        const d4 *vq64 = self ? P<d4>(h->sq64) : P<d4>(h->vq64);
+        const float4 *vo32 = self ? P<float4>(h->so32) : P<float4>(h->vo32);
+        const d4 *vo64 = self ? P<d4>(h->so64) : P<d4>(h->vo64);
+        size_t smem = hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
+        int dev_sms = 0;
+        CM_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device));
+        int grid = std::min<int64_t>((ms + kWarps - 1) / kWarps, (int64_t)dev_sms * 8);
+        const int *slot = rnd ? P<int>(h->slot_of_mol) : nullptr;
+        unsigned char *flags = rnd ? P<unsigned char>(h->flags) : nullptr;
+#define CM_PAIRS_REAL(F, SF)                                                                                                      \
+    k_pairs_real<F, SF><<<grid, kWarps * 32, smem, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), P<int>(h->scell),  \
+                                                         P<float4>(h->sq32), P<d4>(h->sq64), P<float4>(h->so32),              \
+                                                         P<d4>(h->so64), vq32, vq64, vo32, vo64, P<int>(h->cstart),           \
+                                                         P<int>(h->cmol), slot, flags)
+        if (fp32 && self) CM_PAIRS_REAL(true, true);
+        else if (fp32) CM_PAIRS_REAL(true, false);
+        else if (self) CM_PAIRS_REAL(false, true);
+        else CM_PAIRS_REAL(false, false);
+#undef CM_PAIRS_REAL
+        launches++;
+        if (rnd) {
+            k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk), P<int>(h->nbulk));
+            launches++;
+            size_t smr = hsm + kMaxSmallMol * 48;
+            for (int s0 = 0; s0 < nsamp; s0 += 65535) {
+                int ny = std::min(65535, nsamp - s0);
+                dim3 gr(grid_for(mv, 128), ny);
+#define CM_PAIRS_RAND(F, SF)                                                                                                   \
+    k_pairs_random<F, SF><<<gr, 128, smr, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), dS, s0, P<int>(h->scell), \
+                                                P<float4>(h->sq32), P<d4>(h->sq64), P<float4>(h->so32), P<d4>(h->so64), \
+                                                P<d4>(h->u64), P<float>(h->rc), P<int>(h->bulk), P<int>(h->nbulk))
+                if (fp32 && self) CM_PAIRS_RAND(true, true);
+                else if (fp32) CM_PAIRS_RAND(true, false);
+                else if (self) CM_PAIRS_RAND(false, true);
+                else CM_PAIRS_RAND(false, false);
+#undef CM_PAIRS_RAND
+                launches++;
+            }
+        }
+    } else {
+        ensure_cells(h, G.ncell);
+        const T *xsolv = self ? xs : xv;
+        k_prep_atoms_solvent<T><<<grid_for(mv, 128), 128, 0, st>>>(dG, xsolv, mv, apv, iref, P<int>(h->avcell), P<float4>(h->avq32),
+                                                                  P<d4>(h->avq64), h->mddf ? P<d4>(h->u64) : nullptr,
+                                                                  P<float>(h->rc), &FS->rcmax);
+        int64_t nkeys = (int64_t)ms * G.ncell;
+        CM_CUDA(cudaMemsetAsync(h->acount.p, 0, (size_t)(nkeys + 1) * 4, st));
+        k_prep_atoms_solute<T><<<grid_for(h->Ns, 256), 256, 0, st>>>(dG, xs, (int)h->Ns, aps, P<int>(h->akey), P<float4>(h->atq32),
+                                                                    P<d4>(h->atq64), P<int>(h->acount));
+        k_scan<<<1, 1024, 0, st>>>(P<int>(h->acount), (int)nkeys, P<int>(h->astart), P<int>(h->afill));
+        k_scatter_atoms<<<grid_for(h->Ns, 256), 256, 0, st>>>(P<int>(h->akey), (int)h->Ns, P<float4>(h->atq32), P<d4>(h->atq64),
+                                                             P<int>(h->afill), P<float4>(h->asq32), P<d4>(h->asq64));
+        launches += 4;
+        const int *slot = rnd ? P<int>(h->slot_of_mol) : nullptr;
+        unsigned char *flags = rnd ? P<unsigned char>(h->flags) : nullptr;
+        dim3 gr(grid_for(mv, 128), ms);
+#define CM_ATOMS(F, R, GRID, VC, VQ32, VQ64, S0)                                                                                  \
+    k_atoms_eval<F, R><<<GRID, 128, hsm, st>>>(S, dG, P<d4>(h->off64), P<float4>(h->off32), P<int>(h->astart),             \
+                                               P<float4>(h->asq32), P<d4>(h->asq64), VC, VQ32, VQ64, dS, S0, slot, flags)
+        if (fp32) CM_ATOMS(true, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
+        else CM_ATOMS(false, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
+        launches++;
+        if (rnd) {
+            k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk), P<int>(h->nbulk));
+            launches++;
+            for (int s0 = 0; s0 < nsamp; s0 += kChunkSamples) {
+                int ny = std::min(kChunkSamples, nsamp - s0);
+                dim3 gp(grid_for(mv, 128), ny);
+                k_atoms_place<<<gp, 128, 0, st>>>(S, dG, dS, s0, P<d4>(h->u64), P<int>(h->bulk), P<int>(h->nbulk), P<int>(h->pcell),
+                                                  P<float4>(h->pq32), P<d4>(h->pq64));
+                if (fp32) CM_ATOMS(true, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
+                else CM_ATOMS(false, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
+                launches += 2;
+            }
+        }
+#undef CM_ATOMS
+    }
+    if (rnd) {
+        k_slots<<<grid_for(nsamp, 256), 256, 0, st>>>(dS, nsamp, P<int>(h->slot_of_mol), 0);
+        launches++;
+    }
+    CM_CUDA(cudaGetLastError());
+    h->kernels_per_frame = launches;
+}
+
+void fold_class(cm_handle *h) {
+    if (!h->class_open) return;
+    k_fold<<<grid_for(h->hist_n, 256), 256, 0, h->stream>>>(P<unsigned long long>(h->hist), P<double>(h->sums), h->hist_n, h->class_w);
+    CM_CUDA(cudaGetLastError());
+    h->folds++;
+    h->class_open = false;
+}
+
+void submit(cm_handle *h, const cm_frames *f) {
+    const cm_system_desc &d = h->d;
+    if (!f || f->nframes < 0) throw cm_error(CM_EINVAL, "invalid frame batch");
+    if (f->nframes == 0) return;
+    if (!f->solute_xyz || !f->cells || !f->frame_ids) throw cm_error(CM_EINVAL, "solute_xyz, cells and frame_ids are required");
+    if (!d.autocorrelation && !f->solvent_xyz) throw cm_error(CM_EINVAL, "solvent_xyz is required unless autocorrelation");
+    if (f->coord_type != CM_COORD_F32 && f->coord_type != CM_COORD_F64) throw cm_error(CM_EINVAL, "unknown coord_type");
+    if (f->memory != CM_MEM_HOST && f->memory != CM_MEM_DEVICE) throw cm_error(CM_EINVAL, "unknown memory kind");
+    if (!h->planned) plan(h, f);
+    int elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
+    if (elem != h->coord_elem && f->memory == CM_MEM_HOST)
+        throw cm_error(CM_EINVAL, "coordinate type differs from the first batch of this handle");
+    for (int i = 0; i < f->nframes; ++i) {
+        double w = f->weights ? f->weights[i] : 1.0;
+        if (!std::isfinite(w) || w < 0.0) throw cm_error(CM_EINVAL, "frame weights must be finite and non-negative");
+    }
+    const double cs = target_cell(h);
+    const int64_t sbytes = h->Ns * 3 * elem, vbytes = h->Nv * 3 * elem;
+    for (int f0 = 0; f0 < f->nframes; f0 += h->max_frames) {
+        const int nf = std::min(h->max_frames, f->nframes - f0);
+        const int b = h->chunk_parity;
+        h->chunk_parity ^= 1;
+        // host staging of this chunk may be reused only after its previous copy finished
+        CM_CUDA(cudaEventSynchronize(h->ev_copied[b]));
+        FrameGeom *hg = h->h_geoms[b];
+        Sample *hs = h->h_samples[b];
+        std::vector<int> ndist(nf, 0), nsamp(nf, 0);
+        int64_t soff = 0;
+        for (int i = 0; i < nf; ++i) {
+            FrameGeom &G = hg[i];
+            memset(&G, 0, sizeof(G));
+            frame_geometry(f->cells + 9 * (int64_t)(f0 + i), cs, 1023, G);
+            G.weight = f->weights ? f->weights[f0 + i] : 1.0;
+            G.frame_id = f->frame_ids[f0 + i];
+            G.sample_off = (int)soff;
+            if (h->mddf) {
+                nsamp[i] = draw_samples(h, G.frame_id, hs + soff, ndist[i]);
+                G.nsamples = nsamp[i];
+                G.ndistinct = ndist[i];
+                soff += nsamp[i];
+            }
+        }
+        cudaStream_t cp = f->memory == CM_MEM_HOST ? h->copy_stream : h->stream;
+        CM_CUDA(cudaStreamWaitEvent(cp, h->ev_done[b], 0));
+        FrameGeom *dG = P<FrameGeom>(h->geoms) + (size_t)b * h->max_frames;
+        Sample *dS = h->mddf ? P<Sample>(h->samples) + (size_t)b * h->h_samples_cap : nullptr;
+        CM_CUDA(cudaMemcpyAsync(dG, hg, sizeof(FrameGeom) * nf, cudaMemcpyHostToDevice, cp));
+        if (h->mddf && soff > 0) CM_CUDA(cudaMemcpyAsync(dS, hs, sizeof(Sample) * soff, cudaMemcpyHostToDevice, cp));
+        const char *xs_base, *xv_base = nullptr;
+        if (f->memory == CM_MEM_HOST) {
+            CM_CUDA(cudaMemcpyAsync(h->stage_s[b].p, (const char *)f->solute_xyz + sbytes * f0, (size_t)sbytes * nf,
+                                    cudaMemcpyHostToDevice, cp));
+            xs_base = (const char *)h->stage_s[b].p;
+            if (!d.autocorrelation) {
+                CM_CUDA(cudaMemcpyAsync(h->stage_v[b].p, (const char *)f->solvent_xyz + vbytes * f0, (size_t)vbytes * nf,
+                                        cudaMemcpyHostToDevice, cp));
+                xv_base = (const char *)h->stage_v[b].p;
+            }
+        } else {
+            xs_base = (const char *)f->solute_xyz + sbytes * f0;
+            if (!d.autocorrelation) xv_base = (const char *)f->solvent_xyz + vbytes * f0;
+        }
+        CM_CUDA(cudaEventRecord(h->ev_copied[b], cp));
+        CM_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copied[b], 0));
+        for (int i = 0; i < nf; ++i) {
+            const FrameGeom &G = hg[i];
+            if (G.weight == 0.0) continue;  // zero-weight frames are skipped (src/mddf.jl:102)
+            if (h->class_open && G.weight != h->class_w) fold_class(h);
+            h->class_open = true;
+            h->class_w = G.weight;
+            if (G.ncell > h->ncell_cap) ensure_cells(h, G.ncell);
+            const char *xs = xs_base + sbytes * i;
+            const char *xv = xv_base ? xv_base + vbytes * i : nullptr;
+            const Sample *dSi = dS ? dS + G.sample_off : nullptr;
+            if (elem == 4)
+                run_frame<float>(h, dG + i, G, dSi, G.nsamples, G.ndistinct, (const float *)xs, (const float *)xv);
+            else
+                run_frame<double>(h, dG + i, G, dSi, G.nsamples, G.ndistinct, (const double *)xs, (const double *)xv);
+            h->volume_total += G.weight * G.det;  // src/mddf.jl:352
+            h->weight_total += G.weight;
+            h->frames++;
+        }
+        CM_CUDA(cudaEventRecord(h->ev_done[b], h->stream));
+    }
+}
+
+void check_device_error(cm_handle *h) {
+    CM_CUDA(cudaStreamSynchronize(h->stream));
+    int e = 0;
+    CM_CUDA(cudaMemcpy(&e, h->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        std::string m = "device-side check failed:";
+        if (e & ERR_STENCIL) m += " search range wider than the offset table (box too small for the cutoff);";
+        if (e & ERR_BIN) m += " histogram bin out of range;";
+        if (e & ERR_QUEUE) m += " candidate queue overflow;";
+        if (e & ERR_SIZE) m += " molecule too large for the PAIRS layout;";
+        throw cm_error(CM_EDEVICE, m);
+    }
+}
+
+template <typename F>
+int guarded(cm_handle *h, F &&fn) {
+    if (!h) {
+        g_create_error = "NULL handle";
+        return CM_EINVAL;
+    }
+    try {
+        CM_CUDA(cudaSetDevice(h->device));
+        fn();
+        return CM_OK;
+    } catch (const cm_error &e) {
+        h->err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        h->err = "host allocation failed";
+        return CM_ENOMEM;
+    } catch (const std::exception &e) {
+        h->err = e.what();
+        return CM_ECUDA;
+    }
+}
+
+void free_all(cm_handle *h) {
+    DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag,
+                     &h->slot_of_mol, &h->flags, &h->bulk, &h->nbulk, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
+                     &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
+                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->akey, &h->atq32,
+                     &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
+                     &h->pcell, &h->pq32, &h->pq64, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx};
+    for (DevBuf *b : all) {
+        if (b->p) cudaFree(b->p);
+        b->p = nullptr;
+        b->bytes = 0;
+    }
+    for (int i = 0; i < 2; ++i) {
+        if (h->h_geoms[i]) cudaFreeHost(h->h_geoms[i]);
+        if (h->h_samples[i]) cudaFreeHost(h->h_samples[i]);
+        h->h_geoms[i] = nullptr;
+        h->h_samples[i] = nullptr;
+        if (h->ev_copied[i]) cudaEventDestroy(h->ev_copied[i]);
+        if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
+    }
+    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int cm_create(const cm_system_desc *desc, cm_handle **out) {
+    if (!out) {
+        g_create_error = "NULL output pointer";
+        return CM_EINVAL;
+    }
+    *out = nullptr;
+    cm_handle *h = nullptr;
+    try {
+        check_desc(desc);
+        h = new cm_handle();
+        h->d = *desc;
+        h->device = desc->device;
+        h->Ns = (int64_t)desc->solute_nmols * desc->solute_natomspermol;
+        h->Nv = (int64_t)desc->solvent_nmols * desc->solvent_natomspermol;
+        h->mddf = desc->mode == CM_MODE_MDDF;
+        if (desc->solute_group_offsets) {
+            copy_csr(desc->solute_natomspermol, desc->solute_ngroups, desc->solute_group_offsets, desc->solute_groups, h->gs_off,
+                     h->gs_idx, "solute");
+            h->Gs = desc->solute_ngroups;
+        } else {
+            h->Gs = desc->solute_natomspermol;
+        }
+        if (desc->solvent_group_offsets) {
+            copy_csr(h->Nv, desc->solvent_ngroups, desc->solvent_group_offsets, desc->solvent_groups, h->gv_off, h->gv_idx, "solvent");
+            h->Gv = desc->solvent_ngroups;
+        } else {
+            h->Gv = desc->solvent_natomspermol;
+        }
+        if (desc->autocorrelation && h->Gv != h->Gs)
+            throw cm_error(CM_EINVAL, "in self mode the solvent groups must describe the solute selection");
+        int rg = desc->regime;
+        if (rg == CM_REGIME_AUTO)
+            rg = (desc->solute_natomspermol <= kMaxSmallMol && desc->solvent_natomspermol <= kMaxSmallMol) ? CM_REGIME_PAIRS : CM_REGIME_ATOMS;
+        if (rg == CM_REGIME_PAIRS && (desc->solute_natomspermol > kMaxSmallMol || desc->solvent_natomspermol > kMaxSmallMol))
+            throw cm_error(CM_EINVAL, "the PAIRS layout supports at most 32 atoms per molecule");
+        h->regime = rg;
+        h->ndist_max = h->mddf ? std::max(1, std::min(desc->solute_nmols, desc->n_random_samples)) : 0;
+        CM_CUDA(cudaSetDevice(h->device));
+        CM_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        CM_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            CM_CUDA(cudaEventCreateWithFlags(&h->ev_copied[i], cudaEventDisableTiming));
+            CM_CUDA(cudaEventCreateWithFlags(&h->ev_done[i], cudaEventDisableTiming));
+            CM_CUDA(cudaEventRecord(h->ev_copied[i], h->stream));
+            CM_CUDA(cudaEventRecord(h->ev_done[i], h->stream));
+        }
+        // histogram layout
+        int64_t nb = desc->nbins;
+        int64_t Gv = desc->autocorrelation ? 0 : h->Gv;
+        h->o_md = 0;
+        h->o_mdr = nb;
+        h->o_rdf = 2 * nb;
+        h->o_rdfr = 3 * nb;
+        h->o_gs = 4 * nb;
+        h->o_gsr = h->o_gs + h->Gs * nb;
+        h->o_gv = h->o_gsr + h->Gs * nb;
+        h->o_gvr = h->o_gv + Gv * nb;
+        h->hist_n = h->o_gvr + Gv * nb;
+        dev_alloc(h, h->hist, h->hist_n * 8);
+        dev_alloc(h, h->sums, h->hist_n * 8);
+        dev_alloc(h, h->stats, ST_N * 8);
+        dev_alloc(h, h->errflag, 8);
+        CM_CUDA(cudaMemset(h->hist.p, 0, h->hist_n * 8));
+        CM_CUDA(cudaMemset(h->sums.p, 0, h->hist_n * 8));
+        CM_CUDA(cudaMemset(h->stats.p, 0, ST_N * 8));
+        CM_CUDA(cudaMemset(h->errflag.p, 0, 8));
+        upload_groups(h);
+        CM_CUDA(cudaDeviceSynchronize());
+        *out = h;
+        return CM_OK;
+    } catch (const cm_error &e) {
+        g_create_error = e.msg;
+        if (h) { free_all(h); delete h; }
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_create_error = "host allocation failed";
+        if (h) { free_all(h); delete h; }
+        return CM_ENOMEM;
+    }
+}
+
+int cm_submit_frames(cm_handle *h, const cm_frames *frames) {
+    return guarded(h, [&] { submit(h, frames); });
+}
+
+int cm_synchronize(cm_handle *h) {
+    return guarded(h, [&] { check_device_error(h); });
+}
+
+int cm_read_counts(cm_handle *h, cm_counts *out) {
+    return guarded(h, [&] {
+        if (!out) throw cm_error(CM_EINVAL, "NULL output");
+        check_device_error(h);
+        std::vector<unsigned long long> acc(h->hist_n);
+        std::vector<double> sums(h->hist_n);
+        CM_CUDA(cudaMemcpy(acc.data(), h->hist.p, h->hist_n * 8, cudaMemcpyDeviceToHost));
+        CM_CUDA(cudaMemcpy(sums.data(), h->sums.p, h->hist_n * 8, cudaMemcpyDeviceToHost));
+        std::vector<double> tot(h->hist_n);
+        for (int64_t i = 0; i < h->hist_n; ++i)
+            tot[i] = (h->class_open && acc[i]) ? sums[i] + h->class_w * ((double)acc[i] / 2.0) : sums[i];
+        const int64_t nb = h->d.nbins;
+        auto put = [&](double *dst, int64_t off, int64_t n) {
+            if (dst) memcpy(dst, tot.data() + off, n * 8);
+        };
+        put(out->md_count, h->o_md, nb);
+        put(out->md_count_random, h->o_mdr, nb);
+        put(out->rdf_count, h->o_rdf, nb);
+        put(out->rdf_count_random, h->o_rdfr, nb);
+        put(out->solute_group_count, h->o_gs, h->Gs * nb);
+        put(out->solute_group_count_random, h->o_gsr, h->Gs * nb);
+        if (h->d.autocorrelation) {
+            if (out->solvent_group_count) memset(out->solvent_group_count, 0, h->Gv * nb * 8);
+            if (out->solvent_group_count_random) memset(out->solvent_group_count_random, 0, h->Gv * nb * 8);
+        } else {
+            put(out->solvent_group_count, h->o_gv, h->Gv * nb);
+            put(out->solvent_group_count_random, h->o_gvr, h->Gv * nb);
+        }
+        out->volume_total = h->volume_total;
+        out->weight_total = h->weight_total;
+        out->frames = h->frames;
+    });
+}
+
+int cm_read_raw_counts(cm_handle *h, cm_raw_counts *out) {
+    return guarded(h, [&] {
+        if (!out) throw cm_error(CM_EINVAL, "NULL output");
+        if (h->folds > 0) throw cm_error(CM_ESTATE, "raw counts are defined only while all frames carry one weight");
+        check_device_error(h);
+        std::vector<int64_t> acc(h->hist_n);
+        CM_CUDA(cudaMemcpy(acc.data(), h->hist.p, h->hist_n * 8, cudaMemcpyDeviceToHost));
+        const int64_t nb = h->d.nbins;
+        auto put = [&](int64_t *dst, int64_t off, int64_t n) {
+            if (dst) memcpy(dst, acc.data() + off, n * 8);
+        };
+        put(out->md, h->o_md, nb);
+        put(out->md_random, h->o_mdr, nb);
+        put(out->rdf, h->o_rdf, nb);
+        put(out->rdf_random, h->o_rdfr, nb);
+        put(out->solute_group, h->o_gs, h->Gs * nb);
+        put(out->solute_group_random, h->o_gsr, h->Gs * nb);
+        if (h->d.autocorrelation) {
+            if (out->solvent_group) memset(out->solvent_group, 0, h->Gv * nb * 8);
+            if (out->solvent_group_random) memset(out->solvent_group_random, 0, h->Gv * nb * 8);
+        } else {
+            put(out->solvent_group, h->o_gv, h->Gv * nb);
+            put(out->solvent_group_random, h->o_gvr, h->Gv * nb);
+        }
+    });
+}
+
+int cm_get_stats(cm_handle *h, cm_stats *out) {
+    return guarded(h, [&] {
+        if (!out) throw cm_error(CM_EINVAL, "NULL output");
+        CM_CUDA(cudaStreamSynchronize(h->stream));
+        unsigned long long s[ST_N];
+        CM_CUDA(cudaMemcpy(s, h->stats.p, sizeof(s), cudaMemcpyDeviceToHost));
+        memset(out, 0, sizeof(*out));
+        out->frames = h->frames;
+        out->molecule_pairs_evaluated = (int64_t)s[ST_MOLPAIRS];
+        out->atom_pairs_evaluated = (int64_t)s[ST_ATOMPAIRS];
+        out->hits_real = (int64_t)s[ST_HITS_REAL];
+        out->hits_random = (int64_t)s[ST_HITS_RAND];
+        out->guard_reevaluations = (int64_t)s[ST_GUARD];
+        out->guard_pair_evaluations = (int64_t)s[ST_GUARD_PAIRS];
+        double e;
+        memcpy(&e, &s[ST_MAXERR], 8);
+        out->max_guard_error = e;
+        out->guard_band = h->last_guard;
+        out->regime = h->regime;
+        out->kernels_per_frame = h->kernels_per_frame;
+    });
+}
+
+int cm_reset(cm_handle *h) {
+    return guarded(h, [&] {
+        CM_CUDA(cudaStreamSynchronize(h->stream));
+        CM_CUDA(cudaMemset(h->hist.p, 0, h->hist_n * 8));
+        CM_CUDA(cudaMemset(h->sums.p, 0, h->hist_n * 8));
+        CM_CUDA(cudaMemset(h->stats.p, 0, ST_N * 8));
+        CM_CUDA(cudaMemset(h->errflag.p, 0, 8));
+        h->class_open = false;
+        h->class_w = 1.0;
+        h->folds = 0;
+        h->volume_total = h->weight_total = 0.0;
+        h->frames = 0;
+    });
+}
+
+int cm_destroy(cm_handle *h) {
+    if (!h) return CM_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return CM_OK;
+}
+
+const char *cm_last_error(const cm_handle *h) {
+    if (!h) return g_create_error.c_str();
+    return h->err.c_str();
+}
+
+const char *cm_status_string(int status) {
+    switch (status) {
+        case CM_OK: return "ok";
+        case CM_EINVAL: return "invalid argument";
+        case CM_ENOMEM: return "out of memory or over the device memory budget";
+        case CM_ECUDA: return "CUDA runtime error";
+        case CM_EDEVICE: return "device-side check failed";
+        case CM_ESTATE: return "invalid state";
+        default: return "unknown status";
+    }
+}
+
+int64_t cm_device_bytes(const cm_handle *h) { return h ? h->device_bytes : 0; }
+
+void *cm_stream(cm_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+}  // extern "C"

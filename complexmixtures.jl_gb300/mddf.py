@@ -1,0 +1,174 @@
+"""mddf / coordination_number drivers (src/mddf.jl:186-347, 539-585).
+
+The reference reads frames one at a time and hands each to ``mddf_frame!`` on
+a CPU thread.  Here frames are read in batches and handed to the GPU engine
+(``Engine.submit``); the counts come back once at the end, then the unchanged
+host-side finalisation runs (src/results.jl:311-469).
+"""
+from __future__ import annotations
+
+import os
+from typing import Optional
+
+import numpy as np
+
+from .engine import Engine
+from .options import Options, TrajectoryFileOptions
+from .results import Result, check_frame_weights, finalresults, isautocorrelation, setbin
+from .trajectory import ArrayTrajectory, Trajectory, cell_matrix, make_trajectory, trajectory_metadata
+
+STOP_FILE = "stop_complexmixtures"
+
+
+def engine_for(R: Result, options: Options, irefatom: int, *, coordination_number_only: bool = False,
+               precision: str = "fp32", regime: str = "auto", device: int = 0, max_frames_per_batch: int = 0,
+               hbm_budget_bytes: int = 0) -> Engine:
+    """Engine configured from a Result's selections and the run options."""
+    solute_groups = R.solute.solute_credit_table()
+    solvent_sel = R.solute if R.autocorrelation else R.solvent
+    solvent_groups = solvent_sel.solvent_credit_table()
+    return Engine(
+        solute_nmols=R.solute.nmols,
+        solute_natomspermol=R.solute.natomspermol,
+        solvent_nmols=R.solvent.nmols,
+        solvent_natomspermol=R.solvent.natomspermol,
+        autocorrelation=R.autocorrelation,
+        irefatom=irefatom,
+        cutoff=options.cutoff,
+        binstep=options.binstep,
+        dbulk=options.dbulk,
+        usecutoff=options.usecutoff,
+        nbins=R.nbins,
+        n_random_samples=options.n_random_samples,
+        lcell=options.lcell,
+        coordination_number_only=coordination_number_only,
+        precision=precision,
+        regime=regime,
+        seed=options.seed,
+        solute_groups=solute_groups,
+        solute_ngroups=R.solute.ngroups(),
+        solvent_groups=solvent_groups,
+        solvent_ngroups=solvent_sel.ngroups(),
+        device=device,
+        max_frames_per_batch=max_frames_per_batch,
+        hbm_budget_bytes=hbm_budget_bytes,
+    )
+
+
+def new_result(trajectory: Trajectory, options: Options, tmeta, frame_weights) -> Result:
+    """Result constructor (src/results.jl:124-193)."""
+    fw = check_frame_weights(frame_weights, options, tmeta.lastframe_read)
+    return Result(
+        nbins=setbin(options.cutoff, options.binstep),
+        dbulk=options.dbulk,
+        cutoff=options.cutoff,
+        autocorrelation=isautocorrelation(trajectory.solute.indices, trajectory.solvent.indices),
+        solute=trajectory.solute,
+        solvent=trajectory.solvent,
+        files=[
+            TrajectoryFileOptions(
+                filename=trajectory.filename,
+                options=options,
+                irefatom=tmeta.irefatom,
+                lastframe_read=tmeta.lastframe_read,
+                nframes_read=tmeta.nframes_read,
+                frame_weights=[float(w) for w in fw],
+            )
+        ],
+        weights=[1.0],
+    )
+
+
+def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = None, *, frame_weights=None,
+         coordination_number_only: bool = False, low_memory: bool = False, trajectory_format: str = "",
+         precision: str = "fp32", regime: str = "auto", device: int = 0, batch_frames: int = 64) -> Result:
+    """Minimum-distance distribution function (src/mddf.jl:113-347).
+
+    ``mddf(trajectory, options)`` with a Trajectory object, or
+    ``mddf(filename, solute, solvent, options)`` / ``mddf(filename, solute,
+    options)`` (self-MDDF) with a file name.  ``low_memory`` is accepted for
+    signature compatibility; the GPU engine has a single memory layout.
+    ``precision`` selects the FP32+guard ("fp32") or plain FP64 ("fp64") path;
+    both give identical counts.
+    """
+    if isinstance(trajectory, str):
+        if isinstance(solvent, Options) and options is None:
+            options, solvent = solvent, None
+        trajectory = make_trajectory(trajectory, solute, solvent, format=trajectory_format,
+                                     lastframe=(options.lastframe if options else -1))
+    elif isinstance(solute, Options) and options is None:
+        options = solute
+    options = options or Options()
+    tmeta = trajectory_metadata(trajectory, options)
+    R = new_result(trajectory, options, tmeta, frame_weights)
+    fw = np.asarray(R.files[0].frame_weights)
+    to_compute = [i for i in range(options.firstframe, tmeta.lastframe_read + 1, options.stride) if fw[i - 1] != 0.0]
+    eng = engine_for(R, options, tmeta.irefatom, coordination_number_only=coordination_number_only,
+                     precision=precision, regime=regime, device=device, max_frames_per_batch=batch_frames)
+    try:
+        _run_frames(eng, trajectory, to_compute, fw, batch_frames)
+        c = eng.counts()
+    finally:
+        eng.close()
+    for k in ("md_count", "md_count_random", "rdf_count", "rdf_count_random", "solute_group_count",
+              "solute_group_count_random", "solvent_group_count", "solvent_group_count_random"):
+        setattr(R, k, c[k].copy())
+    R.volume.total = c["volume_total"]
+    return finalresults(R, options, coordination_number_only=coordination_number_only)
+
+
+def _run_frames(eng: Engine, trajectory: Trajectory, to_compute, fw, batch_frames: int) -> None:
+    if not to_compute:
+        return
+    if isinstance(trajectory, ArrayTrajectory):
+        for b0 in range(0, len(to_compute), batch_frames):
+            if os.path.isfile(STOP_FILE):
+                break
+            ids = to_compute[b0 : b0 + batch_frames]
+            xs, xv, cells = trajectory.frame_arrays([i - 1 for i in ids])
+            eng.submit(xs, None if eng.autocorrelation else xv, cells, weights=[fw[i - 1] for i in ids], frame_ids=ids)
+        return
+    wanted = set(to_compute)
+    last = max(to_compute)
+    trajectory.opentraj()
+    trajectory.firstframe()
+    xs, xv, cells, ids = [], [], [], []
+
+    def flush():
+        if ids:
+            eng.submit(np.stack(xs), None if eng.autocorrelation else np.stack(xv), np.stack(cells),
+                       weights=[fw[i - 1] for i in ids], frame_ids=list(ids))
+            xs.clear(); xv.clear(); cells.clear(); ids.clear()
+
+    try:
+        for iframe in range(1, last + 1):
+            if os.path.isfile(STOP_FILE):
+                break
+            trajectory.nextframe()
+            if iframe not in wanted:
+                continue
+            xs.append(np.array(trajectory.x_solute, dtype=np.float64))
+            xv.append(np.array(trajectory.x_solvent, dtype=np.float64))
+            cells.append(cell_matrix(trajectory.getunitcell()))
+            ids.append(iframe)
+            if len(ids) >= batch_frames:
+                flush()
+        flush()
+    finally:
+        trajectory.closetraj()
+
+
+def coordination_number(*args, **kw):
+    """Coordination numbers (src/mddf.jl:539-585) when called with a trajectory;
+    with a Result, the group coordination number of
+    src/tools/coordination_number.jl:104-106."""
+    from .contributions import coordination_number as cn_result
+
+    if args and isinstance(args[0], Result):
+        return cn_result(*args, **kw)
+    if "coordination_number_only" in kw:
+        raise ValueError(
+            "The keyword argument `coordination_number_only` is not allowed in the `coordination_number` function. "
+            "It is, by definition, set to `true` in this function."
+        )
+    return mddf(*args, coordination_number_only=True, **kw)

@@ -1,0 +1,213 @@
+/*
+ * cmgpu.h -- C ABI of the GB300 MDDF engine (libcmgpu.so).
+ *
+ * The engine computes, on one GPU, the per-frame hot path of ComplexMixtures.jl:
+ * minimum distances between solute and solvent molecules under periodic
+ * boundary conditions (orthorhombic and triclinic cells), the MDDF / RDF /
+ * group-contribution histograms, and the random-insertion ideal-gas reference
+ * counts.  Everything before the path (trajectory reading, selections, options)
+ * and after it (normalisation, contributions) stays in the host language.
+ *
+ * Reference interfaces replaced (paths relative to ComplexMixtures.jl):
+ *   mddf_frame!(r_chunk, system, buff, options, frame_weight, RNG)  src/mddf.jl:361-429
+ *   coordination_number_frame!(r_chunk, system, buff, frame_weight) src/mddf.jl:438-471
+ *   the per-chunk frame loop and sum!(R, r_chunk)                     src/mddf.jl:287-338,
+ *                                                                     src/results.jl:629-649
+ *   build_particle_system(trajectory, unitcell, options, ...)         src/minimum_distances.jl:157-176
+ *
+ * Conventions
+ *   - Coordinates are xyz triplets in selection order (the order of
+ *     AtomSelection.indices); molecules are contiguous blocks of
+ *     natomspermol atoms (src/viewmol.jl:8-23).
+ *   - A unit cell is 9 doubles, column-major: cell[0..2] is the first lattice
+ *     vector, cell[3..5] the second, cell[6..8] the third (the columns of the
+ *     reference's unit-cell matrix, src/mddf.jl:350-351).  An orthorhombic box
+ *     is the diagonal matrix.
+ *   - All entry points return a cm_status; nothing aborts or throws across
+ *     the ABI.  cm_last_error() gives the message of the last failure.
+ *   - A handle is used by one host thread at a time.  Different handles may
+ *     run concurrently; each owns a CUDA stream on its device.
+ *   - Host arrays passed in are read during the call only.
+ */
+#ifndef CMGPU_H
+#define CMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CM_API_VERSION 1
+
+typedef enum cm_status {
+    CM_OK = 0,
+    CM_EINVAL = 1,    /* invalid argument (ArgumentError in the reference) */
+    CM_ENOMEM = 2,    /* device or host allocation failed, or over the HBM budget */
+    CM_ECUDA = 3,     /* a CUDA runtime call failed */
+    CM_EDEVICE = 4,   /* a device-side consistency check failed (error flag set by a kernel) */
+    CM_ESTATE = 5     /* call not valid in the handle's current state */
+} cm_status;
+
+enum { CM_MODE_MDDF = 0, CM_MODE_COORDINATION_NUMBER = 1 };
+enum { CM_PRECISION_FP64 = 0, CM_PRECISION_FP32_GUARD = 1 };
+enum { CM_REGIME_AUTO = 0, CM_REGIME_PAIRS = 1, CM_REGIME_ATOMS = 2 };
+enum { CM_COORD_F64 = 0, CM_COORD_F32 = 1 };
+enum { CM_MEM_HOST = 0, CM_MEM_DEVICE = 1 };
+
+/*
+ * System description.  Field meanings follow Options (src/Options.jl:6-42),
+ * AtomSelection (src/AtomSelection.jl:48-59) and Result (src/results.jl:61-118).
+ *
+ * Groups.  Histogram credits follow update_group_count! (src/update_counters.jl:22-36):
+ *   - the solute-side atom of a minimum-distance pair is identified by its index
+ *     *within its molecule* (0..solute_natomspermol-1), so solute credits are a
+ *     CSR over those local indices: solute_group_offsets[natomspermol+1],
+ *     solute_groups[...] (group numbers, 0-based);
+ *   - the solvent-side atom is identified by its index in the whole selection
+ *     (0..solvent_nmols*solvent_natomspermol-1): solvent_group_offsets[N+1],
+ *     solvent_groups[...].
+ *   For default groups (custom_groups == false) pass NULL CSRs: the group of an
+ *   atom is then its atom type (src/update_counters.jl:9) and the group count
+ *   equals natomspermol.  In self mode (autocorrelation) both credits go to the
+ *   solute table (src/update_counters.jl:272-277) and the solvent CSR must
+ *   describe the same selection.
+ */
+typedef struct cm_system_desc {
+    int32_t api_version;              /* CM_API_VERSION */
+    int32_t solute_nmols;
+    int32_t solute_natomspermol;
+    int32_t solvent_nmols;
+    int32_t solvent_natomspermol;
+    int32_t autocorrelation;          /* 1: solute and solvent are the same selection */
+    int32_t irefatom;                 /* 1-based reference atom of the solvent molecule */
+    double cutoff;
+    double binstep;
+    double dbulk;
+    int32_t usecutoff;
+    int32_t nbins;                    /* setbin(cutoff, binstep) */
+    int32_t n_random_samples;
+    int32_t lcell;                    /* cell side = cutoff / lcell for atom cell lists */
+    int32_t mode;                     /* CM_MODE_* */
+    int32_t precision;                /* CM_PRECISION_* */
+    int32_t regime;                   /* CM_REGIME_*: search layout, AUTO picks by molecule size */
+    uint64_t seed;                    /* seed of the random-insertion stream */
+    int32_t solute_ngroups;           /* 0 with NULL CSR = default groups */
+    const int64_t *solute_group_offsets;
+    const int32_t *solute_groups;
+    int32_t solvent_ngroups;
+    const int64_t *solvent_group_offsets;
+    const int32_t *solvent_groups;
+    int32_t device;                   /* CUDA device ordinal */
+    int32_t max_frames_per_batch;     /* frames staged on the device per submit chunk; 0 = 64 */
+    int64_t hbm_budget_bytes;         /* 0 = no limit; cm_create fails with CM_ENOMEM above it */
+} cm_system_desc;
+
+/*
+ * A batch of frames.  Counts of all frames are added to the handle's
+ * accumulators, as sum!(R, r_chunk) does (src/results.jl:629-649).
+ */
+typedef struct cm_frames {
+    int32_t nframes;
+    int32_t coord_type;               /* CM_COORD_F64 or CM_COORD_F32 */
+    int32_t memory;                   /* where solute_xyz / solvent_xyz live: CM_MEM_HOST / CM_MEM_DEVICE */
+    int32_t reserved;
+    const void *solute_xyz;           /* [nframes][solute atoms][3] */
+    const void *solvent_xyz;          /* [nframes][solvent atoms][3]; NULL in self mode */
+    const double *cells;              /* host [nframes][9] */
+    const double *weights;            /* host [nframes]; NULL = all 1.0 (frame_weights) */
+    const int64_t *frame_ids;         /* host [nframes]; 1-based trajectory frame numbers,
+                                         they key the random-insertion stream */
+} cm_frames;
+
+/*
+ * Accumulated counts in the units of the reference's Result fields before
+ * finalresults! (src/results.jl:311-376): frame-weighted sums.  All arrays are
+ * caller-owned host buffers; NULL pointers are skipped.
+ */
+typedef struct cm_counts {
+    double *md_count;                     /* [nbins] */
+    double *md_count_random;              /* [nbins] */
+    double *rdf_count;                    /* [nbins] */
+    double *rdf_count_random;             /* [nbins] */
+    double *solute_group_count;           /* [solute_ngroups][nbins] */
+    double *solute_group_count_random;    /* [solute_ngroups][nbins] */
+    double *solvent_group_count;          /* [solvent_ngroups][nbins]; zero in self mode */
+    double *solvent_group_count_random;   /* [solvent_ngroups][nbins]; zero in self mode */
+    double volume_total;                  /* sum of w * det(cell) (src/mddf.jl:350-352) */
+    double weight_total;                  /* sum of w over computed frames */
+    int64_t frames;                       /* frames computed */
+} cm_counts;
+
+/*
+ * Exact integer counts in half units (2 per unit of frame weight), valid while
+ * every frame submitted since the last reset carried the same weight.
+ * Array layout as in cm_counts.
+ */
+typedef struct cm_raw_counts {
+    int64_t *md, *md_random, *rdf, *rdf_random;
+    int64_t *solute_group, *solute_group_random;
+    int64_t *solvent_group, *solvent_group_random;
+} cm_raw_counts;
+
+typedef struct cm_stats {
+    int64_t frames;
+    int64_t molecule_pairs_evaluated;     /* candidate molecule pairs whose atom pairs were evaluated */
+    int64_t atom_pairs_evaluated;         /* atom-pair distance evaluations (FP32 or FP64) */
+    int64_t hits_real;                    /* minimum-distance records within cutoff, real pass */
+    int64_t hits_random;                  /* same, random-insertion passes */
+    int64_t guard_reevaluations;          /* records re-evaluated in FP64 inside the guard band */
+    int64_t guard_pair_evaluations;       /* FP64 atom-pair evaluations done by those re-evaluations */
+    double max_guard_error;               /* max |d_fp32 - d_fp64| seen in re-evaluated pairs (Angstrom) */
+    double guard_band;                    /* guard half-width used in the last frame (Angstrom) */
+    int32_t regime;                       /* CM_REGIME_PAIRS or CM_REGIME_ATOMS actually used */
+    int32_t kernels_per_frame;            /* kernel launches per frame */
+} cm_stats;
+
+typedef struct cm_handle cm_handle;
+
+/* Validate the description, allocate device state.  *out is set on success. */
+int cm_create(const cm_system_desc *desc, cm_handle **out);
+
+/* Enqueue a batch of frames (asynchronous on the handle's stream for device
+ * memory; host memory is staged through pinned buffers before return). */
+int cm_submit_frames(cm_handle *h, const cm_frames *frames);
+
+/* Wait for all submitted work; returns CM_EDEVICE if a kernel raised its error flag. */
+int cm_synchronize(cm_handle *h);
+
+/* Synchronise and copy the weighted accumulators out. */
+int cm_read_counts(cm_handle *h, cm_counts *out);
+
+/* Synchronise and copy the exact half-unit counts (single-weight runs only). */
+int cm_read_raw_counts(cm_handle *h, cm_raw_counts *out);
+
+/* Engine statistics (synchronises). */
+int cm_get_stats(cm_handle *h, cm_stats *out);
+
+/* Zero the accumulators and statistics; keeps device allocations. */
+int cm_reset(cm_handle *h);
+
+/* Release everything owned by the handle.  NULL is accepted. */
+int cm_destroy(cm_handle *h);
+
+/* Message of the last failure on this handle (or of the last cm_create failure
+ * on this thread when h is NULL).  Never NULL. */
+const char *cm_last_error(const cm_handle *h);
+
+/* Static description of a status code. */
+const char *cm_status_string(int status);
+
+/* Device memory the handle holds, in bytes. */
+int64_t cm_device_bytes(const cm_handle *h);
+
+/* The CUDA stream of the handle (as cudaStream_t), for callers that order
+ * their own device work against the engine. */
+void *cm_stream(cm_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CMGPU_H */

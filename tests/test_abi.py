@@ -1,0 +1,74 @@
+"""The C-ABI library: loads without a GPU, exports every symbol declared in
+include/cmgpu.h, and its struct layouts match the ctypes mirror."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "cmgpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(cm_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_header_symbols(cm):
+    entry = __import__("__graft_entry__")
+    path = entry.load_build().build()
+    lib = C.CDLL(path)
+    names = header_functions()
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(cm._native.EXPORTED)
+
+
+def test_struct_sizes_match_header(cm):
+    N = cm._native
+    # field-by-field mirror of include/cmgpu.h on LP64
+    assert C.sizeof(N.cm_system_desc) == 160
+    assert C.sizeof(N.cm_frames) == 56
+    assert C.sizeof(N.cm_counts) == 88
+    assert C.sizeof(N.cm_raw_counts) == 64
+    assert C.sizeof(N.cm_stats) == 80
+
+
+def test_create_rejects_bad_descriptions_without_gpu(cm):
+    """Argument checks run before any CUDA call, so they work without a GPU."""
+    N = cm._native
+    lib = N.load()
+    d = N.cm_system_desc()
+    d.api_version = N.CM_API_VERSION
+    d.solute_nmols = d.solvent_nmols = 10
+    d.solute_natomspermol = d.solvent_natomspermol = 3
+    d.irefatom = 5  # > natomspermol
+    d.cutoff = d.dbulk = 10.0
+    d.binstep = 0.02
+    d.nbins = 500
+    d.n_random_samples = 10
+    d.lcell = 1
+    h = C.c_void_p()
+    assert lib.cm_create(C.byref(d), C.byref(h)) == N.CM_EINVAL
+    assert b"Reference atom index" in lib.cm_last_error(None)
+    d.irefatom = 1
+    d.usecutoff = 1
+    assert lib.cm_create(C.byref(d), C.byref(h)) == N.CM_EINVAL
+    assert b"bulk volume is zero" in lib.cm_last_error(None)
+    d.usecutoff = 0
+    d.nbins = 10
+    assert lib.cm_create(C.byref(d), C.byref(h)) == N.CM_EINVAL
+    assert lib.cm_destroy(None) == N.CM_OK
+    assert lib.cm_status_string(N.CM_EDEVICE) == b"device-side check failed"
+
+
+def test_engine_fails_loudly_without_library(cm, tmp_path):
+    N = cm._native
+    with pytest.raises(N.NativeUnavailable):
+        saved = N._lib
+        N._lib = None
+        try:
+            N.load(str(tmp_path / "missing.so"))
+        finally:
+            N._lib = saved

@@ -1,0 +1,245 @@
+"""GPU engine (through the C ABI) against the CPU oracle, bit for bit.
+
+Counts are int64 half units and must be identical.  Inputs are seeded random
+molecular systems small enough for the oracle, covering orthorhombic and
+triclinic cells, cross and self MDDFs, both search layouts, FP32+guard and
+FP64, default and custom (overlapping) groups, and both bulk definitions.
+"""
+import numpy as np
+import pytest
+
+from helpers import golden, oracle_mddf
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("md", "md_random", "rdf", "rdf_random", "solute_group", "solute_group_random", "solvent_group",
+        "solvent_group_random")
+
+TRICLINIC = np.array([[24.0, 12.0, 0.0], [0.0, 20.78460969082653, 0.0], [0.0, 0.0, 23.0]])
+ORTHO = np.diag([23.0, 25.0, 24.0])
+
+
+def make_system(rng, H, ms, aps, mv, apv, nframes, self_mode, spread=0.9):
+    def mols(n, apm):
+        c = rng.random((n, 1, 3)) @ H.T
+        return (c + rng.normal(scale=spread, size=(n, apm, 3))).reshape(-1, 3)
+
+    xs0 = mols(ms, aps)
+    xv0 = None if self_mode else mols(mv, apv)
+    xs = np.stack([xs0 + rng.normal(scale=0.15, size=xs0.shape) for _ in range(nframes)])
+    xv = None if self_mode else np.stack([xv0 + rng.normal(scale=0.15, size=xv0.shape) for _ in range(nframes)])
+    cells = np.repeat(H[None], nframes, axis=0)
+    return xs, xv, cells
+
+
+def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, regime, frame_ids=None, groups=None,
+            backend="cells", dtype=np.float64, **opt):
+    nf = xs.shape[0]
+    frame_ids = list(range(1, nf + 1)) if frame_ids is None else frame_ids
+    kw = dict(autocorrelation=self_mode, **opt)
+    g = {}
+    if groups == "custom":
+        # overlapping custom groups: atom j in groups j % 3 and 3 (+ a group of
+        # the first half of the atoms); solute side by local index
+        gs = [[a % 3, 3] + ([4] if a < aps // 2 else []) for a in range(aps)]
+        gv_rows = (lambda n, apm: [[j % 3, 3] + ([4] if (j % apm) < apm // 2 else []) for j in range(n)])
+        gv = gv_rows(mv * apv, apv)
+        g = dict(solute_groups=gs, solute_ngroups=5, solvent_groups=gv, solvent_ngroups=5)
+    eng = cm.Engine(solute_nmols=ms, solute_natomspermol=aps, solvent_nmols=mv, solvent_natomspermol=apv,
+                    precision=precision, regime=regime, max_frames_per_batch=2, **kw, **g)
+    eng.submit(xs.astype(dtype), None if self_mode else xv.astype(dtype), cells, frame_ids=frame_ids)
+    got = eng.raw_counts()
+    st = eng.stats()
+    eng.close()
+    ref = orc.run(ms=ms, aps=aps, mv=mv, apv=apv, solute_xyz=xs.astype(dtype).astype(np.float64),
+                  solvent_xyz=None if self_mode else xv.astype(dtype).astype(np.float64), cells=cells,
+                  frame_ids=frame_ids, backend=backend, **kw, **g)
+    for k in KEYS:
+        if self_mode and k.startswith("solvent"):
+            continue
+        assert np.array_equal(got[k], ref[k]), (k, np.nonzero(got[k] != ref[k]))
+    return got, ref, st
+
+
+COMMON = dict(binstep=0.02, nbins=350, seed=77)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("H", [ORTHO, TRICLINIC], ids=["ortho", "triclinic"])
+@pytest.mark.parametrize("usecutoff", [False, True])
+def test_pairs_self(cm, orc, gpu_ready, precision, H, usecutoff):
+    rng = np.random.default_rng(1)
+    xs, xv, cells = make_system(rng, H, 60, 5, 60, 5, 3, True)
+    opt = dict(irefatom=2, cutoff=7.0, dbulk=5.0 if usecutoff else 7.0, usecutoff=usecutoff, n_random_samples=6,
+               **COMMON)
+    got, ref, st = compare(cm, orc, ms=60, aps=5, mv=60, apv=5, xs=xs, xv=None, cells=cells, self_mode=True,
+                           precision=precision, regime="pairs", **opt)
+    assert ref["md"].sum() > 0 and ref["md_random"].sum() > 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("H", [ORTHO, TRICLINIC], ids=["ortho", "triclinic"])
+@pytest.mark.parametrize("groups", ["default", "custom"])
+def test_pairs_cross(cm, orc, gpu_ready, precision, H, groups):
+    rng = np.random.default_rng(2)
+    xs, xv, cells = make_system(rng, H, 20, 7, 150, 3, 3, False)
+    opt = dict(irefatom=1, cutoff=6.0, dbulk=6.0, usecutoff=False, n_random_samples=8, **COMMON)
+    compare(cm, orc, ms=20, aps=7, mv=150, apv=3, xs=xs, xv=xv, cells=cells, self_mode=False, precision=precision,
+            regime="pairs", groups=groups, **opt)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("H", [ORTHO, TRICLINIC], ids=["ortho", "triclinic"])
+@pytest.mark.parametrize("groups", ["default", "custom"])
+def test_atoms_cross(cm, orc, gpu_ready, precision, H, groups):
+    """A 300-atom solute molecule (ATOMS layout) in water-like solvent."""
+    rng = np.random.default_rng(3)
+    steps = rng.normal(size=(300, 3))
+    chain = np.cumsum(steps / np.linalg.norm(steps, axis=1, keepdims=True) * 1.53, axis=0) + H @ np.full(3, 0.5)
+    xs = np.stack([chain + rng.normal(scale=0.2, size=chain.shape) for _ in range(2)])
+    _, xv, cells = make_system(rng, H, 1, 1, 300, 3, 2, False)
+    opt = dict(irefatom=1, cutoff=6.0, dbulk=4.0, usecutoff=True, n_random_samples=5, **COMMON)
+    compare(cm, orc, ms=1, aps=300, mv=300, apv=3, xs=xs, xv=xv, cells=cells, self_mode=False, precision=precision,
+            regime="atoms", groups=groups, **opt)
+
+
+@pytest.mark.parametrize("regime", ["pairs", "atoms"])
+def test_regimes_agree_self(cm, orc, gpu_ready, regime):
+    """Self-MDDF through both layouts (the ATOMS layout handles it directionally)."""
+    rng = np.random.default_rng(4)
+    xs, _, cells = make_system(rng, TRICLINIC, 40, 6, 40, 6, 2, True)
+    opt = dict(irefatom=3, cutoff=6.5, dbulk=6.5, usecutoff=False, n_random_samples=4, **COMMON)
+    compare(cm, orc, ms=40, aps=6, mv=40, apv=6, xs=xs, xv=None, cells=cells, self_mode=True, precision="fp32",
+            regime=regime, groups="custom", **opt)
+
+
+def test_small_box_multi_image(cm, orc, gpu_ready):
+    """Box narrower than twice the search range: several images per pair."""
+    rng = np.random.default_rng(5)
+    H = np.diag([13.0, 12.0, 14.0])
+    xs, _, cells = make_system(rng, H, 12, 4, 12, 4, 2, True, spread=0.7)
+    opt = dict(irefatom=1, cutoff=5.6, dbulk=5.6, usecutoff=False, n_random_samples=3, **COMMON)
+    for regime in ("pairs", "atoms"):
+        compare(cm, orc, ms=12, aps=4, mv=12, apv=4, xs=xs, xv=None, cells=cells, self_mode=True, precision="fp32",
+                regime=regime, backend="brute", **opt)
+
+
+def test_coordination_number_mode(cm, orc, gpu_ready):
+    rng = np.random.default_rng(6)
+    xs, xv, cells = make_system(rng, ORTHO, 10, 5, 120, 3, 2, False)
+    opt = dict(irefatom=1, cutoff=6.0, dbulk=6.0, usecutoff=False, n_random_samples=3, coordination_number_only=True,
+               **COMMON)
+    got, ref, st = compare(cm, orc, ms=10, aps=5, mv=120, apv=3, xs=xs, xv=xv, cells=cells, self_mode=False,
+                           precision="fp32", regime="pairs", **opt)
+    assert got["md_random"].sum() == 0 and ref["md"].sum() > 0
+
+
+def test_fp32_coordinates(cm, orc, gpu_ready):
+    """FP32-stored coordinates (the engine promotes them to FP64 exactly)."""
+    rng = np.random.default_rng(7)
+    xs, _, cells = make_system(rng, TRICLINIC * 2.0, 300, 14, 300, 14, 2, True, spread=1.5)
+    opt = dict(irefatom=1, cutoff=8.0, dbulk=8.0, usecutoff=False, n_random_samples=5, **COMMON)
+    compare(cm, orc, ms=300, aps=14, mv=300, apv=14, xs=xs, xv=None, cells=cells, self_mode=True, precision="fp32",
+            regime="pairs", dtype=np.float32, **{**opt, "nbins": 400})
+
+
+def test_fp32_equals_fp64_larger(cm, gpu_ready):
+    """c3-like self system (2,000 molecules of 14 atoms, triclinic): the FP32 +
+    guard path gives exactly the FP64 path's counts."""
+    syn = cm_synth()
+    s = syn.config3(nmols=2000, edge=64.4, nframes=3)
+    xs, _, cells = s.frames()
+    out = {}
+    for prec in ("fp32", "fp64"):
+        eng = __import__("complexmixtures_gb300").Engine(
+            solute_nmols=2000, solute_natomspermol=14, solvent_nmols=2000, solvent_natomspermol=14,
+            autocorrelation=True, irefatom=1, cutoff=10.0, binstep=0.02, dbulk=10.0, usecutoff=False, nbins=500,
+            n_random_samples=5, seed=5, precision=prec)
+        eng.submit(xs, None, cells)
+        out[prec] = eng.raw_counts()
+        st = eng.stats()
+        eng.close()
+    for k in KEYS[:6]:
+        assert np.array_equal(out["fp32"][k], out["fp64"][k]), k
+    assert out["fp32"]["md"].sum() > 0
+
+
+def cm_synth():
+    import importlib
+
+    return importlib.import_module("complexmixtures_gb300.synth")
+
+
+# ---------------------------------------------------------------- golden
+def test_gpu_toy_cross(cm, gpu_ready):
+    t = golden("toy.npz")
+    protein = cm.AtomSelection.from_indices([10], nmols=1)
+    water = cm.AtomSelection.from_indices(list(range(1, 10)), natomspermol=3)
+    cells = np.array([np.diag(c) for c in t["cross_cell"]])
+    for lastframe in (1, 2):
+        tr = cm.ArrayTrajectory(protein, water, frames=t["cross_xyz"], cells=cells)
+        opts = cm.make_options(seed=321, StableRNG=True, silent=True, n_random_samples=10**5, lastframe=lastframe)
+        R = cm.mddf(tr, opts)
+        assert R.volume.total == 27000.0
+        assert np.isclose(R.volume.domain, (4 * np.pi / 3) * R.dbulk**3, rtol=0.01)
+        assert np.isclose(R.density.solvent_bulk, 2 / R.volume.bulk)
+        assert np.isclose(R.md_count.sum(), 1)
+        assert np.isclose(R.coordination_number.sum(), 51)
+        C = cm.coordination_number(cm.ArrayTrajectory(protein, water, frames=t["cross_xyz"], cells=cells), opts)
+        assert np.array_equal(C.md_count, R.md_count)
+        assert C.density.solvent_bulk == 0.0
+
+
+def test_gpu_toy_self_and_weights(cm, orc, gpu_ready):
+    t = golden("toy.npz")
+    atom = cm.AtomSelection.from_indices([1, 2], natomspermol=1)
+    tr = lambda n="self_monoatomic": cm.ArrayTrajectory(atom, frames=t[n + "_xyz"],
+                                                        cells=np.array([np.diag(c) for c in t[n + "_cell"]]))
+    o = cm.make_options(seed=321, StableRNG=True, silent=True)
+    R = cm.mddf(tr(), cm.make_options(seed=321, silent=True, n_random_samples=10**5, lastframe=1))
+    assert np.isclose(R.md_count.sum(), 1.0)
+    assert np.isclose(R.volume.domain, (4 * np.pi / 3) * R.dbulk**3, rtol=0.1)
+    R1 = cm.mddf(tr(), o)
+    R2 = cm.mddf(tr(), o, frame_weights=[0.3, 0.3])
+    assert np.array_equal(R1.md_count, R2.md_count) and np.array_equal(R1.rdf_count, R2.rdf_count)
+    R1 = cm.mddf(tr("self_monoatomic_duplicated_first_frame"), cm.make_options(silent=True, lastframe=3))
+    R2 = cm.mddf(tr(), o, frame_weights=[2.0, 1.0])
+    assert np.array_equal(R1.md_count, R2.md_count)
+    assert np.isclose(R2.md_count.sum(), 2 / 3)
+    # finalised fields equal the oracle's through the same host code
+    Ro = oracle_mddf(cm, orc, tr(), o, frame_weights=[2.0, 1.0])
+    for f in ("md_count", "md_count_random", "rdf_count", "rdf_count_random", "mddf", "kb", "rdf", "kb_rdf"):
+        assert np.array_equal(getattr(R2, f), getattr(Ro, f)), f
+
+
+def test_gpu_namd_coordination_number(cm, gpu_ready):
+    g = golden("namd_frames.npz")
+    protein = cm.AtomSelection.from_indices(list(range(1, 1464)), nmols=1)
+    tmao = cm.AtomSelection.from_indices(list(range(1479, 4013)), natomspermol=14,
+                                         group_names=[str(s) for s in g["tmao_names"]])
+    cells = np.array([np.diag([c[0], c[2], c[5]]) for c in g["cells"]])
+    for precision in ("fp32", "fp64"):
+        tr = cm.ArrayTrajectory(protein, tmao, solute_frames=g["protein"].astype(np.float64),
+                                solvent_frames=g["tmao"].astype(np.float64), cells=cells)
+        opts = cm.make_options(lastframe=1, seed=321, StableRNG=True, silent=True, n_random_samples=200)
+        R = cm.mddf(tr, opts, precision=precision)
+        assert np.isclose(R.solute_group_count.sum(), R.solvent_group_count.sum())
+        assert R.coordination_number[np.argmax(R.d > 3)] == 7.0
+        assert R.coordination_number[np.argmax(R.d > 5)] == 14.0
+        assert cm.coordination_number(R, cm.SolventGroup(["O1"])).sum() == 1171.0
+
+
+def test_gpu_namd_frames_vs_oracle(cm, orc, gpu_ready):
+    """Real geometry: protein-TMAO (ATOMS layout) and TMAO-water (PAIRS) on two
+    NAMD frames, MDDF with random insertion, bit for bit."""
+    g = golden("namd_frames.npz")
+    cells = np.array([np.diag([c[0], c[2], c[5]]) for c in g["cells"]])
+    prot = g["protein"].astype(np.float64)
+    tmao = g["tmao"].astype(np.float64)
+    opt = dict(irefatom=1, cutoff=10.0, binstep=0.02, dbulk=8.0, usecutoff=True, nbins=500, n_random_samples=4,
+               seed=321)
+    compare(cm, orc, ms=1, aps=1463, mv=181, apv=14, xs=prot, xv=tmao, cells=cells, self_mode=False,
+            precision="fp32", regime="atoms", **opt)
+    water = np.repeat(g["water"].astype(np.float64)[None], 2, axis=0)
+    compare(cm, orc, ms=181, aps=14, mv=2000, apv=3, xs=tmao, xv=water, cells=cells, self_mode=False,
+            precision="fp32", regime="pairs", **opt)
