@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""MDDF throughput on the config-3 workload (self-MDDF in a triclinic cell).
+
+Workload: 10,000 rigid 14-atom molecules (140,000 atoms) in a triclinic cell
+a = b = c = 110 A, gamma = 60 degrees, 500 frames of sigma = 0.4 A jitter stored
+as FP32, cutoff 10 A, binstep 0.02 A, 5 random-insertion samples per frame,
+per-atom groups; seeded synthetic data (no dataset).  One step = all 500
+frames through the engine.
+
+  value   frames/s with the frames resident in HBM (FP32 search + FP64 guard)
+  e2e     the same through the C ABI from pinned host memory, host-to-device
+          copies and the read-out of the counts inside the timed region
+  plain_fp64  the plain FP64 engine path on the same frames
+  roofline    the real-pass kernel (FP32-issue bound; algorithmic flops =
+              8 per atom pair within the cutoff) against the FP32 throughput
+              measured on this GPU, plus its HBM figure
+  cpu_baseline  the CPU restatement of the reference's per-frame path (oracle,
+              all host threads) on a bounded sample of the frames
+
+--impl reference times that CPU path alone (the reference itself is Julia
+and cannot run here).  Multi-GPU runs are independent replicas (the path
+shards by frames with no exchange), launched one rank per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NFRAMES = 500
+NMOLS = 10000
+APM = 14
+CUTOFF = 10.0
+BINSTEP = 0.02
+NRAND = 5
+SEED = 20261203 + 3
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--frames", type=int, default=NFRAMES)
+    p.add_argument("--cpu-frames", type=int, default=0, help="CPU-baseline sample size (0: one frame per host thread)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group(backend="gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(nframes):
+    import __graft_entry__ as entry
+
+    entry.load_package()
+    syn = __import__("importlib").import_module(entry.PKG_NAME + ".synth")
+    s = syn.config3(seed=SEED, nmols=NMOLS, nframes=nframes)
+    xs, _, cells = s.frames(nframes)
+    return xs.astype(np.float32), cells
+
+
+def config_dict(nframes, extra=None):
+    d = {
+        "workload": "c3: self-MDDF, 10,000 rigid 14-atom molecules (140,000 atoms), triclinic a=b=c=110 A "
+                    "gamma=60, FP32 frames, cutoff 10 A, binstep 0.02, 5 random samples/frame, per-atom groups",
+        "frames_per_step": nframes,
+        "atoms": NMOLS * APM,
+        "cutoff": CUTOFF,
+        "n_random_samples": NRAND,
+        "precision": "fp32 search, fp64 guard band",
+        "l2": "inputs are %.0f MB per step (L2 is 129 MB)" % (nframes * NMOLS * APM * 12 / 1e6),
+        "seed": SEED,
+    }
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        load = [v for v in sm if mx and v > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(xs, cells, nframes_sample):
+    """The oracle (CPU restatement of the reference's path), all host threads."""
+    import __graft_entry__ as entry
+
+    orc = entry.load_oracle()
+    threads = os.cpu_count() or 1
+    n = nframes_sample or max(4, min(threads, 16))
+    n = min(n, xs.shape[0])
+    t = time.perf_counter()
+    out = orc.run(ms=NMOLS, aps=APM, mv=NMOLS, apv=APM, autocorrelation=True, irefatom=1, cutoff=CUTOFF,
+                  binstep=BINSTEP, dbulk=CUTOFF, usecutoff=False, nbins=500, n_random_samples=NRAND, seed=SEED,
+                  solute_xyz=xs[:n].astype(np.float64), solvent_xyz=None, cells=cells[:n],
+                  frame_ids=np.arange(1, n + 1), nthreads=threads)
+    dt = time.perf_counter() - t
+    out["nframes"] = n
+    return {"value": n / dt, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} of {xs.shape[0]} frames, one frame per thread (oracle/cm_oracle.c, cells backend)",
+            "seconds": dt}, out
+
+
+def run_reference(args, world, rank):
+    """The reference arm: the CPU path of the reference (its restatement,
+    kind "port"), timed on this machine's host cores."""
+    if rank != 0:
+        return
+    xs, cells = workload(max(16, args.cpu_frames or 16))
+    threads = os.cpu_count() or 1
+    n = args.cpu_frames or max(4, min(threads, 16))
+    times = []
+    for i in range(args.warmup + args.steps):
+        cb, _ = cpu_baseline(xs, cells, n)
+        if i >= args.warmup:
+            times.append(cb["seconds"])
+    T = sum(times)
+    v = args.steps * n / T
+    line = {
+        "impl": "reference", "metric": "MDDF frames/s", "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config-3 shapes)",
+        "config": config_dict(n, {"step": f"{n} frames (bounded sample of the 500-frame workload)"}),
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} frames per step, one per thread"},
+        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Julia (not installed); its per-frame path is timed through the C restatement",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import torch
+
+    import __graft_entry__ as entry
+
+    cm = entry.load_package()
+    torch.cuda.set_device(local)
+    nf = args.frames
+    xs, cells = workload(nf)
+    ids = np.arange(1, nf + 1)
+    xs_dev = torch.from_numpy(xs).to(f"cuda:{local}")
+    xs_pin = torch.from_numpy(xs).pin_memory()
+
+    def engine(precision, timing, chunk=nf):
+        return cm.Engine(solute_nmols=NMOLS, solute_natomspermol=APM, solvent_nmols=NMOLS, solvent_natomspermol=APM,
+                         autocorrelation=True, irefatom=1, cutoff=CUTOFF, binstep=BINSTEP, dbulk=CUTOFF,
+                         usecutoff=False, nbins=500, n_random_samples=NRAND, seed=SEED, precision=precision,
+                         device=local, max_frames_per_batch=chunk, kernel_timing=timing)
+
+    eng = engine("fp32", True)
+    stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=f"cuda:{local}")
+    for _ in range(max(args.warmup, 3)):
+        eng.submit(xs_dev, None, cells, frame_ids=ids)
+    eng.synchronize()
+    eng.reset()
+    st0 = eng.stats()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        eng.submit(xs_dev, None, cells, frame_ids=ids)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ms = allmax(world, ms)
+    st = eng.stats()
+    kt = eng.kernel_times()
+    raw = eng.raw_counts()
+    eng.close()
+    value = world * args.steps * nf / (ms / 1e3)
+
+    # end to end through the C ABI from pinned host memory, counts read back
+    # host frames are staged in chunks of 50 so copies overlap compute
+    eng2 = engine("fp32", False, chunk=min(50, nf))
+    eng2.submit(xs_pin, None, cells, frame_ids=ids)
+    eng2.counts()
+    barrier(world)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        eng2.submit(xs_pin, None, cells, frame_ids=ids)
+        counts = eng2.counts()
+    e2e_s = allmax(world, time.perf_counter() - t)
+    d2h = sum(v.nbytes for v in counts.values() if isinstance(v, np.ndarray))
+    eng2.close()
+    e2e = {"value": world * args.steps * nf / e2e_s, "unit": "frames/s",
+           "h2d_bytes_per_step": int(xs.nbytes + cells.nbytes + 8 * nf * 2), "d2h_bytes_per_step": int(d2h),
+           "api": "Engine.submit (cm_submit_frames, host memory) + Engine.counts (cm_read_counts)"}
+
+    # plain FP64 path
+    plain = None
+    if not args.no_fp64:
+        eng3 = engine("fp64", True)
+        eng3.submit(xs_dev, None, cells, frame_ids=ids)
+        eng3.synchronize()
+        eng3.reset()
+        s3 = torch.cuda.ExternalStream(eng3.stream_ptr(), device=f"cuda:{local}")
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s3)
+        eng3.submit(xs_dev, None, cells, frame_ids=ids)
+        b.record(s3)
+        b.synchronize()
+        ms64 = allmax(world, a.elapsed_time(b))
+        kt64 = eng3.kernel_times()
+        raw64 = eng3.raw_counts()
+        eng3.close()
+        same = all(np.array_equal(raw[k], raw64[k] * args.steps) for k in ("md", "md_random", "rdf", "rdf_random",
+                                                                          "solute_group", "solute_group_random"))
+        plain = {"value": world * nf / (ms64 / 1e3), "unit": "frames/s", "ms_per_step": ms64,
+                 "real_kernel_ms_per_frame": kt64["real"][0] / max(1, kt64["real"][1]),
+                 "counts_identical_to_fp32_guard": bool(same)}
+
+    # roofline of the dominant kernel: the real pass
+    peak = cm._native.measure_fp32_peak(local)
+    t_real = kt["real"][0] / max(1, kt["real"][1])  # ms per launch (one per frame)
+    cpu = None
+    W_real = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, out = cpu_baseline(xs, cells, args.cpu_frames)
+        W_real = out["pairs_real"] / out["nframes"]
+        cpu.pop("seconds", None)
+    else:
+        W_real = 7.13e7
+    flops = 8.0 * W_real
+    achieved = flops / (t_real * 1e-3) / 1e12
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    bytes_launch = 16.0 * NMOLS * APM
+    roofline = {
+        "bound": "fp32", "kernel": "k_pairs_real<fp32, self> (one launch per frame)",
+        "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+        "peak_source": "FP32 FMA throughput measured by cm_measure_fp32_peak on this GPU",
+        "traffic": None,
+        "work": f"8 flops x {W_real:.4g} atom pairs within cutoff per launch (real pass, ordered pairs)",
+        "launch_ms": t_real,
+        "hbm": {"achieved_gbs": bytes_launch / (t_real * 1e-3) / 1e9, "peak_gbs": hbm_peak,
+                "frac": bytes_launch / (t_real * 1e-3) / 1e9 / hbm_peak,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s"},
+    }
+    traffic_file = os.path.join(ROOT, "profiles", "pairs_real_c3_traffic.txt")
+    if os.path.exists(traffic_file):
+        try:
+            roofline["traffic"] = float(open(traffic_file).read().split()[0])
+        except Exception:
+            pass
+
+    launches = st["kernel_launches"] - st0["kernel_launches"]
+    line = {
+        "metric": "MDDF frames/s (config 3, batched FP32 + FP64 guard)", "value": value, "unit": "frames/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, config-3 shapes and distributions)",
+        "config": config_dict(nf, {"parallelism": "replicas" if world > 1 else "single GPU"}),
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
+        "plain_fp64": plain,
+        "fp32_guard_speedup_vs_plain_fp64": (value / world) / plain["value"] * world if plain else None,
+        "pair_evaluations_per_s": st["atom_pairs_evaluated"] / (ms / 1e3) * world,
+        "guard": {"reevaluations_per_frame": st["guard_reevaluations"] / max(1, st["frames"]),
+                  "hits_per_frame": (st["hits_real"] + st["hits_random"]) / max(1, st["frames"]),
+                  "max_fp32_error_A": st["max_guard_error"]},
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

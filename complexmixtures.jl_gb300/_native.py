@@ -57,6 +57,8 @@ class cm_system_desc(C.Structure):
         ("device", C.c_int32),
         ("max_frames_per_batch", C.c_int32),
         ("hbm_budget_bytes", C.c_int64),
+        ("kernel_timing", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -120,7 +122,15 @@ class cm_stats(C.Structure):
         ("guard_band", C.c_double),
         ("regime", C.c_int32),
         ("kernels_per_frame", C.c_int32),
+        ("kernel_launches", C.c_int64),
     ]
+
+
+KERNEL_CLASSES = ("prep", "cells", "real", "bulk", "random", "other")
+
+
+class cm_kernel_times(C.Structure):
+    _fields_ = [("ms", C.c_double * 6), ("launches", C.c_int64 * 6)]
 
 
 EXPORTED = (
@@ -130,12 +140,14 @@ EXPORTED = (
     "cm_read_counts",
     "cm_read_raw_counts",
     "cm_get_stats",
+    "cm_get_kernel_times",
     "cm_reset",
     "cm_destroy",
     "cm_last_error",
     "cm_status_string",
     "cm_device_bytes",
     "cm_stream",
+    "cm_measure_fp32_peak",
 )
 
 _lib: Optional[C.CDLL] = None
@@ -167,6 +179,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_read_raw_counts.restype = C.c_int
     lib.cm_get_stats.argtypes = [H, C.POINTER(cm_stats)]
     lib.cm_get_stats.restype = C.c_int
+    lib.cm_get_kernel_times.argtypes = [H, C.POINTER(cm_kernel_times)]
+    lib.cm_get_kernel_times.restype = C.c_int
     lib.cm_reset.argtypes = [H]
     lib.cm_reset.restype = C.c_int
     lib.cm_destroy.argtypes = [H]
@@ -179,6 +193,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_device_bytes.restype = C.c_int64
     lib.cm_stream.argtypes = [H]
     lib.cm_stream.restype = C.c_void_p
+    lib.cm_measure_fp32_peak.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_double)]
+    lib.cm_measure_fp32_peak.restype = C.c_int
     _lib = lib
     return lib
 
@@ -211,3 +227,11 @@ def csr(rows, nrows: int):
 
 def as_ptr(a: np.ndarray, ctype):
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def measure_fp32_peak(device: int = 0, ms_target: float = 200.0) -> float:
+    """FP32 CUDA-core TFLOP/s of a device (see cm_measure_fp32_peak)."""
+    lib = load()
+    out = C.c_double(0.0)
+    raise_for(lib.cm_measure_fp32_peak(device, ms_target, C.byref(out)), None)
+    return out.value

@@ -10,11 +10,12 @@
 // the whole list with the same counts.
 //
 // Two search layouts ("regimes"):
-//   PAIRS  molecules of both selections are small.  Molecules are binned by an
-//          anchor atom; a warp walks the stencil of one solute molecule, queues
-//          candidate solvent molecules whose anchors pass a bounding-sphere test,
-//          and each lane evaluates all atom pairs of one candidate.  In self mode
-//          each unordered pair is evaluated once and credited in both directions.
+//   PAIRS  molecules of both selections are small.  Molecules are binned by
+//          their centroid; a warp walks the stencil of one solute molecule,
+//          queues candidate solvent molecules whose bounding spheres come within
+//          the cutoff, and each lane evaluates all atom pairs of one candidate.
+//          In self mode each unordered pair is evaluated once and credited in
+//          both directions.
 //   ATOMS  the solute molecule is large (a protein).  Its atoms are counting-
 //          sorted into cells; one thread per solvent molecule scans the stencil
 //          of each of its atoms.
@@ -25,7 +26,8 @@
 // taken from the FP32 value only when the value is farther than the guard band
 // `delta` from the decision boundary; otherwise the pair is re-evaluated in FP64
 // with the same formula the FP64 mode uses, so both modes produce identical
-// integer counts.
+// integer counts.  `delta` is a rigorous bound on the FP32 rounding error,
+// computed per frame from the magnitudes that enter the FP32 displacement.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -42,7 +44,7 @@ using cmfeed::sub;
 using namespace cmgeom;
 
 constexpr int kMaxSmallMol = 32;  // PAIRS regime: atoms per molecule on either side
-constexpr int kWarps = 8;         // warps per CTA of the PAIRS real-pass kernel
+constexpr int kWarps = 8;         // warps per CTA of the PAIRS real-pass kernels
 constexpr int kQueue = 64;        // per-warp candidate queue
 
 enum : int { ERR_STENCIL = 1, ERR_BIN = 2, ERR_QUEUE = 4, ERR_SIZE = 8 };
@@ -80,12 +82,32 @@ struct DevSys {
     int *err;
 };
 
-// Radii found by the prep kernels (max over molecules), per frame.
+// FP32 decision constants of one frame.
+struct Guard {
+    double delta;     // Angstrom
+    float cutp2;      // (cut + delta)^2, rounded up
+    float cutm2;      // (cut - delta)^2, rounded down
+    float two_delta;
+    float inv_bs;     // 1 / binstep in FP32
+    float bin_band;   // half-width of the bin-edge band in units of bins
+    float dbulk_lo, dbulk_hi;
+    float cut_pre;    // cutoff + margin of the bounding-sphere tests
+};
+
+// Per-frame values found by the prep kernels and the constants derived from
+// them by k_frame_consts (one block, before the search kernels).
 struct FrameScratch {
-    float rmax_s;   // solute anchor radius
-    float rmax_v;   // solvent anchor radius
-    float rcmax;    // solvent centroid radius (placed molecules)
-    float pad;
+    float rmax_s;   // largest solute molecule radius (PAIRS: about the centroid)
+    float rmax_v;   // largest solvent molecule radius
+    float rcmax;    // largest solvent centroid radius (ATOMS layout)
+    int gq_count;   // candidates deferred to the guard kernel
+    int rq_count;   // random-insertion slots that reach the sampled solute molecule
+    int ok;         // stencils fit the offset table
+    int L[3];       // PAIRS stencil half-widths
+    int multi;      // PAIRS axes with several images (bit k set for axis k)
+    int La[3];      // ATOMS stencil half-widths
+    int pad;
+    Guard g;
 };
 
 struct Sample {
@@ -220,41 +242,6 @@ __device__ void stats_flush(const DevSys &S, LocalStats &st, bool rnd) {
         if (e > 0.0) atomicMax(S.stats + ST_MAXERR, (unsigned long long)__double_as_longlong(e));
     }
 }
-
-// ------------------------------------------------------------------ geometry
-// Sum of the lengths of the three cell edge vectors: bounds |q| of any site.
-__device__ __forceinline__ double cell_span(const FrameGeom &G) {
-    double s = 0.0;
-    for (int k = 0; k < 3; ++k) s += sqrt(G.Hn[3 * k] * G.Hn[3 * k] + G.Hn[3 * k + 1] * G.Hn[3 * k + 1] + G.Hn[3 * k + 2] * G.Hn[3 * k + 2]);
-    return s;
-}
-__device__ __forceinline__ double edge_len(const FrameGeom &G, int k) {
-    return sqrt(G.Hn[3 * k] * G.Hn[3 * k] + G.Hn[3 * k + 1] * G.Hn[3 * k + 1] + G.Hn[3 * k + 2] * G.Hn[3 * k + 2]);
-}
-
-// Stencil half-widths for a search range; false if the offset table is too small.
-__device__ __forceinline__ bool stencil(const FrameGeom &G, double range, int *L) {
-    bool ok = true;
-    for (int k = 0; k < 3; ++k) {
-        int l = (int)ceil(range * (1.0 + 1e-9) / G.cw[k]);
-        if (l < 1) l = 1;
-        if (l > kLT) { ok = false; l = kLT; }
-        L[k] = l;
-    }
-    return ok;
-}
-
-// Guard half-width (Angstrom) of the FP32 search: 2^-20 times a bound on the
-// magnitudes entering the FP32 displacement (each FP32 rounding contributes at
-// most 2^-24 of its operand; 16x covers the <= 9 roundings per component and
-// the norm).
-__device__ __forceinline__ double guard_band(const FrameGeom &G, const int *L, double radii) {
-    double span = cell_span(G);
-    double off = 0.0;
-    for (int k = 0; k < 3; ++k) off += L[k] * edge_len(G, k);
-    return 0x1.0p-20 * (2.0 * span + off + radii + 1.0);
-}
-
 
 // Images of a candidate pair: along axis k the stencil offsets
 // Delta_k = base_k + t * step_k, t < cnt_k.  A single image (cnt = 1 on every
@@ -475,31 +462,6 @@ __device__ double pairs_one64(const d4 *__restrict__ off64, const Images &im, d4
     return best;
 }
 
-// Guard-band constants of one kernel launch.
-struct Guard {
-    double delta;     // Angstrom
-    float cutp2;      // (cut + delta)^2, rounded up
-    float cutm2;      // (cut - delta)^2, rounded down
-    float two_delta;
-    float inv_bs;     // 1 / binstep in FP32
-    float bin_band;   // half-width of the bin-edge band in units of bins
-    float dbulk_lo, dbulk_hi;
-};
-
-__device__ __forceinline__ Guard make_guard(const DevSys &S, double delta) {
-    Guard g;
-    g.delta = delta;
-    double cp = S.cut + delta, cm = S.cut - delta;
-    g.cutp2 = __double2float_ru(cp * cp);
-    g.cutm2 = cm > 0.0 ? __double2float_rd(cm * cm) : 0.0f;
-    g.two_delta = __double2float_ru(2.0 * delta);
-    g.inv_bs = (float)(1.0 / S.binstep);
-    g.bin_band = __double2float_ru(delta / S.binstep + (double)S.nbins * 0x1.0p-21 + 1e-6);
-    g.dbulk_lo = __double2float_rd(S.dbulk - delta);
-    g.dbulk_hi = __double2float_ru(S.dbulk + delta);
-    return g;
-}
-
 // Bin from an FP32 distance, or -1 when it lies in the band around a bin edge.
 __device__ __forceinline__ int bin32(const Guard &g, float d) {
     float k = d * g.inv_bs;
@@ -631,6 +593,91 @@ __device__ __forceinline__ void unpack_delta(int c, int &dx, int &dy, int &dz) {
     dz = ((c >> 10) & 31) - 16;
 }
 
+// ------------------------------------------------------------------ geometry
+__device__ __forceinline__ double norm3d(double x, double y, double z) { return sqrt(x * x + y * y + z * z); }
+
+// Largest |Hn v| over the 8 sign patterns of v = (+-l0, +-l1, +-l2).
+__device__ double corner_norm(const FrameGeom &G, double l0, double l1, double l2) {
+    double best = 0.0;
+    for (int m = 0; m < 8; ++m) {
+        double v[3];
+        matvec_cm(G.Hn, (m & 1) ? -l0 : l0, (m & 2) ? -l1 : l1, (m & 4) ? -l2 : l2, v);
+        best = fmax(best, norm3d(v[0], v[1], v[2]));
+    }
+    return best;
+}
+
+// Stencil half-widths for a search range; false if the offset table is too small.
+__device__ bool stencil(const FrameGeom &G, double range, int *L) {
+    bool ok = true;
+    for (int k = 0; k < 3; ++k) {
+        int l = (int)ceil(range * (1.0 + 1e-9) / G.cw[k]);
+        if (l < 1) l = 1;
+        if (l > kLT) { ok = false; l = kLT; }
+        L[k] = l;
+    }
+    return ok;
+}
+
+// One thread computes the frame constants: stencils, the FP32 guard band, and
+// the slot table of the sampled solute molecules.
+//
+// Guard band.  In the FP32 displacement of an atom pair,
+//   dx = ((q_v - q_s) + off) + o_b) - o_a,
+// every input is the rounding of an FP64 value and every operation rounds, so
+// with u = 2^-24 each component is within u times the sum of the magnitudes of
+// the inputs and intermediate results of its exact value:
+//   |q| <= Q (a site inside its cell), |off| <= OFF (stencil offsets),
+//   |o| <= r (molecule radii), |q_v - q_s| <= Q, |D| <= Q + OFF,
+//   |t| <= Q + OFF + r_v, |dx| <= cutoff,
+// giving E = u (5Q + 3 OFF + 2 r_v + r_s + cutoff).  The distance is within
+// sqrt(3) E plus 2.5 u d (three roundings of d^2, one of the square root).  The
+// atom-cell layout's displacement (q_a - (q_b - off)) is bounded by the same
+// expression with r = 0.  delta adds 25 % to the bound.
+__global__ void k_frame_consts(DevSys S, const FrameGeom *__restrict__ Gp, FrameScratch *__restrict__ FS,
+                               const Sample *__restrict__ samples, int nsamples, int *__restrict__ slot_of_mol,
+                               int pairs) {
+    for (int i = threadIdx.x; i < nsamples; i += blockDim.x) slot_of_mol[samples[i].s] = samples[i].d;
+    if (threadIdx.x != 0) return;
+    const FrameGeom &G = *Gp;
+    FrameScratch &F = *FS;
+    double rs = S.self ? F.rmax_v : F.rmax_s, rv = F.rmax_v;
+    if (!pairs) rs = rv = 0.0;
+    const double range = S.cut + rs + rv;
+    int L[3], La[3];
+    bool ok = true;
+    if (pairs) ok = stencil(G, range + 1e-6 * (1.0 + range), L) && ok;
+    else L[0] = L[1] = L[2] = 1;
+    ok = stencil(G, S.cut * (1.0 + 1e-7) + 1e-7, La) && ok;
+    int multi = 0;
+    for (int k = 0; k < 3; ++k) {
+        F.L[k] = L[k];
+        F.La[k] = La[k];
+        if (2 * L[k] + 1 > G.n[k]) multi |= 1 << k;
+    }
+    F.multi = multi;
+    F.ok = ok ? 1 : 0;
+    const double Q = corner_norm(G, 1.0, 1.0, 1.0);
+    const int Lm[3] = {max(L[0], La[0]), max(L[1], La[1]), max(L[2], La[2])};
+    const double OFF = corner_norm(G, Lm[0], Lm[1], Lm[2]);
+    const double u = 0x1.0p-24;
+    const double E = u * (5.0 * Q + 3.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
+    const double delta = 1.25 * (1.7320508075688772 * E + 2.5 * u * (S.cut + 1.0)) + 1e-9;
+    Guard g;
+    g.delta = delta;
+    const double cp = S.cut + delta, cm = S.cut - delta;
+    g.cutp2 = __double2float_ru(cp * cp);
+    g.cutm2 = cm > 0.0 ? __double2float_rd(cm * cm) : 0.0f;
+    g.two_delta = __double2float_ru(2.0 * delta);
+    g.inv_bs = (float)(1.0 / S.binstep);
+    // |k - d/binstep| <= delta/binstep + (rounding of d * inv_bs and of inv_bs)
+    g.bin_band = __double2float_ru(delta / S.binstep + (double)(S.nbins + 1) * 4.0 * u + 1e-6);
+    g.dbulk_lo = __double2float_rd(S.dbulk - delta);
+    g.dbulk_hi = __double2float_ru(S.dbulk + delta);
+    g.cut_pre = __double2float_ru(S.cut + 1e-3 * (1.0 + range));
+    F.g = g;
+}
+
 // ------------------------------------------------------------------- kernels
 // Per-frame offset table: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
 __global__ void k_offtable(const FrameGeom *__restrict__ Gp, d4 *__restrict__ off64, float4 *__restrict__ off32) {
@@ -652,81 +699,61 @@ __device__ __forceinline__ void load_xyz(const T *p, double *x) {
 
 __device__ __forceinline__ void atomic_max_pos(float *addr, float v) { atomicMax((int *)addr, __float_as_int(v)); }
 
-// Molecule-centred data for random insertion (src/rigid_body.jl:127-134):
-// the molecule made whole around its reference atom, relative to its mean.
+// PAIRS regime prep, one thread per molecule.  The molecule is made whole
+// around its first atom (minimum image of each atom's displacement), its
+// centroid c = x_0 + mean(d) is binned, and its atoms are stored as FP64 and
+// FP32 offsets from the centroid; the radius is the largest offset (rounded
+// up).  Displacements shorter than 0.45 of the narrowest cell width are their
+// own minimum image, so the FP64 unwrap runs only for longer ones.
 template <typename T>
-__device__ void centroid_data(const FrameGeom &G, const T *x, int apm, int iref, d4 *u64, float &rc) {
-    double xr[3];
-    load_xyz(x + 3 * iref, xr);
-    double cm[3] = {0.0, 0.0, 0.0};
-    for (int b = 0; b < apm; ++b) {
-        double xb[3], d[3];
-        load_xyz(x + 3 * b, xb);
-        for (int k = 0; k < 3; ++k) d[k] = sub(xb[k], xr[k]);
-        double f[3];
-        matvec_rm(G.Hi, d[0], d[1], d[2], f);
-        double n0 = rint(f[0]), n1 = rint(f[1]), n2 = rint(f[2]);
-        if (n0 != 0.0 || n1 != 0.0 || n2 != 0.0) {
-            double sh[3];
-            matvec_cm(G.H, n0, n1, n2, sh);
-            for (int k = 0; k < 3; ++k) xb[k] = sub(xb[k], sh[k]);
-        }
-        u64[b] = make_d4(xb[0], xb[1], xb[2], 0.0);
-        for (int k = 0; k < 3; ++k) cm[k] = add(cm[k], xb[k]);
-    }
-    for (int k = 0; k < 3; ++k) cm[k] = div(cm[k], (double)apm);
-    double r = 0.0;
-    for (int b = 0; b < apm; ++b) {
-        d4 w = u64[b];
-        w.x = sub(w.x, cm[0]);
-        w.y = sub(w.y, cm[1]);
-        w.z = sub(w.z, cm[2]);
-        u64[b] = w;
-        r = fmax(r, sqrt(w.x * w.x + w.y * w.y + w.z * w.z));
-    }
-    rc = __double2float_ru(r * (1.0 + 1e-12) + 1e-12);
-}
-
-// PAIRS regime: anchor (first atom) binned, atoms as offsets from the anchor
-// made whole by minimum image; radius = largest offset.
-template <typename T>
-__global__ void k_prep_pairs(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int nmol, int apm, int iref,
+__global__ void k_prep_pairs(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int nmol, int apm,
                              int *__restrict__ mcell, float4 *__restrict__ mq32, d4 *__restrict__ mq64,
                              float4 *__restrict__ mo32, d4 *__restrict__ mo64, int *__restrict__ cellcount,
-                             float *__restrict__ rmax, d4 *__restrict__ u64, float *__restrict__ rc) {
+                             float *__restrict__ rmax) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmol) return;
     const FrameGeom &G = *Gp;
     const T *x = xyz + (int64_t)m * apm * 3;
+    const int64_t base = (int64_t)m * apm;
     double x0[3];
     load_xyz(x, x0);
-    int c[3];
-    double q[3];
-    bin_position(G, x0[0], x0[1], x0[2], c, q);
-    int cell = cell_linear(G, c[0], c[1], c[2]);
-    double r = 0.0;
+    const float wlim = (float)(0.45 * fmin(G.w[0], fmin(G.w[1], G.w[2])));
+    double sx = 0.0, sy = 0.0, sz = 0.0;
     for (int a = 0; a < apm; ++a) {
         double xa[3], d[3];
         load_xyz(x + 3 * a, xa);
         for (int k = 0; k < 3; ++k) d[k] = sub(xa[k], x0[k]);
-        unwrap(G, d);
-        int64_t ia = (int64_t)m * apm + a;
-        mo64[ia] = make_d4(d[0], d[1], d[2], 0.0);
-        mo32[ia] = make_float4((float)d[0], (float)d[1], (float)d[2], 0.f);
-        r = fmax(r, sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+        float fx = (float)d[0], fy = (float)d[1], fz = (float)d[2];
+        if (fmaf(fz, fz, fmaf(fy, fy, fx * fx)) > wlim * wlim) unwrap(G, d);
+        mo64[base + a] = make_d4(d[0], d[1], d[2], 0.0);
+        sx = add(sx, d[0]);
+        sy = add(sy, d[1]);
+        sz = add(sz, d[2]);
     }
-    float rf = __double2float_ru(r * (1.0 + 1e-12) + 1e-12);
+    const double n = (double)apm;
+    const double mx = div(sx, n), my = div(sy, n), mz = div(sz, n);
+    int c[3];
+    double q[3];
+    bin_position(G, add(x0[0], mx), add(x0[1], my), add(x0[2], mz), c, q);
+    const int cell = cell_linear(G, c[0], c[1], c[2]);
+    float r = 0.f;
+    for (int a = 0; a < apm; ++a) {
+        d4 w = mo64[base + a];
+        w.x = sub(w.x, mx);
+        w.y = sub(w.y, my);
+        w.z = sub(w.z, mz);
+        mo64[base + a] = w;
+        float fx = (float)w.x, fy = (float)w.y, fz = (float)w.z;
+        mo32[base + a] = make_float4(fx, fy, fz, 0.f);
+        r = fmaxf(r, norm3f(fx, fy, fz));
+    }
+    // radius bound: FP32 norm of the rounded offsets, enlarged to cover rounding
+    const float rf = r * (1.0f + 0x1.0p-18f) + 1e-5f;
     mcell[m] = cell;
     mq64[m] = make_d4(q[0], q[1], q[2], 0.0);
     mq32[m] = make_float4((float)q[0], (float)q[1], (float)q[2], rf);
     if (cellcount) atomicAdd(cellcount + cell, 1);
     atomic_max_pos(rmax, rf);
-    if (u64) {
-        float rcm;
-        centroid_data(G, x, apm, iref, u64 + (int64_t)m * apm, rcm);
-        rc[m] = rcm;
-        atomic_max_pos(rmax + 1, rcm);
-    }
 }
 
 // Exclusive scan of n counts into start[0..n] (single CTA of 1024 threads);
@@ -738,7 +765,6 @@ __global__ void __launch_bounds__(1024) k_scan(const int *__restrict__ count, in
     int lo = t * per, hi = min(n, lo + per);
     int local = 0;
     for (int i = lo; i < hi; ++i) local += count[i];
-    // block exclusive scan of `local`
     int lane = t & 31, w = t >> 5;
     int v = local;
     for (int o = 1; o < 32; o <<= 1) {
@@ -773,7 +799,110 @@ __global__ void k_scatter_mols(const int *__restrict__ mcell, int nmol, int *__r
     cmol[p] = m;
 }
 
-// PAIRS regime, real pass: one warp per solute molecule.
+// Images of a PAIRS candidate from its packed stencil offset.
+__device__ __forceinline__ Images images_of(const FrameGeom &G, const FrameScratch &F, int code) {
+    int d[3];
+    unpack_delta(code, d[0], d[1], d[2]);
+    Images im;
+    for (int k = 0; k < 3; ++k) {
+        if (F.multi & (1 << k)) {
+            axis_images(d[k], G.n[k], F.L[k], im.base[k], im.cnt[k]);
+            im.step[k] = G.n[k];
+        } else {
+            im.base[k] = d[k];
+            im.cnt[k] = 1;
+            im.step[k] = 0;
+        }
+    }
+    return im;
+}
+
+// Stencil walk of one solute molecule by one warp: every solvent molecule
+// whose bounding sphere reaches the solute's (cut_pre) is handed to
+// process(v, code) one candidate per lane, 32 at a time, through a warp queue.
+template <bool SELF, typename Proc>
+__device__ __forceinline__ void walk_candidates(const FrameGeom &G, const FrameScratch &F, int s, int sc, float4 qs32,
+                                                const float4 *__restrict__ off32, const float4 *__restrict__ vq32,
+                                                const int *__restrict__ cstart, const int *__restrict__ cmol, int *qv,
+                                                int *qi, int lane, Proc &&process) {
+    const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
+    const bool m0 = F.multi & 1, m1 = F.multi & 2, m2 = F.multi & 4;
+    const bool anymulti = F.multi != 0;
+    const int e0 = m0 ? n0 : 2 * F.L[0] + 1, e1 = m1 ? n1 : 2 * F.L[1] + 1, e2 = m2 ? n2 : 2 * F.L[2] + 1;
+    const int cx = sc % n0, cy = (sc / n0) % n1, cz = sc / (n0 * n1);
+    const float rsc = F.g.cut_pre + qs32.w;
+    int cnt = 0;
+    for (int iz = 0; iz < e2; ++iz) {
+        const int dz = m2 ? iz - cz : iz - F.L[2];
+        const int zc = m2 ? iz : wrapi(cz + dz, n2);
+        for (int iy = 0; iy < e1; ++iy) {
+            const int dy = m1 ? iy - cy : iy - F.L[1];
+            const int yc = m1 ? iy : wrapi(cy + dy, n1);
+            for (int ix = 0; ix < e0; ++ix) {
+                const int dx = m0 ? ix - cx : ix - F.L[0];
+                const int xc = m0 ? ix : wrapi(cx + dx, n0);
+                const int cell = (zc * n1 + yc) * n0 + xc;
+                const int beg = cstart[cell], end = cstart[cell + 1];
+                if (beg == end) continue;
+                const int code = pack_delta(dx, dy, dz);
+                float4 of = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (!anymulti) of = off32[off_index(dx, dy, dz)];
+                const float bx = of.x - qs32.x, by = of.y - qs32.y, bz = of.z - qs32.z;
+                for (int p0 = beg; p0 < end; p0 += 32) {
+                    const int p = p0 + lane;
+                    bool cand = false;
+                    int v = 0;
+                    if (p < end) {
+                        v = cmol[p];
+                        cand = !SELF || v > s;
+                        if (cand && !anymulti) {
+                            const float4 q = vq32[v];
+                            const float ex = q.x + bx, ey = q.y + by, ez = q.z + bz;
+                            const float rr = rsc + q.w;
+                            cand = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= rr * rr;
+                        }
+                    }
+                    const unsigned mask = __ballot_sync(0xffffffffu, cand);
+                    const int pos = cnt + __popc(mask & ((1u << lane) - 1u));
+                    if (cand) { qv[pos] = v; qi[pos] = code; }
+                    cnt += __popc(mask);
+                    if (cnt >= 32) {
+                        __syncwarp();
+                        process(qv[lane], qi[lane]);
+                        __syncwarp();
+                        int rest = cnt - 32, tv = 0, ti = 0;
+                        if (lane < rest) { tv = qv[32 + lane]; ti = qi[32 + lane]; }
+                        __syncwarp();
+                        if (lane < rest) { qv[lane] = tv; qi[lane] = ti; }
+                        cnt = rest;
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (lane < cnt) process(qv[lane], qi[lane]);
+    __syncwarp();
+}
+
+// Records of one direction written into the histograms and the bulk flags.
+template <bool SELF>
+__device__ __forceinline__ void emit(const DevSys &S, const SHist &h, const DirRec &r1, const DirRec &r2, int s, int v,
+                                     const int *__restrict__ slot_of_mol, unsigned char *__restrict__ flags, LocalStats &st) {
+    if (r1.within) { apply_hit(S, h, false, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
+    if (SELF && r2.within) { apply_hit(S, h, false, r2.bin, r2.i_local, r2.j, r2.ref, r2.rbin); st.hits++; }
+    if (slot_of_mol) {
+        int sl = slot_of_mol[s];
+        if (sl >= 0) flags[(int64_t)sl * S.mv + v] = flag_code(r1);
+        if (SELF) {
+            int vs = slot_of_mol[v];
+            if (vs >= 0) flags[(int64_t)vs * S.mv + s] = flag_code(r2);
+        }
+    }
+}
+
+// PAIRS regime, real pass, generic (any molecule size, FP32 or FP64).
 template <bool FP32, bool SELF>
 __global__ void __launch_bounds__(kWarps * 32)
     k_pairs_real(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS, const d4 *__restrict__ off64,
@@ -791,41 +920,21 @@ __global__ void __launch_bounds__(kWarps * 32)
     __syncthreads();
     SHist h = shist_bind(S, hbase);
     const FrameGeom &G = *Gp;
+    const FrameScratch &F = *FS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4 *os = os_all + warp * kMaxSmallMol;
     int *qv = q_all + warp * kQueue * 2;
     int *qi = qv + kQueue;
     LocalStats st;
-
-    const double rv = FS->rmax_v;
-    const double rs = SELF ? rv : (double)FS->rmax_s;
-    const double range = S.cut + rs + rv;
-    int L[3];
-    const bool ok = stencil(G, range + 1e-6 * (1.0 + range), L);
-    const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
-    const bool m0 = 2 * L[0] + 1 > n0, m1 = 2 * L[1] + 1 > n1, m2 = 2 * L[2] + 1 > n2;
-    const bool anymulti = m0 || m1 || m2;
-    const int e0 = m0 ? n0 : 2 * L[0] + 1, e1 = m1 ? n1 : 2 * L[1] + 1, e2 = m2 ? n2 : 2 * L[2] + 1;
-    const Guard g = make_guard(S, guard_band(G, L, 2.0 * (rs + rv)));
-    const float pre_margin = (float)(1e-3 * (1.0 + range));
-
-    if (ok) {
+    const Guard g = F.g;
+    if (F.ok) {
         for (int s = blockIdx.x * kWarps + warp; s < S.ms; s += gridDim.x * kWarps) {
-            const int sc = scell[s];
-            const int cx = sc % n0, cy = (sc / n0) % n1, cz = sc / (n0 * n1);
             const float4 qs32 = sq32[s];
             const d4 qs64 = sq64[s];
             for (int a = lane; a < S.aps; a += 32) os[a] = so32[(int64_t)s * S.aps + a];
             __syncwarp();
-            const int sslot = slot_of_mol ? slot_of_mol[s] : -1;
-            int cnt = 0;
             auto process = [&](int v, int code) {
-                int d0, d1, d2;
-                unpack_delta(code, d0, d1, d2);
-                Images im;
-                if (m0) { axis_images(d0, n0, L[0], im.base[0], im.cnt[0]); im.step[0] = n0; } else { im.base[0] = d0; im.cnt[0] = 1; im.step[0] = 0; }
-                if (m1) { axis_images(d1, n1, L[1], im.base[1], im.cnt[1]); im.step[1] = n1; } else { im.base[1] = d1; im.cnt[1] = 1; im.step[1] = 0; }
-                if (m2) { axis_images(d2, n2, L[2], im.base[2], im.cnt[2]); im.step[2] = n2; } else { im.base[2] = d2; im.cnt[2] = 1; im.step[2] = 0; }
+                const Images im = images_of(G, F, code);
                 const float4 qv32 = vq32[v];
                 const d4 qv64 = vq64[v];
                 const float4 *ov32 = vo32 + (int64_t)v * S.apv;
@@ -843,64 +952,9 @@ __global__ void __launch_bounds__(kWarps * 32)
                     pairs_exact<false, SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, 0.f, 0.f, 0.f, E);
                     records_from_exact<SELF>(S, E, s, v, r1, r2);
                 }
-                if (r1.within) { apply_hit(S, h, false, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
-                if (SELF && r2.within) { apply_hit(S, h, false, r2.bin, r2.i_local, r2.j, r2.ref, r2.rbin); st.hits++; }
-                if (sslot >= 0) flags[(int64_t)sslot * S.mv + v] = flag_code(r1);
-                if (SELF && slot_of_mol) {
-                    int vs = slot_of_mol[v];
-                    if (vs >= 0) flags[(int64_t)vs * S.mv + s] = flag_code(r2);
-                }
+                emit<SELF>(S, h, r1, r2, s, v, slot_of_mol, flags, st);
             };
-            for (int iz = 0; iz < e2; ++iz) {
-                int dz = m2 ? iz - cz : iz - L[2];
-                int zc = m2 ? iz : wrapi(cz + dz, n2);
-                for (int iy = 0; iy < e1; ++iy) {
-                    int dy = m1 ? iy - cy : iy - L[1];
-                    int yc = m1 ? iy : wrapi(cy + dy, n1);
-                    for (int ix = 0; ix < e0; ++ix) {
-                        int dx = m0 ? ix - cx : ix - L[0];
-                        int xc = m0 ? ix : wrapi(cx + dx, n0);
-                        const int cell = (zc * n1 + yc) * n0 + xc;
-                        const int beg = cstart[cell], end = cstart[cell + 1];
-                        const int code = pack_delta(dx, dy, dz);
-                        float4 of = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (!anymulti) of = off32[off_index(dx, dy, dz)];
-                        for (int p0 = beg; p0 < end; p0 += 32) {
-                            const int p = p0 + lane;
-                            bool cand = false;
-                            int v = 0;
-                            if (p < end) {
-                                v = cmol[p];
-                                cand = !SELF || v > s;
-                                if (cand && !anymulti) {
-                                    float4 qv = vq32[v];
-                                    float Dx = (qv.x - qs32.x) + of.x, Dy = (qv.y - qs32.y) + of.y, Dz = (qv.z - qs32.z) + of.z;
-                                    float rr = S.cut + qs32.w + qv.w + pre_margin;
-                                    cand = fmaf(Dz, Dz, fmaf(Dy, Dy, Dx * Dx)) <= rr * rr;
-                                }
-                            }
-                            const unsigned mask = __ballot_sync(0xffffffffu, cand);
-                            const int pos = cnt + __popc(mask & ((1u << lane) - 1u));
-                            if (cand) { qv[pos] = v; qi[pos] = code; }
-                            cnt += __popc(mask);
-                            if (cnt >= 32) {
-                                __syncwarp();
-                                process(qv[lane], qi[lane]);
-                                __syncwarp();
-                                int rest = cnt - 32, tv = 0, ti = 0;
-                                if (lane < rest) { tv = qv[32 + lane]; ti = qi[32 + lane]; }
-                                __syncwarp();
-                                if (lane < rest) { qv[lane] = tv; qi[lane] = ti; }
-                                cnt = rest;
-                                __syncwarp();
-                            }
-                        }
-                    }
-                }
-            }
-            __syncwarp();
-            if (lane < cnt) process(qv[lane], qi[lane]);
-            __syncwarp();
+            walk_candidates<SELF>(G, F, s, scell[s], qs32, off32, vq32, cstart, cmol, qv, qi, lane, process);
         }
     } else if (threadIdx.x == 0) {
         raise_err(S, ERR_STENCIL);
@@ -911,29 +965,35 @@ __global__ void __launch_bounds__(kWarps * 32)
 }
 
 // Bulk-molecule list of each distinct sampled solute molecule, ascending
-// (src/mddf.jl:406-415); one CTA per sampled molecule.
+// (src/mddf.jl:406-415); one CTA per sampled molecule.  Clears the molecule's
+// entry of the slot table when done (it was set by k_frame_consts).
 __global__ void __launch_bounds__(1024) k_bulk(const DevSys S, const Sample *__restrict__ samples, int nsamples,
-                                              const unsigned char *__restrict__ flags, int *__restrict__ bulk, int *__restrict__ nbulk) {
+                                              const unsigned char *__restrict__ flags, int *__restrict__ bulk,
+                                              int *__restrict__ nbulk, int *__restrict__ slot_of_mol) {
     __shared__ int wsum[32];
     __shared__ int carry;
-    // find the sample that introduces distinct index blockIdx.x
-    int d = blockIdx.x;
-    int s = -1;
-    for (int i = 0; i < nsamples; ++i)
-        if (samples[i].d == d) { s = samples[i].s; break; }
-    if (threadIdx.x == 0) carry = 0;
+    __shared__ int s_sh;
+    const int d = blockIdx.x;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        s_sh = -1;
+    }
     __syncthreads();
+    for (int i = threadIdx.x; i < nsamples; i += blockDim.x)
+        if (samples[i].d == d && samples[i].rep == 0) s_sh = samples[i].s;
+    __syncthreads();
+    const int s = s_sh;
     const unsigned char *f = flags + (int64_t)d * S.mv;
     int *out = bulk + (int64_t)d * S.mv;
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int base = 0; base < S.mv; base += blockDim.x) {
-        int v = base + threadIdx.x;
+        const int v = base + threadIdx.x;
         int keep = 0;
         if (v < S.mv && !(S.self && v == s)) {
-            unsigned char c = f[v];
+            const unsigned char c = f[v];
             keep = S.usecutoff ? (c == 2) : (c == 0);
         }
-        unsigned m = __ballot_sync(0xffffffffu, keep);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) wsum[w] = __popc(m);
         __syncthreads();
         if (w == 0) {
@@ -945,13 +1005,16 @@ __global__ void __launch_bounds__(1024) k_bulk(const DevSys S, const Sample *__r
             wsum[lane] = x;
         }
         __syncthreads();
-        int pos = carry + (w > 0 ? wsum[w - 1] : 0) + __popc(m & ((1u << lane) - 1u));
+        const int pos = carry + (w > 0 ? wsum[w - 1] : 0) + __popc(m & ((1u << lane) - 1u));
         if (keep) out[pos] = v;
         __syncthreads();
         if (threadIdx.x == 0) carry += wsum[(blockDim.x >> 5) - 1];
         __syncthreads();
     }
-    if (threadIdx.x == 0) nbulk[d] = carry;
+    if (threadIdx.x == 0) {
+        nbulk[d] = carry;
+        if (s >= 0) slot_of_mol[s] = -1;
+    }
 }
 
 // Draws of one placement slot, in stream order: bulk pick, centre, angles.
@@ -982,96 +1045,154 @@ __device__ __forceinline__ void draw_rotation(uint64_t &st, double *A) {
     cmfeed::eulermat(cb, sb, cg, sg, ct, stt, A);
 }
 
-// PAIRS regime, random pass: one thread per (slot, sample).  Each slot gets a
-// copy of a bulk molecule, rotated and centred at a random point
-// (src/mddf.jl:65-88, src/rigid_body.jl:107-137); only slots whose bounding
-// sphere reaches the sampled solute molecule are rotated and evaluated.
-template <bool FP32, bool SELF>
+// Images of a placed molecule (centre in fractional coordinates fc) relative
+// to solute molecule s, and its cell-relative position.
+__device__ __forceinline__ Images placed_images(const FrameGeom &G, const FrameScratch &F, int sc, const double *fc,
+                                                double *qp) {
+    int cp[3];
+    bin_fractional(G, fc, cp, qp);
+    const int cs[3] = {sc % G.n[0], (sc / G.n[0]) % G.n[1], sc / (G.n[0] * G.n[1])};
+    Images im;
+    for (int q = 0; q < 3; ++q) {
+        axis_images(cp[q] - cs[q], G.n[q], F.L[q], im.base[q], im.cnt[q]);
+        im.step[q] = G.n[q];
+    }
+    return im;
+}
+
+// PAIRS random pass, stage 1: one thread per (sample, slot).  Draws the bulk
+// molecule and the new centre (src/mddf.jl:65-88, src/rigid_body.jl:115-120)
+// and keeps the slot if the placed molecule's bounding sphere reaches the
+// sampled solute molecule's.  Nothing outside the kept slots is evaluated:
+// their molecules cannot come within the cutoff.
 __global__ void __launch_bounds__(128)
-    k_pairs_random(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS, const d4 *__restrict__ off64,
-                   const float4 *__restrict__ off32, const Sample *__restrict__ samples, int sample0, const int *__restrict__ scell,
-                   const float4 *__restrict__ sq32, const d4 *__restrict__ sq64, const float4 *__restrict__ so32,
-                   const d4 *__restrict__ so64, const d4 *__restrict__ u64, const float *__restrict__ rc,
-                   const int *__restrict__ bulk, const int *__restrict__ nbulk) {
+    k_random_filter(DevSys S, const FrameGeom *__restrict__ Gp, FrameScratch *__restrict__ FS,
+                    const float4 *__restrict__ off32, const Sample *__restrict__ samples, int sample0, int nsamp,
+                    const int *__restrict__ scell, const float4 *__restrict__ sq32, const float4 *__restrict__ vq32,
+                    const int *__restrict__ bulk, const int *__restrict__ nbulk, int2 *__restrict__ rq, int rq_cap) {
+    const FrameGeom &G = *Gp;
+    const FrameScratch &F = *FS;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (!F.ok || t >= (int64_t)nsamp * S.mv) return;
+    const int i = sample0 + (int)(t / S.mv), k = (int)(t % S.mv);
+    const Sample sm = samples[i];
+    const int s = sm.s;
+    if (S.self && k == s) return;
+    const Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
+    double qp[3];
+    const Images im = placed_images(G, F, scell[s], P.fc, qp);
+    const float4 qs = sq32[s];
+    const float rr = F.g.cut_pre + qs.w + vq32[P.jmol].w;
+    const float px = (float)qp[0] - qs.x, py = (float)qp[1] - qs.y, pz = (float)qp[2] - qs.z;
+    bool any = false;
+    CM_FOR_IMAGES(im, ix, iy, iz) {
+        const float4 o = off32[off_index(ix, iy, iz)];
+        const float Dx = px + o.x, Dy = py + o.y, Dz = pz + o.z;
+        any |= fmaf(Dz, Dz, fmaf(Dy, Dy, Dx * Dx)) <= rr * rr;
+    }
+    if (!any) return;
+    const int slot = atomicAdd(&FS->rq_count, 1);
+    if (slot < rq_cap) rq[slot] = make_int2(i, k);
+    else raise_err(S, ERR_QUEUE);
+}
+
+// PAIRS random pass, stage 2: one thread per kept slot.  Rotates the bulk
+// molecule about its centroid (src/rigid_body.jl:73-80, 122-134) and evaluates
+// it against the sampled solute molecule (one direction).
+template <bool FP32>
+__global__ void __launch_bounds__(128)
+    k_random_eval(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS,
+                  const d4 *__restrict__ off64, const float4 *__restrict__ off32, const Sample *__restrict__ samples,
+                  const int *__restrict__ scell, const float4 *__restrict__ sq32, const d4 *__restrict__ sq64,
+                  const float4 *__restrict__ so32, const d4 *__restrict__ so64, const d4 *__restrict__ vo64,
+                  const int *__restrict__ bulk, const int *__restrict__ nbulk, const int2 *__restrict__ rq, int rq_cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
-    const int hw = hist_words(S);
-    float4 *os32 = (float4 *)(smem_raw + (((size_t)hw * 4 + 15) & ~(size_t)15));
-    d4 *os64 = (d4 *)(os32 + kMaxSmallMol);
     shist_zero(S, hbase);
-    const Sample sm = samples[sample0 + blockIdx.y];
-    const int s = sm.s;
-    for (int a = threadIdx.x; a < S.aps; a += blockDim.x) {
-        os32[a] = so32[(int64_t)s * S.aps + a];
-        os64[a] = so64[(int64_t)s * S.aps + a];
-    }
     __syncthreads();
     SHist h = shist_bind(S, hbase);
     const FrameGeom &G = *Gp;
+    const FrameScratch &F = *FS;
     LocalStats st;
-    const double rs = SELF ? (double)FS->rmax_v : (double)FS->rmax_s;
-    const double rcm = FS->rcmax;
-    const double range = S.cut + rs + rcm;
-    int L[3];
-    const bool ok = stencil(G, range + 1e-6 * (1.0 + range), L);
-    const Guard g = make_guard(S, guard_band(G, L, 2.0 * (rs + rcm)));
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!ok) {
-        if (threadIdx.x == 0) raise_err(S, ERR_STENCIL);
-    } else if (k < S.mv && !(SELF && k == s)) {
+    const Guard g = F.g;
+    const int n = min(F.rq_count, rq_cap);
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
+        const int2 e = rq[it];
+        const Sample sm = samples[e.x];
+        const int s = sm.s, k = e.y;
         Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
-        int cp[3];
         double qp[3];
-        bin_fractional(G, P.fc, cp, qp);
-        const int sc = scell[s];
-        const int cs[3] = {sc % G.n[0], (sc / G.n[0]) % G.n[1], sc / (G.n[0] * G.n[1])};
-        Images im;
-        for (int q = 0; q < 3; ++q) {
-            axis_images(cp[q] - cs[q], G.n[q], L[q], im.base[q], im.cnt[q]);
-            im.step[q] = G.n[q];
+        const Images im = placed_images(G, F, scell[s], P.fc, qp);
+        double A[9];
+        draw_rotation(P.st, A);
+        d4 ov64[kMaxSmallMol];
+        float4 ov32[kMaxSmallMol];
+        const d4 *o = vo64 + (int64_t)P.jmol * S.apv;
+        for (int b = 0; b < S.apv; ++b) {
+            const d4 w = o[b];
+            double r[3];
+            matvec_rm(A, w.x, w.y, w.z, r);
+            ov64[b] = make_d4(r[0], r[1], r[2], 0.0);
+            ov32[b] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
         }
         const float4 qs32 = sq32[s];
         const d4 qs64 = sq64[s];
         const float4 qp32 = make_float4((float)qp[0], (float)qp[1], (float)qp[2], 0.f);
         const d4 qp64 = make_d4(qp[0], qp[1], qp[2], 0.0);
-        const float rr = (float)(S.cut + rs + rc[P.jmol] + 1e-3 * (1.0 + range));
-        bool any = false;
-        CM_FOR_IMAGES(im, ix, iy, iz) {
-            float4 o = off32[off_index(ix, iy, iz)];
-            float Dx = (qp32.x - qs32.x) + o.x, Dy = (qp32.y - qs32.y) + o.y, Dz = (qp32.z - qs32.z) + o.z;
-            any |= fmaf(Dz, Dz, fmaf(Dy, Dy, Dx * Dx)) <= rr * rr;
+        const float4 *os32 = so32 + (int64_t)s * S.aps;
+        const d4 *os64 = so64 + (int64_t)s * S.aps;
+        DirRec r1, r2;
+        st.molpairs++;
+        st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
+        if (FP32) {
+            Pass32 Q;
+            pairs_pass32<false>(S, off32, im, qs32, qp32, os32, ov32, Q);
+            pairs_decide<false>(S, g, Q, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, s, k, r1, r2, st);
+        } else {
+            Exact64 E;
+            pairs_exact<false, false>(S, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, 0.f, 0.f, 0.f, E);
+            records_from_exact<false>(S, E, s, k, r1, r2);
         }
-        if (any) {
-            double A[9];
-            draw_rotation(P.st, A);
-            d4 ov64[kMaxSmallMol];
-            float4 ov32[kMaxSmallMol];
-            const d4 *u = u64 + (int64_t)P.jmol * S.apv;
-            for (int b = 0; b < S.apv; ++b) {
-                d4 w = u[b];
-                double o[3];
-                matvec_rm(A, w.x, w.y, w.z, o);
-                ov64[b] = make_d4(o[0], o[1], o[2], 0.0);
-                ov32[b] = make_float4((float)o[0], (float)o[1], (float)o[2], 0.f);
-            }
-            DirRec r1, r2;
-            st.molpairs++;
-            st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
-            if (FP32) {
-                Pass32 Q;
-                pairs_pass32<false>(S, off32, im, qs32, qp32, os32, ov32, Q);
-                pairs_decide<false>(S, g, Q, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, s, k, r1, r2, st);
-            } else {
-                Exact64 E;
-                pairs_exact<false, false>(S, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, 0.f, 0.f, 0.f, E);
-                records_from_exact<false>(S, E, s, k, r1, r2);
-            }
-            if (r1.within) { apply_hit(S, h, true, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
-        }
+        if (r1.within) { apply_hit(S, h, true, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
     }
     stats_flush(S, st, true);
     __syncthreads();
     shist_flush(S, h, true);
+}
+
+// Molecule-centred data for random insertion (src/rigid_body.jl:127-134):
+// the molecule made whole around its reference atom, relative to its mean.
+template <typename T>
+__device__ void centroid_data(const FrameGeom &G, const T *x, int apm, int iref, d4 *u64, float &rc) {
+    double xr[3];
+    load_xyz(x + 3 * iref, xr);
+    double cm[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < apm; ++b) {
+        double xb[3], d[3];
+        load_xyz(x + 3 * b, xb);
+        for (int k = 0; k < 3; ++k) d[k] = sub(xb[k], xr[k]);
+        double f[3];
+        matvec_rm(G.Hi, d[0], d[1], d[2], f);
+        double n0 = rint(f[0]), n1 = rint(f[1]), n2 = rint(f[2]);
+        if (n0 != 0.0 || n1 != 0.0 || n2 != 0.0) {
+            double sh[3];
+            matvec_cm(G.H, n0, n1, n2, sh);
+            for (int k = 0; k < 3; ++k) xb[k] = sub(xb[k], sh[k]);
+        }
+        u64[b] = make_d4(xb[0], xb[1], xb[2], 0.0);
+        for (int k = 0; k < 3; ++k) cm[k] = add(cm[k], xb[k]);
+    }
+    for (int k = 0; k < 3; ++k) cm[k] = div(cm[k], (double)apm);
+    double r = 0.0;
+    for (int b = 0; b < apm; ++b) {
+        d4 w = u64[b];
+        w.x = sub(w.x, cm[0]);
+        w.y = sub(w.y, cm[1]);
+        w.z = sub(w.z, cm[2]);
+        u64[b] = w;
+        r = fmax(r, sqrt(w.x * w.x + w.y * w.y + w.z * w.z));
+    }
+    rc = __double2float_ru(r * (1.0 + 1e-12) + 1e-12);
 }
 
 // ----------------------------------------------------------- ATOMS regime
@@ -1181,7 +1302,8 @@ struct AtomPass {
 // molecule (real pass) or sample of the chunk (random pass).
 template <bool FP32, bool RANDOM>
 __global__ void __launch_bounds__(128)
-    k_atoms_eval(DevSys S, const FrameGeom *__restrict__ Gp, const d4 *__restrict__ off64, const float4 *__restrict__ off32,
+    k_atoms_eval(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS, const d4 *__restrict__ off64,
+                 const float4 *__restrict__ off32,
                  const int *__restrict__ sstart, const float4 *__restrict__ sq32, const d4 *__restrict__ sq64,
                  const int *__restrict__ vcell, const float4 *__restrict__ vq32, const d4 *__restrict__ vq64,
                  const Sample *__restrict__ samples, int sample0, const int *__restrict__ slot_of_mol,
@@ -1201,9 +1323,10 @@ __global__ void __launch_bounds__(128)
     } else {
         s = blockIdx.y;
     }
-    int L[3];
-    const bool ok = stencil(G, S.cut * (1.0 + 1e-7) + 1e-7, L);
-    const Guard g = make_guard(S, guard_band(G, L, 0.0));
+    const FrameScratch &F = *FS;
+    const int L[3] = {F.La[0], F.La[1], F.La[2]};
+    const bool ok = F.ok;
+    const Guard g = F.g;
     const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     const int *cs = sstart + (int64_t)s * G.ncell;
@@ -1402,11 +1525,22 @@ __global__ void k_fold(unsigned long long *__restrict__ acc, double *__restrict_
     }
 }
 
-// Slot table of the sampled solute molecules (set / clear).
-__global__ void k_slots(const Sample *__restrict__ samples, int n, int *__restrict__ slot_of_mol, int set) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    slot_of_mol[samples[i].s] = set ? samples[i].d : -1;
+// FP32 throughput probe: kProbeChains independent multiply-add chains per
+// thread kept in registers, so the loop is issue-bound on the FP32 pipes.
+constexpr int kProbeChains = 8;
+__global__ void __launch_bounds__(256) k_fma_probe(float *__restrict__ sink, int iters, float m) {
+    float a[kProbeChains];
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) a[k] = (float)(threadIdx.x + k) * 1e-3f;
+    const float c = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < kProbeChains; ++k) a[k] = fmaf(a[k], m, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) s += a[k];
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
 }  // namespace cmk

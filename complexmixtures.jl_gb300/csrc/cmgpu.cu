@@ -21,6 +21,7 @@
 
 #include "../../include/cmgpu.h"
 #include "cm_kernels.cuh"
+#include "cm_pairs32.cuh"
 
 using namespace cmk;
 using cmgeom::FrameGeom;
@@ -79,7 +80,8 @@ struct cm_handle {
     DevBuf geoms, samples, fscratch, off64, off32, hist, sums, stats, errflag, slot_of_mol, flags, bulk, nbulk;
     DevBuf stage_s[2], stage_v[2];
     // PAIRS
-    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, u64, rc, ccount, cstart, cfill, cmol;
+    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, u64, rc, ccount, cstart, cfill, cmol, gq, rq;
+    int gq_cap = 0, rq_cap = 0;
     // group tables
     DevBuf g_soff, g_sidx, g_voff, g_vidx;
     // ATOMS
@@ -101,6 +103,20 @@ struct cm_handle {
     double last_guard = 0.0;
     int kernels_per_frame = 0;
     int chunk_parity = 0;
+
+    // launch accounting and optional per-launch event timing
+    int64_t launches_total = 0;
+    int64_t class_launches[CM_K_NCLASSES] = {0, 0, 0, 0, 0, 0};
+    double class_ms[CM_K_NCLASSES] = {0, 0, 0, 0, 0, 0};
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_free;
+    struct Pending {
+        int cls;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    cudaEvent_t cur_start = nullptr;
+    int cur_class = 0;
 };
 
 namespace {
@@ -169,18 +185,26 @@ void frame_geometry(const double *H, double cs, int ncap_axis, FrameGeom &G) {
     G.ncell = G.n[0] * G.n[1] * G.n[2];
 }
 
-// Host restatement of the anchor radius of a selection (largest distance of an
-// atom to its molecule's first atom, minimum image), used to size PAIRS cells.
-double anchor_radius(const double *xyz, int nmol, int apm, const double *H) {
+// Largest distance of an atom to its molecule's centroid (molecule made whole
+// around its first atom by minimum image); sizes the PAIRS cells on the host.
+double centroid_radius(const double *xyz, int nmol, int apm, const double *H) {
     FrameGeom G;
     frame_geometry(H, 1e30, 1, G);
     double r = 0.0;
+    std::vector<double> d(3 * (size_t)apm);
     for (int m = 0; m < nmol; ++m) {
         const double *x0 = xyz + (int64_t)m * apm * 3;
-        for (int a = 1; a < apm; ++a) {
-            double d[3] = {x0[3 * a] - x0[0], x0[3 * a + 1] - x0[1], x0[3 * a + 2] - x0[2]};
-            cmgeom::unwrap(G, d);
-            r = std::max(r, std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+        double c[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < apm; ++a) {
+            double *e = &d[3 * (size_t)a];
+            for (int k = 0; k < 3; ++k) e[k] = x0[3 * a + k] - x0[k];
+            cmgeom::unwrap(G, e);
+            for (int k = 0; k < 3; ++k) c[k] += e[k];
+        }
+        for (int a = 0; a < apm; ++a) {
+            double *e = &d[3 * (size_t)a];
+            double dx = e[0] - c[0] / apm, dy = e[1] - c[1] / apm, dz = e[2] - c[2] / apm;
+            r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz));
         }
     }
     return r;
@@ -337,16 +361,19 @@ void plan(cm_handle *h, const cm_frames *f) {
                 out[i] = h->coord_elem == 4 ? (double)reinterpret_cast<float *>(raw.data())[i] : reinterpret_cast<double *>(raw.data())[i];
         };
         fetch(f->solute_xyz, h->Ns, xs);
-        double rs = anchor_radius(xs.data(), d.solute_nmols, d.solute_natomspermol, f->cells);
+        double rs = centroid_radius(xs.data(), d.solute_nmols, d.solute_natomspermol, f->cells);
         double rv = rs;
         if (!d.autocorrelation) {
             fetch(f->solvent_xyz, h->Nv, xv);
-            rv = anchor_radius(xv.data(), d.solvent_nmols, d.solvent_natomspermol, f->cells);
+            rv = centroid_radius(xv.data(), d.solvent_nmols, d.solvent_natomspermol, f->cells);
         }
         double cut = d.usecutoff ? d.cutoff : d.dbulk;
         h->pair_cell = (cut + rs + rv) * 1.05 + 0.25;
     }
     h->max_frames = d.max_frames_per_batch > 0 ? d.max_frames_per_batch : 64;
+    // keep the per-chunk sample table bounded (n_random_samples can be 10^5)
+    if (h->mddf && (int64_t)h->max_frames * d.n_random_samples > (1 << 22))
+        h->max_frames = (int)std::max<int64_t>(1, (1 << 22) / std::max(1, d.n_random_samples));
 
     // common buffers
     dev_alloc(h, h->geoms, sizeof(FrameGeom) * h->max_frames * 2);
@@ -389,6 +416,19 @@ void plan(cm_handle *h, const cm_frames *f) {
             dev_alloc(h, h->vo64, h->Nv * 32);
         }
         dev_alloc(h, h->cmol, mv * 4);
+        // guard queue: every candidate fits when the system is small enough
+        // (candidates <= ms * mv); otherwise 64 per solute molecule, far above
+        // the guard-band rate
+        const int64_t pairs_bound = ms * mv;
+        h->gq_cap = (int)(pairs_bound <= (1LL << 24) ? std::max<int64_t>(pairs_bound, 1024)
+                                                     : std::min<int64_t>(std::max<int64_t>(1 << 20, 64 * ms), 1LL << 26));
+        dev_alloc(h, h->gq, (size_t)h->gq_cap * sizeof(int4));
+        if (h->mddf) {
+            // random-insertion queue: every slot of up to `chunk` samples fits
+            const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(d.n_random_samples, (1 << 22) / mv));
+            h->rq_cap = (int)(chunk * mv);
+            dev_alloc(h, h->rq, (size_t)h->rq_cap * sizeof(int2));
+        }
     } else {
         dev_alloc(h, h->akey, h->Ns * 4);
         dev_alloc(h, h->atq32, h->Ns * 16);
@@ -405,7 +445,7 @@ void plan(cm_handle *h, const cm_frames *f) {
             dev_alloc(h, h->pq64, (size_t)chunk * h->Nv * 32);
         }
     }
-    if (h->mddf) {
+    if (h->mddf && h->regime == CM_REGIME_ATOMS) {
         dev_alloc(h, h->u64, h->Nv * 32);
         dev_alloc(h, h->rc, mv * 4);
     }
@@ -417,18 +457,29 @@ void plan(cm_handle *h, const cm_frames *f) {
     size_t smem_max = std::max(smem_real, smem_rand);
     if (smem_max > 48 * 1024) {
         int a = (int)smem_max;
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_real<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_pairs_random<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
-        CM_CUDA(cudaFuncSetAttribute(k_atoms_eval<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a));
+        auto attr = [&](const void *f) { CM_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, a)); };
+        attr((const void *)k_pairs_real<true, true>);
+        attr((const void *)k_pairs_real<true, false>);
+        attr((const void *)k_pairs_real<false, true>);
+        attr((const void *)k_pairs_real<false, false>);
+        attr((const void *)k_random_eval<true>);
+        attr((const void *)k_random_eval<false>);
+        attr((const void *)k_atoms_eval<true, true>);
+        attr((const void *)k_atoms_eval<true, false>);
+        attr((const void *)k_atoms_eval<false, true>);
+        attr((const void *)k_atoms_eval<false, false>);
+        attr((const void *)k_pairs_guard<true>);
+        attr((const void *)k_pairs_guard<false>);
+        attr((const void *)k_pairs_real32<1, true>);
+        attr((const void *)k_pairs_real32<1, false>);
+        attr((const void *)k_pairs_real32<3, true>);
+        attr((const void *)k_pairs_real32<3, false>);
+        attr((const void *)k_pairs_real32<4, true>);
+        attr((const void *)k_pairs_real32<4, false>);
+        attr((const void *)k_pairs_real32<5, true>);
+        attr((const void *)k_pairs_real32<5, false>);
+        attr((const void *)k_pairs_real32<14, true>);
+        attr((const void *)k_pairs_real32<14, false>);
     }
     h->planned = true;
 }
@@ -459,6 +510,56 @@ int draw_samples(const cm_handle *h, int64_t frame_id, Sample *out, int &ndistin
 
 int grid_for(int64_t n, int block) { return (int)std::max<int64_t>(1, (n + block - 1) / block); }
 
+cudaEvent_t ev_get(cm_handle *h) {
+    if (!h->ev_free.empty()) {
+        cudaEvent_t e = h->ev_free.back();
+        h->ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    CM_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+// Fold finished timing events into the per-class totals (synchronises).
+void timing_drain(cm_handle *h) {
+    if (h->pending.empty()) return;
+    CM_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto &p : h->pending) {
+        float ms = 0.f;
+        CM_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+        h->class_ms[p.cls] += ms;
+        h->ev_free.push_back(p.a);
+        h->ev_free.push_back(p.b);
+    }
+    h->pending.clear();
+}
+
+void kbegin(cm_handle *h, int cls) {
+    h->cur_class = cls;
+    if (!h->timing) return;
+    if (h->pending.size() > 65536) timing_drain(h);
+    h->cur_start = ev_get(h);
+    CM_CUDA(cudaEventRecord(h->cur_start, h->stream));
+}
+
+void kend(cm_handle *h) {
+    h->launches_total++;
+    h->class_launches[h->cur_class]++;
+    if (!h->timing) return;
+    cudaEvent_t e = ev_get(h);
+    CM_CUDA(cudaEventRecord(e, h->stream));
+    h->pending.push_back({h->cur_class, h->cur_start, e});
+}
+
+#define CM_LAUNCH(cls, ...)   \
+    do {                      \
+        kbegin(h, cls);       \
+        __VA_ARGS__;          \
+        kend(h);              \
+        launches++;           \
+    } while (0)
+
 template <typename T>
 void run_frame(cm_handle *h, const FrameGeom *dG, const FrameGeom &G, const Sample *dS, int nsamp, int ndist, const T *xs,
                const T *xv) {
@@ -471,118 +572,137 @@ void run_frame(cm_handle *h, const FrameGeom *dG, const FrameGeom &G, const Samp
     const int iref = d.irefatom - 1;
     FrameScratch *FS = P<FrameScratch>(h->fscratch);
     int launches = 0;
-    CM_CUDA(cudaMemsetAsync(FS, 0, sizeof(FrameScratch), st));
-    k_offtable<<<grid_for(cmgeom::kOffEntries, 256), 256, 0, st>>>(dG, P<d4>(h->off64), P<float4>(h->off32));
-    launches++;
     const bool rnd = h->mddf && nsamp > 0;
-    if (rnd) {
-        k_slots<<<grid_for(nsamp, 256), 256, 0, st>>>(dS, nsamp, P<int>(h->slot_of_mol), 1);
-        launches++;
-    }
+    const int *slot = rnd ? P<int>(h->slot_of_mol) : nullptr;
+    unsigned char *flags = rnd ? P<unsigned char>(h->flags) : nullptr;
     const size_t hsm = hist_smem_bytes(h, h->smem_groups);
+    int sms = 0;
+    CM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    CM_CUDA(cudaMemsetAsync(FS, 0, sizeof(FrameScratch), st));
+    CM_LAUNCH(CM_K_PREP, k_offtable<<<grid_for(cmgeom::kOffEntries, 256), 256, 0, st>>>(dG, P<d4>(h->off64), P<float4>(h->off32)));
+    ensure_cells(h, G.ncell);
     if (h->regime == CM_REGIME_PAIRS) {
-        ensure_cells(h, G.ncell);
         if (rnd) CM_CUDA(cudaMemsetAsync(h->flags.p, 0, (size_t)ndist * mv, st));
         CM_CUDA(cudaMemsetAsync(h->ccount.p, 0, (size_t)(G.ncell + 1) * 4, st));
-        // solute molecules (and, in self mode, the solvent cell list)
-        float *rmax_s = self ? &FS->rmax_v : &FS->rmax_s;
-        k_prep_pairs<T><<<grid_for(ms, 128), 128, 0, st>>>(dG, xs, ms, aps, iref, P<int>(h->scell), P<float4>(h->sq32), P<d4>(h->sq64),
-                                                          P<float4>(h->so32), P<d4>(h->so64), self ? P<int>(h->ccount) : nullptr,
-                                                          rmax_s, (self && h->mddf) ? P<d4>(h->u64) : nullptr, P<float>(h->rc));
-        launches++;
-        if (!self) {
-            k_prep_pairs<T><<<grid_for(mv, 128), 128, 0, st>>>(dG, xv, mv, apv, iref, P<int>(h->vcell), P<float4>(h->vq32),
-                                                              P<d4>(h->vq64), P<float4>(h->vo32), P<d4>(h->vo64),
-                                                              P<int>(h->ccount), &FS->rmax_v, h->mddf ? P<d4>(h->u64) : nullptr,
-                                                              P<float>(h->rc));
-            launches++;
-        }
-        k_scan<<<1, 1024, 0, st>>>(P<int>(h->ccount), G.ncell, P<int>(h->cstart), P<int>(h->cfill));
-        k_scatter_mols<<<grid_for(mv, 256), 256, 0, st>>>(self ? P<int>(h->scell) : P<int>(h->vcell), mv, P<int>(h->cfill), P<int>(h->cmol));
-        launches += 2;
-        const int *vcell = self ? P<int>(h->scell) : P<int>(h->vcell);
-        (void)vcell;
+        // solute molecules (in self mode also the solvent cell list)
+        CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<grid_for(ms, 128), 128, 0, st>>>(
+                                 dG, xs, ms, aps, P<int>(h->scell), P<float4>(h->sq32), P<d4>(h->sq64), P<float4>(h->so32),
+                                 P<d4>(h->so64), self ? P<int>(h->ccount) : nullptr, self ? &FS->rmax_v : &FS->rmax_s));
+        if (!self)
+            CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<grid_for(mv, 128), 128, 0, st>>>(
+                                     dG, xv, mv, apv, P<int>(h->vcell), P<float4>(h->vq32), P<d4>(h->vq64), P<float4>(h->vo32),
+                                     P<d4>(h->vo64), P<int>(h->ccount), &FS->rmax_v));
+        CM_LAUNCH(CM_K_PREP, k_frame_consts<<<1, 128, 0, st>>>(S, dG, FS, dS, rnd ? nsamp : 0, P<int>(h->slot_of_mol), 1));
+        CM_LAUNCH(CM_K_CELLS, k_scan<<<1, 1024, 0, st>>>(P<int>(h->ccount), G.ncell, P<int>(h->cstart), P<int>(h->cfill)));
+        CM_LAUNCH(CM_K_CELLS, k_scatter_mols<<<grid_for(mv, 256), 256, 0, st>>>(self ? P<int>(h->scell) : P<int>(h->vcell), mv,
+                                                                               P<int>(h->cfill), P<int>(h->cmol)));
         const float4 *vq32 = self ? P<float4>(h->sq32) : P<float4>(h->vq32);
         const d4 *vq64 = self ? P<d4>(h->sq64) : P<d4>(h->vq64);
         const float4 *vo32 = self ? P<float4>(h->so32) : P<float4>(h->vo32);
         const d4 *vo64 = self ? P<d4>(h->so64) : P<d4>(h->vo64);
-        size_t smem = hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
-        int dev_sms = 0;
-        CM_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device));
-        int grid = std::min<int64_t>((ms + kWarps - 1) / kWarps, (int64_t)dev_sms * 8);
-        const int *slot = rnd ? P<int>(h->slot_of_mol) : nullptr;
-        unsigned char *flags = rnd ? P<unsigned char>(h->flags) : nullptr;
-#define CM_PAIRS_REAL(F, SF)                                                                                                      \
-    k_pairs_real<F, SF><<<grid, kWarps * 32, smem, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), P<int>(h->scell),  \
-                                                         P<float4>(h->sq32), P<d4>(h->sq64), P<float4>(h->so32),              \
-                                                         P<d4>(h->so64), vq32, vq64, vo32, vo64, P<int>(h->cstart),           \
-                                                         P<int>(h->cmol), slot, flags)
-        if (fp32 && self) CM_PAIRS_REAL(true, true);
-        else if (fp32) CM_PAIRS_REAL(true, false);
-        else if (self) CM_PAIRS_REAL(false, true);
-        else CM_PAIRS_REAL(false, false);
+        const size_t smem = hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
+        const int grid = (int)std::min<int64_t>((ms + kWarps - 1) / kWarps, (int64_t)sms * 8);
+        GuardQueue gq{P<int4>(h->gq), h->gq_cap};
+        bool special = false;
+        if (fp32) {
+#define CM_PAIRS_R32(A, SF)                                                                                            \
+    CM_LAUNCH(CM_K_REAL, k_pairs_real32<A, SF><<<grid, kWarps * 32, smem, st>>>(                                       \
+                             S, dG, FS, P<float4>(h->off32), P<int>(h->scell), P<float4>(h->sq32), P<float4>(h->so32), \
+                             vq32, vo32, P<int>(h->cstart), P<int>(h->cmol), slot, flags, gq))
+#define CM_PAIRS_R32_APV(A)              \
+    case A:                              \
+        if (self) CM_PAIRS_R32(A, true); \
+        else CM_PAIRS_R32(A, false);     \
+        special = true;                  \
+        break;
+            switch (apv) {
+                CM_PAIRS_R32_APV(1)
+                CM_PAIRS_R32_APV(3)
+                CM_PAIRS_R32_APV(4)
+                CM_PAIRS_R32_APV(5)
+                CM_PAIRS_R32_APV(14)
+                default: break;
+            }
+#undef CM_PAIRS_R32_APV
+#undef CM_PAIRS_R32
+        }
+        if (special) {
+#define CM_GUARD(SF)                                                                                                     \
+    CM_LAUNCH(CM_K_REAL, k_pairs_guard<SF><<<sms * 4, 128, hsm, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32),  \
+                                                                      P<float4>(h->sq32), P<d4>(h->sq64),                \
+                                                                      P<float4>(h->so32), P<d4>(h->so64), vq32, vq64,    \
+                                                                      vo32, vo64, slot, flags, gq))
+            if (self) CM_GUARD(true);
+            else CM_GUARD(false);
+#undef CM_GUARD
+        } else {
+#define CM_PAIRS_REAL(F, SF)                                                                                              \
+    CM_LAUNCH(CM_K_REAL, k_pairs_real<F, SF><<<grid, kWarps * 32, smem, st>>>(                                            \
+                             S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), P<int>(h->scell), P<float4>(h->sq32),       \
+                             P<d4>(h->sq64), P<float4>(h->so32), P<d4>(h->so64), vq32, vq64, vo32, vo64,                  \
+                             P<int>(h->cstart), P<int>(h->cmol), slot, flags))
+            if (fp32 && self) CM_PAIRS_REAL(true, true);
+            else if (fp32) CM_PAIRS_REAL(true, false);
+            else if (self) CM_PAIRS_REAL(false, true);
+            else CM_PAIRS_REAL(false, false);
 #undef CM_PAIRS_REAL
-        launches++;
+        }
         if (rnd) {
-            k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk), P<int>(h->nbulk));
-            launches++;
-            size_t smr = hsm + kMaxSmallMol * 48;
-            for (int s0 = 0; s0 < nsamp; s0 += 65535) {
-                int ny = std::min(65535, nsamp - s0);
-                dim3 gr(grid_for(mv, 128), ny);
-#define CM_PAIRS_RAND(F, SF)                                                                                                   \
-    k_pairs_random<F, SF><<<gr, 128, smr, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), dS, s0, P<int>(h->scell), \
-                                                P<float4>(h->sq32), P<d4>(h->sq64), P<float4>(h->so32), P<d4>(h->so64), \
-                                                P<d4>(h->u64), P<float>(h->rc), P<int>(h->bulk), P<int>(h->nbulk))
-                if (fp32 && self) CM_PAIRS_RAND(true, true);
-                else if (fp32) CM_PAIRS_RAND(true, false);
-                else if (self) CM_PAIRS_RAND(false, true);
-                else CM_PAIRS_RAND(false, false);
-#undef CM_PAIRS_RAND
-                launches++;
+            CM_LAUNCH(CM_K_BULK, k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk),
+                                                                P<int>(h->nbulk), P<int>(h->slot_of_mol)));
+            const int chunk = std::max(1, h->rq_cap / mv);
+            for (int s0 = 0; s0 < nsamp; s0 += chunk) {
+                const int ny = std::min(chunk, nsamp - s0);
+                CM_CUDA(cudaMemsetAsync(&FS->rq_count, 0, sizeof(int), st));
+                CM_LAUNCH(CM_K_RANDOM, k_random_filter<<<grid_for((int64_t)ny * mv, 128), 128, 0, st>>>(
+                                           S, dG, FS, P<float4>(h->off32), dS, s0, ny, P<int>(h->scell), P<float4>(h->sq32),
+                                           vq32, P<int>(h->bulk), P<int>(h->nbulk), P<int2>(h->rq), h->rq_cap));
+#define CM_RAND(F)                                                                                                        \
+    CM_LAUNCH(CM_K_RANDOM, k_random_eval<F><<<sms * 2, 128, hsm, st>>>(                                                 \
+                               S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), dS, P<int>(h->scell), P<float4>(h->sq32), \
+                               P<d4>(h->sq64), P<float4>(h->so32), P<d4>(h->so64), vo64, P<int>(h->bulk),                \
+                               P<int>(h->nbulk), P<int2>(h->rq), h->rq_cap))
+                if (fp32) CM_RAND(true);
+                else CM_RAND(false);
+#undef CM_RAND
             }
         }
     } else {
-        ensure_cells(h, G.ncell);
         const T *xsolv = self ? xs : xv;
-        k_prep_atoms_solvent<T><<<grid_for(mv, 128), 128, 0, st>>>(dG, xsolv, mv, apv, iref, P<int>(h->avcell), P<float4>(h->avq32),
-                                                                  P<d4>(h->avq64), h->mddf ? P<d4>(h->u64) : nullptr,
-                                                                  P<float>(h->rc), &FS->rcmax);
-        int64_t nkeys = (int64_t)ms * G.ncell;
+        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solvent<T><<<grid_for(mv, 128), 128, 0, st>>>(
+                                 dG, xsolv, mv, apv, iref, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64),
+                                 h->mddf ? P<d4>(h->u64) : nullptr, P<float>(h->rc), &FS->rcmax));
+        const int64_t nkeys = (int64_t)ms * G.ncell;
         CM_CUDA(cudaMemsetAsync(h->acount.p, 0, (size_t)(nkeys + 1) * 4, st));
-        k_prep_atoms_solute<T><<<grid_for(h->Ns, 256), 256, 0, st>>>(dG, xs, (int)h->Ns, aps, P<int>(h->akey), P<float4>(h->atq32),
-                                                                    P<d4>(h->atq64), P<int>(h->acount));
-        k_scan<<<1, 1024, 0, st>>>(P<int>(h->acount), (int)nkeys, P<int>(h->astart), P<int>(h->afill));
-        k_scatter_atoms<<<grid_for(h->Ns, 256), 256, 0, st>>>(P<int>(h->akey), (int)h->Ns, P<float4>(h->atq32), P<d4>(h->atq64),
-                                                             P<int>(h->afill), P<float4>(h->asq32), P<d4>(h->asq64));
-        launches += 4;
-        const int *slot = rnd ? P<int>(h->slot_of_mol) : nullptr;
-        unsigned char *flags = rnd ? P<unsigned char>(h->flags) : nullptr;
+        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solute<T><<<grid_for(h->Ns, 256), 256, 0, st>>>(
+                                 dG, xs, (int)h->Ns, aps, P<int>(h->akey), P<float4>(h->atq32), P<d4>(h->atq64), P<int>(h->acount)));
+        CM_LAUNCH(CM_K_PREP, k_frame_consts<<<1, 128, 0, st>>>(S, dG, FS, dS, rnd ? nsamp : 0, P<int>(h->slot_of_mol), 0));
+        CM_LAUNCH(CM_K_CELLS, k_scan<<<1, 1024, 0, st>>>(P<int>(h->acount), (int)nkeys, P<int>(h->astart), P<int>(h->afill)));
+        CM_LAUNCH(CM_K_CELLS, k_scatter_atoms<<<grid_for(h->Ns, 256), 256, 0, st>>>(
+                                  P<int>(h->akey), (int)h->Ns, P<float4>(h->atq32), P<d4>(h->atq64), P<int>(h->afill),
+                                  P<float4>(h->asq32), P<d4>(h->asq64)));
+        if (ms > 65535) throw cm_error(CM_EINVAL, "the ATOMS layout supports at most 65535 solute molecules");
         dim3 gr(grid_for(mv, 128), ms);
-#define CM_ATOMS(F, R, GRID, VC, VQ32, VQ64, S0)                                                                                  \
-    k_atoms_eval<F, R><<<GRID, 128, hsm, st>>>(S, dG, P<d4>(h->off64), P<float4>(h->off32), P<int>(h->astart),             \
-                                               P<float4>(h->asq32), P<d4>(h->asq64), VC, VQ32, VQ64, dS, S0, slot, flags)
-        if (fp32) CM_ATOMS(true, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
-        else CM_ATOMS(false, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
-        launches++;
+#define CM_ATOMS(CLS, F, R, GRID, VC, VQ32, VQ64, S0)                                                                     \
+    CM_LAUNCH(CLS, k_atoms_eval<F, R><<<GRID, 128, hsm, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32),          \
+                                                              P<int>(h->astart), P<float4>(h->asq32), P<d4>(h->asq64), \
+                                                              VC, VQ32, VQ64, dS, S0, slot, flags))
+        if (fp32) CM_ATOMS(CM_K_REAL, true, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
+        else CM_ATOMS(CM_K_REAL, false, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
         if (rnd) {
-            k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk), P<int>(h->nbulk));
-            launches++;
+            CM_LAUNCH(CM_K_BULK, k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk),
+                                                                P<int>(h->nbulk), P<int>(h->slot_of_mol)));
             for (int s0 = 0; s0 < nsamp; s0 += kChunkSamples) {
-                int ny = std::min(kChunkSamples, nsamp - s0);
+                const int ny = std::min(kChunkSamples, nsamp - s0);
                 dim3 gp(grid_for(mv, 128), ny);
-                k_atoms_place<<<gp, 128, 0, st>>>(S, dG, dS, s0, P<d4>(h->u64), P<int>(h->bulk), P<int>(h->nbulk), P<int>(h->pcell),
-                                                  P<float4>(h->pq32), P<d4>(h->pq64));
-                if (fp32) CM_ATOMS(true, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
-                else CM_ATOMS(false, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
-                launches += 2;
+                CM_LAUNCH(CM_K_RANDOM, k_atoms_place<<<gp, 128, 0, st>>>(S, dG, dS, s0, P<d4>(h->u64), P<int>(h->bulk),
+                                                                         P<int>(h->nbulk), P<int>(h->pcell), P<float4>(h->pq32),
+                                                                         P<d4>(h->pq64)));
+                if (fp32) CM_ATOMS(CM_K_RANDOM, true, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
+                else CM_ATOMS(CM_K_RANDOM, false, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
             }
         }
 #undef CM_ATOMS
-    }
-    if (rnd) {
-        k_slots<<<grid_for(nsamp, 256), 256, 0, st>>>(dS, nsamp, P<int>(h->slot_of_mol), 0);
-        launches++;
     }
     CM_CUDA(cudaGetLastError());
     h->kernels_per_frame = launches;
@@ -590,7 +710,9 @@ void run_frame(cm_handle *h, const FrameGeom *dG, const FrameGeom &G, const Samp
 
 void fold_class(cm_handle *h) {
     if (!h->class_open) return;
-    k_fold<<<grid_for(h->hist_n, 256), 256, 0, h->stream>>>(P<unsigned long long>(h->hist), P<double>(h->sums), h->hist_n, h->class_w);
+    int launches = 0;
+    CM_LAUNCH(CM_K_OTHER, k_fold<<<grid_for(h->hist_n, 256), 256, 0, h->stream>>>(P<unsigned long long>(h->hist), P<double>(h->sums), h->hist_n, h->class_w));
+    (void)launches;
     CM_CUDA(cudaGetLastError());
     h->folds++;
     h->class_open = false;
@@ -690,7 +812,7 @@ void check_device_error(cm_handle *h) {
         std::string m = "device-side check failed:";
         if (e & ERR_STENCIL) m += " search range wider than the offset table (box too small for the cutoff);";
         if (e & ERR_BIN) m += " histogram bin out of range;";
-        if (e & ERR_QUEUE) m += " candidate queue overflow;";
+        if (e & ERR_QUEUE) m += " guard or random-insertion queue overflow (rerun with FP64 precision);";
         if (e & ERR_SIZE) m += " molecule too large for the PAIRS layout;";
         throw cm_error(CM_EDEVICE, m);
     }
@@ -722,7 +844,7 @@ void free_all(cm_handle *h) {
     DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag,
                      &h->slot_of_mol, &h->flags, &h->bulk, &h->nbulk, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
-                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->akey, &h->atq32,
+                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->gq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
                      &h->pcell, &h->pq32, &h->pq64, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx};
     for (DevBuf *b : all) {
@@ -738,6 +860,13 @@ void free_all(cm_handle *h) {
         if (h->ev_copied[i]) cudaEventDestroy(h->ev_copied[i]);
         if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
     }
+    for (auto &p : h->pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    h->pending.clear();
+    for (cudaEvent_t e : h->ev_free) cudaEventDestroy(e);
+    h->ev_free.clear();
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
 }
@@ -761,6 +890,7 @@ int cm_create(const cm_system_desc *desc, cm_handle **out) {
         h->Ns = (int64_t)desc->solute_nmols * desc->solute_natomspermol;
         h->Nv = (int64_t)desc->solvent_nmols * desc->solvent_natomspermol;
         h->mddf = desc->mode == CM_MODE_MDDF;
+        h->timing = desc->kernel_timing != 0;
         if (desc->solute_group_offsets) {
             copy_csr(desc->solute_natomspermol, desc->solute_ngroups, desc->solute_group_offsets, desc->solute_groups, h->gs_off,
                      h->gs_idx, "solute");
@@ -916,6 +1046,19 @@ int cm_get_stats(cm_handle *h, cm_stats *out) {
         out->guard_band = h->last_guard;
         out->regime = h->regime;
         out->kernels_per_frame = h->kernels_per_frame;
+        out->kernel_launches = h->launches_total;
+    });
+}
+
+int cm_get_kernel_times(cm_handle *h, cm_kernel_times *out) {
+    return guarded(h, [&] {
+        if (!out) throw cm_error(CM_EINVAL, "NULL output");
+        if (!h->timing) throw cm_error(CM_ESTATE, "kernel timing was not enabled at cm_create");
+        timing_drain(h);
+        for (int i = 0; i < CM_K_NCLASSES; ++i) {
+            out->ms[i] = h->class_ms[i];
+            out->launches[i] = h->class_launches[i];
+        }
     });
 }
 
@@ -931,6 +1074,12 @@ int cm_reset(cm_handle *h) {
         h->folds = 0;
         h->volume_total = h->weight_total = 0.0;
         h->frames = 0;
+        timing_drain(h);
+        h->launches_total = 0;
+        for (int i = 0; i < CM_K_NCLASSES; ++i) {
+            h->class_ms[i] = 0.0;
+            h->class_launches[i] = 0;
+        }
     });
 }
 
@@ -961,6 +1110,45 @@ const char *cm_status_string(int status) {
 }
 
 int64_t cm_device_bytes(const cm_handle *h) { return h ? h->device_bytes : 0; }
+
+int cm_measure_fp32_peak(int32_t device, double ms_target, double *tflops) {
+    if (!tflops) return CM_EINVAL;
+    try {
+        CM_CUDA(cudaSetDevice(device));
+        int sms = 0;
+        CM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        const int block = 256, blocks = sms * 8;
+        float *sink = nullptr;
+        CM_CUDA(cudaMalloc(&sink, sizeof(float) * block * blocks));
+        cudaStream_t st;
+        CM_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        cudaEvent_t a, b;
+        CM_CUDA(cudaEventCreate(&a));
+        CM_CUDA(cudaEventCreate(&b));
+        int iters = 1 << 12;
+        double best = 0.0;
+        for (int rep = 0; rep < 6; ++rep) {
+            CM_CUDA(cudaEventRecord(a, st));
+            k_fma_probe<<<blocks, block, 0, st>>>(sink, iters, 1.0000001f);
+            CM_CUDA(cudaEventRecord(b, st));
+            CM_CUDA(cudaEventSynchronize(b));
+            float ms = 0.f;
+            CM_CUDA(cudaEventElapsedTime(&ms, a, b));
+            double flops = (double)blocks * block * iters * kProbeChains * 2.0;
+            best = std::max(best, flops / (ms * 1e-3) / 1e12);
+            if (ms < ms_target / 6.0 && iters < (1 << 24)) iters *= 2;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        cudaStreamDestroy(st);
+        cudaFree(sink);
+        *tflops = best;
+        return CM_OK;
+    } catch (const cm_error &e) {
+        g_create_error = e.msg;
+        return e.code;
+    }
+}
 
 void *cm_stream(cm_handle *h) { return h ? (void *)h->stream : nullptr; }
 

@@ -58,6 +58,7 @@ class Engine:
         device: int = 0,
         max_frames_per_batch: int = 0,
         hbm_budget_bytes: int = 0,
+        kernel_timing: bool = False,
     ):
         self._lib = N.load()
         self._h = C.c_void_p()
@@ -96,6 +97,7 @@ class Engine:
         d.device = device
         d.max_frames_per_batch = max_frames_per_batch
         d.hbm_budget_bytes = hbm_budget_bytes
+        d.kernel_timing = 1 if kernel_timing else 0
         st = self._lib.cm_create(C.byref(d), C.byref(self._h))
         N.raise_for(st, None)
         self.desc = d
@@ -218,6 +220,13 @@ class Engine:
         st = self._lib.cm_get_stats(self._h, C.byref(s))
         N.raise_for(st, self._h)
         return {name: getattr(s, name) for name, _ in N.cm_stats._fields_}
+
+    def kernel_times(self) -> dict:
+        """{class: (ms, launches)} since create / reset (kernel_timing=True)."""
+        t = N.cm_kernel_times()
+        st = self._lib.cm_get_kernel_times(self._h, C.byref(t))
+        N.raise_for(st, self._h)
+        return {k: (t.ms[i], t.launches[i]) for i, k in enumerate(N.KERNEL_CLASSES)}
 
     def synchronize(self) -> None:
         N.raise_for(self._lib.cm_synchronize(self._h), self._h)

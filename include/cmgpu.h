@@ -102,6 +102,8 @@ typedef struct cm_system_desc {
     int32_t device;                   /* CUDA device ordinal */
     int32_t max_frames_per_batch;     /* frames staged on the device per submit chunk; 0 = 64 */
     int64_t hbm_budget_bytes;         /* 0 = no limit; cm_create fails with CM_ENOMEM above it */
+    int32_t kernel_timing;            /* 1: time every launch with CUDA events (cm_get_kernel_times) */
+    int32_t reserved;
 } cm_system_desc;
 
 /*
@@ -162,8 +164,27 @@ typedef struct cm_stats {
     double max_guard_error;               /* max |d_fp32 - d_fp64| seen in re-evaluated pairs (Angstrom) */
     double guard_band;                    /* guard half-width used in the last frame (Angstrom) */
     int32_t regime;                       /* CM_REGIME_PAIRS or CM_REGIME_ATOMS actually used */
-    int32_t kernels_per_frame;            /* kernel launches per frame */
+    int32_t kernels_per_frame;            /* kernel launches of the last frame */
+    int64_t kernel_launches;              /* kernel launches since create / reset */
 } cm_stats;
+
+/* Kernel classes of cm_get_kernel_times. */
+enum {
+    CM_K_PREP = 0,        /* binning, offsets, centroid data, offset table */
+    CM_K_CELLS = 1,       /* counting sort: scan + scatter */
+    CM_K_REAL = 2,        /* real-frame minimum distances + histograms */
+    CM_K_BULK = 3,        /* bulk-molecule lists */
+    CM_K_RANDOM = 4,      /* random-insertion placement + minimum distances */
+    CM_K_OTHER = 5,       /* sample slots, weight folds */
+    CM_K_NCLASSES = 6
+};
+
+/* Per-class GPU time (ms, from CUDA events around each launch on the handle's
+ * stream) and launch counts since create / reset; needs kernel_timing = 1. */
+typedef struct cm_kernel_times {
+    double ms[CM_K_NCLASSES];
+    int64_t launches[CM_K_NCLASSES];
+} cm_kernel_times;
 
 typedef struct cm_handle cm_handle;
 
@@ -186,6 +207,9 @@ int cm_read_raw_counts(cm_handle *h, cm_raw_counts *out);
 /* Engine statistics (synchronises). */
 int cm_get_stats(cm_handle *h, cm_stats *out);
 
+/* Kernel times per class (synchronises). */
+int cm_get_kernel_times(cm_handle *h, cm_kernel_times *out);
+
 /* Zero the accumulators and statistics; keeps device allocations. */
 int cm_reset(cm_handle *h);
 
@@ -198,6 +222,11 @@ const char *cm_last_error(const cm_handle *h);
 
 /* Static description of a status code. */
 const char *cm_status_string(int status);
+
+/* Measure the FP32 CUDA-core throughput of a device (TFLOP/s, FMA = 2 flops)
+ * with a register-resident multiply-add loop over all SMs; the denominator of
+ * the engine's compute roofline.  Runs for about `ms_target` milliseconds. */
+int cm_measure_fp32_peak(int32_t device, double ms_target, double *tflops);
 
 /* Device memory the handle holds, in bytes. */
 int64_t cm_device_bytes(const cm_handle *h);

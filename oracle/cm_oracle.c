@@ -353,6 +353,8 @@ static int64_t min_distances(ctx *C, int s, const double *xs, const double *y, m
         return npairs;
     }
     /* cells backend: the anchors of y are binned in C (cells_build must have run on y) */
+    double pre = cut + C->rmax + 1e-6 * (1.0 + cut);
+    double pre2 = pre * pre;
     for (int a = 0; a < D->aps; ++a) {
         const double *x = xs + 3 * a;
         double f[3];
@@ -385,6 +387,9 @@ static int64_t min_distances(ctx *C, int s, const double *xs, const double *y, m
                         if (D->autocorrelation && v == s) continue;
                         if (C->stamp[v] == C->stampc) continue;
                         C->stamp[v] = C->stampc;
+                        /* no atom of v can be within the cutoff if its anchor is
+                         * farther than cutoff + rmax (exact, conservative) */
+                        if (mindist2(ci, x, y + (int64_t)v * D->apv * 3) > pre2) continue;
                         for (int b = 0; b < D->apv; ++b) {
                             int64_t j = (int64_t)v * D->apv + b;
                             double d2 = mindist2(ci, x, y + 3 * j);

@@ -28,11 +28,12 @@ def test_library_exports_header_symbols(cm):
 def test_struct_sizes_match_header(cm):
     N = cm._native
     # field-by-field mirror of include/cmgpu.h on LP64
-    assert C.sizeof(N.cm_system_desc) == 160
+    assert C.sizeof(N.cm_system_desc) == 168
     assert C.sizeof(N.cm_frames) == 56
     assert C.sizeof(N.cm_counts) == 88
     assert C.sizeof(N.cm_raw_counts) == 64
-    assert C.sizeof(N.cm_stats) == 80
+    assert C.sizeof(N.cm_stats) == 88
+    assert C.sizeof(N.cm_kernel_times) == 96
 
 
 def test_create_rejects_bad_descriptions_without_gpu(cm):
