@@ -126,11 +126,11 @@ class cm_stats(C.Structure):
     ]
 
 
-KERNEL_CLASSES = ("prep", "cells", "real", "bulk", "random", "other")
+KERNEL_CLASSES = ("prep", "cells", "real", "bulk", "random", "other", "guard")
 
 
 class cm_kernel_times(C.Structure):
-    _fields_ = [("ms", C.c_double * 6), ("launches", C.c_int64 * 6)]
+    _fields_ = [("ms", C.c_double * 7), ("launches", C.c_int64 * 7)]
 
 
 EXPORTED = (

@@ -619,75 +619,70 @@ __device__ bool stencil(const FrameGeom &G, double range, int *L) {
     return ok;
 }
 
-// One thread computes the frame constants: stencils, the FP32 guard band, and
-// the slot table of the sampled solute molecules.
-//
-// Guard band.  In the FP32 displacement of an atom pair,
-//   dx = ((q_v - q_s) + off) + o_b) - o_a,
-// every input is the rounding of an FP64 value and every operation rounds, so
-// with u = 2^-24 each component is within u times the sum of the magnitudes of
-// the inputs and intermediate results of its exact value:
-//   |q| <= Q (a site inside its cell), |off| <= OFF (stencil offsets),
-//   |o| <= r (molecule radii), |q_v - q_s| <= Q, |D| <= Q + OFF,
-//   |t| <= Q + OFF + r_v, |dx| <= cutoff,
-// giving E = u (5Q + 3 OFF + 2 r_v + r_s + cutoff).  The distance is within
-// sqrt(3) E plus 2.5 u d (three roundings of d^2, one of the square root).  The
-// atom-cell layout's displacement (q_a - (q_b - off)) is bounded by the same
-// expression with r = 0.  delta adds 25 % to the bound.
-__global__ void k_frame_consts(DevSys S, const FrameGeom *__restrict__ Gp, FrameScratch *__restrict__ FS,
-                               const Sample *__restrict__ samples, int nsamples, int *__restrict__ slot_of_mol,
-                               int pairs) {
-    for (int i = threadIdx.x; i < nsamples; i += blockDim.x) slot_of_mol[samples[i].s] = samples[i].d;
-    if (threadIdx.x != 0) return;
-    const FrameGeom &G = *Gp;
-    FrameScratch &F = *FS;
-    double rs = S.self ? F.rmax_v : F.rmax_s, rv = F.rmax_v;
-    if (!pairs) rs = rv = 0.0;
-    const double range = S.cut + rs + rv;
-    int L[3], La[3];
-    bool ok = true;
-    if (pairs) ok = stencil(G, range + 1e-6 * (1.0 + range), L) && ok;
-    else L[0] = L[1] = L[2] = 1;
-    ok = stencil(G, S.cut * (1.0 + 1e-7) + 1e-7, La) && ok;
-    int multi = 0;
-    for (int k = 0; k < 3; ++k) {
-        F.L[k] = L[k];
-        F.La[k] = La[k];
-        if (2 * L[k] + 1 > G.n[k]) multi |= 1 << k;
-    }
-    F.multi = multi;
-    F.ok = ok ? 1 : 0;
-    const double Q = corner_norm(G, 1.0, 1.0, 1.0);
-    const int Lm[3] = {max(L[0], La[0]), max(L[1], La[1]), max(L[2], La[2])};
-    const double OFF = corner_norm(G, Lm[0], Lm[1], Lm[2]);
-    const double u = 0x1.0p-24;
-    const double E = u * (5.0 * Q + 3.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
-    const double delta = 1.25 * (1.7320508075688772 * E + 2.5 * u * (S.cut + 1.0)) + 1e-9;
-    Guard g;
-    g.delta = delta;
-    const double cp = S.cut + delta, cm = S.cut - delta;
-    g.cutp2 = __double2float_ru(cp * cp);
-    g.cutm2 = cm > 0.0 ? __double2float_rd(cm * cm) : 0.0f;
-    g.two_delta = __double2float_ru(2.0 * delta);
-    g.inv_bs = (float)(1.0 / S.binstep);
-    // |k - d/binstep| <= delta/binstep + (rounding of d * inv_bs and of inv_bs)
-    g.bin_band = __double2float_ru(delta / S.binstep + (double)(S.nbins + 1) * 4.0 * u + 1e-6);
-    g.dbulk_lo = __double2float_rd(S.dbulk - delta);
-    g.dbulk_hi = __double2float_ru(S.dbulk + delta);
-    g.cut_pre = __double2float_ru(S.cut + 1e-3 * (1.0 + range));
-    F.g = g;
-}
-
 // ------------------------------------------------------------------- kernels
-// Per-frame offset table: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
-__global__ void k_offtable(const FrameGeom *__restrict__ Gp, d4 *__restrict__ off64, float4 *__restrict__ off32) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Frames are processed in chunks.  Every per-frame buffer holds the chunk's
+// frames at a fixed stride, and each kernel finds the frame of its work item
+// (grid y, or the item's own frame tag), so one launch per stage serves all
+// frames of the chunk.
+struct Bufs {
+    int nf;                         // frames in the chunk
+    int ndist;                      // rows per frame of flags / bulk
+    int64_t ms, Ns, mv, Nv;
+    const FrameGeom *G;             // [nf]
+    FrameScratch *FS;               // [nf]
+    d4 *off64;                      // [nf][kOffEntries]
+    float4 *off32;
+    // PAIRS molecules; in self mode the solvent pointers alias the solute ones
+    int *scell;                     // [nf][ms]
+    float4 *sq32;
+    d4 *sq64;
+    float4 *so32;                   // [nf][Ns]
+    d4 *so64;
+    int *vcell;                     // [nf][mv]
+    float4 *vq32;
+    d4 *vq64;
+    float4 *vo32;                   // [nf][Nv]
+    d4 *vo64;
+    int *ccount, *cstart, *cfill;   // [nf][cs]
+    int64_t cs;
+    int *cmol;                      // [nf][mv]
+    // random insertion
+    int *slot;                      // [nf][ms], -1 where not sampled
+    unsigned char *flags;           // [nf][ndist][mv]
+    int *bulk;                      // [nf][ndist][mv]
+    int *nbulk;                     // [nf][ndist]
+    const Sample *samples;          // the chunk's samples; .pad = frame
+    // queues of the chunk
+    int4 *gq;                       // (s, v, packed delta, frame)
+    int gq_cap;
+    int2 *rq;                       // (sample, slot)
+    int rq_cap;
+    int *counters;                  // [0] guard queue, [1] random queue
+    // ATOMS
+    int *akey;                      // [nf][Ns]
+    float4 *atq32, *asq32;
+    d4 *atq64, *asq64;
+    int *acount, *astart, *afill;   // [nf][as]
+    int64_t as;
+    int *avcell;                    // [nf][Nv]
+    float4 *avq32;
+    d4 *avq64;
+    d4 *u64;                        // [nf][Nv]
+    float *rc;                      // [nf][mv]
+    int *pcell;                     // [placed samples][Nv]
+    float4 *pq32;
+    d4 *pq64;
+};
+
+// Per-frame offset tables: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
+__global__ void k_offtable(Bufs B) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y;
     if (i >= kOffEntries) return;
-    int dx = i % kLTW - kLT, dy = (i / kLTW) % kLTW - kLT, dz = i / (kLTW * kLTW) - kLT;
+    const int dx = i % kLTW - kLT, dy = (i / kLTW) % kLTW - kLT, dz = i / (kLTW * kLTW) - kLT;
     double v[3];
-    matvec_cm(Gp->Hn, (double)dx, (double)dy, (double)dz, v);
-    off64[i] = make_d4(v[0], v[1], v[2], 0.0);
-    off32[i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+    matvec_cm(B.G[f].Hn, (double)dx, (double)dy, (double)dz, v);
+    B.off64[(int64_t)f * kOffEntries + i] = make_d4(v[0], v[1], v[2], 0.0);
+    B.off32[(int64_t)f * kOffEntries + i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
 }
 
 template <typename T>
@@ -699,21 +694,28 @@ __device__ __forceinline__ void load_xyz(const T *p, double *x) {
 
 __device__ __forceinline__ void atomic_max_pos(float *addr, float v) { atomicMax((int *)addr, __float_as_int(v)); }
 
-// PAIRS regime prep, one thread per molecule.  The molecule is made whole
-// around its first atom (minimum image of each atom's displacement), its
+// PAIRS prep, one thread per molecule (grid y = frame).  The molecule is made
+// whole around its first atom (minimum image of each atom's displacement), its
 // centroid c = x_0 + mean(d) is binned, and its atoms are stored as FP64 and
 // FP32 offsets from the centroid; the radius is the largest offset (rounded
 // up).  Displacements shorter than 0.45 of the narrowest cell width are their
 // own minimum image, so the FP64 unwrap runs only for longer ones.
 template <typename T>
-__global__ void k_prep_pairs(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int nmol, int apm,
-                             int *__restrict__ mcell, float4 *__restrict__ mq32, d4 *__restrict__ mq64,
-                             float4 *__restrict__ mo32, d4 *__restrict__ mo64, int *__restrict__ cellcount,
-                             float *__restrict__ rmax) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_prep_pairs(Bufs B, const T *__restrict__ xyz, int64_t xyz_stride, int solvent_side, int count_cells) {
+    const int f = blockIdx.y;
+    const int nmol = (int)(solvent_side ? B.mv : B.ms);
+    const int64_t Nmol_atoms = solvent_side ? B.Nv : B.Ns;
+    const int apm = (int)(Nmol_atoms / nmol);
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmol) return;
-    const FrameGeom &G = *Gp;
-    const T *x = xyz + (int64_t)m * apm * 3;
+    const FrameGeom &G = B.G[f];
+    int *mcell = (solvent_side ? B.vcell : B.scell) + (int64_t)f * nmol;
+    float4 *mq32 = (solvent_side ? B.vq32 : B.sq32) + (int64_t)f * nmol;
+    d4 *mq64 = (solvent_side ? B.vq64 : B.sq64) + (int64_t)f * nmol;
+    float4 *mo32 = (solvent_side ? B.vo32 : B.so32) + (int64_t)f * Nmol_atoms;
+    d4 *mo64 = (solvent_side ? B.vo64 : B.so64) + (int64_t)f * Nmol_atoms;
+    FrameScratch &F = B.FS[f];
+    const T *x = xyz + (int64_t)f * xyz_stride + (int64_t)m * apm * 3;
     const int64_t base = (int64_t)m * apm;
     double x0[3];
     load_xyz(x, x0);
@@ -723,7 +725,7 @@ __global__ void k_prep_pairs(const FrameGeom *__restrict__ Gp, const T *__restri
         double xa[3], d[3];
         load_xyz(x + 3 * a, xa);
         for (int k = 0; k < 3; ++k) d[k] = sub(xa[k], x0[k]);
-        float fx = (float)d[0], fy = (float)d[1], fz = (float)d[2];
+        const float fx = (float)d[0], fy = (float)d[1], fz = (float)d[2];
         if (fmaf(fz, fz, fmaf(fy, fy, fx * fx)) > wlim * wlim) unwrap(G, d);
         mo64[base + a] = make_d4(d[0], d[1], d[2], 0.0);
         sx = add(sx, d[0]);
@@ -743,7 +745,7 @@ __global__ void k_prep_pairs(const FrameGeom *__restrict__ Gp, const T *__restri
         w.y = sub(w.y, my);
         w.z = sub(w.z, mz);
         mo64[base + a] = w;
-        float fx = (float)w.x, fy = (float)w.y, fz = (float)w.z;
+        const float fx = (float)w.x, fy = (float)w.y, fz = (float)w.z;
         mo32[base + a] = make_float4(fx, fy, fz, 0.f);
         r = fmaxf(r, norm3f(fx, fy, fz));
     }
@@ -752,20 +754,28 @@ __global__ void k_prep_pairs(const FrameGeom *__restrict__ Gp, const T *__restri
     mcell[m] = cell;
     mq64[m] = make_d4(q[0], q[1], q[2], 0.0);
     mq32[m] = make_float4((float)q[0], (float)q[1], (float)q[2], rf);
-    if (cellcount) atomicAdd(cellcount + cell, 1);
-    atomic_max_pos(rmax, rf);
+    if (count_cells) atomicAdd(B.ccount + (int64_t)f * B.cs + cell, 1);
+    atomic_max_pos(solvent_side ? &F.rmax_v : &F.rmax_s, rf);
 }
 
-// Exclusive scan of n counts into start[0..n] (single CTA of 1024 threads);
-// also copies start into fill for the scatter.
-__global__ void __launch_bounds__(1024) k_scan(const int *__restrict__ count, int n, int *__restrict__ start, int *__restrict__ fill) {
+// Exclusive scans of the chunk's per-frame count arrays (one CTA of 1024
+// threads per frame): start[0..n] and a copy in fill for the scatter.  n is
+// the frame's cell count times `mult` (1: molecule cells, ms: per-molecule
+// atom cells).
+__global__ void __launch_bounds__(1024) k_scan(Bufs B, int atoms_layout) {
     __shared__ int wsum[32];
-    int t = threadIdx.x;
-    int per = (n + 1023) / 1024;
-    int lo = t * per, hi = min(n, lo + per);
+    const int f = blockIdx.x;
+    const int64_t stride = atoms_layout ? B.as : B.cs;
+    const int *count = (atoms_layout ? B.acount : B.ccount) + (int64_t)f * stride;
+    int *start = (atoms_layout ? B.astart : B.cstart) + (int64_t)f * stride;
+    int *fill = (atoms_layout ? B.afill : B.cfill) + (int64_t)f * stride;
+    const int n = B.G[f].ncell * (atoms_layout ? (int)B.ms : 1);
+    const int t = threadIdx.x;
+    const int per = (n + 1023) / 1024;
+    const int lo = t * per, hi = min(n, lo + per);
     int local = 0;
     for (int i = lo; i < hi; ++i) local += count[i];
-    int lane = t & 31, w = t >> 5;
+    const int lane = t & 31, w = t >> 5;
     int v = local;
     for (int o = 1; o < 32; o <<= 1) {
         int y = __shfl_up_sync(0xffffffffu, v, o);
@@ -785,18 +795,20 @@ __global__ void __launch_bounds__(1024) k_scan(const int *__restrict__ count, in
     int excl = v - local + (w > 0 ? wsum[w - 1] : 0);
     for (int i = lo; i < hi; ++i) {
         start[i] = excl;
-        if (fill) fill[i] = excl;
+        fill[i] = excl;
         excl += count[i];
     }
     if (hi == n && lo < hi) start[n] = excl;
     if (n == 0 && t == 0) start[0] = 0;
 }
 
-__global__ void k_scatter_mols(const int *__restrict__ mcell, int nmol, int *__restrict__ fill, int *__restrict__ cmol) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nmol) return;
-    int p = atomicAdd(fill + mcell[m], 1);
-    cmol[p] = m;
+__global__ void k_scatter_mols(Bufs B, int self) {
+    const int f = blockIdx.y;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= B.mv) return;
+    const int *mcell = (self ? B.scell : B.vcell) + (int64_t)f * B.mv;
+    const int p = atomicAdd(B.cfill + (int64_t)f * B.cs + mcell[m], 1);
+    B.cmol[(int64_t)f * B.mv + p] = m;
 }
 
 // Images of a PAIRS candidate from its packed stencil offset.
@@ -815,6 +827,53 @@ __device__ __forceinline__ Images images_of(const FrameGeom &G, const FrameScrat
         }
     }
     return im;
+}
+
+// Pointers of one frame of a PAIRS chunk.
+struct PairsFrame {
+    const FrameGeom *G;
+    FrameScratch *F;
+    const d4 *off64;
+    const float4 *off32;
+    const int *scell;
+    const float4 *sq32;
+    const d4 *sq64;
+    const float4 *so32;
+    const d4 *so64;
+    const float4 *vq32;
+    const d4 *vq64;
+    const float4 *vo32;
+    const d4 *vo64;
+    const int *cstart;
+    const int *cmol;
+    int *slot;
+    unsigned char *flags;
+    int *bulk;
+    int *nbulk;
+};
+
+__device__ __forceinline__ PairsFrame pairs_frame(const Bufs &B, int f, bool self) {
+    PairsFrame P;
+    P.G = B.G + f;
+    P.F = B.FS + f;
+    P.off64 = B.off64 + (int64_t)f * kOffEntries;
+    P.off32 = B.off32 + (int64_t)f * kOffEntries;
+    P.scell = B.scell + (int64_t)f * B.ms;
+    P.sq32 = B.sq32 + (int64_t)f * B.ms;
+    P.sq64 = B.sq64 + (int64_t)f * B.ms;
+    P.so32 = B.so32 + (int64_t)f * B.Ns;
+    P.so64 = B.so64 + (int64_t)f * B.Ns;
+    P.vq32 = (self ? B.sq32 : B.vq32) + (int64_t)f * B.mv;
+    P.vq64 = (self ? B.sq64 : B.vq64) + (int64_t)f * B.mv;
+    P.vo32 = (self ? B.so32 : B.vo32) + (int64_t)f * B.Nv;
+    P.vo64 = (self ? B.so64 : B.vo64) + (int64_t)f * B.Nv;
+    P.cstart = B.cstart + (int64_t)f * B.cs;
+    P.cmol = B.cmol + (int64_t)f * B.mv;
+    P.slot = B.slot ? B.slot + (int64_t)f * B.ms : nullptr;
+    P.flags = B.flags ? B.flags + (int64_t)f * B.ndist * B.mv : nullptr;
+    P.bulk = B.bulk ? B.bulk + (int64_t)f * B.ndist * B.mv : nullptr;
+    P.nbulk = B.nbulk ? B.nbulk + (int64_t)f * B.ndist : nullptr;
+    return P;
 }
 
 // Stencil walk of one solute molecule by one warp: every solvent molecule
@@ -886,31 +945,28 @@ __device__ __forceinline__ void walk_candidates(const FrameGeom &G, const FrameS
     __syncwarp();
 }
 
-// Records of one direction written into the histograms and the bulk flags.
+// Records of both directions written into the histograms and the bulk flags.
 template <bool SELF>
 __device__ __forceinline__ void emit(const DevSys &S, const SHist &h, const DirRec &r1, const DirRec &r2, int s, int v,
-                                     const int *__restrict__ slot_of_mol, unsigned char *__restrict__ flags, LocalStats &st) {
+                                     const int *__restrict__ slot, unsigned char *__restrict__ flags, LocalStats &st) {
     if (r1.within) { apply_hit(S, h, false, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
     if (SELF && r2.within) { apply_hit(S, h, false, r2.bin, r2.i_local, r2.j, r2.ref, r2.rbin); st.hits++; }
-    if (slot_of_mol) {
-        int sl = slot_of_mol[s];
+    if (slot) {
+        const int sl = slot[s];
         if (sl >= 0) flags[(int64_t)sl * S.mv + v] = flag_code(r1);
         if (SELF) {
-            int vs = slot_of_mol[v];
+            const int vs = slot[v];
             if (vs >= 0) flags[(int64_t)vs * S.mv + s] = flag_code(r2);
         }
     }
 }
 
-// PAIRS regime, real pass, generic (any molecule size, FP32 or FP64).
+// PAIRS real pass, generic (any molecule size, FP32 or FP64): one warp per
+// (frame, solute molecule) work item.  With only_multi set it processes only
+// the frames that need several images per molecule pair (the rest were done by
+// the specialised FP32 kernel).
 template <bool FP32, bool SELF>
-__global__ void __launch_bounds__(kWarps * 32)
-    k_pairs_real(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS, const d4 *__restrict__ off64,
-                 const float4 *__restrict__ off32, const int *__restrict__ scell, const float4 *__restrict__ sq32,
-                 const d4 *__restrict__ sq64, const float4 *__restrict__ so32, const d4 *__restrict__ so64,
-                 const float4 *__restrict__ vq32, const d4 *__restrict__ vq64, const float4 *__restrict__ vo32,
-                 const d4 *__restrict__ vo64, const int *__restrict__ cstart, const int *__restrict__ cmol,
-                 const int *__restrict__ slot_of_mol, unsigned char *__restrict__ flags) {
+__global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, int only_multi) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
     const int hw = hist_words(S);
@@ -919,78 +975,77 @@ __global__ void __launch_bounds__(kWarps * 32)
     shist_zero(S, hbase);
     __syncthreads();
     SHist h = shist_bind(S, hbase);
-    const FrameGeom &G = *Gp;
-    const FrameScratch &F = *FS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4 *os = os_all + warp * kMaxSmallMol;
     int *qv = q_all + warp * kQueue * 2;
     int *qi = qv + kQueue;
     LocalStats st;
-    const Guard g = F.g;
-    if (F.ok) {
-        for (int s = blockIdx.x * kWarps + warp; s < S.ms; s += gridDim.x * kWarps) {
-            const float4 qs32 = sq32[s];
-            const d4 qs64 = sq64[s];
-            for (int a = lane; a < S.aps; a += 32) os[a] = so32[(int64_t)s * S.aps + a];
-            __syncwarp();
-            auto process = [&](int v, int code) {
-                const Images im = images_of(G, F, code);
-                const float4 qv32 = vq32[v];
-                const d4 qv64 = vq64[v];
-                const float4 *ov32 = vo32 + (int64_t)v * S.apv;
-                const d4 *ov64 = vo64 + (int64_t)v * S.apv;
-                const d4 *os64 = so64 + (int64_t)s * S.aps;
-                DirRec r1, r2;
-                st.molpairs++;
-                st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
-                if (FP32) {
-                    Pass32 P;
-                    pairs_pass32<SELF>(S, off32, im, qs32, qv32, os, ov32, P);
-                    pairs_decide<SELF>(S, g, P, off64, off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, s, v, r1, r2, st);
-                } else {
-                    Exact64 E;
-                    pairs_exact<false, SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, 0.f, 0.f, 0.f, E);
-                    records_from_exact<SELF>(S, E, s, v, r1, r2);
-                }
-                emit<SELF>(S, h, r1, r2, s, v, slot_of_mol, flags, st);
-            };
-            walk_candidates<SELF>(G, F, s, scell[s], qs32, off32, vq32, cstart, cmol, qv, qi, lane, process);
+    const int64_t items = (int64_t)B.nf * B.ms;
+    for (int64_t t = (int64_t)blockIdx.x * kWarps + warp; t < items; t += (int64_t)gridDim.x * kWarps) {
+        const int f = (int)(t / B.ms), s = (int)(t - (int64_t)f * B.ms);
+        const PairsFrame Pf = pairs_frame(B, f, SELF);
+        const FrameGeom &G = *Pf.G;
+        const FrameScratch &F = *Pf.F;
+        if (only_multi && !F.multi) continue;
+        if (!F.ok) {
+            if (lane == 0) raise_err(S, ERR_STENCIL);
+            continue;
         }
-    } else if (threadIdx.x == 0) {
-        raise_err(S, ERR_STENCIL);
+        const Guard g = F.g;
+        const float4 qs32 = Pf.sq32[s];
+        const d4 qs64 = Pf.sq64[s];
+        __syncwarp();
+        for (int a = lane; a < S.aps; a += 32) os[a] = Pf.so32[(int64_t)s * S.aps + a];
+        __syncwarp();
+        auto process = [&](int v, int code) {
+            const Images im = images_of(G, F, code);
+            const float4 qv32 = Pf.vq32[v];
+            const d4 qv64 = Pf.vq64[v];
+            const float4 *ov32 = Pf.vo32 + (int64_t)v * S.apv;
+            const d4 *ov64 = Pf.vo64 + (int64_t)v * S.apv;
+            const d4 *os64 = Pf.so64 + (int64_t)s * S.aps;
+            DirRec r1, r2;
+            st.molpairs++;
+            st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
+            if (FP32) {
+                Pass32 P;
+                pairs_pass32<SELF>(S, Pf.off32, im, qs32, qv32, os, ov32, P);
+                pairs_decide<SELF>(S, g, P, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, s, v, r1, r2,
+                                   st);
+            } else {
+                Exact64 E;
+                pairs_exact<false, SELF>(S, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, 0.f, 0.f, 0.f,
+                                         E);
+                records_from_exact<SELF>(S, E, s, v, r1, r2);
+            }
+            emit<SELF>(S, h, r1, r2, s, v, Pf.slot, Pf.flags, st);
+        };
+        walk_candidates<SELF>(G, F, s, Pf.scell[s], qs32, Pf.off32, Pf.vq32, Pf.cstart, Pf.cmol, qv, qi, lane, process);
     }
     stats_flush(S, st, false);
     __syncthreads();
     shist_flush(S, h, false);
 }
 
-// Bulk-molecule list of each distinct sampled solute molecule, ascending
-// (src/mddf.jl:406-415); one CTA per sampled molecule.  Clears the molecule's
+// Bulk-molecule list of each distinct sampled solute molecule of each frame,
+// ascending (src/mddf.jl:406-415); one CTA per (frame, sampled molecule) entry
+// of `tab` = (frame, distinct index, solute molecule).  Clears the molecule's
 // entry of the slot table when done (it was set by k_frame_consts).
-__global__ void __launch_bounds__(1024) k_bulk(const DevSys S, const Sample *__restrict__ samples, int nsamples,
-                                              const unsigned char *__restrict__ flags, int *__restrict__ bulk,
-                                              int *__restrict__ nbulk, int *__restrict__ slot_of_mol) {
+__global__ void __launch_bounds__(1024) k_bulk(const DevSys S, Bufs B, const int4 *__restrict__ tab) {
     __shared__ int wsum[32];
     __shared__ int carry;
-    __shared__ int s_sh;
-    const int d = blockIdx.x;
-    if (threadIdx.x == 0) {
-        carry = 0;
-        s_sh = -1;
-    }
+    const int4 e = tab[blockIdx.x];
+    const int f = e.x, d = e.y, s = e.z;
+    if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < nsamples; i += blockDim.x)
-        if (samples[i].d == d && samples[i].rep == 0) s_sh = samples[i].s;
-    __syncthreads();
-    const int s = s_sh;
-    const unsigned char *f = flags + (int64_t)d * S.mv;
-    int *out = bulk + (int64_t)d * S.mv;
+    const unsigned char *fl = B.flags + ((int64_t)f * B.ndist + d) * B.mv;
+    int *out = B.bulk + ((int64_t)f * B.ndist + d) * B.mv;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int base = 0; base < S.mv; base += blockDim.x) {
+    for (int base = 0; base < B.mv; base += blockDim.x) {
         const int v = base + threadIdx.x;
         int keep = 0;
-        if (v < S.mv && !(S.self && v == s)) {
-            const unsigned char c = f[v];
+        if (v < B.mv && !(S.self && v == s)) {
+            const unsigned char c = fl[v];
             keep = S.usecutoff ? (c == 2) : (c == 0);
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -1012,8 +1067,8 @@ __global__ void __launch_bounds__(1024) k_bulk(const DevSys S, const Sample *__r
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        nbulk[d] = carry;
-        if (s >= 0) slot_of_mol[s] = -1;
+        B.nbulk[(int64_t)f * B.ndist + d] = carry;
+        B.slot[(int64_t)f * B.ms + s] = -1;
     }
 }
 
@@ -1029,7 +1084,7 @@ __device__ __forceinline__ Placement draw_placement(const DevSys &S, int64_t fra
     Placement P;
     uint64_t st = cmfeed::key(S.seed, cmfeed::kTagSlot, (uint64_t)frame_id, (uint64_t)sm.s,
                               ((uint64_t)(uint32_t)sm.rep << 32) | (uint64_t)(uint32_t)k);
-    int nb = nbulk[sm.d];
+    const int nb = nbulk[sm.d];
     if (nb > 0) P.jmol = bulk[(int64_t)sm.d * S.mv + (int64_t)cmfeed::below(st, (uint64_t)nb)];
     else P.jmol = (int)cmfeed::below(st, (uint64_t)S.mv);
     for (int q = 0; q < 3; ++q) P.fc[q] = cmfeed::uniform(st);
@@ -1060,39 +1115,37 @@ __device__ __forceinline__ Images placed_images(const FrameGeom &G, const FrameS
     return im;
 }
 
-// PAIRS random pass, stage 1: one thread per (sample, slot).  Draws the bulk
-// molecule and the new centre (src/mddf.jl:65-88, src/rigid_body.jl:115-120)
-// and keeps the slot if the placed molecule's bounding sphere reaches the
-// sampled solute molecule's.  Nothing outside the kept slots is evaluated:
-// their molecules cannot come within the cutoff.
-__global__ void __launch_bounds__(128)
-    k_random_filter(DevSys S, const FrameGeom *__restrict__ Gp, FrameScratch *__restrict__ FS,
-                    const float4 *__restrict__ off32, const Sample *__restrict__ samples, int sample0, int nsamp,
-                    const int *__restrict__ scell, const float4 *__restrict__ sq32, const float4 *__restrict__ vq32,
-                    const int *__restrict__ bulk, const int *__restrict__ nbulk, int2 *__restrict__ rq, int rq_cap) {
-    const FrameGeom &G = *Gp;
-    const FrameScratch &F = *FS;
+// PAIRS random pass, stage 1: one thread per (sample, slot) of the chunk.
+// Draws the bulk molecule and the new centre (src/mddf.jl:65-88,
+// src/rigid_body.jl:115-120) and keeps the slot if the placed molecule's
+// bounding sphere reaches the sampled solute molecule's.  The other slots
+// cannot come within the cutoff and need no further work.
+__global__ void __launch_bounds__(128) k_random_filter(DevSys S, Bufs B, int sample0, int nsamp) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (!F.ok || t >= (int64_t)nsamp * S.mv) return;
-    const int i = sample0 + (int)(t / S.mv), k = (int)(t % S.mv);
-    const Sample sm = samples[i];
-    const int s = sm.s;
+    if (t >= (int64_t)nsamp * B.mv) return;
+    const int i = sample0 + (int)(t / B.mv), k = (int)(t % B.mv);
+    const Sample sm = B.samples[i];
+    const int s = sm.s, f = sm.pad;
     if (S.self && k == s) return;
-    const Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
+    const PairsFrame Pf = pairs_frame(B, f, S.self);
+    const FrameGeom &G = *Pf.G;
+    const FrameScratch &F = *Pf.F;
+    if (!F.ok) return;
+    const Placement P = draw_placement(S, G.frame_id, sm, k, Pf.bulk, Pf.nbulk);
     double qp[3];
-    const Images im = placed_images(G, F, scell[s], P.fc, qp);
-    const float4 qs = sq32[s];
-    const float rr = F.g.cut_pre + qs.w + vq32[P.jmol].w;
+    const Images im = placed_images(G, F, Pf.scell[s], P.fc, qp);
+    const float4 qs = Pf.sq32[s];
+    const float rr = F.g.cut_pre + qs.w + Pf.vq32[P.jmol].w;
     const float px = (float)qp[0] - qs.x, py = (float)qp[1] - qs.y, pz = (float)qp[2] - qs.z;
     bool any = false;
     CM_FOR_IMAGES(im, ix, iy, iz) {
-        const float4 o = off32[off_index(ix, iy, iz)];
+        const float4 o = Pf.off32[off_index(ix, iy, iz)];
         const float Dx = px + o.x, Dy = py + o.y, Dz = pz + o.z;
         any |= fmaf(Dz, Dz, fmaf(Dy, Dy, Dx * Dx)) <= rr * rr;
     }
     if (!any) return;
-    const int slot = atomicAdd(&FS->rq_count, 1);
-    if (slot < rq_cap) rq[slot] = make_int2(i, k);
+    const int slotq = atomicAdd(B.counters + 1, 1);
+    if (slotq < B.rq_cap) B.rq[slotq] = make_int2(i, k);
     else raise_err(S, ERR_QUEUE);
 }
 
@@ -1100,34 +1153,30 @@ __global__ void __launch_bounds__(128)
 // molecule about its centroid (src/rigid_body.jl:73-80, 122-134) and evaluates
 // it against the sampled solute molecule (one direction).
 template <bool FP32>
-__global__ void __launch_bounds__(128)
-    k_random_eval(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS,
-                  const d4 *__restrict__ off64, const float4 *__restrict__ off32, const Sample *__restrict__ samples,
-                  const int *__restrict__ scell, const float4 *__restrict__ sq32, const d4 *__restrict__ sq64,
-                  const float4 *__restrict__ so32, const d4 *__restrict__ so64, const d4 *__restrict__ vo64,
-                  const int *__restrict__ bulk, const int *__restrict__ nbulk, const int2 *__restrict__ rq, int rq_cap) {
+__global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);
     __syncthreads();
     SHist h = shist_bind(S, hbase);
-    const FrameGeom &G = *Gp;
-    const FrameScratch &F = *FS;
     LocalStats st;
-    const Guard g = F.g;
-    const int n = min(F.rq_count, rq_cap);
+    const int n = min(B.counters[1], B.rq_cap);
     for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
-        const int2 e = rq[it];
-        const Sample sm = samples[e.x];
-        const int s = sm.s, k = e.y;
-        Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
+        const int2 e = B.rq[it];
+        const Sample sm = B.samples[e.x];
+        const int s = sm.s, k = e.y, f = sm.pad;
+        const PairsFrame Pf = pairs_frame(B, f, S.self);
+        const FrameGeom &G = *Pf.G;
+        const FrameScratch &F = *Pf.F;
+        const Guard g = F.g;
+        Placement P = draw_placement(S, G.frame_id, sm, k, Pf.bulk, Pf.nbulk);
         double qp[3];
-        const Images im = placed_images(G, F, scell[s], P.fc, qp);
+        const Images im = placed_images(G, F, Pf.scell[s], P.fc, qp);
         double A[9];
         draw_rotation(P.st, A);
         d4 ov64[kMaxSmallMol];
         float4 ov32[kMaxSmallMol];
-        const d4 *o = vo64 + (int64_t)P.jmol * S.apv;
+        const d4 *o = Pf.vo64 + (int64_t)P.jmol * S.apv;
         for (int b = 0; b < S.apv; ++b) {
             const d4 w = o[b];
             double r[3];
@@ -1135,22 +1184,24 @@ __global__ void __launch_bounds__(128)
             ov64[b] = make_d4(r[0], r[1], r[2], 0.0);
             ov32[b] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
         }
-        const float4 qs32 = sq32[s];
-        const d4 qs64 = sq64[s];
+        const float4 qs32 = Pf.sq32[s];
+        const d4 qs64 = Pf.sq64[s];
         const float4 qp32 = make_float4((float)qp[0], (float)qp[1], (float)qp[2], 0.f);
         const d4 qp64 = make_d4(qp[0], qp[1], qp[2], 0.0);
-        const float4 *os32 = so32 + (int64_t)s * S.aps;
-        const d4 *os64 = so64 + (int64_t)s * S.aps;
+        const float4 *os32 = Pf.so32 + (int64_t)s * S.aps;
+        const d4 *os64 = Pf.so64 + (int64_t)s * S.aps;
         DirRec r1, r2;
         st.molpairs++;
         st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
         if (FP32) {
             Pass32 Q;
-            pairs_pass32<false>(S, off32, im, qs32, qp32, os32, ov32, Q);
-            pairs_decide<false>(S, g, Q, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, s, k, r1, r2, st);
+            pairs_pass32<false>(S, Pf.off32, im, qs32, qp32, os32, ov32, Q);
+            pairs_decide<false>(S, g, Q, Pf.off64, Pf.off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, s, k, r1, r2,
+                                st);
         } else {
             Exact64 E;
-            pairs_exact<false, false>(S, off64, off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, 0.f, 0.f, 0.f, E);
+            pairs_exact<false, false>(S, Pf.off64, Pf.off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, 0.f, 0.f, 0.f,
+                                      E);
             records_from_exact<false>(S, E, s, k, r1, r2);
         }
         if (r1.within) { apply_hit(S, h, true, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
@@ -1158,6 +1209,92 @@ __global__ void __launch_bounds__(128)
     stats_flush(S, st, true);
     __syncthreads();
     shist_flush(S, h, true);
+}
+
+// One block per frame computes the frame constants: stencils, the FP32 guard
+// band, and the slot table of the frame's sampled solute molecules.
+//
+// Guard band.  In the FP32 displacement of an atom pair,
+//   dx = ((q_v - q_s) + off) + o_b) - o_a,
+// every input is the rounding of an FP64 value and every operation rounds, so
+// with u = 2^-24 each component is within u times the sum of the magnitudes of
+// the inputs and intermediate results of its exact value:
+//   |q| <= Q (a site inside its cell), |off| <= OFF (stencil offsets),
+//   |o| <= r (molecule radii), |q_v - q_s| <= Q, |D| <= Q + OFF,
+//   |t| <= Q + OFF + r_v, |dx| <= cutoff,
+// giving E = u (5Q + 3 OFF + 2 r_v + r_s + cutoff).  The distance is within
+// sqrt(3) E plus 2.5 u d (three roundings of d^2, one of the square root).  The
+// atom-cell layout's displacement (q_a - (q_b - off)) is bounded by the same
+// expression with r = 0.  delta adds 25 % to the bound.
+__global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
+    const int f = blockIdx.x;
+    const FrameGeom &G = B.G[f];
+    FrameScratch &F = B.FS[f];
+    if (B.slot)
+        for (int i = threadIdx.x; i < G.nsamples; i += blockDim.x) {
+            const Sample sm = B.samples[G.sample_off + i];
+            B.slot[(int64_t)f * B.ms + sm.s] = sm.d;
+        }
+    // the two corner norms in parallel: lanes 0-7 and 8-15
+    const int lane = threadIdx.x;
+    __shared__ double cn[16];
+    __shared__ int Ls[6];
+    __shared__ double radii[2];
+    if (lane == 0) {
+        double rs = F.rmax_s, rv = S.self ? F.rmax_s : F.rmax_v;
+        if (!pairs) rs = rv = 0.0;
+        radii[0] = rs;
+        radii[1] = rv;
+        const double range = S.cut + rs + rv;
+        int L[3], La[3];
+        bool ok = true;
+        if (pairs) ok = stencil(G, range + 1e-6 * (1.0 + range), L) && ok;
+        else L[0] = L[1] = L[2] = 1;
+        ok = stencil(G, S.cut * (1.0 + 1e-7) + 1e-7, La) && ok;
+        int multi = 0;
+        for (int k = 0; k < 3; ++k) {
+            F.L[k] = L[k];
+            F.La[k] = La[k];
+            Ls[k] = max(L[k], La[k]);
+            if (2 * L[k] + 1 > G.n[k]) multi |= 1 << k;
+        }
+        F.multi = multi;
+        F.ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (lane < 16) {
+        const int m = lane & 7;
+        const double l0 = lane < 8 ? 1.0 : (double)Ls[0], l1 = lane < 8 ? 1.0 : (double)Ls[1],
+                     l2 = lane < 8 ? 1.0 : (double)Ls[2];
+        double v[3];
+        matvec_cm(G.Hn, (m & 1) ? -l0 : l0, (m & 2) ? -l1 : l1, (m & 4) ? -l2 : l2, v);
+        cn[lane] = norm3d(v[0], v[1], v[2]);
+    }
+    __syncthreads();
+    if (lane != 0) return;
+    double Q = 0.0, OFF = 0.0;
+    for (int k = 0; k < 8; ++k) {
+        Q = fmax(Q, cn[k]);
+        OFF = fmax(OFF, cn[8 + k]);
+    }
+    const double rs = radii[0], rv = radii[1];
+    const double range = S.cut + rs + rv;
+    const double u = 0x1.0p-24;
+    const double E = u * (5.0 * Q + 3.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
+    const double delta = 1.25 * (1.7320508075688772 * E + 2.5 * u * (S.cut + 1.0)) + 1e-9;
+    Guard g;
+    g.delta = delta;
+    const double cp = S.cut + delta, cm = S.cut - delta;
+    g.cutp2 = __double2float_ru(cp * cp);
+    g.cutm2 = cm > 0.0 ? __double2float_rd(cm * cm) : 0.0f;
+    g.two_delta = __double2float_ru(2.0 * delta);
+    g.inv_bs = (float)(1.0 / S.binstep);
+    // |k - d/binstep| <= delta/binstep + (rounding of d * inv_bs and of inv_bs)
+    g.bin_band = __double2float_ru(delta / S.binstep + (double)(S.nbins + 1) * 4.0 * u + 1e-6);
+    g.dbulk_lo = __double2float_rd(S.dbulk - delta);
+    g.dbulk_hi = __double2float_ru(S.dbulk + delta);
+    g.cut_pre = __double2float_ru(S.cut + 1e-3 * (1.0 + range));
+    F.g = g;
 }
 
 // Molecule-centred data for random insertion (src/rigid_body.jl:127-134):
@@ -1198,96 +1335,101 @@ __device__ void centroid_data(const FrameGeom &G, const T *x, int apm, int iref,
 // ----------------------------------------------------------- ATOMS regime
 __device__ __forceinline__ int pack_cell(const int *c) { return c[0] | (c[1] << 10) | (c[2] << 20); }
 
-// Solvent atoms binned individually (real frame).
+// Solvent atoms binned individually (grid y = frame); molecule-centred data
+// for random insertion.
 template <typename T>
-__global__ void k_prep_atoms_solvent(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int nmol, int apm, int iref,
-                                     int *__restrict__ acell, float4 *__restrict__ aq32, d4 *__restrict__ aq64,
-                                     d4 *__restrict__ u64, float *__restrict__ rc, float *__restrict__ rcmax) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nmol) return;
-    const FrameGeom &G = *Gp;
-    const T *x = xyz + (int64_t)m * apm * 3;
+__global__ void k_prep_atoms_solvent(Bufs B, const T *__restrict__ xyz, int64_t xyz_stride, int iref, int centroids) {
+    const int f = blockIdx.y;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= B.mv) return;
+    const int apm = (int)(B.Nv / B.mv);
+    const FrameGeom &G = B.G[f];
+    const T *x = xyz + (int64_t)f * xyz_stride + (int64_t)m * apm * 3;
+    const int64_t fo = (int64_t)f * B.Nv;
     for (int b = 0; b < apm; ++b) {
         double xb[3];
         load_xyz(x + 3 * b, xb);
         int c[3];
         double q[3];
         bin_position(G, xb[0], xb[1], xb[2], c, q);
-        int64_t i = (int64_t)m * apm + b;
-        acell[i] = pack_cell(c);
-        aq32[i] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
-        aq64[i] = make_d4(q[0], q[1], q[2], 0.0);
+        const int64_t i = fo + (int64_t)m * apm + b;
+        B.avcell[i] = pack_cell(c);
+        B.avq32[i] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
+        B.avq64[i] = make_d4(q[0], q[1], q[2], 0.0);
     }
-    if (u64) {
+    if (centroids) {
         float r;
-        centroid_data(G, x, apm, iref, u64 + (int64_t)m * apm, r);
-        rc[m] = r;
-        atomic_max_pos(rcmax, r);
+        centroid_data(G, x, apm, iref, B.u64 + fo + (int64_t)m * apm, r);
+        B.rc[(int64_t)f * B.mv + m] = r;
+        atomic_max_pos(&B.FS[f].rcmax, r);
     }
 }
 
 // Solute atoms binned into per-molecule cell lists: key = s * ncell + cell.
 template <typename T>
-__global__ void k_prep_atoms_solute(const FrameGeom *__restrict__ Gp, const T *__restrict__ xyz, int natoms, int aps,
-                                    int *__restrict__ key, float4 *__restrict__ tq32, d4 *__restrict__ tq64,
-                                    int *__restrict__ count) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= natoms) return;
-    const FrameGeom &G = *Gp;
+__global__ void k_prep_atoms_solute(Bufs B, const T *__restrict__ xyz, int64_t xyz_stride) {
+    const int f = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.Ns) return;
+    const int aps = (int)(B.Ns / B.ms);
+    const FrameGeom &G = B.G[f];
     double x[3];
-    load_xyz(xyz + 3 * (int64_t)i, x);
+    load_xyz(xyz + (int64_t)f * xyz_stride + 3 * (int64_t)i, x);
     int c[3];
     double q[3];
     bin_position(G, x[0], x[1], x[2], c, q);
-    int s = i / aps, a = i - s * aps;
-    int k = s * G.ncell + cell_linear(G, c[0], c[1], c[2]);
-    key[i] = k;
-    tq32[i] = make_float4((float)q[0], (float)q[1], (float)q[2], __int_as_float(a));
-    tq64[i] = make_d4(q[0], q[1], q[2], 0.0);
-    atomicAdd(count + k, 1);
+    const int s = i / aps, a = i - s * aps;
+    const int k = s * G.ncell + cell_linear(G, c[0], c[1], c[2]);
+    const int64_t fi = (int64_t)f * B.Ns + i;
+    B.akey[fi] = k;
+    B.atq32[fi] = make_float4((float)q[0], (float)q[1], (float)q[2], __int_as_float(a));
+    B.atq64[fi] = make_d4(q[0], q[1], q[2], 0.0);
+    atomicAdd(B.acount + (int64_t)f * B.as + k, 1);
 }
 
-__global__ void k_scatter_atoms(const int *__restrict__ key, int natoms, const float4 *__restrict__ tq32,
-                                const d4 *__restrict__ tq64, int *__restrict__ fill, float4 *__restrict__ sq32,
-                                d4 *__restrict__ sq64) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= natoms) return;
-    int p = atomicAdd(fill + key[i], 1);
-    sq32[p] = tq32[i];
-    sq64[p] = tq64[i];
+__global__ void k_scatter_atoms(Bufs B) {
+    const int f = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.Ns) return;
+    const int64_t fi = (int64_t)f * B.Ns + i;
+    const int p = atomicAdd(B.afill + (int64_t)f * B.as + B.akey[fi], 1);
+    B.asq32[(int64_t)f * B.Ns + p] = B.atq32[fi];
+    B.asq64[(int64_t)f * B.Ns + p] = B.atq64[fi];
 }
 
-// Placed solvent for the ATOMS regime: every slot of every sample in the
-// chunk, absolute FP64 positions A u + centre, then binned per atom.
-__global__ void k_atoms_place(DevSys S, const FrameGeom *__restrict__ Gp, const Sample *__restrict__ samples, int sample0,
-                              const d4 *__restrict__ u64, const int *__restrict__ bulk, const int *__restrict__ nbulk,
-                              int *__restrict__ pcell, float4 *__restrict__ pq32, d4 *__restrict__ pq64) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+// Placed solvent for the ATOMS regime: every slot of samples sample0 ..
+// sample0 + gridDim.y - 1 of the chunk, absolute FP64 positions A u + centre,
+// binned per atom.
+__global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= S.mv) return;
-    const FrameGeom &G = *Gp;
-    const Sample sm = samples[sample0 + blockIdx.y];
-    int64_t base = (int64_t)blockIdx.y * S.mv * S.apv + (int64_t)k * S.apv;
+    const Sample sm = B.samples[sample0 + blockIdx.y];
+    const int f = sm.pad;
+    const FrameGeom &G = B.G[f];
+    const int64_t base = (int64_t)blockIdx.y * B.Nv + (int64_t)k * S.apv;
     if (S.self && k == sm.s) {
-        for (int b = 0; b < S.apv; ++b) pcell[base + b] = -1;
+        for (int b = 0; b < S.apv; ++b) B.pcell[base + b] = -1;
         return;
     }
-    Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
+    const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
+                                       B.nbulk + (int64_t)f * B.ndist);
+    uint64_t rs = P.st;
     double A[9];
-    draw_rotation(P.st, A);
+    draw_rotation(rs, A);
     double cm[3];
     matvec_cm(G.H, P.fc[0], P.fc[1], P.fc[2], cm);
-    const d4 *u = u64 + (int64_t)P.jmol * S.apv;
+    const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
     for (int b = 0; b < S.apv; ++b) {
-        d4 w = u[b];
+        const d4 w = u[b];
         double o[3];
         matvec_rm(A, w.x, w.y, w.z, o);
-        double y0 = add(o[0], cm[0]), y1 = add(o[1], cm[1]), y2 = add(o[2], cm[2]);
+        const double y0 = add(o[0], cm[0]), y1 = add(o[1], cm[1]), y2 = add(o[2], cm[2]);
         int c[3];
         double q[3];
         bin_position(G, y0, y1, y2, c, q);
-        pcell[base + b] = pack_cell(c);
-        pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
-        pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
+        B.pcell[base + b] = pack_cell(c);
+        B.pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
+        B.pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
     }
 }
 
@@ -1298,95 +1440,104 @@ struct AtomPass {
     float r1;     // row minimum of the reference atom
 };
 
-// ATOMS regime evaluation: thread per solvent molecule v; grid.y = solute
-// molecule (real pass) or sample of the chunk (random pass).
+// ATOMS evaluation: thread per solvent molecule v.  Real pass: grid y =
+// frame * ms + solute molecule.  Random pass: grid y = placed sample (of
+// samples sample0 ..), solvent sites from the placed buffers.
 template <bool FP32, bool RANDOM>
-__global__ void __launch_bounds__(128)
-    k_atoms_eval(DevSys S, const FrameGeom *__restrict__ Gp, const FrameScratch *__restrict__ FS, const d4 *__restrict__ off64,
-                 const float4 *__restrict__ off32,
-                 const int *__restrict__ sstart, const float4 *__restrict__ sq32, const d4 *__restrict__ sq64,
-                 const int *__restrict__ vcell, const float4 *__restrict__ vq32, const d4 *__restrict__ vq64,
-                 const Sample *__restrict__ samples, int sample0, const int *__restrict__ slot_of_mol,
-                 unsigned char *__restrict__ flags) {
+__global__ void __launch_bounds__(128) k_atoms_eval(DevSys S, Bufs B, int sample0) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);
     __syncthreads();
     SHist h = shist_bind(S, hbase);
-    const FrameGeom &G = *Gp;
     LocalStats st;
-    int s;
-    int64_t vbase = 0;
+    int s, f;
+    const int *vcell;
+    const float4 *vq32;
+    const d4 *vq64;
     if (RANDOM) {
-        s = samples[sample0 + blockIdx.y].s;
-        vbase = (int64_t)blockIdx.y * S.mv * S.apv;
+        const Sample sm = B.samples[sample0 + blockIdx.y];
+        s = sm.s;
+        f = sm.pad;
+        vcell = B.pcell + (int64_t)blockIdx.y * B.Nv;
+        vq32 = B.pq32 + (int64_t)blockIdx.y * B.Nv;
+        vq64 = B.pq64 + (int64_t)blockIdx.y * B.Nv;
     } else {
-        s = blockIdx.y;
+        f = (int)(blockIdx.y / B.ms);
+        s = (int)(blockIdx.y - (int64_t)f * B.ms);
+        vcell = B.avcell + (int64_t)f * B.Nv;
+        vq32 = B.avq32 + (int64_t)f * B.Nv;
+        vq64 = B.avq64 + (int64_t)f * B.Nv;
     }
-    const FrameScratch &F = *FS;
+    const FrameGeom &G = B.G[f];
+    const FrameScratch &F = B.FS[f];
+    const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
+    const float4 *off32 = B.off32 + (int64_t)f * kOffEntries;
+    const float4 *sq32 = B.asq32 + (int64_t)f * B.Ns;
+    const d4 *sq64 = B.asq64 + (int64_t)f * B.Ns;
     const int L[3] = {F.La[0], F.La[1], F.La[2]};
     const bool ok = F.ok;
     const Guard g = F.g;
     const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    const int *cs = sstart + (int64_t)s * G.ncell;
+    const int *cs = B.astart + (int64_t)f * B.as + (int64_t)s * G.ncell;
     if (!ok) {
         if (threadIdx.x == 0) raise_err(S, ERR_STENCIL);
     } else if (v < S.mv && !(S.self && v == s)) {
         const int apv = S.apv, iref = S.iref;
         DirRec r = dir_none(S);
         auto cells_of = [&](int b, int &cx, int &cy, int &cz) {
-            int c = vcell[vbase + (int64_t)v * apv + b];
+            const int c = vcell[(int64_t)v * apv + b];
             cx = c & 1023; cy = (c >> 10) & 1023; cz = (c >> 20) & 1023;
         };
-        // exact (FP64) scan; with FILTER only pairs whose FP32 squared distance
-        // is within the thresholds are evaluated in FP64
-        auto exact = [&](bool filter, float thr_arg, float thr_r1, Best64 &B, double &rr1, long long &evals) {
-            best_init(B);
+        // exact (FP64) scan; with `filter` only pairs whose FP32 squared
+        // distance is within the thresholds are evaluated in FP64
+        auto exact = [&](bool filter, float thr_arg, float thr_r1, Best64 &Bst, double &rr1, long long &evals) {
+            best_init(Bst);
             rr1 = INFINITY;
             evals = 0;
             for (int b = 0; b < apv; ++b) {
                 int cx, cy, cz;
                 cells_of(b, cx, cy, cz);
-                const d4 qb = vq64[vbase + (int64_t)v * apv + b];
-                const float4 qf = vq32[vbase + (int64_t)v * apv + b];
+                const d4 qb = vq64[(int64_t)v * apv + b];
+                const float4 qf = vq32[(int64_t)v * apv + b];
                 for (int dz = -L[2]; dz <= L[2]; ++dz)
                     for (int dy = -L[1]; dy <= L[1]; ++dy)
                         for (int dx = -L[0]; dx <= L[0]; ++dx) {
-                            int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
-                            int beg = cs[cell], end = cs[cell + 1];
+                            const int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                            const int beg = cs[cell], end = cs[cell + 1];
                             if (beg == end) continue;
-                            int oi = off_index(dx, dy, dz);
-                            d4 o = off64[oi];
-                            double tx = sub(qb.x, o.x), ty = sub(qb.y, o.y), tz = sub(qb.z, o.z);
-                            float4 of = off32[oi];
-                            float fx = qf.x - of.x, fy = qf.y - of.y, fz = qf.z - of.z;
+                            const int oi = off_index(dx, dy, dz);
+                            const d4 o = off64[oi];
+                            const double tx = sub(qb.x, o.x), ty = sub(qb.y, o.y), tz = sub(qb.z, o.z);
+                            const float4 of = off32[oi];
+                            const float fx = qf.x - of.x, fy = qf.y - of.y, fz = qf.z - of.z;
                             for (int p = beg; p < end; ++p) {
-                                float4 qa32 = sq32[p];
+                                const float4 qa32 = sq32[p];
                                 if (filter) {
-                                    float ex = qa32.x - fx, ey = qa32.y - fy, ez = qa32.z - fz;
-                                    float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                                    const float ex = qa32.x - fx, ey = qa32.y - fy, ez = qa32.z - fz;
+                                    const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
                                     if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1))) continue;
                                 }
-                                d4 qa = sq64[p];
+                                const d4 qa = sq64[p];
                                 // displacement solute atom -> solvent atom: (q_b - off) - q_a
-                                double d2 = pair_d2_64(tx, ty, tz, qa.x, qa.y, qa.z);
+                                const double d2 = pair_d2_64(tx, ty, tz, qa.x, qa.y, qa.z);
                                 evals++;
                                 if (d2 <= S.cut2) {
                                     if (b == iref) rr1 = fmin(rr1, d2);
-                                    best_update<false>(B, d2, __float_as_int(qa32.w), b);
+                                    best_update<false>(Bst, d2, __float_as_int(qa32.w), b);
                                 }
                             }
                         }
             }
         };
-        auto from_exact = [&](Best64 &B, double rr1) {
+        auto from_exact = [&](Best64 &Bst, double rr1) {
             DirRec q = dir_none(S);
-            if (B.d2 <= S.cut2) {
-                double d = best_d(B);
+            if (Bst.d2 <= S.cut2) {
+                const double d = best_d(Bst);
                 q.within = 1;
-                q.i_local = B.a;
-                q.j = (int64_t)v * apv + B.b;
+                q.i_local = Bst.a;
+                q.j = (int64_t)v * apv + Bst.b;
                 q.bin = setbin0(d, S.binstep);
                 q.bulk = inbulk64(S, true, d);
                 if (rr1 <= S.cut2) { q.ref = 1; q.rbin = setbin0(sqrt(rr1), S.binstep); }
@@ -1394,12 +1545,12 @@ __global__ void __launch_bounds__(128)
             return q;
         };
         if (!FP32) {
-            Best64 B;
+            Best64 Bst;
             double rr1;
             long long ev;
-            exact(false, 0.f, 0.f, B, rr1, ev);
+            exact(false, 0.f, 0.f, Bst, rr1, ev);
             st.atompairs += ev;
-            r = from_exact(B, rr1);
+            r = from_exact(Bst, rr1);
         } else {
             AtomPass P;
             P.m1 = P.m2 = P.r1 = INFINITY;
@@ -1409,24 +1560,24 @@ __global__ void __launch_bounds__(128)
             for (int b = 0; b < apv; ++b) {
                 int cx, cy, cz;
                 cells_of(b, cx, cy, cz);
-                const float4 qf = vq32[vbase + (int64_t)v * apv + b];
+                const float4 qf = vq32[(int64_t)v * apv + b];
                 const bool isref = b == iref;
                 for (int dz = -L[2]; dz <= L[2]; ++dz)
                     for (int dy = -L[1]; dy <= L[1]; ++dy)
                         for (int dx = -L[0]; dx <= L[0]; ++dx) {
-                            int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
-                            int beg = cs[cell], end = cs[cell + 1];
+                            const int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                            const int beg = cs[cell], end = cs[cell + 1];
                             if (beg == end) continue;
-                            float4 of = off32[off_index(dx, dy, dz)];
-                            float tx = qf.x - of.x, ty = qf.y - of.y, tz = qf.z - of.z;
+                            const float4 of = off32[off_index(dx, dy, dz)];
+                            const float tx = qf.x - of.x, ty = qf.y - of.y, tz = qf.z - of.z;
                             evals += end - beg;
                             float row = P.r1;
                             for (int p = beg; p < end; ++p) {
-                                float4 qa = sq32[p];
-                                float ex = qa.x - tx, ey = qa.y - ty, ez = qa.z - tz;
-                                float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                                const float4 qa = sq32[p];
+                                const float ex = qa.x - tx, ey = qa.y - ty, ez = qa.z - tz;
+                                const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
                                 P.m2 = fminf(P.m2, fmaxf(P.m1, d2));
-                                bool lt = d2 < P.m1;
+                                const bool lt = d2 < P.m1;
                                 P.p1 = lt ? p : P.p1;
                                 P.b1 = lt ? b : P.b1;
                                 P.m1 = fminf(P.m1, d2);
@@ -1437,38 +1588,41 @@ __global__ void __launch_bounds__(128)
             }
             st.atompairs += evals;
             if (P.m1 <= g.cutp2) {
-                float d1 = sqrtf(P.m1);
-                bool amb = P.m1 >= g.cutm2 || (sqrtf(P.m2) - d1) <= g.two_delta;
+                const float d1 = sqrtf(P.m1);
+                const bool amb = P.m1 >= g.cutm2 || (sqrtf(P.m2) - d1) <= g.two_delta;
                 if (amb) {
-                    float t = d1 + g.two_delta;
+                    const float t = d1 + g.two_delta;
                     float thr1 = -1.f;
-                    if (P.r1 <= g.cutp2) { float u = sqrtf(P.r1) + g.two_delta; thr1 = __fmul_ru(u, u); }
-                    Best64 B;
+                    if (P.r1 <= g.cutp2) {
+                        const float u = sqrtf(P.r1) + g.two_delta;
+                        thr1 = __fmul_ru(u, u);
+                    }
+                    Best64 Bst;
                     double rr1;
                     long long ev;
-                    exact(true, __fmul_ru(t, t), thr1, B, rr1, ev);
-                    r = from_exact(B, rr1);
+                    exact(true, __fmul_ru(t, t), thr1, Bst, rr1, ev);
+                    r = from_exact(Bst, rr1);
                     st.guard++;
                     st.guard_pairs += ev;
-                    if (B.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(B)));
+                    if (Bst.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(Bst)));
                 } else {
                     int bin = bin32(g, d1);
                     double d64 = -1.0;
                     const float4 qa32 = sq32[P.p1];
                     if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
-                        // exact distance of the minimum pair: its own image is the
-                        // one of smallest FP64 distance among the stencil cells
+                        // exact distance of the minimum pair over the stencil images
+                        // that contain its solute atom
                         int cx, cy, cz;
                         cells_of(P.b1, cx, cy, cz);
-                        const d4 qb = vq64[vbase + (int64_t)v * apv + P.b1];
+                        const d4 qb = vq64[(int64_t)v * apv + P.b1];
                         const d4 qa = sq64[P.p1];
                         double best = INFINITY;
                         for (int dz = -L[2]; dz <= L[2]; ++dz)
                             for (int dy = -L[1]; dy <= L[1]; ++dy)
                                 for (int dx = -L[0]; dx <= L[0]; ++dx) {
-                                    int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                                    const int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
                                     if (P.p1 < cs[cell] || P.p1 >= cs[cell + 1]) continue;
-                                    d4 o = off64[off_index(dx, dy, dz)];
+                                    const d4 o = off64[off_index(dx, dy, dz)];
                                     best = fmin(best, pair_d2_64(sub(qb.x, o.x), sub(qb.y, o.y), sub(qb.z, o.z), qa.x, qa.y, qa.z));
                                 }
                         d64 = sqrt(best);
@@ -1483,16 +1637,16 @@ __global__ void __launch_bounds__(128)
                     r.bin = bin;
                     r.bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
                     if (P.r1 <= g.cutp2) {
-                        int rb = P.r1 < g.cutm2 ? bin32(g, sqrtf(P.r1)) : -1;
+                        const int rb = P.r1 < g.cutm2 ? bin32(g, sqrtf(P.r1)) : -1;
                         if (rb >= 0) {
                             r.ref = 1;
                             r.rbin = rb;
                         } else {
-                            float u = sqrtf(P.r1) + g.two_delta;
-                            Best64 B;
+                            const float u = sqrtf(P.r1) + g.two_delta;
+                            Best64 Bst;
                             double rr1;
                             long long ev;
-                            exact(true, -1.f, __fmul_ru(u, u), B, rr1, ev);
+                            exact(true, -1.f, __fmul_ru(u, u), Bst, rr1, ev);
                             st.guard++;
                             st.guard_pairs += ev;
                             if (rr1 <= S.cut2) { r.ref = 1; r.rbin = setbin0(sqrt(rr1), S.binstep); }
@@ -1503,9 +1657,9 @@ __global__ void __launch_bounds__(128)
         }
         st.molpairs++;
         if (r.within) { apply_hit(S, h, RANDOM, r.bin, r.i_local, r.j, r.ref, r.rbin); st.hits++; }
-        if (!RANDOM && slot_of_mol) {
-            int sl = slot_of_mol[s];
-            if (sl >= 0) flags[(int64_t)sl * S.mv + v] = flag_code(r);
+        if (!RANDOM && B.slot) {
+            const int sl = B.slot[(int64_t)f * B.ms + s];
+            if (sl >= 0) B.flags[((int64_t)f * B.ndist + sl) * S.mv + v] = flag_code(r);
         }
     }
     stats_flush(S, st, RANDOM);

@@ -63,6 +63,7 @@ struct cm_handle {
     int ndist_max = 0;
     bool mddf = true;
     int device = 0;
+    int sms = 0;
     cudaStream_t stream = nullptr, copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
     std::string err;
@@ -71,24 +72,25 @@ struct cm_handle {
     bool planned = false;
     double pair_cell = 0.0;
     int64_t ncell_cap = 0;
-    int max_frames = 64;
-    int coord_elem = 0;  // bytes per coordinate of the staging buffers
+    int max_frames = 64;  // frames staged per submit chunk
+    int fc = 32;          // frames per compute chunk (one launch per stage)
+    int coord_elem = 0;   // bytes per coordinate of the staging buffers
 
     // device memory
-    std::vector<DevBuf *> owned;
     int64_t device_bytes = 0;
-    DevBuf geoms, samples, fscratch, off64, off32, hist, sums, stats, errflag, slot_of_mol, flags, bulk, nbulk;
+    DevBuf geoms, samples, tabs, fscratch, off64, off32, hist, sums, stats, errflag, counters, slot, flags, bulk, nbulk;
     DevBuf stage_s[2], stage_v[2];
     // PAIRS
-    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, u64, rc, ccount, cstart, cfill, cmol, gq, rq;
+    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, ccount, cstart, cfill, cmol, gq, rq;
     int gq_cap = 0, rq_cap = 0;
     // group tables
     DevBuf g_soff, g_sidx, g_voff, g_vidx;
     // ATOMS
-    DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, pcell, pq32, pq64;
+    DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, u64, rc, pcell, pq32, pq64;
     // pinned host staging
     FrameGeom *h_geoms[2] = {nullptr, nullptr};
     Sample *h_samples[2] = {nullptr, nullptr};
+    int4 *h_tabs[2] = {nullptr, nullptr};
     int64_t h_samples_cap = 0;
 
     // accumulation state
@@ -106,8 +108,8 @@ struct cm_handle {
 
     // launch accounting and optional per-launch event timing
     int64_t launches_total = 0;
-    int64_t class_launches[CM_K_NCLASSES] = {0, 0, 0, 0, 0, 0};
-    double class_ms[CM_K_NCLASSES] = {0, 0, 0, 0, 0, 0};
+    int64_t class_launches[CM_K_NCLASSES] = {};
+    double class_ms[CM_K_NCLASSES] = {};
     bool timing = false;
     std::vector<cudaEvent_t> ev_free;
     struct Pending {
@@ -330,28 +332,31 @@ double target_cell(const cm_handle *h) {
     return h->pair_cell;
 }
 
-// Reallocate the cell arrays if a frame needs more cells than planned.
+// Reallocate the per-frame cell arrays of a compute chunk if a frame needs
+// more cells than planned.
 void ensure_cells(cm_handle *h, int64_t ncell) {
     if (ncell <= h->ncell_cap) return;
     h->ncell_cap = ncell;
     if (h->regime == CM_REGIME_PAIRS) {
-        dev_alloc(h, h->ccount, (ncell + 1) * 4);
-        dev_alloc(h, h->cstart, (ncell + 1) * 4);
-        dev_alloc(h, h->cfill, (ncell + 1) * 4);
+        const size_t n = (size_t)h->fc * (ncell + 1) * 4;
+        dev_alloc(h, h->ccount, n);
+        dev_alloc(h, h->cstart, n);
+        dev_alloc(h, h->cfill, n);
     } else {
-        int64_t n = (int64_t)h->d.solute_nmols * ncell + 1;
-        dev_alloc(h, h->acount, n * 4);
-        dev_alloc(h, h->astart, n * 4);
-        dev_alloc(h, h->afill, n * 4);
+        const size_t n = (size_t)h->fc * ((int64_t)h->d.solute_nmols * ncell + 1) * 4;
+        dev_alloc(h, h->acount, n);
+        dev_alloc(h, h->astart, n);
+        dev_alloc(h, h->afill, n);
     }
 }
 
 void plan(cm_handle *h, const cm_frames *f) {
     const cm_system_desc &d = h->d;
     h->coord_elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
-    // radii of the first frame for the PAIRS cell size
+    CM_CUDA(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device));
+    // molecule radii of the first frame size the PAIRS cells
     if (h->regime == CM_REGIME_PAIRS) {
-        std::vector<double> xs(h->Ns * 3), xv;
+        std::vector<double> xs, xv;
         auto fetch = [&](const void *src, int64_t n, std::vector<double> &out) {
             out.resize(n * 3);
             std::vector<char> raw(n * 3 * h->coord_elem);
@@ -367,97 +372,100 @@ void plan(cm_handle *h, const cm_frames *f) {
             fetch(f->solvent_xyz, h->Nv, xv);
             rv = centroid_radius(xv.data(), d.solvent_nmols, d.solvent_natomspermol, f->cells);
         }
-        double cut = d.usecutoff ? d.cutoff : d.dbulk;
+        const double cut = d.usecutoff ? d.cutoff : d.dbulk;
         h->pair_cell = (cut + rs + rv) * 1.05 + 0.25;
     }
     h->max_frames = d.max_frames_per_batch > 0 ? d.max_frames_per_batch : 64;
     // keep the per-chunk sample table bounded (n_random_samples can be 10^5)
     if (h->mddf && (int64_t)h->max_frames * d.n_random_samples > (1 << 22))
         h->max_frames = (int)std::max<int64_t>(1, (1 << 22) / std::max(1, d.n_random_samples));
+    h->fc = std::min(h->max_frames, 32);
+    const int fc = h->fc;
+    const int64_t ms = d.solute_nmols, mv = d.solvent_nmols;
 
-    // common buffers
+    // staging of geometries, samples and bulk tables (two chunks in flight)
     dev_alloc(h, h->geoms, sizeof(FrameGeom) * h->max_frames * 2);
-    dev_alloc(h, h->fscratch, sizeof(FrameScratch));
-    dev_alloc(h, h->off64, sizeof(d4) * cmgeom::kOffEntries);
-    dev_alloc(h, h->off32, sizeof(float4) * cmgeom::kOffEntries);
-    for (int i = 0; i < 2; ++i) {
-        CM_CUDA(cudaMallocHost((void **)&h->h_geoms[i], sizeof(FrameGeom) * h->max_frames));
-    }
+    for (int i = 0; i < 2; ++i) CM_CUDA(cudaMallocHost((void **)&h->h_geoms[i], sizeof(FrameGeom) * h->max_frames));
     if (h->mddf) {
-        int nd = h->ndist_max;
-        dev_alloc(h, h->slot_of_mol, (size_t)d.solute_nmols * 4);
-        CM_CUDA(cudaMemset(h->slot_of_mol.p, 0xff, (size_t)d.solute_nmols * 4));
-        dev_alloc(h, h->flags, (size_t)nd * d.solvent_nmols);
-        dev_alloc(h, h->bulk, (size_t)nd * d.solvent_nmols * 4);
-        dev_alloc(h, h->nbulk, (size_t)nd * 4);
         h->h_samples_cap = (int64_t)h->max_frames * d.n_random_samples;
         dev_alloc(h, h->samples, sizeof(Sample) * h->h_samples_cap * 2);
-        for (int i = 0; i < 2; ++i) CM_CUDA(cudaMallocHost((void **)&h->h_samples[i], sizeof(Sample) * h->h_samples_cap));
+        dev_alloc(h, h->tabs, sizeof(int4) * (size_t)h->max_frames * h->ndist_max * 2);
+        for (int i = 0; i < 2; ++i) {
+            CM_CUDA(cudaMallocHost((void **)&h->h_samples[i], sizeof(Sample) * h->h_samples_cap));
+            CM_CUDA(cudaMallocHost((void **)&h->h_tabs[i], sizeof(int4) * (size_t)h->max_frames * h->ndist_max));
+        }
     }
-    // staging for host coordinates
     if (f->memory == CM_MEM_HOST) {
         for (int i = 0; i < 2; ++i) {
             dev_alloc(h, h->stage_s[i], (size_t)h->max_frames * h->Ns * 3 * h->coord_elem);
             if (!d.autocorrelation) dev_alloc(h, h->stage_v[i], (size_t)h->max_frames * h->Nv * 3 * h->coord_elem);
         }
     }
-    int64_t ms = d.solute_nmols, mv = d.solvent_nmols;
+    // per-frame buffers of one compute chunk
+    dev_alloc(h, h->fscratch, sizeof(FrameScratch) * fc);
+    dev_alloc(h, h->off64, sizeof(d4) * cmgeom::kOffEntries * fc);
+    dev_alloc(h, h->off32, sizeof(float4) * cmgeom::kOffEntries * fc);
+    dev_alloc(h, h->counters, 16);
+    if (h->mddf) {
+        const int nd = h->ndist_max;
+        dev_alloc(h, h->slot, (size_t)fc * ms * 4);
+        CM_CUDA(cudaMemset(h->slot.p, 0xff, (size_t)fc * ms * 4));
+        dev_alloc(h, h->flags, (size_t)fc * nd * mv);
+        dev_alloc(h, h->bulk, (size_t)fc * nd * mv * 4);
+        dev_alloc(h, h->nbulk, (size_t)fc * nd * 4);
+    }
     if (h->regime == CM_REGIME_PAIRS) {
-        dev_alloc(h, h->scell, ms * 4);
-        dev_alloc(h, h->sq32, ms * 16);
-        dev_alloc(h, h->sq64, ms * 32);
-        dev_alloc(h, h->so32, h->Ns * 16);
-        dev_alloc(h, h->so64, h->Ns * 32);
+        dev_alloc(h, h->scell, fc * ms * 4);
+        dev_alloc(h, h->sq32, fc * ms * 16);
+        dev_alloc(h, h->sq64, fc * ms * 32);
+        dev_alloc(h, h->so32, fc * h->Ns * 16);
+        dev_alloc(h, h->so64, fc * h->Ns * 32);
         if (!d.autocorrelation) {
-            dev_alloc(h, h->vcell, mv * 4);
-            dev_alloc(h, h->vq32, mv * 16);
-            dev_alloc(h, h->vq64, mv * 32);
-            dev_alloc(h, h->vo32, h->Nv * 16);
-            dev_alloc(h, h->vo64, h->Nv * 32);
+            dev_alloc(h, h->vcell, fc * mv * 4);
+            dev_alloc(h, h->vq32, fc * mv * 16);
+            dev_alloc(h, h->vq64, fc * mv * 32);
+            dev_alloc(h, h->vo32, fc * h->Nv * 16);
+            dev_alloc(h, h->vo64, fc * h->Nv * 32);
         }
-        dev_alloc(h, h->cmol, mv * 4);
-        // guard queue: every candidate fits when the system is small enough
-        // (candidates <= ms * mv); otherwise 64 per solute molecule, far above
-        // the guard-band rate
-        const int64_t pairs_bound = ms * mv;
-        h->gq_cap = (int)(pairs_bound <= (1LL << 24) ? std::max<int64_t>(pairs_bound, 1024)
-                                                     : std::min<int64_t>(std::max<int64_t>(1 << 20, 64 * ms), 1LL << 26));
+        dev_alloc(h, h->cmol, fc * mv * 4);
+        // guard queue of a chunk: every candidate fits when the system is small
+        // (candidates <= ms * mv per frame); otherwise 64 per solute molecule and
+        // frame, far above the guard-band rate
+        const int64_t bound = ms * mv * fc;
+        h->gq_cap = (int)(bound <= (1LL << 24) ? std::max<int64_t>(bound, 1024)
+                                               : std::min<int64_t>(std::max<int64_t>(1 << 20, 64 * ms * fc), 1LL << 25));
         dev_alloc(h, h->gq, (size_t)h->gq_cap * sizeof(int4));
         if (h->mddf) {
-            // random-insertion queue: every slot of up to `chunk` samples fits
-            const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(d.n_random_samples, (1 << 22) / mv));
+            // random-insertion queue: every slot of `chunk` samples fits
+            const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>((int64_t)fc * d.n_random_samples, (1 << 23) / mv));
             h->rq_cap = (int)(chunk * mv);
             dev_alloc(h, h->rq, (size_t)h->rq_cap * sizeof(int2));
         }
     } else {
-        dev_alloc(h, h->akey, h->Ns * 4);
-        dev_alloc(h, h->atq32, h->Ns * 16);
-        dev_alloc(h, h->atq64, h->Ns * 32);
-        dev_alloc(h, h->asq32, h->Ns * 16);
-        dev_alloc(h, h->asq64, h->Ns * 32);
-        dev_alloc(h, h->avcell, h->Nv * 4);
-        dev_alloc(h, h->avq32, h->Nv * 16);
-        dev_alloc(h, h->avq64, h->Nv * 32);
+        dev_alloc(h, h->akey, fc * h->Ns * 4);
+        dev_alloc(h, h->atq32, fc * h->Ns * 16);
+        dev_alloc(h, h->atq64, fc * h->Ns * 32);
+        dev_alloc(h, h->asq32, fc * h->Ns * 16);
+        dev_alloc(h, h->asq64, fc * h->Ns * 32);
+        dev_alloc(h, h->avcell, fc * h->Nv * 4);
+        dev_alloc(h, h->avq32, fc * h->Nv * 16);
+        dev_alloc(h, h->avq64, fc * h->Nv * 32);
         if (h->mddf) {
-            int chunk = std::min(kChunkSamples, std::max(1, d.n_random_samples));
+            dev_alloc(h, h->u64, fc * h->Nv * 32);
+            dev_alloc(h, h->rc, fc * mv * 4);
+            const int chunk = std::min(kChunkSamples, std::max(1, fc * d.n_random_samples));
             dev_alloc(h, h->pcell, (size_t)chunk * h->Nv * 4);
             dev_alloc(h, h->pq32, (size_t)chunk * h->Nv * 16);
             dev_alloc(h, h->pq64, (size_t)chunk * h->Nv * 32);
         }
     }
-    if (h->mddf && h->regime == CM_REGIME_ATOMS) {
-        dev_alloc(h, h->u64, h->Nv * 32);
-        dev_alloc(h, h->rc, mv * 4);
-    }
     // histogram shared-memory plan
-    size_t extra = h->regime == CM_REGIME_PAIRS ? (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8 : 0;
+    const size_t extra = h->regime == CM_REGIME_PAIRS ? (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8 : 0;
     h->smem_groups = hist_smem_bytes(h, 1) + extra + 2048 <= 160 * 1024 ? 1 : 0;
-    size_t smem_real = hist_smem_bytes(h, h->smem_groups) + extra;
-    size_t smem_rand = hist_smem_bytes(h, h->smem_groups) + kMaxSmallMol * 48;
-    size_t smem_max = std::max(smem_real, smem_rand);
+    const size_t smem_max = hist_smem_bytes(h, h->smem_groups) + extra;
     if (smem_max > 48 * 1024) {
-        int a = (int)smem_max;
-        auto attr = [&](const void *f) { CM_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, a)); };
+        const int a = (int)smem_max;
+        auto attr = [&](const void *fn) { CM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a)); };
         attr((const void *)k_pairs_real<true, true>);
         attr((const void *)k_pairs_real<true, false>);
         attr((const void *)k_pairs_real<false, true>);
@@ -560,55 +568,118 @@ void kend(cm_handle *h) {
         launches++;           \
     } while (0)
 
+// One compute chunk: consecutive frames of one staging batch that carry the
+// same non-zero weight.  Every stage of the chain is one launch per chunk.
+struct Chunk {
+    int c0 = 0, nf = 0;       // first frame (in the staging batch) and count
+    int smp0 = 0, nsmp = 0;   // the chunk's samples in the staging sample table
+    int tab0 = 0, ntab = 0;   // its (frame, distinct, molecule) bulk-table rows
+    int ncell_max = 0;
+    double weight = 1.0;
+};
+
+Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *dS) {
+    const cm_system_desc &d = h->d;
+    Bufs B{};
+    B.nf = c.nf;
+    B.ndist = h->ndist_max;
+    B.ms = d.solute_nmols;
+    B.Ns = h->Ns;
+    B.mv = d.solvent_nmols;
+    B.Nv = h->Nv;
+    B.G = dG + c.c0;
+    B.FS = P<FrameScratch>(h->fscratch);
+    B.off64 = P<d4>(h->off64);
+    B.off32 = P<float4>(h->off32);
+    B.counters = P<int>(h->counters);
+    B.samples = dS;
+    if (h->mddf) {
+        B.slot = P<int>(h->slot);
+        B.flags = P<unsigned char>(h->flags);
+        B.bulk = P<int>(h->bulk);
+        B.nbulk = P<int>(h->nbulk);
+    }
+    if (h->regime == CM_REGIME_PAIRS) {
+        B.scell = P<int>(h->scell);
+        B.sq32 = P<float4>(h->sq32);
+        B.sq64 = P<d4>(h->sq64);
+        B.so32 = P<float4>(h->so32);
+        B.so64 = P<d4>(h->so64);
+        if (!d.autocorrelation) {
+            B.vcell = P<int>(h->vcell);
+            B.vq32 = P<float4>(h->vq32);
+            B.vq64 = P<d4>(h->vq64);
+            B.vo32 = P<float4>(h->vo32);
+            B.vo64 = P<d4>(h->vo64);
+        }
+        B.ccount = P<int>(h->ccount);
+        B.cstart = P<int>(h->cstart);
+        B.cfill = P<int>(h->cfill);
+        B.cs = h->ncell_cap + 1;
+        B.cmol = P<int>(h->cmol);
+        B.gq = P<int4>(h->gq);
+        B.gq_cap = h->gq_cap;
+        B.rq = P<int2>(h->rq);
+        B.rq_cap = h->rq_cap;
+    } else {
+        B.akey = P<int>(h->akey);
+        B.atq32 = P<float4>(h->atq32);
+        B.asq32 = P<float4>(h->asq32);
+        B.atq64 = P<d4>(h->atq64);
+        B.asq64 = P<d4>(h->asq64);
+        B.acount = P<int>(h->acount);
+        B.astart = P<int>(h->astart);
+        B.afill = P<int>(h->afill);
+        B.as = (int64_t)d.solute_nmols * h->ncell_cap + 1;
+        B.avcell = P<int>(h->avcell);
+        B.avq32 = P<float4>(h->avq32);
+        B.avq64 = P<d4>(h->avq64);
+        if (h->mddf) {
+            B.u64 = P<d4>(h->u64);
+            B.rc = P<float>(h->rc);
+            B.pcell = P<int>(h->pcell);
+            B.pq32 = P<float4>(h->pq32);
+            B.pq64 = P<d4>(h->pq64);
+        }
+    }
+    return B;
+}
+
 template <typename T>
-void run_frame(cm_handle *h, const FrameGeom *dG, const FrameGeom &G, const Sample *dS, int nsamp, int ndist, const T *xs,
+void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *dS, const int4 *dtab, const T *xs,
                const T *xv) {
     const cm_system_desc &d = h->d;
     cudaStream_t st = h->stream;
+    ensure_cells(h, c.ncell_max);
     DevSys S = devsys_full(h);
+    const Bufs B = chunk_bufs(h, c, dG, dS);
     const bool self = d.autocorrelation;
     const bool fp32 = d.precision == CM_PRECISION_FP32_GUARD;
-    const int ms = d.solute_nmols, mv = d.solvent_nmols, aps = d.solute_natomspermol, apv = d.solvent_natomspermol;
+    const int nf = c.nf;
+    const int64_t ms = d.solute_nmols, mv = d.solvent_nmols, apv = d.solvent_natomspermol;
     const int iref = d.irefatom - 1;
-    FrameScratch *FS = P<FrameScratch>(h->fscratch);
-    int launches = 0;
-    const bool rnd = h->mddf && nsamp > 0;
-    const int *slot = rnd ? P<int>(h->slot_of_mol) : nullptr;
-    unsigned char *flags = rnd ? P<unsigned char>(h->flags) : nullptr;
+    const bool rnd = h->mddf && c.nsmp > 0;
     const size_t hsm = hist_smem_bytes(h, h->smem_groups);
-    int sms = 0;
-    CM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-    CM_CUDA(cudaMemsetAsync(FS, 0, sizeof(FrameScratch), st));
-    CM_LAUNCH(CM_K_PREP, k_offtable<<<grid_for(cmgeom::kOffEntries, 256), 256, 0, st>>>(dG, P<d4>(h->off64), P<float4>(h->off32)));
-    ensure_cells(h, G.ncell);
+    const int sms = h->sms;
+    int launches = 0;
+    CM_CUDA(cudaMemsetAsync(B.FS, 0, sizeof(FrameScratch) * nf, st));
+    CM_CUDA(cudaMemsetAsync(B.counters, 0, 2 * sizeof(int), st));
+    CM_LAUNCH(CM_K_PREP, k_offtable<<<dim3(grid_for(cmgeom::kOffEntries, 256), nf), 256, 0, st>>>(B));
     if (h->regime == CM_REGIME_PAIRS) {
-        if (rnd) CM_CUDA(cudaMemsetAsync(h->flags.p, 0, (size_t)ndist * mv, st));
-        CM_CUDA(cudaMemsetAsync(h->ccount.p, 0, (size_t)(G.ncell + 1) * 4, st));
-        // solute molecules (in self mode also the solvent cell list)
-        CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<grid_for(ms, 128), 128, 0, st>>>(
-                                 dG, xs, ms, aps, P<int>(h->scell), P<float4>(h->sq32), P<d4>(h->sq64), P<float4>(h->so32),
-                                 P<d4>(h->so64), self ? P<int>(h->ccount) : nullptr, self ? &FS->rmax_v : &FS->rmax_s));
+        if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
+        CM_CUDA(cudaMemsetAsync(B.ccount, 0, (size_t)nf * B.cs * 4, st));
+        // solute molecules (in self mode they also fill the cell counts)
+        CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<dim3(grid_for(ms, 128), nf), 128, 0, st>>>(B, xs, h->Ns * 3, 0, self ? 1 : 0));
         if (!self)
-            CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<grid_for(mv, 128), 128, 0, st>>>(
-                                     dG, xv, mv, apv, P<int>(h->vcell), P<float4>(h->vq32), P<d4>(h->vq64), P<float4>(h->vo32),
-                                     P<d4>(h->vo64), P<int>(h->ccount), &FS->rmax_v));
-        CM_LAUNCH(CM_K_PREP, k_frame_consts<<<1, 128, 0, st>>>(S, dG, FS, dS, rnd ? nsamp : 0, P<int>(h->slot_of_mol), 1));
-        CM_LAUNCH(CM_K_CELLS, k_scan<<<1, 1024, 0, st>>>(P<int>(h->ccount), G.ncell, P<int>(h->cstart), P<int>(h->cfill)));
-        CM_LAUNCH(CM_K_CELLS, k_scatter_mols<<<grid_for(mv, 256), 256, 0, st>>>(self ? P<int>(h->scell) : P<int>(h->vcell), mv,
-                                                                               P<int>(h->cfill), P<int>(h->cmol)));
-        const float4 *vq32 = self ? P<float4>(h->sq32) : P<float4>(h->vq32);
-        const d4 *vq64 = self ? P<d4>(h->sq64) : P<d4>(h->vq64);
-        const float4 *vo32 = self ? P<float4>(h->so32) : P<float4>(h->vo32);
-        const d4 *vo64 = self ? P<d4>(h->so64) : P<d4>(h->vo64);
+            CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<dim3(grid_for(mv, 128), nf), 128, 0, st>>>(B, xv, h->Nv * 3, 1, 1));
+        CM_LAUNCH(CM_K_PREP, k_frame_consts<<<nf, 128, 0, st>>>(S, B, 1));
+        CM_LAUNCH(CM_K_CELLS, k_scan<<<nf, 1024, 0, st>>>(B, 0));
+        CM_LAUNCH(CM_K_CELLS, k_scatter_mols<<<dim3(grid_for(mv, 256), nf), 256, 0, st>>>(B, self ? 1 : 0));
         const size_t smem = hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
-        const int grid = (int)std::min<int64_t>((ms + kWarps - 1) / kWarps, (int64_t)sms * 8);
-        GuardQueue gq{P<int4>(h->gq), h->gq_cap};
+        const int grid = (int)std::min<int64_t>(((int64_t)nf * ms + kWarps - 1) / kWarps, (int64_t)sms * 8);
         bool special = false;
         if (fp32) {
-#define CM_PAIRS_R32(A, SF)                                                                                            \
-    CM_LAUNCH(CM_K_REAL, k_pairs_real32<A, SF><<<grid, kWarps * 32, smem, st>>>(                                       \
-                             S, dG, FS, P<float4>(h->off32), P<int>(h->scell), P<float4>(h->sq32), P<float4>(h->so32), \
-                             vq32, vo32, P<int>(h->cstart), P<int>(h->cmol), slot, flags, gq))
+#define CM_PAIRS_R32(A, SF) CM_LAUNCH(CM_K_REAL, k_pairs_real32<A, SF><<<grid, kWarps * 32, smem, st>>>(S, B))
 #define CM_PAIRS_R32_APV(A)              \
     case A:                              \
         if (self) CM_PAIRS_R32(A, true); \
@@ -626,86 +697,54 @@ void run_frame(cm_handle *h, const FrameGeom *dG, const FrameGeom &G, const Samp
 #undef CM_PAIRS_R32_APV
 #undef CM_PAIRS_R32
         }
+        // the generic kernel takes every frame, or after the specialised one
+        // only the frames that need several images per molecule pair
+        const int only_multi = special ? 1 : 0;
+        if (fp32 && self) CM_LAUNCH(CM_K_REAL, k_pairs_real<true, true><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
+        else if (fp32) CM_LAUNCH(CM_K_REAL, k_pairs_real<true, false><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
+        else if (self) CM_LAUNCH(CM_K_REAL, k_pairs_real<false, true><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
+        else CM_LAUNCH(CM_K_REAL, k_pairs_real<false, false><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
         if (special) {
-#define CM_GUARD(SF)                                                                                                     \
-    CM_LAUNCH(CM_K_REAL, k_pairs_guard<SF><<<sms * 4, 128, hsm, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32),  \
-                                                                      P<float4>(h->sq32), P<d4>(h->sq64),                \
-                                                                      P<float4>(h->so32), P<d4>(h->so64), vq32, vq64,    \
-                                                                      vo32, vo64, slot, flags, gq))
-            if (self) CM_GUARD(true);
-            else CM_GUARD(false);
-#undef CM_GUARD
-        } else {
-#define CM_PAIRS_REAL(F, SF)                                                                                              \
-    CM_LAUNCH(CM_K_REAL, k_pairs_real<F, SF><<<grid, kWarps * 32, smem, st>>>(                                            \
-                             S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), P<int>(h->scell), P<float4>(h->sq32),       \
-                             P<d4>(h->sq64), P<float4>(h->so32), P<d4>(h->so64), vq32, vq64, vo32, vo64,                  \
-                             P<int>(h->cstart), P<int>(h->cmol), slot, flags))
-            if (fp32 && self) CM_PAIRS_REAL(true, true);
-            else if (fp32) CM_PAIRS_REAL(true, false);
-            else if (self) CM_PAIRS_REAL(false, true);
-            else CM_PAIRS_REAL(false, false);
-#undef CM_PAIRS_REAL
+            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_guard<true><<<sms * 4, 128, hsm, st>>>(S, B));
+            else CM_LAUNCH(CM_K_GUARD, k_pairs_guard<false><<<sms * 4, 128, hsm, st>>>(S, B));
         }
         if (rnd) {
-            CM_LAUNCH(CM_K_BULK, k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk),
-                                                                P<int>(h->nbulk), P<int>(h->slot_of_mol)));
-            const int chunk = std::max(1, h->rq_cap / mv);
-            for (int s0 = 0; s0 < nsamp; s0 += chunk) {
-                const int ny = std::min(chunk, nsamp - s0);
-                CM_CUDA(cudaMemsetAsync(&FS->rq_count, 0, sizeof(int), st));
-                CM_LAUNCH(CM_K_RANDOM, k_random_filter<<<grid_for((int64_t)ny * mv, 128), 128, 0, st>>>(
-                                           S, dG, FS, P<float4>(h->off32), dS, s0, ny, P<int>(h->scell), P<float4>(h->sq32),
-                                           vq32, P<int>(h->bulk), P<int>(h->nbulk), P<int2>(h->rq), h->rq_cap));
-#define CM_RAND(F)                                                                                                        \
-    CM_LAUNCH(CM_K_RANDOM, k_random_eval<F><<<sms * 2, 128, hsm, st>>>(                                                 \
-                               S, dG, FS, P<d4>(h->off64), P<float4>(h->off32), dS, P<int>(h->scell), P<float4>(h->sq32), \
-                               P<d4>(h->sq64), P<float4>(h->so32), P<d4>(h->so64), vo64, P<int>(h->bulk),                \
-                               P<int>(h->nbulk), P<int2>(h->rq), h->rq_cap))
-                if (fp32) CM_RAND(true);
-                else CM_RAND(false);
-#undef CM_RAND
+            CM_LAUNCH(CM_K_BULK, k_bulk<<<c.ntab, 1024, 0, st>>>(S, B, dtab + c.tab0));
+            // the random queue holds every slot of `piece` samples
+            const int piece = (int)std::max<int64_t>(1, h->rq_cap / mv);
+            for (int s0 = 0; s0 < c.nsmp; s0 += piece) {
+                const int ny = std::min(piece, c.nsmp - s0);
+                if (s0 > 0) CM_CUDA(cudaMemsetAsync(B.counters + 1, 0, sizeof(int), st));
+                CM_LAUNCH(CM_K_RANDOM, k_random_filter<<<grid_for((int64_t)ny * mv, 128), 128, 0, st>>>(S, B, c.smp0 + s0, ny));
+                if (fp32) CM_LAUNCH(CM_K_RANDOM, k_random_eval<true><<<sms * 4, 128, hsm, st>>>(S, B));
+                else CM_LAUNCH(CM_K_RANDOM, k_random_eval<false><<<sms * 4, 128, hsm, st>>>(S, B));
             }
         }
     } else {
         const T *xsolv = self ? xs : xv;
-        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solvent<T><<<grid_for(mv, 128), 128, 0, st>>>(
-                                 dG, xsolv, mv, apv, iref, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64),
-                                 h->mddf ? P<d4>(h->u64) : nullptr, P<float>(h->rc), &FS->rcmax));
-        const int64_t nkeys = (int64_t)ms * G.ncell;
-        CM_CUDA(cudaMemsetAsync(h->acount.p, 0, (size_t)(nkeys + 1) * 4, st));
-        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solute<T><<<grid_for(h->Ns, 256), 256, 0, st>>>(
-                                 dG, xs, (int)h->Ns, aps, P<int>(h->akey), P<float4>(h->atq32), P<d4>(h->atq64), P<int>(h->acount)));
-        CM_LAUNCH(CM_K_PREP, k_frame_consts<<<1, 128, 0, st>>>(S, dG, FS, dS, rnd ? nsamp : 0, P<int>(h->slot_of_mol), 0));
-        CM_LAUNCH(CM_K_CELLS, k_scan<<<1, 1024, 0, st>>>(P<int>(h->acount), (int)nkeys, P<int>(h->astart), P<int>(h->afill)));
-        CM_LAUNCH(CM_K_CELLS, k_scatter_atoms<<<grid_for(h->Ns, 256), 256, 0, st>>>(
-                                  P<int>(h->akey), (int)h->Ns, P<float4>(h->atq32), P<d4>(h->atq64), P<int>(h->afill),
-                                  P<float4>(h->asq32), P<d4>(h->asq64)));
-        if (ms > 65535) throw cm_error(CM_EINVAL, "the ATOMS layout supports at most 65535 solute molecules");
-        dim3 gr(grid_for(mv, 128), ms);
-#define CM_ATOMS(CLS, F, R, GRID, VC, VQ32, VQ64, S0)                                                                     \
-    CM_LAUNCH(CLS, k_atoms_eval<F, R><<<GRID, 128, hsm, st>>>(S, dG, FS, P<d4>(h->off64), P<float4>(h->off32),          \
-                                                              P<int>(h->astart), P<float4>(h->asq32), P<d4>(h->asq64), \
-                                                              VC, VQ32, VQ64, dS, S0, slot, flags))
-        if (fp32) CM_ATOMS(CM_K_REAL, true, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
-        else CM_ATOMS(CM_K_REAL, false, false, gr, P<int>(h->avcell), P<float4>(h->avq32), P<d4>(h->avq64), 0);
+        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solvent<T><<<dim3(grid_for(mv, 128), nf), 128, 0, st>>>(B, xsolv, h->Nv * 3, iref,
+                                                                                                 h->mddf ? 1 : 0));
+        CM_CUDA(cudaMemsetAsync(B.acount, 0, (size_t)nf * B.as * 4, st));
+        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solute<T><<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B, xs, h->Ns * 3));
+        CM_LAUNCH(CM_K_PREP, k_frame_consts<<<nf, 128, 0, st>>>(S, B, 0));
+        CM_LAUNCH(CM_K_CELLS, k_scan<<<nf, 1024, 0, st>>>(B, 1));
+        CM_LAUNCH(CM_K_CELLS, k_scatter_atoms<<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B));
+        const dim3 gr(grid_for(mv, 128), (unsigned)(nf * ms));
+        if (fp32) CM_LAUNCH(CM_K_REAL, k_atoms_eval<true, false><<<gr, 128, hsm, st>>>(S, B, 0));
+        else CM_LAUNCH(CM_K_REAL, k_atoms_eval<false, false><<<gr, 128, hsm, st>>>(S, B, 0));
         if (rnd) {
-            CM_LAUNCH(CM_K_BULK, k_bulk<<<ndist, 1024, 0, st>>>(S, dS, nsamp, P<unsigned char>(h->flags), P<int>(h->bulk),
-                                                                P<int>(h->nbulk), P<int>(h->slot_of_mol)));
-            for (int s0 = 0; s0 < nsamp; s0 += kChunkSamples) {
-                const int ny = std::min(kChunkSamples, nsamp - s0);
-                dim3 gp(grid_for(mv, 128), ny);
-                CM_LAUNCH(CM_K_RANDOM, k_atoms_place<<<gp, 128, 0, st>>>(S, dG, dS, s0, P<d4>(h->u64), P<int>(h->bulk),
-                                                                         P<int>(h->nbulk), P<int>(h->pcell), P<float4>(h->pq32),
-                                                                         P<d4>(h->pq64)));
-                if (fp32) CM_ATOMS(CM_K_RANDOM, true, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
-                else CM_ATOMS(CM_K_RANDOM, false, true, gp, P<int>(h->pcell), P<float4>(h->pq32), P<d4>(h->pq64), s0);
+            CM_LAUNCH(CM_K_BULK, k_bulk<<<c.ntab, 1024, 0, st>>>(S, B, dtab + c.tab0));
+            for (int s0 = 0; s0 < c.nsmp; s0 += kChunkSamples) {
+                const int ny = std::min(kChunkSamples, c.nsmp - s0);
+                const dim3 gp(grid_for(mv, 128), ny);
+                CM_LAUNCH(CM_K_RANDOM, k_atoms_place<<<gp, 128, 0, st>>>(S, B, c.smp0 + s0));
+                if (fp32) CM_LAUNCH(CM_K_RANDOM, k_atoms_eval<true, true><<<gp, 128, hsm, st>>>(S, B, c.smp0 + s0));
+                else CM_LAUNCH(CM_K_RANDOM, k_atoms_eval<false, true><<<gp, 128, hsm, st>>>(S, B, c.smp0 + s0));
             }
         }
-#undef CM_ATOMS
     }
     CM_CUDA(cudaGetLastError());
-    h->kernels_per_frame = launches;
+    h->kernels_per_frame = (launches + nf - 1) / nf;
 }
 
 void fold_class(cm_handle *h) {
@@ -718,6 +757,13 @@ void fold_class(cm_handle *h) {
     h->class_open = false;
 }
 
+// Frames per compute chunk: the ATOMS real pass indexes (frame, solute
+// molecule) in grid.y, which holds at most 65535 entries.
+int chunk_frames(const cm_handle *h) {
+    if (h->regime == CM_REGIME_ATOMS) return std::max(1, std::min(h->fc, 65535 / h->d.solute_nmols));
+    return h->fc;
+}
+
 void submit(cm_handle *h, const cm_frames *f) {
     const cm_system_desc &d = h->d;
     if (!f || f->nframes < 0) throw cm_error(CM_EINVAL, "invalid frame batch");
@@ -726,6 +772,8 @@ void submit(cm_handle *h, const cm_frames *f) {
     if (!d.autocorrelation && !f->solvent_xyz) throw cm_error(CM_EINVAL, "solvent_xyz is required unless autocorrelation");
     if (f->coord_type != CM_COORD_F32 && f->coord_type != CM_COORD_F64) throw cm_error(CM_EINVAL, "unknown coord_type");
     if (f->memory != CM_MEM_HOST && f->memory != CM_MEM_DEVICE) throw cm_error(CM_EINVAL, "unknown memory kind");
+    if (h->regime == CM_REGIME_ATOMS && d.solute_nmols > 65535)
+        throw cm_error(CM_EINVAL, "the ATOMS layout supports at most 65535 solute molecules");
     if (!h->planned) plan(h, f);
     int elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
     if (elem != h->coord_elem && f->memory == CM_MEM_HOST)
@@ -735,37 +783,71 @@ void submit(cm_handle *h, const cm_frames *f) {
         if (!std::isfinite(w) || w < 0.0) throw cm_error(CM_EINVAL, "frame weights must be finite and non-negative");
     }
     const double cs = target_cell(h);
+    const int fce = chunk_frames(h);
     const int64_t sbytes = h->Ns * 3 * elem, vbytes = h->Nv * 3 * elem;
     for (int f0 = 0; f0 < f->nframes; f0 += h->max_frames) {
         const int nf = std::min(h->max_frames, f->nframes - f0);
         const int b = h->chunk_parity;
         h->chunk_parity ^= 1;
-        // host staging of this chunk may be reused only after its previous copy finished
+        // host staging of this batch may be reused only after its previous copy finished
         CM_CUDA(cudaEventSynchronize(h->ev_copied[b]));
         FrameGeom *hg = h->h_geoms[b];
         Sample *hs = h->h_samples[b];
-        std::vector<int> ndist(nf, 0), nsamp(nf, 0);
-        int64_t soff = 0;
+        int4 *ht = h->h_tabs[b];
+        int soff = 0;
         for (int i = 0; i < nf; ++i) {
             FrameGeom &G = hg[i];
             memset(&G, 0, sizeof(G));
             frame_geometry(f->cells + 9 * (int64_t)(f0 + i), cs, 1023, G);
             G.weight = f->weights ? f->weights[f0 + i] : 1.0;
             G.frame_id = f->frame_ids[f0 + i];
-            G.sample_off = (int)soff;
+            G.sample_off = soff;
             if (h->mddf) {
-                nsamp[i] = draw_samples(h, G.frame_id, hs + soff, ndist[i]);
-                G.nsamples = nsamp[i];
-                G.ndistinct = ndist[i];
-                soff += nsamp[i];
+                int nd = 0;
+                G.nsamples = draw_samples(h, G.frame_id, hs + soff, nd);
+                G.ndistinct = nd;
+                soff += G.nsamples;
             }
+        }
+        // compute chunks: runs of equal non-zero weight (zero-weight frames are
+        // skipped, src/mddf.jl:102), at most fce frames each
+        std::vector<Chunk> chunks;
+        int ntab = 0;
+        for (int i = 0; i < nf;) {
+            if (hg[i].weight == 0.0) {
+                ++i;
+                continue;
+            }
+            Chunk c;
+            c.c0 = i;
+            c.weight = hg[i].weight;
+            c.smp0 = hg[i].sample_off;
+            c.tab0 = ntab;
+            int j = i;
+            while (j < nf && j - i < fce && hg[j].weight == c.weight) {
+                const FrameGeom &G = hg[j];
+                c.ncell_max = std::max(c.ncell_max, G.ncell);
+                for (int k = 0; k < G.nsamples; ++k) {
+                    Sample &sm = hs[G.sample_off + k];
+                    sm.pad = j - i;
+                    if (sm.rep == 0) ht[ntab++] = make_int4(j - i, sm.d, sm.s, 0);
+                }
+                ++j;
+            }
+            c.nf = j - i;
+            c.nsmp = hg[j - 1].sample_off + hg[j - 1].nsamples - c.smp0;
+            c.ntab = ntab - c.tab0;
+            chunks.push_back(c);
+            i = j;
         }
         cudaStream_t cp = f->memory == CM_MEM_HOST ? h->copy_stream : h->stream;
         CM_CUDA(cudaStreamWaitEvent(cp, h->ev_done[b], 0));
         FrameGeom *dG = P<FrameGeom>(h->geoms) + (size_t)b * h->max_frames;
         Sample *dS = h->mddf ? P<Sample>(h->samples) + (size_t)b * h->h_samples_cap : nullptr;
+        int4 *dT = h->mddf ? P<int4>(h->tabs) + (size_t)b * h->max_frames * h->ndist_max : nullptr;
         CM_CUDA(cudaMemcpyAsync(dG, hg, sizeof(FrameGeom) * nf, cudaMemcpyHostToDevice, cp));
         if (h->mddf && soff > 0) CM_CUDA(cudaMemcpyAsync(dS, hs, sizeof(Sample) * soff, cudaMemcpyHostToDevice, cp));
+        if (h->mddf && ntab > 0) CM_CUDA(cudaMemcpyAsync(dT, ht, sizeof(int4) * ntab, cudaMemcpyHostToDevice, cp));
         const char *xs_base, *xv_base = nullptr;
         if (f->memory == CM_MEM_HOST) {
             CM_CUDA(cudaMemcpyAsync(h->stage_s[b].p, (const char *)f->solute_xyz + sbytes * f0, (size_t)sbytes * nf,
@@ -782,23 +864,19 @@ void submit(cm_handle *h, const cm_frames *f) {
         }
         CM_CUDA(cudaEventRecord(h->ev_copied[b], cp));
         CM_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copied[b], 0));
-        for (int i = 0; i < nf; ++i) {
-            const FrameGeom &G = hg[i];
-            if (G.weight == 0.0) continue;  // zero-weight frames are skipped (src/mddf.jl:102)
-            if (h->class_open && G.weight != h->class_w) fold_class(h);
+        for (const Chunk &c : chunks) {
+            if (h->class_open && c.weight != h->class_w) fold_class(h);
             h->class_open = true;
-            h->class_w = G.weight;
-            if (G.ncell > h->ncell_cap) ensure_cells(h, G.ncell);
-            const char *xs = xs_base + sbytes * i;
-            const char *xv = xv_base ? xv_base + vbytes * i : nullptr;
-            const Sample *dSi = dS ? dS + G.sample_off : nullptr;
-            if (elem == 4)
-                run_frame<float>(h, dG + i, G, dSi, G.nsamples, G.ndistinct, (const float *)xs, (const float *)xv);
-            else
-                run_frame<double>(h, dG + i, G, dSi, G.nsamples, G.ndistinct, (const double *)xs, (const double *)xv);
-            h->volume_total += G.weight * G.det;  // src/mddf.jl:352
-            h->weight_total += G.weight;
-            h->frames++;
+            h->class_w = c.weight;
+            const char *xs = xs_base + sbytes * c.c0;
+            const char *xv = xv_base ? xv_base + vbytes * c.c0 : nullptr;
+            if (elem == 4) run_chunk<float>(h, c, dG, dS, dT, (const float *)xs, (const float *)xv);
+            else run_chunk<double>(h, c, dG, dS, dT, (const double *)xs, (const double *)xv);
+            for (int i = c.c0; i < c.c0 + c.nf; ++i) {
+                h->volume_total += hg[i].weight * hg[i].det;  // src/mddf.jl:352
+                h->weight_total += hg[i].weight;
+                h->frames++;
+            }
         }
         CM_CUDA(cudaEventRecord(h->ev_done[b], h->stream));
     }
@@ -842,7 +920,7 @@ int guarded(cm_handle *h, F &&fn) {
 
 void free_all(cm_handle *h) {
     DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag,
-                     &h->slot_of_mol, &h->flags, &h->bulk, &h->nbulk, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
+                     &h->slot, &h->flags, &h->bulk, &h->nbulk, &h->tabs, &h->counters, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
                      &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->gq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
@@ -855,8 +933,10 @@ void free_all(cm_handle *h) {
     for (int i = 0; i < 2; ++i) {
         if (h->h_geoms[i]) cudaFreeHost(h->h_geoms[i]);
         if (h->h_samples[i]) cudaFreeHost(h->h_samples[i]);
+        if (h->h_tabs[i]) cudaFreeHost(h->h_tabs[i]);
         h->h_geoms[i] = nullptr;
         h->h_samples[i] = nullptr;
+        h->h_tabs[i] = nullptr;
         if (h->ev_copied[i]) cudaEventDestroy(h->ev_copied[i]);
         if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
     }
@@ -1043,6 +1123,11 @@ int cm_get_stats(cm_handle *h, cm_stats *out) {
         double e;
         memcpy(&e, &s[ST_MAXERR], 8);
         out->max_guard_error = e;
+        if (h->planned && h->frames > 0) {
+            FrameScratch F0;
+            CM_CUDA(cudaMemcpy(&F0, h->fscratch.p, sizeof(F0), cudaMemcpyDeviceToHost));
+            h->last_guard = F0.g.delta;  // guard band of the last chunk's first frame
+        }
         out->guard_band = h->last_guard;
         out->regime = h->regime;
         out->kernels_per_frame = h->kernels_per_frame;

@@ -175,8 +175,9 @@ enum {
     CM_K_REAL = 2,        /* real-frame minimum distances + histograms */
     CM_K_BULK = 3,        /* bulk-molecule lists */
     CM_K_RANDOM = 4,      /* random-insertion placement + minimum distances */
-    CM_K_OTHER = 5,       /* sample slots, weight folds */
-    CM_K_NCLASSES = 6
+    CM_K_OTHER = 5,       /* weight folds */
+    CM_K_GUARD = 6,       /* FP64 re-evaluation of the candidates deferred by the FP32 real pass */
+    CM_K_NCLASSES = 7
 };
 
 /* Per-class GPU time (ms, from CUDA events around each launch on the handle's

@@ -33,7 +33,7 @@ def test_struct_sizes_match_header(cm):
     assert C.sizeof(N.cm_counts) == 88
     assert C.sizeof(N.cm_raw_counts) == 64
     assert C.sizeof(N.cm_stats) == 88
-    assert C.sizeof(N.cm_kernel_times) == 96
+    assert C.sizeof(N.cm_kernel_times) == 112
 
 
 def test_create_rejects_bad_descriptions_without_gpu(cm):
