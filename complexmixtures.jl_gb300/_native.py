@@ -19,6 +19,8 @@ CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
 CM_REGIME_AUTO, CM_REGIME_PAIRS, CM_REGIME_ATOMS = 0, 1, 2
 CM_COORD_F64, CM_COORD_F32 = 0, 1
 CM_MEM_HOST, CM_MEM_DEVICE = 0, 1
+CM_NOALLOC_SCRATCH_BYTES = 32 << 20
+CM_NOALLOC_MAX_SAMPLES = 4096
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libcmgpu.so")
@@ -148,6 +150,7 @@ EXPORTED = (
     "cm_device_bytes",
     "cm_stream",
     "cm_measure_fp32_peak",
+    "cm_frame_counts_noalloc",
 )
 
 _lib: Optional[C.CDLL] = None
@@ -195,6 +198,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_stream.restype = C.c_void_p
     lib.cm_measure_fp32_peak.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_double)]
     lib.cm_measure_fp32_peak.restype = C.c_int
+    lib.cm_frame_counts_noalloc.argtypes = [C.POINTER(cm_system_desc), C.POINTER(cm_frames), C.POINTER(C.c_int64),
+                                            C.c_int64, C.c_void_p]
+    lib.cm_frame_counts_noalloc.restype = C.c_int
     _lib = lib
     return lib
 

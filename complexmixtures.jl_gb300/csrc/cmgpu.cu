@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -953,6 +954,305 @@ void free_all(cm_handle *h) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Allocation-free one-frame entry point (cm_frame_counts_noalloc).
+//
+// Every device buffer the frame needs beyond the caller's coordinates and
+// output lives in g_noalloc_scratch, a file-scope array of
+// CM_NOALLOC_SCRATCH_BYTES.  Its address is looked up once per device, with
+// that device current, by the first call on the device.  All calls share the
+// array and find the previous call's contents in it: each call clears what
+// must start at zero (frame scratch, queue counters, cell counts, bulk flags,
+// the slot table, statistics, the error flag and the output), and calls whose
+// GPU work overlaps race on it.
+namespace {
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[CM_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+unsigned char *noalloc_scratch(int device) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            throw cm_error(CM_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_noalloc_ptr[device] = (unsigned char *)p;
+    }
+    return g_noalloc_ptr[device];
+}
+
+// Bump allocator over the scratch array, 256-byte aligned pieces.  With a
+// null base it only adds up the sizes.
+struct Carve {
+    unsigned char *base = nullptr;
+    size_t off = 0;
+    void take(DevBuf &b, size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        b.p = base ? base + off : nullptr;
+        b.bytes = bytes;
+        off += std::max<size_t>(bytes, 16);
+    }
+};
+
+void noalloc_fits(size_t bytes) {
+    if (bytes > (size_t)CM_NOALLOC_SCRATCH_BYTES)
+        throw cm_error(CM_EINVAL, "the system needs " + std::to_string(bytes) +
+                                      " bytes of scratch; the allocation-free entry point has " +
+                                      std::to_string((size_t)CM_NOALLOC_SCRATCH_BYTES) + " (use cm_create / cm_submit_frames)");
+}
+
+// Buffers of one frame that do not depend on the cell grid.
+void noalloc_fixed(cm_handle *h, Carve &c) {
+    const cm_system_desc &d = h->d;
+    const int64_t ms = d.solute_nmols, mv = d.solvent_nmols;
+    c.take(h->geoms, sizeof(FrameGeom));
+    c.take(h->fscratch, sizeof(FrameScratch));
+    c.take(h->off64, sizeof(d4) * cmgeom::kOffEntries);
+    c.take(h->off32, sizeof(float4) * cmgeom::kOffEntries);
+    c.take(h->counters, 16);
+    c.take(h->stats, ST_N * 8);
+    c.take(h->errflag, 8);
+    if (h->mddf) {
+        const int nd = h->ndist_max;
+        c.take(h->samples, sizeof(Sample) * d.n_random_samples);
+        c.take(h->tabs, sizeof(int4) * nd);
+        c.take(h->slot, ms * 4);
+        c.take(h->flags, (size_t)nd * mv);
+        c.take(h->bulk, (size_t)nd * mv * 4);
+        c.take(h->nbulk, (size_t)nd * 4);
+    }
+    c.take(h->scell, ms * 4);
+    c.take(h->sq32, ms * 16);
+    c.take(h->sq64, ms * 32);
+    c.take(h->so32, h->Ns * 16);
+    c.take(h->so64, h->Ns * 32);
+    if (!d.autocorrelation) {
+        c.take(h->vcell, mv * 4);
+        c.take(h->vq32, mv * 16);
+        c.take(h->vq64, mv * 32);
+        c.take(h->vo32, h->Nv * 16);
+        c.take(h->vo64, h->Nv * 32);
+    }
+    c.take(h->cmol, mv * 4);
+    h->gq_cap = (int)std::min<int64_t>(std::max<int64_t>(ms * mv, 1024), 1 << 18);
+    c.take(h->gq, (size_t)h->gq_cap * sizeof(int4));
+    if (h->mddf) {
+        h->rq_cap = (int)std::min<int64_t>(std::max<int64_t>((int64_t)d.n_random_samples * mv, mv), std::max<int64_t>(mv, 1 << 18));
+        c.take(h->rq, (size_t)h->rq_cap * sizeof(int2));
+    }
+}
+
+// Reference solute molecules of one frame into a caller-provided array
+// (same draws and order as draw_samples, without a temporary vector).
+int noalloc_samples(const cm_system_desc &d, int64_t frame_id, Sample *out, int4 *tab, int &ntab) {
+    const int nrs = d.n_random_samples;
+    uint64_t st = cmfeed::key(d.seed, cmfeed::kTagRef, (uint64_t)frame_id, 0, 0);
+    for (int i = 0; i < nrs; ++i) {
+        out[i].s = (int)cmfeed::below(st, (uint64_t)d.solute_nmols);
+        out[i].pad = 0;
+    }
+    std::sort(out, out + nrs, [](const Sample &a, const Sample &b) { return a.s < b.s; });
+    int nd = 0;
+    ntab = 0;
+    for (int i = 0; i < nrs; ++i) {
+        if (i == 0 || out[i].s != out[i - 1].s) {
+            out[i].rep = 0;
+            out[i].d = nd++;
+            tab[ntab++] = make_int4(0, out[i].d, out[i].s, 0);
+        } else {
+            out[i].rep = out[i - 1].rep + 1;
+            out[i].d = out[i - 1].d;
+        }
+    }
+    return nd;
+}
+
+void noalloc_smem_attributes(cm_handle *h) {
+    const size_t extra = (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
+    const size_t smem_max = hist_smem_bytes(h, h->smem_groups) + extra;
+    if (smem_max <= 48 * 1024) return;
+    const int a = (int)smem_max;
+    auto attr = [&](const void *fn) { CM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a)); };
+    attr((const void *)k_pairs_real<true, true>);
+    attr((const void *)k_pairs_real<true, false>);
+    attr((const void *)k_pairs_real<false, true>);
+    attr((const void *)k_pairs_real<false, false>);
+    attr((const void *)k_random_eval<true>);
+    attr((const void *)k_random_eval<false>);
+    attr((const void *)k_pairs_guard<true>);
+    attr((const void *)k_pairs_guard<false>);
+    attr((const void *)k_pairs_real32<1, true>);
+    attr((const void *)k_pairs_real32<1, false>);
+    attr((const void *)k_pairs_real32<3, true>);
+    attr((const void *)k_pairs_real32<3, false>);
+    attr((const void *)k_pairs_real32<4, true>);
+    attr((const void *)k_pairs_real32<4, false>);
+    attr((const void *)k_pairs_real32<5, true>);
+    attr((const void *)k_pairs_real32<5, false>);
+    attr((const void *)k_pairs_real32<14, true>);
+    attr((const void *)k_pairs_real32<14, false>);
+}
+
+thread_local Sample t_noalloc_samples[CM_NOALLOC_MAX_SAMPLES];
+thread_local int4 t_noalloc_tab[CM_NOALLOC_MAX_SAMPLES];
+
+template <typename T>
+void noalloc_run(cm_handle *h, const cm_frames *f, cudaStream_t stream) {
+    const cm_system_desc &d = h->d;
+    Carve c{noalloc_scratch(h->device), 0};
+    noalloc_fixed(h, c);
+    const T *xs = (const T *)f->solute_xyz;
+    const T *xv = d.autocorrelation ? nullptr : (const T *)f->solvent_xyz;
+    FrameGeom *dG = P<FrameGeom>(h->geoms);
+
+    // molecule radii on a one-cell grid of the box size the PAIRS cells
+    FrameGeom G;
+    memset(&G, 0, sizeof(G));
+    frame_geometry(f->cells, 1e30, 1, G);
+    G.weight = 1.0;
+    G.frame_id = f->frame_ids[0];
+    h->ncell_cap = 0;
+    CM_CUDA(cudaMemcpyAsync(dG, &G, sizeof(G), cudaMemcpyHostToDevice, stream));
+    CM_CUDA(cudaMemsetAsync(h->fscratch.p, 0, sizeof(FrameScratch), stream));
+    {
+        Chunk one;
+        one.nf = 1;
+        const Bufs B = chunk_bufs(h, one, dG, nullptr);
+        k_prep_pairs<T><<<grid_for(d.solute_nmols, 128), 128, 0, stream>>>(B, xs, h->Ns * 3, 0, 0);
+        if (!d.autocorrelation) k_prep_pairs<T><<<grid_for(d.solvent_nmols, 128), 128, 0, stream>>>(B, xv, h->Nv * 3, 1, 0);
+        CM_CUDA(cudaGetLastError());
+    }
+    FrameScratch F;
+    CM_CUDA(cudaMemcpyAsync(&F, h->fscratch.p, sizeof(F), cudaMemcpyDeviceToHost, stream));
+    CM_CUDA(cudaStreamSynchronize(stream));
+    const double rs = F.rmax_s, rv = d.autocorrelation ? F.rmax_s : F.rmax_v;
+    const double cut = d.usecutoff ? d.cutoff : d.dbulk;
+    h->pair_cell = (cut + rs + rv) * 1.05 + 0.25;
+
+    // the frame on its cell grid
+    memset(&G, 0, sizeof(G));
+    frame_geometry(f->cells, h->pair_cell, 1023, G);
+    G.weight = 1.0;
+    G.frame_id = f->frame_ids[0];
+    Chunk one;
+    one.nf = 1;
+    one.ncell_max = G.ncell;
+    if (h->mddf) {
+        int ntab = 0;
+        G.nsamples = d.n_random_samples;
+        G.ndistinct = noalloc_samples(d, G.frame_id, t_noalloc_samples, t_noalloc_tab, ntab);
+        one.nsmp = G.nsamples;
+        one.ntab = ntab;
+    }
+    c.take(h->ccount, (size_t)(G.ncell + 1) * 4);
+    c.take(h->cstart, (size_t)(G.ncell + 1) * 4);
+    c.take(h->cfill, (size_t)(G.ncell + 1) * 4);
+    noalloc_fits(c.off);
+    h->ncell_cap = G.ncell;
+    CM_CUDA(cudaMemcpyAsync(dG, &G, sizeof(G), cudaMemcpyHostToDevice, stream));
+    if (h->mddf) {
+        CM_CUDA(cudaMemcpyAsync(h->samples.p, t_noalloc_samples, sizeof(Sample) * one.nsmp, cudaMemcpyHostToDevice, stream));
+        CM_CUDA(cudaMemcpyAsync(h->tabs.p, t_noalloc_tab, sizeof(int4) * one.ntab, cudaMemcpyHostToDevice, stream));
+        CM_CUDA(cudaMemsetAsync(h->slot.p, 0xff, (size_t)d.solute_nmols * 4, stream));
+    }
+    CM_CUDA(cudaMemsetAsync(h->stats.p, 0, ST_N * 8, stream));
+    CM_CUDA(cudaMemsetAsync(h->errflag.p, 0, 8, stream));
+    CM_CUDA(cudaMemsetAsync(h->hist.p, 0, h->hist_n * 8, stream));
+    run_chunk<T>(h, one, dG, P<Sample>(h->samples), P<int4>(h->tabs), xs, xv);
+    int e = 0;
+    CM_CUDA(cudaMemcpyAsync(&e, h->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CM_CUDA(cudaStreamSynchronize(stream));
+    if (e) {
+        std::string m = "device-side check failed:";
+        if (e & ERR_STENCIL) m += " search range wider than the offset table (box too small for the cutoff);";
+        if (e & ERR_BIN) m += " histogram bin out of range;";
+        if (e & ERR_QUEUE) m += " guard queue overflow (rerun with FP64 precision);";
+        if (e & ERR_SIZE) m += " molecule too large for the PAIRS layout;";
+        throw cm_error(CM_EDEVICE, m);
+    }
+}
+
+int noalloc_frame(const cm_system_desc *desc, const cm_frames *f, int64_t *counts, int64_t counts_len, void *stream) {
+    int prev = -1;
+    try {
+        check_desc(desc);
+        if (desc->solute_group_offsets || desc->solvent_group_offsets)
+            throw cm_error(CM_EINVAL, "the allocation-free entry point uses the default per-atom groups (no group tables)");
+        if (desc->regime == CM_REGIME_ATOMS || desc->solute_natomspermol > kMaxSmallMol || desc->solvent_natomspermol > kMaxSmallMol)
+            throw cm_error(CM_EINVAL, "the allocation-free entry point runs the PAIRS layout only (at most 32 atoms per molecule)");
+        if (desc->mode == CM_MODE_MDDF && desc->n_random_samples > CM_NOALLOC_MAX_SAMPLES)
+            throw cm_error(CM_EINVAL, "the allocation-free entry point takes at most " + std::to_string(CM_NOALLOC_MAX_SAMPLES) +
+                                          " random samples per frame");
+        if (desc->device < 0 || desc->device >= kNoAllocMaxDevices) throw cm_error(CM_EINVAL, "device index out of range");
+        if (!f || f->nframes != 1) throw cm_error(CM_EINVAL, "the allocation-free entry point takes exactly one frame");
+        if (f->memory != CM_MEM_DEVICE) throw cm_error(CM_EINVAL, "the allocation-free entry point takes coordinates in device memory");
+        if (f->coord_type != CM_COORD_F32 && f->coord_type != CM_COORD_F64) throw cm_error(CM_EINVAL, "unknown coord_type");
+        if (!f->solute_xyz || !f->cells || !f->frame_ids) throw cm_error(CM_EINVAL, "solute_xyz, cells and frame_ids are required");
+        if (!desc->autocorrelation && !f->solvent_xyz) throw cm_error(CM_EINVAL, "solvent_xyz is required unless autocorrelation");
+        if (f->weights) throw cm_error(CM_EINVAL, "the allocation-free entry point counts one unweighted frame (weights must be NULL)");
+        if (!counts) throw cm_error(CM_EINVAL, "NULL counts");
+
+        cm_handle h;
+        h.d = *desc;
+        h.device = desc->device;
+        h.Ns = (int64_t)desc->solute_nmols * desc->solute_natomspermol;
+        h.Nv = (int64_t)desc->solvent_nmols * desc->solvent_natomspermol;
+        h.mddf = desc->mode == CM_MODE_MDDF;
+        h.regime = CM_REGIME_PAIRS;
+        h.Gs = desc->solute_natomspermol;
+        h.Gv = desc->solvent_natomspermol;
+        h.ndist_max = h.mddf ? std::max(1, std::min(desc->solute_nmols, desc->n_random_samples)) : 0;
+        h.fc = h.max_frames = 1;
+        h.coord_elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
+        // histogram layout of cm_raw_counts, concatenated
+        const int64_t nb = desc->nbins, Gv = desc->autocorrelation ? 0 : h.Gv;
+        h.o_md = 0;
+        h.o_mdr = nb;
+        h.o_rdf = 2 * nb;
+        h.o_rdfr = 3 * nb;
+        h.o_gs = 4 * nb;
+        h.o_gsr = h.o_gs + h.Gs * nb;
+        h.o_gv = h.o_gsr + h.Gs * nb;
+        h.o_gvr = h.o_gv + Gv * nb;
+        h.hist_n = h.o_gvr + Gv * nb;
+        if (counts_len != h.hist_n)
+            throw cm_error(CM_EINVAL, "counts must hold " + std::to_string(h.hist_n) + " int64 values");
+        h.hist.p = counts;
+        h.hist.bytes = (size_t)h.hist_n * 8;
+        const size_t extra = (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
+        h.smem_groups = hist_smem_bytes(&h, 1) + extra + 2048 <= 160 * 1024 ? 1 : 0;
+        {
+            Carve dry;
+            noalloc_fixed(&h, dry);
+            noalloc_fits(dry.off);
+        }
+        CM_CUDA(cudaGetDevice(&prev));
+        CM_CUDA(cudaSetDevice(h.device));
+        CM_CUDA(cudaDeviceGetAttribute(&h.sms, cudaDevAttrMultiProcessorCount, h.device));
+        h.stream = (cudaStream_t)stream;
+        noalloc_smem_attributes(&h);
+        if (h.coord_elem == 4) noalloc_run<float>(&h, f, h.stream);
+        else noalloc_run<double>(&h, f, h.stream);
+        h.stream = nullptr;
+        cudaSetDevice(prev);
+        return CM_OK;
+    } catch (const cm_error &e) {
+        g_create_error = e.msg;
+        if (prev >= 0) cudaSetDevice(prev);
+        return e.code;
+    } catch (const std::exception &e) {
+        g_create_error = e.what();
+        if (prev >= 0) cudaSetDevice(prev);
+        return CM_ECUDA;
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 int cm_create(const cm_system_desc *desc, cm_handle **out) {
@@ -1236,5 +1536,10 @@ int cm_measure_fp32_peak(int32_t device, double ms_target, double *tflops) {
 }
 
 void *cm_stream(cm_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+int cm_frame_counts_noalloc(const cm_system_desc *desc, const cm_frames *frame, int64_t *counts, int64_t counts_len,
+                            void *stream) {
+    return noalloc_frame(desc, frame, counts, counts_len, stream);
+}
 
 }  // extern "C"

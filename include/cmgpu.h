@@ -236,6 +236,42 @@ int64_t cm_device_bytes(const cm_handle *h);
  * their own device work against the engine. */
 void *cm_stream(cm_handle *h);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free entry point.  No counterpart in the reference: it serves
+ * callers that cannot allocate device memory (an in-situ analysis callback
+ * inside a simulation engine that owns the device memory, a host program whose
+ * memory pool must not grow while its streams are captured).
+ *
+ * Computes the exact half-unit counts of ONE frame -- the values
+ * cm_read_raw_counts gives for a handle that was given only that frame -- into
+ * `counts` (device memory, int64, overwritten), laid out as
+ *   md[nbins] md_random[nbins] rdf[nbins] rdf_random[nbins]
+ *   solute_group[Gs][nbins] solute_group_random[Gs][nbins]
+ *   solvent_group[Gv][nbins] solvent_group_random[Gv][nbins]
+ * with Gs, Gv the atoms per solute / solvent molecule (the two solvent blocks
+ * are absent with autocorrelation); counts_len must equal that total.
+ *
+ * It calls no device allocator: every buffer beyond the caller's coordinates
+ * and `counts` is carved from one file-scope device array of
+ * CM_NOALLOC_SCRATCH_BYTES.  Limits, refused with CM_EINVAL and a message:
+ * the PAIRS layout (at most 32 atoms per molecule), default per-atom groups,
+ * frame->nframes == 1 with coordinates in device memory and weights NULL,
+ * n_random_samples <= CM_NOALLOC_MAX_SAMPLES, and the frame's buffers within
+ * the scratch array (the message gives the size needed).
+ *
+ * The first call on a device looks up the scratch array's address
+ * (cudaGetSymbolAddress, with desc->device current); make that first call
+ * before any stream capture.  Every call shares the array and finds the
+ * previous call's contents in it; each call clears what must start at zero.
+ * Calls whose GPU work overlaps (several streams or host threads) race on the
+ * array.  Work is ordered on `stream` (NULL: the legacy default stream) and
+ * the call synchronises it before returning (it reads the molecule radii and
+ * the device error flag back).  Errors: cm_last_error(NULL). */
+#define CM_NOALLOC_SCRATCH_BYTES (32ull << 20)
+#define CM_NOALLOC_MAX_SAMPLES 4096
+int cm_frame_counts_noalloc(const cm_system_desc *desc, const cm_frames *frame, int64_t *counts, int64_t counts_len,
+                            void *stream);
+
 #ifdef __cplusplus
 }
 #endif
