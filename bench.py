@@ -45,6 +45,13 @@ CUTOFF = 10.0
 BINSTEP = 0.02
 NRAND = 5
 SEED = 20261203 + 3
+METRIC = "MDDF frames/s (config 3, batched FP32 + FP64 guard)"
+
+# serving leg (config-5 shapes, scaled): request pool and arrival process
+SERVE_SYSTEMS = 8            # c3-like systems, atoms log-uniform in [5,000, 500,000]
+SERVE_REQUESTS = 160
+SERVE_MAX_FRAMES = 16        # frames per request uniform in [1, 16]
+SERVE_SEED = 20261203 + 5
 
 
 def parse():
@@ -57,6 +64,7 @@ def parse():
     p.add_argument("--cpu-frames", type=int, default=0, help="CPU-baseline sample size (0: one frame per host thread)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
     return p.parse_args()
 
 
@@ -162,6 +170,167 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def serving_pool(syn):
+    """SERVE_SYSTEMS c3-like base systems (frame 0 from the config-5 generator)
+    with SERVE_MAX_FRAMES frames each: rigid molecule translations of
+    sigma = 0.4 A per frame."""
+    rng = np.random.default_rng(SERVE_SEED)
+    sizes = np.exp(np.linspace(np.log(5000), np.log(500000), SERVE_SYSTEMS)).astype(int)
+    pool = []
+    for i, n in enumerate(sizes):
+        sysm = syn.config5_request(int(n), SERVE_SEED + i, SERVE_MAX_FRAMES)
+        x0 = sysm.solute0.astype(np.float32).reshape(-1, 14, 3)
+        frames = np.empty((SERVE_MAX_FRAMES,) + x0.shape, np.float32)
+        for k in range(SERVE_MAX_FRAMES):
+            frames[k] = x0 + rng.normal(scale=0.4, size=(x0.shape[0], 1, 3)).astype(np.float32)
+        pool.append((frames.reshape(SERVE_MAX_FRAMES, -1, 3), sysm.cell, x0.shape[0]))
+    return pool
+
+
+def serving_requests(pool):
+    rng = np.random.default_rng(SERVE_SEED + 1)
+    reqs = []
+    for _ in range(SERVE_REQUESTS):
+        i = int(rng.integers(len(pool)))
+        nf = int(rng.integers(1, SERVE_MAX_FRAMES + 1))
+        cutoff = float(f"{round(rng.uniform(8.0, 14.0) / 0.02) * 0.02:.2f}")
+        reqs.append((i, nf, cutoff))
+    return reqs
+
+
+def serving_leg(cm, device):
+    """Config-5 shaped serving load: Poisson arrivals of c3-like self-MDDF
+    requests into the continuous-batching server (FP32 + guard), against the
+    same requests run one at a time on the plain FP64 engine."""
+    import torch
+
+    syn = __import__("importlib").import_module("complexmixtures_gb300.synth")
+    pool = serving_pool(syn)
+    reqs = serving_requests(pool)
+
+    def kw(i, cutoff, precision):
+        nm = pool[i][2]
+        return dict(solute_nmols=nm, solute_natomspermol=14, solvent_nmols=nm, solvent_natomspermol=14,
+                    autocorrelation=True, irefatom=1, cutoff=cutoff, binstep=0.02, dbulk=cutoff, usecutoff=False,
+                    nbins=cm.setbin(cutoff, 0.02), n_random_samples=5, seed=SERVE_SEED, precision=precision,
+                    device=device)
+
+    def cells(i, nf):
+        return np.repeat(pool[i][1][None], nf, axis=0)
+
+    frames_total = sum(nf for _, nf, _ in reqs)
+
+    def serial(precision):
+        out = []
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for i, nf, cutoff in reqs:
+            eng = cm.Engine(**kw(i, cutoff, precision))
+            eng.submit(pool[i][0][:nf], None, cells(i, nf))
+            out.append(eng.raw_counts())
+            eng.close()
+        return time.perf_counter() - t, out
+
+    serial("fp32")  # warm-up: module load, first allocations
+    t64, ref = serial("fp64")
+    t32, _ = serial("fp32")
+    # arrivals at the serial FP32 service rate (the server's overlap is the headroom)
+    rate = len(reqs) / t32
+    gaps = np.random.default_rng(SERVE_SEED + 2).exponential(1.0 / rate, len(reqs))
+    with cm.Server(device=device, frames_per_turn=4) as srv:
+        ids = []
+        t0 = time.perf_counter()
+        due = t0
+        for (i, nf, cutoff), g in zip(reqs, gaps):
+            due += g
+            while time.perf_counter() < due:
+                time.sleep(min(1e-4, max(0.0, due - time.perf_counter())))
+            ids.append(srv.submit(pool[i][0][:nf], None, cells(i, nf), **kw(i, cutoff, "fp32")))
+        infos = [srv.wait(r, timeout=600) for r in ids]
+        span = max(x["t_done"] for x in infos) - min(x["t_submit"] for x in infos)
+        same = all(np.array_equal(srv.raw_counts(r)["md"], ref[k]["md"]) and
+                   np.array_equal(srv.raw_counts(r)["md_random"], ref[k]["md_random"]) and
+                   np.array_equal(srv.raw_counts(r)["solute_group"], ref[k]["solute_group"])
+                   for k, r in enumerate(ids))
+    pct = cm.latency_percentiles(infos)
+    return {
+        "workload": f"{len(reqs)} Poisson-arrival self-MDDF requests over {SERVE_SYSTEMS} c3-like systems "
+                    f"(5,000-500,000 atoms, log-spaced), 1-{SERVE_MAX_FRAMES} frames each, cutoff U[8,14] "
+                    f"rounded to 0.02, 5 random samples; arrival rate = serial FP32 service rate",
+        "requests": len(reqs), "frames": frames_total,
+        "p50_ms": pct["p50"], "p99_ms": pct["p99"],
+        "frames_per_s": frames_total / span,
+        "serial_fp64_frames_per_s": frames_total / t64,
+        "serial_fp32_frames_per_s": frames_total / t32,
+        "arrival_rate_per_s": rate,
+        "failed": sum(1 for x in infos if x["state"] != "done"),
+        "counts_identical_to_serial_fp64": bool(same),
+    }
+
+
+C4_FRAMES = 8               # frames per config-4 system (config 4 has 50)
+
+
+def batched_c4_leg(cm, device):
+    """Config-4 load: 64 independent systems of uneven size (2,000-200,000
+    atoms, 5 % chain + water) run one at a time, then submitted together to
+    the request server, which runs them concurrently on the device; the cell
+    size comes from the autotuner on the median system."""
+    import torch
+
+    syn = __import__("importlib").import_module("complexmixtures_gb300.synth")
+    sizes = syn.config4_sizes()
+    systems = []
+    for k, n in enumerate(sizes):
+        sysm = syn.config4_system(int(n), 20261207 + k, nframes=C4_FRAMES)
+        xs, xv, cells = sysm.frames(C4_FRAMES)
+        aps = sysm.solute_natomspermol
+        sv = sysm.solvents[0]
+        kw = dict(solute_nmols=1, solute_natomspermol=aps, solvent_nmols=sv.nmols, solvent_natomspermol=3,
+                  autocorrelation=False, irefatom=1, cutoff=10.0, binstep=0.02, dbulk=10.0, usecutoff=False, nbins=500,
+                  n_random_samples=10, seed=sysm.seed, solute_groups=[[i // 10] for i in range(aps)],
+                  solute_ngroups=(aps + 9) // 10, precision="fp32", device=device)
+        systems.append((xs, xv, cells, kw))
+    med = int(np.argsort(sizes)[len(sizes) // 2])
+    xs, xv, cells, kw = systems[med]
+    tune = cm.autotune(xs[:2], xv[:2], cells[:2], **kw)
+    pct = tune["cell_scale_pct"]
+    frames_total = C4_FRAMES * len(systems)
+
+    def serial():
+        out = []
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for xs, xv, cells, kw in systems:
+            eng = cm.Engine(cell_scale_pct=pct, **kw)
+            eng.submit(xs, xv, cells)
+            out.append(eng.raw_counts())
+            eng.close()
+        return time.perf_counter() - t, out
+
+    serial()  # warm-up
+    ts, ref = serial()
+    with cm.Server(device=device, frames_per_turn=C4_FRAMES) as srv:
+        t0 = time.perf_counter()
+        ids = [srv.submit(xs, xv, cells, cell_scale_pct=pct, **kw) for xs, xv, cells, kw in systems]
+        infos = [srv.wait(r, timeout=600) for r in ids]
+        tb = time.perf_counter() - t0
+        same = all(all(np.array_equal(srv.raw_counts(r)[k], ref[i][k]) for k in ("md", "md_random", "solute_group"))
+                   for i, r in enumerate(ids))
+    pct_lat = cm.latency_percentiles(infos)
+    return {
+        "workload": f"64 systems, atoms log-uniform in [2,000, 200,000] (5 % chain, rest 3-site water, "
+                    f"0.1 atoms/A^3), {C4_FRAMES} FP32 frames each, cutoff 10 A, 10 random samples, groups of 10",
+        "frames": frames_total,
+        "serial_frames_per_s": frames_total / ts,
+        "batched_frames_per_s": frames_total / tb,
+        "p50_ms": pct_lat["p50"], "p99_ms": pct_lat["p99"],
+        "cell_scale_pct": pct, "autotune_ms_per_frame": tune["candidates"],
+        "failed": sum(1 for x in infos if x["state"] != "done"),
+        "counts_identical_to_serial": bool(same),
+    }
+
+
 def cpu_baseline(xs, cells, nframes_sample):
     """The oracle (CPU restatement of the reference's path), all host threads."""
     import __graft_entry__ as entry
@@ -198,7 +367,7 @@ def run_reference(args, world, rank):
     T = sum(times)
     v = args.steps * n / T
     line = {
-        "impl": "reference", "metric": "MDDF frames/s", "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config-3 shapes)",
         "config": config_dict(n, {"step": f"{n} frames (bounded sample of the 500-frame workload)"}),
@@ -329,7 +498,7 @@ def main():
     # (centroid float4) and atom offsets (float4) it reads
     bytes_frame = 16.0 * NMOLS + 16.0 * NMOLS * APM
     roofline = {
-        "bound": "fp32", "kernel": "k_pairs_real32<14, self> (one launch per chunk of 32 frames)",
+        "bound": "fp32", "kernel": "k_pairs_flat32<self, 14> (one launch per chunk of 32 frames)",
         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
         "peak_source": "FP32 FMA throughput measured by cm_measure_fp32_peak on this GPU (of measured)",
         "traffic": None,
@@ -342,16 +511,21 @@ def main():
     }
     # DRAM bytes per launch from the committed ncu capture of this kernel on
     # this workload (first number of the file)
-    traffic_file = os.path.join(ROOT, "profiles", "pairs_real32_c3_traffic.txt")
+    traffic_file = os.path.join(ROOT, "profiles", "pairs_flat32_c3_traffic.txt")
     if os.path.exists(traffic_file):
         try:
             roofline["traffic"] = float(open(traffic_file).read().split()[0])
         except Exception:
             pass
 
+    serving = batched = None
+    if not args.no_serving and world == 1:
+        serving = serving_leg(cm, local)
+        batched = batched_c4_leg(cm, local)
+
     launches = st["kernel_launches"] - st0["kernel_launches"]
     line = {
-        "metric": "MDDF frames/s (config 3, batched FP32 + FP64 guard)", "value": value, "unit": "frames/s",
+        "metric": METRIC, "value": value, "unit": "frames/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, config-3 shapes and distributions)",
@@ -364,6 +538,8 @@ def main():
                   "hits_per_frame": (st["hits_real"] + st["hits_random"]) / max(1, st["frames"]),
                   "max_fp32_error_A": st["max_guard_error"]},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
+        "serving": serving,
+        "batched_c4": batched,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

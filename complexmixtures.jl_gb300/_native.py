@@ -60,7 +60,7 @@ class cm_system_desc(C.Structure):
         ("max_frames_per_batch", C.c_int32),
         ("hbm_budget_bytes", C.c_int64),
         ("kernel_timing", C.c_int32),
-        ("reserved", C.c_int32),
+        ("cell_scale_pct", C.c_int32),
     ]
 
 
@@ -135,6 +135,42 @@ class cm_kernel_times(C.Structure):
     _fields_ = [("ms", C.c_double * 7), ("launches", C.c_int64 * 7)]
 
 
+CM_TUNE_MAX = 8
+
+
+class cm_tuning(C.Structure):
+    _fields_ = [
+        ("cell_scale_pct", C.c_int32),
+        ("ncandidates", C.c_int32),
+        ("candidates", C.c_int32 * CM_TUNE_MAX),
+        ("ms_per_frame", C.c_double * CM_TUNE_MAX),
+    ]
+
+
+class cm_server_desc(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("max_active", C.c_int32),
+        ("hbm_budget_bytes", C.c_int64),
+        ("frames_per_turn", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class cm_request_info(C.Structure):
+    _fields_ = [
+        ("state", C.c_int32),
+        ("status", C.c_int32),
+        ("t_submit", C.c_double),
+        ("t_admit", C.c_double),
+        ("t_done", C.c_double),
+        ("frames_submitted", C.c_int64),
+        ("device_bytes", C.c_int64),
+    ]
+
+
+CM_REQ_QUEUED, CM_REQ_RUNNING, CM_REQ_DONE, CM_REQ_FAILED, CM_REQ_CANCELLED = range(5)
+
 EXPORTED = (
     "cm_create",
     "cm_submit_frames",
@@ -151,6 +187,17 @@ EXPORTED = (
     "cm_stream",
     "cm_measure_fp32_peak",
     "cm_frame_counts_noalloc",
+    "cm_autotune",
+    "cm_server_create",
+    "cm_server_submit",
+    "cm_server_poll",
+    "cm_server_wait",
+    "cm_server_read_counts",
+    "cm_server_read_raw_counts",
+    "cm_server_cancel",
+    "cm_server_release",
+    "cm_server_destroy",
+    "cm_server_last_error",
 )
 
 _lib: Optional[C.CDLL] = None
@@ -201,16 +248,36 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_frame_counts_noalloc.argtypes = [C.POINTER(cm_system_desc), C.POINTER(cm_frames), C.POINTER(C.c_int64),
                                             C.c_int64, C.c_void_p]
     lib.cm_frame_counts_noalloc.restype = C.c_int
+    lib.cm_autotune.argtypes = [C.POINTER(cm_system_desc), C.POINTER(cm_frames), C.POINTER(cm_tuning)]
+    lib.cm_autotune.restype = C.c_int
+    S = C.c_void_p
+    lib.cm_server_create.argtypes = [C.POINTER(cm_server_desc), C.POINTER(S)]
+    lib.cm_server_submit.argtypes = [S, C.POINTER(cm_system_desc), C.POINTER(cm_frames), C.POINTER(C.c_int64)]
+    lib.cm_server_poll.argtypes = [S, C.c_int64, C.POINTER(cm_request_info)]
+    lib.cm_server_wait.argtypes = [S, C.c_int64, C.c_double, C.POINTER(cm_request_info)]
+    lib.cm_server_read_counts.argtypes = [S, C.c_int64, C.POINTER(cm_counts)]
+    lib.cm_server_read_raw_counts.argtypes = [S, C.c_int64, C.POINTER(cm_raw_counts)]
+    lib.cm_server_cancel.argtypes = [S, C.c_int64]
+    lib.cm_server_release.argtypes = [S, C.c_int64]
+    lib.cm_server_destroy.argtypes = [S]
+    for f in ("cm_server_create", "cm_server_submit", "cm_server_poll", "cm_server_wait", "cm_server_read_counts",
+              "cm_server_read_raw_counts", "cm_server_cancel", "cm_server_release", "cm_server_destroy"):
+        getattr(lib, f).restype = C.c_int
+    lib.cm_server_last_error.argtypes = [S]
+    lib.cm_server_last_error.restype = C.c_char_p
     _lib = lib
     return lib
 
 
-def raise_for(status: int, handle) -> None:
+def raise_for(status: int, handle, server=None) -> None:
     """Turn a cm_status into the exception the reference raises for it."""
     if status == CM_OK:
         return
     lib = load()
-    msg = lib.cm_last_error(handle).decode(errors="replace")
+    if server is not None:
+        msg = lib.cm_server_last_error(server).decode(errors="replace")
+    else:
+        msg = lib.cm_last_error(handle).decode(errors="replace")
     what = lib.cm_status_string(status).decode()
     text = f"{what}: {msg}" if msg else what
     if status == CM_EINVAL:

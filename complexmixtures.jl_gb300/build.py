@@ -1,4 +1,5 @@
-"""Build recipe of libcmgpu.so: one nvcc invocation for sm_103a.
+"""Build recipe of libcmgpu.so: one nvcc invocation for sm_103a (the engine's
+CUDA translation unit and the host-only request server).
 
 FP64 arithmetic on the decision path uses explicit round-to-nearest
 intrinsics in the device code, so contraction flags only affect FP32 code;
@@ -11,7 +12,7 @@ import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "csrc", "cmgpu.cu")
+SRCS = [os.path.join(HERE, "csrc", "cmgpu.cu"), os.path.join(HERE, "csrc", "cm_server.cpp")]
 OUT_DIR = os.path.join(HERE, "_build")
 OUT = os.path.join(OUT_DIR, "libcmgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -26,7 +27,7 @@ def nvcc() -> str:
 
 def sources():
     d = os.path.join(HERE, "csrc")
-    return [os.path.join(d, f) for f in sorted(os.listdir(d)) if f.endswith((".cu", ".cuh", ".h"))] + [
+    return [os.path.join(d, f) for f in sorted(os.listdir(d)) if f.endswith((".cu", ".cuh", ".h", ".cpp"))] + [
         os.path.join(os.path.dirname(HERE), "include", "cmgpu.h")
     ]
 
@@ -38,7 +39,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if all(os.path.getmtime(s) <= t for s in sources()):
             return OUT
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-           "-shared", "-o", OUT + ".tmp", SRC]
+           "-shared", "-o", OUT + ".tmp", *SRCS]
     if verbose:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

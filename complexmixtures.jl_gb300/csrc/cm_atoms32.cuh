@@ -1,0 +1,468 @@
+// cm_atoms32.cuh -- ATOMS layout (molecules above 32 atoms): one warp per
+// (solute molecule, solvent molecule) pair that can hold a pair within the
+// cutoff.
+//
+// The solute atoms of each molecule are binned into a cell list; k_atoms_near
+// marks every cell within one stencil of an occupied cell ("near").  A solvent
+// molecule none of whose atoms sits in a near cell has every atom pair beyond
+// the cutoff and is dropped by k_atoms_filter (real pass) or by the placement
+// kernel (random insertion); the others go to a queue.  For dense solutes
+// (many atoms per occupied cell) k_atoms_eval takes one queue entry per warp:
+// for each solvent atom and stencil cell, the lanes read consecutive solute
+// atoms of the cell (coalesced) and keep their own top-2, and a shuffle
+// reduction gives the molecule pair's closest pair, second-closest distance
+// and reference-atom row; for sparse solutes one thread takes an entry.  Cells
+// whose box is farther than the cutoff from the atom are skipped.  The
+// decision follows the FP32 + guard rules; inside the guard band the exact
+// FP64 scan (warp-cooperative in warp mode, reduced in the order of the
+// reference's tie rule: distance, then the larger atom-index pair) decides.
+// The FP64 engine path runs that exact scan directly.
+#pragma once
+#include "cm_kernels.cuh"
+
+namespace cmk {
+
+constexpr int kAtomsWarps = 8;  // warps per CTA of k_atoms_eval
+
+// Dilated occupancy of each solute molecule's cell list: near = some cell
+// within the ATOMS stencil half-widths La holds an atom of the molecule.
+// Grid: x over ms * ncell, y = frame.
+__global__ void k_atoms_near(Bufs B) {
+    const int f = blockIdx.y;
+    const FrameGeom &G = B.G[f];
+    const FrameScratch &F = B.FS[f];
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)B.ms * G.ncell) return;
+    const int s = (int)(t / G.ncell), cell = (int)(t - (int64_t)s * G.ncell);
+    const int *cs = B.astart + (int64_t)f * B.as + (int64_t)s * G.ncell;
+    const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
+    const int cx = cell % n0, cy = (cell / n0) % n1, cz = cell / (n0 * n1);
+    unsigned char near = 0;
+    for (int dz = -F.La[2]; dz <= F.La[2] && !near; ++dz)
+        for (int dy = -F.La[1]; dy <= F.La[1] && !near; ++dy)
+            for (int dx = -F.La[0]; dx <= F.La[0]; ++dx) {
+                const int c = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                if (cs[c + 1] > cs[c]) {
+                    near = 1;
+                    break;
+                }
+            }
+    B.anear[(int64_t)f * B.as + t] = near;
+}
+
+__device__ __forceinline__ int unpack_cell_linear(const FrameGeom &G, int c) {
+    return ((c >> 20) * G.n[1] + ((c >> 10) & 1023)) * G.n[0] + (c & 1023);
+}
+
+// True if some atom of the solvent molecule at sites[0 .. apv) lies in a
+// near cell of solute molecule s.
+__device__ __forceinline__ bool atoms_near(const Bufs &B, const FrameGeom &G, int f, int s, const int *cells, int apv) {
+    const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)s * G.ncell;
+    for (int b = 0; b < apv; ++b)
+        if (nm[unpack_cell_linear(G, cells[b])]) return true;
+    return false;
+}
+
+__device__ __forceinline__ void atoms_push(const DevSys &S, const Bufs &B, int4 e) {
+    const int slot = atomicAdd(B.counters + 2, 1);
+    if (slot < B.aq_cap) B.aq[slot] = e;
+    else raise_err(S, ERR_QUEUE);
+}
+
+// Real pass filter, thread per (frame, solute molecule, solvent molecule)
+// item in [i0, i0 + n): queue entry (v, s, frame, 0).
+__global__ void k_atoms_filter(DevSys S, Bufs B, int64_t i0, int64_t n) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int64_t it = i0 + t;
+    const int64_t per_frame = B.ms * B.mv;
+    const int f = (int)(it / per_frame);
+    const int64_t r = it - (int64_t)f * per_frame;
+    const int s = (int)(r / B.mv), v = (int)(r - (int64_t)s * B.mv);
+    if (S.self && v == s) return;
+    if (!B.FS[f].ok) {
+        raise_err(S, ERR_STENCIL);
+        return;
+    }
+    const FrameGeom &G = B.G[f];
+    if (atoms_near(B, G, f, s, B.avcell + (int64_t)f * B.Nv + (int64_t)v * S.apv, S.apv)) atoms_push(S, B, make_int4(v, s, f, 0));
+}
+
+// FP32 top-2 of one lane.
+struct Top2 {
+    float m1, m2, r1;
+    int p1, b1;
+};
+
+__device__ __forceinline__ void top2_merge(Top2 &A, const Top2 &Bt) {
+    const float m2 = fminf(fmaxf(A.m1, Bt.m1), fminf(A.m2, Bt.m2));
+    const bool take = Bt.m1 < A.m1 || (Bt.m1 == A.m1 && (Bt.p1 < A.p1 || (Bt.p1 == A.p1 && Bt.b1 < A.b1)));
+    if (take) {
+        A.m1 = Bt.m1;
+        A.p1 = Bt.p1;
+        A.b1 = Bt.b1;
+    }
+    A.m2 = m2;
+    A.r1 = fminf(A.r1, Bt.r1);
+}
+
+__device__ __forceinline__ void top2_reduce(Top2 &T) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Top2 U;
+        U.m1 = __shfl_xor_sync(0xffffffffu, T.m1, o);
+        U.m2 = __shfl_xor_sync(0xffffffffu, T.m2, o);
+        U.r1 = __shfl_xor_sync(0xffffffffu, T.r1, o);
+        U.p1 = __shfl_xor_sync(0xffffffffu, T.p1, o);
+        U.b1 = __shfl_xor_sync(0xffffffffu, T.b1, o);
+        top2_merge(T, U);
+    }
+}
+
+// Exact minimum of one lane, reduced in the reference's order: smaller
+// distance first, then the larger (solute atom, solvent atom) index pair.
+__device__ __forceinline__ void best_reduce(Best64 &Bst, double &rr1, long long &evals) {
+    double d = Bst.d2 <= 1e300 ? best_d(Bst) : INFINITY;
+    int a = Bst.a, b = Bst.b;
+    double d2 = Bst.d2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double od = __shfl_xor_sync(0xffffffffu, d, o);
+        const double od2 = __shfl_xor_sync(0xffffffffu, d2, o);
+        const int oa = __shfl_xor_sync(0xffffffffu, a, o), ob = __shfl_xor_sync(0xffffffffu, b, o);
+        const bool take = od < d || (od == d && (oa > a || (oa == a && ob > b)));
+        if (take) {
+            d = od;
+            d2 = od2;
+            a = oa;
+            b = ob;
+        }
+        rr1 = fmin(rr1, __shfl_xor_sync(0xffffffffu, rr1, o));
+        evals += __shfl_xor_sync(0xffffffffu, evals, o);
+    }
+    Bst.d2 = d2;
+    Bst.d = d;
+    Bst.a = a;
+    Bst.b = b;
+}
+
+// Geometry of one solvent site for the stencil walk: its cell, its FP32
+// cell-relative position and its fractional position inside the cell.
+struct Site {
+    int cx, cy, cz;
+    float4 q;
+    float g[3];
+};
+
+__device__ __forceinline__ Site site_of(const FrameScratch &F, int packed, float4 q) {
+    Site st;
+    st.cx = packed & 1023;
+    st.cy = (packed >> 10) & 1023;
+    st.cz = (packed >> 20) & 1023;
+    st.q = q;
+    for (int k = 0; k < 3; ++k) st.g[k] = fmaf(F.hin[3 * k + 2], q.z, fmaf(F.hin[3 * k + 1], q.y, F.hin[3 * k] * q.x));
+    return st;
+}
+
+// Lower bound of the squared distance from the site to every atom of the
+// stencil cell image at offset d: per axis k the cell lies in a slab whose
+// distance from the site is (grid units outside the slab) x (cell width
+// between the faces).  Orthogonal cells: the slabs' distances add in
+// quadrature (the exact box distance); other cells: the largest of them.
+__device__ __forceinline__ float cell_d2(const FrameScratch &F, const Site &st, int dx, int dy, int dz) {
+    const float ux = (fminf(fmaxf(st.g[0], (float)dx), (float)dx + 1.f) - st.g[0]) * F.cw[0];
+    const float uy = (fminf(fmaxf(st.g[1], (float)dy), (float)dy + 1.f) - st.g[1]) * F.cw[1];
+    const float uz = (fminf(fmaxf(st.g[2], (float)dz), (float)dz + 1.f) - st.g[2]) * F.cw[2];
+    if (F.ortho) return fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+    const float m = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
+    return m * m;
+}
+
+// Walk the stencil cells of one site that can hold an atom within the
+// cutoff; body(beg, end, oi) for each non-empty one.
+template <typename Body>
+__device__ __forceinline__ void atoms_walk(const FrameGeom &G, const FrameScratch &F, const int *cs, const Site &st,
+                                           float prune2, Body &&body) {
+    const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
+    for (int dz = -F.La[2]; dz <= F.La[2]; ++dz) {
+        const int zc = wrapi(st.cz + dz, n2);
+        for (int dy = -F.La[1]; dy <= F.La[1]; ++dy) {
+            const int row = (zc * n1 + wrapi(st.cy + dy, n1)) * n0;
+            for (int dx = -F.La[0]; dx <= F.La[0]; ++dx) {
+                const int cell = row + wrapi(st.cx + dx, n0);
+                const int beg = cs[cell], end = cs[cell + 1];
+                if (beg == end) continue;
+                if (cell_d2(F, st, dx, dy, dz) > prune2) continue;
+                body(beg, end, off_index(dx, dy, dz));
+            }
+        }
+    }
+}
+
+// What the exact scan of one queued molecule pair reads.
+struct AtomsPair {
+    const FrameGeom *G;
+    const FrameScratch *F;
+    const int *vcell;
+    const float4 *vq32;
+    const d4 *vq64;
+    const d4 *off64;
+    const float4 *off32;
+    const float4 *sq32;
+    const d4 *sq64;
+    const int *cs;
+    int64_t vb;
+    float prune2;
+};
+
+// Exact scan of a molecule pair; STRIDE 32: lanes over the atoms of each cell
+// (the whole warp calls it, the result is reduced over the lanes); STRIDE 1:
+// one thread.  With `filter` only pairs whose FP32 squared distance is within
+// the thresholds are evaluated in FP64.  Out of line: it runs only in
+// the FP64 engine path and for records inside the guard band, and keeps its
+// registers away from the FP32 loop.
+template <int STRIDE>
+__device__ __noinline__ void atoms_exact(const DevSys &S, const AtomsPair &A, int lane, bool filter, float thr_arg,
+                                         float thr_r1, Best64 &Bst, double &rr1, long long &evals) {
+    best_init(Bst);
+    rr1 = INFINITY;
+    evals = 0;
+    const int apv = S.apv, iref = S.iref;
+    for (int b = 0; b < apv; ++b) {
+        const Site sb = site_of(*A.F, A.vcell[A.vb + b], A.vq32[A.vb + b]);
+        const d4 qb = A.vq64[A.vb + b];
+        atoms_walk(*A.G, *A.F, A.cs, sb, A.prune2, [&](int beg, int end, int oi) {
+            const d4 o = A.off64[oi];
+            const double tx = sub(qb.x, o.x), ty = sub(qb.y, o.y), tz = sub(qb.z, o.z);
+            const float4 of = A.off32[oi];
+            const float fx = sb.q.x - of.x, fy = sb.q.y - of.y, fz = sb.q.z - of.z;
+            for (int p = beg + lane; p < end; p += STRIDE) {
+                const float4 qa32 = A.sq32[p];
+                if (filter) {
+                    const float ex = qa32.x - fx, ey = qa32.y - fy, ez = qa32.z - fz;
+                    const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                    if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1))) continue;
+                }
+                const d4 qa = A.sq64[p];
+                const double d2 = pair_d2_64(tx, ty, tz, qa.x, qa.y, qa.z);
+                evals++;
+                if (d2 <= S.cut2) {
+                    if (b == iref) rr1 = fmin(rr1, d2);
+                    best_update<false>(Bst, d2, __float_as_int(qa32.w), b);
+                }
+            }
+        });
+    }
+    if (STRIDE == 32) best_reduce(Bst, rr1, evals);
+}
+
+// ATOMS evaluation of the queue (persistent grid): one warp per entry for
+// dense solutes (many atoms per cell), one thread per entry for sparse ones.
+template <bool FP32, bool RANDOM, bool WARP>
+__global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bufs B) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    shist_zero(S, hbase);
+    __syncthreads();
+    SHist h = shist_bind(S, hbase);
+    LocalStats st;
+    // WARP: one warp per queue entry, lanes over the atoms of each cell;
+    // otherwise one thread per entry (lane 0 of a one-thread "warp")
+    constexpr int STRIDE = WARP ? 32 : 1;
+    const int lane = WARP ? (threadIdx.x & 31) : 0;
+    const int worker = WARP ? (threadIdx.x >> 5) : threadIdx.x;
+    const int per_block = WARP ? kAtomsWarps : kAtomsWarps * 32;
+    const int n = min(B.counters[2], B.aq_cap);
+    const int apv = S.apv, iref = S.iref;
+    for (int it = blockIdx.x * per_block + worker; it < n; it += gridDim.x * per_block) {
+        const int4 e = B.aq[it];
+        int v, s, f;
+        const int *vcell;
+        const float4 *vq32;
+        const d4 *vq64;
+        if (RANDOM) {
+            const Sample sm = B.samples[e.z];
+            v = e.x;
+            s = sm.s;
+            f = sm.pad;
+            vcell = B.pcell + (int64_t)e.y * B.Nv;
+            vq32 = B.pq32 + (int64_t)e.y * B.Nv;
+            vq64 = B.pq64 + (int64_t)e.y * B.Nv;
+        } else {
+            v = e.x;
+            s = e.y;
+            f = e.z;
+            vcell = B.avcell + (int64_t)f * B.Nv;
+            vq32 = B.avq32 + (int64_t)f * B.Nv;
+            vq64 = B.avq64 + (int64_t)f * B.Nv;
+        }
+        const FrameGeom &G = B.G[f];
+        const FrameScratch &F = B.FS[f];
+        const Guard g = F.g;
+        const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
+        const float4 *off32 = B.off32 + (int64_t)f * kOffEntries;
+        const float4 *sq32 = B.asq32 + (int64_t)f * B.Ns;
+        const d4 *sq64 = B.asq64 + (int64_t)f * B.Ns;
+        const int *cs = B.astart + (int64_t)f * B.as + (int64_t)s * G.ncell;
+        const float prune2 = g.cut_pre * g.cut_pre;
+        const int64_t vb = (int64_t)v * apv;
+
+        AtomsPair A;
+        A.G = &G;
+        A.F = &F;
+        A.vcell = vcell;
+        A.vq32 = vq32;
+        A.vq64 = vq64;
+        A.off64 = off64;
+        A.off32 = off32;
+        A.sq32 = sq32;
+        A.sq64 = sq64;
+        A.cs = cs;
+        A.vb = vb;
+        A.prune2 = prune2;
+        auto exact = [&](bool filter, float thr_arg, float thr_r1, Best64 &Bst, double &rr1, long long &evals) {
+            atoms_exact<STRIDE>(S, A, lane, filter, thr_arg, thr_r1, Bst, rr1, evals);
+        };
+        auto from_exact = [&](Best64 &Bst, double rr1) {
+            DirRec q = dir_none(S);
+            if (Bst.d2 <= S.cut2) {
+                const double d = best_d(Bst);
+                q.within = 1;
+                q.i_local = Bst.a;
+                q.j = vb + Bst.b;
+                q.bin = setbin0(d, S.binstep);
+                q.bulk = inbulk64(S, true, d);
+                if (rr1 <= S.cut2) { q.ref = 1; q.rbin = setbin0(sqrt(rr1), S.binstep); }
+            }
+            return q;
+        };
+        DirRec r = dir_none(S);
+        long long lane_evals = 0;
+        if (!FP32) {
+            Best64 Bst;
+            double rr1;
+            exact(false, 0.f, 0.f, Bst, rr1, lane_evals);
+            r = from_exact(Bst, rr1);
+            if (lane != 0) lane_evals = 0;  // the reduction left the total in every lane
+        } else {
+            Top2 T;
+            T.m1 = T.m2 = T.r1 = INFINITY;
+            T.p1 = 0x7fffffff;
+            T.b1 = 0;
+            for (int b = 0; b < apv; ++b) {
+                const Site sb = site_of(F, vcell[vb + b], vq32[vb + b]);
+                const bool isref = b == iref;
+                atoms_walk(G, F, cs, sb, prune2, [&](int beg, int end, int oi) {
+                    const float4 of = off32[oi];
+                    const float tx = sb.q.x - of.x, ty = sb.q.y - of.y, tz = sb.q.z - of.z;
+                    for (int p = beg + lane; p < end; p += STRIDE) {
+                        lane_evals++;
+                        const float4 qa = sq32[p];
+                        const float ex = qa.x - tx, ey = qa.y - ty, ez = qa.z - tz;
+                        const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                        T.m2 = fminf(T.m2, fmaxf(T.m1, d2));
+                        const bool lt = d2 < T.m1;
+                        T.p1 = lt ? p : T.p1;
+                        T.b1 = lt ? b : T.b1;
+                        T.m1 = fminf(T.m1, d2);
+                        if (isref) T.r1 = fminf(T.r1, d2);
+                    }
+                });
+            }
+            if (WARP) top2_reduce(T);
+            if (T.m1 <= g.cutp2) {
+                const float d1 = sqrtf(T.m1);
+                const bool amb = T.m1 >= g.cutm2 || (sqrtf(T.m2) - d1) <= g.two_delta;
+                if (amb) {
+                    const float t = d1 + g.two_delta;
+                    float thr1 = -1.f;
+                    if (T.r1 <= g.cutp2) {
+                        const float u = sqrtf(T.r1) + g.two_delta;
+                        thr1 = __fmul_ru(u, u);
+                    }
+                    Best64 Bst;
+                    double rr1;
+                    long long ev;
+                    exact(true, __fmul_ru(t, t), thr1, Bst, rr1, ev);
+                    r = from_exact(Bst, rr1);
+                    if (lane == 0) {
+                        st.guard++;
+                        st.guard_pairs += ev;
+                        if (Bst.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(Bst)));
+                    }
+                } else {
+                    int bin = bin32(g, d1);
+                    double d64 = -1.0;
+                    const float4 qa32 = sq32[T.p1];
+                    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
+                        // exact distance of the minimum pair over the stencil
+                        // images that hold its solute atom
+                        const int pk = vcell[vb + T.b1];
+                        const int cx = pk & 1023, cy = (pk >> 10) & 1023, cz = (pk >> 20) & 1023;
+                        const d4 qb = vq64[vb + T.b1];
+                        const d4 qa = sq64[T.p1];
+                        double best = INFINITY;
+                        for (int dz = -F.La[2]; dz <= F.La[2]; ++dz)
+                            for (int dy = -F.La[1]; dy <= F.La[1]; ++dy)
+                                for (int dx = -F.La[0]; dx <= F.La[0]; ++dx) {
+                                    const int cell = (wrapi(cz + dz, G.n[2]) * G.n[1] + wrapi(cy + dy, G.n[1])) * G.n[0] +
+                                                     wrapi(cx + dx, G.n[0]);
+                                    if (T.p1 < cs[cell] || T.p1 >= cs[cell + 1]) continue;
+                                    const d4 o = off64[off_index(dx, dy, dz)];
+                                    best = fmin(best, pair_d2_64(sub(qb.x, o.x), sub(qb.y, o.y), sub(qb.z, o.z), qa.x, qa.y,
+                                                                 qa.z));
+                                }
+                        d64 = sqrt(best);
+                        bin = setbin0(d64, S.binstep);
+                        if (lane == 0) {
+                            st.guard++;
+                            st.guard_pairs++;
+                            st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
+                        }
+                    }
+                    r.within = 1;
+                    r.i_local = __float_as_int(qa32.w);
+                    r.j = vb + T.b1;
+                    r.bin = bin;
+                    r.bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
+                    if (T.r1 <= g.cutp2) {
+                        const int rb = T.r1 < g.cutm2 ? bin32(g, sqrtf(T.r1)) : -1;
+                        if (rb >= 0) {
+                            r.ref = 1;
+                            r.rbin = rb;
+                        } else {
+                            const float u = sqrtf(T.r1) + g.two_delta;
+                            Best64 Bst;
+                            double rr1;
+                            long long ev;
+                            exact(true, -1.f, __fmul_ru(u, u), Bst, rr1, ev);
+                            if (lane == 0) {
+                                st.guard++;
+                                st.guard_pairs += ev;
+                            }
+                            if (rr1 <= S.cut2) { r.ref = 1; r.rbin = setbin0(sqrt(rr1), S.binstep); }
+                        }
+                    }
+                }
+            }
+        }
+        st.atompairs += (unsigned long long)lane_evals;
+        if (lane == 0) {
+            st.molpairs++;
+            if (r.within) {
+                apply_hit(S, h, RANDOM, r.bin, r.i_local, r.j, r.ref, r.rbin);
+                st.hits++;
+                if (!RANDOM && B.slot) {
+                    const int sl = B.slot[(int64_t)f * B.ms + s];
+                    if (sl >= 0) B.flags[((int64_t)f * B.ndist + sl) * S.mv + v] = flag_code(r);
+                }
+            }
+        }
+        if (WARP) __syncwarp();
+    }
+    stats_flush(S, st, RANDOM);
+    __syncthreads();
+    shist_flush(S, h, RANDOM);
+}
+
+}  // namespace cmk

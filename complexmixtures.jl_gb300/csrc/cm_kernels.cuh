@@ -100,8 +100,9 @@ struct FrameScratch {
     float rmax_s;   // largest solute molecule radius (PAIRS: about the centroid)
     float rmax_v;   // largest solvent molecule radius
     float rcmax;    // largest solvent centroid radius (ATOMS layout)
-    int gq_count;   // candidates deferred to the guard kernel
-    int rq_count;   // random-insertion slots that reach the sampled solute molecule
+    float hin[9];   // n_k * (H^-1 row k): cell-relative position -> grid units in the cell (FP32)
+    float cw[3];    // cell widths between opposite faces (FP32)
+    int ortho;      // cell axes orthogonal (H/n diagonal)
     int ok;         // stencils fit the offset table
     int L[3];       // PAIRS stencil half-widths
     int multi;      // PAIRS axes with several images (bit k set for axis k)
@@ -193,18 +194,22 @@ __device__ __forceinline__ void credit_solute(const DevSys &S, const SHist &h, b
 
 // The solvent-side atom, identified by its index in the whole selection; in
 // self mode it credits the solute table (src/update_counters.jl:272-277).
-__device__ __forceinline__ void credit_solvent(const DevSys &S, const SHist &h, bool rnd, int64_t j, int bin, unsigned inc) {
+// j_local is the atom's index within its molecule.
+__device__ __forceinline__ void credit_solvent(const DevSys &S, const SHist &h, bool rnd, int64_t j, int j_local, int bin,
+                                               unsigned inc) {
     bool to_solvent = !S.self;
     if (S.default_v) {
-        add_group(S, h, rnd, to_solvent, (int)(j % S.apv), bin, inc);
+        add_group(S, h, rnd, to_solvent, j_local, bin, inc);
     } else {
         for (int64_t p = S.gv_off[j]; p < S.gv_off[j + 1]; ++p) add_group(S, h, rnd, to_solvent, S.gv_idx[p], bin, inc);
     }
 }
 
 // One within-cutoff record of the reference's list, binned (update_counters!).
-__device__ __forceinline__ void apply_hit(const DevSys &S, const SHist &h, bool rnd, int bin, int i_local, int64_t j, bool ref,
-                                          int rbin) {
+// j is the solvent atom's index in the selection, j_local its index within
+// its molecule.
+__device__ __forceinline__ void apply_hit_local(const DevSys &S, const SHist &h, bool rnd, int bin, int i_local, int64_t j,
+                                                int j_local, bool ref, int rbin) {
     if (bin < 0 || bin >= S.nbins || (ref && (rbin < 0 || rbin >= S.nbins))) {
         raise_err(S, ERR_BIN);
         return;
@@ -212,12 +217,17 @@ __device__ __forceinline__ void apply_hit(const DevSys &S, const SHist &h, bool 
     atomicAdd(h.md + bin, 2u);
     if (S.self) {
         credit_solute(S, h, rnd, i_local, bin, 1u);
-        credit_solvent(S, h, rnd, j, bin, 1u);
+        credit_solvent(S, h, rnd, j, j_local, bin, 1u);
     } else {
         credit_solute(S, h, rnd, i_local, bin, 2u);
-        credit_solvent(S, h, rnd, j, bin, 2u);
+        credit_solvent(S, h, rnd, j, j_local, bin, 2u);
     }
     if (ref) atomicAdd(h.rdf + rbin, 2u);
+}
+
+__device__ __forceinline__ void apply_hit(const DevSys &S, const SHist &h, bool rnd, int bin, int i_local, int64_t j, bool ref,
+                                          int rbin) {
+    apply_hit_local(S, h, rnd, bin, i_local, j, (int)j % S.apv, ref, rbin);
 }
 
 // Warp-aggregated statistics counters.
@@ -646,6 +656,7 @@ struct Bufs {
     int *ccount, *cstart, *cfill;   // [nf][cs]
     int64_t cs;
     int *cmol;                      // [nf][mv]
+    float4 *cq32;                   // [nf][mv] molecule table (FP32 centroid, radius) in cell order
     // random insertion
     int *slot;                      // [nf][ms], -1 where not sampled
     unsigned char *flags;           // [nf][ndist][mv]
@@ -672,6 +683,9 @@ struct Bufs {
     int *pcell;                     // [placed samples][Nv]
     float4 *pq32;
     d4 *pq64;
+    unsigned char *anear;           // [nf][as] cells within a stencil of a solute molecule's atoms
+    int4 *aq;                       // ATOMS work queue; count in counters[2]
+    int aq_cap;
 };
 
 // Per-frame offset tables: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
@@ -809,6 +823,7 @@ __global__ void k_scatter_mols(Bufs B, int self) {
     const int *mcell = (self ? B.scell : B.vcell) + (int64_t)f * B.mv;
     const int p = atomicAdd(B.cfill + (int64_t)f * B.cs + mcell[m], 1);
     B.cmol[(int64_t)f * B.mv + p] = m;
+    B.cq32[(int64_t)f * B.mv + p] = (self ? B.sq32 : B.vq32)[(int64_t)f * B.mv + m];
 }
 
 // Images of a PAIRS candidate from its packed stencil offset.
@@ -1220,9 +1235,10 @@ __global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
 // with u = 2^-24 each component is within u times the sum of the magnitudes of
 // the inputs and intermediate results of its exact value:
 //   |q| <= Q (a site inside its cell), |off| <= OFF (stencil offsets),
-//   |o| <= r (molecule radii), |q_v - q_s| <= Q, |D| <= Q + OFF,
-//   |t| <= Q + OFF + r_v, |dx| <= cutoff,
-// giving E = u (5Q + 3 OFF + 2 r_v + r_s + cutoff).  The distance is within
+//   |o| <= r (molecule radii), |q_v - q_s| <= Q, |off - q_s| <= Q + OFF,
+//   |D| <= Q + OFF, |t| <= Q + OFF + r_v, |dx| <= cutoff,
+// and D formed either as (q_v - q_s) + off or as q_v + (off - q_s), giving
+// E = u (5Q + 4 OFF + 2 r_v + r_s + cutoff).  The distance is within
 // sqrt(3) E plus 2.5 u d (three roundings of d^2, one of the square root).  The
 // atom-cell layout's displacement (q_a - (q_b - off)) is bounded by the same
 // expression with r = 0.  delta adds 25 % to the bound.
@@ -1241,6 +1257,12 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
     __shared__ int Ls[6];
     __shared__ double radii[2];
     if (lane == 0) {
+        for (int k = 0; k < 3; ++k) {
+            for (int m = 0; m < 3; ++m) F.hin[3 * k + m] = (float)(G.Hi[3 * k + m] * (double)G.n[k]);
+            F.cw[k] = (float)G.cw[k];
+        }
+        F.ortho = (G.Hn[1] == 0.0 && G.Hn[2] == 0.0 && G.Hn[3] == 0.0 && G.Hn[5] == 0.0 && G.Hn[6] == 0.0 &&
+                   G.Hn[7] == 0.0) ? 1 : 0;
         double rs = F.rmax_s, rv = S.self ? F.rmax_s : F.rmax_v;
         if (!pairs) rs = rv = 0.0;
         radii[0] = rs;
@@ -1280,7 +1302,7 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
     const double rs = radii[0], rv = radii[1];
     const double range = S.cut + rs + rv;
     const double u = 0x1.0p-24;
-    const double E = u * (5.0 * Q + 3.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
+    const double E = u * (5.0 * Q + 4.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
     const double delta = 1.25 * (1.7320508075688772 * E + 2.5 * u * (S.cut + 1.0)) + 1e-9;
     Guard g;
     g.delta = delta;
@@ -1399,7 +1421,8 @@ __global__ void k_scatter_atoms(Bufs B) {
 
 // Placed solvent for the ATOMS regime: every slot of samples sample0 ..
 // sample0 + gridDim.y - 1 of the chunk, absolute FP64 positions A u + centre,
-// binned per atom.
+// binned per atom; slots that can reach the solute molecule are queued for
+// k_atoms_warp (the near mask of k_atoms_near must be built).
 __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= S.mv) return;
@@ -1431,240 +1454,19 @@ __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
         B.pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
         B.pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
     }
-}
-
-// FP32 pass of one solvent molecule against one solute molecule's atom cells.
-struct AtomPass {
-    float m1, m2;
-    int p1, b1;   // sorted position of the solute atom, solvent atom index
-    float r1;     // row minimum of the reference atom
-};
-
-// ATOMS evaluation: thread per solvent molecule v.  Real pass: grid y =
-// frame * ms + solute molecule.  Random pass: grid y = placed sample (of
-// samples sample0 ..), solvent sites from the placed buffers.
-template <bool FP32, bool RANDOM>
-__global__ void __launch_bounds__(128) k_atoms_eval(DevSys S, Bufs B, int sample0) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    unsigned int *hbase = (unsigned int *)smem_raw;
-    shist_zero(S, hbase);
-    __syncthreads();
-    SHist h = shist_bind(S, hbase);
-    LocalStats st;
-    int s, f;
-    const int *vcell;
-    const float4 *vq32;
-    const d4 *vq64;
-    if (RANDOM) {
-        const Sample sm = B.samples[sample0 + blockIdx.y];
-        s = sm.s;
-        f = sm.pad;
-        vcell = B.pcell + (int64_t)blockIdx.y * B.Nv;
-        vq32 = B.pq32 + (int64_t)blockIdx.y * B.Nv;
-        vq64 = B.pq64 + (int64_t)blockIdx.y * B.Nv;
-    } else {
-        f = (int)(blockIdx.y / B.ms);
-        s = (int)(blockIdx.y - (int64_t)f * B.ms);
-        vcell = B.avcell + (int64_t)f * B.Nv;
-        vq32 = B.avq32 + (int64_t)f * B.Nv;
-        vq64 = B.avq64 + (int64_t)f * B.Nv;
+    // queue the slot if one of its atoms lies in a near cell of the solute
+    // molecule: (slot, placed sample, sample, 1)
+    const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
+    bool near = false;
+    for (int b = 0; b < S.apv && !near; ++b) {
+        const int pc = B.pcell[base + b];
+        near = nm[((pc >> 20) * G.n[1] + ((pc >> 10) & 1023)) * G.n[0] + (pc & 1023)] != 0;
     }
-    const FrameGeom &G = B.G[f];
-    const FrameScratch &F = B.FS[f];
-    const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
-    const float4 *off32 = B.off32 + (int64_t)f * kOffEntries;
-    const float4 *sq32 = B.asq32 + (int64_t)f * B.Ns;
-    const d4 *sq64 = B.asq64 + (int64_t)f * B.Ns;
-    const int L[3] = {F.La[0], F.La[1], F.La[2]};
-    const bool ok = F.ok;
-    const Guard g = F.g;
-    const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    const int *cs = B.astart + (int64_t)f * B.as + (int64_t)s * G.ncell;
-    if (!ok) {
-        if (threadIdx.x == 0) raise_err(S, ERR_STENCIL);
-    } else if (v < S.mv && !(S.self && v == s)) {
-        const int apv = S.apv, iref = S.iref;
-        DirRec r = dir_none(S);
-        auto cells_of = [&](int b, int &cx, int &cy, int &cz) {
-            const int c = vcell[(int64_t)v * apv + b];
-            cx = c & 1023; cy = (c >> 10) & 1023; cz = (c >> 20) & 1023;
-        };
-        // exact (FP64) scan; with `filter` only pairs whose FP32 squared
-        // distance is within the thresholds are evaluated in FP64
-        auto exact = [&](bool filter, float thr_arg, float thr_r1, Best64 &Bst, double &rr1, long long &evals) {
-            best_init(Bst);
-            rr1 = INFINITY;
-            evals = 0;
-            for (int b = 0; b < apv; ++b) {
-                int cx, cy, cz;
-                cells_of(b, cx, cy, cz);
-                const d4 qb = vq64[(int64_t)v * apv + b];
-                const float4 qf = vq32[(int64_t)v * apv + b];
-                for (int dz = -L[2]; dz <= L[2]; ++dz)
-                    for (int dy = -L[1]; dy <= L[1]; ++dy)
-                        for (int dx = -L[0]; dx <= L[0]; ++dx) {
-                            const int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
-                            const int beg = cs[cell], end = cs[cell + 1];
-                            if (beg == end) continue;
-                            const int oi = off_index(dx, dy, dz);
-                            const d4 o = off64[oi];
-                            const double tx = sub(qb.x, o.x), ty = sub(qb.y, o.y), tz = sub(qb.z, o.z);
-                            const float4 of = off32[oi];
-                            const float fx = qf.x - of.x, fy = qf.y - of.y, fz = qf.z - of.z;
-                            for (int p = beg; p < end; ++p) {
-                                const float4 qa32 = sq32[p];
-                                if (filter) {
-                                    const float ex = qa32.x - fx, ey = qa32.y - fy, ez = qa32.z - fz;
-                                    const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                                    if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1))) continue;
-                                }
-                                const d4 qa = sq64[p];
-                                // displacement solute atom -> solvent atom: (q_b - off) - q_a
-                                const double d2 = pair_d2_64(tx, ty, tz, qa.x, qa.y, qa.z);
-                                evals++;
-                                if (d2 <= S.cut2) {
-                                    if (b == iref) rr1 = fmin(rr1, d2);
-                                    best_update<false>(Bst, d2, __float_as_int(qa32.w), b);
-                                }
-                            }
-                        }
-            }
-        };
-        auto from_exact = [&](Best64 &Bst, double rr1) {
-            DirRec q = dir_none(S);
-            if (Bst.d2 <= S.cut2) {
-                const double d = best_d(Bst);
-                q.within = 1;
-                q.i_local = Bst.a;
-                q.j = (int64_t)v * apv + Bst.b;
-                q.bin = setbin0(d, S.binstep);
-                q.bulk = inbulk64(S, true, d);
-                if (rr1 <= S.cut2) { q.ref = 1; q.rbin = setbin0(sqrt(rr1), S.binstep); }
-            }
-            return q;
-        };
-        if (!FP32) {
-            Best64 Bst;
-            double rr1;
-            long long ev;
-            exact(false, 0.f, 0.f, Bst, rr1, ev);
-            st.atompairs += ev;
-            r = from_exact(Bst, rr1);
-        } else {
-            AtomPass P;
-            P.m1 = P.m2 = P.r1 = INFINITY;
-            P.p1 = 0;
-            P.b1 = 0;
-            long long evals = 0;
-            for (int b = 0; b < apv; ++b) {
-                int cx, cy, cz;
-                cells_of(b, cx, cy, cz);
-                const float4 qf = vq32[(int64_t)v * apv + b];
-                const bool isref = b == iref;
-                for (int dz = -L[2]; dz <= L[2]; ++dz)
-                    for (int dy = -L[1]; dy <= L[1]; ++dy)
-                        for (int dx = -L[0]; dx <= L[0]; ++dx) {
-                            const int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
-                            const int beg = cs[cell], end = cs[cell + 1];
-                            if (beg == end) continue;
-                            const float4 of = off32[off_index(dx, dy, dz)];
-                            const float tx = qf.x - of.x, ty = qf.y - of.y, tz = qf.z - of.z;
-                            evals += end - beg;
-                            float row = P.r1;
-                            for (int p = beg; p < end; ++p) {
-                                const float4 qa = sq32[p];
-                                const float ex = qa.x - tx, ey = qa.y - ty, ez = qa.z - tz;
-                                const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                                P.m2 = fminf(P.m2, fmaxf(P.m1, d2));
-                                const bool lt = d2 < P.m1;
-                                P.p1 = lt ? p : P.p1;
-                                P.b1 = lt ? b : P.b1;
-                                P.m1 = fminf(P.m1, d2);
-                                row = fminf(row, d2);
-                            }
-                            if (isref) P.r1 = row;
-                        }
-            }
-            st.atompairs += evals;
-            if (P.m1 <= g.cutp2) {
-                const float d1 = sqrtf(P.m1);
-                const bool amb = P.m1 >= g.cutm2 || (sqrtf(P.m2) - d1) <= g.two_delta;
-                if (amb) {
-                    const float t = d1 + g.two_delta;
-                    float thr1 = -1.f;
-                    if (P.r1 <= g.cutp2) {
-                        const float u = sqrtf(P.r1) + g.two_delta;
-                        thr1 = __fmul_ru(u, u);
-                    }
-                    Best64 Bst;
-                    double rr1;
-                    long long ev;
-                    exact(true, __fmul_ru(t, t), thr1, Bst, rr1, ev);
-                    r = from_exact(Bst, rr1);
-                    st.guard++;
-                    st.guard_pairs += ev;
-                    if (Bst.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(Bst)));
-                } else {
-                    int bin = bin32(g, d1);
-                    double d64 = -1.0;
-                    const float4 qa32 = sq32[P.p1];
-                    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
-                        // exact distance of the minimum pair over the stencil images
-                        // that contain its solute atom
-                        int cx, cy, cz;
-                        cells_of(P.b1, cx, cy, cz);
-                        const d4 qb = vq64[(int64_t)v * apv + P.b1];
-                        const d4 qa = sq64[P.p1];
-                        double best = INFINITY;
-                        for (int dz = -L[2]; dz <= L[2]; ++dz)
-                            for (int dy = -L[1]; dy <= L[1]; ++dy)
-                                for (int dx = -L[0]; dx <= L[0]; ++dx) {
-                                    const int cell = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
-                                    if (P.p1 < cs[cell] || P.p1 >= cs[cell + 1]) continue;
-                                    const d4 o = off64[off_index(dx, dy, dz)];
-                                    best = fmin(best, pair_d2_64(sub(qb.x, o.x), sub(qb.y, o.y), sub(qb.z, o.z), qa.x, qa.y, qa.z));
-                                }
-                        d64 = sqrt(best);
-                        bin = setbin0(d64, S.binstep);
-                        st.guard++;
-                        st.guard_pairs++;
-                        st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
-                    }
-                    r.within = 1;
-                    r.i_local = __float_as_int(qa32.w);
-                    r.j = (int64_t)v * apv + P.b1;
-                    r.bin = bin;
-                    r.bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
-                    if (P.r1 <= g.cutp2) {
-                        const int rb = P.r1 < g.cutm2 ? bin32(g, sqrtf(P.r1)) : -1;
-                        if (rb >= 0) {
-                            r.ref = 1;
-                            r.rbin = rb;
-                        } else {
-                            const float u = sqrtf(P.r1) + g.two_delta;
-                            Best64 Bst;
-                            double rr1;
-                            long long ev;
-                            exact(true, -1.f, __fmul_ru(u, u), Bst, rr1, ev);
-                            st.guard++;
-                            st.guard_pairs += ev;
-                            if (rr1 <= S.cut2) { r.ref = 1; r.rbin = setbin0(sqrt(rr1), S.binstep); }
-                        }
-                    }
-                }
-            }
-        }
-        st.molpairs++;
-        if (r.within) { apply_hit(S, h, RANDOM, r.bin, r.i_local, r.j, r.ref, r.rbin); st.hits++; }
-        if (!RANDOM && B.slot) {
-            const int sl = B.slot[(int64_t)f * B.ms + s];
-            if (sl >= 0) B.flags[((int64_t)f * B.ndist + sl) * S.mv + v] = flag_code(r);
-        }
+    if (near) {
+        const int slot = atomicAdd(B.counters + 2, 1);
+        if (slot < B.aq_cap) B.aq[slot] = make_int4(k, (int)blockIdx.y, sample0 + (int)blockIdx.y, 1);
+        else raise_err(S, ERR_QUEUE);
     }
-    stats_flush(S, st, RANDOM);
-    __syncthreads();
-    shist_flush(S, h, RANDOM);
 }
 
 // Weight change: fold the integer class accumulators into FP64 sums

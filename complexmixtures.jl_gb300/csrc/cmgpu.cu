@@ -22,7 +22,8 @@
 
 #include "../../include/cmgpu.h"
 #include "cm_kernels.cuh"
-#include "cm_pairs32.cuh"
+#include "cm_atoms32.cuh"
+#include "cm_flat32.cuh"
 
 using namespace cmk;
 using cmgeom::FrameGeom;
@@ -82,12 +83,18 @@ struct cm_handle {
     DevBuf geoms, samples, tabs, fscratch, off64, off32, hist, sums, stats, errflag, counters, slot, flags, bulk, nbulk;
     DevBuf stage_s[2], stage_v[2];
     // PAIRS
-    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, ccount, cstart, cfill, cmol, gq, rq;
+    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, ccount, cstart, cfill, cmol, cq32, gq, rq;
     int gq_cap = 0, rq_cap = 0;
+    int flat_ctas = 0;  // resident CTAs per SM of k_pairs_flat32
     // group tables
     DevBuf g_soff, g_sidx, g_voff, g_vidx;
     // ATOMS
-    DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, u64, rc, pcell, pq32, pq64;
+    DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, u64, rc, pcell, pq32, pq64,
+        anear, aq;
+    int aq_cap = 0;
+    int atoms_ctas = 0;    // resident CTAs per SM of k_atoms_eval
+    bool atoms_warp = true; // ATOMS evaluation: one warp (dense solutes) or one thread per queued pair
+    int atoms_piece = 0;   // samples placed per random-insertion launch
     // pinned host staging
     FrameGeom *h_geoms[2] = {nullptr, nullptr};
     Sample *h_samples[2] = {nullptr, nullptr};
@@ -234,6 +241,8 @@ void check_desc(const cm_system_desc *d) {
     if (d->precision != CM_PRECISION_FP64 && d->precision != CM_PRECISION_FP32_GUARD) bad("unknown precision");
     if (d->regime < CM_REGIME_AUTO || d->regime > CM_REGIME_ATOMS) bad("unknown regime");
     if (d->lcell < 1) bad("lcell must be >= 1");
+    if (d->cell_scale_pct != 0 && (d->cell_scale_pct < 30 || d->cell_scale_pct > 300))
+        bad("cell_scale_pct must be 0 or within 30-300");
     int64_t Nv = (int64_t)d->solvent_nmols * d->solvent_natomspermol;
     int64_t Ns = (int64_t)d->solute_nmols * d->solute_natomspermol;
     if (Ns >= (1LL << 31) || Nv >= (1LL << 31)) bad("selections above 2^31 atoms are not supported");
@@ -327,10 +336,171 @@ void upload_groups(cm_handle *h) {
     }
 }
 
+// Search-cell side: PAIRS the molecule cell (cutoff + both radii, with a
+// margin), ATOMS cutoff / lcell; both scaled by cell_scale_pct.
 double target_cell(const cm_handle *h) {
     double cut = h->d.usecutoff ? h->d.cutoff : h->d.dbulk;
-    if (h->regime == CM_REGIME_ATOMS) return cut / h->d.lcell * (1.0 + 1e-6);
-    return h->pair_cell;
+    const double scale = (h->d.cell_scale_pct > 0 ? h->d.cell_scale_pct : 100) / 100.0;
+    if (h->regime == CM_REGIME_ATOMS) return cut / h->d.lcell * (1.0 + 1e-6) * scale;
+    return h->pair_cell * scale;
+}
+
+// Per-CTA shared memory of the PAIRS real-pass kernels beyond the histograms.
+size_t pairs_extra_smem() {
+    const size_t real = (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
+    const size_t flat = (size_t)kFlatWarps * flat_warp_smem();
+    return std::max(real, flat);
+}
+
+// The FP32 real-pass kernel for a system: specialised on the solute molecule
+// size for the common sizes, generic otherwise.
+using FlatLaunch = void (*)(int, size_t, cudaStream_t, const DevSys &, const Bufs &);
+struct FlatKernel {
+    const void *fn;
+    FlatLaunch launch;
+};
+
+template <bool SELF, int APS>
+void launch_flat(int grid, size_t smem, cudaStream_t st, const DevSys &S, const Bufs &B) {
+    k_pairs_flat32<SELF, APS><<<grid, kFlatWarps * 32, smem, st>>>(S, B);
+}
+
+template <bool SELF>
+FlatKernel flat_kernel_of(int aps) {
+    switch (aps) {
+        case 1: return {(const void *)k_pairs_flat32<SELF, 1>, launch_flat<SELF, 1>};
+        case 3: return {(const void *)k_pairs_flat32<SELF, 3>, launch_flat<SELF, 3>};
+        case 4: return {(const void *)k_pairs_flat32<SELF, 4>, launch_flat<SELF, 4>};
+        case 5: return {(const void *)k_pairs_flat32<SELF, 5>, launch_flat<SELF, 5>};
+        case 14: return {(const void *)k_pairs_flat32<SELF, 14>, launch_flat<SELF, 14>};
+        default: return {(const void *)k_pairs_flat32<SELF, 0>, launch_flat<SELF, 0>};
+    }
+}
+
+FlatKernel flat_kernel(const cm_handle *h) {
+    return h->d.autocorrelation ? flat_kernel_of<true>(h->d.solute_natomspermol)
+                                : flat_kernel_of<false>(h->d.solute_natomspermol);
+}
+
+// The dynamic shared-memory limit of a kernel is a property of the function
+// shared by every handle of the process, so it is raised once per device to
+// the opt-in maximum (less the kernel's static shared memory) for every kernel
+// that takes dynamic shared memory; each launch then asks for what its system
+// needs, and handles with different needs never lower one another's limit.
+std::mutex g_smem_mu;
+bool g_smem_done[64] = {};
+
+void kernel_smem_limits(int device) {
+    std::lock_guard<std::mutex> lock(g_smem_mu);
+    if (device < 0 || device >= 64) throw cm_error(CM_EINVAL, "device index out of range");
+    if (g_smem_done[device]) return;
+    int optin = 0;
+    CM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    auto raise = [&](const void *fn) {
+        cudaFuncAttributes fa;
+        CM_CUDA(cudaFuncGetAttributes(&fa, fn));
+        CM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    };
+    raise((const void *)k_pairs_real<true, true>);
+    raise((const void *)k_pairs_real<true, false>);
+    raise((const void *)k_pairs_real<false, true>);
+    raise((const void *)k_pairs_real<false, false>);
+    raise((const void *)k_random_eval<true>);
+    raise((const void *)k_random_eval<false>);
+    raise((const void *)k_atoms_eval<true, true, true>);
+    raise((const void *)k_atoms_eval<true, false, true>);
+    raise((const void *)k_atoms_eval<false, true, true>);
+    raise((const void *)k_atoms_eval<false, false, true>);
+    raise((const void *)k_atoms_eval<true, true, false>);
+    raise((const void *)k_atoms_eval<true, false, false>);
+    raise((const void *)k_atoms_eval<false, true, false>);
+    raise((const void *)k_atoms_eval<false, false, false>);
+    raise((const void *)k_pairs_guard<true>);
+    raise((const void *)k_pairs_guard<false>);
+    for (int aps : {0, 1, 3, 4, 5, 14}) {
+        raise(flat_kernel_of<true>(aps).fn);
+        raise(flat_kernel_of<false>(aps).fn);
+    }
+    g_smem_done[device] = true;
+}
+
+// Shared memory one CTA of the system's kernels needs at most; fails when
+// it is beyond the device's opt-in limit (very many histogram bins).
+void check_smem(const cm_handle *h, size_t need) {
+    int optin = 0;
+    CM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+    if (need > (size_t)optin)
+        throw cm_error(CM_EINVAL, "the histograms need " + std::to_string(need) +
+                                      " bytes of shared memory per block, more than the device's " +
+                                      std::to_string(optin) + " (use fewer bins)");
+}
+
+// Resident CTAs per SM of the FP32 real pass.
+int flat_setup(cm_handle *h) {
+    const size_t smem = hist_smem_bytes(h, h->smem_groups) + (size_t)kFlatWarps * flat_warp_smem();
+    const FlatKernel k = flat_kernel(h);
+    int n = 0;
+    CM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, kFlatWarps * 32, smem));
+    return std::max(1, n);
+}
+
+// The ATOMS evaluation kernels of a system (precision x schedule).
+using AtomsLaunch = void (*)(int, size_t, cudaStream_t, const DevSys &, const Bufs &);
+struct AtomsKernels {
+    const void *fn;
+    AtomsLaunch real, random;
+};
+
+template <bool FP32, bool RANDOM, bool WARP>
+void launch_atoms(int grid, size_t smem, cudaStream_t st, const DevSys &S, const Bufs &B) {
+    k_atoms_eval<FP32, RANDOM, WARP><<<grid, kAtomsWarps * 32, smem, st>>>(S, B);
+}
+
+template <bool FP32, bool WARP>
+AtomsKernels atoms_kernels_of() {
+    return {(const void *)k_atoms_eval<FP32, false, WARP>, launch_atoms<FP32, false, WARP>, launch_atoms<FP32, true, WARP>};
+}
+
+AtomsKernels atoms_kernels(const cm_handle *h) {
+    const bool fp32 = h->d.precision == CM_PRECISION_FP32_GUARD;
+    if (fp32) return h->atoms_warp ? atoms_kernels_of<true, true>() : atoms_kernels_of<true, false>();
+    return h->atoms_warp ? atoms_kernels_of<false, true>() : atoms_kernels_of<false, false>();
+}
+
+// Resident CTAs per SM of the ATOMS evaluation kernel.
+int atoms_setup(cm_handle *h) {
+    const size_t smem = hist_smem_bytes(h, h->smem_groups);
+    int n = 0;
+    CM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, atoms_kernels(h).fn, kAtomsWarps * 32, smem));
+    return std::max(1, n);
+}
+
+// Mean solute atoms per occupied search cell in the first frame: a warp per
+// queued molecule pair pays off when the cells it walks hold about a warp's
+// worth of atoms; sparse solutes (chains spread through the box) take a
+// thread per pair.
+bool atoms_dense(const cm_handle *h, const cm_frames *f) {
+    const int64_t n = h->Ns;
+    std::vector<double> x(n * 3);
+    std::vector<char> raw(n * 3 * h->coord_elem);
+    if (f->memory == CM_MEM_DEVICE) CM_CUDA(cudaMemcpy(raw.data(), f->solute_xyz, raw.size(), cudaMemcpyDeviceToHost));
+    else memcpy(raw.data(), f->solute_xyz, raw.size());
+    for (int64_t i = 0; i < n * 3; ++i)
+        x[i] = h->coord_elem == 4 ? (double)reinterpret_cast<float *>(raw.data())[i] : reinterpret_cast<double *>(raw.data())[i];
+    FrameGeom G;
+    memset(&G, 0, sizeof(G));
+    frame_geometry(f->cells, target_cell(h), 1023, G);
+    const int aps = h->d.solute_natomspermol;
+    std::vector<int64_t> keys(n);
+    for (int64_t i = 0; i < n; ++i) {
+        int c[3];
+        double q[3];
+        cmgeom::bin_position(G, x[3 * i], x[3 * i + 1], x[3 * i + 2], c, q);
+        keys[i] = (i / aps) * (int64_t)G.ncell + cmgeom::cell_linear(G, c[0], c[1], c[2]);
+    }
+    std::sort(keys.begin(), keys.end());
+    const int64_t occupied = std::unique(keys.begin(), keys.end()) - keys.begin();
+    return (double)n / (double)std::max<int64_t>(1, occupied) >= 64.0;
 }
 
 // Reallocate the per-frame cell arrays of a compute chunk if a frame needs
@@ -344,10 +514,11 @@ void ensure_cells(cm_handle *h, int64_t ncell) {
         dev_alloc(h, h->cstart, n);
         dev_alloc(h, h->cfill, n);
     } else {
-        const size_t n = (size_t)h->fc * ((int64_t)h->d.solute_nmols * ncell + 1) * 4;
-        dev_alloc(h, h->acount, n);
-        dev_alloc(h, h->astart, n);
-        dev_alloc(h, h->afill, n);
+        const size_t n = (size_t)h->fc * ((int64_t)h->d.solute_nmols * ncell + 1);
+        dev_alloc(h, h->acount, n * 4);
+        dev_alloc(h, h->astart, n * 4);
+        dev_alloc(h, h->afill, n * 4);
+        dev_alloc(h, h->anear, n);
     }
 }
 
@@ -429,6 +600,7 @@ void plan(cm_handle *h, const cm_frames *f) {
             dev_alloc(h, h->vo64, fc * h->Nv * 32);
         }
         dev_alloc(h, h->cmol, fc * mv * 4);
+        dev_alloc(h, h->cq32, fc * mv * 16);
         // guard queue of a chunk: every candidate fits when the system is small
         // (candidates <= ms * mv per frame); otherwise 64 per solute molecule and
         // frame, far above the guard-band rate
@@ -454,41 +626,32 @@ void plan(cm_handle *h, const cm_frames *f) {
         if (h->mddf) {
             dev_alloc(h, h->u64, fc * h->Nv * 32);
             dev_alloc(h, h->rc, fc * mv * 4);
-            const int chunk = std::min(kChunkSamples, std::max(1, fc * d.n_random_samples));
+            // the work queue holds every slot of the samples placed in one launch
+            const int64_t want = std::min<int64_t>((int64_t)kChunkSamples * mv, std::max<int64_t>(1 << 22, mv));
+            h->atoms_piece = (int)std::max<int64_t>(1, std::min<int64_t>(kChunkSamples, want / mv));
+            const int chunk = std::min(h->atoms_piece, std::max(1, fc * d.n_random_samples));
             dev_alloc(h, h->pcell, (size_t)chunk * h->Nv * 4);
             dev_alloc(h, h->pq32, (size_t)chunk * h->Nv * 16);
             dev_alloc(h, h->pq64, (size_t)chunk * h->Nv * 32);
         }
     }
+    if (h->regime == CM_REGIME_ATOMS) {
+        // real pass: (frame, solute molecule, solvent molecule) items in
+        // pieces of the queue's capacity
+        const int64_t items = (int64_t)fc * ms * mv;
+        h->aq_cap = (int)std::max<int64_t>(std::min<int64_t>(std::max<int64_t>(items, (int64_t)h->atoms_piece * mv), 1 << 25),
+                                           (int64_t)h->atoms_piece * mv);
+        dev_alloc(h, h->aq, (size_t)h->aq_cap * sizeof(int4));
+    }
     // histogram shared-memory plan
-    const size_t extra = h->regime == CM_REGIME_PAIRS ? (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8 : 0;
+    const size_t extra = h->regime == CM_REGIME_PAIRS ? pairs_extra_smem() : 0;
     h->smem_groups = hist_smem_bytes(h, 1) + extra + 2048 <= 160 * 1024 ? 1 : 0;
-    const size_t smem_max = hist_smem_bytes(h, h->smem_groups) + extra;
-    if (smem_max > 48 * 1024) {
-        const int a = (int)smem_max;
-        auto attr = [&](const void *fn) { CM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a)); };
-        attr((const void *)k_pairs_real<true, true>);
-        attr((const void *)k_pairs_real<true, false>);
-        attr((const void *)k_pairs_real<false, true>);
-        attr((const void *)k_pairs_real<false, false>);
-        attr((const void *)k_random_eval<true>);
-        attr((const void *)k_random_eval<false>);
-        attr((const void *)k_atoms_eval<true, true>);
-        attr((const void *)k_atoms_eval<true, false>);
-        attr((const void *)k_atoms_eval<false, true>);
-        attr((const void *)k_atoms_eval<false, false>);
-        attr((const void *)k_pairs_guard<true>);
-        attr((const void *)k_pairs_guard<false>);
-        attr((const void *)k_pairs_real32<1, true>);
-        attr((const void *)k_pairs_real32<1, false>);
-        attr((const void *)k_pairs_real32<3, true>);
-        attr((const void *)k_pairs_real32<3, false>);
-        attr((const void *)k_pairs_real32<4, true>);
-        attr((const void *)k_pairs_real32<4, false>);
-        attr((const void *)k_pairs_real32<5, true>);
-        attr((const void *)k_pairs_real32<5, false>);
-        attr((const void *)k_pairs_real32<14, true>);
-        attr((const void *)k_pairs_real32<14, false>);
+    kernel_smem_limits(h->device);
+    check_smem(h, hist_smem_bytes(h, h->smem_groups) + extra);
+    if (h->regime == CM_REGIME_PAIRS) h->flat_ctas = flat_setup(h);
+    else {
+        h->atoms_warp = atoms_dense(h, f);
+        h->atoms_ctas = atoms_setup(h);
     }
     h->planned = true;
 }
@@ -618,6 +781,7 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         B.cfill = P<int>(h->cfill);
         B.cs = h->ncell_cap + 1;
         B.cmol = P<int>(h->cmol);
+        B.cq32 = P<float4>(h->cq32);
         B.gq = P<int4>(h->gq);
         B.gq_cap = h->gq_cap;
         B.rq = P<int2>(h->rq);
@@ -635,6 +799,9 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         B.avcell = P<int>(h->avcell);
         B.avq32 = P<float4>(h->avq32);
         B.avq64 = P<d4>(h->avq64);
+        B.anear = P<unsigned char>(h->anear);
+        B.aq = P<int4>(h->aq);
+        B.aq_cap = h->aq_cap;
         if (h->mddf) {
             B.u64 = P<d4>(h->u64);
             B.rc = P<float>(h->rc);
@@ -664,7 +831,7 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
     const int sms = h->sms;
     int launches = 0;
     CM_CUDA(cudaMemsetAsync(B.FS, 0, sizeof(FrameScratch) * nf, st));
-    CM_CUDA(cudaMemsetAsync(B.counters, 0, 2 * sizeof(int), st));
+    CM_CUDA(cudaMemsetAsync(B.counters, 0, 3 * sizeof(int), st));
     CM_LAUNCH(CM_K_PREP, k_offtable<<<dim3(grid_for(cmgeom::kOffEntries, 256), nf), 256, 0, st>>>(B));
     if (h->regime == CM_REGIME_PAIRS) {
         if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
@@ -678,25 +845,15 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         CM_LAUNCH(CM_K_CELLS, k_scatter_mols<<<dim3(grid_for(mv, 256), nf), 256, 0, st>>>(B, self ? 1 : 0));
         const size_t smem = hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
         const int grid = (int)std::min<int64_t>(((int64_t)nf * ms + kWarps - 1) / kWarps, (int64_t)sms * 8);
-        bool special = false;
+        // FP32: one lane per solvent atom; the frames that need several images
+        // per molecule pair are left to the generic kernel below
+        const bool special = fp32;
         if (fp32) {
-#define CM_PAIRS_R32(A, SF) CM_LAUNCH(CM_K_REAL, k_pairs_real32<A, SF><<<grid, kWarps * 32, smem, st>>>(S, B))
-#define CM_PAIRS_R32_APV(A)              \
-    case A:                              \
-        if (self) CM_PAIRS_R32(A, true); \
-        else CM_PAIRS_R32(A, false);     \
-        special = true;                  \
-        break;
-            switch (apv) {
-                CM_PAIRS_R32_APV(1)
-                CM_PAIRS_R32_APV(3)
-                CM_PAIRS_R32_APV(4)
-                CM_PAIRS_R32_APV(5)
-                CM_PAIRS_R32_APV(14)
-                default: break;
-            }
-#undef CM_PAIRS_R32_APV
-#undef CM_PAIRS_R32
+            const size_t fsm = hsm + (size_t)kFlatWarps * flat_warp_smem();
+            const int fgrid = (int)std::min<int64_t>(((int64_t)nf * ms + kFlatWarps - 1) / kFlatWarps,
+                                                     (int64_t)sms * h->flat_ctas);
+            const FlatKernel fk = flat_kernel(h);
+            CM_LAUNCH(CM_K_REAL, fk.launch(fgrid, fsm, st, S, B));
         }
         // the generic kernel takes every frame, or after the specialised one
         // only the frames that need several images per molecule pair
@@ -730,17 +887,27 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         CM_LAUNCH(CM_K_PREP, k_frame_consts<<<nf, 128, 0, st>>>(S, B, 0));
         CM_LAUNCH(CM_K_CELLS, k_scan<<<nf, 1024, 0, st>>>(B, 1));
         CM_LAUNCH(CM_K_CELLS, k_scatter_atoms<<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B));
-        const dim3 gr(grid_for(mv, 128), (unsigned)(nf * ms));
-        if (fp32) CM_LAUNCH(CM_K_REAL, k_atoms_eval<true, false><<<gr, 128, hsm, st>>>(S, B, 0));
-        else CM_LAUNCH(CM_K_REAL, k_atoms_eval<false, false><<<gr, 128, hsm, st>>>(S, B, 0));
+        if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
+        CM_LAUNCH(CM_K_CELLS, k_atoms_near<<<dim3(grid_for(ms * h->ncell_cap, 256), nf), 256, 0, st>>>(B));
+        const int wgrid = sms * h->atoms_ctas;
+        const AtomsKernels ak = atoms_kernels(h);
+        // real pass: molecule pairs that can hold a pair within the cutoff,
+        // in pieces of the queue's capacity
+        const int64_t items = (int64_t)nf * ms * mv;
+        for (int64_t i0 = 0; i0 < items; i0 += h->aq_cap) {
+            const int64_t n = std::min<int64_t>(h->aq_cap, items - i0);
+            CM_CUDA(cudaMemsetAsync(B.counters + 2, 0, sizeof(int), st));
+            CM_LAUNCH(CM_K_REAL, k_atoms_filter<<<grid_for(n, 256), 256, 0, st>>>(S, B, i0, n));
+            CM_LAUNCH(CM_K_REAL, ak.real(wgrid, hsm, st, S, B));
+        }
         if (rnd) {
             CM_LAUNCH(CM_K_BULK, k_bulk<<<c.ntab, 1024, 0, st>>>(S, B, dtab + c.tab0));
-            for (int s0 = 0; s0 < c.nsmp; s0 += kChunkSamples) {
-                const int ny = std::min(kChunkSamples, c.nsmp - s0);
+            for (int s0 = 0; s0 < c.nsmp; s0 += h->atoms_piece) {
+                const int ny = std::min(h->atoms_piece, c.nsmp - s0);
                 const dim3 gp(grid_for(mv, 128), ny);
+                CM_CUDA(cudaMemsetAsync(B.counters + 2, 0, sizeof(int), st));
                 CM_LAUNCH(CM_K_RANDOM, k_atoms_place<<<gp, 128, 0, st>>>(S, B, c.smp0 + s0));
-                if (fp32) CM_LAUNCH(CM_K_RANDOM, k_atoms_eval<true, true><<<gp, 128, hsm, st>>>(S, B, c.smp0 + s0));
-                else CM_LAUNCH(CM_K_RANDOM, k_atoms_eval<false, true><<<gp, 128, hsm, st>>>(S, B, c.smp0 + s0));
+                CM_LAUNCH(CM_K_RANDOM, ak.random(wgrid, hsm, st, S, B));
             }
         }
     }
@@ -758,12 +925,8 @@ void fold_class(cm_handle *h) {
     h->class_open = false;
 }
 
-// Frames per compute chunk: the ATOMS real pass indexes (frame, solute
-// molecule) in grid.y, which holds at most 65535 entries.
-int chunk_frames(const cm_handle *h) {
-    if (h->regime == CM_REGIME_ATOMS) return std::max(1, std::min(h->fc, 65535 / h->d.solute_nmols));
-    return h->fc;
-}
+// Frames per compute chunk.
+int chunk_frames(const cm_handle *h) { return h->fc; }
 
 void submit(cm_handle *h, const cm_frames *f) {
     const cm_system_desc &d = h->d;
@@ -773,8 +936,6 @@ void submit(cm_handle *h, const cm_frames *f) {
     if (!d.autocorrelation && !f->solvent_xyz) throw cm_error(CM_EINVAL, "solvent_xyz is required unless autocorrelation");
     if (f->coord_type != CM_COORD_F32 && f->coord_type != CM_COORD_F64) throw cm_error(CM_EINVAL, "unknown coord_type");
     if (f->memory != CM_MEM_HOST && f->memory != CM_MEM_DEVICE) throw cm_error(CM_EINVAL, "unknown memory kind");
-    if (h->regime == CM_REGIME_ATOMS && d.solute_nmols > 65535)
-        throw cm_error(CM_EINVAL, "the ATOMS layout supports at most 65535 solute molecules");
     if (!h->planned) plan(h, f);
     int elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
     if (elem != h->coord_elem && f->memory == CM_MEM_HOST)
@@ -923,9 +1084,9 @@ void free_all(cm_handle *h) {
     DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag,
                      &h->slot, &h->flags, &h->bulk, &h->nbulk, &h->tabs, &h->counters, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
-                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->gq, &h->rq, &h->akey, &h->atq32,
+                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
-                     &h->pcell, &h->pq32, &h->pq64, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx};
+                     &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx};
     for (DevBuf *b : all) {
         if (b->p) cudaFree(b->p);
         b->p = nullptr;
@@ -1038,6 +1199,7 @@ void noalloc_fixed(cm_handle *h, Carve &c) {
         c.take(h->vo64, h->Nv * 32);
     }
     c.take(h->cmol, mv * 4);
+    c.take(h->cq32, mv * 16);
     h->gq_cap = (int)std::min<int64_t>(std::max<int64_t>(ms * mv, 1024), 1 << 18);
     c.take(h->gq, (size_t)h->gq_cap * sizeof(int4));
     if (h->mddf) {
@@ -1072,29 +1234,9 @@ int noalloc_samples(const cm_system_desc &d, int64_t frame_id, Sample *out, int4
 }
 
 void noalloc_smem_attributes(cm_handle *h) {
-    const size_t extra = (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
-    const size_t smem_max = hist_smem_bytes(h, h->smem_groups) + extra;
-    if (smem_max <= 48 * 1024) return;
-    const int a = (int)smem_max;
-    auto attr = [&](const void *fn) { CM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a)); };
-    attr((const void *)k_pairs_real<true, true>);
-    attr((const void *)k_pairs_real<true, false>);
-    attr((const void *)k_pairs_real<false, true>);
-    attr((const void *)k_pairs_real<false, false>);
-    attr((const void *)k_random_eval<true>);
-    attr((const void *)k_random_eval<false>);
-    attr((const void *)k_pairs_guard<true>);
-    attr((const void *)k_pairs_guard<false>);
-    attr((const void *)k_pairs_real32<1, true>);
-    attr((const void *)k_pairs_real32<1, false>);
-    attr((const void *)k_pairs_real32<3, true>);
-    attr((const void *)k_pairs_real32<3, false>);
-    attr((const void *)k_pairs_real32<4, true>);
-    attr((const void *)k_pairs_real32<4, false>);
-    attr((const void *)k_pairs_real32<5, true>);
-    attr((const void *)k_pairs_real32<5, false>);
-    attr((const void *)k_pairs_real32<14, true>);
-    attr((const void *)k_pairs_real32<14, false>);
+    kernel_smem_limits(h->device);
+    check_smem(h, hist_smem_bytes(h, h->smem_groups) + pairs_extra_smem());
+    h->flat_ctas = flat_setup(h);
 }
 
 thread_local Sample t_noalloc_samples[CM_NOALLOC_MAX_SAMPLES];
@@ -1223,7 +1365,7 @@ int noalloc_frame(const cm_system_desc *desc, const cm_frames *f, int64_t *count
             throw cm_error(CM_EINVAL, "counts must hold " + std::to_string(h.hist_n) + " int64 values");
         h.hist.p = counts;
         h.hist.bytes = (size_t)h.hist_n * 8;
-        const size_t extra = (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
+        const size_t extra = pairs_extra_smem();
         h.smem_groups = hist_smem_bytes(&h, 1) + extra + 2048 <= 160 * 1024 ? 1 : 0;
         {
             Carve dry;
@@ -1540,6 +1682,56 @@ void *cm_stream(cm_handle *h) { return h ? (void *)h->stream : nullptr; }
 int cm_frame_counts_noalloc(const cm_system_desc *desc, const cm_frames *frame, int64_t *counts, int64_t counts_len,
                             void *stream) {
     return noalloc_frame(desc, frame, counts, counts_len, stream);
+}
+
+int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *out) {
+    if (!desc || !sample || !out) {
+        g_create_error = "NULL argument";
+        return CM_EINVAL;
+    }
+    memset(out, 0, sizeof(*out));
+    const bool atoms = desc->regime == CM_REGIME_ATOMS ||
+                       (desc->regime == CM_REGIME_AUTO &&
+                        (desc->solute_natomspermol > kMaxSmallMol || desc->solvent_natomspermol > kMaxSmallMol));
+    // ATOMS: cutoff / (lcell k); PAIRS: the molecule cell and smaller ones
+    const int cand_atoms[] = {100, 67, 50, 40};
+    const int cand_pairs[] = {100, 75, 60, 50};
+    const int *cand = atoms ? cand_atoms : cand_pairs;
+    const int ncand = 4;
+    double best = 0.0;
+    for (int c = 0; c < ncand; ++c) {
+        cm_system_desc d = *desc;
+        d.cell_scale_pct = cand[c];
+        d.kernel_timing = 1;
+        cm_handle *h = nullptr;
+        int st = cm_create(&d, &h);
+        if (st != CM_OK) return st;
+        double ms = 0.0;
+        st = guarded(h, [&] {
+            submit(h, sample);  // warm-up: allocations, first launches
+            check_device_error(h);
+            timing_drain(h);
+            for (int k = 0; k < CM_K_NCLASSES; ++k) h->class_ms[k] = 0.0;
+            submit(h, sample);
+            check_device_error(h);
+            timing_drain(h);
+            for (int k = 0; k < CM_K_NCLASSES; ++k) ms += h->class_ms[k];
+        });
+        if (st != CM_OK) {
+            g_create_error = h->err;
+            cm_destroy(h);
+            return st;
+        }
+        cm_destroy(h);
+        out->candidates[c] = cand[c];
+        out->ms_per_frame[c] = ms / std::max(1, sample->nframes);
+        if (c == 0 || out->ms_per_frame[c] < best) {
+            best = out->ms_per_frame[c];
+            out->cell_scale_pct = cand[c];
+        }
+    }
+    out->ncandidates = ncand;
+    return CM_OK;
 }
 
 }  // extern "C"

@@ -103,7 +103,8 @@ typedef struct cm_system_desc {
     int32_t max_frames_per_batch;     /* frames staged on the device per submit chunk; 0 = 64 */
     int64_t hbm_budget_bytes;         /* 0 = no limit; cm_create fails with CM_ENOMEM above it */
     int32_t kernel_timing;            /* 1: time every launch with CUDA events (cm_get_kernel_times) */
-    int32_t reserved;
+    int32_t cell_scale_pct;           /* search-cell size in percent of the default (0 = 100, range 30-300);
+                                         the counts do not depend on it, only the speed (cm_autotune) */
 } cm_system_desc;
 
 /*
@@ -235,6 +236,94 @@ int64_t cm_device_bytes(const cm_handle *h);
 /* The CUDA stream of the handle (as cudaStream_t), for callers that order
  * their own device work against the engine. */
 void *cm_stream(cm_handle *h);
+
+/* ---------------------------------------------------------------------------
+ * Autotuner.  No counterpart in the reference (its cell size is
+ * cutoff / lcell).  Times the real and random-insertion passes of a sample
+ * of frames for each candidate search-cell size, with temporary handles and
+ * CUDA events, and returns the fastest as cell_scale_pct for cm_create.  The
+ * candidates are the default cell (100 %) and smaller cells (more, finer
+ * stencil cells: less volume searched per molecule, more cells to walk). */
+#define CM_TUNE_MAX 8
+typedef struct cm_tuning {
+    int32_t cell_scale_pct;           /* the fastest candidate */
+    int32_t ncandidates;
+    int32_t candidates[CM_TUNE_MAX];  /* cell_scale_pct of each candidate */
+    double ms_per_frame[CM_TUNE_MAX]; /* measured GPU time per frame of each candidate */
+} cm_tuning;
+
+int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *out);
+
+/* ---------------------------------------------------------------------------
+ * Request server: continuous batching of MDDF jobs on one device.  No
+ * counterpart in the reference (it runs one mddf call at a time); each
+ * request's counts are those of cm_create + cm_submit_frames +
+ * cm_read_counts for its system and frames alone.
+ *
+ * Requests queue in arrival order.  The server admits one when fewer than
+ * max_active requests are on the device and its handle fits in what is left
+ * of hbm_budget_bytes (0: no budget, only the device's memory); a request that
+ * does not fit waits while smaller ones behind it may be admitted.  Admitted
+ * requests keep their coordinates, cell lists and accumulators on the device,
+ * run on their own streams (their work overlaps on the GPU) and take turns of
+ * frames_per_turn frames.  A request's counts are read back as soon as its
+ * last frame is done and its device memory goes back to the budget.  The
+ * caller keeps the request's coordinate arrays alive until it is finished
+ * (cells, weights and frame ids are copied at submit). */
+enum {
+    CM_REQ_QUEUED = 0,
+    CM_REQ_RUNNING = 1,
+    CM_REQ_DONE = 2,
+    CM_REQ_FAILED = 3,
+    CM_REQ_CANCELLED = 4
+};
+
+typedef struct cm_server_desc {
+    int32_t device;
+    int32_t max_active;             /* requests on the device at once, 0: no limit */
+    int64_t hbm_budget_bytes;       /* device memory for admitted requests, 0: no budget */
+    int32_t frames_per_turn;        /* frames a request submits per turn, 0: 32 */
+    int32_t reserved;
+} cm_server_desc;
+
+typedef struct cm_request_info {
+    int32_t state;                  /* CM_REQ_* */
+    int32_t status;                 /* cm_status of a failed request */
+    double t_submit, t_admit, t_done; /* seconds since cm_server_create (host clock) */
+    int64_t frames_submitted;
+    int64_t device_bytes;           /* device memory of the request's handle */
+} cm_request_info;
+
+typedef struct cm_server cm_server;
+
+/* Start a server (and its scheduler thread) on one device. */
+int cm_server_create(const cm_server_desc *desc, cm_server **out);
+
+/* Queue a request: a system and its frames in host memory. */
+int cm_server_submit(cm_server *s, const cm_system_desc *desc, const cm_frames *frames, int64_t *request_id);
+
+/* State of a request. */
+int cm_server_poll(cm_server *s, int64_t request_id, cm_request_info *out);
+
+/* Wait until a request is done, failed or cancelled (timeout_s < 0: no
+ * timeout); CM_ESTATE if it is still running at the timeout. */
+int cm_server_wait(cm_server *s, int64_t request_id, double timeout_s, cm_request_info *out);
+
+/* Results of a finished request (weighted FP64, and exact half units). */
+int cm_server_read_counts(cm_server *s, int64_t request_id, cm_counts *out);
+int cm_server_read_raw_counts(cm_server *s, int64_t request_id, cm_raw_counts *out);
+
+/* Cancel a queued or running request. */
+int cm_server_cancel(cm_server *s, int64_t request_id);
+
+/* Forget a finished request and its results. */
+int cm_server_release(cm_server *s, int64_t request_id);
+
+/* Stop the scheduler and free every request. */
+int cm_server_destroy(cm_server *s);
+
+/* Message of the last failure of a server call (s NULL: of cm_server_create). */
+const char *cm_server_last_error(const cm_server *s);
 
 /* ---------------------------------------------------------------------------
  * Allocation-free entry point.  No counterpart in the reference: it serves

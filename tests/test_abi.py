@@ -34,6 +34,8 @@ def test_struct_sizes_match_header(cm):
     assert C.sizeof(N.cm_raw_counts) == 64
     assert C.sizeof(N.cm_stats) == 88
     assert C.sizeof(N.cm_kernel_times) == 112
+    assert C.sizeof(N.cm_server_desc) == 24
+    assert C.sizeof(N.cm_request_info) == 48
 
 
 def test_create_rejects_bad_descriptions_without_gpu(cm):
@@ -73,3 +75,16 @@ def test_engine_fails_loudly_without_library(cm, tmp_path):
             N.load(str(tmp_path / "missing.so"))
         finally:
             N._lib = saved
+
+
+def test_server_create_rejects_bad_arguments_without_gpu(cm):
+    """Server argument checks come before any device use."""
+    N = cm._native
+    lib = N.load()
+    d = N.cm_server_desc()
+    d.device = 0
+    d.frames_per_turn = -1
+    s = C.c_void_p()
+    assert lib.cm_server_create(C.byref(d), C.byref(s)) == N.CM_EINVAL
+    assert b"negative" in lib.cm_server_last_error(None)
+    assert lib.cm_server_destroy(None) == N.CM_OK

@@ -33,7 +33,7 @@ def make_system(rng, H, ms, aps, mv, apv, nframes, self_mode, spread=0.9):
 
 
 def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, regime, frame_ids=None, groups=None,
-            backend="cells", dtype=np.float64, **opt):
+            backend="cells", dtype=np.float64, cell_scale_pct=0, **opt):
     nf = xs.shape[0]
     frame_ids = list(range(1, nf + 1)) if frame_ids is None else frame_ids
     kw = dict(autocorrelation=self_mode, **opt)
@@ -46,7 +46,8 @@ def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, r
         gv = gv_rows(mv * apv, apv)
         g = dict(solute_groups=gs, solute_ngroups=5, solvent_groups=gv, solvent_ngroups=5)
     eng = cm.Engine(solute_nmols=ms, solute_natomspermol=aps, solvent_nmols=mv, solvent_natomspermol=apv,
-                    precision=precision, regime=regime, max_frames_per_batch=2, **kw, **g)
+                    precision=precision, regime=regime, max_frames_per_batch=2, cell_scale_pct=cell_scale_pct, **kw,
+                    **g)
     eng.submit(xs.astype(dtype), None if self_mode else xv.astype(dtype), cells, frame_ids=frame_ids)
     got = eng.raw_counts()
     st = eng.stats()
@@ -243,3 +244,25 @@ def test_gpu_namd_frames_vs_oracle(cm, orc, gpu_ready):
     water = np.repeat(g["water"].astype(np.float64)[None], 2, axis=0)
     compare(cm, orc, ms=181, aps=14, mv=2000, apv=3, xs=tmao, xv=water, cells=cells, self_mode=False,
             precision="fp32", regime="pairs", **opt)
+
+
+@pytest.mark.parametrize("pct", [40, 60, 150])
+@pytest.mark.parametrize("regime", ["pairs", "atoms"])
+def test_cell_scale_does_not_change_counts(cm, orc, gpu_ready, pct, regime):
+    """Search cells of another size (cell_scale_pct) give the same counts."""
+    rng = np.random.default_rng(21)
+    xs, xv, cells = make_system(rng, TRICLINIC, 30, 4, 200, 3, 2, False)
+    opt = dict(irefatom=1, cutoff=6.0, dbulk=6.0, usecutoff=False, n_random_samples=5, **COMMON)
+    compare(cm, orc, ms=30, aps=4, mv=200, apv=3, xs=xs, xv=xv, cells=cells, self_mode=False, precision="fp32",
+            regime=regime, cell_scale_pct=pct, **opt)
+
+
+def test_autotune_reports_candidates(cm, gpu_ready):
+    rng = np.random.default_rng(22)
+    xs, xv, cells = make_system(rng, ORTHO, 200, 5, 200, 5, 3, True)
+    t = cm.autotune(xs, None, cells, solute_nmols=200, solute_natomspermol=5, solvent_nmols=200,
+                    solvent_natomspermol=5, autocorrelation=True, irefatom=1, cutoff=7.0, binstep=0.02, dbulk=7.0,
+                    usecutoff=False, nbins=350, n_random_samples=4)
+    assert t["cell_scale_pct"] in t["candidates"]
+    assert len(t["candidates"]) == 4 and all(v > 0 for v in t["candidates"].values())
+    assert t["candidates"][t["cell_scale_pct"]] == min(t["candidates"].values())
