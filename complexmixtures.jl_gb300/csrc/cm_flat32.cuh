@@ -180,9 +180,11 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
     const int a1 = (int)((unsigned)k1 >> 8) & 0xff, b1 = (int)(k1 & 0xff);
     const float m2 = __uint_as_float(C.m2), r1 = __uint_as_float(C.r1), r2 = __uint_as_float(C.r2);
     const float dmin = sqrtf(m1);
+    // hard: the closest pair or the cutoff / dbulk decision needs the full
+    // FP64 rules; edge: only the md bin does (closest pair known)
     bool hard = m1 >= g.cutm2 || (sqrtf(m2) - dmin) <= g.two_delta;
     const int bin = hard ? -1 : bin32(g, dmin);
-    hard = hard || bin < 0;
+    const bool edge = !hard && bin < 0;
     if (S.usecutoff) hard = hard || (dmin >= g.dbulk_lo && dmin <= g.dbulk_hi);
     int rb1 = -1, rb2 = -1;
     if (!hard && r1 <= g.cutp2) {
@@ -197,6 +199,16 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
         const int slot = atomicAdd(B.counters + 0, 1);
         if (slot < B.gq_cap) B.gq[slot] = make_int4(s, v, code, f);
         else raise_err(S, ERR_QUEUE);
+        return;
+    }
+    if (edge) {
+        const int slot = atomicAdd(B.counters + 3, 1);
+        if (slot < B.eq_cap) {
+            B.eq[2 * slot] = make_int4(s, v, code, f);
+            B.eq[2 * slot + 1] = make_int4(a1 | b1 << 8, rb1, rb2, __float_as_int(dmin));
+        } else {
+            raise_err(S, ERR_QUEUE);
+        }
         return;
     }
     const int bulk = S.usecutoff ? (dmin > g.dbulk_hi) : 0;
@@ -368,6 +380,55 @@ __global__ void __launch_bounds__(128) k_pairs_guard(DevSys S, Bufs B) {
         pairs_decide<SELF>(S, F.g, P, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, Pf.so64 + (int64_t)s * S.aps, os,
                            Pf.vo64 + (int64_t)v * S.apv, ov, s, v, r1, r2, st);
         emit<SELF>(S, h, r1, r2, s, v, Pf.slot, Pf.flags, st);
+    }
+    stats_flush(S, st, false);
+    __syncthreads();
+    shist_flush(S, h, false);
+}
+
+// Edge kernel: records whose closest atom pair is known from the FP32 pass
+// and whose md bin lies within the guard band of a bin edge.  The FP64
+// distance of that pair, formed as in the exact scan, gives the bin; the
+// rest of the record was decided in FP32.
+template <bool SELF>
+__global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    shist_zero(S, hbase);
+    __syncthreads();
+    SHist h = shist_bind(S, hbase);
+    LocalStats st;
+    const int n = min(B.counters[3], B.eq_cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int4 e = B.eq[2 * i], x = B.eq[2 * i + 1];
+        const int s = e.x, v = e.y, f = e.w;
+        const int a1 = x.x & 0xff, b1 = (x.x >> 8) & 0xff, rb1 = x.y, rb2 = x.z;
+        const float d32 = __int_as_float(x.w);
+        const PairsFrame Pf = pairs_frame(B, f, SELF);
+        const Images im = images_of(*Pf.G, *Pf.F, e.z);
+        const double q = pairs_one64(Pf.off64, im, Pf.sq64[s], Pf.vq64[v], Pf.so64[(int64_t)s * S.aps + a1],
+                                     Pf.vo64[(int64_t)v * S.apv + b1]);
+        const double d64 = sqrt(q);
+        const int bin = setbin0(d64, S.binstep);
+        st.guard++;
+        st.guard_pairs += image_count(im);
+        st.maxerr = fmax(st.maxerr, fabs((double)d32 - d64));
+        const int bulk = S.usecutoff ? (d64 > S.dbulk) : 0;
+        apply_hit_local(S, h, false, bin, a1, (int64_t)v * S.apv + b1, b1, rb1 >= 0, rb1);
+        st.hits++;
+        if (SELF) {
+            apply_hit_local(S, h, false, bin, b1, (int64_t)s * S.aps + a1, a1, rb2 >= 0, rb2);
+            st.hits++;
+        }
+        if (Pf.slot) {
+            const unsigned char code1 = (unsigned char)(1 + bulk);
+            const int sl = Pf.slot[s];
+            if (sl >= 0) Pf.flags[(int64_t)sl * S.mv + v] = code1;
+            if (SELF) {
+                const int vs = Pf.slot[v];
+                if (vs >= 0) Pf.flags[(int64_t)vs * S.mv + s] = code1;
+            }
+        }
     }
     stats_flush(S, st, false);
     __syncthreads();

@@ -668,7 +668,9 @@ struct Bufs {
     int gq_cap;
     int2 *rq;                       // (sample, slot)
     int rq_cap;
-    int *counters;                  // [0] guard queue, [1] random queue
+    int4 *eq;                       // edge queue: 2 int4 per entry (s, v, code, frame), (a | b << 8, rb1, rb2, d32 bits)
+    int eq_cap;
+    int *counters;                  // [0] guard queue, [1] random queue, [2] ATOMS queue, [3] edge queue
     // ATOMS
     int *akey;                      // [nf][Ns]
     float4 *atq32, *asq32;

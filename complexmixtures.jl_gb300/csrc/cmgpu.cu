@@ -83,7 +83,7 @@ struct cm_handle {
     DevBuf geoms, samples, tabs, fscratch, off64, off32, hist, sums, stats, errflag, counters, slot, flags, bulk, nbulk;
     DevBuf stage_s[2], stage_v[2];
     // PAIRS
-    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, ccount, cstart, cfill, cmol, cq32, gq, rq;
+    DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, ccount, cstart, cfill, cmol, cq32, gq, rq, eq;
     int gq_cap = 0, rq_cap = 0;
     int flat_ctas = 0;  // resident CTAs per SM of k_pairs_flat32
     // group tables
@@ -417,6 +417,8 @@ void kernel_smem_limits(int device) {
     raise((const void *)k_atoms_eval<false, false, false>);
     raise((const void *)k_pairs_guard<true>);
     raise((const void *)k_pairs_guard<false>);
+    raise((const void *)k_pairs_edge<true>);
+    raise((const void *)k_pairs_edge<false>);
     for (int aps : {0, 1, 3, 4, 5, 14}) {
         raise(flat_kernel_of<true>(aps).fn);
         raise(flat_kernel_of<false>(aps).fn);
@@ -608,6 +610,7 @@ void plan(cm_handle *h, const cm_frames *f) {
         h->gq_cap = (int)(bound <= (1LL << 24) ? std::max<int64_t>(bound, 1024)
                                                : std::min<int64_t>(std::max<int64_t>(1 << 20, 64 * ms * fc), 1LL << 25));
         dev_alloc(h, h->gq, (size_t)h->gq_cap * sizeof(int4));
+        dev_alloc(h, h->eq, (size_t)h->gq_cap * 2 * sizeof(int4));
         if (h->mddf) {
             // random-insertion queue: every slot of `chunk` samples fits
             const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>((int64_t)fc * d.n_random_samples, (1 << 23) / mv));
@@ -784,6 +787,8 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         B.cq32 = P<float4>(h->cq32);
         B.gq = P<int4>(h->gq);
         B.gq_cap = h->gq_cap;
+        B.eq = P<int4>(h->eq);
+        B.eq_cap = h->gq_cap;
         B.rq = P<int2>(h->rq);
         B.rq_cap = h->rq_cap;
     } else {
@@ -831,7 +836,7 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
     const int sms = h->sms;
     int launches = 0;
     CM_CUDA(cudaMemsetAsync(B.FS, 0, sizeof(FrameScratch) * nf, st));
-    CM_CUDA(cudaMemsetAsync(B.counters, 0, 3 * sizeof(int), st));
+    CM_CUDA(cudaMemsetAsync(B.counters, 0, 4 * sizeof(int), st));
     CM_LAUNCH(CM_K_PREP, k_offtable<<<dim3(grid_for(cmgeom::kOffEntries, 256), nf), 256, 0, st>>>(B));
     if (h->regime == CM_REGIME_PAIRS) {
         if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
@@ -865,6 +870,8 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         if (special) {
             if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_guard<true><<<sms * 4, 128, hsm, st>>>(S, B));
             else CM_LAUNCH(CM_K_GUARD, k_pairs_guard<false><<<sms * 4, 128, hsm, st>>>(S, B));
+            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_edge<true><<<sms * 2, 128, hsm, st>>>(S, B));
+            else CM_LAUNCH(CM_K_GUARD, k_pairs_edge<false><<<sms * 2, 128, hsm, st>>>(S, B));
         }
         if (rnd) {
             CM_LAUNCH(CM_K_BULK, k_bulk<<<c.ntab, 1024, 0, st>>>(S, B, dtab + c.tab0));
@@ -1084,7 +1091,7 @@ void free_all(cm_handle *h) {
     DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag,
                      &h->slot, &h->flags, &h->bulk, &h->nbulk, &h->tabs, &h->counters, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
-                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->rq, &h->akey, &h->atq32,
+                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->eq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
                      &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx};
     for (DevBuf *b : all) {
@@ -1202,6 +1209,7 @@ void noalloc_fixed(cm_handle *h, Carve &c) {
     c.take(h->cq32, mv * 16);
     h->gq_cap = (int)std::min<int64_t>(std::max<int64_t>(ms * mv, 1024), 1 << 18);
     c.take(h->gq, (size_t)h->gq_cap * sizeof(int4));
+    c.take(h->eq, (size_t)h->gq_cap * 2 * sizeof(int4));
     if (h->mddf) {
         h->rq_cap = (int)std::min<int64_t>(std::max<int64_t>((int64_t)d.n_random_samples * mv, mv), std::max<int64_t>(mv, 1 << 18));
         c.take(h->rq, (size_t)h->rq_cap * sizeof(int2));
