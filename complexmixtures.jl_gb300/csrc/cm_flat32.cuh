@@ -180,32 +180,37 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
     const int a1 = (int)((unsigned)k1 >> 8) & 0xff, b1 = (int)(k1 & 0xff);
     const float m2 = __uint_as_float(C.m2), r1 = __uint_as_float(C.r1), r2 = __uint_as_float(C.r2);
     const float dmin = sqrtf(m1);
-    // hard: the closest pair or the cutoff / dbulk decision needs the full
-    // FP64 rules; edge: only the md bin does (closest pair known)
+    // hard: the closest pair, or the cutoff or dbulk decision, needs the full
+    // FP64 rules (guard queue)
     bool hard = m1 >= g.cutm2 || (sqrtf(m2) - dmin) <= g.two_delta;
-    const int bin = hard ? -1 : bin32(g, dmin);
-    const bool edge = !hard && bin < 0;
     if (S.usecutoff) hard = hard || (dmin >= g.dbulk_lo && dmin <= g.dbulk_hi);
-    int rb1 = -1, rb2 = -1;
-    if (!hard && r1 <= g.cutp2) {
-        rb1 = r1 < g.cutm2 ? bin32(g, sqrtf(r1)) : -1;
-        hard = rb1 < 0;
-    }
-    if (SELF && !hard && r2 <= g.cutp2) {
-        rb2 = r2 < g.cutm2 ? bin32(g, sqrtf(r2)) : -1;
-        hard = rb2 < 0;
-    }
     if (hard) {
         const int slot = atomicAdd(B.counters + 0, 1);
         if (slot < B.gq_cap) B.gq[slot] = make_int4(s, v, code, f);
         else raise_err(S, ERR_QUEUE);
         return;
     }
-    if (edge) {
+    // otherwise each of the md bin, the solvent reference-atom row and (self)
+    // the solute reference-atom column is decided here, or marked -2 when it
+    // lies within the guard band of a bin edge or of the cutoff: the edge
+    // kernel then computes it from FP64 pair distances
+    int bin = bin32(g, dmin);
+    if (bin < 0) bin = -2;
+    int rb1 = -1, rb2 = -1;
+    if (r1 <= g.cutp2) {
+        rb1 = r1 < g.cutm2 ? bin32(g, sqrtf(r1)) : -1;
+        if (rb1 < 0) rb1 = -2;
+    }
+    if (SELF && r2 <= g.cutp2) {
+        rb2 = r2 < g.cutm2 ? bin32(g, sqrtf(r2)) : -1;
+        if (rb2 < 0) rb2 = -2;
+    }
+    if (bin == -2 || rb1 == -2 || rb2 == -2) {
         const int slot = atomicAdd(B.counters + 3, 1);
         if (slot < B.eq_cap) {
-            B.eq[2 * slot] = make_int4(s, v, code, f);
-            B.eq[2 * slot + 1] = make_int4(a1 | b1 << 8, rb1, rb2, __float_as_int(dmin));
+            B.eq[3 * slot] = make_int4(s, v, code, f);
+            B.eq[3 * slot + 1] = make_int4(a1 | b1 << 8, rb1, rb2, bin);
+            B.eq[3 * slot + 2] = make_int4(__float_as_int(dmin), 0, 0, 0);
         } else {
             raise_err(S, ERR_QUEUE);
         }
@@ -387,9 +392,13 @@ __global__ void __launch_bounds__(128) k_pairs_guard(DevSys S, Bufs B) {
 }
 
 // Edge kernel: records whose closest atom pair is known from the FP32 pass
-// and whose md bin lies within the guard band of a bin edge.  The FP64
-// distance of that pair, formed as in the exact scan, gives the bin; the
-// rest of the record was decided in FP32.
+// (second-closest pair beyond 2 delta, cutoff and dbulk clear) but whose md
+// bin, solvent reference-atom row or solute reference-atom column (marked -2)
+// lies within the guard band of a bin edge or of the cutoff.  Each marked
+// value comes from FP64 pair distances formed as in the exact scan: the
+// closest pair for the md bin, the aps pairs of the solvent molecule's
+// reference atom for the row, the apv pairs of the solute molecule's
+// reference atom for the column.
 template <bool SELF>
 __global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -400,20 +409,38 @@ __global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
     LocalStats st;
     const int n = min(B.counters[3], B.eq_cap);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int4 e = B.eq[2 * i], x = B.eq[2 * i + 1];
+        const int4 e = B.eq[3 * i], x = B.eq[3 * i + 1], y = B.eq[3 * i + 2];
         const int s = e.x, v = e.y, f = e.w;
-        const int a1 = x.x & 0xff, b1 = (x.x >> 8) & 0xff, rb1 = x.y, rb2 = x.z;
-        const float d32 = __int_as_float(x.w);
+        const int a1 = x.x & 0xff, b1 = (x.x >> 8) & 0xff;
+        int rb1 = x.y, rb2 = x.z, bin = x.w;
+        const float d32 = __int_as_float(y.x);
         const PairsFrame Pf = pairs_frame(B, f, SELF);
         const Images im = images_of(*Pf.G, *Pf.F, e.z);
-        const double q = pairs_one64(Pf.off64, im, Pf.sq64[s], Pf.vq64[v], Pf.so64[(int64_t)s * S.aps + a1],
-                                     Pf.vo64[(int64_t)v * S.apv + b1]);
-        const double d64 = sqrt(q);
-        const int bin = setbin0(d64, S.binstep);
+        const d4 qs = Pf.sq64[s], qv = Pf.vq64[v];
+        const d4 *os = Pf.so64 + (int64_t)s * S.aps;
+        const d4 *ov = Pf.vo64 + (int64_t)v * S.apv;
+        const int nimg = image_count(im);
         st.guard++;
-        st.guard_pairs += image_count(im);
-        st.maxerr = fmax(st.maxerr, fabs((double)d32 - d64));
-        const int bulk = S.usecutoff ? (d64 > S.dbulk) : 0;
+        int bulk = S.usecutoff ? (d32 > Pf.F->g.dbulk_hi) : 0;
+        if (bin == -2) {
+            const double d64 = sqrt(pairs_one64(Pf.off64, im, qs, qv, os[a1], ov[b1]));
+            bin = setbin0(d64, S.binstep);
+            bulk = S.usecutoff ? (d64 > S.dbulk) : 0;
+            st.guard_pairs += nimg;
+            st.maxerr = fmax(st.maxerr, fabs((double)d32 - d64));
+        }
+        if (rb1 == -2) {
+            double rr = INFINITY;
+            for (int a = 0; a < S.aps; ++a) rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[a], ov[S.iref]));
+            rb1 = rr <= S.cut2 ? setbin0(sqrt(rr), S.binstep) : -1;
+            st.guard_pairs += (unsigned long long)S.aps * nimg;
+        }
+        if (SELF && rb2 == -2) {
+            double rr = INFINITY;
+            for (int b = 0; b < S.apv; ++b) rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[S.iref], ov[b]));
+            rb2 = rr <= S.cut2 ? setbin0(sqrt(rr), S.binstep) : -1;
+            st.guard_pairs += (unsigned long long)S.apv * nimg;
+        }
         apply_hit_local(S, h, false, bin, a1, (int64_t)v * S.apv + b1, b1, rb1 >= 0, rb1);
         st.hits++;
         if (SELF) {

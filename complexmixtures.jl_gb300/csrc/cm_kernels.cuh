@@ -668,7 +668,7 @@ struct Bufs {
     int gq_cap;
     int2 *rq;                       // (sample, slot)
     int rq_cap;
-    int4 *eq;                       // edge queue: 2 int4 per entry (s, v, code, frame), (a | b << 8, rb1, rb2, d32 bits)
+    int4 *eq;                       // edge queue: 3 int4 per entry (s, v, code, frame), (a | b << 8, rb1, rb2, bin), (d32 bits)
     int eq_cap;
     int *counters;                  // [0] guard queue, [1] random queue, [2] ATOMS queue, [3] edge queue
     // ATOMS
@@ -989,6 +989,12 @@ __global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, in
     const int hw = hist_words(S);
     float4 *os_all = (float4 *)(smem_raw + (((size_t)hw * 4 + 15) & ~(size_t)15));
     int *q_all = (int *)(os_all + kWarps * kMaxSmallMol);
+    if (only_multi) {
+        // nothing to do unless a frame of the chunk needs several images
+        int any = 0;
+        for (int f = threadIdx.x; f < B.nf; f += blockDim.x) any |= B.FS[f].multi;
+        if (!__syncthreads_or(any)) return;
+    }
     shist_zero(S, hbase);
     __syncthreads();
     SHist h = shist_bind(S, hbase);

@@ -610,7 +610,7 @@ void plan(cm_handle *h, const cm_frames *f) {
         h->gq_cap = (int)(bound <= (1LL << 24) ? std::max<int64_t>(bound, 1024)
                                                : std::min<int64_t>(std::max<int64_t>(1 << 20, 64 * ms * fc), 1LL << 25));
         dev_alloc(h, h->gq, (size_t)h->gq_cap * sizeof(int4));
-        dev_alloc(h, h->eq, (size_t)h->gq_cap * 2 * sizeof(int4));
+        dev_alloc(h, h->eq, (size_t)h->gq_cap * 3 * sizeof(int4));
         if (h->mddf) {
             // random-insertion queue: every slot of `chunk` samples fits
             const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>((int64_t)fc * d.n_random_samples, (1 << 23) / mv));
@@ -1209,7 +1209,7 @@ void noalloc_fixed(cm_handle *h, Carve &c) {
     c.take(h->cq32, mv * 16);
     h->gq_cap = (int)std::min<int64_t>(std::max<int64_t>(ms * mv, 1024), 1 << 18);
     c.take(h->gq, (size_t)h->gq_cap * sizeof(int4));
-    c.take(h->eq, (size_t)h->gq_cap * 2 * sizeof(int4));
+    c.take(h->eq, (size_t)h->gq_cap * 3 * sizeof(int4));
     if (h->mddf) {
         h->rq_cap = (int)std::min<int64_t>(std::max<int64_t>((int64_t)d.n_random_samples * mv, mv), std::max<int64_t>(mv, 1 << 18));
         c.take(h->rq, (size_t)h->rq_cap * sizeof(int2));
