@@ -217,10 +217,11 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
         return;
     }
     const int bulk = S.usecutoff ? (dmin > g.dbulk_hi) : 0;
-    apply_hit_local(S, h, false, bin, a1, (int64_t)v * apv + b1, b1, rb1 >= 0, rb1);
-    st.hits++;
     if (SELF) {
-        apply_hit_local(S, h, false, bin, b1, (int64_t)s * S.aps + a1, a1, rb2 >= 0, rb2);
+        apply_pair_self(S, h, bin, a1, (int64_t)s * S.aps + a1, b1, (int64_t)v * apv + b1, rb1 >= 0, rb1, rb2 >= 0, rb2);
+        st.hits += 2;
+    } else {
+        apply_hit_local(S, h, false, bin, a1, (int64_t)v * apv + b1, b1, rb1 >= 0, rb1);
         st.hits++;
     }
     if (Pf.slot) {

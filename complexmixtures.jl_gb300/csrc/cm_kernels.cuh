@@ -225,6 +225,37 @@ __device__ __forceinline__ void apply_hit_local(const DevSys &S, const SHist &h,
     if (ref) atomicAdd(h.rdf + rbin, 2u);
 }
 
+// Both directions of one unordered self-MDDF pair: the same md bin, the
+// solute molecule's atom a and the solvent molecule's atom b each credited
+// once per direction (both into the solute table), and each direction's
+// reference-atom row.  Equals two apply_hit_local calls with fewer atomics.
+__device__ __forceinline__ void apply_pair_self(const DevSys &S, const SHist &h, int bin, int a, int64_t ja, int b,
+                                                int64_t jb, bool ref1, int rbin1, bool ref2, int rbin2) {
+    if (bin < 0 || bin >= S.nbins || (ref1 && (rbin1 < 0 || rbin1 >= S.nbins)) ||
+        (ref2 && (rbin2 < 0 || rbin2 >= S.nbins))) {
+        raise_err(S, ERR_BIN);
+        return;
+    }
+    atomicAdd(h.md + bin, 4u);
+    if (S.default_s && S.default_v) {
+        if (a == b) {
+            add_group(S, h, false, false, a, bin, 4u);
+        } else {
+            add_group(S, h, false, false, a, bin, 2u);
+            add_group(S, h, false, false, b, bin, 2u);
+        }
+    } else {
+        // direction 1: solute atom a (local), solvent atom jb (global index);
+        // direction 2: solute atom b, solvent atom ja
+        credit_solute(S, h, false, a, bin, 1u);
+        credit_solvent(S, h, false, jb, b, bin, 1u);
+        credit_solute(S, h, false, b, bin, 1u);
+        credit_solvent(S, h, false, ja, a, bin, 1u);
+    }
+    if (ref1) atomicAdd(h.rdf + rbin1, 2u);
+    if (ref2) atomicAdd(h.rdf + rbin2, 2u);
+}
+
 __device__ __forceinline__ void apply_hit(const DevSys &S, const SHist &h, bool rnd, int bin, int i_local, int64_t j, bool ref,
                                           int rbin) {
     apply_hit_local(S, h, rnd, bin, i_local, j, (int)j % S.apv, ref, rbin);
