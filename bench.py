@@ -18,6 +18,9 @@ frames through the engine.
   cpu_baseline  the CPU restatement of the reference's per-frame path (oracle,
               all host threads) on a bounded sample of the frames
 
+--workload c1 | c2-water | c2-cosolvent | c4 prints the frames/s of that
+configuration's system (ATOMS layout) instead of the headline line.
+
 --impl reference times that CPU path alone (the reference itself is Julia
 and cannot run here).  Multi-GPU runs are independent replicas (the path
 shards by frames with no exchange), launched one rank per GPU.
@@ -65,6 +68,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4"],
+                   help="c3 (default): the headline line; the others: frames/s of that configuration's system "
+                        "(ATOMS layout) on device-resident frames")
     return p.parse_args()
 
 
@@ -379,11 +385,73 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def other_workload(args, local):
+    """Frames/s of one ATOMS-layout configuration (FP32 + guard, frames in
+    HBM), with the per-class kernel times; the config-4 case is its median
+    system (43,000 atoms)."""
+    import torch
+
+    import __graft_entry__ as entry
+
+    cm = entry.load_package()
+    torch.cuda.set_device(local)
+    syn = __import__("importlib").import_module("complexmixtures_gb300.synth")
+    nframes, solvent = 10, 0
+    if args.workload == "c1":
+        sysm = syn.config1()
+    elif args.workload.startswith("c2"):
+        sysm, nframes = syn.config2(), 4
+        solvent = 0 if args.workload == "c2-water" else 1
+    else:
+        sysm = syn.config4_system(43000, 20261207 + 43000, nframes=16)
+        nframes = 16
+    xs, xv, cells = sysm.frames(nframes, solvent=solvent)
+    sv = sysm.solvents[solvent]
+    aps = sysm.solute_natomspermol
+    kw = dict(solute_nmols=sysm.solute_nmols, solute_natomspermol=aps, solvent_nmols=sv.nmols,
+              solvent_natomspermol=sv.natomspermol, autocorrelation=False, irefatom=1, cutoff=sysm.cutoff,
+              binstep=sysm.binstep, dbulk=sysm.cutoff, usecutoff=False, nbins=cm.setbin(sysm.cutoff, sysm.binstep),
+              n_random_samples=sysm.n_random_samples, seed=sysm.seed, device=local,
+              solute_groups=[[i // 10] for i in range(aps)], solute_ngroups=(aps + 9) // 10)
+    xd = torch.from_numpy(xs).to(f"cuda:{local}")
+    vd = torch.from_numpy(xv).to(f"cuda:{local}")
+    ids = np.arange(1, nframes + 1)
+    eng = cm.Engine(precision="fp32", kernel_timing=True, **kw)
+    stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=f"cuda:{local}")
+    for _ in range(max(args.warmup, 1)):
+        eng.submit(xd, vd, cells, frame_ids=ids)
+    eng.synchronize()
+    eng.reset()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        eng.submit(xd, vd, cells, frame_ids=ids)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    kt = eng.kernel_times()
+    st = eng.stats()
+    eng.close()
+    frames = args.steps * nframes
+    print(json.dumps({
+        "workload": args.workload, "metric": "MDDF frames/s", "value": frames / (ms / 1e3), "unit": "frames/s",
+        "steps": args.steps, "warmup": args.warmup, "frames_per_step": nframes,
+        "atoms": {"solute": int(sysm.solute_nmols * aps), "solvent": int(sv.nmols * sv.natomspermol)},
+        "layout": "ATOMS" if st["regime"] == 2 else "PAIRS",
+        "kernel_ms_per_frame": {k: v[0] / frames for k, v in kt.items()},
+        "precision": "fp32 search, fp64 guard band", "data": "synthetic (seeded generator of the configuration)",
+    }), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload != "c3":
+        if rank == 0:
+            other_workload(args, local)
         return
     import torch
 

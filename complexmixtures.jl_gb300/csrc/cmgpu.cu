@@ -1702,7 +1702,7 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
                        (desc->regime == CM_REGIME_AUTO &&
                         (desc->solute_natomspermol > kMaxSmallMol || desc->solvent_natomspermol > kMaxSmallMol));
     // ATOMS: cutoff / (lcell k); PAIRS: the molecule cell and smaller ones
-    const int cand_atoms[] = {100, 67, 50, 40};
+    const int cand_atoms[] = {100, 80, 50, 34};
     const int cand_pairs[] = {100, 75, 60, 50};
     const int *cand = atoms ? cand_atoms : cand_pairs;
     const int ncand = 4;
