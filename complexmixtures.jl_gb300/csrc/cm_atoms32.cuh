@@ -41,7 +41,7 @@ __global__ void k_atoms_near(Bufs B) {
     for (int dz = -F.La[2]; dz <= F.La[2] && !near; ++dz)
         for (int dy = -F.La[1]; dy <= F.La[1] && !near; ++dy)
             for (int dx = -F.La[0]; dx <= F.La[0]; ++dx) {
-                const int c = (wrapi(cz + dz, n2) * n1 + wrapi(cy + dy, n1)) * n0 + wrapi(cx + dx, n0);
+                const int c = (wrap_cell(cz + dz, n2) * n1 + wrap_cell(cy + dy, n1)) * n0 + wrap_cell(cx + dx, n0);
                 if (cs[c + 1] > cs[c]) {
                     near = 1;
                     break;
@@ -185,11 +185,11 @@ __device__ __forceinline__ void atoms_walk(const FrameGeom &G, const FrameScratc
                                            float prune2, Body &&body) {
     const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
     for (int dz = -F.La[2]; dz <= F.La[2]; ++dz) {
-        const int zc = wrapi(st.cz + dz, n2);
+        const int zc = wrap_cell(st.cz + dz, n2);
         for (int dy = -F.La[1]; dy <= F.La[1]; ++dy) {
-            const int row = (zc * n1 + wrapi(st.cy + dy, n1)) * n0;
+            const int row = (zc * n1 + wrap_cell(st.cy + dy, n1)) * n0;
             for (int dx = -F.La[0]; dx <= F.La[0]; ++dx) {
-                const int cell = row + wrapi(st.cx + dx, n0);
+                const int cell = row + wrap_cell(st.cx + dx, n0);
                 const int beg = cs[cell], end = cs[cell + 1];
                 if (beg == end) continue;
                 if (cell_d2(F, st, dx, dy, dz) > prune2) continue;
@@ -405,8 +405,8 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bu
                         for (int dz = -F.La[2]; dz <= F.La[2]; ++dz)
                             for (int dy = -F.La[1]; dy <= F.La[1]; ++dy)
                                 for (int dx = -F.La[0]; dx <= F.La[0]; ++dx) {
-                                    const int cell = (wrapi(cz + dz, G.n[2]) * G.n[1] + wrapi(cy + dy, G.n[1])) * G.n[0] +
-                                                     wrapi(cx + dx, G.n[0]);
+                                    const int cell = (wrap_cell(cz + dz, G.n[2]) * G.n[1] + wrap_cell(cy + dy, G.n[1])) * G.n[0] +
+                                                     wrap_cell(cx + dx, G.n[0]);
                                     if (T.p1 < cs[cell] || T.p1 >= cs[cell + 1]) continue;
                                     const d4 o = off64[off_index(dx, dy, dz)];
                                     best = fmin(best, pair_d2_64(sub(qb.x, o.x), sub(qb.y, o.y), sub(qb.z, o.z), qa.x, qa.y,

@@ -117,4 +117,8 @@ CM_HD int wrapi(int c, int n) {
     return r < 0 ? r + n : r;
 }
 
+// wrapi for cell coordinates that are almost always in range already (a
+// stencil offset from an in-range cell): the modulo only when they are not.
+CM_HD int wrap_cell(int c, int n) { return (unsigned)c < (unsigned)n ? c : wrapi(c, n); }
+
 }  // namespace cmgeom

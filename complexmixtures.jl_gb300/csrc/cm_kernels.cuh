@@ -941,13 +941,13 @@ __device__ __forceinline__ void walk_candidates(const FrameGeom &G, const FrameS
     int cnt = 0;
     for (int iz = 0; iz < e2; ++iz) {
         const int dz = m2 ? iz - cz : iz - F.L[2];
-        const int zc = m2 ? iz : wrapi(cz + dz, n2);
+        const int zc = m2 ? iz : wrap_cell(cz + dz, n2);
         for (int iy = 0; iy < e1; ++iy) {
             const int dy = m1 ? iy - cy : iy - F.L[1];
-            const int yc = m1 ? iy : wrapi(cy + dy, n1);
+            const int yc = m1 ? iy : wrap_cell(cy + dy, n1);
             for (int ix = 0; ix < e0; ++ix) {
                 const int dx = m0 ? ix - cx : ix - F.L[0];
-                const int xc = m0 ? ix : wrapi(cx + dx, n0);
+                const int xc = m0 ? ix : wrap_cell(cx + dx, n0);
                 const int cell = (zc * n1 + yc) * n0 + xc;
                 const int beg = cstart[cell], end = cstart[cell + 1];
                 if (beg == end) continue;

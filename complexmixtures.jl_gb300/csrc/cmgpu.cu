@@ -1207,7 +1207,7 @@ void noalloc_fixed(cm_handle *h, Carve &c) {
     }
     c.take(h->cmol, mv * 4);
     c.take(h->cq32, mv * 16);
-    h->gq_cap = (int)std::min<int64_t>(std::max<int64_t>(ms * mv, 1024), 1 << 18);
+    h->gq_cap = (int)std::min<int64_t>(std::max<int64_t>(ms * mv, 1024), 1 << 17);
     c.take(h->gq, (size_t)h->gq_cap * sizeof(int4));
     c.take(h->eq, (size_t)h->gq_cap * 3 * sizeof(int4));
     if (h->mddf) {
