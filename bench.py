@@ -279,9 +279,10 @@ C4_FRAMES = 8               # frames per config-4 system (config 4 has 50)
 
 def batched_c4_leg(cm, device):
     """Config-4 load: 64 independent systems of uneven size (2,000-200,000
-    atoms, 5 % chain + water) run one at a time, then submitted together to
-    the request server, which runs them concurrently on the device; the cell
-    size comes from the autotuner on the median system."""
+    atoms, 5 % chain + water) run one at a time; as one batch whose kernels
+    of all systems are one CUDA graph launch per staging round; and submitted
+    together to the request server, which runs them concurrently on the
+    device.  The cell size comes from the autotuner on the median system."""
     import torch
 
     syn = __import__("importlib").import_module("complexmixtures_gb300.synth")
@@ -314,8 +315,25 @@ def batched_c4_leg(cm, device):
             eng.close()
         return time.perf_counter() - t, out
 
+    def graph_batch():
+        # all 64 systems in one cm_batch: one CUDA graph launch per staging round
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        engines = [cm.Engine(cell_scale_pct=pct, **kw) for xs, xv, cells, kw in systems]
+        with cm.Batch(engines) as b:
+            b.submit([(xs, xv, cells) for xs, xv, cells, kw in systems])
+            gst = b.graph_stats()
+        out = [e.raw_counts() for e in engines]
+        for e in engines:
+            e.close()
+        return time.perf_counter() - t, out, gst
+
     serial()  # warm-up
     ts, ref = serial()
+    graph_batch()  # warm-up
+    tg, gout, gst = graph_batch()
+    same_graph = all(all(np.array_equal(gout[i][k], ref[i][k]) for k in ("md", "md_random", "solute_group"))
+                     for i in range(len(systems)))
     with cm.Server(device=device, frames_per_turn=C4_FRAMES) as srv:
         t0 = time.perf_counter()
         ids = [srv.submit(xs, xv, cells, cell_scale_pct=pct, **kw) for xs, xv, cells, kw in systems]
@@ -330,6 +348,9 @@ def batched_c4_leg(cm, device):
         "frames": frames_total,
         "serial_frames_per_s": frames_total / ts,
         "batched_frames_per_s": frames_total / tb,
+        "graph_batch_frames_per_s": frames_total / tg,
+        "graph_batch_launches": gst["graph_launches"],
+        "graph_batch_counts_identical_to_serial": bool(same_graph),
         "p50_ms": pct_lat["p50"], "p99_ms": pct_lat["p99"],
         "cell_scale_pct": pct, "autotune_ms_per_frame": tune["candidates"],
         "failed": sum(1 for x in infos if x["state"] != "done"),

@@ -15,7 +15,7 @@ from .results import (Density, Result, Volume, finalresults, renormalize, result
 from .trajectory import (ArrayTrajectory, NamdDCD, PDBTraj, Trajectory, TrajectoryMetaData, convert_unitcell,
                          make_trajectory, trajectory_metadata, unitcell_from_lengths_angles)
 from .contributions import contributions
-from .engine import Engine, autotune
+from .engine import Batch, Engine, autotune, memory_cache
 from .server import Server, latency_percentiles
 from .mddf import coordination_number, engine_for, mddf, new_result
 from ._native import NativeUnavailable
@@ -26,5 +26,5 @@ __all__ = [
     "Volume", "finalresults", "renormalize", "result_from_json", "setbin", "shellradius", "sphericalshellvolume",
     "sum_results", "units", "ArrayTrajectory", "NamdDCD", "PDBTraj", "Trajectory", "TrajectoryMetaData",
     "convert_unitcell", "make_trajectory", "trajectory_metadata", "unitcell_from_lengths_angles", "contributions",
-    "Engine", "autotune", "Server", "latency_percentiles", "coordination_number", "engine_for", "mddf", "new_result", "NativeUnavailable",
+    "Batch", "Engine", "autotune", "memory_cache", "Server", "latency_percentiles", "coordination_number", "engine_for", "mddf", "new_result", "NativeUnavailable",
 ]

@@ -12,11 +12,12 @@ from typing import Optional
 
 import numpy as np
 
-CM_API_VERSION = 1
+CM_API_VERSION = 2
 CM_OK, CM_EINVAL, CM_ENOMEM, CM_ECUDA, CM_EDEVICE, CM_ESTATE = range(6)
 CM_MODE_MDDF, CM_MODE_COORDINATION_NUMBER = 0, 1
 CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
 CM_REGIME_AUTO, CM_REGIME_PAIRS, CM_REGIME_ATOMS = 0, 1, 2
+CM_LAUNCH_AUTO, CM_LAUNCH_STREAM, CM_LAUNCH_GRAPH = 0, 1, 2
 CM_COORD_F64, CM_COORD_F32 = 0, 1
 CM_MEM_HOST, CM_MEM_DEVICE = 0, 1
 CM_NOALLOC_SCRATCH_BYTES = 32 << 20
@@ -61,6 +62,8 @@ class cm_system_desc(C.Structure):
         ("hbm_budget_bytes", C.c_int64),
         ("kernel_timing", C.c_int32),
         ("cell_scale_pct", C.c_int32),
+        ("launch", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -125,6 +128,8 @@ class cm_stats(C.Structure):
         ("regime", C.c_int32),
         ("kernels_per_frame", C.c_int32),
         ("kernel_launches", C.c_int64),
+        ("graph_launches", C.c_int64),
+        ("graph_instantiations", C.c_int64),
     ]
 
 
@@ -175,6 +180,11 @@ EXPORTED = (
     "cm_create",
     "cm_submit_frames",
     "cm_synchronize",
+    "cm_batch_create",
+    "cm_batch_submit",
+    "cm_batch_graph_stats",
+    "cm_batch_destroy",
+    "cm_batch_last_error",
     "cm_read_counts",
     "cm_read_raw_counts",
     "cm_get_stats",
@@ -184,6 +194,7 @@ EXPORTED = (
     "cm_last_error",
     "cm_status_string",
     "cm_device_bytes",
+    "cm_memory_cache",
     "cm_stream",
     "cm_measure_fp32_peak",
     "cm_frame_counts_noalloc",
@@ -241,6 +252,18 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_status_string.restype = C.c_char_p
     lib.cm_device_bytes.argtypes = [H]
     lib.cm_device_bytes.restype = C.c_int64
+    lib.cm_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
+    lib.cm_batch_create.restype = C.c_int
+    lib.cm_batch_submit.argtypes = [C.c_void_p, C.POINTER(cm_frames)]
+    lib.cm_batch_submit.restype = C.c_int
+    lib.cm_batch_graph_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.cm_batch_graph_stats.restype = C.c_int
+    lib.cm_batch_destroy.argtypes = [C.c_void_p]
+    lib.cm_batch_destroy.restype = C.c_int
+    lib.cm_batch_last_error.argtypes = [C.c_void_p]
+    lib.cm_batch_last_error.restype = C.c_char_p
+    lib.cm_memory_cache.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.cm_memory_cache.restype = C.c_int
     lib.cm_stream.argtypes = [H]
     lib.cm_stream.restype = C.c_void_p
     lib.cm_measure_fp32_peak.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_double)]
@@ -269,13 +292,15 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     return lib
 
 
-def raise_for(status: int, handle, server=None) -> None:
+def raise_for(status: int, handle, server=None, batch=None) -> None:
     """Turn a cm_status into the exception the reference raises for it."""
     if status == CM_OK:
         return
     lib = load()
     if server is not None:
         msg = lib.cm_server_last_error(server).decode(errors="replace")
+    elif batch is not None:
+        msg = lib.cm_batch_last_error(batch).decode(errors="replace")
     else:
         msg = lib.cm_last_error(handle).decode(errors="replace")
     what = lib.cm_status_string(status).decode()

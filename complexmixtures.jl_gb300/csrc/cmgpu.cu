@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -34,7 +35,8 @@ thread_local std::string g_create_error;
 
 struct DevBuf {
     void *p = nullptr;
-    size_t bytes = 0;
+    size_t bytes = 0;    // size of the block
+    size_t charged = 0;  // what the handle's memory budget counts: the request rounded to the allocation step
 };
 
 struct cm_error : std::exception {
@@ -49,6 +51,101 @@ struct cm_error : std::exception {
         if (_e != cudaSuccess)                                                                         \
             throw cm_error(CM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e));              \
     } while (0)
+
+// Process-wide cache of device and pinned host blocks.  cudaFree and
+// cudaFreeHost wait for the whole device, so a handle that closed (or grew a
+// buffer) while other handles had work queued stalled all of them: a request
+// server that opens and closes a handle per request then runs its requests
+// one after the other.  Handles return their blocks here instead, and a later
+// handle takes the smallest free block within 12.5 % of its request (rounded
+// to the allocation step).  Blocks go back to the driver only on an
+// allocation failure (then the device's free blocks are released and the
+// allocation retried once) or through cm_release_cached_memory.
+class BlockCache {
+  public:
+    static constexpr int kMaxDevices = 64;
+
+    static size_t round_up(size_t bytes) {
+        const size_t step = bytes >= (size_t(1) << 20) ? (size_t(2) << 20) : 4096;
+        return (std::max<size_t>(bytes, 16) + step - 1) / step * step;
+    }
+
+    // A block of at least `bytes` (its size in *got).  `host` selects pinned
+    // host memory (cudaMallocHost) instead of device memory.
+    void *get(int device, bool host, size_t bytes, size_t *got) {
+        const size_t want = round_up(bytes);
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            auto &fl = list(device, host);
+            auto it = fl.lower_bound(want);
+            if (it != fl.end() && it->first <= want + want / 8) {
+                void *p = it->second;
+                *got = it->first;
+                cached_[host][device] -= it->first;
+                fl.erase(it);
+                return p;
+            }
+        }
+        void *p = nullptr;
+        cudaError_t e = host ? cudaMallocHost(&p, want) : cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            release(device, host);
+            e = host ? cudaMallocHost(&p, want) : cudaMalloc(&p, want);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                *got = 0;
+                return nullptr;
+            }
+        }
+        *got = want;
+        return p;
+    }
+
+    void put(int device, bool host, void *p, size_t bytes) {
+        if (!p) return;
+        std::lock_guard<std::mutex> lock(mu_);
+        list(device, host).emplace(bytes, p);
+        cached_[host][device] += bytes;
+    }
+
+    // Return the free blocks of one device (or all devices for -1) to the driver.
+    void release(int device, bool host) {
+        std::multimap<size_t, void *> drop;
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            for (int dv = 0; dv < kMaxDevices; ++dv) {
+                if (device >= 0 && dv != device) continue;
+                drop.insert(free_[host][dv].begin(), free_[host][dv].end());
+                free_[host][dv].clear();
+                cached_[host][dv] = 0;
+            }
+        }
+        for (auto &kv : drop) {
+            if (host) cudaFreeHost(kv.second);
+            else cudaFree(kv.second);
+        }
+    }
+
+    size_t cached(int device, bool host) {
+        std::lock_guard<std::mutex> lock(mu_);
+        return device >= 0 && device < kMaxDevices ? cached_[host][device] : 0;
+    }
+
+  private:
+    std::multimap<size_t, void *> &list(int device, bool host) {
+        if (device < 0 || device >= kMaxDevices) throw cm_error(CM_EINVAL, "device index out of range");
+        return free_[host][device];
+    }
+    std::mutex mu_;
+    std::multimap<size_t, void *> free_[2][kMaxDevices];
+    size_t cached_[2][kMaxDevices] = {};
+};
+
+BlockCache &blocks() {
+    static BlockCache *c = new BlockCache();  // never destroyed: blocks outlive static destructors
+    return *c;
+}
 
 constexpr int kChunkSamples = 32;  // random samples placed per launch in the ATOMS regime
 
@@ -100,6 +197,7 @@ struct cm_handle {
     Sample *h_samples[2] = {nullptr, nullptr};
     int4 *h_tabs[2] = {nullptr, nullptr};
     int64_t h_samples_cap = 0;
+    std::vector<DevBuf> host_blocks;  // the pinned blocks above, as taken from the block cache
 
     // accumulation state
     bool class_open = false;
@@ -113,6 +211,11 @@ struct cm_handle {
     double last_guard = 0.0;
     int kernels_per_frame = 0;
     int chunk_parity = 0;
+
+    // CUDA-graph launch of compute chunks
+    bool graphs = false;
+    cudaGraphExec_t gexec = nullptr;
+    int64_t graph_launches = 0, graph_instantiations = 0;
 
     // launch accounting and optional per-launch event timing
     int64_t launches_total = 0;
@@ -131,25 +234,41 @@ struct cm_handle {
 
 namespace {
 
+// Wait for the handle's own queued work (not the device's), so that its
+// blocks can go back to the cache.
+void quiesce(cm_handle *h) {
+    if (h->stream) CM_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->copy_stream) CM_CUDA(cudaStreamSynchronize(h->copy_stream));
+}
+
 void dev_alloc(cm_handle *h, DevBuf &b, size_t bytes) {
     if (b.bytes >= bytes && b.p) return;
     if (b.p) {
-        cudaFree(b.p);
-        h->device_bytes -= (int64_t)b.bytes;
+        quiesce(h);  // queued kernels of this handle may still read the old block
+        blocks().put(h->device, false, b.p, b.bytes);
+        h->device_bytes -= (int64_t)b.charged;
         b.p = nullptr;
-        b.bytes = 0;
+        b.bytes = b.charged = 0;
     }
-    if (bytes == 0) bytes = 16;
-    if (h->d.hbm_budget_bytes > 0 && h->device_bytes + (int64_t)bytes > h->d.hbm_budget_bytes)
-        throw cm_error(CM_ENOMEM, "device memory budget exceeded (" + std::to_string(h->device_bytes + (int64_t)bytes) +
+    const size_t want = BlockCache::round_up(bytes);
+    if (h->d.hbm_budget_bytes > 0 && h->device_bytes + (int64_t)want > h->d.hbm_budget_bytes)
+        throw cm_error(CM_ENOMEM, "device memory budget exceeded (" + std::to_string(h->device_bytes + (int64_t)want) +
                                       " > " + std::to_string(h->d.hbm_budget_bytes) + " bytes)");
-    cudaError_t e = cudaMalloc(&b.p, bytes);
-    if (e != cudaSuccess) {
-        b.p = nullptr;
-        throw cm_error(CM_ENOMEM, std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
-    }
-    b.bytes = bytes;
-    h->device_bytes += (int64_t)bytes;
+    size_t got = 0;
+    b.p = blocks().get(h->device, false, bytes, &got);
+    if (!b.p) throw cm_error(CM_ENOMEM, "cudaMalloc(" + std::to_string(want) + "): out of device memory");
+    b.bytes = got;
+    b.charged = want;  // independent of which cached block was reused
+    h->device_bytes += (int64_t)want;
+}
+
+// Pinned host staging from the block cache.
+template <typename T>
+void host_alloc(cm_handle *h, T *&p, size_t bytes) {
+    size_t got = 0;
+    p = static_cast<T *>(blocks().get(h->device, true, bytes, &got));
+    if (!p) throw cm_error(CM_ENOMEM, "cudaMallocHost(" + std::to_string(bytes) + "): out of pinned host memory");
+    h->host_blocks.push_back({(void *)p, got});
 }
 
 template <typename T>
@@ -224,6 +343,7 @@ void check_desc(const cm_system_desc *d) {
     auto bad = [](const std::string &m) { throw cm_error(CM_EINVAL, m); };
     if (!d) bad("NULL system description");
     if (d->api_version != CM_API_VERSION) bad("api_version mismatch");
+    if (d->launch < CM_LAUNCH_AUTO || d->launch > CM_LAUNCH_GRAPH) bad("unknown launch mode");
     if (d->solute_nmols < 1 || d->solute_natomspermol < 1 || d->solvent_nmols < 1 || d->solvent_natomspermol < 1)
         bad("selections must have at least one molecule of at least one atom");
     if (d->autocorrelation && (d->solute_nmols != d->solvent_nmols || d->solute_natomspermol != d->solvent_natomspermol))
@@ -324,7 +444,8 @@ DevSys devsys_full(cm_handle *h) {
 void upload_groups(cm_handle *h) {
     auto up = [&](DevBuf &b, const void *src, size_t bytes) {
         dev_alloc(h, b, bytes);
-        if (bytes) CM_CUDA(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
+        // on the handle's stream: the caller's next stream sync covers the copy
+        if (bytes) CM_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, h->stream));
     };
     if (!h->gs_off.empty()) {
         up(h->g_soff, h->gs_off.data(), h->gs_off.size() * 8);
@@ -559,14 +680,14 @@ void plan(cm_handle *h, const cm_frames *f) {
 
     // staging of geometries, samples and bulk tables (two chunks in flight)
     dev_alloc(h, h->geoms, sizeof(FrameGeom) * h->max_frames * 2);
-    for (int i = 0; i < 2; ++i) CM_CUDA(cudaMallocHost((void **)&h->h_geoms[i], sizeof(FrameGeom) * h->max_frames));
+    for (int i = 0; i < 2; ++i) host_alloc(h, h->h_geoms[i], sizeof(FrameGeom) * h->max_frames);
     if (h->mddf) {
         h->h_samples_cap = (int64_t)h->max_frames * d.n_random_samples;
         dev_alloc(h, h->samples, sizeof(Sample) * h->h_samples_cap * 2);
         dev_alloc(h, h->tabs, sizeof(int4) * (size_t)h->max_frames * h->ndist_max * 2);
         for (int i = 0; i < 2; ++i) {
-            CM_CUDA(cudaMallocHost((void **)&h->h_samples[i], sizeof(Sample) * h->h_samples_cap));
-            CM_CUDA(cudaMallocHost((void **)&h->h_tabs[i], sizeof(int4) * (size_t)h->max_frames * h->ndist_max));
+            host_alloc(h, h->h_samples[i], sizeof(Sample) * h->h_samples_cap);
+            host_alloc(h, h->h_tabs[i], sizeof(int4) * (size_t)h->max_frames * h->ndist_max);
         }
     }
     if (f->memory == CM_MEM_HOST) {
@@ -583,7 +704,7 @@ void plan(cm_handle *h, const cm_frames *f) {
     if (h->mddf) {
         const int nd = h->ndist_max;
         dev_alloc(h, h->slot, (size_t)fc * ms * 4);
-        CM_CUDA(cudaMemset(h->slot.p, 0xff, (size_t)fc * ms * 4));
+        CM_CUDA(cudaMemsetAsync(h->slot.p, 0xff, (size_t)fc * ms * 4, h->stream));
         dev_alloc(h, h->flags, (size_t)fc * nd * mv);
         dev_alloc(h, h->bulk, (size_t)fc * nd * mv * 4);
         dev_alloc(h, h->nbulk, (size_t)fc * nd * 4);
@@ -935,7 +1056,63 @@ void fold_class(cm_handle *h) {
 // Frames per compute chunk.
 int chunk_frames(const cm_handle *h) { return h->fc; }
 
-void submit(cm_handle *h, const cm_frames *f) {
+// Capture one compute chunk's chain (memsets and kernels on the handle's
+// stream) as a CUDA graph and replay it through the handle's executable graph.
+// Consecutive chunks of a system have the same chain with other arguments and
+// grid sizes, so the executable graph is updated in place; a chain of another
+// shape (fewer frames, another number of queue pieces) instantiates it anew.
+// Launches already queued are not affected by the update.
+template <typename Fn>
+void launch_captured(cm_handle *h, Fn &&chain) {
+    CM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t g = nullptr;
+    try {
+        chain();
+    } catch (...) {
+        cudaStreamEndCapture(h->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        throw;
+    }
+    CM_CUDA(cudaStreamEndCapture(h->stream, &g));
+    bool updated = false;
+    if (h->gexec) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(h->gexec, g, &info) == cudaSuccess;
+        if (!updated) {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(h->gexec);  // freed once its queued launches finish
+            h->gexec = nullptr;
+        }
+    }
+    if (!updated) {
+        const cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            h->gexec = nullptr;
+            throw cm_error(CM_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+        h->graph_instantiations++;
+    }
+    cudaGraphDestroy(g);
+    CM_CUDA(cudaGraphLaunch(h->gexec, h->stream));
+    h->graph_launches++;
+}
+
+// One staging batch of a submit: frames [f0, f0 + nf) of the caller's batch,
+// copied into the handle's staging buffers of parity b and split into chunks.
+struct Staged {
+    int b = 0, f0 = 0, nf = 0, elem = 0;
+    const FrameGeom *hg = nullptr;
+    FrameGeom *dG = nullptr;
+    Sample *dS = nullptr;
+    int4 *dT = nullptr;
+    const char *xs_base = nullptr, *xv_base = nullptr;
+    int64_t sbytes = 0, vbytes = 0;
+    std::vector<Chunk> chunks;
+};
+
+void check_frames(cm_handle *h, const cm_frames *f) {
     const cm_system_desc &d = h->d;
     if (!f || f->nframes < 0) throw cm_error(CM_EINVAL, "invalid frame batch");
     if (f->nframes == 0) return;
@@ -944,110 +1121,142 @@ void submit(cm_handle *h, const cm_frames *f) {
     if (f->coord_type != CM_COORD_F32 && f->coord_type != CM_COORD_F64) throw cm_error(CM_EINVAL, "unknown coord_type");
     if (f->memory != CM_MEM_HOST && f->memory != CM_MEM_DEVICE) throw cm_error(CM_EINVAL, "unknown memory kind");
     if (!h->planned) plan(h, f);
-    int elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
+    const int elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
     if (elem != h->coord_elem && f->memory == CM_MEM_HOST)
         throw cm_error(CM_EINVAL, "coordinate type differs from the first batch of this handle");
     for (int i = 0; i < f->nframes; ++i) {
         double w = f->weights ? f->weights[i] : 1.0;
         if (!std::isfinite(w) || w < 0.0) throw cm_error(CM_EINVAL, "frame weights must be finite and non-negative");
     }
+}
+
+// Host preparation (geometries, random samples, chunking) and the copies of
+// one staging batch; the copies end with ev_copied[b] on the copy stream.
+Staged stage(cm_handle *h, const cm_frames *f, int f0) {
+    const cm_system_desc &d = h->d;
+    Staged S;
+    S.elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
+    S.f0 = f0;
+    S.sbytes = h->Ns * 3 * S.elem;
+    S.vbytes = h->Nv * 3 * S.elem;
     const double cs = target_cell(h);
     const int fce = chunk_frames(h);
-    const int64_t sbytes = h->Ns * 3 * elem, vbytes = h->Nv * 3 * elem;
-    for (int f0 = 0; f0 < f->nframes; f0 += h->max_frames) {
-        const int nf = std::min(h->max_frames, f->nframes - f0);
-        const int b = h->chunk_parity;
-        h->chunk_parity ^= 1;
-        // host staging of this batch may be reused only after its previous copy finished
-        CM_CUDA(cudaEventSynchronize(h->ev_copied[b]));
-        FrameGeom *hg = h->h_geoms[b];
-        Sample *hs = h->h_samples[b];
-        int4 *ht = h->h_tabs[b];
-        int soff = 0;
-        for (int i = 0; i < nf; ++i) {
-            FrameGeom &G = hg[i];
-            memset(&G, 0, sizeof(G));
-            frame_geometry(f->cells + 9 * (int64_t)(f0 + i), cs, 1023, G);
-            G.weight = f->weights ? f->weights[f0 + i] : 1.0;
-            G.frame_id = f->frame_ids[f0 + i];
-            G.sample_off = soff;
-            if (h->mddf) {
-                int nd = 0;
-                G.nsamples = draw_samples(h, G.frame_id, hs + soff, nd);
-                G.ndistinct = nd;
-                soff += G.nsamples;
-            }
+    const int nf = S.nf = std::min(h->max_frames, f->nframes - f0);
+    const int b = S.b = h->chunk_parity;
+    h->chunk_parity ^= 1;
+    // host staging of this batch may be reused only after its previous copy finished
+    CM_CUDA(cudaEventSynchronize(h->ev_copied[b]));
+    FrameGeom *hg = h->h_geoms[b];
+    Sample *hs = h->h_samples[b];
+    int4 *ht = h->h_tabs[b];
+    S.hg = hg;
+    int soff = 0;
+    for (int i = 0; i < nf; ++i) {
+        FrameGeom &G = hg[i];
+        memset(&G, 0, sizeof(G));
+        frame_geometry(f->cells + 9 * (int64_t)(f0 + i), cs, 1023, G);
+        G.weight = f->weights ? f->weights[f0 + i] : 1.0;
+        G.frame_id = f->frame_ids[f0 + i];
+        G.sample_off = soff;
+        if (h->mddf) {
+            int nd = 0;
+            G.nsamples = draw_samples(h, G.frame_id, hs + soff, nd);
+            G.ndistinct = nd;
+            soff += G.nsamples;
         }
-        // compute chunks: runs of equal non-zero weight (zero-weight frames are
-        // skipped, src/mddf.jl:102), at most fce frames each
-        std::vector<Chunk> chunks;
-        int ntab = 0;
-        for (int i = 0; i < nf;) {
-            if (hg[i].weight == 0.0) {
-                ++i;
-                continue;
-            }
-            Chunk c;
-            c.c0 = i;
-            c.weight = hg[i].weight;
-            c.smp0 = hg[i].sample_off;
-            c.tab0 = ntab;
-            int j = i;
-            while (j < nf && j - i < fce && hg[j].weight == c.weight) {
-                const FrameGeom &G = hg[j];
-                c.ncell_max = std::max(c.ncell_max, G.ncell);
-                for (int k = 0; k < G.nsamples; ++k) {
-                    Sample &sm = hs[G.sample_off + k];
-                    sm.pad = j - i;
-                    if (sm.rep == 0) ht[ntab++] = make_int4(j - i, sm.d, sm.s, 0);
-                }
-                ++j;
-            }
-            c.nf = j - i;
-            c.nsmp = hg[j - 1].sample_off + hg[j - 1].nsamples - c.smp0;
-            c.ntab = ntab - c.tab0;
-            chunks.push_back(c);
-            i = j;
+    }
+    // compute chunks: runs of equal non-zero weight (zero-weight frames are
+    // skipped, src/mddf.jl:102), at most fce frames each
+    int ntab = 0;
+    for (int i = 0; i < nf;) {
+        if (hg[i].weight == 0.0) {
+            ++i;
+            continue;
         }
-        cudaStream_t cp = f->memory == CM_MEM_HOST ? h->copy_stream : h->stream;
-        CM_CUDA(cudaStreamWaitEvent(cp, h->ev_done[b], 0));
-        FrameGeom *dG = P<FrameGeom>(h->geoms) + (size_t)b * h->max_frames;
-        Sample *dS = h->mddf ? P<Sample>(h->samples) + (size_t)b * h->h_samples_cap : nullptr;
-        int4 *dT = h->mddf ? P<int4>(h->tabs) + (size_t)b * h->max_frames * h->ndist_max : nullptr;
-        CM_CUDA(cudaMemcpyAsync(dG, hg, sizeof(FrameGeom) * nf, cudaMemcpyHostToDevice, cp));
-        if (h->mddf && soff > 0) CM_CUDA(cudaMemcpyAsync(dS, hs, sizeof(Sample) * soff, cudaMemcpyHostToDevice, cp));
-        if (h->mddf && ntab > 0) CM_CUDA(cudaMemcpyAsync(dT, ht, sizeof(int4) * ntab, cudaMemcpyHostToDevice, cp));
-        const char *xs_base, *xv_base = nullptr;
-        if (f->memory == CM_MEM_HOST) {
-            CM_CUDA(cudaMemcpyAsync(h->stage_s[b].p, (const char *)f->solute_xyz + sbytes * f0, (size_t)sbytes * nf,
+        Chunk c;
+        c.c0 = i;
+        c.weight = hg[i].weight;
+        c.smp0 = hg[i].sample_off;
+        c.tab0 = ntab;
+        int j = i;
+        while (j < nf && j - i < fce && hg[j].weight == c.weight) {
+            const FrameGeom &G = hg[j];
+            c.ncell_max = std::max(c.ncell_max, G.ncell);
+            for (int k = 0; k < G.nsamples; ++k) {
+                Sample &sm = hs[G.sample_off + k];
+                sm.pad = j - i;
+                if (sm.rep == 0) ht[ntab++] = make_int4(j - i, sm.d, sm.s, 0);
+            }
+            ++j;
+        }
+        c.nf = j - i;
+        c.nsmp = hg[j - 1].sample_off + hg[j - 1].nsamples - c.smp0;
+        c.ntab = ntab - c.tab0;
+        S.chunks.push_back(c);
+        i = j;
+    }
+    cudaStream_t cp = f->memory == CM_MEM_HOST ? h->copy_stream : h->stream;
+    CM_CUDA(cudaStreamWaitEvent(cp, h->ev_done[b], 0));
+    S.dG = P<FrameGeom>(h->geoms) + (size_t)b * h->max_frames;
+    S.dS = h->mddf ? P<Sample>(h->samples) + (size_t)b * h->h_samples_cap : nullptr;
+    S.dT = h->mddf ? P<int4>(h->tabs) + (size_t)b * h->max_frames * h->ndist_max : nullptr;
+    CM_CUDA(cudaMemcpyAsync(S.dG, hg, sizeof(FrameGeom) * nf, cudaMemcpyHostToDevice, cp));
+    if (h->mddf && soff > 0) CM_CUDA(cudaMemcpyAsync(S.dS, hs, sizeof(Sample) * soff, cudaMemcpyHostToDevice, cp));
+    if (h->mddf && ntab > 0) CM_CUDA(cudaMemcpyAsync(S.dT, ht, sizeof(int4) * ntab, cudaMemcpyHostToDevice, cp));
+    if (f->memory == CM_MEM_HOST) {
+        CM_CUDA(cudaMemcpyAsync(h->stage_s[b].p, (const char *)f->solute_xyz + S.sbytes * f0, (size_t)S.sbytes * nf,
+                                cudaMemcpyHostToDevice, cp));
+        S.xs_base = (const char *)h->stage_s[b].p;
+        if (!d.autocorrelation) {
+            CM_CUDA(cudaMemcpyAsync(h->stage_v[b].p, (const char *)f->solvent_xyz + S.vbytes * f0, (size_t)S.vbytes * nf,
                                     cudaMemcpyHostToDevice, cp));
-            xs_base = (const char *)h->stage_s[b].p;
-            if (!d.autocorrelation) {
-                CM_CUDA(cudaMemcpyAsync(h->stage_v[b].p, (const char *)f->solvent_xyz + vbytes * f0, (size_t)vbytes * nf,
-                                        cudaMemcpyHostToDevice, cp));
-                xv_base = (const char *)h->stage_v[b].p;
-            }
-        } else {
-            xs_base = (const char *)f->solute_xyz + sbytes * f0;
-            if (!d.autocorrelation) xv_base = (const char *)f->solvent_xyz + vbytes * f0;
+            S.xv_base = (const char *)h->stage_v[b].p;
         }
-        CM_CUDA(cudaEventRecord(h->ev_copied[b], cp));
-        CM_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copied[b], 0));
-        for (const Chunk &c : chunks) {
-            if (h->class_open && c.weight != h->class_w) fold_class(h);
-            h->class_open = true;
-            h->class_w = c.weight;
-            const char *xs = xs_base + sbytes * c.c0;
-            const char *xv = xv_base ? xv_base + vbytes * c.c0 : nullptr;
-            if (elem == 4) run_chunk<float>(h, c, dG, dS, dT, (const float *)xs, (const float *)xv);
-            else run_chunk<double>(h, c, dG, dS, dT, (const double *)xs, (const double *)xv);
-            for (int i = c.c0; i < c.c0 + c.nf; ++i) {
-                h->volume_total += hg[i].weight * hg[i].det;  // src/mddf.jl:352
-                h->weight_total += hg[i].weight;
-                h->frames++;
-            }
+    } else {
+        S.xs_base = (const char *)f->solute_xyz + S.sbytes * f0;
+        if (!d.autocorrelation) S.xv_base = (const char *)f->solvent_xyz + S.vbytes * f0;
+    }
+    CM_CUDA(cudaEventRecord(h->ev_copied[b], cp));
+    for (const Chunk &c : S.chunks) ensure_cells(h, c.ncell_max);  // may wait for this handle's stream: never inside a capture
+    return S;
+}
+
+// The kernels of one chunk of a staged batch on the handle's stream.
+void run_staged_chunk(cm_handle *h, const Staged &S, const Chunk &c) {
+    const char *xs = S.xs_base + S.sbytes * c.c0;
+    const char *xv = S.xv_base ? S.xv_base + S.vbytes * c.c0 : nullptr;
+    if (S.elem == 4) run_chunk<float>(h, c, S.dG, S.dS, S.dT, (const float *)xs, (const float *)xv);
+    else run_chunk<double>(h, c, S.dG, S.dS, S.dT, (const double *)xs, (const double *)xv);
+}
+
+// Host accumulators of a chunk's frames (src/mddf.jl:352).
+void account_chunk(cm_handle *h, const Staged &S, const Chunk &c) {
+    for (int i = c.c0; i < c.c0 + c.nf; ++i) {
+        h->volume_total += S.hg[i].weight * S.hg[i].det;
+        h->weight_total += S.hg[i].weight;
+        h->frames++;
+    }
+}
+
+// Weight classes: a chunk of another weight first folds the open class.
+void open_class(cm_handle *h, double w) {
+    if (h->class_open && w != h->class_w) fold_class(h);
+    h->class_open = true;
+    h->class_w = w;
+}
+
+void submit(cm_handle *h, const cm_frames *f) {
+    check_frames(h, f);
+    for (int f0 = 0; f0 < f->nframes; f0 += h->max_frames) {
+        const Staged S = stage(h, f, f0);
+        CM_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copied[S.b], 0));
+        for (const Chunk &c : S.chunks) {
+            open_class(h, c.weight);
+            if (h->graphs) launch_captured(h, [&] { run_staged_chunk(h, S, c); });
+            else run_staged_chunk(h, S, c);
+            account_chunk(h, S, c);
         }
-        CM_CUDA(cudaEventRecord(h->ev_done[b], h->stream));
+        CM_CUDA(cudaEventRecord(h->ev_done[S.b], h->stream));
     }
 }
 
@@ -1088,6 +1297,9 @@ int guarded(cm_handle *h, F &&fn) {
 }
 
 void free_all(cm_handle *h) {
+    // the blocks go back to the cache: nothing of this handle may still use them
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
     DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag,
                      &h->slot, &h->flags, &h->bulk, &h->nbulk, &h->tabs, &h->counters, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
@@ -1095,14 +1307,14 @@ void free_all(cm_handle *h) {
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
                      &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx};
     for (DevBuf *b : all) {
-        if (b->p) cudaFree(b->p);
+        blocks().put(h->device, false, b->p, b->bytes);
         b->p = nullptr;
-        b->bytes = 0;
+        b->bytes = b->charged = 0;
     }
+    h->device_bytes = 0;
+    for (const DevBuf &b : h->host_blocks) blocks().put(h->device, true, b.p, b.bytes);
+    h->host_blocks.clear();
     for (int i = 0; i < 2; ++i) {
-        if (h->h_geoms[i]) cudaFreeHost(h->h_geoms[i]);
-        if (h->h_samples[i]) cudaFreeHost(h->h_samples[i]);
-        if (h->h_tabs[i]) cudaFreeHost(h->h_tabs[i]);
         h->h_geoms[i] = nullptr;
         h->h_samples[i] = nullptr;
         h->h_tabs[i] = nullptr;
@@ -1116,6 +1328,8 @@ void free_all(cm_handle *h) {
     h->pending.clear();
     for (cudaEvent_t e : h->ev_free) cudaEventDestroy(e);
     h->ev_free.clear();
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
 }
@@ -1403,6 +1617,132 @@ int noalloc_frame(const cm_system_desc *desc, const cm_frames *f, int64_t *count
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Batches of systems in one CUDA graph.
+
+struct cm_batch {
+    std::vector<cm_handle *> hs;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, after = nullptr;
+    std::vector<cudaEvent_t> pre, join;
+    cudaGraphExec_t gexec = nullptr;
+    int64_t launches = 0, instantiations = 0;
+    std::string err;
+};
+
+namespace {
+
+void batch_free(cm_batch *b) {
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (cudaEvent_t e : b->pre) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->join) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->after) cudaEventDestroy(b->after);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// One staging round: frames [r * max_frames, ...) of every system that has
+// them, captured as one graph on the batch stream and launched once.
+void batch_round(cm_batch *bt, const cm_frames *frames, int r) {
+    const size_t n = bt->hs.size();
+    std::vector<Staged> st(n);
+    std::vector<char> active(n, 0);
+    for (size_t i = 0; i < n; ++i) {
+        cm_handle *h = bt->hs[i];
+        const int64_t f0 = (int64_t)r * h->max_frames;
+        if (frames[i].nframes == 0 || f0 >= frames[i].nframes) continue;
+        st[i] = stage(h, &frames[i], (int)f0);
+        active[i] = 1;
+    }
+    // outside the capture: each system's stream after its copies and its
+    // earlier work, and the batch stream after all of them
+    for (size_t i = 0; i < n; ++i) {
+        if (!active[i]) continue;
+        cm_handle *h = bt->hs[i];
+        CM_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copied[st[i].b], 0));
+        CM_CUDA(cudaEventRecord(bt->pre[i], h->stream));
+        CM_CUDA(cudaStreamWaitEvent(bt->stream, bt->pre[i], 0));
+    }
+    CM_CUDA(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t g = nullptr;
+    try {
+        CM_CUDA(cudaEventRecord(bt->fork, bt->stream));
+        for (size_t i = 0; i < n; ++i) {
+            if (!active[i]) continue;
+            cm_handle *h = bt->hs[i];
+            CM_CUDA(cudaStreamWaitEvent(h->stream, bt->fork, 0));
+            for (const Chunk &c : st[i].chunks) {
+                open_class(h, c.weight);
+                run_staged_chunk(h, st[i], c);
+                account_chunk(h, st[i], c);
+            }
+            CM_CUDA(cudaEventRecord(bt->join[i], h->stream));
+            CM_CUDA(cudaStreamWaitEvent(bt->stream, bt->join[i], 0));
+        }
+    } catch (...) {
+        cudaStreamEndCapture(bt->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        throw;
+    }
+    CM_CUDA(cudaStreamEndCapture(bt->stream, &g));
+    bool updated = false;
+    if (bt->gexec) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(bt->gexec, g, &info) == cudaSuccess;
+        if (!updated) {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(bt->gexec);
+            bt->gexec = nullptr;
+        }
+    }
+    if (!updated) {
+        const cudaError_t e = cudaGraphInstantiate(&bt->gexec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            bt->gexec = nullptr;
+            throw cm_error(CM_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+        bt->instantiations++;
+    }
+    cudaGraphDestroy(g);
+    CM_CUDA(cudaGraphLaunch(bt->gexec, bt->stream));
+    bt->launches++;
+    CM_CUDA(cudaEventRecord(bt->after, bt->stream));
+    for (size_t i = 0; i < n; ++i) {
+        if (!active[i]) continue;
+        cm_handle *h = bt->hs[i];
+        CM_CUDA(cudaStreamWaitEvent(h->stream, bt->after, 0));
+        CM_CUDA(cudaEventRecord(h->ev_done[st[i].b], h->stream));
+    }
+}
+
+template <typename F>
+int batch_guarded(cm_batch *b, F &&fn) {
+    if (!b) {
+        g_create_error = "NULL batch";
+        return CM_EINVAL;
+    }
+    try {
+        CM_CUDA(cudaSetDevice(b->device));
+        fn();
+        return CM_OK;
+    } catch (const cm_error &e) {
+        b->err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        b->err = "host allocation failed";
+        return CM_ENOMEM;
+    } catch (const std::exception &e) {
+        b->err = e.what();
+        return CM_ECUDA;
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 int cm_create(const cm_system_desc *desc, cm_handle **out) {
@@ -1421,6 +1761,10 @@ int cm_create(const cm_system_desc *desc, cm_handle **out) {
         h->Nv = (int64_t)desc->solvent_nmols * desc->solvent_natomspermol;
         h->mddf = desc->mode == CM_MODE_MDDF;
         h->timing = desc->kernel_timing != 0;
+        // per-launch timing events cannot sit inside a captured chain
+        h->graphs = desc->launch == CM_LAUNCH_GRAPH || (desc->launch == CM_LAUNCH_AUTO && !h->timing);
+        if (desc->launch == CM_LAUNCH_GRAPH && h->timing)
+            throw cm_error(CM_EINVAL, "kernel_timing needs stream launches (launch = CM_LAUNCH_STREAM or AUTO)");
         if (desc->solute_group_offsets) {
             copy_csr(desc->solute_natomspermol, desc->solute_ngroups, desc->solute_group_offsets, desc->solute_groups, h->gs_off,
                      h->gs_idx, "solute");
@@ -1468,12 +1812,12 @@ int cm_create(const cm_system_desc *desc, cm_handle **out) {
         dev_alloc(h, h->sums, h->hist_n * 8);
         dev_alloc(h, h->stats, ST_N * 8);
         dev_alloc(h, h->errflag, 8);
-        CM_CUDA(cudaMemset(h->hist.p, 0, h->hist_n * 8));
-        CM_CUDA(cudaMemset(h->sums.p, 0, h->hist_n * 8));
-        CM_CUDA(cudaMemset(h->stats.p, 0, ST_N * 8));
-        CM_CUDA(cudaMemset(h->errflag.p, 0, 8));
+        CM_CUDA(cudaMemsetAsync(h->hist.p, 0, h->hist_n * 8, h->stream));
+        CM_CUDA(cudaMemsetAsync(h->sums.p, 0, h->hist_n * 8, h->stream));
+        CM_CUDA(cudaMemsetAsync(h->stats.p, 0, ST_N * 8, h->stream));
+        CM_CUDA(cudaMemsetAsync(h->errflag.p, 0, 8, h->stream));
         upload_groups(h);
-        CM_CUDA(cudaDeviceSynchronize());
+        CM_CUDA(cudaStreamSynchronize(h->stream));  // this handle only: other handles keep running
         *out = h;
         return CM_OK;
     } catch (const cm_error &e) {
@@ -1493,6 +1837,85 @@ int cm_submit_frames(cm_handle *h, const cm_frames *frames) {
 
 int cm_synchronize(cm_handle *h) {
     return guarded(h, [&] { check_device_error(h); });
+}
+
+int cm_batch_create(cm_handle *const *handles, int32_t nhandles, cm_batch **out) {
+    if (!out || !handles || nhandles < 1) {
+        g_create_error = "cm_batch_create needs an output pointer and at least one handle";
+        return CM_EINVAL;
+    }
+    *out = nullptr;
+    cm_batch *b = nullptr;
+    try {
+        for (int i = 0; i < nhandles; ++i) {
+            if (!handles[i]) throw cm_error(CM_EINVAL, "NULL handle in the batch");
+            if (handles[i]->device != handles[0]->device) throw cm_error(CM_EINVAL, "the handles of a batch share one device");
+            if (handles[i]->timing) throw cm_error(CM_EINVAL, "handles with kernel_timing cannot be batched");
+            for (int j = 0; j < i; ++j)
+                if (handles[j] == handles[i]) throw cm_error(CM_EINVAL, "a handle appears twice in the batch");
+        }
+        b = new cm_batch();
+        b->hs.assign(handles, handles + nhandles);
+        b->device = handles[0]->device;
+        CM_CUDA(cudaSetDevice(b->device));
+        CM_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        CM_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        CM_CUDA(cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming));
+        b->pre.assign(nhandles, nullptr);
+        b->join.assign(nhandles, nullptr);
+        for (int i = 0; i < nhandles; ++i) {
+            CM_CUDA(cudaEventCreateWithFlags(&b->pre[i], cudaEventDisableTiming));
+            CM_CUDA(cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming));
+        }
+        *out = b;
+        return CM_OK;
+    } catch (const cm_error &e) {
+        g_create_error = e.msg;
+        if (b) { batch_free(b); delete b; }
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_create_error = "host allocation failed";
+        if (b) { batch_free(b); delete b; }
+        return CM_ENOMEM;
+    }
+}
+
+int cm_batch_submit(cm_batch *b, const cm_frames *frames) {
+    return batch_guarded(b, [&] {
+        if (!frames) throw cm_error(CM_EINVAL, "NULL frames");
+        int rounds = 0;
+        for (size_t i = 0; i < b->hs.size(); ++i) {
+            cm_handle *h = b->hs[i];
+            try {
+                check_frames(h, &frames[i]);
+            } catch (const cm_error &e) {
+                throw cm_error(e.code, "system " + std::to_string(i) + ": " + e.msg);
+            }
+            if (frames[i].nframes > 0)
+                rounds = std::max<int>(rounds, (frames[i].nframes + h->max_frames - 1) / h->max_frames);
+        }
+        for (int r = 0; r < rounds; ++r) batch_round(b, frames, r);
+    });
+}
+
+int cm_batch_graph_stats(const cm_batch *b, int64_t *graph_launches, int64_t *graph_instantiations) {
+    if (!b) return CM_EINVAL;
+    if (graph_launches) *graph_launches = b->launches;
+    if (graph_instantiations) *graph_instantiations = b->instantiations;
+    return CM_OK;
+}
+
+int cm_batch_destroy(cm_batch *b) {
+    if (!b) return CM_OK;
+    cudaSetDevice(b->device);
+    batch_free(b);
+    delete b;
+    return CM_OK;
+}
+
+const char *cm_batch_last_error(const cm_batch *b) {
+    if (!b) return g_create_error.c_str();
+    return b->err.c_str();
 }
 
 int cm_read_counts(cm_handle *h, cm_counts *out) {
@@ -1582,6 +2005,8 @@ int cm_get_stats(cm_handle *h, cm_stats *out) {
         out->regime = h->regime;
         out->kernels_per_frame = h->kernels_per_frame;
         out->kernel_launches = h->launches_total;
+        out->graph_launches = h->graph_launches;
+        out->graph_instantiations = h->graph_instantiations;
     });
 }
 
@@ -1599,11 +2024,11 @@ int cm_get_kernel_times(cm_handle *h, cm_kernel_times *out) {
 
 int cm_reset(cm_handle *h) {
     return guarded(h, [&] {
+        CM_CUDA(cudaMemsetAsync(h->hist.p, 0, h->hist_n * 8, h->stream));
+        CM_CUDA(cudaMemsetAsync(h->sums.p, 0, h->hist_n * 8, h->stream));
+        CM_CUDA(cudaMemsetAsync(h->stats.p, 0, ST_N * 8, h->stream));
+        CM_CUDA(cudaMemsetAsync(h->errflag.p, 0, 8, h->stream));
         CM_CUDA(cudaStreamSynchronize(h->stream));
-        CM_CUDA(cudaMemset(h->hist.p, 0, h->hist_n * 8));
-        CM_CUDA(cudaMemset(h->sums.p, 0, h->hist_n * 8));
-        CM_CUDA(cudaMemset(h->stats.p, 0, ST_N * 8));
-        CM_CUDA(cudaMemset(h->errflag.p, 0, 8));
         h->class_open = false;
         h->class_w = 1.0;
         h->folds = 0;
@@ -1611,6 +2036,7 @@ int cm_reset(cm_handle *h) {
         h->frames = 0;
         timing_drain(h);
         h->launches_total = 0;
+        h->graph_launches = h->graph_instantiations = 0;
         for (int i = 0; i < CM_K_NCLASSES; ++i) {
             h->class_ms[i] = 0.0;
             h->class_launches[i] = 0;
@@ -1645,6 +2071,24 @@ const char *cm_status_string(int status) {
 }
 
 int64_t cm_device_bytes(const cm_handle *h) { return h ? h->device_bytes : 0; }
+
+int cm_memory_cache(int32_t device, int32_t release, int64_t *cached_device_bytes, int64_t *cached_host_bytes) {
+    if (device < 0 || device >= BlockCache::kMaxDevices) {
+        g_create_error = "device index out of range";
+        return CM_EINVAL;
+    }
+    if (release) {
+        int prev = -1;
+        cudaGetDevice(&prev);
+        cudaSetDevice(device);
+        blocks().release(device, false);
+        blocks().release(device, true);
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    if (cached_device_bytes) *cached_device_bytes = (int64_t)blocks().cached(device, false);
+    if (cached_host_bytes) *cached_host_bytes = (int64_t)blocks().cached(device, true);
+    return CM_OK;
+}
 
 int cm_measure_fp32_peak(int32_t device, double ms_target, double *tflops) {
     if (!tflops) return CM_EINVAL;

@@ -50,10 +50,13 @@ def system_desc(
     hbm_budget_bytes: int = 0,
     kernel_timing: bool = False,
     cell_scale_pct: int = 0,
+    launch: str = "auto",
 ):
     """cm_system_desc of a system, and the arrays it points to (keep them
     alive while the description is in use).  ``cell_scale_pct`` scales the
-    search cells (speed only; see ``autotune``)."""
+    search cells (speed only; see ``autotune``); ``launch`` ("auto", "stream"
+    or "graph") says whether each compute chunk's kernels are launched one by
+    one or replayed as a captured CUDA graph (speed only)."""
     d = N.cm_system_desc()
     d.api_version = N.CM_API_VERSION
     d.solute_nmols = solute_nmols
@@ -91,6 +94,10 @@ def system_desc(
     d.hbm_budget_bytes = hbm_budget_bytes
     d.kernel_timing = 1 if kernel_timing else 0
     d.cell_scale_pct = cell_scale_pct
+    modes = {"auto": N.CM_LAUNCH_AUTO, "stream": N.CM_LAUNCH_STREAM, "graph": N.CM_LAUNCH_GRAPH}
+    if launch not in modes:
+        raise ValueError(f"launch must be one of {sorted(modes)}")
+    d.launch = modes[launch]
     return d, keep
 
 
@@ -107,6 +114,16 @@ def autotune(solute_xyz, solvent_xyz, cells, frame_ids=None, **system) -> dict:
     del keep, keep_f
     return {"cell_scale_pct": t.cell_scale_pct,
             "candidates": {t.candidates[i]: t.ms_per_frame[i] for i in range(t.ncandidates)}}
+
+
+def memory_cache(device: int = 0, release: bool = False) -> dict:
+    """Free device and pinned host bytes held by the process-wide block cache
+    that closed engines return their memory to (cm_memory_cache); with
+    ``release`` they are first handed back to the driver."""
+    lib = N.load()
+    dev, host = C.c_int64(0), C.c_int64(0)
+    N.raise_for(lib.cm_memory_cache(int(device), 1 if release else 0, C.byref(dev), C.byref(host)), None)
+    return {"device_bytes": dev.value, "host_bytes": host.value}
 
 
 def frames_struct(solute_xyz, solvent_xyz, cells, weights, frame_ids, natoms_solute, natoms_solvent, autocorrelation):
@@ -306,3 +323,52 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Batch:
+    """Several engines whose frames run as one CUDA graph per staging round
+    (cm_batch_*): each system's kernels on its own stream, forked from and
+    joined to one capture, launched once.  Counts are those of submitting to
+    each engine alone.  Close the batch before its engines."""
+
+    def __init__(self, engines):
+        self._lib = N.load()
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e._h.value for e in self.engines])
+        self._b = C.c_void_p()
+        N.raise_for(self._lib.cm_batch_create(arr, len(self.engines), C.byref(self._b)), None)
+
+    def submit(self, items) -> None:
+        """``items[i]`` = (solute_xyz, solvent_xyz, cells[, frame_ids]) for
+        engine i, or None to give it no frames in this call."""
+        if len(items) != len(self.engines):
+            raise ValueError("one item per engine")
+        frs = (N.cm_frames * len(self.engines))()
+        keeps = []
+        for i, (e, it) in enumerate(zip(self.engines, items)):
+            if it is None:
+                continue
+            xs, xv, cells = it[:3]
+            ids = it[3] if len(it) > 3 else None
+            fr, keep = frames_struct(xs, xv, cells, None, ids, e.Ns, e.Nv, e.autocorrelation)
+            frs[i] = fr
+            keeps.append(keep)
+            e._inflight.append(keep)
+        N.raise_for(self._lib.cm_batch_submit(self._b, frs), None, batch=self._b)
+
+    def graph_stats(self) -> dict:
+        a, b = C.c_int64(0), C.c_int64(0)
+        N.raise_for(self._lib.cm_batch_graph_stats(self._b, C.byref(a), C.byref(b)), None, batch=self._b)
+        return {"graph_launches": a.value, "graph_instantiations": b.value}
+
+    def close(self) -> None:
+        if self._b:
+            self._lib.cm_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define CM_API_VERSION 1
+#define CM_API_VERSION 2
 
 typedef enum cm_status {
     CM_OK = 0,
@@ -53,6 +53,11 @@ typedef enum cm_status {
 enum { CM_MODE_MDDF = 0, CM_MODE_COORDINATION_NUMBER = 1 };
 enum { CM_PRECISION_FP64 = 0, CM_PRECISION_FP32_GUARD = 1 };
 enum { CM_REGIME_AUTO = 0, CM_REGIME_PAIRS = 1, CM_REGIME_ATOMS = 2 };
+/* How a compute chunk's chain of kernels is launched: one launch per kernel on
+ * the handle's stream, or captured as a CUDA graph and replayed through one
+ * executable graph per handle (updated in place while the chain keeps its
+ * shape).  AUTO takes GRAPH unless kernel_timing is set. */
+enum { CM_LAUNCH_AUTO = 0, CM_LAUNCH_STREAM = 1, CM_LAUNCH_GRAPH = 2 };
 enum { CM_COORD_F64 = 0, CM_COORD_F32 = 1 };
 enum { CM_MEM_HOST = 0, CM_MEM_DEVICE = 1 };
 
@@ -105,6 +110,8 @@ typedef struct cm_system_desc {
     int32_t kernel_timing;            /* 1: time every launch with CUDA events (cm_get_kernel_times) */
     int32_t cell_scale_pct;           /* search-cell size in percent of the default (0 = 100, range 30-300);
                                          the counts do not depend on it, only the speed (cm_autotune) */
+    int32_t launch;                   /* CM_LAUNCH_*; the counts do not depend on it */
+    int32_t reserved;                 /* 0 */
 } cm_system_desc;
 
 /*
@@ -167,6 +174,8 @@ typedef struct cm_stats {
     int32_t regime;                       /* CM_REGIME_PAIRS or CM_REGIME_ATOMS actually used */
     int32_t kernels_per_frame;            /* kernel launches of the last frame */
     int64_t kernel_launches;              /* kernel launches since create / reset */
+    int64_t graph_launches;               /* chunks replayed as a CUDA graph since create / reset */
+    int64_t graph_instantiations;         /* of those, chunks whose chain changed shape (graph built anew) */
 } cm_stats;
 
 /* Kernel classes of cm_get_kernel_times. */
@@ -200,6 +209,26 @@ int cm_submit_frames(cm_handle *h, const cm_frames *frames);
 /* Wait for all submitted work; returns CM_EDEVICE if a kernel raised its error flag. */
 int cm_synchronize(cm_handle *h);
 
+/*
+ * Batches of systems (no counterpart in the reference, which runs one system
+ * per mddf call).  cm_batch_submit gives frames[i] to handles[i] like
+ * cm_submit_frames, but the kernels of all systems are captured into one CUDA
+ * graph -- each system's chain on its own stream, forked from and joined to the
+ * batch's stream -- and launched once, so systems of uneven size run side by
+ * side with one launch per staging round.  The executable graph is updated in
+ * place while the systems and their chunk shapes repeat.  Counts are those of
+ * cm_submit_frames on each handle.  All handles live on one device, have
+ * kernel_timing off, and are used by no other thread during a call; destroy
+ * the batch before its handles.  After a failed cm_batch_submit the handles'
+ * counts are undefined until cm_reset.
+ */
+typedef struct cm_batch cm_batch;
+int cm_batch_create(cm_handle *const *handles, int32_t nhandles, cm_batch **out);
+int cm_batch_submit(cm_batch *b, const cm_frames *frames);  /* frames[nhandles]; nframes 0 skips a system */
+int cm_batch_graph_stats(const cm_batch *b, int64_t *graph_launches, int64_t *graph_instantiations);
+int cm_batch_destroy(cm_batch *b);
+const char *cm_batch_last_error(const cm_batch *b);
+
 /* Synchronise and copy the weighted accumulators out. */
 int cm_read_counts(cm_handle *h, cm_counts *out);
 
@@ -232,6 +261,15 @@ int cm_measure_fp32_peak(int32_t device, double ms_target, double *tflops);
 
 /* Device memory the handle holds, in bytes. */
 int64_t cm_device_bytes(const cm_handle *h);
+
+/* Process-wide block cache (no counterpart in the reference, whose arrays
+ * are garbage-collected Julia memory).  A destroyed handle returns its device
+ * and pinned host blocks to a per-device cache that later handles draw from,
+ * because freeing them waits for every stream of the device.  Report the
+ * cached (free) bytes of `device` and, when `release` is nonzero, return them
+ * to the driver first (that waits for the device).  Either output may be
+ * NULL. */
+int cm_memory_cache(int32_t device, int32_t release, int64_t *cached_device_bytes, int64_t *cached_host_bytes);
 
 /* The CUDA stream of the handle (as cudaStream_t), for callers that order
  * their own device work against the engine. */

@@ -28,11 +28,11 @@ def test_library_exports_header_symbols(cm):
 def test_struct_sizes_match_header(cm):
     N = cm._native
     # field-by-field mirror of include/cmgpu.h on LP64
-    assert C.sizeof(N.cm_system_desc) == 168
+    assert C.sizeof(N.cm_system_desc) == 176
     assert C.sizeof(N.cm_frames) == 56
     assert C.sizeof(N.cm_counts) == 88
     assert C.sizeof(N.cm_raw_counts) == 64
-    assert C.sizeof(N.cm_stats) == 88
+    assert C.sizeof(N.cm_stats) == 104
     assert C.sizeof(N.cm_kernel_times) == 112
     assert C.sizeof(N.cm_server_desc) == 24
     assert C.sizeof(N.cm_request_info) == 48
@@ -62,6 +62,14 @@ def test_create_rejects_bad_descriptions_without_gpu(cm):
     d.usecutoff = 0
     d.nbins = 10
     assert lib.cm_create(C.byref(d), C.byref(h)) == N.CM_EINVAL
+    d.nbins = 500
+    d.launch = 7
+    assert lib.cm_create(C.byref(d), C.byref(h)) == N.CM_EINVAL
+    assert b"launch mode" in lib.cm_last_error(None)
+    d.launch = N.CM_LAUNCH_GRAPH
+    d.kernel_timing = 1   # per-launch timing events cannot be captured
+    assert lib.cm_create(C.byref(d), C.byref(h)) == N.CM_EINVAL
+    assert b"kernel_timing" in lib.cm_last_error(None)
     assert lib.cm_destroy(None) == N.CM_OK
     assert lib.cm_status_string(N.CM_EDEVICE) == b"device-side check failed"
 
@@ -75,6 +83,32 @@ def test_engine_fails_loudly_without_library(cm, tmp_path):
             N.load(str(tmp_path / "missing.so"))
         finally:
             N._lib = saved
+
+
+def test_memory_cache_query_without_gpu(cm):
+    """cm_memory_cache reads the process-wide block cache without touching a
+    device (nothing is cached in a process that opened no handle) and rejects a
+    bad device index."""
+    N = cm._native
+    lib = N.load()
+    dev, host = C.c_int64(-1), C.c_int64(-1)
+    assert lib.cm_memory_cache(0, 0, C.byref(dev), C.byref(host)) == N.CM_OK
+    assert dev.value >= 0 and host.value >= 0
+    assert lib.cm_memory_cache(-1, 0, None, None) == N.CM_EINVAL
+    assert lib.cm_memory_cache(1 << 20, 0, None, None) == N.CM_EINVAL
+
+
+def test_batch_create_rejects_bad_arguments_without_gpu(cm):
+    N = cm._native
+    lib = N.load()
+    out = C.c_void_p()
+    assert lib.cm_batch_create(None, 1, C.byref(out)) == N.CM_EINVAL
+    arr = (C.c_void_p * 2)(None, None)
+    assert lib.cm_batch_create(arr, 0, C.byref(out)) == N.CM_EINVAL
+    assert lib.cm_batch_create(arr, 2, C.byref(out)) == N.CM_EINVAL
+    assert b"NULL handle" in lib.cm_last_error(None)
+    assert lib.cm_batch_submit(None, None) == N.CM_EINVAL
+    assert lib.cm_batch_destroy(None) == N.CM_OK
 
 
 def test_server_create_rejects_bad_arguments_without_gpu(cm):

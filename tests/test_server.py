@@ -140,3 +140,21 @@ def test_handles_with_different_shared_memory_interleave(cm, gpu_ready):
     ref = alone(cm, *big)
     for k in KEYS:
         assert np.array_equal(got[k], ref[k]), k
+
+
+def test_closed_engines_return_memory_to_the_block_cache(cm):
+    """A closed engine's device and pinned blocks go to the process-wide cache
+    (freeing them would wait for every stream of the device); an engine of the
+    same system opened next takes them back, and its counts are unchanged on
+    the reused (not zeroed) memory."""
+    xs, xv, cells, kw = requests()[3]
+    first = alone(cm, xs, xv, cells, kw)
+    before = cm.memory_cache(0)
+    assert before["device_bytes"] > 0 and before["host_bytes"] > 0
+    again = alone(cm, xs, xv, cells, kw)
+    after = cm.memory_cache(0)
+    assert after["device_bytes"] <= before["device_bytes"]
+    for k in KEYS:
+        assert np.array_equal(first[k], again[k]), k
+    released = cm.memory_cache(0, release=True)
+    assert released["device_bytes"] == 0 and released["host_bytes"] == 0
