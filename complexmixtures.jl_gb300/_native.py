@@ -18,7 +18,7 @@ CM_MODE_MDDF, CM_MODE_COORDINATION_NUMBER = 0, 1
 CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
 CM_REGIME_AUTO, CM_REGIME_PAIRS, CM_REGIME_ATOMS = 0, 1, 2
 CM_LAUNCH_AUTO, CM_LAUNCH_STREAM, CM_LAUNCH_GRAPH = 0, 1, 2
-CM_COORD_F64, CM_COORD_F32 = 0, 1
+CM_COORD_F64, CM_COORD_F32, CM_COORD_DCD = 0, 1, 2
 CM_MEM_HOST, CM_MEM_DEVICE = 0, 1
 CM_NOALLOC_SCRATCH_BYTES = 32 << 20
 CM_NOALLOC_MAX_SAMPLES = 4096
@@ -64,6 +64,20 @@ class cm_system_desc(C.Structure):
         ("cell_scale_pct", C.c_int32),
         ("launch", C.c_int32),
         ("reserved", C.c_int32),
+    ]
+
+
+class cm_dcd_layout(C.Structure):
+    _fields_ = [
+        ("natoms", C.c_int64),
+        ("frame_bytes", C.c_int64),
+        ("x_offset", C.c_int64),
+        ("y_offset", C.c_int64),
+        ("z_offset", C.c_int64),
+        ("big_endian", C.c_int32),
+        ("reserved", C.c_int32),
+        ("solute_atoms", C.POINTER(C.c_int32)),
+        ("solvent_atoms", C.POINTER(C.c_int32)),
     ]
 
 
@@ -180,6 +194,7 @@ EXPORTED = (
     "cm_create",
     "cm_submit_frames",
     "cm_synchronize",
+    "cm_set_dcd_layout",
     "cm_batch_create",
     "cm_batch_submit",
     "cm_batch_graph_stats",
@@ -252,6 +267,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_status_string.restype = C.c_char_p
     lib.cm_device_bytes.argtypes = [H]
     lib.cm_device_bytes.restype = C.c_int64
+    lib.cm_set_dcd_layout.argtypes = [H, C.POINTER(cm_dcd_layout)]
+    lib.cm_set_dcd_layout.restype = C.c_int
     lib.cm_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
     lib.cm_batch_create.restype = C.c_int
     lib.cm_batch_submit.argtypes = [C.c_void_p, C.POINTER(cm_frames)]

@@ -1508,6 +1508,31 @@ __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
     }
 }
 
+// DCD decode (src/trajectory_formats/NamdDCD.jl:141-169): a frame of the file
+// is its unit-cell record followed by three Fortran records holding the x, y
+// and z float32 arrays of all atoms.  Raw frames go to the device as read
+// from the file; this kernel gathers the selection's atoms (0-based indices
+// into the frame) into the engine's [frame][atom][xyz] float32 staging
+// layout, swapping bytes for big-endian files.  All offsets are multiples of
+// four bytes (records of float32 with 4-byte markers), so the loads are
+// aligned.
+__global__ void k_dcd_gather(const unsigned char *__restrict__ raw, int64_t frame_bytes, int64_t xoff, int64_t yoff,
+                             int64_t zoff, int swap, const int32_t *__restrict__ atoms, int64_t nsel,
+                             float *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsel) return;
+    const int f = blockIdx.y;
+    const unsigned char *fr = raw + (int64_t)f * frame_bytes;
+    const int64_t a = atoms[i];
+    unsigned int w[3];
+    w[0] = reinterpret_cast<const unsigned int *>(fr + xoff)[a];
+    w[1] = reinterpret_cast<const unsigned int *>(fr + yoff)[a];
+    w[2] = reinterpret_cast<const unsigned int *>(fr + zoff)[a];
+    float *o = out + ((int64_t)f * nsel + i) * 3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o[k] = __uint_as_float(swap ? __byte_perm(w[k], 0, 0x0123) : w[k]);
+}
+
 // Weight change: fold the integer class accumulators into FP64 sums
 // (acc += w * count / 2) and clear them.
 __global__ void k_fold(unsigned long long *__restrict__ acc, double *__restrict__ sums, int64_t n, double w) {

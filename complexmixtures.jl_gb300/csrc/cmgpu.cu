@@ -212,6 +212,13 @@ struct cm_handle {
     int kernels_per_frame = 0;
     int chunk_parity = 0;
 
+    // raw DCD frames (cm_set_dcd_layout)
+    bool dcd = false;
+    int64_t dcd_natoms = 0, dcd_frame_bytes = 0, dcd_off[3] = {0, 0, 0};
+    int dcd_swap = 0;
+    std::vector<int32_t> dcd_s, dcd_v;  // host copies of the selections' atom indices
+    DevBuf dcd_sidx, dcd_vidx, dcd_raw[2];
+
     // CUDA-graph launch of compute chunks
     bool graphs = false;
     cudaGraphExec_t gexec = nullptr;
@@ -1112,17 +1119,61 @@ struct Staged {
     std::vector<Chunk> chunks;
 };
 
+// Frame 0 of a raw DCD batch gathered on the host (float32, selection order):
+// the planner sizes the cells from one frame's coordinates.
+struct DcdFirstFrame {
+    std::vector<float> xs, xv;
+    cm_frames f{};
+};
+
+void dcd_first_frame(cm_handle *h, const cm_frames *f, DcdFirstFrame &out) {
+    std::vector<unsigned char> raw((size_t)h->dcd_frame_bytes);
+    if (f->memory == CM_MEM_DEVICE) CM_CUDA(cudaMemcpy(raw.data(), f->solute_xyz, raw.size(), cudaMemcpyDeviceToHost));
+    else memcpy(raw.data(), f->solute_xyz, raw.size());
+    auto gather = [&](const std::vector<int32_t> &idx, std::vector<float> &xyz) {
+        xyz.resize(idx.size() * 3);
+        for (size_t i = 0; i < idx.size(); ++i)
+            for (int k = 0; k < 3; ++k) {
+                uint32_t w;
+                memcpy(&w, raw.data() + h->dcd_off[k] + 4 * (int64_t)idx[i], 4);
+                if (h->dcd_swap) w = (w >> 24) | ((w >> 8) & 0xff00u) | ((w << 8) & 0xff0000u) | (w << 24);
+                memcpy(&xyz[3 * i + k], &w, 4);
+            }
+    };
+    gather(h->dcd_s, out.xs);
+    if (!h->d.autocorrelation) gather(h->dcd_v, out.xv);
+    out.f = *f;
+    out.f.nframes = 1;
+    out.f.coord_type = CM_COORD_F32;
+    out.f.memory = CM_MEM_HOST;
+    out.f.solute_xyz = out.xs.data();
+    out.f.solvent_xyz = h->d.autocorrelation ? nullptr : out.xv.data();
+}
+
 void check_frames(cm_handle *h, const cm_frames *f) {
     const cm_system_desc &d = h->d;
     if (!f || f->nframes < 0) throw cm_error(CM_EINVAL, "invalid frame batch");
     if (f->nframes == 0) return;
     if (!f->solute_xyz || !f->cells || !f->frame_ids) throw cm_error(CM_EINVAL, "solute_xyz, cells and frame_ids are required");
-    if (!d.autocorrelation && !f->solvent_xyz) throw cm_error(CM_EINVAL, "solvent_xyz is required unless autocorrelation");
-    if (f->coord_type != CM_COORD_F32 && f->coord_type != CM_COORD_F64) throw cm_error(CM_EINVAL, "unknown coord_type");
+    if (f->coord_type != CM_COORD_F32 && f->coord_type != CM_COORD_F64 && f->coord_type != CM_COORD_DCD)
+        throw cm_error(CM_EINVAL, "unknown coord_type");
     if (f->memory != CM_MEM_HOST && f->memory != CM_MEM_DEVICE) throw cm_error(CM_EINVAL, "unknown memory kind");
-    if (!h->planned) plan(h, f);
-    const int elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
-    if (elem != h->coord_elem && f->memory == CM_MEM_HOST)
+    const bool dcd = f->coord_type == CM_COORD_DCD;
+    if (dcd && !h->dcd) throw cm_error(CM_ESTATE, "raw DCD frames need cm_set_dcd_layout first");
+    if (dcd && f->solvent_xyz) throw cm_error(CM_EINVAL, "raw DCD frames hold both selections: solvent_xyz must be NULL");
+    if (!dcd && !d.autocorrelation && !f->solvent_xyz) throw cm_error(CM_EINVAL, "solvent_xyz is required unless autocorrelation");
+    if (!h->planned) {
+        if (dcd) {
+            DcdFirstFrame ff;
+            dcd_first_frame(h, f, ff);
+            plan(h, &ff.f);
+        } else {
+            plan(h, f);
+        }
+    }
+    if (dcd && h->coord_elem != 4) throw cm_error(CM_EINVAL, "raw DCD frames are float32: this handle was planned for float64");
+    const int elem = (f->coord_type == CM_COORD_F32 || dcd) ? 4 : 8;
+    if (elem != h->coord_elem && (f->memory == CM_MEM_HOST || dcd))
         throw cm_error(CM_EINVAL, "coordinate type differs from the first batch of this handle");
     for (int i = 0; i < f->nframes; ++i) {
         double w = f->weights ? f->weights[i] : 1.0;
@@ -1135,7 +1186,8 @@ void check_frames(cm_handle *h, const cm_frames *f) {
 Staged stage(cm_handle *h, const cm_frames *f, int f0) {
     const cm_system_desc &d = h->d;
     Staged S;
-    S.elem = f->coord_type == CM_COORD_F32 ? 4 : 8;
+    const bool dcd = f->coord_type == CM_COORD_DCD;
+    S.elem = (f->coord_type == CM_COORD_F32 || dcd) ? 4 : 8;
     S.f0 = f0;
     S.sbytes = h->Ns * 3 * S.elem;
     S.vbytes = h->Nv * 3 * S.elem;
@@ -1203,7 +1255,31 @@ Staged stage(cm_handle *h, const cm_frames *f, int f0) {
     CM_CUDA(cudaMemcpyAsync(S.dG, hg, sizeof(FrameGeom) * nf, cudaMemcpyHostToDevice, cp));
     if (h->mddf && soff > 0) CM_CUDA(cudaMemcpyAsync(S.dS, hs, sizeof(Sample) * soff, cudaMemcpyHostToDevice, cp));
     if (h->mddf && ntab > 0) CM_CUDA(cudaMemcpyAsync(S.dT, ht, sizeof(int4) * ntab, cudaMemcpyHostToDevice, cp));
-    if (f->memory == CM_MEM_HOST) {
+    if (dcd) {
+        // raw frames to the device (unless they are there already), then the
+        // selections gathered into the staging buffers, on the copy stream
+        const unsigned char *raw = (const unsigned char *)f->solute_xyz + h->dcd_frame_bytes * f0;
+        dev_alloc(h, h->stage_s[b], (size_t)h->max_frames * h->Ns * 3 * 4);
+        if (!d.autocorrelation) dev_alloc(h, h->stage_v[b], (size_t)h->max_frames * h->Nv * 3 * 4);
+        if (f->memory == CM_MEM_HOST) {
+            dev_alloc(h, h->dcd_raw[b], (size_t)h->dcd_frame_bytes * h->max_frames);
+            CM_CUDA(cudaMemcpyAsync(h->dcd_raw[b].p, raw, (size_t)h->dcd_frame_bytes * nf, cudaMemcpyHostToDevice, cp));
+            raw = (const unsigned char *)h->dcd_raw[b].p;
+        }
+        auto gather = [&](DevBuf &idx, int64_t n, DevBuf &out) {
+            k_dcd_gather<<<dim3(grid_for(n, 256), nf), 256, 0, cp>>>(raw, h->dcd_frame_bytes, h->dcd_off[0], h->dcd_off[1],
+                                                                      h->dcd_off[2], h->dcd_swap, P<int32_t>(idx), n,
+                                                                      P<float>(out));
+        };
+        gather(h->dcd_sidx, h->Ns, h->stage_s[b]);
+        S.xs_base = (const char *)h->stage_s[b].p;
+        if (!d.autocorrelation) {
+            gather(h->dcd_vidx, h->Nv, h->stage_v[b]);
+            S.xv_base = (const char *)h->stage_v[b].p;
+        }
+        CM_CUDA(cudaGetLastError());
+        h->launches_total += d.autocorrelation ? 1 : 2;
+    } else if (f->memory == CM_MEM_HOST) {
         CM_CUDA(cudaMemcpyAsync(h->stage_s[b].p, (const char *)f->solute_xyz + S.sbytes * f0, (size_t)S.sbytes * nf,
                                 cudaMemcpyHostToDevice, cp));
         S.xs_base = (const char *)h->stage_s[b].p;
@@ -1305,7 +1381,8 @@ void free_all(cm_handle *h) {
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
                      &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->eq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
-                     &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx};
+                     &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx,
+                     &h->dcd_sidx, &h->dcd_vidx, &h->dcd_raw[0], &h->dcd_raw[1]};
     for (DevBuf *b : all) {
         blocks().put(h->device, false, b->p, b->bytes);
         b->p = nullptr;
@@ -1837,6 +1914,37 @@ int cm_submit_frames(cm_handle *h, const cm_frames *frames) {
 
 int cm_synchronize(cm_handle *h) {
     return guarded(h, [&] { check_device_error(h); });
+}
+
+int cm_set_dcd_layout(cm_handle *h, const cm_dcd_layout *L) {
+    return guarded(h, [&] {
+        if (!L) throw cm_error(CM_EINVAL, "NULL layout");
+        if (L->natoms < 1 || L->natoms >= (1LL << 31)) throw cm_error(CM_EINVAL, "natoms out of range");
+        if (L->frame_bytes < 12 * L->natoms || L->frame_bytes % 4) throw cm_error(CM_EINVAL, "frame_bytes must hold three float32 arrays and be a multiple of 4");
+        const int64_t off[3] = {L->x_offset, L->y_offset, L->z_offset};
+        for (int k = 0; k < 3; ++k)
+            if (off[k] < 0 || off[k] % 4 || off[k] + 4 * L->natoms > L->frame_bytes)
+                throw cm_error(CM_EINVAL, "x/y/z offsets must be multiples of 4 with the arrays inside the frame");
+        if (!L->solute_atoms) throw cm_error(CM_EINVAL, "solute_atoms is required");
+        if (h->d.autocorrelation != (L->solvent_atoms == nullptr))
+            throw cm_error(CM_EINVAL, "solvent_atoms is required for a cross MDDF and must be NULL in self mode");
+        if (h->planned && h->coord_elem != 4) throw cm_error(CM_ESTATE, "this handle was planned for float64 frames");
+        auto take = [&](const int32_t *src, int64_t n, std::vector<int32_t> &dst, DevBuf &dev) {
+            dst.assign(src, src + n);
+            for (int32_t a : dst)
+                if (a < 0 || a >= L->natoms) throw cm_error(CM_EINVAL, "selection atom index outside the DCD frame");
+            dev_alloc(h, dev, (size_t)n * 4);
+            CM_CUDA(cudaMemcpyAsync(dev.p, dst.data(), (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+        };
+        take(L->solute_atoms, h->Ns, h->dcd_s, h->dcd_sidx);
+        if (!h->d.autocorrelation) take(L->solvent_atoms, h->Nv, h->dcd_v, h->dcd_vidx);
+        CM_CUDA(cudaStreamSynchronize(h->stream));
+        h->dcd_natoms = L->natoms;
+        h->dcd_frame_bytes = L->frame_bytes;
+        for (int k = 0; k < 3; ++k) h->dcd_off[k] = off[k];
+        h->dcd_swap = L->big_endian ? 1 : 0;
+        h->dcd = true;
+    });
 }
 
 int cm_batch_create(cm_handle *const *handles, int32_t nhandles, cm_batch **out) {

@@ -260,6 +260,51 @@ class Engine:
         # contiguous copies made here) until the next synchronising call
         self._inflight.append(keep)
 
+    def set_dcd_layout(self, *, natoms, frame_bytes, x_offset, y_offset, z_offset, big_endian, solute_atoms,
+                       solvent_atoms=None) -> None:
+        """Declare the raw DCD frame layout and the selections' 0-based atom
+        indices in the frame (cm_set_dcd_layout), for ``submit_dcd``."""
+        s = np.ascontiguousarray(np.asarray(solute_atoms, dtype=np.int32).reshape(-1))
+        v = None if solvent_atoms is None else np.ascontiguousarray(np.asarray(solvent_atoms, dtype=np.int32).reshape(-1))
+        if s.size != self.Ns or (v is not None and v.size != self.Nv):
+            raise ValueError("one atom index per selection atom")
+        L = N.cm_dcd_layout(natoms=natoms, frame_bytes=frame_bytes, x_offset=x_offset, y_offset=y_offset,
+                            z_offset=z_offset, big_endian=1 if big_endian else 0)
+        L.solute_atoms = N.as_ptr(s, C.c_int32)
+        L.solvent_atoms = N.as_ptr(v, C.c_int32) if v is not None else None
+        N.raise_for(self._lib.cm_set_dcd_layout(self._h, C.byref(L)), self._h)
+
+    def submit_dcd(self, raw, cells, weights=None, frame_ids=None) -> None:
+        """Add frames given as raw DCD bytes [nframes, frame_bytes] (uint8
+        numpy array, or torch tensor on the host or the device); the engine
+        gathers the selections on the device."""
+        if _is_torch(raw):
+            nf = int(raw.shape[0])
+            keep_raw = raw.contiguous()
+            mem = N.CM_MEM_DEVICE if keep_raw.is_cuda else N.CM_MEM_HOST
+            ptr = keep_raw.data_ptr()
+        else:
+            keep_raw = np.ascontiguousarray(np.asarray(raw, dtype=np.uint8))
+            nf = int(keep_raw.shape[0])
+            mem = N.CM_MEM_HOST
+            ptr = keep_raw.ctypes.data
+        cells = np.asarray(cells, dtype=np.float64).reshape(nf, 3, 3)
+        cm = np.ascontiguousarray(np.transpose(cells, (0, 2, 1))).reshape(nf, 9)
+        w = None if weights is None else np.ascontiguousarray(np.asarray(weights, dtype=np.float64).reshape(nf))
+        ids = np.arange(1, nf + 1, dtype=np.int64) if frame_ids is None else np.ascontiguousarray(
+            np.asarray(frame_ids, dtype=np.int64).reshape(nf))
+        fr = N.cm_frames()
+        fr.nframes = nf
+        fr.coord_type = N.CM_COORD_DCD
+        fr.memory = mem
+        fr.solute_xyz = C.c_void_p(ptr)
+        fr.solvent_xyz = None
+        fr.cells = N.as_ptr(cm, C.c_double)
+        fr.weights = N.as_ptr(w, C.c_double) if w is not None else None
+        fr.frame_ids = N.as_ptr(ids, C.c_int64)
+        N.raise_for(self._lib.cm_submit_frames(self._h, C.byref(fr)), self._h)
+        self._inflight.append([keep_raw, cm, w, ids])
+
     # -------------------------------------------------------------- output
     def counts(self) -> dict:
         """Frame-weighted counts (the Result fields before finalresults!)."""

@@ -15,7 +15,7 @@ import numpy as np
 from .engine import Engine
 from .options import Options, TrajectoryFileOptions
 from .results import Result, check_frame_weights, finalresults, isautocorrelation, setbin
-from .trajectory import ArrayTrajectory, Trajectory, cell_matrix, make_trajectory, trajectory_metadata
+from .trajectory import ArrayTrajectory, NamdDCD, Trajectory, cell_matrix, make_trajectory, trajectory_metadata
 
 STOP_FILE = "stop_complexmixtures"
 
@@ -128,6 +128,9 @@ def _run_frames(eng: Engine, trajectory: Trajectory, to_compute, fw, batch_frame
             xs, xv, cells = trajectory.frame_arrays([i - 1 for i in ids])
             eng.submit(xs, None if eng.autocorrelation else xv, cells, weights=[fw[i - 1] for i in ids], frame_ids=ids)
         return
+    if isinstance(trajectory, NamdDCD):
+        _run_dcd_frames(eng, trajectory, to_compute, fw, batch_frames)
+        return
     wanted = set(to_compute)
     last = max(to_compute)
     trajectory.opentraj()
@@ -156,6 +159,28 @@ def _run_frames(eng: Engine, trajectory: Trajectory, to_compute, fw, batch_frame
         flush()
     finally:
         trajectory.closetraj()
+
+
+def _run_dcd_frames(eng: Engine, traj: NamdDCD, to_compute, fw, batch_frames: int) -> None:
+    """DCD frames go to the engine as the bytes read from the file; the
+    engine gathers the selections on the device (no host-side gather or
+    float32 -> float64 conversion)."""
+    lay = traj.dcd_layout()
+    s = np.asarray(traj.solute.indices, dtype=np.int64) - 1
+    v = None if eng.autocorrelation else np.asarray(traj.solvent.indices, dtype=np.int64) - 1
+    eng.set_dcd_layout(solute_atoms=s, solvent_atoms=v, **lay)
+    for b0 in range(0, len(to_compute), batch_frames):
+        if os.path.isfile(STOP_FILE):
+            break
+        ids = to_compute[b0 : b0 + batch_frames]
+        lo, hi = ids[0], ids[-1]
+        if hi - lo + 1 == len(ids):           # consecutive frames: one read
+            raw, cells = traj.read_raw(lo - 1, len(ids))
+        else:                                 # strided frames: read each one
+            parts = [traj.read_raw(i - 1, 1) for i in ids]
+            raw = np.concatenate([p[0] for p in parts])
+            cells = np.concatenate([p[1] for p in parts])
+        eng.submit_dcd(raw, cells, weights=[fw[i - 1] for i in ids], frame_ids=ids)
 
 
 def coordination_number(*args, **kw):

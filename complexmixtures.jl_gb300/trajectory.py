@@ -180,10 +180,51 @@ class NamdDCD(Trajectory):
         self._gather(np.stack([x, y, z], axis=1))
 
     def getunitcell(self):
-        A, gamma, B, beta, alpha, Cc = self._unitcell
+        return self._cell_of(self._unitcell)
+
+    @staticmethod
+    def _cell_of(uc):
+        A, gamma, B, beta, alpha, Cc = (float(x) for x in uc)
         if alpha == 0.0 or beta == 0.0 or gamma == 0.0:
             alpha = beta = gamma = 90.0
         return unitcell_from_lengths_angles(A, B, Cc, alpha, beta, gamma)
+
+    # raw frames for the engine's device-side decode (cm_set_dcd_layout)
+    @property
+    def frame_bytes(self) -> int:
+        return (8 + 48) + 3 * (8 + 4 * self.natoms_file)
+
+    def dcd_layout(self) -> dict:
+        """Byte layout of one frame: the unit-cell record, then the x, y and
+        z records (each float32 array behind a 4-byte marker)."""
+        n4 = 4 * self.natoms_file
+        x = 56 + 4
+        return dict(natoms=self.natoms_file, frame_bytes=self.frame_bytes, x_offset=x, y_offset=x + n4 + 8,
+                    z_offset=x + 2 * (n4 + 8), big_endian=self._endian == ">")
+
+    def read_raw(self, first: int, n: int):
+        """Frames first .. first + n - 1 (0-based) as bytes [n, frame_bytes]
+        and their cells [n, 3, 3]; the record markers are checked."""
+        fb = self.frame_bytes
+        with open(self.filename, "rb") as f:
+            f.seek(self._data_start + first * fb)
+            raw = np.fromfile(f, dtype=np.uint8, count=n * fb)
+        if raw.size != n * fb:
+            raise ValueError("DCD file ends inside a frame")
+        raw = raw.reshape(n, fb)
+        marks = raw.view(self._endian + "i4")
+        n4 = 4 * self.natoms_file
+        want = {0: 48, 13: 48}
+        for k in range(3):
+            o = 56 + k * (n4 + 8)
+            want[o // 4] = n4
+            want[(o + 4 + n4) // 4] = n4
+        for col, val in want.items():
+            if np.any(marks[:, col] != val):
+                raise ValueError("corrupted Fortran record in DCD file")
+        uc = np.ascontiguousarray(raw[:, 4:52]).view(self._endian + "f8").reshape(n, 6)
+        cells = np.stack([self._cell_of(u) for u in uc])
+        return raw, cells
 
     def closetraj(self):
         if self._f:

@@ -58,7 +58,10 @@ enum { CM_REGIME_AUTO = 0, CM_REGIME_PAIRS = 1, CM_REGIME_ATOMS = 2 };
  * executable graph per handle (updated in place while the chain keeps its
  * shape).  AUTO takes GRAPH unless kernel_timing is set. */
 enum { CM_LAUNCH_AUTO = 0, CM_LAUNCH_STREAM = 1, CM_LAUNCH_GRAPH = 2 };
-enum { CM_COORD_F64 = 0, CM_COORD_F32 = 1 };
+/* CM_COORD_DCD: solute_xyz points at nframes raw DCD frames (frame_bytes each,
+ * laid out as cm_set_dcd_layout declared) and solvent_xyz is NULL; the
+ * engine gathers the selections on the device. */
+enum { CM_COORD_F64 = 0, CM_COORD_F32 = 1, CM_COORD_DCD = 2 };
 enum { CM_MEM_HOST = 0, CM_MEM_DEVICE = 1 };
 
 /*
@@ -120,7 +123,7 @@ typedef struct cm_system_desc {
  */
 typedef struct cm_frames {
     int32_t nframes;
-    int32_t coord_type;               /* CM_COORD_F64 or CM_COORD_F32 */
+    int32_t coord_type;               /* CM_COORD_F64, CM_COORD_F32 or CM_COORD_DCD */
     int32_t memory;                   /* where solute_xyz / solvent_xyz live: CM_MEM_HOST / CM_MEM_DEVICE */
     int32_t reserved;
     const void *solute_xyz;           /* [nframes][solute atoms][3] */
@@ -208,6 +211,29 @@ int cm_submit_frames(cm_handle *h, const cm_frames *frames);
 
 /* Wait for all submitted work; returns CM_EDEVICE if a kernel raised its error flag. */
 int cm_synchronize(cm_handle *h);
+
+/*
+ * Raw DCD frames (replaces the host-side read and gather of
+ * src/trajectory_formats/NamdDCD.jl:141-169 and the selection copy of
+ * src/Trajectory.jl's nextframe!): frames are given to cm_submit_frames with
+ * coord_type CM_COORD_DCD as the bytes read from the file, from the first byte
+ * of a frame's unit-cell record to the last byte of its z record, and the
+ * engine gathers the selected atoms on the device.  The unit cells still come
+ * through cm_frames.cells (parsed on the host: the frame geometry is host
+ * work).  Set once per handle, before the first DCD submit.
+ */
+typedef struct cm_dcd_layout {
+    int64_t natoms;                   /* atoms per frame in the file */
+    int64_t frame_bytes;              /* bytes per frame (a multiple of 4) */
+    int64_t x_offset;                 /* byte offset, within a frame, of the first x value (past its record marker) */
+    int64_t y_offset;
+    int64_t z_offset;
+    int32_t big_endian;               /* 1: the file's floats are big-endian */
+    int32_t reserved;
+    const int32_t *solute_atoms;      /* host [solute atoms]: 0-based atom index in the frame, selection order */
+    const int32_t *solvent_atoms;     /* host [solvent atoms]; NULL in self mode */
+} cm_dcd_layout;
+int cm_set_dcd_layout(cm_handle *h, const cm_dcd_layout *layout);
 
 /*
  * Batches of systems (no counterpart in the reference, which runs one system
