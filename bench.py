@@ -302,6 +302,7 @@ def batched_c4_leg(cm, device):
     xs, xv, cells, kw = systems[med]
     tune = cm.autotune(xs[:2], xv[:2], cells[:2], **kw)
     pct = tune["cell_scale_pct"]
+    sched = tune["atoms_schedule"]
     frames_total = C4_FRAMES * len(systems)
 
     def serial():
@@ -309,7 +310,7 @@ def batched_c4_leg(cm, device):
         torch.cuda.synchronize()
         t = time.perf_counter()
         for xs, xv, cells, kw in systems:
-            eng = cm.Engine(cell_scale_pct=pct, **kw)
+            eng = cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, **kw)
             eng.submit(xs, xv, cells)
             out.append(eng.raw_counts())
             eng.close()
@@ -319,7 +320,7 @@ def batched_c4_leg(cm, device):
         # all 64 systems in one cm_batch: one CUDA graph launch per staging round
         torch.cuda.synchronize()
         t = time.perf_counter()
-        engines = [cm.Engine(cell_scale_pct=pct, **kw) for xs, xv, cells, kw in systems]
+        engines = [cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, **kw) for xs, xv, cells, kw in systems]
         with cm.Batch(engines) as b:
             b.submit([(xs, xv, cells) for xs, xv, cells, kw in systems])
             gst = b.graph_stats()
@@ -336,7 +337,7 @@ def batched_c4_leg(cm, device):
                      for i in range(len(systems)))
     with cm.Server(device=device, frames_per_turn=C4_FRAMES) as srv:
         t0 = time.perf_counter()
-        ids = [srv.submit(xs, xv, cells, cell_scale_pct=pct, **kw) for xs, xv, cells, kw in systems]
+        ids = [srv.submit(xs, xv, cells, cell_scale_pct=pct, atoms_schedule=sched, **kw) for xs, xv, cells, kw in systems]
         infos = [srv.wait(r, timeout=600) for r in ids]
         tb = time.perf_counter() - t0
         same = all(all(np.array_equal(srv.raw_counts(r)[k], ref[i][k]) for k in ("md", "md_random", "solute_group"))
@@ -352,7 +353,9 @@ def batched_c4_leg(cm, device):
         "graph_batch_launches": gst["graph_launches"],
         "graph_batch_counts_identical_to_serial": bool(same_graph),
         "p50_ms": pct_lat["p50"], "p99_ms": pct_lat["p99"],
-        "cell_scale_pct": pct, "autotune_ms_per_frame": tune["candidates"],
+        "cell_scale_pct": pct, "atoms_schedule": sched,
+        "autotune_ms_per_frame": {f'{c["cell_scale_pct"]}/{c["atoms_schedule"]}': round(c["ms_per_frame"], 4)
+                                  for c in tune["candidates"]},
         "failed": sum(1 for x in infos if x["state"] != "done"),
         "counts_identical_to_serial": bool(same),
     }

@@ -10,8 +10,8 @@ ABI of include/cmgpu.h; there is no CPU fallback.
 from .options import Options, TrajectoryFileOptions, make_options
 from .selection import (AtomSelection, SoluteGroup, SolventGroup, atom_group, atom_group_name,
                         atom_group_names, set_nmols_natomspermol)
-from .results import (Density, Result, Volume, finalresults, renormalize, result_from_json, setbin, shellradius,
-                      sphericalshellvolume, sum_results, units)
+from .results import (Density, Result, Volume, finalresults, load, merge, renormalize, result_from_json, save, setbin,
+                      shellradius, sphericalshellvolume, sum_results, units)
 from .trajectory import (ArrayTrajectory, NamdDCD, PDBTraj, Trajectory, TrajectoryMetaData, convert_unitcell,
                          make_trajectory, trajectory_metadata, unitcell_from_lengths_angles)
 from .contributions import contributions
@@ -24,7 +24,7 @@ __all__ = [
     "Options", "TrajectoryFileOptions", "make_options", "AtomSelection", "SoluteGroup", "SolventGroup",
     "atom_group", "atom_group_name", "atom_group_names", "set_nmols_natomspermol", "Density", "Result",
     "Volume", "finalresults", "renormalize", "result_from_json", "setbin", "shellradius", "sphericalshellvolume",
-    "sum_results", "units", "ArrayTrajectory", "NamdDCD", "PDBTraj", "Trajectory", "TrajectoryMetaData",
+    "sum_results", "units", "save", "load", "merge", "ArrayTrajectory", "NamdDCD", "PDBTraj", "Trajectory", "TrajectoryMetaData",
     "convert_unitcell", "make_trajectory", "trajectory_metadata", "unitcell_from_lengths_angles", "contributions",
     "Batch", "Engine", "autotune", "memory_cache", "Server", "latency_percentiles", "coordination_number", "engine_for", "mddf", "new_result", "NativeUnavailable",
 ]

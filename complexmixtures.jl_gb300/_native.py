@@ -18,6 +18,7 @@ CM_MODE_MDDF, CM_MODE_COORDINATION_NUMBER = 0, 1
 CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
 CM_REGIME_AUTO, CM_REGIME_PAIRS, CM_REGIME_ATOMS = 0, 1, 2
 CM_LAUNCH_AUTO, CM_LAUNCH_STREAM, CM_LAUNCH_GRAPH = 0, 1, 2
+CM_SCHED_AUTO, CM_SCHED_CELL, CM_SCHED_BALANCED = 0, 1, 2
 CM_COORD_F64, CM_COORD_F32, CM_COORD_DCD = 0, 1, 2
 CM_MEM_HOST, CM_MEM_DEVICE = 0, 1
 CM_NOALLOC_SCRATCH_BYTES = 32 << 20
@@ -63,7 +64,7 @@ class cm_system_desc(C.Structure):
         ("kernel_timing", C.c_int32),
         ("cell_scale_pct", C.c_int32),
         ("launch", C.c_int32),
-        ("reserved", C.c_int32),
+        ("atoms_schedule", C.c_int32),
     ]
 
 
@@ -163,6 +164,9 @@ class cm_tuning(C.Structure):
         ("ncandidates", C.c_int32),
         ("candidates", C.c_int32 * CM_TUNE_MAX),
         ("ms_per_frame", C.c_double * CM_TUNE_MAX),
+        ("atoms_schedule", C.c_int32),
+        ("schedules", C.c_int32 * CM_TUNE_MAX),
+        ("reserved", C.c_int32),
     ]
 
 

@@ -6,12 +6,14 @@
 // marks every cell within one stencil of an occupied cell ("near").  A solvent
 // molecule none of whose atoms sits in a near cell has every atom pair beyond
 // the cutoff and is dropped by k_atoms_filter (real pass) or by the placement
-// kernel (random insertion); the others go to a queue.  For dense solutes
-// (many atoms per occupied cell) k_atoms_eval takes one queue entry per warp:
+// kernel (random insertion); the others go to a queue.  k_atoms_eval takes
+// one queue entry per warp.  For dense solutes (many atoms per occupied cell),
 // for each solvent atom and stencil cell, the lanes read consecutive solute
-// atoms of the cell (coalesced) and keep their own top-2, and a shuffle
-// reduction gives the molecule pair's closest pair, second-closest distance
-// and reference-atom row; for sparse solutes one thread takes an entry.  Cells
+// atoms of the cell (coalesced); for sparse solutes the lanes run through the
+// atoms of all stencil cells end to end, so no lane idles on a short cell.
+// Each lane keeps its own top-2, and a shuffle reduction gives the molecule
+// pair's closest pair, second-closest distance and reference-atom row (the
+// FP64 engine path takes one thread per entry for sparse solutes).  Cells
 // whose box is farther than the cutoff from the atom are skipped.  The
 // decision follows the FP32 + guard rules; inside the guard band the exact
 // FP64 scan (warp-cooperative in warp mode, reduced in the order of the
@@ -199,6 +201,64 @@ __device__ __forceinline__ void atoms_walk(const FrameGeom &G, const FrameScratc
     }
 }
 
+// Warp-cooperative FP32 walk of a site's stencil, balanced over the lanes
+// whatever the cells' sizes.  The lanes take the stencil's cells 32 at a time
+// and prefix-sum their atom counts (cells beyond the cutoff count zero); the
+// cells' atoms, end to end, are then run through 32 at a time, one pair per
+// lane.  Lane l of the window of pairs [kb, kb + 32) belongs to the last cell
+// that starts at or before kb + l: every cell with atoms in the window sets
+// bit (start - kb, or 0 for the cell running into the window) of a mask and
+// leaves its displacement base and atom base in win[that bit], and the lane
+// takes the highest set bit at or below l.  body(p, tx, ty, tz) gets the
+// solute atom and the site's position relative to that cell image.
+template <typename Body>
+__device__ __forceinline__ void atoms_walk_flat(const FrameGeom &G, const FrameScratch &F, const int *cs, const Site &st,
+                                                float prune2, const float4 *off32, int lane, float4 *win, Body &&body) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int nx = 2 * F.La[0] + 1, ny = 2 * F.La[1] + 1;
+    const int ncells = nx * ny * (2 * F.La[2] + 1);
+    for (int c0 = 0; c0 < ncells; c0 += 32) {
+        const int ci = c0 + lane;
+        int cnt = 0, beg = 0;
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        if (ci < ncells) {
+            const int dx = ci % nx - F.La[0], dy = (ci / nx) % ny - F.La[1], dz = ci / (nx * ny) - F.La[2];
+            const int cell = (wrap_cell(st.cz + dz, G.n[2]) * G.n[1] + wrap_cell(st.cy + dy, G.n[1])) * G.n[0] +
+                             wrap_cell(st.cx + dx, G.n[0]);
+            beg = cs[cell];
+            const int end = cs[cell + 1];
+            if (end > beg && cell_d2(F, st, dx, dy, dz) <= prune2) {
+                cnt = end - beg;
+                const float4 of = off32[off_index(dx, dy, dz)];
+                tx = st.q.x - of.x;
+                ty = st.q.y - of.y;
+                tz = st.q.z - of.z;
+            }
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += u;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        const int excl = incl - cnt;
+        for (int kb = 0; kb < total; kb += 32) {
+            const bool in = cnt > 0 && excl < kb + 32 && incl > kb;
+            const int pos = in ? max(excl - kb, 0) : 0;
+            if (in) win[pos] = make_float4(tx, ty, tz, __int_as_float(beg - excl));
+            const unsigned m = __reduce_or_sync(kFull, in ? (1u << pos) : 0u);
+            __syncwarp();
+            const int k = kb + lane;
+            if (k < total) {
+                const float4 w = win[31 - __clz(m & (kFull >> (31 - lane)))];
+                body(__float_as_int(w.w) + k, w.x, w.y, w.z);
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // What the exact scan of one queued molecule pair reads.
 struct AtomsPair {
     const FrameGeom *G;
@@ -256,16 +316,25 @@ __device__ __noinline__ void atoms_exact(const DevSys &S, const AtomsPair &A, in
     if (STRIDE == 32) best_reduce(Bst, rr1, evals);
 }
 
-// ATOMS evaluation of the queue (persistent grid): one warp per entry for
-// dense solutes (many atoms per cell), one thread per entry for sparse ones.
-template <bool FP32, bool RANDOM, bool WARP>
+// Schedules of k_atoms_eval.  CELL: one warp per queue entry, the lanes over
+// the atoms of each stencil cell in turn (dense solutes: cells of a warp's
+// worth of atoms or more).  BALANCED: one warp per entry, the lanes over the
+// cells' atoms end to end (atoms_walk_flat; sparse solutes in FP32).  THREAD:
+// one thread per entry (sparse solutes in the FP64 engine path).
+enum AtomsSched { kSchedThread = 0, kSchedCell = 1, kSchedBalanced = 2 };
+
+// ATOMS evaluation of the queue (persistent grid).
+template <bool FP32, bool RANDOM, int SCHED>
 __global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bufs B) {
+    constexpr bool WARP = SCHED != kSchedThread;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float4 s_win[kAtomsWarps][32];  // atoms_walk_flat's window table, one per warp
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);
     __syncthreads();
     SHist h = shist_bind(S, hbase);
     LocalStats st;
+    float4 *win = s_win[threadIdx.x >> 5];
     // WARP: one warp per queue entry, lanes over the atoms of each cell;
     // otherwise one thread per entry (lane 0 of a one-thread "warp")
     constexpr int STRIDE = WARP ? 32 : 1;
@@ -352,22 +421,27 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bu
             for (int b = 0; b < apv; ++b) {
                 const Site sb = site_of(F, vcell[vb + b], vq32[vb + b]);
                 const bool isref = b == iref;
-                atoms_walk(G, F, cs, sb, prune2, [&](int beg, int end, int oi) {
-                    const float4 of = off32[oi];
-                    const float tx = sb.q.x - of.x, ty = sb.q.y - of.y, tz = sb.q.z - of.z;
-                    for (int p = beg + lane; p < end; p += STRIDE) {
-                        lane_evals++;
-                        const float4 qa = sq32[p];
-                        const float ex = qa.x - tx, ey = qa.y - ty, ez = qa.z - tz;
-                        const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                        T.m2 = fminf(T.m2, fmaxf(T.m1, d2));
-                        const bool lt = d2 < T.m1;
-                        T.p1 = lt ? p : T.p1;
-                        T.b1 = lt ? b : T.b1;
-                        T.m1 = fminf(T.m1, d2);
-                        if (isref) T.r1 = fminf(T.r1, d2);
-                    }
-                });
+                auto pair = [&](int p, float tx, float ty, float tz) {
+                    lane_evals++;
+                    const float4 qa = sq32[p];
+                    const float ex = qa.x - tx, ey = qa.y - ty, ez = qa.z - tz;
+                    const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                    T.m2 = fminf(T.m2, fmaxf(T.m1, d2));
+                    const bool lt = d2 < T.m1;
+                    T.p1 = lt ? p : T.p1;
+                    T.b1 = lt ? b : T.b1;
+                    T.m1 = fminf(T.m1, d2);
+                    if (isref) T.r1 = fminf(T.r1, d2);
+                };
+                if (SCHED == kSchedBalanced) {
+                    atoms_walk_flat(G, F, cs, sb, prune2, off32, lane, win, pair);
+                } else {
+                    atoms_walk(G, F, cs, sb, prune2, [&](int beg, int end, int oi) {
+                        const float4 of = off32[oi];
+                        const float tx = sb.q.x - of.x, ty = sb.q.y - of.y, tz = sb.q.z - of.z;
+                        for (int p = beg + lane; p < end; p += STRIDE) pair(p, tx, ty, tz);
+                    });
+                }
             }
             if (WARP) top2_reduce(T);
             if (T.m1 <= g.cutp2) {

@@ -190,7 +190,7 @@ struct cm_handle {
         anear, aq;
     int aq_cap = 0;
     int atoms_ctas = 0;    // resident CTAs per SM of k_atoms_eval
-    bool atoms_warp = true; // ATOMS evaluation: one warp (dense solutes) or one thread per queued pair
+    bool atoms_dense = true; // ATOMS evaluation schedule: dense solutes (many atoms per occupied cell) or sparse
     int atoms_piece = 0;   // samples placed per random-insertion launch
     // pinned host staging
     FrameGeom *h_geoms[2] = {nullptr, nullptr};
@@ -351,6 +351,7 @@ void check_desc(const cm_system_desc *d) {
     if (!d) bad("NULL system description");
     if (d->api_version != CM_API_VERSION) bad("api_version mismatch");
     if (d->launch < CM_LAUNCH_AUTO || d->launch > CM_LAUNCH_GRAPH) bad("unknown launch mode");
+    if (d->atoms_schedule < CM_SCHED_AUTO || d->atoms_schedule > CM_SCHED_BALANCED) bad("unknown atoms_schedule");
     if (d->solute_nmols < 1 || d->solute_natomspermol < 1 || d->solvent_nmols < 1 || d->solvent_natomspermol < 1)
         bad("selections must have at least one molecule of at least one atom");
     if (d->autocorrelation && (d->solute_nmols != d->solvent_nmols || d->solute_natomspermol != d->solvent_natomspermol))
@@ -510,6 +511,52 @@ FlatKernel flat_kernel(const cm_handle *h) {
                                 : flat_kernel_of<false>(h->d.solute_natomspermol);
 }
 
+// Shared memory one CTA of the system's kernels needs at most; fails when
+// it is beyond the device's opt-in limit (very many histogram bins).
+void check_smem(const cm_handle *h, size_t need) {
+    int optin = 0;
+    CM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+    if (need > (size_t)optin)
+        throw cm_error(CM_EINVAL, "the histograms need " + std::to_string(need) +
+                                      " bytes of shared memory per block, more than the device's " +
+                                      std::to_string(optin) + " (use fewer bins)");
+}
+
+// Resident CTAs per SM of the FP32 real pass.
+int flat_setup(cm_handle *h) {
+    const size_t smem = hist_smem_bytes(h, h->smem_groups) + (size_t)kFlatWarps * flat_warp_smem();
+    const FlatKernel k = flat_kernel(h);
+    int n = 0;
+    CM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, kFlatWarps * 32, smem));
+    return std::max(1, n);
+}
+
+// The ATOMS evaluation kernels of a system (precision x schedule).
+using AtomsLaunch = void (*)(int, size_t, cudaStream_t, const DevSys &, const Bufs &);
+struct AtomsKernels {
+    const void *fn, *fn_random;
+    AtomsLaunch real, random;
+};
+
+template <bool FP32, bool RANDOM, int SCHED>
+void launch_atoms(int grid, size_t smem, cudaStream_t st, const DevSys &S, const Bufs &B) {
+    k_atoms_eval<FP32, RANDOM, SCHED><<<grid, kAtomsWarps * 32, smem, st>>>(S, B);
+}
+
+template <bool FP32, int SCHED>
+AtomsKernels atoms_kernels_of() {
+    return {(const void *)k_atoms_eval<FP32, false, SCHED>, (const void *)k_atoms_eval<FP32, true, SCHED>,
+            launch_atoms<FP32, false, SCHED>, launch_atoms<FP32, true, SCHED>};
+}
+
+// Dense solutes: a warp over each cell's atoms; sparse: the balanced warp
+// walk in FP32, a thread per entry in FP64.
+AtomsKernels atoms_kernels(const cm_handle *h) {
+    const bool fp32 = h->d.precision == CM_PRECISION_FP32_GUARD;
+    if (fp32) return h->atoms_dense ? atoms_kernels_of<true, kSchedCell>() : atoms_kernels_of<true, kSchedBalanced>();
+    return h->atoms_dense ? atoms_kernels_of<false, kSchedCell>() : atoms_kernels_of<false, kSchedThread>();
+}
+
 // The dynamic shared-memory limit of a kernel is a property of the function
 // shared by every handle of the process, so it is raised once per device to
 // the opt-in maximum (less the kernel's static shared memory) for every kernel
@@ -535,14 +582,11 @@ void kernel_smem_limits(int device) {
     raise((const void *)k_pairs_real<false, false>);
     raise((const void *)k_random_eval<true>);
     raise((const void *)k_random_eval<false>);
-    raise((const void *)k_atoms_eval<true, true, true>);
-    raise((const void *)k_atoms_eval<true, false, true>);
-    raise((const void *)k_atoms_eval<false, true, true>);
-    raise((const void *)k_atoms_eval<false, false, true>);
-    raise((const void *)k_atoms_eval<true, true, false>);
-    raise((const void *)k_atoms_eval<true, false, false>);
-    raise((const void *)k_atoms_eval<false, true, false>);
-    raise((const void *)k_atoms_eval<false, false, false>);
+    for (const AtomsKernels &k : {atoms_kernels_of<true, kSchedCell>(), atoms_kernels_of<true, kSchedBalanced>(),
+                                  atoms_kernels_of<false, kSchedCell>(), atoms_kernels_of<false, kSchedThread>()}) {
+        raise(k.fn);
+        raise(k.fn_random);
+    }
     raise((const void *)k_pairs_guard<true>);
     raise((const void *)k_pairs_guard<false>);
     raise((const void *)k_pairs_edge<true>);
@@ -554,49 +598,6 @@ void kernel_smem_limits(int device) {
     g_smem_done[device] = true;
 }
 
-// Shared memory one CTA of the system's kernels needs at most; fails when
-// it is beyond the device's opt-in limit (very many histogram bins).
-void check_smem(const cm_handle *h, size_t need) {
-    int optin = 0;
-    CM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-    if (need > (size_t)optin)
-        throw cm_error(CM_EINVAL, "the histograms need " + std::to_string(need) +
-                                      " bytes of shared memory per block, more than the device's " +
-                                      std::to_string(optin) + " (use fewer bins)");
-}
-
-// Resident CTAs per SM of the FP32 real pass.
-int flat_setup(cm_handle *h) {
-    const size_t smem = hist_smem_bytes(h, h->smem_groups) + (size_t)kFlatWarps * flat_warp_smem();
-    const FlatKernel k = flat_kernel(h);
-    int n = 0;
-    CM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, kFlatWarps * 32, smem));
-    return std::max(1, n);
-}
-
-// The ATOMS evaluation kernels of a system (precision x schedule).
-using AtomsLaunch = void (*)(int, size_t, cudaStream_t, const DevSys &, const Bufs &);
-struct AtomsKernels {
-    const void *fn;
-    AtomsLaunch real, random;
-};
-
-template <bool FP32, bool RANDOM, bool WARP>
-void launch_atoms(int grid, size_t smem, cudaStream_t st, const DevSys &S, const Bufs &B) {
-    k_atoms_eval<FP32, RANDOM, WARP><<<grid, kAtomsWarps * 32, smem, st>>>(S, B);
-}
-
-template <bool FP32, bool WARP>
-AtomsKernels atoms_kernels_of() {
-    return {(const void *)k_atoms_eval<FP32, false, WARP>, launch_atoms<FP32, false, WARP>, launch_atoms<FP32, true, WARP>};
-}
-
-AtomsKernels atoms_kernels(const cm_handle *h) {
-    const bool fp32 = h->d.precision == CM_PRECISION_FP32_GUARD;
-    if (fp32) return h->atoms_warp ? atoms_kernels_of<true, true>() : atoms_kernels_of<true, false>();
-    return h->atoms_warp ? atoms_kernels_of<false, true>() : atoms_kernels_of<false, false>();
-}
-
 // Resident CTAs per SM of the ATOMS evaluation kernel.
 int atoms_setup(cm_handle *h) {
     const size_t smem = hist_smem_bytes(h, h->smem_groups);
@@ -605,10 +606,10 @@ int atoms_setup(cm_handle *h) {
     return std::max(1, n);
 }
 
-// Mean solute atoms per occupied search cell in the first frame: a warp per
-// queued molecule pair pays off when the cells it walks hold about a warp's
-// worth of atoms; sparse solutes (chains spread through the box) take a
-// thread per pair.
+// Mean solute atoms per occupied search cell in the first frame: lanes over
+// each cell's atoms pay off when the cells hold about a warp's worth of atoms
+// or more; sparse solutes (chains spread through the box) take the balanced
+// walk (FP32) or a thread per queued pair (FP64).
 bool atoms_dense(const cm_handle *h, const cm_frames *f) {
     const int64_t n = h->Ns;
     std::vector<double> x(n * 3);
@@ -775,13 +776,14 @@ void plan(cm_handle *h, const cm_frames *f) {
         dev_alloc(h, h->aq, (size_t)h->aq_cap * sizeof(int4));
     }
     // histogram shared-memory plan
-    const size_t extra = h->regime == CM_REGIME_PAIRS ? pairs_extra_smem() : 0;
+    // (the ATOMS evaluation's window tables are static shared memory)
+    const size_t extra = h->regime == CM_REGIME_PAIRS ? pairs_extra_smem() : sizeof(float4) * 32 * kAtomsWarps;
     h->smem_groups = hist_smem_bytes(h, 1) + extra + 2048 <= 160 * 1024 ? 1 : 0;
     kernel_smem_limits(h->device);
     check_smem(h, hist_smem_bytes(h, h->smem_groups) + extra);
     if (h->regime == CM_REGIME_PAIRS) h->flat_ctas = flat_setup(h);
     else {
-        h->atoms_warp = atoms_dense(h, f);
+        h->atoms_dense = h->d.atoms_schedule == CM_SCHED_AUTO ? atoms_dense(h, f) : h->d.atoms_schedule == CM_SCHED_CELL;
         h->atoms_ctas = atoms_setup(h);
     }
     h->planned = true;
@@ -2253,16 +2255,19 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
     const bool atoms = desc->regime == CM_REGIME_ATOMS ||
                        (desc->regime == CM_REGIME_AUTO &&
                         (desc->solute_natomspermol > kMaxSmallMol || desc->solvent_natomspermol > kMaxSmallMol));
-    // ATOMS: cutoff / (lcell k); PAIRS: the molecule cell and smaller ones
+    // ATOMS: cutoff / (lcell k), each with both evaluation schedules;
+    // PAIRS: the molecule cell and smaller ones
     const int cand_atoms[] = {100, 80, 50, 34};
     const int cand_pairs[] = {100, 75, 60, 50};
     const int *cand = atoms ? cand_atoms : cand_pairs;
-    const int ncand = 4;
+    const int ncand = atoms ? 8 : 4;
     double best = 0.0;
     for (int c = 0; c < ncand; ++c) {
         cm_system_desc d = *desc;
-        d.cell_scale_pct = cand[c];
+        d.cell_scale_pct = cand[c % 4];
+        d.atoms_schedule = atoms ? (c < 4 ? CM_SCHED_CELL : CM_SCHED_BALANCED) : CM_SCHED_AUTO;
         d.kernel_timing = 1;
+        d.launch = CM_LAUNCH_STREAM;
         cm_handle *h = nullptr;
         int st = cm_create(&d, &h);
         if (st != CM_OK) return st;
@@ -2283,11 +2288,13 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
             return st;
         }
         cm_destroy(h);
-        out->candidates[c] = cand[c];
+        out->candidates[c] = cand[c % 4];
+        out->schedules[c] = d.atoms_schedule;
         out->ms_per_frame[c] = ms / std::max(1, sample->nframes);
         if (c == 0 || out->ms_per_frame[c] < best) {
             best = out->ms_per_frame[c];
-            out->cell_scale_pct = cand[c];
+            out->cell_scale_pct = cand[c % 4];
+            out->atoms_schedule = d.atoms_schedule;
         }
     }
     out->ncandidates = ncand;

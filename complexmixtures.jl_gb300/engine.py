@@ -22,6 +22,10 @@ def _is_torch(x) -> bool:
     return type(x).__module__.startswith("torch")
 
 
+SCHEDULES = {"auto": N.CM_SCHED_AUTO, "cell": N.CM_SCHED_CELL, "balanced": N.CM_SCHED_BALANCED}
+SCHEDULE_NAMES = {v: k for k, v in SCHEDULES.items()}
+
+
 def system_desc(
     *,
     solute_nmols: int,
@@ -51,12 +55,15 @@ def system_desc(
     kernel_timing: bool = False,
     cell_scale_pct: int = 0,
     launch: str = "auto",
+    atoms_schedule: str = "auto",
 ):
     """cm_system_desc of a system, and the arrays it points to (keep them
     alive while the description is in use).  ``cell_scale_pct`` scales the
     search cells (speed only; see ``autotune``); ``launch`` ("auto", "stream"
     or "graph") says whether each compute chunk's kernels are launched one by
-    one or replayed as a captured CUDA graph (speed only)."""
+    one or replayed as a captured CUDA graph; ``atoms_schedule`` ("auto",
+    "cell" or "balanced") picks the ATOMS-layout evaluation schedule (both
+    speed only)."""
     d = N.cm_system_desc()
     d.api_version = N.CM_API_VERSION
     d.solute_nmols = solute_nmols
@@ -98,12 +105,18 @@ def system_desc(
     if launch not in modes:
         raise ValueError(f"launch must be one of {sorted(modes)}")
     d.launch = modes[launch]
+    if atoms_schedule not in SCHEDULES:
+        raise ValueError(f"atoms_schedule must be one of {sorted(SCHEDULES)}")
+    d.atoms_schedule = SCHEDULES[atoms_schedule]
     return d, keep
 
 
 def autotune(solute_xyz, solvent_xyz, cells, frame_ids=None, **system) -> dict:
-    """Time the candidate search-cell sizes on sample frames (cm_autotune);
-    returns {"cell_scale_pct": best, "candidates": {pct: ms per frame}}."""
+    """Time the candidate search-cell sizes (and, in the ATOMS layout, both
+    evaluation schedules) on sample frames (cm_autotune).  Returns the fastest
+    as {"cell_scale_pct", "atoms_schedule"} plus "candidates", a list of
+    {"cell_scale_pct", "atoms_schedule", "ms_per_frame"}; pass the first two to
+    Engine."""
     lib = N.load()
     d, keep = system_desc(**system)
     Ns = d.solute_nmols * d.solute_natomspermol
@@ -112,8 +125,9 @@ def autotune(solute_xyz, solvent_xyz, cells, frame_ids=None, **system) -> dict:
     t = N.cm_tuning()
     N.raise_for(lib.cm_autotune(C.byref(d), C.byref(fr), C.byref(t)), None)
     del keep, keep_f
-    return {"cell_scale_pct": t.cell_scale_pct,
-            "candidates": {t.candidates[i]: t.ms_per_frame[i] for i in range(t.ncandidates)}}
+    return {"cell_scale_pct": t.cell_scale_pct, "atoms_schedule": SCHEDULE_NAMES[t.atoms_schedule],
+            "candidates": [{"cell_scale_pct": t.candidates[i], "atoms_schedule": SCHEDULE_NAMES[t.schedules[i]],
+                            "ms_per_frame": t.ms_per_frame[i]} for i in range(t.ncandidates)]}
 
 
 def memory_cache(device: int = 0, release: bool = False) -> dict:

@@ -346,3 +346,125 @@ def result_from_json(path: str) -> Result:
     v = D["volume"]
     R.volume = Volume(v["total"], v["bulk"], v["domain"], np.asarray(v["shell"], dtype=np.float64))
     return R
+
+
+def _json_value(x):
+    if isinstance(x, np.ndarray):
+        return x.tolist()
+    if isinstance(x, (np.floating, np.integer, np.bool_)):
+        return x.item()
+    return x
+
+
+def result_to_json(R: Result) -> dict:
+    """The fields of a Result in the reference's JSON layout and key order
+    (JSON3 of the struct, src/results.jl:61-118, 533-540)."""
+    def sel(a: AtomSelection):
+        return {"nmols": a.nmols, "natomspermol": a.natomspermol, "indices": list(a.indices),
+                "custom_groups": bool(a.custom_groups), "group_atom_indices": [list(g) for g in a.group_atom_indices],
+                "group_names": list(a.group_names)}
+
+    def rows(m):
+        return [list(map(float, r)) for r in np.asarray(m, dtype=np.float64).reshape(-1, R.nbins)]
+
+    files = []
+    for f in R.files:
+        o = f.options
+        files.append({"filename": f.filename,
+                      "options": {k: _json_value(getattr(o, k)) for k in Options.__dataclass_fields__},
+                      "irefatom": f.irefatom, "lastframe_read": f.lastframe_read, "nframes_read": f.nframes_read,
+                      "frame_weights": [float(w) for w in f.frame_weights]})
+    v = R.volume
+    return {
+        "Version": R.Version, "nbins": R.nbins, "dbulk": float(R.dbulk), "cutoff": float(R.cutoff),
+        "d": _json_value(R.d), "md_count": _json_value(R.md_count), "md_count_random": _json_value(R.md_count_random),
+        "coordination_number": _json_value(R.coordination_number),
+        "coordination_number_random": _json_value(R.coordination_number_random),
+        "mddf": _json_value(R.mddf), "kb": _json_value(R.kb), "autocorrelation": bool(R.autocorrelation),
+        "solute": sel(R.solute), "solvent": sel(R.solvent),
+        "solute_group_count": rows(R.solute_group_count), "solvent_group_count": rows(R.solvent_group_count),
+        "solute_group_count_random": rows(R.solute_group_count_random),
+        "solvent_group_count_random": rows(R.solvent_group_count_random),
+        "rdf_count": _json_value(R.rdf_count), "rdf_count_random": _json_value(R.rdf_count_random),
+        "sum_rdf_count": _json_value(R.sum_rdf_count), "sum_rdf_count_random": _json_value(R.sum_rdf_count_random),
+        "rdf": _json_value(R.rdf), "kb_rdf": _json_value(R.kb_rdf),
+        "density": {"solute": float(R.density.solute), "solvent": float(R.density.solvent),
+                    "solvent_bulk": float(R.density.solvent_bulk)},
+        "volume": {"total": float(v.total), "bulk": float(v.bulk), "domain": float(v.domain),
+                   "shell": _json_value(v.shell)},
+        "files": files, "weights": [float(w) for w in R.weights],
+    }
+
+
+def save(filename: str, R: Result) -> str:
+    """Write a Result as JSON that the reference's ``load`` reads
+    (src/results.jl:533-540); ``load`` here reads it back unchanged (floats
+    are written with enough digits to round-trip)."""
+    import os
+
+    filename = os.path.expanduser(filename)
+    with open(filename, "w") as f:
+        json.dump(result_to_json(R), f, separators=(",", ":"), allow_nan=True)
+    return f"Results saved in JSON file: {filename}"
+
+
+def load(filename: str) -> Result:
+    """Read a Result saved by ``save`` or by the reference (src/results.jl:567-588)."""
+    import os
+
+    try:
+        return result_from_json(os.path.expanduser(filename))
+    except (KeyError, TypeError, ValueError, json.JSONDecodeError) as e:
+        raise ValueError(f"The file {filename} does not appear to contain a Result object.") from e
+
+
+def merge(results: List[Result]) -> Result:
+    """Average of Results of the same analysis over several trajectories or
+    parts of one (src/tools/merge.jl:10-150): every function and counter is
+    weighted by the frame weight of each Result over the total; ``weights``
+    holds each file's share of the frames read."""
+    if not results:
+        raise ValueError("merge needs at least one Result")
+    for i, a in enumerate(results):
+        for b in results[i + 1:]:
+            if a.nbins != b.nbins:
+                raise ValueError("To merge Results, the number of bins of the histograms of the sets must be the same.")
+            if not math.isclose(a.cutoff, b.cutoff, rel_tol=math.sqrt(np.finfo(float).eps)):
+                raise ValueError("To merge Results, cutoff distance of the of the histograms of the sets must be the same.")
+            if a.solute != b.solute or a.solvent != b.solvent:
+                raise ValueError("To merge Results, the solute and solvent selections of the sets must be the same.")
+            for name in ("solute_group_count", "solvent_group_count"):
+                if np.shape(getattr(a, name)) != np.shape(getattr(b, name)):
+                    raise ValueError(f"field {name} of the results are incompatible.")
+    ntot_frames = sum(f.nframes_read for r in results for f in r.files)
+    tot_frame_weight = sum(sum_frame_weights(r) for r in results)
+    files = [f for r in results for f in r.files]
+    weights = [f.nframes_read / ntot_frames for f in files]
+    r0 = results[0]
+    R = Result(nbins=r0.nbins, dbulk=r0.dbulk, cutoff=r0.cutoff, autocorrelation=r0.autocorrelation, solute=r0.solute,
+               solvent=r0.solvent, files=files, weights=weights,
+               solute_group_count=np.zeros_like(np.asarray(r0.solute_group_count, dtype=np.float64)),
+               solvent_group_count=np.zeros_like(np.asarray(r0.solvent_group_count, dtype=np.float64)),
+               solute_group_count_random=np.zeros_like(np.asarray(r0.solute_group_count, dtype=np.float64)),
+               solvent_group_count_random=np.zeros_like(np.asarray(r0.solvent_group_count, dtype=np.float64)))
+    R.d = np.array(r0.d, dtype=np.float64)
+    warned = False
+    for k, r in enumerate(results):
+        w = sum_frame_weights(r) / tot_frame_weight
+        if not math.isclose(w, R.weights[k], rel_tol=math.sqrt(np.finfo(float).eps)) and not warned:
+            warned = True
+            warnings.warn("Frame weights and file weights differ, because custom frame weights were provided.")
+        for name in ("mddf", "kb", "rdf", "kb_rdf", "md_count", "md_count_random", "coordination_number",
+                     "coordination_number_random", "solute_group_count", "solute_group_count_random",
+                     "solvent_group_count", "solvent_group_count_random", "rdf_count", "rdf_count_random",
+                     "sum_rdf_count", "sum_rdf_count_random"):
+            setattr(R, name, getattr(R, name) + w * np.asarray(getattr(r, name), dtype=np.float64))
+        R.density.solute += w * r.density.solute
+        R.density.solvent += w * r.density.solvent
+        R.density.solvent_bulk += w * r.density.solvent_bulk
+        R.volume.total += w * r.volume.total
+        R.volume.bulk += w * r.volume.bulk
+        R.volume.domain += w * r.volume.domain
+        R.volume.shell = R.volume.shell + w * np.asarray(r.volume.shell, dtype=np.float64)
+    return R
+

@@ -58,6 +58,12 @@ enum { CM_REGIME_AUTO = 0, CM_REGIME_PAIRS = 1, CM_REGIME_ATOMS = 2 };
  * executable graph per handle (updated in place while the chain keeps its
  * shape).  AUTO takes GRAPH unless kernel_timing is set. */
 enum { CM_LAUNCH_AUTO = 0, CM_LAUNCH_STREAM = 1, CM_LAUNCH_GRAPH = 2 };
+/* ATOMS-layout evaluation schedule: CELL = a warp per queued molecule pair,
+ * lanes over each stencil cell's solute atoms in turn (dense solutes);
+ * BALANCED = lanes over the atoms of all stencil cells end to end in FP32 (a
+ * thread per pair in the FP64 path) for sparse solutes.  AUTO picks by the
+ * solute atoms per occupied cell of the first frame (64 or more: CELL). */
+enum { CM_SCHED_AUTO = 0, CM_SCHED_CELL = 1, CM_SCHED_BALANCED = 2 };
 /* CM_COORD_DCD: solute_xyz points at nframes raw DCD frames (frame_bytes each,
  * laid out as cm_set_dcd_layout declared) and solvent_xyz is NULL; the
  * engine gathers the selections on the device. */
@@ -114,7 +120,7 @@ typedef struct cm_system_desc {
     int32_t cell_scale_pct;           /* search-cell size in percent of the default (0 = 100, range 30-300);
                                          the counts do not depend on it, only the speed (cm_autotune) */
     int32_t launch;                   /* CM_LAUNCH_*; the counts do not depend on it */
-    int32_t reserved;                 /* 0 */
+    int32_t atoms_schedule;           /* CM_SCHED_*; the counts do not depend on it */
 } cm_system_desc;
 
 /*
@@ -305,15 +311,20 @@ void *cm_stream(cm_handle *h);
  * Autotuner.  No counterpart in the reference (its cell size is
  * cutoff / lcell).  Times the real and random-insertion passes of a sample
  * of frames for each candidate search-cell size, with temporary handles and
- * CUDA events, and returns the fastest as cell_scale_pct for cm_create.  The
- * candidates are the default cell (100 %) and smaller cells (more, finer
- * stencil cells: less volume searched per molecule, more cells to walk). */
+ * CUDA events, and returns the fastest as cell_scale_pct (and, in the ATOMS
+ * layout, atoms_schedule) for cm_create.  The candidates are the default cell
+ * (100 %) and smaller cells (more, finer stencil cells: less volume searched
+ * per molecule, more cells to walk), in the ATOMS layout each with both
+ * evaluation schedules. */
 #define CM_TUNE_MAX 8
 typedef struct cm_tuning {
     int32_t cell_scale_pct;           /* the fastest candidate */
     int32_t ncandidates;
     int32_t candidates[CM_TUNE_MAX];  /* cell_scale_pct of each candidate */
     double ms_per_frame[CM_TUNE_MAX]; /* measured GPU time per frame of each candidate */
+    int32_t atoms_schedule;           /* the fastest candidate's CM_SCHED_* (ATOMS layout; 0 otherwise) */
+    int32_t schedules[CM_TUNE_MAX];   /* CM_SCHED_* of each candidate */
+    int32_t reserved;
 } cm_tuning;
 
 int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *out);

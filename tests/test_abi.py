@@ -36,6 +36,42 @@ def test_struct_sizes_match_header(cm):
     assert C.sizeof(N.cm_kernel_times) == 112
     assert C.sizeof(N.cm_server_desc) == 24
     assert C.sizeof(N.cm_request_info) == 48
+    assert C.sizeof(N.cm_tuning) == 144
+    assert C.sizeof(N.cm_dcd_layout) == 64
+
+
+STRUCTS = ("cm_system_desc", "cm_frames", "cm_counts", "cm_raw_counts", "cm_stats", "cm_kernel_times", "cm_tuning",
+           "cm_dcd_layout", "cm_server_desc", "cm_request_info")
+
+
+def test_struct_layouts_match_c_compiler(cm, tmp_path):
+    """Every field offset and struct size of the ctypes mirror equals what a
+    C compiler makes of include/cmgpu.h."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    N = cm._native
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cmgpu.h"', 'int main(void) {']
+    for name in STRUCTS:
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for fname, _ in getattr(N, name)._fields_:
+            lines.append(f'printf("{name}.{fname} %zu\\n", offsetof({name}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], check=True, capture_output=True, text=True)
+               .stdout.splitlines())
+    for name in STRUCTS:
+        S = getattr(N, name)
+        assert int(out[name]) == C.sizeof(S), name
+        for fname, _ in S._fields_:
+            assert int(out[f"{name}.{fname}"]) == getattr(S, fname).offset, f"{name}.{fname}"
 
 
 def test_create_rejects_bad_descriptions_without_gpu(cm):

@@ -33,7 +33,7 @@ def make_system(rng, H, ms, aps, mv, apv, nframes, self_mode, spread=0.9):
 
 
 def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, regime, frame_ids=None, groups=None,
-            backend="cells", dtype=np.float64, cell_scale_pct=0, **opt):
+            backend="cells", dtype=np.float64, cell_scale_pct=0, atoms_schedule="auto", **opt):
     nf = xs.shape[0]
     frame_ids = list(range(1, nf + 1)) if frame_ids is None else frame_ids
     kw = dict(autocorrelation=self_mode, **opt)
@@ -46,7 +46,8 @@ def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, r
         gv = gv_rows(mv * apv, apv)
         g = dict(solute_groups=gs, solute_ngroups=5, solvent_groups=gv, solvent_ngroups=5)
     eng = cm.Engine(solute_nmols=ms, solute_natomspermol=aps, solvent_nmols=mv, solvent_natomspermol=apv,
-                    precision=precision, regime=regime, max_frames_per_batch=2, cell_scale_pct=cell_scale_pct, **kw,
+                    precision=precision, regime=regime, max_frames_per_batch=2, cell_scale_pct=cell_scale_pct,
+                    atoms_schedule=atoms_schedule, **kw,
                     **g)
     eng.submit(xs.astype(dtype), None if self_mode else xv.astype(dtype), cells, frame_ids=frame_ids)
     got = eng.raw_counts()
@@ -257,12 +258,44 @@ def test_cell_scale_does_not_change_counts(cm, orc, gpu_ready, pct, regime):
             regime=regime, cell_scale_pct=pct, **opt)
 
 
+@pytest.mark.parametrize("sched", ["cell", "balanced"])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("self_mode", [False, True], ids=["cross", "self"])
+def test_atoms_schedules_match_oracle(cm, orc, gpu_ready, sched, precision, self_mode):
+    """Both ATOMS evaluation schedules, forced whatever the solute density,
+    give the oracle's counts (triclinic cell, custom groups, a cell size that
+    widens the stencil beyond 27 cells)."""
+    rng = np.random.default_rng(23 + self_mode)
+    if self_mode:
+        xs, xv, cells = make_system(rng, TRICLINIC, 12, 40, 12, 40, 2, True, spread=2.5)
+        dims = dict(ms=12, aps=40, mv=12, apv=40)
+    else:
+        xs, xv, cells = make_system(rng, TRICLINIC, 2, 90, 300, 3, 2, False, spread=3.0)
+        dims = dict(ms=2, aps=90, mv=300, apv=3)
+    opt = dict(irefatom=2, cutoff=6.0, dbulk=6.0, usecutoff=False, n_random_samples=5, **COMMON)
+    for pct in (0, 50):
+        compare(cm, orc, xs=xs, xv=xv, cells=cells, self_mode=self_mode, precision=precision, regime="atoms",
+                groups="custom", cell_scale_pct=pct, atoms_schedule=sched, **dims, **opt)
+
+
 def test_autotune_reports_candidates(cm, gpu_ready):
     rng = np.random.default_rng(22)
     xs, xv, cells = make_system(rng, ORTHO, 200, 5, 200, 5, 3, True)
     t = cm.autotune(xs, None, cells, solute_nmols=200, solute_natomspermol=5, solvent_nmols=200,
                     solvent_natomspermol=5, autocorrelation=True, irefatom=1, cutoff=7.0, binstep=0.02, dbulk=7.0,
                     usecutoff=False, nbins=350, n_random_samples=4)
-    assert t["cell_scale_pct"] in t["candidates"]
-    assert len(t["candidates"]) == 4 and all(v > 0 for v in t["candidates"].values())
-    assert t["candidates"][t["cell_scale_pct"]] == min(t["candidates"].values())
+    ms = {c["cell_scale_pct"]: c["ms_per_frame"] for c in t["candidates"]}
+    assert len(ms) == 4 and all(v > 0 for v in ms.values()) and t["atoms_schedule"] == "auto"
+    assert ms[t["cell_scale_pct"]] == min(ms.values())
+
+
+def test_autotune_atoms_tries_both_schedules(cm, gpu_ready):
+    rng = np.random.default_rng(24)
+    xs, xv, cells = make_system(rng, ORTHO, 1, 120, 400, 3, 2, False, spread=3.0)
+    t = cm.autotune(xs, xv, cells, solute_nmols=1, solute_natomspermol=120, solvent_nmols=400, solvent_natomspermol=3,
+                    autocorrelation=False, irefatom=1, cutoff=7.0, binstep=0.02, dbulk=7.0, usecutoff=False,
+                    nbins=350, n_random_samples=4)
+    assert len(t["candidates"]) == 8
+    assert {c["atoms_schedule"] for c in t["candidates"]} == {"cell", "balanced"}
+    best = min(t["candidates"], key=lambda c: c["ms_per_frame"])
+    assert (best["cell_scale_pct"], best["atoms_schedule"]) == (t["cell_scale_pct"], t["atoms_schedule"])
