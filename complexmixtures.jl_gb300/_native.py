@@ -129,6 +129,19 @@ class cm_raw_counts(C.Structure):
     ]
 
 
+RESULT_VECTORS = ("d", "md_count", "md_count_random", "coordination_number", "coordination_number_random", "mddf", "kb",
+                  "rdf_count", "rdf_count_random", "sum_rdf_count", "sum_rdf_count_random", "rdf", "kb_rdf",
+                  "volume_shell")
+RESULT_GROUPS = ("solute_group_count", "solute_group_count_random", "solvent_group_count", "solvent_group_count_random")
+RESULT_SCALARS = ("volume_total", "volume_bulk", "volume_domain", "density_solute", "density_solvent",
+                  "density_solvent_bulk", "density_fix")
+
+
+class cm_results(C.Structure):
+    _fields_ = ([(k, C.POINTER(C.c_double)) for k in RESULT_VECTORS + RESULT_GROUPS]
+                + [(k, C.c_double) for k in RESULT_SCALARS] + [("zero_random_bins", C.c_int64)])
+
+
 class cm_stats(C.Structure):
     _fields_ = [
         ("frames", C.c_int64),
@@ -206,6 +219,7 @@ EXPORTED = (
     "cm_batch_last_error",
     "cm_read_counts",
     "cm_read_raw_counts",
+    "cm_read_results",
     "cm_get_stats",
     "cm_get_kernel_times",
     "cm_reset",
@@ -271,6 +285,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_status_string.restype = C.c_char_p
     lib.cm_device_bytes.argtypes = [H]
     lib.cm_device_bytes.restype = C.c_int64
+    lib.cm_read_results.argtypes = [H, C.c_double, C.POINTER(cm_results)]
+    lib.cm_read_results.restype = C.c_int
     lib.cm_set_dcd_layout.argtypes = [H, C.POINTER(cm_dcd_layout)]
     lib.cm_set_dcd_layout.restype = C.c_int
     lib.cm_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]

@@ -25,6 +25,7 @@
 #include "cm_kernels.cuh"
 #include "cm_atoms32.cuh"
 #include "cm_flat32.cuh"
+#include "cm_final.cuh"
 
 using namespace cmk;
 using cmgeom::FrameGeom;
@@ -218,6 +219,7 @@ struct cm_handle {
     int dcd_swap = 0;
     std::vector<int32_t> dcd_s, dcd_v;  // host copies of the selections' atom indices
     DevBuf dcd_sidx, dcd_vidx, dcd_raw[2];
+    DevBuf final_out, final_job;  // cm_read_results
 
     // CUDA-graph launch of compute chunks
     bool graphs = false;
@@ -1384,7 +1386,7 @@ void free_all(cm_handle *h) {
                      &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->eq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
                      &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx,
-                     &h->dcd_sidx, &h->dcd_vidx, &h->dcd_raw[0], &h->dcd_raw[1]};
+                     &h->dcd_sidx, &h->dcd_vidx, &h->dcd_raw[0], &h->dcd_raw[1], &h->final_out, &h->final_job};
     for (DevBuf *b : all) {
         blocks().put(h->device, false, b->p, b->bytes);
         b->p = nullptr;
@@ -2059,6 +2061,71 @@ int cm_read_counts(cm_handle *h, cm_counts *out) {
         out->volume_total = h->volume_total;
         out->weight_total = h->weight_total;
         out->frames = h->frames;
+    });
+}
+
+int cm_read_results(cm_handle *h, double frame_weight_sum, cm_results *out) {
+    return guarded(h, [&] {
+        if (!out) throw cm_error(CM_EINVAL, "NULL output");
+        if (!(frame_weight_sum >= 0.0) || !std::isfinite(frame_weight_sum))
+            throw cm_error(CM_EINVAL, "frame_weight_sum must be finite and non-negative");
+        check_device_error(h);
+        const cm_system_desc &d = h->d;
+        const int64_t nb = d.nbins, Gs = h->Gs, Gv = d.autocorrelation ? h->Gs : h->Gv;
+        const int64_t n = FV_NVEC * nb + 2 * Gs * nb + 2 * Gv * nb + FS_NSCALAR;
+        FinalJob J{};
+        J.acc = P<unsigned long long>(h->hist);
+        J.sums = P<double>(h->sums);
+        J.class_w = h->class_w;
+        J.class_open = h->class_open ? 1 : 0;
+        J.nbins = d.nbins;
+        J.Gs = h->Gs;
+        J.Gv = d.autocorrelation ? 0 : h->Gv;
+        J.autocorrelation = d.autocorrelation;
+        J.mddf_mode = h->mddf ? 1 : 0;
+        J.usecutoff = d.usecutoff;
+        J.o_md = h->o_md; J.o_mdr = h->o_mdr; J.o_rdf = h->o_rdf; J.o_rdfr = h->o_rdfr;
+        J.o_gs = h->o_gs; J.o_gsr = h->o_gsr; J.o_gv = h->o_gv; J.o_gvr = h->o_gvr;
+        J.binstep = d.binstep;
+        J.dbulk = d.dbulk;
+        J.Q = frame_weight_sum > 0.0 ? frame_weight_sum : h->weight_total;
+        J.volume_sum = h->volume_total;
+        J.solute_nmols = d.solute_nmols;
+        J.solvent_nmols = d.solvent_nmols;
+        J.solvent_nmols_samples = d.autocorrelation ? d.solvent_nmols - 1 : d.solvent_nmols;  // src/results.jl:230-237
+        J.nrandom = d.n_random_samples;
+        J.units_f = 6.022140857e23 / 1e24;  // units.Angs3tocm3permol = mole / Angs3tocm3 (src/io.jl:6-14)
+        J.ibulk = std::max(1, (int)std::ceil((d.dbulk + 0.5 * d.binstep) / d.binstep));  // setbin (src/results.jl:28)
+        dev_alloc(h, h->final_out, (size_t)n * 8);
+        dev_alloc(h, h->final_job, sizeof(FinalJob));
+        J.out = P<double>(h->final_out);
+        CM_CUDA(cudaMemcpyAsync(h->final_job.p, &J, sizeof(J), cudaMemcpyHostToDevice, h->stream));
+        k_finalize<<<1, 256, 0, h->stream>>>(P<FinalJob>(h->final_job));
+        CM_CUDA(cudaGetLastError());
+        std::vector<double> v(n);
+        CM_CUDA(cudaMemcpyAsync(v.data(), h->final_out.p, (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
+        CM_CUDA(cudaStreamSynchronize(h->stream));
+        auto put = [&](double *dst, int64_t off, int64_t len) {
+            if (dst) memcpy(dst, v.data() + off, len * 8);
+        };
+        double *arr[FV_NVEC] = {out->d, out->md_count, out->md_count_random, out->coordination_number,
+                                out->coordination_number_random, out->mddf, out->kb, out->rdf_count, out->rdf_count_random,
+                                out->sum_rdf_count, out->sum_rdf_count_random, out->rdf, out->kb_rdf, out->volume_shell};
+        for (int k = 0; k < FV_NVEC; ++k) put(arr[k], k * nb, nb);
+        int64_t o = FV_NVEC * nb;
+        put(out->solute_group_count, o, Gs * nb);
+        put(out->solute_group_count_random, o + Gs * nb, Gs * nb);
+        put(out->solvent_group_count, o + 2 * Gs * nb, Gv * nb);
+        put(out->solvent_group_count_random, o + 2 * Gs * nb + Gv * nb, Gv * nb);
+        const double *sc = v.data() + o + 2 * Gs * nb + 2 * Gv * nb;
+        out->volume_total = sc[FS_TOTAL];
+        out->volume_bulk = sc[FS_BULK];
+        out->volume_domain = sc[FS_DOMAIN];
+        out->density_solute = sc[FS_DSOLUTE];
+        out->density_solvent = sc[FS_DSOLVENT];
+        out->density_solvent_bulk = sc[FS_DSOLVENT_BULK];
+        out->density_fix = sc[FS_DENSITY_FIX];
+        out->zero_random_bins = (int64_t)sc[FS_ZERO_RANDOM_BINS];
     });
 }
 

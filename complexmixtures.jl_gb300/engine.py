@@ -331,6 +331,25 @@ class Engine:
         out["frames"] = c.frames
         return out
 
+    def results(self, frame_weight_sum: float = 0.0) -> dict:
+        """Finalised Result fields computed on the device (cm_read_results):
+        the vectors of finalresults! plus volumes, densities, density_fix
+        and the count of random bins without samples."""
+        nb = self.nbins
+        gv = self.ngroups_solute if self.autocorrelation else self.ngroups_solvent
+        out = {k: np.zeros(nb) for k in N.RESULT_VECTORS}
+        out.update({k: np.zeros((self.ngroups_solute if k.startswith("solute") else gv, nb)) for k in N.RESULT_GROUPS})
+        r = N.cm_results()
+        for k in N.RESULT_VECTORS + N.RESULT_GROUPS:
+            setattr(r, k, N.as_ptr(out[k], C.c_double))
+        st = self._lib.cm_read_results(self._h, float(frame_weight_sum), C.byref(r))
+        N.raise_for(st, self._h)
+        self._inflight.clear()
+        for k in N.RESULT_SCALARS:
+            out[k] = getattr(r, k)
+        out["zero_random_bins"] = r.zero_random_bins
+        return out
+
     def raw_counts(self) -> dict:
         """Exact int64 half-unit counts (runs with a single frame weight)."""
         out, c = raw_arrays(self.nbins, self.ngroups_solute, self.ngroups_solvent)

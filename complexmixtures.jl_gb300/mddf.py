@@ -14,7 +14,7 @@ import numpy as np
 
 from .engine import Engine
 from .options import Options, TrajectoryFileOptions
-from .results import Result, check_frame_weights, finalresults, isautocorrelation, setbin
+from .results import Result, check_frame_weights, finalresults, isautocorrelation, setbin, sum_frame_weights
 from .trajectory import ArrayTrajectory, NamdDCD, Trajectory, cell_matrix, make_trajectory, trajectory_metadata
 
 STOP_FILE = "stop_complexmixtures"
@@ -81,7 +81,8 @@ def new_result(trajectory: Trajectory, options: Options, tmeta, frame_weights) -
 
 def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = None, *, frame_weights=None,
          coordination_number_only: bool = False, low_memory: bool = False, trajectory_format: str = "",
-         precision: str = "fp32", regime: str = "auto", device: int = 0, batch_frames: int = 64) -> Result:
+         precision: str = "fp32", regime: str = "auto", device: int = 0, batch_frames: int = 64,
+         finalize: str = "host") -> Result:
     """Minimum-distance distribution function (src/mddf.jl:113-347).
 
     ``mddf(trajectory, options)`` with a Trajectory object, or
@@ -89,8 +90,13 @@ def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = Non
     options)`` (self-MDDF) with a file name.  ``low_memory`` is accepted for
     signature compatibility; the GPU engine has a single memory layout.
     ``precision`` selects the FP32+guard ("fp32") or plain FP64 ("fp64") path;
-    both give identical counts.
+    both give identical counts.  ``finalize="device"`` computes the
+    normalisation, densities, MDDF, RDF and KB integrals on the GPU
+    (cm_read_results) instead of the host restatement of finalresults!; both
+    agree to 1e-12.
     """
+    if finalize not in ("host", "device"):
+        raise ValueError("finalize must be 'host' or 'device'")
     if isinstance(trajectory, str):
         if isinstance(solvent, Options) and options is None:
             options, solvent = solvent, None
@@ -107,14 +113,44 @@ def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = Non
                      precision=precision, regime=regime, device=device, max_frames_per_batch=batch_frames)
     try:
         _run_frames(eng, trajectory, to_compute, fw, batch_frames)
-        c = eng.counts()
+        if finalize == "device":
+            res = eng.results(sum_frame_weights(R))
+        else:
+            c = eng.counts()
     finally:
         eng.close()
+    if finalize == "device":
+        return _device_result(R, res, options, coordination_number_only)
     for k in ("md_count", "md_count_random", "rdf_count", "rdf_count_random", "solute_group_count",
               "solute_group_count_random", "solvent_group_count", "solvent_group_count_random"):
         setattr(R, k, c[k].copy())
     R.volume.total = c["volume_total"]
     return finalresults(R, options, coordination_number_only=coordination_number_only)
+
+
+def _device_result(R: Result, res: dict, options: Options, coordination_number_only: bool) -> Result:
+    """A Result filled from cm_read_results, with the reference's warnings."""
+    import warnings
+
+    if coordination_number_only and not options.silent:
+        warnings.warn("coordination_number_only was set to true, so the MDDF and KB integrals were not computed. "
+                      "(to remove this warning use Options(silent=true))")
+    if not coordination_number_only and res["zero_random_bins"] > 0 and not options.silent:
+        warnings.warn("Ideal-gas histogram bins with zero samples. Increase n_random_samples, number of trajectory "
+                      "frames, and/or bin size.")
+    for k in ("d", "md_count", "md_count_random", "coordination_number", "coordination_number_random", "mddf", "kb",
+              "rdf_count", "rdf_count_random", "sum_rdf_count", "sum_rdf_count_random", "rdf", "kb_rdf",
+              "solute_group_count", "solute_group_count_random", "solvent_group_count", "solvent_group_count_random"):
+        setattr(R, k, res[k])
+    R.volume.total = res["volume_total"]
+    R.volume.shell = res["volume_shell"]
+    if not coordination_number_only:
+        R.volume.bulk = res["volume_bulk"]
+        R.volume.domain = res["volume_domain"]
+        R.density.solvent_bulk = res["density_solvent_bulk"]
+    R.density.solute = res["density_solute"]
+    R.density.solvent = res["density_solvent"]
+    return R
 
 
 def _run_frames(eng: Engine, trajectory: Trajectory, to_compute, fw, batch_frames: int) -> None:

@@ -264,6 +264,28 @@ const char *cm_batch_last_error(const cm_batch *b);
 /* Synchronise and copy the weighted accumulators out. */
 int cm_read_counts(cm_handle *h, cm_counts *out);
 
+/*
+ * Finalised results (finalresults!, src/results.jl:311-469) computed on the
+ * device in FP64 from the handle's accumulators: the normalisation by frames
+ * and molecules, the shell and bulk volumes, the bulk density and its
+ * correction of the random counts, coordination numbers, MDDF, RDF and KB
+ * integrals, in the reference's order of operations.  frame_weight_sum is
+ * sum_frame_weights of the Result (0: the sum of the weights submitted).
+ * Caller-owned host arrays; NULL pointers are skipped.  In self mode the
+ * solvent group arrays receive the solute's (src/results.jl:335-337).
+ */
+typedef struct cm_results {
+    double *d, *md_count, *md_count_random, *coordination_number, *coordination_number_random, *mddf, *kb;  /* [nbins] */
+    double *rdf_count, *rdf_count_random, *sum_rdf_count, *sum_rdf_count_random, *rdf, *kb_rdf;         /* [nbins] */
+    double *volume_shell;                                                                                /* [nbins] */
+    double *solute_group_count, *solute_group_count_random;      /* [solute groups][nbins] */
+    double *solvent_group_count, *solvent_group_count_random;    /* [solvent groups][nbins] */
+    double volume_total, volume_bulk, volume_domain;
+    double density_solute, density_solvent, density_solvent_bulk, density_fix;
+    int64_t zero_random_bins;         /* bins with no random-insertion count (the reference warns about them) */
+} cm_results;
+int cm_read_results(cm_handle *h, double frame_weight_sum, cm_results *out);
+
 /* Synchronise and copy the exact half-unit counts (single-weight runs only). */
 int cm_read_raw_counts(cm_handle *h, cm_raw_counts *out);
 
