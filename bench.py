@@ -19,7 +19,9 @@ frames through the engine.
               all host threads) on a bounded sample of the frames
 
 --workload c1 | c2-water | c2-cosolvent | c4 prints the frames/s of that
-configuration's system (ATOMS layout) instead of the headline line.
+configuration's system (ATOMS layout) instead of the headline line;
+--workload grid3d times grid3D's grid search on a 1,463-atom protein (the
+NAMD test fixture) against the CPU restatement on a sample of the points.
 
 --impl reference times that CPU path alone (the reference itself is Julia
 and cannot run here).  Multi-GPU runs are independent replicas (the path
@@ -68,7 +70,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-serving", action="store_true")
-    p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4"],
+    p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4", "grid3d"],
                    help="c3 (default): the headline line; the others: frames/s of that configuration's system "
                         "(ATOMS layout) on device-resident frames")
     return p.parse_args()
@@ -467,11 +469,54 @@ def other_workload(args, local):
     }), flush=True)
 
 
+def grid3d_workload(args, local):
+    """grid3D's grid search (cm_grid3d) around the 1,463-atom protein of the
+    NAMD test fixture, dmin 1.5, dmax 5, step 0.5 (about 10^6 points), from
+    the MDDF of the protein against TMAO; the CPU restatement (numpy, one
+    thread) is timed on a sample of the points and scaled per point."""
+    import __graft_entry__ as entry
+
+    cm = entry.load_package()
+    g = np.load(os.path.join(ROOT, "tests", "golden", "namd_frames.npz"))
+    cells = np.array([np.diag([c[0], c[2], c[5]]) for c in g["cells"]])
+    protein = cm.AtomSelection.from_indices(list(range(1, 1464)), nmols=1)
+    tmao = cm.AtomSelection.from_indices(list(range(1479, 4013)), natomspermol=14)
+    tr = cm.ArrayTrajectory(protein, tmao, solute_frames=g["protein"].astype(np.float64),
+                            solvent_frames=g["tmao"].astype(np.float64), cells=cells)
+    R = cm.mddf(tr, cm.make_options(dbulk=10.0, n_random_samples=20, seed=4, silent=True), device=local)
+    atoms = cm.Atoms(g["protein"][0].astype(np.float64))
+    for _ in range(max(args.warmup, 1)):
+        G = cm.grid3D(R, atoms, device=local)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        G = cm.grid3D(R, atoms, device=local)
+    dt = (time.perf_counter() - t) / args.steps
+    npts = int(np.prod(G.n))
+    orc = entry.load_oracle()
+    idx = np.asarray(R.solute.indices)
+    table = cm.grid3d.atom_contribution_table(R, "mddf")
+    t = time.perf_counter()
+    sample = orc.grid3d(atoms.xyz[idx - 1], (idx - idx[0]) % R.solute.natomspermol, table, R.d, dmin=1.5, dmax=5.0,
+                        step=0.5, limit=20000)
+    dc = time.perf_counter() - t
+    print(json.dumps({
+        "workload": "grid3d", "metric": "grid points/s", "value": npts / dt, "unit": "points/s",
+        "points": npts, "kept": len(G), "ms_per_grid": dt * 1e3, "steps": args.steps,
+        "api": "grid3D (cm_grid3d, host cell list and copies included)",
+        "cpu_baseline": {"value": sample["evaluated"] / dc, "unit": "points/s", "cores": 1, "kind": "port",
+                         "sample": f"first {sample['evaluated']} grid points (oracle/oracle.py grid3d, numpy)"},
+    }), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "grid3d":
+        if rank == 0:
+            grid3d_workload(args, local)
         return
     if args.workload != "c3":
         if rank == 0:

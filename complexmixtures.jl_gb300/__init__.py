@@ -16,6 +16,7 @@ from .trajectory import (ArrayTrajectory, NamdDCD, PDBTraj, Trajectory, Trajecto
                          make_trajectory, trajectory_metadata, unitcell_from_lengths_angles)
 from .contributions import contributions
 from .engine import Batch, Engine, autotune, memory_cache
+from .grid3d import Atoms, Grid3D, grid3D, read_pdb_atoms
 from .server import Server, latency_percentiles
 from .mddf import coordination_number, engine_for, mddf, new_result
 from ._native import NativeUnavailable
@@ -26,5 +27,5 @@ __all__ = [
     "Volume", "finalresults", "renormalize", "result_from_json", "setbin", "shellradius", "sphericalshellvolume",
     "sum_results", "units", "save", "load", "merge", "ArrayTrajectory", "NamdDCD", "PDBTraj", "Trajectory", "TrajectoryMetaData",
     "convert_unitcell", "make_trajectory", "trajectory_metadata", "unitcell_from_lengths_angles", "contributions",
-    "Batch", "Engine", "autotune", "memory_cache", "Server", "latency_percentiles", "coordination_number", "engine_for", "mddf", "new_result", "NativeUnavailable",
+    "Atoms", "Grid3D", "grid3D", "read_pdb_atoms", "Batch", "Engine", "autotune", "memory_cache", "Server", "latency_percentiles", "coordination_number", "engine_for", "mddf", "new_result", "NativeUnavailable",
 ]

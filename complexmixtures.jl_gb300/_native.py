@@ -142,6 +142,23 @@ class cm_results(C.Structure):
                 + [(k, C.c_double) for k in RESULT_SCALARS] + [("zero_random_bins", C.c_int64)])
 
 
+class cm_grid3d_desc(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32), ("nbins", C.c_int32), ("natoms", C.c_int64), ("xyz", C.POINTER(C.c_double)),
+        ("atom_type", C.POINTER(C.c_int32)), ("ntypes", C.c_int32), ("reserved", C.c_int32),
+        ("table", C.POINTER(C.c_double)), ("d", C.POINTER(C.c_double)), ("dmin", C.c_double), ("dmax", C.c_double),
+        ("step", C.c_double),
+    ]
+
+
+class cm_grid3d_out(C.Structure):
+    _fields_ = [
+        ("capacity", C.c_int64), ("count", C.c_int64), ("n", C.c_int64 * 3), ("origin", C.c_double * 3),
+        ("point", C.POINTER(C.c_int64)), ("atom", C.POINTER(C.c_int32)), ("distance", C.POINTER(C.c_double)),
+        ("value", C.POINTER(C.c_double)),
+    ]
+
+
 class cm_stats(C.Structure):
     _fields_ = [
         ("frames", C.c_int64),
@@ -228,6 +245,7 @@ EXPORTED = (
     "cm_status_string",
     "cm_device_bytes",
     "cm_memory_cache",
+    "cm_grid3d",
     "cm_stream",
     "cm_measure_fp32_peak",
     "cm_frame_counts_noalloc",
@@ -299,6 +317,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_batch_destroy.restype = C.c_int
     lib.cm_batch_last_error.argtypes = [C.c_void_p]
     lib.cm_batch_last_error.restype = C.c_char_p
+    lib.cm_grid3d.argtypes = [C.POINTER(cm_grid3d_desc), C.POINTER(cm_grid3d_out)]
+    lib.cm_grid3d.restype = C.c_int
     lib.cm_memory_cache.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.cm_memory_cache.restype = C.c_int
     lib.cm_stream.argtypes = [H]

@@ -26,6 +26,7 @@
 #include "cm_atoms32.cuh"
 #include "cm_flat32.cuh"
 #include "cm_final.cuh"
+#include "cm_grid3d.cuh"
 
 using namespace cmk;
 using cmgeom::FrameGeom;
@@ -2248,6 +2249,141 @@ const char *cm_status_string(int status) {
 }
 
 int64_t cm_device_bytes(const cm_handle *h) { return h ? h->device_bytes : 0; }
+
+int cm_grid3d(const cm_grid3d_desc *D, cm_grid3d_out *out) {
+    if (!D || !out) {
+        g_create_error = "NULL argument";
+        return CM_EINVAL;
+    }
+    std::vector<std::pair<void *, size_t>> taken;  // device blocks from the cache, returned at the end
+    cudaStream_t st = nullptr;
+    int prev = -1;
+    auto release = [&] {
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+        for (auto &b : taken) blocks().put(D->device, false, b.first, b.second);
+        if (prev >= 0) cudaSetDevice(prev);
+    };
+    try {
+        if (D->natoms < 1 || D->natoms >= (1LL << 31) || !D->xyz || !D->atom_type || !D->table || !D->d)
+            throw cm_error(CM_EINVAL, "natoms, xyz, atom_type, table and d are required");
+        if (D->nbins < 2 || D->ntypes < 1) throw cm_error(CM_EINVAL, "nbins must be >= 2 and ntypes >= 1");
+        if (!(D->step > 0.0) || !(D->dmax > D->dmin) || !(D->dmin >= 0.0))
+            throw cm_error(CM_EINVAL, "need step > 0 and 0 <= dmin < dmax");
+        if (!(D->d[0] <= D->dmin) || !(D->dmax < D->d[D->nbins - 1]))
+            throw cm_error(CM_EINVAL, "dmin and dmax must lie within the bin distances (d[0] <= dmin, dmax < d[end])");
+        for (int64_t i = 0; i < D->natoms; ++i)
+            if (D->atom_type[i] < 0 || D->atom_type[i] >= D->ntypes) throw cm_error(CM_EINVAL, "atom_type out of range");
+        // grid (PDBTools.maxmin and the point count of src/tools/grid3D.jl:76-77)
+        double xmin[3], xmax[3];
+        for (int k = 0; k < 3; ++k) xmin[k] = xmax[k] = D->xyz[k];
+        for (int64_t i = 1; i < D->natoms; ++i)
+            for (int k = 0; k < 3; ++k) {
+                xmin[k] = std::min(xmin[k], D->xyz[3 * i + k]);
+                xmax[k] = std::max(xmax[k], D->xyz[3 * i + k]);
+            }
+        GridJob J{};
+        for (int k = 0; k < 3; ++k) {
+            J.n[k] = (int64_t)std::ceil((xmax[k] - xmin[k] + 2 * D->dmax) / D->step + 1);
+            J.origin[k] = xmin[k] - D->dmax;
+            out->n[k] = J.n[k];
+            out->origin[k] = J.origin[k];
+        }
+        J.step = D->step;
+        J.dmin = D->dmin;
+        J.dmax = D->dmax;
+        J.nbins = D->nbins;
+        // atoms binned into cells a little wider than dmax
+        J.cell = D->dmax * 1.001;
+        for (int k = 0; k < 3; ++k) J.c[k] = (int64_t)std::floor((xmax[k] - J.origin[k]) / J.cell) + 2;
+        const int64_t ncell = J.c[0] * J.c[1] * J.c[2];
+        if (ncell > (1LL << 28)) throw cm_error(CM_EINVAL, "grid box too large for its cell list");
+        std::vector<int64_t> acell(D->natoms);
+        std::vector<int> cstart(ncell + 1, 0);
+        for (int64_t i = 0; i < D->natoms; ++i) {
+            int64_t ci[3];
+            for (int k = 0; k < 3; ++k)
+                ci[k] = std::min<int64_t>(J.c[k] - 1, std::max<int64_t>(0, (int64_t)std::floor((D->xyz[3 * i + k] - J.origin[k]) / J.cell)));
+            acell[i] = (ci[2] * J.c[1] + ci[1]) * J.c[0] + ci[0];
+            cstart[acell[i] + 1]++;
+        }
+        for (int64_t c = 0; c < ncell; ++c) cstart[c + 1] += cstart[c];
+        std::vector<int> fill(cstart.begin(), cstart.end() - 1);
+        std::vector<d4> sorted(D->natoms);
+        for (int64_t i = 0; i < D->natoms; ++i)
+            sorted[fill[acell[i]]++] = cmgeom::make_d4(D->xyz[3 * i], D->xyz[3 * i + 1], D->xyz[3 * i + 2], (double)i);
+        const int64_t total = J.n[0] * J.n[1] * J.n[2];
+        CM_CUDA(cudaGetDevice(&prev));
+        CM_CUDA(cudaSetDevice(D->device));
+        CM_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        auto take = [&](size_t bytes) {
+            size_t got = 0;
+            void *p = blocks().get(D->device, false, bytes, &got);
+            if (!p) throw cm_error(CM_ENOMEM, "out of device memory");
+            taken.push_back({p, got});
+            return p;
+        };
+        auto up = [&](const void *src, size_t bytes) {
+            void *p = take(bytes);
+            CM_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, st));
+            return p;
+        };
+        J.cstart = (const int *)up(cstart.data(), cstart.size() * 4);
+        J.atoms = (const d4 *)up(sorted.data(), sorted.size() * sizeof(d4));
+        J.type = (const int *)up(D->atom_type, (size_t)D->natoms * 4);
+        J.table = (const double *)up(D->table, (size_t)D->ntypes * D->nbins * 8);
+        J.d = (const double *)up(D->d, (size_t)D->nbins * 8);
+        J.cap = total;
+        J.count = (unsigned long long *)take(8);
+        CM_CUDA(cudaMemsetAsync(J.count, 0, 8, st));
+        J.out_point = (long long *)take((size_t)total * 8);
+        J.out_atom = (int *)take((size_t)total * 4);
+        J.out_r = (double *)take((size_t)total * 8);
+        J.out_v = (double *)take((size_t)total * 8);
+        int sms = 0;
+        CM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device));
+        const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16);
+        k_grid3d<<<grid, 256, 0, st>>>(J);
+        CM_CUDA(cudaGetLastError());
+        unsigned long long cnt = 0;
+        CM_CUDA(cudaMemcpyAsync(&cnt, J.count, 8, cudaMemcpyDeviceToHost, st));
+        CM_CUDA(cudaStreamSynchronize(st));
+        out->count = (int64_t)cnt;
+        if ((int64_t)cnt > out->capacity) throw cm_error(CM_ENOMEM, "cm_grid3d_out.capacity below the kept points (see count)");
+        std::vector<long long> pt(cnt);
+        std::vector<int> at(cnt);
+        std::vector<double> rr(cnt), vv(cnt);
+        if (cnt) {
+            CM_CUDA(cudaMemcpyAsync(pt.data(), J.out_point, cnt * 8, cudaMemcpyDeviceToHost, st));
+            CM_CUDA(cudaMemcpyAsync(at.data(), J.out_atom, cnt * 4, cudaMemcpyDeviceToHost, st));
+            CM_CUDA(cudaMemcpyAsync(rr.data(), J.out_r, cnt * 8, cudaMemcpyDeviceToHost, st));
+            CM_CUDA(cudaMemcpyAsync(vv.data(), J.out_v, cnt * 8, cudaMemcpyDeviceToHost, st));
+            CM_CUDA(cudaStreamSynchronize(st));
+        }
+        std::vector<int64_t> order(cnt);
+        for (int64_t i = 0; i < (int64_t)cnt; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return pt[a] < pt[b]; });
+        for (int64_t i = 0; i < (int64_t)cnt; ++i) {
+            const int64_t j = order[i];
+            if (out->point) out->point[i] = pt[j];
+            if (out->atom) out->atom[i] = at[j];
+            if (out->distance) out->distance[i] = rr[j];
+            if (out->value) out->value[i] = vv[j];
+        }
+        release();
+        return CM_OK;
+    } catch (const cm_error &e) {
+        g_create_error = e.msg;
+        release();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_create_error = "host allocation failed";
+        release();
+        return CM_ENOMEM;
+    }
+}
 
 int cm_memory_cache(int32_t device, int32_t release, int64_t *cached_device_bytes, int64_t *cached_host_bytes) {
     if (device < 0 || device >= BlockCache::kMaxDevices) {

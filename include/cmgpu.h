@@ -316,6 +316,43 @@ int cm_measure_fp32_peak(int32_t device, double ms_target, double *tflops);
 /* Device memory the handle holds, in bytes. */
 int64_t cm_device_bytes(const cm_handle *h);
 
+/*
+ * grid3D (src/tools/grid3D.jl:47-147) on the device.  For every point of the
+ * grid spanning the solute's bounding box widened by dmax (n = ceil((length +
+ * 2 dmax) / step + 1) points per axis, point (ix, iy, iz) at xmin - dmax +
+ * step * ix, 0-based), the closest solute atom (Euclidean, no periodic images,
+ * ties to the lower index) is found; the point is kept when dmin < r < dmax
+ * and the atom's contribution curve, linearly interpolated at r over the bin
+ * distances d, is positive.  Kept points come back in ascending point order.
+ * The reference's ArgumentErrors (custom groups) and the beta scaling and PDB
+ * output are host-side.
+ */
+typedef struct cm_grid3d_desc {
+    int32_t device;
+    int32_t nbins;
+    int64_t natoms;                   /* solute atoms */
+    const double *xyz;                /* host [natoms][3] */
+    const int32_t *atom_type;         /* host [natoms]: row of `table` (the atom's position in its molecule) */
+    int32_t ntypes;
+    int32_t reserved;
+    const double *table;              /* host [ntypes][nbins]: contribution curve of each atom type */
+    const double *d;                  /* host [nbins]: bin distances (Result.d), increasing; d[0] <= dmin, dmax < d[nbins-1] */
+    double dmin, dmax, step;
+} cm_grid3d_desc;
+
+typedef struct cm_grid3d_out {
+    int64_t capacity;                 /* entries the arrays below hold */
+    int64_t count;                    /* kept points (when above capacity: CM_ENOMEM, arrays untouched) */
+    int64_t n[3];                     /* grid points per axis */
+    double origin[3];                 /* position of point (0, 0, 0) */
+    int64_t *point;                   /* [capacity] (ix * n[1] + iy) * n[2] + iz, ascending */
+    int32_t *atom;                    /* [capacity] 0-based solute atom closest to the point */
+    double *distance;                 /* [capacity] */
+    double *value;                    /* [capacity] interpolated contribution */
+} cm_grid3d_out;
+
+int cm_grid3d(const cm_grid3d_desc *desc, cm_grid3d_out *out);
+
 /* Process-wide block cache (no counterpart in the reference, whose arrays
  * are garbage-collected Julia memory).  A destroyed handle returns its device
  * and pinned host blocks to a per-device cache that later handles draw from,

@@ -7,6 +7,7 @@ thing measured for the GPU engine or shipped with it.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -178,3 +179,54 @@ def move(x, newcm, A):
     lib().orc_move(_dp(x), len(x), _dp(np.ascontiguousarray(newcm, dtype=np.float64)),
                    _dp(np.ascontiguousarray(A, dtype=np.float64).reshape(9)))
     return x
+
+
+# ----------------------------------------------------------------- grid3D
+def grid3d(solute_xyz, atom_type, table, d, *, dmin, dmax, step, chunk=2048, limit=None):
+    """CPU restatement of grid3D's grid loop (src/tools/grid3D.jl:71-137),
+    the checker of the engine's cm_grid3d.
+
+    The grid spans the solute's bounding box (PDBTools.maxmin) widened by
+    dmax, n = ceil((length + 2 dmax) / step + 1) points per axis, point
+    (ix, iy, iz) at xmin - dmax + step (ix - 1), ...  Each point's closest
+    solute atom (PDBTools.closest: Euclidean, no periodic images, the first
+    atom at the minimum distance) is kept when dmin < r < dmax and the atom's
+    contribution curve (``table[atom_type]`` over the bin distances ``d``),
+    linearly interpolated at r, is positive.  Returns the kept points in loop
+    order (ix outermost): linear index, 0-based solute atom, r and the value,
+    plus n and the grid origin (``limit`` stops after that many points).
+    """
+    x = np.asarray(solute_xyz, dtype=np.float64)
+    xmin = x.min(axis=0)
+    xlen = x.max(axis=0) - xmin
+    n = [int(math.ceil((xlen[k] + 2 * dmax) / step + 1)) for k in range(3)]
+    origin = xmin - dmax
+    table = np.asarray(table, dtype=np.float64)
+    d = np.asarray(d, dtype=np.float64)
+    atom_type = np.asarray(atom_type, dtype=np.int64)
+    total = n[0] * n[1] * n[2] if limit is None else min(limit, n[0] * n[1] * n[2])
+    pts, atoms, rs, vals = [], [], [], []
+    for g0 in range(0, total, chunk):
+        g = np.arange(g0, min(total, g0 + chunk), dtype=np.int64)
+        ix, rem = np.divmod(g, n[1] * n[2])
+        iy, iz = np.divmod(rem, n[2])
+        p = np.stack([origin[k] + step * idx.astype(np.float64) for k, idx in enumerate((ix, iy, iz))], axis=1)
+        dx = p[:, None, 0] - x[None, :, 0]
+        dy = p[:, None, 1] - x[None, :, 1]
+        dz = p[:, None, 2] - x[None, :, 2]
+        d2 = (dx * dx + dy * dy) + dz * dz
+        iat = np.argmin(d2, axis=1)              # first atom at the minimum
+        r = np.sqrt(d2[np.arange(len(g)), iat])
+        keep = (dmin < r) & (r < dmax)
+        for j in np.nonzero(keep)[0]:
+            c = table[atom_type[iat[j]]]
+            iright = int(np.searchsorted(d, r[j], side="right"))   # first d > r
+            ileft = iright - 1
+            cr = c[ileft] + (c[iright] - c[ileft]) / (d[iright] - d[ileft]) * (r[j] - d[ileft])
+            if cr > 0:
+                pts.append(int(g[j]))
+                atoms.append(int(iat[j]))
+                rs.append(float(r[j]))
+                vals.append(float(cr))
+    return {"point": np.array(pts, dtype=np.int64), "atom": np.array(atoms, dtype=np.int32),
+            "distance": np.array(rs), "value": np.array(vals), "n": n, "origin": origin, "evaluated": total}

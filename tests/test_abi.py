@@ -41,7 +41,7 @@ def test_struct_sizes_match_header(cm):
 
 
 STRUCTS = ("cm_system_desc", "cm_frames", "cm_counts", "cm_raw_counts", "cm_stats", "cm_kernel_times", "cm_tuning",
-           "cm_dcd_layout", "cm_results", "cm_server_desc", "cm_request_info")
+           "cm_dcd_layout", "cm_results", "cm_grid3d_desc", "cm_grid3d_out", "cm_server_desc", "cm_request_info")
 
 
 def test_struct_layouts_match_c_compiler(cm, tmp_path):
