@@ -14,7 +14,7 @@ from .results import (Density, Result, Volume, finalresults, load, merge, renorm
                       shellradius, sphericalshellvolume, sum_results, units)
 from .trajectory import (ArrayTrajectory, NamdDCD, PDBTraj, Trajectory, TrajectoryMetaData, convert_unitcell,
                          make_trajectory, trajectory_metadata, unitcell_from_lengths_angles)
-from .contributions import contributions
+from .contributions import ResidueContributions, contribution_terms, contributions
 from .engine import Batch, Engine, autotune, memory_cache
 from .grid3d import Atoms, Grid3D, grid3D, read_pdb_atoms
 from .server import Server, latency_percentiles
@@ -26,6 +26,6 @@ __all__ = [
     "atom_group", "atom_group_name", "atom_group_names", "set_nmols_natomspermol", "Density", "Result",
     "Volume", "finalresults", "renormalize", "result_from_json", "setbin", "shellradius", "sphericalshellvolume",
     "sum_results", "units", "save", "load", "merge", "ArrayTrajectory", "NamdDCD", "PDBTraj", "Trajectory", "TrajectoryMetaData",
-    "convert_unitcell", "make_trajectory", "trajectory_metadata", "unitcell_from_lengths_angles", "contributions",
+    "convert_unitcell", "make_trajectory", "trajectory_metadata", "unitcell_from_lengths_angles", "contributions", "contribution_terms", "ResidueContributions",
     "Atoms", "Grid3D", "grid3D", "read_pdb_atoms", "Batch", "Engine", "autotune", "memory_cache", "Server", "latency_percentiles", "coordination_number", "engine_for", "mddf", "new_result", "NativeUnavailable",
 ]

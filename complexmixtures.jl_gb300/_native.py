@@ -142,6 +142,15 @@ class cm_results(C.Structure):
                 + [(k, C.c_double) for k in RESULT_SCALARS] + [("zero_random_bins", C.c_int64)])
 
 
+class cm_contrib_query(C.Structure):
+    _fields_ = [("side", C.c_int32), ("type", C.c_int32), ("divide", C.c_int32), ("nterms", C.c_int32),
+                ("groups", C.POINTER(C.c_int32))]
+
+
+CM_GROUP_SOLUTE, CM_GROUP_SOLVENT = 0, 1
+CM_CONTRIB_TYPES = {"mddf": 0, "coordination_number": 1, "md_count": 2, "kbi": 3}
+
+
 class cm_grid3d_desc(C.Structure):
     _fields_ = [
         ("device", C.c_int32), ("nbins", C.c_int32), ("natoms", C.c_int64), ("xyz", C.POINTER(C.c_double)),
@@ -237,6 +246,7 @@ EXPORTED = (
     "cm_read_counts",
     "cm_read_raw_counts",
     "cm_read_results",
+    "cm_contributions",
     "cm_get_stats",
     "cm_get_kernel_times",
     "cm_reset",
@@ -305,6 +315,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_device_bytes.restype = C.c_int64
     lib.cm_read_results.argtypes = [H, C.c_double, C.POINTER(cm_results)]
     lib.cm_read_results.restype = C.c_int
+    lib.cm_contributions.argtypes = [H, C.c_double, C.c_int32, C.POINTER(cm_contrib_query), C.POINTER(C.c_double)]
+    lib.cm_contributions.restype = C.c_int
     lib.cm_set_dcd_layout.argtypes = [H, C.POINTER(cm_dcd_layout)]
     lib.cm_set_dcd_layout.restype = C.c_int
     lib.cm_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]

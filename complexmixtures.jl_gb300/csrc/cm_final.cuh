@@ -174,4 +174,75 @@ __global__ void k_finalize(const FinalJob *__restrict__ jobs) {
     if (threadIdx.x == 0) sc[FS_ZERO_RANDOM_BINS] = (double)s_zero;
 }
 
+// Contribution queries (contributions, src/tools/contributions.jl:70-248) on
+// the packed output of k_finalize.  A query sums group-count rows of one side
+// in the order of its terms (sel_count .+= group_count[g], or
+// group_count[g] / nmols when the query names atoms of a multi-molecule
+// selection), then converts the sum as the reference does for its type.
+// ResidueContributions (src/tools/residue_contributions.jl:157-215) is one
+// query per residue, so a whole protein is one launch.
+enum ContribType { CT_MDDF = 0, CT_COORDINATION_NUMBER = 1, CT_MD_COUNT = 2, CT_KBI = 3 };
+
+struct ContribQuery {
+    int side;      // 0: solute groups, 1: solvent groups
+    int type;      // ContribType
+    int divide;    // terms are group_count[g] / nmols
+    int t0, t1;    // terms [t0, t1) of the group list
+    double nmols;  // molecules of the side's selection
+};
+
+struct ContribJob {
+    const double *fin;    // k_finalize output of the handle
+    int nbins, Gs, Gv;    // Gv = Gs in self mode (the solvent rows are the solute's)
+    double units_f;       // units.Angs3tocm3permol (src/io.jl:6-14)
+    const ContribQuery *q;
+    const int *groups;
+    double *out;          // [queries][nbins]
+    double *scratch;      // [queries][nbins]: the random-count sums of KBI queries
+};
+
+__global__ void k_contrib(ContribJob J) {
+    const ContribQuery Q = J.q[blockIdx.x];
+    const int nb = J.nbins;
+    const double *fin = J.fin;
+    const double *mdr = fin + (int64_t)FV_MDR * nb;
+    const double *gs = fin + (int64_t)FV_NVEC * nb;
+    const double *gsr = gs + (int64_t)J.Gs * nb;
+    const double *gv = gsr + (int64_t)J.Gs * nb;
+    const double *gvr = gv + (int64_t)J.Gv * nb;
+    const double *sc = gvr + (int64_t)J.Gv * nb;
+    const double *gc = Q.side ? gv : gs, *gcr = Q.side ? gvr : gsr;
+    double *out = J.out + (int64_t)blockIdx.x * nb;
+    double *selr_out = J.scratch + (int64_t)blockIdx.x * nb;
+    const bool kbi = Q.type == CT_KBI;
+    // sel_count and sel_count_random, bin by bin, terms in order
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        double sel = 0.0, selr = 0.0;
+        for (int t = Q.t0; t < Q.t1; ++t) {
+            const int64_t row = (int64_t)J.groups[t] * nb + i;
+            const double x = Q.divide ? div(gc[row], Q.nmols) : gc[row];
+            sel = add(sel, x);
+            if (kbi) selr = add(selr, Q.divide ? div(gcr[row], Q.nmols) : gcr[row]);
+        }
+        if (Q.type == CT_MDDF) sel = mdr[i] == 0.0 ? 0.0 : div(sel, mdr[i]);
+        out[i] = sel;
+        if (kbi) selr_out[i] = selr;
+    }
+    if (Q.type != CT_COORDINATION_NUMBER && !kbi) return;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    // cumulative sums in index order (cumsum), then the KBI expression
+    double c = 0.0, cr = 0.0;
+    const double fi = kbi ? mul(J.units_f, div(1.0, sc[FS_DSOLVENT_BULK])) : 0.0;
+    for (int i = 0; i < nb; ++i) {
+        c = i == 0 ? out[i] : add(c, out[i]);
+        if (kbi) {
+            cr = i == 0 ? selr_out[i] : add(cr, selr_out[i]);
+            out[i] = mul(fi, sub(c, cr));
+        } else {
+            out[i] = c;
+        }
+    }
+}
+
 }  // namespace cmk

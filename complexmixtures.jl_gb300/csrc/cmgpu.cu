@@ -221,6 +221,7 @@ struct cm_handle {
     std::vector<int32_t> dcd_s, dcd_v;  // host copies of the selections' atom indices
     DevBuf dcd_sidx, dcd_vidx, dcd_raw[2];
     DevBuf final_out, final_job;  // cm_read_results
+    DevBuf contrib_q, contrib_g, contrib_out;  // cm_contributions
 
     // CUDA-graph launch of compute chunks
     bool graphs = false;
@@ -1387,7 +1388,8 @@ void free_all(cm_handle *h) {
                      &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->eq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
                      &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx,
-                     &h->dcd_sidx, &h->dcd_vidx, &h->dcd_raw[0], &h->dcd_raw[1], &h->final_out, &h->final_job};
+                     &h->dcd_sidx, &h->dcd_vidx, &h->dcd_raw[0], &h->dcd_raw[1], &h->final_out, &h->final_job,
+                     &h->contrib_q, &h->contrib_g, &h->contrib_out};
     for (DevBuf *b : all) {
         blocks().put(h->device, false, b->p, b->bytes);
         b->p = nullptr;
@@ -2065,44 +2067,53 @@ int cm_read_counts(cm_handle *h, cm_counts *out) {
     });
 }
 
+// Launch k_finalize on the handle's accumulators into h->final_out (packed
+// FinalVec vectors, group blocks, FinalScalar scalars); returns its length in
+// doubles.  Asynchronous on the handle's stream.
+static int64_t launch_finalize(cm_handle *h, double frame_weight_sum) {
+    if (!(frame_weight_sum >= 0.0) || !std::isfinite(frame_weight_sum))
+        throw cm_error(CM_EINVAL, "frame_weight_sum must be finite and non-negative");
+    check_device_error(h);
+    const cm_system_desc &d = h->d;
+    const int64_t nb = d.nbins, Gs = h->Gs, Gv = d.autocorrelation ? h->Gs : h->Gv;
+    const int64_t n = FV_NVEC * nb + 2 * Gs * nb + 2 * Gv * nb + FS_NSCALAR;
+    FinalJob J{};
+    J.acc = P<unsigned long long>(h->hist);
+    J.sums = P<double>(h->sums);
+    J.class_w = h->class_w;
+    J.class_open = h->class_open ? 1 : 0;
+    J.nbins = d.nbins;
+    J.Gs = h->Gs;
+    J.Gv = d.autocorrelation ? 0 : h->Gv;
+    J.autocorrelation = d.autocorrelation;
+    J.mddf_mode = h->mddf ? 1 : 0;
+    J.usecutoff = d.usecutoff;
+    J.o_md = h->o_md; J.o_mdr = h->o_mdr; J.o_rdf = h->o_rdf; J.o_rdfr = h->o_rdfr;
+    J.o_gs = h->o_gs; J.o_gsr = h->o_gsr; J.o_gv = h->o_gv; J.o_gvr = h->o_gvr;
+    J.binstep = d.binstep;
+    J.dbulk = d.dbulk;
+    J.Q = frame_weight_sum > 0.0 ? frame_weight_sum : h->weight_total;
+    J.volume_sum = h->volume_total;
+    J.solute_nmols = d.solute_nmols;
+    J.solvent_nmols = d.solvent_nmols;
+    J.solvent_nmols_samples = d.autocorrelation ? d.solvent_nmols - 1 : d.solvent_nmols;  // src/results.jl:230-237
+    J.nrandom = d.n_random_samples;
+    J.units_f = 6.022140857e23 / 1e24;  // units.Angs3tocm3permol = mole / Angs3tocm3 (src/io.jl:6-14)
+    J.ibulk = std::max(1, (int)std::ceil((d.dbulk + 0.5 * d.binstep) / d.binstep));  // setbin (src/results.jl:28)
+    dev_alloc(h, h->final_out, (size_t)n * 8);
+    dev_alloc(h, h->final_job, sizeof(FinalJob));
+    J.out = P<double>(h->final_out);
+    CM_CUDA(cudaMemcpyAsync(h->final_job.p, &J, sizeof(J), cudaMemcpyHostToDevice, h->stream));
+    k_finalize<<<1, 256, 0, h->stream>>>(P<FinalJob>(h->final_job));
+    CM_CUDA(cudaGetLastError());
+    return n;
+}
+
 int cm_read_results(cm_handle *h, double frame_weight_sum, cm_results *out) {
     return guarded(h, [&] {
         if (!out) throw cm_error(CM_EINVAL, "NULL output");
-        if (!(frame_weight_sum >= 0.0) || !std::isfinite(frame_weight_sum))
-            throw cm_error(CM_EINVAL, "frame_weight_sum must be finite and non-negative");
-        check_device_error(h);
-        const cm_system_desc &d = h->d;
-        const int64_t nb = d.nbins, Gs = h->Gs, Gv = d.autocorrelation ? h->Gs : h->Gv;
-        const int64_t n = FV_NVEC * nb + 2 * Gs * nb + 2 * Gv * nb + FS_NSCALAR;
-        FinalJob J{};
-        J.acc = P<unsigned long long>(h->hist);
-        J.sums = P<double>(h->sums);
-        J.class_w = h->class_w;
-        J.class_open = h->class_open ? 1 : 0;
-        J.nbins = d.nbins;
-        J.Gs = h->Gs;
-        J.Gv = d.autocorrelation ? 0 : h->Gv;
-        J.autocorrelation = d.autocorrelation;
-        J.mddf_mode = h->mddf ? 1 : 0;
-        J.usecutoff = d.usecutoff;
-        J.o_md = h->o_md; J.o_mdr = h->o_mdr; J.o_rdf = h->o_rdf; J.o_rdfr = h->o_rdfr;
-        J.o_gs = h->o_gs; J.o_gsr = h->o_gsr; J.o_gv = h->o_gv; J.o_gvr = h->o_gvr;
-        J.binstep = d.binstep;
-        J.dbulk = d.dbulk;
-        J.Q = frame_weight_sum > 0.0 ? frame_weight_sum : h->weight_total;
-        J.volume_sum = h->volume_total;
-        J.solute_nmols = d.solute_nmols;
-        J.solvent_nmols = d.solvent_nmols;
-        J.solvent_nmols_samples = d.autocorrelation ? d.solvent_nmols - 1 : d.solvent_nmols;  // src/results.jl:230-237
-        J.nrandom = d.n_random_samples;
-        J.units_f = 6.022140857e23 / 1e24;  // units.Angs3tocm3permol = mole / Angs3tocm3 (src/io.jl:6-14)
-        J.ibulk = std::max(1, (int)std::ceil((d.dbulk + 0.5 * d.binstep) / d.binstep));  // setbin (src/results.jl:28)
-        dev_alloc(h, h->final_out, (size_t)n * 8);
-        dev_alloc(h, h->final_job, sizeof(FinalJob));
-        J.out = P<double>(h->final_out);
-        CM_CUDA(cudaMemcpyAsync(h->final_job.p, &J, sizeof(J), cudaMemcpyHostToDevice, h->stream));
-        k_finalize<<<1, 256, 0, h->stream>>>(P<FinalJob>(h->final_job));
-        CM_CUDA(cudaGetLastError());
+        const int64_t n = launch_finalize(h, frame_weight_sum);
+        const int64_t nb = h->d.nbins, Gs = h->Gs, Gv = h->d.autocorrelation ? h->Gs : h->Gv;
         std::vector<double> v(n);
         CM_CUDA(cudaMemcpyAsync(v.data(), h->final_out.p, (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
         CM_CUDA(cudaStreamSynchronize(h->stream));
@@ -2127,6 +2138,62 @@ int cm_read_results(cm_handle *h, double frame_weight_sum, cm_results *out) {
         out->density_solvent_bulk = sc[FS_DSOLVENT_BULK];
         out->density_fix = sc[FS_DENSITY_FIX];
         out->zero_random_bins = (int64_t)sc[FS_ZERO_RANDOM_BINS];
+    });
+}
+
+int cm_contributions(cm_handle *h, double frame_weight_sum, int32_t nqueries, const cm_contrib_query *queries,
+                     double *out) {
+    return guarded(h, [&] {
+        if (nqueries < 1 || !queries || !out) throw cm_error(CM_EINVAL, "contributions need at least one query and an output");
+        if (nqueries > 65535) throw cm_error(CM_EINVAL, "at most 65535 queries per call");
+        const cm_system_desc &d = h->d;
+        const int Gs = (int)h->Gs, Gv = d.autocorrelation ? (int)h->Gs : (int)h->Gv;
+        std::vector<ContribQuery> q(nqueries);
+        std::vector<int> groups;
+        for (int k = 0; k < nqueries; ++k) {
+            const cm_contrib_query &c = queries[k];
+            if (c.side != CM_GROUP_SOLUTE && c.side != CM_GROUP_SOLVENT)
+                throw cm_error(CM_EINVAL, "query " + std::to_string(k) + ": side must be CM_GROUP_SOLUTE or CM_GROUP_SOLVENT");
+            if (c.type < CM_CONTRIB_MDDF || c.type > CM_CONTRIB_KBI)
+                throw cm_error(CM_EINVAL, "query " + std::to_string(k) + ": type must be :mddf (default), :coordination_number, :md_count, :kbi");
+            if (c.nterms < 1 || !c.groups)
+                throw cm_error(CM_EINVAL, "query " + std::to_string(k) + ": a query sums at least one group");
+            const int G = c.side == CM_GROUP_SOLUTE ? Gs : Gv;
+            q[k].side = c.side;
+            q[k].type = c.type;
+            q[k].divide = c.divide ? 1 : 0;
+            q[k].nmols = c.side == CM_GROUP_SOLUTE ? (double)d.solute_nmols : (double)d.solvent_nmols;
+            q[k].t0 = (int)groups.size();
+            for (int t = 0; t < c.nterms; ++t) {
+                const int g = c.groups[t];
+                if (g < 0 || g >= G)
+                    throw cm_error(CM_EINVAL, "query " + std::to_string(k) + ": group " + std::to_string(g + 1) +
+                                                  " greater than number of groups (" + std::to_string(G) + ")");
+                groups.push_back(g);
+            }
+            q[k].t1 = (int)groups.size();
+        }
+        launch_finalize(h, frame_weight_sum);
+        const int64_t nb = d.nbins;
+        dev_alloc(h, h->contrib_q, q.size() * sizeof(ContribQuery));
+        dev_alloc(h, h->contrib_g, groups.size() * sizeof(int));
+        dev_alloc(h, h->contrib_out, (size_t)2 * nqueries * nb * 8);
+        CM_CUDA(cudaMemcpyAsync(h->contrib_q.p, q.data(), q.size() * sizeof(ContribQuery), cudaMemcpyHostToDevice, h->stream));
+        CM_CUDA(cudaMemcpyAsync(h->contrib_g.p, groups.data(), groups.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        ContribJob J{};
+        J.fin = P<double>(h->final_out);
+        J.nbins = d.nbins;
+        J.Gs = Gs;
+        J.Gv = Gv;
+        J.units_f = 6.022140857e23 / 1e24;  // units.Angs3tocm3permol (src/io.jl:6-14)
+        J.q = P<ContribQuery>(h->contrib_q);
+        J.groups = P<int>(h->contrib_g);
+        J.out = P<double>(h->contrib_out);
+        J.scratch = J.out + (int64_t)nqueries * nb;
+        k_contrib<<<nqueries, 128, 0, h->stream>>>(J);
+        CM_CUDA(cudaGetLastError());
+        CM_CUDA(cudaMemcpyAsync(out, h->contrib_out.p, (size_t)nqueries * nb * 8, cudaMemcpyDeviceToHost, h->stream));
+        CM_CUDA(cudaStreamSynchronize(h->stream));
     });
 }
 

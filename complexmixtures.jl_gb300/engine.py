@@ -350,6 +350,36 @@ class Engine:
         out["zero_random_bins"] = r.zero_random_bins
         return out
 
+    def contributions(self, queries, frame_weight_sum: float = 0.0) -> np.ndarray:
+        """Group contributions on the device (cm_contributions), one row per
+        query.  A query is (side, type, rows, divide): side "solute" or
+        "solvent", type "mddf" / "coordination_number" / "md_count" / "kbi",
+        the 0-based group rows summed in order, and whether each row is divided
+        by the side's nmols.  ``contribution_terms`` resolves a SoluteGroup or
+        SolventGroup into (side, rows, divide)."""
+        nq = len(queries)
+        if nq == 0:
+            return np.zeros((0, self.nbins))
+        arr = (N.cm_contrib_query * nq)()
+        keep = []
+        for k, (side, type, rows, divide) in enumerate(queries):
+            if side not in ("solute", "solvent"):
+                raise ValueError("side must be 'solute' or 'solvent'")
+            if type not in N.CM_CONTRIB_TYPES:
+                raise ValueError("type must be :mddf (default), :coordination_number, :md_count, :kbi")
+            g = np.ascontiguousarray(rows, dtype=np.int32)
+            keep.append(g)
+            arr[k].side = N.CM_GROUP_SOLUTE if side == "solute" else N.CM_GROUP_SOLVENT
+            arr[k].type = N.CM_CONTRIB_TYPES[type]
+            arr[k].divide = 1 if divide else 0
+            arr[k].nterms = len(g)
+            arr[k].groups = N.as_ptr(g, C.c_int32)
+        out = np.zeros((nq, self.nbins))
+        st = self._lib.cm_contributions(self._h, float(frame_weight_sum), nq, arr, N.as_ptr(out, C.c_double))
+        N.raise_for(st, self._h)
+        self._inflight.clear()
+        return out
+
     def raw_counts(self) -> dict:
         """Exact int64 half-unit counts (runs with a single frame weight)."""
         out, c = raw_arrays(self.nbins, self.ngroups_solute, self.ngroups_solvent)

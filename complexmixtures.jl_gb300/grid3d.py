@@ -29,15 +29,26 @@ class Atoms:
     chain: List[str] = field(default_factory=list)
     resnum: List[int] = field(default_factory=list)
     element: List[str] = field(default_factory=list)
+    index: List[int] = field(default_factory=list)   # 1-based atom indices (PDBTools.index); default 1..N
 
     def __post_init__(self):
         self.xyz = np.asarray(self.xyz, dtype=np.float64).reshape(-1, 3)
         n = len(self.xyz)
+        self.index = [int(i) for i in self.index] or list(range(1, n + 1))
         self.name = list(self.name) or ["X"] * n
         self.resname = list(self.resname) or ["UNK"] * n
         self.chain = list(self.chain) or ["A"] * n
         self.resnum = [int(r) for r in self.resnum] or [1] * n
         self.element = list(self.element) or [""] * n
+
+    def take(self, keep) -> "Atoms":
+        """The atoms at the given positions, or where a boolean mask is true,
+        keeping their indices (a PDBTools selection of the structure)."""
+        keep = np.asarray(keep)
+        pos = np.nonzero(keep)[0] if keep.dtype == bool else keep.astype(np.int64)
+        pick = lambda v: [v[int(k)] for k in pos]
+        return Atoms(self.xyz[pos], pick(self.name), pick(self.resname), pick(self.chain), pick(self.resnum),
+                     pick(self.element), pick(self.index))
 
 
 def read_pdb_atoms(path: str) -> Atoms:

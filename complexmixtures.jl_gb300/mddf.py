@@ -82,7 +82,7 @@ def new_result(trajectory: Trajectory, options: Options, tmeta, frame_weights) -
 def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = None, *, frame_weights=None,
          coordination_number_only: bool = False, low_memory: bool = False, trajectory_format: str = "",
          precision: str = "fp32", regime: str = "auto", device: int = 0, batch_frames: int = 64,
-         finalize: str = "host") -> Result:
+         finalize: str = "host", keep_engine: bool = False) -> Result:
     """Minimum-distance distribution function (src/mddf.jl:113-347).
 
     ``mddf(trajectory, options)`` with a Trajectory object, or
@@ -93,7 +93,10 @@ def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = Non
     both give identical counts.  ``finalize="device"`` computes the
     normalisation, densities, MDDF, RDF and KB integrals on the GPU
     (cm_read_results) instead of the host restatement of finalresults!; both
-    agree to 1e-12.
+    agree to 1e-12.  ``keep_engine=True`` leaves the engine open, with the
+    run's accumulators on the device, as ``R.engine``: ``contributions`` and
+    ``ResidueContributions`` then run on the GPU.  Close it with
+    ``R.engine.close()``.
     """
     if finalize not in ("host", "device"):
         raise ValueError("finalize must be 'host' or 'device'")
@@ -111,14 +114,19 @@ def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = Non
     to_compute = [i for i in range(options.firstframe, tmeta.lastframe_read + 1, options.stride) if fw[i - 1] != 0.0]
     eng = engine_for(R, options, tmeta.irefatom, coordination_number_only=coordination_number_only,
                      precision=precision, regime=regime, device=device, max_frames_per_batch=batch_frames)
+    ok = False
     try:
         _run_frames(eng, trajectory, to_compute, fw, batch_frames)
         if finalize == "device":
             res = eng.results(sum_frame_weights(R))
         else:
             c = eng.counts()
+        ok = True
     finally:
-        eng.close()
+        if not (ok and keep_engine):
+            eng.close()
+    if keep_engine:
+        R.engine = eng
     if finalize == "device":
         return _device_result(R, res, options, coordination_number_only)
     for k in ("md_count", "md_count_random", "rdf_count", "rdf_count_random", "solute_group_count",

@@ -5,8 +5,10 @@
  * minimum distances between solute and solvent molecules under periodic
  * boundary conditions (orthorhombic and triclinic cells), the MDDF / RDF /
  * group-contribution histograms, and the random-insertion ideal-gas reference
- * counts.  Everything before the path (trajectory reading, selections, options)
- * and after it (normalisation, contributions) stays in the host language.
+ * counts.  Everything before the path (trajectory file parsing, selections,
+ * options) stays in the host language.  The steps after it can run on the
+ * device or stay on the host: normalisation (cm_read_results) and the group and
+ * residue contributions (cm_contributions).
  *
  * Reference interfaces replaced (paths relative to ComplexMixtures.jl):
  *   mddf_frame!(r_chunk, system, buff, options, frame_weight, RNG)  src/mddf.jl:361-429
@@ -285,6 +287,39 @@ typedef struct cm_results {
     int64_t zero_random_bins;         /* bins with no random-insertion count (the reference warns about them) */
 } cm_results;
 int cm_read_results(cm_handle *h, double frame_weight_sum, cm_results *out);
+
+/*
+ * Group contributions on the device, many queries per call.  Replaces
+ * contributions(R, SoluteGroup|SolventGroup; type) (src/tools/contributions.jl:70-248)
+ * and the per-residue loop of ResidueContributions
+ * (src/tools/residue_contributions.jl:157-215), which calls it once per residue.
+ * The handle's accumulators are finalised as cm_read_results does
+ * (frame_weight_sum has the same meaning).  Then each query sums the finalised
+ * group-count rows `groups[0..nterms-1]` of its side, in that order,
+ * bin by bin.  With `divide` set, each term is group_count[g] / nmols, the
+ * reference's rule for atom indices of a selection with more than one molecule.
+ * The sum is then converted by `type`, in FP64 and in the reference's order of
+ * operations:
+ *   - MDDF: sum / md_count_random, or 0 where md_count_random is 0;
+ *   - COORDINATION_NUMBER: its cumulative sum;
+ *   - MD_COUNT: the sum itself;
+ *   - KBI: Angs3tocm3permol * (1 / density.solvent_bulk) * (cumsum(sum) - cumsum(random sum)).
+ * The host resolves group names, atom names and atom indices into
+ * 0-based group rows, which is where the reference raises its argument errors.
+ * out: caller-owned [nqueries][nbins] doubles.  In self mode the solvent rows
+ * are the solute's.
+ */
+enum { CM_GROUP_SOLUTE = 0, CM_GROUP_SOLVENT = 1 };
+enum { CM_CONTRIB_MDDF = 0, CM_CONTRIB_COORDINATION_NUMBER = 1, CM_CONTRIB_MD_COUNT = 2, CM_CONTRIB_KBI = 3 };
+typedef struct cm_contrib_query {
+    int32_t side;            /* CM_GROUP_SOLUTE or CM_GROUP_SOLVENT */
+    int32_t type;            /* CM_CONTRIB_* */
+    int32_t divide;          /* nonzero: each term is divided by the side's number of molecules */
+    int32_t nterms;          /* >= 1 */
+    const int32_t *groups;   /* host [nterms]: 0-based group rows, summed in this order */
+} cm_contrib_query;
+int cm_contributions(cm_handle *h, double frame_weight_sum, int32_t nqueries, const cm_contrib_query *queries,
+                     double *out);
 
 /* Synchronise and copy the exact half-unit counts (single-weight runs only). */
 int cm_read_raw_counts(cm_handle *h, cm_raw_counts *out);

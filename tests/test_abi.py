@@ -38,10 +38,12 @@ def test_struct_sizes_match_header(cm):
     assert C.sizeof(N.cm_request_info) == 48
     assert C.sizeof(N.cm_tuning) == 144
     assert C.sizeof(N.cm_dcd_layout) == 64
+    assert C.sizeof(N.cm_contrib_query) == 24
 
 
 STRUCTS = ("cm_system_desc", "cm_frames", "cm_counts", "cm_raw_counts", "cm_stats", "cm_kernel_times", "cm_tuning",
-           "cm_dcd_layout", "cm_results", "cm_grid3d_desc", "cm_grid3d_out", "cm_server_desc", "cm_request_info")
+           "cm_dcd_layout", "cm_results", "cm_grid3d_desc", "cm_grid3d_out", "cm_server_desc", "cm_request_info",
+           "cm_contrib_query")
 
 
 def test_struct_layouts_match_c_compiler(cm, tmp_path):
