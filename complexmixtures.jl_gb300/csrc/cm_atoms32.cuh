@@ -171,13 +171,16 @@ __device__ __forceinline__ Site site_of(const FrameScratch &F, int packed, float
 // distance from the site is (grid units outside the slab) x (cell width
 // between the faces).  Orthogonal cells: the slabs' distances add in
 // quadrature (the exact box distance); other cells: the largest of them.
-__device__ __forceinline__ float cell_d2(const FrameScratch &F, const Site &st, int dx, int dy, int dz) {
-    const float ux = (fminf(fmaxf(st.g[0], (float)dx), (float)dx + 1.f) - st.g[0]) * F.cw[0];
-    const float uy = (fminf(fmaxf(st.g[1], (float)dy), (float)dy + 1.f) - st.g[1]) * F.cw[1];
-    const float uz = (fminf(fmaxf(st.g[2], (float)dz), (float)dz + 1.f) - st.g[2]) * F.cw[2];
+__device__ __forceinline__ float cell_d2(const FrameScratch &F, float g0, float g1, float g2, int dx, int dy, int dz) {
+    const float ux = (fminf(fmaxf(g0, (float)dx), (float)dx + 1.f) - g0) * F.cw[0];
+    const float uy = (fminf(fmaxf(g1, (float)dy), (float)dy + 1.f) - g1) * F.cw[1];
+    const float uz = (fminf(fmaxf(g2, (float)dz), (float)dz + 1.f) - g2) * F.cw[2];
     if (F.ortho) return fmaf(uz, uz, fmaf(uy, uy, ux * ux));
     const float m = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
     return m * m;
+}
+__device__ __forceinline__ float cell_d2(const FrameScratch &F, const Site &st, int dx, int dy, int dz) {
+    return cell_d2(F, st.g[0], st.g[1], st.g[2], dx, dy, dz);
 }
 
 // Walk the stencil cells of one site that can hold an atom within the
@@ -247,6 +250,143 @@ __device__ __forceinline__ void atoms_walk_flat(const FrameGeom &G, const FrameS
             const bool in = cnt > 0 && excl < kb + 32 && incl > kb;
             const int pos = in ? max(excl - kb, 0) : 0;
             if (in) win[pos] = make_float4(tx, ty, tz, __int_as_float(beg - excl));
+            const unsigned m = __reduce_or_sync(kFull, in ? (1u << pos) : 0u);
+            __syncwarp();
+            const int k = kb + lane;
+            if (k < total) {
+                const float4 w = win[31 - __clz(m & (kFull >> (31 - lane)))];
+                body(__float_as_int(w.w) + k, w.x, w.y, w.z);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Up to kSiteGroup sites of one solvent molecule walked together (FP32): the
+// stencils of the sites are one box of cells around the cell of the group's
+// first site (the reference cell), each solute atom is loaded once per walk
+// and compared with every site of the group.  Sites are given relative to the
+// reference cell's origin, q_j + off(d_j) with d_j the site's cell offset
+// from the reference cell, so the displacement of a pair is
+// (q_a + off(cell_a - ref)) - (q_j + off(d_j)); its FP32 error is within the
+// frame's guard band, whose offset bound covers one cell beyond the ATOMS
+// stencil for that reason.
+constexpr int kSiteGroup = 4;
+
+struct SiteGroup {
+    int ns;                           // sites in the group
+    int cx, cy, cz;                   // reference cell
+    int lo[3], hi[3];                 // range of the sites' cell offsets d_j
+    float qx[kSiteGroup], qy[kSiteGroup], qz[kSiteGroup];  // q_j + off(d_j)
+    const float4 *site;               // per-warp shared table: (fractional position in the cell, packed d_j)
+};
+
+__device__ __forceinline__ int unpack_d(float w, int k) { return ((__float_as_int(w) >> (2 * k)) & 3) - 1; }
+
+// Sets up the group of sites [b0, b0 + ns) of a molecule, lane j taking site
+// j; false when a site's cell is more than one cell from the reference cell
+// or the walk box would leave the offset table (the sites are then walked one
+// by one).  `tab` is the warp's kSiteGroup-entry shared table.
+__device__ __forceinline__ bool site_group(const FrameGeom &G, const FrameScratch &F, const float4 *off32,
+                                           const int *cells, const float4 *q32, int b0, int ns, int lane, float4 *tab,
+                                           SiteGroup &sg) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int pk0 = cells[b0];
+    sg.ns = ns;
+    sg.cx = pk0 & 1023;
+    sg.cy = (pk0 >> 10) & 1023;
+    sg.cz = (pk0 >> 20) & 1023;
+    const int ref[3] = {sg.cx, sg.cy, sg.cz};
+    bool bad = false;
+    int d[3] = {0, 0, 0};
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    if (lane < ns) {
+        const int pk = cells[b0 + lane];
+        const int c[3] = {pk & 1023, (pk >> 10) & 1023, (pk >> 20) & 1023};
+        const float4 q = q32[b0 + lane];
+        float g[3];
+        int code = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            int t = c[k] - ref[k];
+            if (2 * t > G.n[k]) t -= G.n[k];
+            else if (2 * t < -G.n[k]) t += G.n[k];
+            if (t < -1 || t > 1) bad = true;
+            d[k] = max(-1, min(1, t));
+            code |= (d[k] + 1) << (2 * k);
+            g[k] = fmaf(F.hin[3 * k + 2], q.z, fmaf(F.hin[3 * k + 1], q.y, F.hin[3 * k] * q.x));
+        }
+        const float4 of = off32[off_index(d[0], d[1], d[2])];
+        qx = q.x + of.x;
+        qy = q.y + of.y;
+        qz = q.z + of.z;
+        tab[lane] = make_float4(g[0], g[1], g[2], __int_as_float(code));
+    }
+#pragma unroll
+    for (int j = 0; j < kSiteGroup; ++j) {
+        sg.qx[j] = __shfl_sync(kFull, qx, j);
+        sg.qy[j] = __shfl_sync(kFull, qy, j);
+        sg.qz[j] = __shfl_sync(kFull, qz, j);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        sg.lo[k] = __reduce_min_sync(kFull, d[k]);
+        sg.hi[k] = __reduce_max_sync(kFull, d[k]);
+        if (sg.hi[k] + F.La[k] > kLT || sg.lo[k] - F.La[k] < -kLT) bad = true;
+    }
+    sg.site = tab;
+    __syncwarp();
+    return !__any_sync(kFull, bad);
+}
+
+// The group's walk box: cells at offsets [lo - La, hi + La] from the
+// reference cell; a cell is kept if its box lies within the cutoff of some
+// site.  The kept cells' atoms run end to end, 32 pairs of lanes at a time
+// (as in atoms_walk_flat).  body(p, ox, oy, oz) gets the solute atom and
+// off(cell - ref).
+template <typename Body>
+__device__ __forceinline__ void atoms_walk_group(const FrameGeom &G, const FrameScratch &F, const int *cs,
+                                                 const SiteGroup &sg, float prune2, const float4 *off32, int lane,
+                                                 float4 *win, Body &&body) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int x0 = sg.lo[0] - F.La[0], y0 = sg.lo[1] - F.La[1], z0 = sg.lo[2] - F.La[2];
+    const int nx = sg.hi[0] - x0 + F.La[0] + 1, ny = sg.hi[1] - y0 + F.La[1] + 1, nz = sg.hi[2] - z0 + F.La[2] + 1;
+    const int ncells = nx * ny * nz;
+    auto probe = [&](int ci, int &beg, int &end, float4 &of) {
+        const int dx = x0 + ci % nx, dy = y0 + (ci / nx) % ny, dz = z0 + ci / (nx * ny);
+        const int cell = (wrap_cell(sg.cz + dz, G.n[2]) * G.n[1] + wrap_cell(sg.cy + dy, G.n[1])) * G.n[0] +
+                         wrap_cell(sg.cx + dx, G.n[0]);
+        beg = cs[cell];
+        end = cs[cell + 1];
+        bool near = false;
+        for (int j = 0; j < sg.ns; ++j) {
+            const float4 t = sg.site[j];
+            near = near || cell_d2(F, t.x, t.y, t.z, dx - unpack_d(t.w, 0), dy - unpack_d(t.w, 1), dz - unpack_d(t.w, 2)) <= prune2;
+        }
+        if (!near) end = beg;
+        if (end > beg) of = off32[off_index(dx, dy, dz)];
+    };
+    for (int c0 = 0; c0 < ncells; c0 += 32) {
+        const int ci = c0 + lane;
+        int cnt = 0, beg = 0;
+        float4 of = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ci < ncells) {
+            int end;
+            probe(ci, beg, end, of);
+            cnt = end - beg;
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += u;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        const int excl = incl - cnt;
+        for (int kb = 0; kb < total; kb += 32) {
+            const bool in = cnt > 0 && excl < kb + 32 && incl > kb;
+            const int pos = in ? max(excl - kb, 0) : 0;
+            if (in) win[pos] = make_float4(of.x, of.y, of.z, __int_as_float(beg - excl));
             const unsigned m = __reduce_or_sync(kFull, in ? (1u << pos) : 0u);
             __syncwarp();
             const int k = kb + lane;
@@ -329,6 +469,7 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bu
     constexpr bool WARP = SCHED != kSchedThread;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float4 s_win[kAtomsWarps][32];  // atoms_walk_flat's window table, one per warp
+    __shared__ float4 s_site[kAtomsWarps][kSiteGroup];  // site_group's table, one per warp
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);
     __syncthreads();
@@ -418,7 +559,8 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bu
             T.m1 = T.m2 = T.r1 = INFINITY;
             T.p1 = 0x7fffffff;
             T.b1 = 0;
-            for (int b = 0; b < apv; ++b) {
+            // one site with its own stencil walk
+            auto one_site = [&](int b) {
                 const Site sb = site_of(F, vcell[vb + b], vq32[vb + b]);
                 const bool isref = b == iref;
                 auto pair = [&](int p, float tx, float ty, float tz) {
@@ -442,6 +584,39 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bu
                         for (int p = beg + lane; p < end; p += STRIDE) pair(p, tx, ty, tz);
                     });
                 }
+            };
+            if constexpr (SCHED == kSchedBalanced) {
+                // sparse solutes: the sites of a group share one walk (dense solutes
+                // keep per-site stencils, whose cells each hold many atoms)
+                for (int b0 = 0; b0 < apv; b0 += kSiteGroup) {
+                    const int ns = min(kSiteGroup, apv - b0);
+                    SiteGroup sg;
+                    if (!site_group(G, F, off32, vcell + vb, vq32 + vb, b0, ns, lane, s_site[threadIdx.x >> 5], sg)) {
+                        for (int b = b0; b < b0 + ns; ++b) one_site(b);
+                        continue;
+                    }
+                    // the group's sites against each solute atom of the walk box
+                    auto pairs = [&](int p, float ox, float oy, float oz) {
+                        lane_evals += ns;
+                        const float4 qa = sq32[p];
+                        const float ux = qa.x + ox, uy = qa.y + oy, uz = qa.z + oz;
+#pragma unroll
+                        for (int j = 0; j < kSiteGroup; ++j) {
+                            if (j >= ns) break;
+                            const float ex = ux - sg.qx[j], ey = uy - sg.qy[j], ez = uz - sg.qz[j];
+                            const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                            T.m2 = fminf(T.m2, fmaxf(T.m1, d2));
+                            const bool lt = d2 < T.m1;
+                            T.p1 = lt ? p : T.p1;
+                            T.b1 = lt ? b0 + j : T.b1;
+                            T.m1 = fminf(T.m1, d2);
+                            if (b0 + j == iref) T.r1 = fminf(T.r1, d2);
+                        }
+                    };
+                    atoms_walk_group(G, F, cs, sg, prune2, off32, lane, win, pairs);
+                }
+            } else {
+                for (int b = 0; b < apv; ++b) one_site(b);
             }
             if (WARP) top2_reduce(T);
             if (T.m1 <= g.cutp2) {

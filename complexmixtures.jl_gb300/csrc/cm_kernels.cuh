@@ -1316,7 +1316,8 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
         for (int k = 0; k < 3; ++k) {
             F.L[k] = L[k];
             F.La[k] = La[k];
-            Ls[k] = max(L[k], La[k]);
+            // ATOMS: one cell beyond the stencil, for the grouped site walk
+            Ls[k] = pairs ? max(L[k], La[k]) : La[k] + 1;
             if (2 * L[k] + 1 > G.n[k]) multi |= 1 << k;
         }
         F.multi = multi;

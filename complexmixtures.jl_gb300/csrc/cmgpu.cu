@@ -1286,6 +1286,9 @@ Staged stage(cm_handle *h, const cm_frames *f, int f0) {
         CM_CUDA(cudaGetLastError());
         h->launches_total += d.autocorrelation ? 1 : 2;
     } else if (f->memory == CM_MEM_HOST) {
+        // the staging buffers exist already unless the handle's first frames came from device memory
+        dev_alloc(h, h->stage_s[b], (size_t)h->max_frames * h->Ns * 3 * h->coord_elem);
+        if (!d.autocorrelation) dev_alloc(h, h->stage_v[b], (size_t)h->max_frames * h->Nv * 3 * h->coord_elem);
         CM_CUDA(cudaMemcpyAsync(h->stage_s[b].p, (const char *)f->solute_xyz + S.sbytes * f0, (size_t)S.sbytes * nf,
                                 cudaMemcpyHostToDevice, cp));
         S.xs_base = (const char *)h->stage_s[b].p;

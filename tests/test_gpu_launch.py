@@ -103,3 +103,33 @@ def test_batch_graph_counts_equal_each_system_alone(cm):
         e.close()
         for key in KEYS:
             assert np.array_equal(got[key], alone[k][key]), (k, key)
+
+
+@pytest.mark.parametrize("batched", [False, True], ids=["engine", "batch"])
+def test_device_frames_then_host_frames(cm, batched):
+    """A handle whose first frames come from device memory stages later
+    host-memory frames too (its staging buffers are made on first use), alone
+    and inside a batch; the counts equal one host-memory submit of all frames."""
+    import torch
+
+    rng = np.random.default_rng(47)
+    xs, xv, cells = system(rng, 25, 6, 500, 3, 8, False)
+    xs, xv = xs.astype(np.float32), xv.astype(np.float32)
+    kw = dict(solute_nmols=25, solute_natomspermol=6, solvent_nmols=500, solvent_natomspermol=3, autocorrelation=False,
+              precision="fp32", regime="pairs", max_frames_per_batch=4, **OPT)
+    want = run(cm, "stream", xs, xv, cells, **kw)[0]
+    ids = np.arange(1, 9)
+    first = (torch.from_numpy(xs[:4]).cuda(), torch.from_numpy(xv[:4]).cuda(), cells[:4], ids[:4])
+    second = (xs[4:], xv[4:], cells[4:], ids[4:])
+    eng = cm.Engine(**kw)
+    if batched:
+        with cm.Batch([eng]) as b:
+            b.submit([first])
+            b.submit([second])
+    else:
+        eng.submit(*first[:3], frame_ids=first[3])
+        eng.submit(*second[:3], frame_ids=second[3])
+    got = eng.raw_counts()
+    eng.close()
+    for k in KEYS:
+        assert np.array_equal(got[k], want[k]), k
