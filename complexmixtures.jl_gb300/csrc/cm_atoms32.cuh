@@ -25,6 +25,9 @@
 namespace cmk {
 
 constexpr int kAtomsWarps = 8;  // warps per CTA of k_atoms_eval
+#ifndef CM_ATOMS_MIN_CTAS
+#define CM_ATOMS_MIN_CTAS 2         // resident CTAs per SM that k_atoms_eval's register budget is sized for
+#endif
 
 // Dilated occupancy of each solute molecule's cell list: near = some cell
 // within the ATOMS stencil half-widths La holds an atom of the molecule.
@@ -465,7 +468,7 @@ enum AtomsSched { kSchedThread = 0, kSchedCell = 1, kSchedBalanced = 2 };
 
 // ATOMS evaluation of the queue (persistent grid).
 template <bool FP32, bool RANDOM, int SCHED>
-__global__ void __launch_bounds__(kAtomsWarps * 32, 2) k_atoms_eval(DevSys S, Bufs B) {
+__global__ void __launch_bounds__(kAtomsWarps * 32, CM_ATOMS_MIN_CTAS) k_atoms_eval(DevSys S, Bufs B) {
     constexpr bool WARP = SCHED != kSchedThread;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float4 s_win[kAtomsWarps][32];  // atoms_walk_flat's window table, one per warp

@@ -358,34 +358,282 @@ __global__ void __launch_bounds__(kFlatWarps * 32, 2) k_pairs_flat32(DevSys S, B
     shist_flush(S, h, false);
 }
 
-// Guard kernel: exact processing of the candidates deferred by the FP32 real
-// pass (the FP32 pass of the molecule pair is recomputed and pairs_decide
-// takes every decision with the FP64 rules).
+// ------------------------------------------------------------ guard kernel
+// Exact processing of the candidates deferred by the FP32 real pass, one warp
+// per queued molecule pair: the lanes split the pair's atom pairs (over its
+// images), for the FP32 pass and for the filtered FP64 scan, and the lanes'
+// results are merged.  The FP64 minimum is merged by the reference's tie rule
+// (distance, then the larger (solute atom, solvent atom) pair; in self mode the
+// second direction's key is (solvent atom, solute atom)), which does not
+// depend on the order in which pairs are visited, so the records are those of
+// pairs_decide.
+
+// Atom pair i of a molecule pair: image i / (aps apv), then solvent atom b and
+// solute atom a; the quotients from FP32 reciprocals are exact for i < 2^16.
+struct PairIndex {
+    float inv_pi, inv_aps;
+    int per_img, aps;
+    __device__ __forceinline__ void at(int i, int &img, int &b, int &a) const {
+        img = (int)((float(i) + 0.5f) * inv_pi);
+        const int r = i - img * per_img;
+        b = (int)((float(r) + 0.5f) * inv_aps);
+        a = r - b * aps;
+    }
+};
+
+__device__ __forceinline__ void image_at(const Images &im, int img, int &dx, int &dy, int &dz) {
+    const int ix = img % im.cnt[0], iy = (img / im.cnt[0]) % im.cnt[1], iz = img / (im.cnt[0] * im.cnt[1]);
+    dx = im.base[0] + ix * im.step[0];
+    dy = im.base[1] + iy * im.step[1];
+    dz = im.base[2] + iz * im.step[2];
+}
+
+// FP32 pass of pairs_pass32 with the pairs split over the lanes; every lane
+// ends with the merged result (second-smallest over the union: the smaller of
+// the larger minimum and the smaller second minima).
 template <bool SELF>
-__global__ void __launch_bounds__(128) k_pairs_guard(DevSys S, Bufs B) {
+__device__ __forceinline__ void pass32_warp(const DevSys &S, const float4 *__restrict__ off32, const Images &im, float4 qs,
+                                            float4 qv, const float4 *os, const float4 *ov, const PairIndex &pi, int total,
+                                            int lane, Pass32 &P) {
+    constexpr unsigned kFull = 0xffffffffu;
+    P.m1 = P.m2 = P.r1 = P.r2 = INFINITY;
+    P.k1 = 0x7fffffff;
+    const int apv = S.apv, iref = S.iref;
+    int cur = -1;
+    float Dx = 0.f, Dy = 0.f, Dz = 0.f;
+    for (int i = lane; i < total; i += 32) {
+        int img, b, a;
+        pi.at(i, img, b, a);
+        if (img != cur) {
+            int dx, dy, dz;
+            image_at(im, img, dx, dy, dz);
+            const float4 o = off32[off_index(dx, dy, dz)];
+            Dx = (qv.x - qs.x) + o.x;
+            Dy = (qv.y - qs.y) + o.y;
+            Dz = (qv.z - qs.z) + o.z;
+            cur = img;
+        }
+        const float4 ob = ov[b], oa = os[a];
+        const float tx = Dx + ob.x, ty = Dy + ob.y, tz = Dz + ob.z;
+        const float ex = tx - oa.x, ey = ty - oa.y, ez = tz - oa.z;
+        const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+        const int k = a * apv + b;
+        P.m2 = fminf(P.m2, fmaxf(P.m1, d2));
+        P.k1 = d2 < P.m1 ? k : P.k1;
+        P.m1 = fminf(P.m1, d2);
+        if (b == iref) P.r1 = fminf(P.r1, d2);
+        if (SELF && a == iref) P.r2 = fminf(P.r2, d2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float m1 = __shfl_xor_sync(kFull, P.m1, o), m2 = __shfl_xor_sync(kFull, P.m2, o);
+        const int k1 = __shfl_xor_sync(kFull, P.k1, o);
+        P.m2 = fminf(fmaxf(P.m1, m1), fminf(P.m2, m2));
+        if (m1 < P.m1 || (m1 == P.m1 && k1 < P.k1)) {
+            P.m1 = m1;
+            P.k1 = k1;
+        }
+        P.r1 = fminf(P.r1, __shfl_xor_sync(kFull, P.r1, o));
+        if (SELF) P.r2 = fminf(P.r2, __shfl_xor_sync(kFull, P.r2, o));
+    }
+}
+
+// pairs_exact<true, SELF> with the pairs split over the lanes, merged over the
+// warp; every lane ends with the result.
+template <bool SELF>
+__device__ void exact_warp(const DevSys &S, const d4 *__restrict__ off64, const float4 *__restrict__ off32, const Images &im,
+                           d4 qs64, float4 qs32, d4 qv64, float4 qv32, const d4 *os64, const float4 *os32, const d4 *ov64,
+                           const float4 *ov32, float thr_arg, float thr_r1, float thr_r2, const PairIndex &pi, int total,
+                           int lane, Exact64 &E) {
+    constexpr unsigned kFull = 0xffffffffu;
+    best_init(E.B);
+    E.rr1 = INFINITY;
+    E.rr2 = INFINITY;
+    E.evals = 0;
+    const int iref = S.iref;
+    const double cut2 = S.cut2;
+    int cur = -1;
+    double Dx = 0.0, Dy = 0.0, Dz = 0.0;
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+    for (int i = lane; i < total; i += 32) {
+        int img, b, a;
+        pi.at(i, img, b, a);
+        if (img != cur) {
+            int dx, dy, dz;
+            image_at(im, img, dx, dy, dz);
+            const int oi = off_index(dx, dy, dz);
+            const float4 of = off32[oi];
+            Fx = (qv32.x - qs32.x) + of.x;
+            Fy = (qv32.y - qs32.y) + of.y;
+            Fz = (qv32.z - qs32.z) + of.z;
+            const d4 o = off64[oi];
+            Dx = add(sub(qv64.x, qs64.x), o.x);
+            Dy = add(sub(qv64.y, qs64.y), o.y);
+            Dz = add(sub(qv64.z, qs64.z), o.z);
+            cur = img;
+        }
+        const float4 ob32 = ov32[b], oa32 = os32[a];
+        const float ex = (Fx + ob32.x) - oa32.x, ey = (Fy + ob32.y) - oa32.y, ez = (Fz + ob32.z) - oa32.z;
+        const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+        if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1) || (SELF && a == iref && d2f <= thr_r2))) continue;
+        const d4 ob = ov64[b], oa = os64[a];
+        const double d2 = pair_d2_64(add(Dx, ob.x), add(Dy, ob.y), add(Dz, ob.z), oa.x, oa.y, oa.z);
+        E.evals++;
+        if (d2 <= cut2) {
+            if (b == iref) E.rr1 = fmin(E.rr1, d2);
+            if (SELF && a == iref) E.rr2 = fmin(E.rr2, d2);
+            best_update<SELF>(E.B, d2, a, b);
+        }
+    }
+    // merge: smallest d = sqrt(d2); among equal d the larger (a, b), and in
+    // self mode separately the larger (b, a)
+    double d = E.B.d2 <= cut2 ? best_d(E.B) : INFINITY;
+    double d2 = E.B.d2;
+    int a1 = E.B.a, b1 = E.B.b, a2 = E.B.a2, b2 = E.B.b2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double od = __shfl_xor_sync(kFull, d, o), od2 = __shfl_xor_sync(kFull, d2, o);
+        const int oa1 = __shfl_xor_sync(kFull, a1, o), ob1 = __shfl_xor_sync(kFull, b1, o);
+        const int oa2 = __shfl_xor_sync(kFull, a2, o), ob2 = __shfl_xor_sync(kFull, b2, o);
+        if (od < d) {
+            d = od;
+            d2 = od2;
+            a1 = oa1; b1 = ob1; a2 = oa2; b2 = ob2;
+        } else if (od == d) {
+            if (oa1 > a1 || (oa1 == a1 && ob1 > b1)) { a1 = oa1; b1 = ob1; }
+            if (SELF && (ob2 > b2 || (ob2 == b2 && oa2 > a2))) { a2 = oa2; b2 = ob2; }
+        }
+        E.rr1 = fmin(E.rr1, __shfl_xor_sync(kFull, E.rr1, o));
+        if (SELF) E.rr2 = fmin(E.rr2, __shfl_xor_sync(kFull, E.rr2, o));
+        E.evals += __shfl_xor_sync(kFull, E.evals, o);
+    }
+    E.B.d2 = d2;
+    E.B.d = d <= 1e300 ? d : -1.0;
+    E.B.a = a1; E.B.b = b1; E.B.a2 = a2; E.B.b2 = b2;
+}
+
+// pairs_decide with the warp-parallel pass and scans; the statistics are
+// counted on lane 0.
+template <bool SELF>
+__device__ void decide_warp(const DevSys &S, const Guard &g, const Pass32 &P, const d4 *__restrict__ off64,
+                            const float4 *__restrict__ off32, const Images &im, d4 qs64, float4 qs32, d4 qv64, float4 qv32,
+                            const d4 *os64, const float4 *os32, const d4 *ov64, const float4 *ov32, int s, int64_t v,
+                            const PairIndex &pi, int total, int lane, DirRec &r1, DirRec &r2, LocalStats &st) {
+    r1 = dir_none(S);
+    r2 = dir_none(S);
+    if (P.m1 > g.cutp2) return;
+    const float d1 = sqrtf(P.m1);
+    const bool amb = P.m1 >= g.cutm2 || (sqrtf(P.m2) - d1) <= g.two_delta;
+    if (amb) {
+        const float t = d1 + g.two_delta;
+        const float thr = __fmul_ru(t, t);
+        float thr1 = -1.f, thr2 = -1.f;
+        if (P.r1 <= g.cutp2) { const float u = sqrtf(P.r1) + g.two_delta; thr1 = __fmul_ru(u, u); }
+        if (SELF && P.r2 <= g.cutp2) { const float u = sqrtf(P.r2) + g.two_delta; thr2 = __fmul_ru(u, u); }
+        if (!SELF) thr2 = INFINITY;
+        Exact64 E;
+        exact_warp<SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, thr, thr1, thr2, pi, total,
+                         lane, E);
+        records_from_exact<SELF>(S, E, s, v, r1, r2);
+        if (lane == 0) {
+            st.guard++;
+            st.guard_pairs += E.evals;
+            if (E.B.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(E.B)));
+        }
+        return;
+    }
+    // unambiguous: the FP32 minimum pair is the exact minimum pair, within cutoff
+    const int a = P.k1 / S.apv, b = P.k1 - a * S.apv;
+    int bin = bin32(g, d1);
+    double d64 = -1.0;
+    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
+        d64 = sqrt(pairs_one64(off64, im, qs64, qv64, os64[a], ov64[b]));
+        bin = setbin0(d64, S.binstep);
+        if (lane == 0) {
+            st.guard++;
+            st.guard_pairs += image_count(im);
+            st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
+        }
+    }
+    const int bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
+    r1.within = 1;
+    r1.i_local = a;
+    r1.j = v * S.apv + b;
+    r1.bin = bin;
+    r1.bulk = bulk;
+    if (SELF) {
+        r2.within = 1;
+        r2.i_local = b;
+        r2.j = (int64_t)s * S.aps + a;
+        r2.bin = bin;
+        r2.bulk = bulk;
+    }
+    // reference-atom rows (and columns in self mode)
+    for (int dir = 0; dir < (SELF ? 2 : 1); ++dir) {
+        const float rm = dir == 0 ? P.r1 : P.r2;
+        DirRec &r = dir == 0 ? r1 : r2;
+        if (rm > g.cutp2) continue;
+        const int rb = rm < g.cutm2 ? bin32(g, sqrtf(rm)) : -1;
+        if (rb >= 0) {
+            r.ref = 1;
+            r.rbin = rb;
+            continue;
+        }
+        const float u = sqrtf(rm) + g.two_delta;
+        const float thr = __fmul_ru(u, u);
+        Exact64 E;
+        exact_warp<SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, -1.f, dir == 0 ? thr : -1.f,
+                         dir == 1 ? thr : -1.f, pi, total, lane, E);
+        const double rr = dir == 0 ? E.rr1 : E.rr2;
+        if (lane == 0) {
+            st.guard++;
+            st.guard_pairs += E.evals;
+        }
+        if (rr <= S.cut2) {
+            r.ref = 1;
+            r.rbin = setbin0(sqrt(rr), S.binstep);
+        }
+    }
+}
+
+constexpr int kGuardWarps = 4;  // warps per CTA of k_pairs_guard
+
+template <bool SELF>
+__global__ void __launch_bounds__(kGuardWarps * 32) k_pairs_guard(DevSys S, Bufs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float4 s_os[kGuardWarps][kMaxSmallMol], s_ov[kGuardWarps][kMaxSmallMol];
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);
     __syncthreads();
     SHist h = shist_bind(S, hbase);
     LocalStats st;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int aps = S.aps, apv = S.apv;
+    PairIndex pi;
+    pi.per_img = aps * apv;
+    pi.aps = aps;
+    pi.inv_pi = 1.0f / (float)pi.per_img;
+    pi.inv_aps = 1.0f / (float)aps;
     const int n = min(B.counters[0], B.gq_cap);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = blockIdx.x * kGuardWarps + warp; i < n; i += gridDim.x * kGuardWarps) {
         const int4 it = B.gq[i];
         const int s = it.x, v = it.y, f = it.w;
         const PairsFrame Pf = pairs_frame(B, f, SELF);
         const FrameScratch &F = *Pf.F;
         const Images im = images_of(*Pf.G, F, it.z);
+        const int total = pi.per_img * image_count(im);
         const float4 qs32 = Pf.sq32[s], qv32 = Pf.vq32[v];
         const d4 qs64 = Pf.sq64[s], qv64 = Pf.vq64[v];
-        const float4 *os = Pf.so32 + (int64_t)s * S.aps;
-        const float4 *ov = Pf.vo32 + (int64_t)v * S.apv;
+        __syncwarp();
+        if (lane < aps) s_os[warp][lane] = Pf.so32[(int64_t)s * aps + lane];
+        if (lane < apv) s_ov[warp][lane] = Pf.vo32[(int64_t)v * apv + lane];
+        __syncwarp();
         Pass32 P;
-        pairs_pass32<SELF>(S, Pf.off32, im, qs32, qv32, os, ov, P);
+        pass32_warp<SELF>(S, Pf.off32, im, qs32, qv32, s_os[warp], s_ov[warp], pi, total, lane, P);
         DirRec r1, r2;
-        pairs_decide<SELF>(S, F.g, P, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, Pf.so64 + (int64_t)s * S.aps, os,
-                           Pf.vo64 + (int64_t)v * S.apv, ov, s, v, r1, r2, st);
-        emit<SELF>(S, h, r1, r2, s, v, Pf.slot, Pf.flags, st);
+        decide_warp<SELF>(S, F.g, P, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, Pf.so64 + (int64_t)s * aps, s_os[warp],
+                          Pf.vo64 + (int64_t)v * apv, s_ov[warp], s, v, pi, total, lane, r1, r2, st);
+        if (lane == 0) emit<SELF>(S, h, r1, r2, s, v, Pf.slot, Pf.flags, st);
     }
     stats_flush(S, st, false);
     __syncthreads();
