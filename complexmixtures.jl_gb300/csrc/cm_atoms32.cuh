@@ -402,6 +402,50 @@ __device__ __forceinline__ void atoms_walk_group(const FrameGeom &G, const Frame
     }
 }
 
+// Dense solutes (cell schedule): the group's walk box with the lanes probing
+// 32 cells at once; each kept cell carries the mask of the sites whose own
+// stencil keeps it (its box within the cutoff of the site), so every site
+// meets exactly the cells of its per-site walk, and the lanes then run over
+// each kept cell's atoms.  body(p, ox, oy, oz, mask).
+template <typename Body>
+__device__ __forceinline__ void atoms_walk_group_cells(const FrameGeom &G, const FrameScratch &F, const int *cs,
+                                                       const SiteGroup &sg, float prune2, const float4 *off32, int lane,
+                                                       Body &&body) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int x0 = sg.lo[0] - F.La[0], y0 = sg.lo[1] - F.La[1], z0 = sg.lo[2] - F.La[2];
+    const int nx = sg.hi[0] - x0 + F.La[0] + 1, ny = sg.hi[1] - y0 + F.La[1] + 1, nz = sg.hi[2] - z0 + F.La[2] + 1;
+    const int ncells = nx * ny * nz;
+    for (int c0 = 0; c0 < ncells; c0 += 32) {
+        const int ci = c0 + lane;
+        int beg = 0, end = 0;
+        unsigned mask = 0;
+        float4 of = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ci < ncells) {
+            const int dx = x0 + ci % nx, dy = y0 + (ci / nx) % ny, dz = z0 + ci / (nx * ny);
+            const int cell = (wrap_cell(sg.cz + dz, G.n[2]) * G.n[1] + wrap_cell(sg.cy + dy, G.n[1])) * G.n[0] +
+                             wrap_cell(sg.cx + dx, G.n[0]);
+            beg = cs[cell];
+            end = cs[cell + 1];
+            for (int j = 0; j < sg.ns; ++j) {
+                const float4 t = sg.site[j];
+                if (cell_d2(F, t.x, t.y, t.z, dx - unpack_d(t.w, 0), dy - unpack_d(t.w, 1), dz - unpack_d(t.w, 2)) <= prune2)
+                    mask |= 1u << j;
+            }
+            if (end > beg && mask) of = off32[off_index(dx, dy, dz)];
+        }
+        unsigned todo = __ballot_sync(kFull, end > beg && mask != 0);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int b0 = __shfl_sync(kFull, beg, src), e0 = __shfl_sync(kFull, end, src);
+            const unsigned m = __shfl_sync(kFull, mask, src);
+            const float ox = __shfl_sync(kFull, of.x, src), oy = __shfl_sync(kFull, of.y, src),
+                        oz = __shfl_sync(kFull, of.z, src);
+            for (int p = b0 + lane; p < e0; p += 32) body(p, ox, oy, oz, m);
+        }
+    }
+}
+
 // What the exact scan of one queued molecule pair reads.
 struct AtomsPair {
     const FrameGeom *G;
@@ -588,9 +632,37 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, CM_ATOMS_MIN_CTAS) k_atoms_e
                     });
                 }
             };
-            if constexpr (SCHED == kSchedBalanced) {
-                // sparse solutes: the sites of a group share one walk (dense solutes
-                // keep per-site stencils, whose cells each hold many atoms)
+            if constexpr (SCHED == kSchedCell) {
+                // dense solutes: the sites of a group probe their cells together and
+                // share each solute-atom load; a site meets only its own stencil's cells
+                for (int b0 = 0; b0 < apv; b0 += kSiteGroup) {
+                    const int ns = min(kSiteGroup, apv - b0);
+                    SiteGroup sg;
+                    if (!site_group(G, F, off32, vcell + vb, vq32 + vb, b0, ns, lane, s_site[threadIdx.x >> 5], sg)) {
+                        for (int b = b0; b < b0 + ns; ++b) one_site(b);
+                        continue;
+                    }
+                    auto pairs = [&](int p, float ox, float oy, float oz, unsigned m) {
+                        const float4 qa = sq32[p];
+                        const float ux = qa.x + ox, uy = qa.y + oy, uz = qa.z + oz;
+#pragma unroll
+                        for (int j = 0; j < kSiteGroup; ++j) {
+                            if (!((m >> j) & 1u)) continue;
+                            lane_evals++;
+                            const float ex = ux - sg.qx[j], ey = uy - sg.qy[j], ez = uz - sg.qz[j];
+                            const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                            T.m2 = fminf(T.m2, fmaxf(T.m1, d2));
+                            const bool lt = d2 < T.m1;
+                            T.p1 = lt ? p : T.p1;
+                            T.b1 = lt ? b0 + j : T.b1;
+                            T.m1 = fminf(T.m1, d2);
+                            if (b0 + j == iref) T.r1 = fminf(T.r1, d2);
+                        }
+                    };
+                    atoms_walk_group_cells(G, F, cs, sg, prune2, off32, lane, pairs);
+                }
+            } else if constexpr (SCHED == kSchedBalanced) {
+                // sparse solutes: the sites of a group share one walk
                 for (int b0 = 0; b0 < apv; b0 += kSiteGroup) {
                     const int ns = min(kSiteGroup, apv - b0);
                     SiteGroup sg;
