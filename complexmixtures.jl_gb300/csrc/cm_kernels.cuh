@@ -1479,17 +1479,42 @@ __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
     uint64_t rs = P.st;
     double A[9];
     draw_rotation(rs, A);
-    double cm[3];
-    matvec_cm(G.H, P.fc[0], P.fc[1], P.fc[2], cm);
+    // the new centre's cell c0 and its position q0 from that cell's origin
+    int c0[3];
+    double q0[3];
+    bin_fractional(G, P.fc, c0, q0);
+    const FrameScratch &F = B.FS[f];
+    const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
     const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
     for (int b = 0; b < S.apv; ++b) {
         const d4 w = u[b];
         double o[3];
         matvec_rm(A, w.x, w.y, w.z, o);
-        const double y0 = add(o[0], cm[0]), y1 = add(o[1], cm[1]), y2 = add(o[2], cm[2]);
-        int c[3];
+        // the atom from c0's origin; its cell is c0 shifted by the floor of its
+        // grid coordinates (FP32 picks the shift; the FP64 offset is taken from
+        // the shifted cell's origin, so the two stay consistent)
+        const double t[3] = {add(q0[0], o[0]), add(q0[1], o[1]), add(q0[2], o[2])};
+        const float tx = (float)t[0], ty = (float)t[1], tz = (float)t[2];
+        int dl[3], c[3];
+        bool in_table = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            dl[k] = (int)floorf(fmaf(F.hin[3 * k + 2], tz, fmaf(F.hin[3 * k + 1], ty, F.hin[3 * k] * tx)));
+            if (dl[k] < -kLT || dl[k] > kLT) in_table = false;
+            c[k] = wrap_cell(c0[k] + dl[k], G.n[k]);
+        }
         double q[3];
-        bin_position(G, y0, y1, y2, c, q);
+        if (in_table) {
+            const d4 ov = off64[off_index(dl[0], dl[1], dl[2])];
+            q[0] = sub(t[0], ov.x);
+            q[1] = sub(t[1], ov.y);
+            q[2] = sub(t[2], ov.z);
+        } else {
+            // a molecule much larger than a cell: bin its absolute position
+            double cm[3];
+            matvec_cm(G.H, P.fc[0], P.fc[1], P.fc[2], cm);
+            bin_position(G, add(o[0], cm[0]), add(o[1], cm[1]), add(o[2], cm[2]), c, q);
+        }
         B.pcell[base + b] = pack_cell(c);
         B.pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
         B.pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
