@@ -1476,14 +1476,38 @@ __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
     }
     const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
                                        B.nbulk + (int64_t)f * B.ndist);
-    uint64_t rs = P.st;
-    double A[9];
-    draw_rotation(rs, A);
     // the new centre's cell c0 and its position q0 from that cell's origin
     int c0[3];
     double q0[3];
     bin_fractional(G, P.fc, c0, q0);
     const FrameScratch &F = B.FS[f];
+    const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
+    {
+        // far slots: every atom lies within the molecule's radius rc of the
+        // centre, so its cell is in the box of cells that sphere touches; if no
+        // cell of the box is near the solute molecule the slot is not queued,
+        // and nothing reads its atoms
+        const float rc = B.rc[(int64_t)f * B.mv + P.jmol];
+        int lo[3], hi[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float g = (float)(P.fc[q] * (double)G.n[q]) - (float)c0[q];  // grid units inside the cell
+            const float reach = rc / F.cw[q] + 1e-3f;
+            lo[q] = (int)floorf(g - reach);
+            hi[q] = (int)floorf(g + reach);
+        }
+        bool maybe = false;
+        if (hi[0] - lo[0] >= G.n[0] || hi[1] - lo[1] >= G.n[1] || hi[2] - lo[2] >= G.n[2]) maybe = true;
+        for (int dz = lo[2]; dz <= hi[2] && !maybe; ++dz)
+            for (int dy = lo[1]; dy <= hi[1] && !maybe; ++dy)
+                for (int dx = lo[0]; dx <= hi[0] && !maybe; ++dx)
+                    maybe = nm[(wrap_cell(c0[2] + dz, G.n[2]) * G.n[1] + wrap_cell(c0[1] + dy, G.n[1])) * G.n[0] +
+                               wrap_cell(c0[0] + dx, G.n[0])] != 0;
+        if (!maybe) return;
+    }
+    uint64_t rs = P.st;
+    double A[9];
+    draw_rotation(rs, A);
     const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
     const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
     for (int b = 0; b < S.apv; ++b) {
@@ -1521,7 +1545,6 @@ __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
     }
     // queue the slot if one of its atoms lies in a near cell of the solute
     // molecule: (slot, placed sample, sample, 1)
-    const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
     bool near = false;
     for (int b = 0; b < S.apv && !near; ++b) {
         const int pc = B.pcell[base + b];
