@@ -331,12 +331,38 @@ def batched_c4_leg(cm, device):
             e.close()
         return time.perf_counter() - t, out, gst
 
+    def resident_batch(steps=3):
+        # the systems stay resident: engines and batch made once, frames on the
+        # device, each step one cm_batch_submit of every system's frames
+        dev = [(torch.as_tensor(xs, device=device), torch.as_tensor(xv, device=device), cells)
+               for xs, xv, cells, kw in systems]
+        engines = [cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, **kw) for xs, xv, cells, kw in systems]
+        with cm.Batch(engines) as b:
+            b.submit(dev)  # warm-up
+            for e in engines:
+                e.reset()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for _ in range(steps):
+                b.submit(dev)
+            for e in engines:
+                e.synchronize()
+            dt = time.perf_counter() - t
+        out = [e.raw_counts() for e in engines]
+        for e in engines:
+            e.close()
+        return dt / steps, out
+
     serial()  # warm-up
     ts, ref = serial()
     graph_batch()  # warm-up
     tg, gout, gst = graph_batch()
     same_graph = all(all(np.array_equal(gout[i][k], ref[i][k]) for k in ("md", "md_random", "solute_group"))
                      for i in range(len(systems)))
+    tr, rout = resident_batch()
+    # three steps of the same frames: each count is three times the one-pass count
+    same_resident = all(all(np.array_equal(rout[i][k], 3 * ref[i][k]) for k in ("md", "md_random", "solute_group"))
+                        for i in range(len(systems)))
     with cm.Server(device=device, frames_per_turn=C4_FRAMES) as srv:
         t0 = time.perf_counter()
         ids = [srv.submit(xs, xv, cells, cell_scale_pct=pct, atoms_schedule=sched, **kw) for xs, xv, cells, kw in systems]
@@ -354,6 +380,8 @@ def batched_c4_leg(cm, device):
         "graph_batch_frames_per_s": frames_total / tg,
         "graph_batch_launches": gst["graph_launches"],
         "graph_batch_counts_identical_to_serial": bool(same_graph),
+        "graph_batch_resident_frames_per_s": frames_total / tr,
+        "graph_batch_resident_counts_identical_to_serial": bool(same_resident),
         "p50_ms": pct_lat["p50"], "p99_ms": pct_lat["p99"],
         "cell_scale_pct": pct, "atoms_schedule": sched,
         "autotune_ms_per_frame": {f'{c["cell_scale_pct"]}/{c["atoms_schedule"]}': round(c["ms_per_frame"], 4)

@@ -640,6 +640,21 @@ __global__ void __launch_bounds__(kGuardWarps * 32) k_pairs_guard(DevSys S, Bufs
     shist_flush(S, h, false);
 }
 
+// FP32 squared distance of one atom pair, the smallest over the images,
+// formed as in the FP32 passes ((q_v - q_s) + off + offset of b - offset of a).
+__device__ __forceinline__ float edge_d2(const PairsFrame &Pf, const Images &im, int s, int v, float4 oa, float4 ob) {
+    const float4 qs = Pf.sq32[s], qv = Pf.vq32[v];
+    float best = INFINITY;
+    CM_FOR_IMAGES(im, dx, dy, dz) {
+        const float4 o = Pf.off32[off_index(dx, dy, dz)];
+        const float ex = (((qv.x - qs.x) + o.x) + ob.x) - oa.x;
+        const float ey = (((qv.y - qs.y) + o.y) + ob.y) - oa.y;
+        const float ez = (((qv.z - qs.z) + o.z) + ob.z) - oa.z;
+        best = fminf(best, fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
+    }
+    return best;
+}
+
 // Edge kernel: records whose closest atom pair is known from the FP32 pass
 // (second-closest pair beyond 2 delta, cutoff and dbulk clear) but whose md
 // bin, solvent reference-atom row or solute reference-atom column (marked -2)
@@ -678,17 +693,37 @@ __global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
             st.guard_pairs += nimg;
             st.maxerr = fmax(st.maxerr, fabs((double)d32 - d64));
         }
+        // a row or column minimum in the band: its FP32 pass picks the pairs
+        // within 2 delta of the FP32 minimum (the exact minimum is among them),
+        // which are then evaluated in FP64
+        const Guard &g = Pf.F->g;
         if (rb1 == -2) {
+            const float4 ob = Pf.vo32[(int64_t)v * S.apv + S.iref];
+            const float4 *os32 = Pf.so32 + (int64_t)s * S.aps;
+            float m = INFINITY;
+            for (int a = 0; a < S.aps; ++a) m = fminf(m, edge_d2(Pf, im, s, v, os32[a], ob));
+            const float t = sqrtf(m) + g.two_delta, thr = __fmul_ru(t, t);
             double rr = INFINITY;
-            for (int a = 0; a < S.aps; ++a) rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[a], ov[S.iref]));
+            for (int a = 0; a < S.aps; ++a) {
+                if (!(edge_d2(Pf, im, s, v, os32[a], ob) <= thr)) continue;
+                rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[a], ov[S.iref]));
+                st.guard_pairs += nimg;
+            }
             rb1 = rr <= S.cut2 ? setbin0(sqrt(rr), S.binstep) : -1;
-            st.guard_pairs += (unsigned long long)S.aps * nimg;
         }
         if (SELF && rb2 == -2) {
+            const float4 oa = Pf.so32[(int64_t)s * S.aps + S.iref];
+            const float4 *ov32 = Pf.vo32 + (int64_t)v * S.apv;
+            float m = INFINITY;
+            for (int b = 0; b < S.apv; ++b) m = fminf(m, edge_d2(Pf, im, s, v, oa, ov32[b]));
+            const float t = sqrtf(m) + g.two_delta, thr = __fmul_ru(t, t);
             double rr = INFINITY;
-            for (int b = 0; b < S.apv; ++b) rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[S.iref], ov[b]));
+            for (int b = 0; b < S.apv; ++b) {
+                if (!(edge_d2(Pf, im, s, v, oa, ov32[b]) <= thr)) continue;
+                rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[S.iref], ov[b]));
+                st.guard_pairs += nimg;
+            }
             rb2 = rr <= S.cut2 ? setbin0(sqrt(rr), S.binstep) : -1;
-            st.guard_pairs += (unsigned long long)S.apv * nimg;
         }
         apply_hit_local(S, h, false, bin, a1, (int64_t)v * S.apv + b1, b1, rb1 >= 0, rb1);
         st.hits++;

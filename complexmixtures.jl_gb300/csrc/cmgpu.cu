@@ -1004,8 +1004,8 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         if (special) {
             if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_guard<true><<<sms * 4, 128, hsm, st>>>(S, B));
             else CM_LAUNCH(CM_K_GUARD, k_pairs_guard<false><<<sms * 4, 128, hsm, st>>>(S, B));
-            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_edge<true><<<sms * 2, 128, hsm, st>>>(S, B));
-            else CM_LAUNCH(CM_K_GUARD, k_pairs_edge<false><<<sms * 2, 128, hsm, st>>>(S, B));
+            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_edge<true><<<sms * 4, 128, hsm, st>>>(S, B));
+            else CM_LAUNCH(CM_K_GUARD, k_pairs_edge<false><<<sms * 4, 128, hsm, st>>>(S, B));
         }
         if (rnd) {
             CM_LAUNCH(CM_K_BULK, k_bulk<<<c.ntab, 1024, 0, st>>>(S, B, dtab + c.tab0));
