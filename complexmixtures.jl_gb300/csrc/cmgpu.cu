@@ -1002,8 +1002,8 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         else if (self) CM_LAUNCH(CM_K_REAL, k_pairs_real<false, true><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
         else CM_LAUNCH(CM_K_REAL, k_pairs_real<false, false><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
         if (special) {
-            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_guard<true><<<sms * 4, 128, hsm, st>>>(S, B));
-            else CM_LAUNCH(CM_K_GUARD, k_pairs_guard<false><<<sms * 4, 128, hsm, st>>>(S, B));
+            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_guard<true><<<sms * 4, kGuardWarps * 32, hsm, st>>>(S, B));
+            else CM_LAUNCH(CM_K_GUARD, k_pairs_guard<false><<<sms * 4, kGuardWarps * 32, hsm, st>>>(S, B));
             if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_edge<true><<<sms * 4, 128, hsm, st>>>(S, B));
             else CM_LAUNCH(CM_K_GUARD, k_pairs_edge<false><<<sms * 4, 128, hsm, st>>>(S, B));
         }

@@ -212,6 +212,18 @@ def test_device_contributions_self_and_residues(cm, gpu_ready):
                      resnum=[1 + k // 10 for k in range(1463)])
     eng = R.engine
     try:
+        # the reference's decomposition identities through the device path
+        # (src/tools/contributions.jl:320-349): all solute atoms, the sum over
+        # residues, a partition of the KBI, all solvent atoms, one molecule x nmols
+        allp = list(range(1, 1464))
+        assert close(cm.contributions(R, cm.SoluteGroup(allp)), R.mddf)
+        rc_all = cm.ResidueContributions(R, atoms, dmin=0.0, dmax=100.0, silent=True)
+        assert close(sum(rc_all.residue_contributions), R.mddf)
+        kbi = cm.contributions(R, cm.SoluteGroup(allp[:700]), type="kbi") + cm.contributions(
+            R, cm.SoluteGroup(allp[700:]), type="kbi")
+        assert close(kbi, R.kb)
+        assert close(cm.contributions(R, cm.SolventGroup(list(range(4013, 10013)))), R.mddf)
+        assert close(R.solvent.nmols * cm.contributions(R, cm.SolventGroup([4013, 4014, 4015])), R.mddf)
         for type in ("mddf", "coordination_number"):
             dev = cm.ResidueContributions(R, atoms, dmin=0.0, dmax=10.0, type=type, silent=True)
             R.engine = None

@@ -100,3 +100,12 @@ def test_contributions_of_all_atoms_sum_to_the_mddf(cm, path):
     # one molecule's atoms: 1/nmols of the total (the reference's per-residue identity)
     one = cm.SolventGroup(list(R.solvent.indices[: R.solvent.natomspermol]))
     assert close(R.solvent.nmols * cm.contributions(R, one), R.mddf)
+    # the KB integral is the sum of the KBI contributions of a partition of the
+    # solute atoms (src/tools/contributions.jl:327-330); atoms of one molecule
+    # of a multi-molecule solute carry 1/nmols of it
+    half = R.solute.natomspermol // 2 or 1
+    mol = list(R.solute.indices[: R.solute.natomspermol])
+    parts = [cm.contributions(R, cm.SoluteGroup(mol[:half]), type="kbi")]
+    if mol[half:]:
+        parts.append(cm.contributions(R, cm.SoluteGroup(mol[half:]), type="kbi"))
+    assert close(R.solute.nmols * sum(parts), R.kb)
