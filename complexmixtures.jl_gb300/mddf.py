@@ -55,6 +55,24 @@ def engine_for(R: Result, options: Options, irefatom: int, *, coordination_numbe
     )
 
 
+def engine_stats_summary(st: dict) -> dict:
+    """The engine's statistics of one run, reported with its Result (not saved
+    with it): the FP32 search's guard band, how many minimum-distance records
+    it sent to the exact FP64 rules (count and rate per record within the
+    cutoff), and the largest FP32 distance error seen among them."""
+    hits = st["hits_real"] + st["hits_random"]
+    return {
+        "frames": st["frames"],
+        "atom_pairs_evaluated": st["atom_pairs_evaluated"],
+        "records_within_cutoff": hits,
+        "guard_reevaluations": st["guard_reevaluations"],
+        "guard_rate": st["guard_reevaluations"] / hits if hits else 0.0,
+        "max_fp32_error": st["max_guard_error"],
+        "guard_band": st["guard_band"],
+        "regime": "atoms" if st["regime"] == 2 else "pairs",
+    }
+
+
 def new_result(trajectory: Trajectory, options: Options, tmeta, frame_weights) -> Result:
     """Result constructor (src/results.jl:124-193)."""
     fw = check_frame_weights(frame_weights, options, tmeta.lastframe_read)
@@ -121,12 +139,14 @@ def mddf(trajectory, solute=None, solvent=None, options: Optional[Options] = Non
             res = eng.results(sum_frame_weights(R))
         else:
             c = eng.counts()
+        stats = eng.stats()
         ok = True
     finally:
         if not (ok and keep_engine):
             eng.close()
     if keep_engine:
         R.engine = eng
+    R.engine_stats = engine_stats_summary(stats)
     if finalize == "device":
         return _device_result(R, res, options, coordination_number_only)
     for k in ("md_count", "md_count_random", "rdf_count", "rdf_count_random", "solute_group_count",

@@ -31,6 +31,11 @@ def both(cm, traj_fn, opts, **kw):
         Rd = cm.mddf(traj_fn(), opts, finalize="device", **kw)
     for f in FIELDS:
         assert close(getattr(Rd, f), getattr(Rh, f)), f
+    # every Result reports its run's guard band, re-evaluation rate and largest FP32 error
+    for R in (Rh, Rd):
+        st = R.engine_stats
+        assert st["records_within_cutoff"] > 0 and 0.0 <= st["guard_rate"] < 1.0
+        assert 0.0 <= st["max_fp32_error"] <= st["guard_band"]
     assert close(Rd.volume.shell, Rh.volume.shell)
     for got, want in ((Rd.volume.total, Rh.volume.total), (Rd.volume.bulk, Rh.volume.bulk),
                       (Rd.volume.domain, Rh.volume.domain), (Rd.density.solute, Rh.density.solute),
