@@ -276,7 +276,7 @@ def serving_leg(cm, device):
     }
 
 
-C4_FRAMES = 8               # frames per config-4 system (config 4 has 50)
+C4_FRAMES = 50              # frames per config-4 system
 
 
 def batched_c4_leg(cm, device):
