@@ -199,6 +199,25 @@ class ResidueContributions:
         self.xticks = (list(self.resnums), [f"{key[1]}{key[0]}" for key, _ in residues])
         self.single = len(residues) == 1
 
+    def to_json(self) -> dict:
+        """The reference's JSON fields of a ResidueContributions."""
+        from .results import CURRENT_VERSION
+
+        return {"Version": ".".join(map(str, CURRENT_VERSION)), "d": [float(x) for x in self.d],
+                "residue_contributions": [[float(x) for x in c] for c in self.residue_contributions],
+                "resnums": [int(r) for r in self.resnums],
+                "xticks": [[int(x) for x in self.xticks[0]], [str(x) for x in self.xticks[1]]]}
+
+    @classmethod
+    def from_json(cls, D: dict) -> "ResidueContributions":
+        """Read back to_json's fields; one residue reads as a single-residue
+        object, as in the reference."""
+        curves = [np.asarray(c, dtype=np.float64) for c in D["residue_contributions"]]
+        if not curves:
+            raise ValueError("no residue contributions")
+        return cls(_parts=(np.asarray(D["d"], dtype=np.float64), curves, [int(r) for r in D["resnums"]],
+                           ([int(x) for x in D["xticks"][0]], [str(x) for x in D["xticks"][1]]), len(curves) == 1))
+
     def _new(self, curves, resnums=None, xticks=None, single=None):
         return ResidueContributions(_parts=(self.d.copy(), curves, list(self.resnums if resnums is None else resnums),
                                             (list((xticks or self.xticks)[0]), list((xticks or self.xticks)[1])),

@@ -396,22 +396,76 @@ def result_to_json(R: Result) -> dict:
     }
 
 
-def save(filename: str, R: Result) -> str:
-    """Write a Result as JSON that the reference's ``load`` reads
-    (src/results.jl:533-540); ``load`` here reads it back unchanged (floats
-    are written with enough digits to round-trip)."""
+CURRENT_VERSION = (2, 18, 3)
+
+
+def _version_tuple(v: str):
+    """(major, minor, patch) of a version string such as "2.18.3" or "2.18.3-DEV"."""
+    core = str(v).split("-")[0].split("+")[0]
+    parts = [int(x) for x in core.split(".")[:3]]
+    return tuple(parts + [0] * (3 - len(parts)))
+
+
+def check_version(filename: str) -> None:
+    """The reference's loading rules (src/io.jl:31-88): a file written by a
+    newer version, or by one older than 2.0.0, is an argument error."""
     import os
 
+    with open(os.path.expanduser(filename)) as f:
+        try:
+            v = json.load(f).get("Version", None)
+        except (json.JSONDecodeError, AttributeError):
+            return  # not JSON of a saved object: the loader reports it
+    if v is None:
+        return
+    jv = _version_tuple(v)
+    cur = ".".join(map(str, CURRENT_VERSION))
+    if jv > CURRENT_VERSION:
+        raise ValueError("Trying to load a json result file created with a newer version of ComplexMixtures. "
+                         f"This can cause unpredictable errors. Current version of ComplexMixtures: {cur}. "
+                         f"Version used to create the output .json file: {v}. Please update ComplexMixtures and try again.")
+    if jv < (2, 0, 0):
+        raise ValueError("Trying to load a json result created with an older, and incompatible, version of "
+                         f"ComplexMixtures. Current version of ComplexMixtures: {cur}. Version used to create the "
+                         f"output .json file: {v}.")
+
+
+def save(filename: str, R) -> str:
+    """Write a Result (or a ResidueContributions) as JSON that the reference's
+    ``load`` reads (src/results.jl:533-540, src/tools/residue_contributions.jl:486-492);
+    ``load`` here reads it back unchanged (floats are written with enough
+    digits to round-trip)."""
+    import os
+
+    from .contributions import ResidueContributions
+
     filename = os.path.expanduser(filename)
+    if isinstance(R, ResidueContributions):
+        with open(filename, "w") as f:
+            json.dump(R.to_json(), f, separators=(",", ":"), allow_nan=True)
+        return f"ResidueContributions saved in JSON file: {filename}"
     with open(filename, "w") as f:
         json.dump(result_to_json(R), f, separators=(",", ":"), allow_nan=True)
     return f"Results saved in JSON file: {filename}"
 
 
-def load(filename: str) -> Result:
-    """Read a Result saved by ``save`` or by the reference (src/results.jl:567-588)."""
+def load(filename: str, kind=None):
+    """Read a Result saved by ``save`` or by the reference (src/results.jl:567-588);
+    ``load(filename, ResidueContributions)`` reads residue contributions
+    (src/tools/residue_contributions.jl:509-528)."""
     import os
 
+    check_version(filename)
+    if kind is not None and kind is not Result:
+        from .contributions import ResidueContributions
+
+        if kind is not ResidueContributions:
+            raise ValueError(f"load: unsupported type {kind}")
+        try:
+            with open(os.path.expanduser(filename)) as f:
+                return ResidueContributions.from_json(json.load(f))
+        except (KeyError, TypeError, ValueError, json.JSONDecodeError) as e:
+            raise ValueError(f"The file {filename} does not appear to contain a ResidueContributions object.") from e
     try:
         return result_from_json(os.path.expanduser(filename))
     except (KeyError, TypeError, ValueError, json.JSONDecodeError) as e:

@@ -234,3 +234,27 @@ def test_device_contributions_self_and_residues(cm, gpu_ready):
                 assert close(a, b)
     finally:
         eng.close()
+
+
+def test_residue_contributions_save_load(cm, tmp_path):
+    """save / load of ResidueContributions and the version rules of the
+    reference's loader (src/tools/residue_contributions.jl:570-608)."""
+    import json
+
+    R = _result(cm)
+    rc = cm.ResidueContributions(R, _atoms(cm), silent=True)
+    f = tmp_path / "rc.json"
+    assert "saved" in cm.save(str(f), rc)
+    assert cm.load(str(f), cm.ResidueContributions) == rc
+    cm.save(str(f), rc[0])
+    one = cm.load(str(f), cm.ResidueContributions)
+    assert one == rc[0] and len(one) == len(rc.d)
+    f.write_text(json.dumps({"Version": "2.18.3"}))
+    with pytest.raises(ValueError, match="does not appear"):
+        cm.load(str(f), cm.ResidueContributions)
+    for version in ("1000.0.0", "1.0.0"):
+        D = rc.to_json()
+        D["Version"] = version
+        f.write_text(json.dumps(D))
+        with pytest.raises(ValueError, match="version"):
+            cm.load(str(f), cm.ResidueContributions)
