@@ -485,14 +485,33 @@ def other_workload(args, local):
     ms = e0.elapsed_time(e1)
     kt = eng.kernel_times()
     st = eng.stats()
+    raw32 = eng.raw_counts()
     eng.close()
     frames = args.steps * nframes
+    # the plain FP64 path on the same frames: its frames/s and the count comparison
+    eng64 = cm.Engine(precision="fp64", **kw)
+    s64 = torch.cuda.ExternalStream(eng64.stream_ptr(), device=f"cuda:{local}")
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s64)
+    for _ in range(args.steps):
+        eng64.submit(xd, vd, cells, frame_ids=ids)
+    b.record(s64)
+    b.synchronize()
+    ms64 = a.elapsed_time(b)
+    raw64 = eng64.raw_counts()
+    eng64.close()
+    hits = st["hits_real"] + st["hits_random"]
     print(json.dumps({
         "workload": args.workload, "metric": "MDDF frames/s", "value": frames / (ms / 1e3), "unit": "frames/s",
         "steps": args.steps, "warmup": args.warmup, "frames_per_step": nframes,
         "atoms": {"solute": int(sysm.solute_nmols * aps), "solvent": int(sv.nmols * sv.natomspermol)},
         "layout": "ATOMS" if st["regime"] == 2 else "PAIRS",
         "kernel_ms_per_frame": {k: v[0] / frames for k, v in kt.items()},
+        "guard": {"band_A": st["guard_band"], "reevaluations": st["guard_reevaluations"],
+                  "rate_per_record": st["guard_reevaluations"] / hits if hits else 0.0,
+                  "max_fp32_error_A": st["max_guard_error"]},
+        "plain_fp64": {"value": frames / (ms64 / 1e3), "unit": "frames/s",
+                       "counts_identical_to_fp32_guard": all(np.array_equal(raw32[k], raw64[k]) for k in raw32)},
         "precision": "fp32 search, fp64 guard band", "data": "synthetic (seeded generator of the configuration)",
     }), flush=True)
 
