@@ -30,7 +30,16 @@
 
 namespace cmk {
 
-constexpr int kFlatWarps = 16;   // warps per CTA (2 CTAs per SM at 64 registers)
+// One CTA of 32 warps per SM at 64 registers: the SM's 32 warps share one
+// privatised histogram (measured 3.8% faster on config 3 than 2 CTAs of 16
+// warps, each zeroing and flushing its own histogram).
+#ifndef CM_FLAT_WARPS
+#define CM_FLAT_WARPS 32
+#endif
+#ifndef CM_FLAT_MIN_CTAS
+#define CM_FLAT_MIN_CTAS 1
+#endif
+constexpr int kFlatWarps = CM_FLAT_WARPS;  // warps per CTA
 constexpr int kAtomQueue = 64;   // per-warp atom queue (float4: t, tag)
 
 struct CandSlot {
@@ -235,7 +244,7 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
 }
 
 template <bool SELF, int APS>
-__global__ void __launch_bounds__(kFlatWarps * 32, 2) k_pairs_flat32(DevSys S, Bufs B) {
+__global__ void __launch_bounds__(kFlatWarps * 32, CM_FLAT_MIN_CTAS) k_pairs_flat32(DevSys S, Bufs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
     const int hw = hist_words(S);
