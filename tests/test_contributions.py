@@ -258,3 +258,36 @@ def test_residue_contributions_save_load(cm, tmp_path):
         f.write_text(json.dumps(D))
         with pytest.raises(ValueError, match="version"):
             cm.load(str(f), cm.ResidueContributions)
+
+
+def test_argument_errors_of_the_reference(cm):
+    """The reference's contributions argument errors
+    (src/tools/contributions.jl:269-314), on a custom-group solute and a
+    per-atom solvent."""
+    custom = cm.AtomSelection.from_indices(list(range(1, 41)), nmols=1,
+                                           group_atom_indices=[[1, 2, 3], [4, 5], [6, 7, 8, 9], [10]],
+                                           group_names=["acidic", "basic", "polar", "nonpolar"])
+    water = cm.AtomSelection.from_indices(list(range(41, 71)), natomspermol=3, group_names=["OH2", "H1", "H2"])
+    R = cm.Result(nbins=5, dbulk=8.0, cutoff=10.0, autocorrelation=False, solute=custom, solvent=water, files=[],
+                  weights=[1.0])
+    R.solute_group_count[:] = 1.0
+    R.md_count_random[:] = 1.0
+    assert np.all(cm.contributions(R, cm.SoluteGroup("acidic"), type="md_count") == 1.0)
+    assert np.all(cm.contributions(R, cm.SoluteGroup(2), type="md_count") == 1.0)
+    bad = [
+        (cm.SolventGroup([41]), "wrong_type"),           # type must be one of the four
+        (cm.SoluteGroup([1, 2, 3]), "mddf"),             # custom groups: no atom indices
+        (cm.SoluteGroup(["N", "CA"]), "mddf"),           # custom groups: no atom names
+        (cm.SolventGroup("acidic"), "mddf"),             # no custom solvent groups: no group name
+        (cm.SolventGroup(1), "mddf"),                    # ... nor group index
+        (cm.SolventGroup([5000]), "mddf"),               # atom index not in the selection
+        (cm.SoluteGroup("NOT_FOUND"), "mddf"),           # group name not found
+        (cm.SoluteGroup(1000), "mddf"),                  # group index beyond the groups
+        (cm.SolventGroup([]), "mddf"),                   # empty selections
+        (cm.SolventGroup(["NOT_FOUND"]), "mddf"),        # atom name not found
+        (cm.SolventGroup([41, 41]), "mddf"),             # repeated indices
+        (cm.SolventGroup(["OH2", "OH2"]), "mddf"),       # repeated names
+    ]
+    for grp, kind in bad:
+        with pytest.raises(ValueError):
+            cm.contributions(R, grp, type=kind)
