@@ -291,3 +291,17 @@ def test_argument_errors_of_the_reference(cm):
     for grp, kind in bad:
         with pytest.raises(ValueError):
             cm.contributions(R, grp, type=kind)
+
+
+def test_residue_window_lengths_of_the_reference(cm):
+    """The reference's window sizes for binstep 0.02 and 500 bins
+    (src/tools/residue_contributions.jl:549-561): 101 distances between the
+    default dmin = 1.5 and dmax = 3.5, all 500 for dmin = 0 and dmax = 10."""
+    R = _result(cm, nb=500)
+    R.d = np.array([cm.shellradius(i, 0.02) for i in range(1, 501)])
+    atoms = _atoms(cm)
+    rc = cm.ResidueContributions(R, atoms, silent=True)
+    assert len(rc.d) == 101 and all(len(c) == 101 for c in rc.residue_contributions)
+    full = cm.ResidueContributions(R, atoms, dmin=0.0, dmax=10.0, silent=True)
+    assert len(full.d) == 500 and full.d[0] == R.d[0] and full.d[-1] == R.d[-1]
+    assert len(rc.xticks[0]) == len(rc.xticks[1]) == len(rc) == 8
