@@ -8,60 +8,9 @@ FP64, default and custom (overlapping) groups, and both bulk definitions.
 import numpy as np
 import pytest
 
-from helpers import golden, oracle_mddf
+from helpers import KEYS, ORTHO, TRICLINIC, compare, golden, make_system, oracle_mddf
 
 pytestmark = pytest.mark.gpu
-
-KEYS = ("md", "md_random", "rdf", "rdf_random", "solute_group", "solute_group_random", "solvent_group",
-        "solvent_group_random")
-
-TRICLINIC = np.array([[24.0, 12.0, 0.0], [0.0, 20.78460969082653, 0.0], [0.0, 0.0, 23.0]])
-ORTHO = np.diag([23.0, 25.0, 24.0])
-
-
-def make_system(rng, H, ms, aps, mv, apv, nframes, self_mode, spread=0.9):
-    def mols(n, apm):
-        c = rng.random((n, 1, 3)) @ H.T
-        return (c + rng.normal(scale=spread, size=(n, apm, 3))).reshape(-1, 3)
-
-    xs0 = mols(ms, aps)
-    xv0 = None if self_mode else mols(mv, apv)
-    xs = np.stack([xs0 + rng.normal(scale=0.15, size=xs0.shape) for _ in range(nframes)])
-    xv = None if self_mode else np.stack([xv0 + rng.normal(scale=0.15, size=xv0.shape) for _ in range(nframes)])
-    cells = np.repeat(H[None], nframes, axis=0)
-    return xs, xv, cells
-
-
-def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, regime, frame_ids=None, groups=None,
-            backend="cells", dtype=np.float64, cell_scale_pct=0, atoms_schedule="auto", **opt):
-    nf = xs.shape[0]
-    frame_ids = list(range(1, nf + 1)) if frame_ids is None else frame_ids
-    kw = dict(autocorrelation=self_mode, **opt)
-    g = {}
-    if groups == "custom":
-        # overlapping custom groups: atom j in groups j % 3 and 3 (+ a group of
-        # the first half of the atoms); solute side by local index
-        gs = [[a % 3, 3] + ([4] if a < aps // 2 else []) for a in range(aps)]
-        gv_rows = (lambda n, apm: [[j % 3, 3] + ([4] if (j % apm) < apm // 2 else []) for j in range(n)])
-        gv = gv_rows(mv * apv, apv)
-        g = dict(solute_groups=gs, solute_ngroups=5, solvent_groups=gv, solvent_ngroups=5)
-    eng = cm.Engine(solute_nmols=ms, solute_natomspermol=aps, solvent_nmols=mv, solvent_natomspermol=apv,
-                    precision=precision, regime=regime, max_frames_per_batch=2, cell_scale_pct=cell_scale_pct,
-                    atoms_schedule=atoms_schedule, **kw,
-                    **g)
-    eng.submit(xs.astype(dtype), None if self_mode else xv.astype(dtype), cells, frame_ids=frame_ids)
-    got = eng.raw_counts()
-    st = eng.stats()
-    eng.close()
-    ref = orc.run(ms=ms, aps=aps, mv=mv, apv=apv, solute_xyz=xs.astype(dtype).astype(np.float64),
-                  solvent_xyz=None if self_mode else xv.astype(dtype).astype(np.float64), cells=cells,
-                  frame_ids=frame_ids, backend=backend, **kw, **g)
-    for k in KEYS:
-        if self_mode and k.startswith("solvent"):
-            continue
-        assert np.array_equal(got[k], ref[k]), (k, np.nonzero(got[k] != ref[k]))
-    return got, ref, st
-
 
 COMMON = dict(binstep=0.02, nbins=350, seed=77)
 
