@@ -99,14 +99,24 @@ __global__ void k_atoms_filter(DevSys S, Bufs B, int64_t i0, int64_t n) {
     if (atoms_near(B, G, f, s, B.avcell + (int64_t)f * B.Nv + (int64_t)v * S.apv, S.apv)) atoms_push(S, B, make_int4(v, s, f, 0));
 }
 
-// FP32 top-2 of one lane.
-struct Top2 {
-    float m1, m2, r1;
+// Top-2 of one lane in the search precision R.
+template <typename R>
+struct Top2T {
+    R m1, m2, r1;
     int p1, b1;
 };
+using Top2 = Top2T<float>;
 
-__device__ __forceinline__ void top2_merge(Top2 &A, const Top2 &Bt) {
-    const float m2 = fminf(fmaxf(A.m1, Bt.m1), fminf(A.m2, Bt.m2));
+template <typename R>
+__device__ __forceinline__ void top2_init(Top2T<R> &T) {
+    T.m1 = T.m2 = T.r1 = (R)INFINITY;
+    T.p1 = 0x7fffffff;
+    T.b1 = 0;
+}
+
+template <typename R>
+__device__ __forceinline__ void top2_merge(Top2T<R> &A, const Top2T<R> &Bt) {
+    const R m2 = r_min(r_max(A.m1, Bt.m1), r_min(A.m2, Bt.m2));
     const bool take = Bt.m1 < A.m1 || (Bt.m1 == A.m1 && (Bt.p1 < A.p1 || (Bt.p1 == A.p1 && Bt.b1 < A.b1)));
     if (take) {
         A.m1 = Bt.m1;
@@ -114,13 +124,14 @@ __device__ __forceinline__ void top2_merge(Top2 &A, const Top2 &Bt) {
         A.b1 = Bt.b1;
     }
     A.m2 = m2;
-    A.r1 = fminf(A.r1, Bt.r1);
+    A.r1 = r_min(A.r1, Bt.r1);
 }
 
-__device__ __forceinline__ void top2_reduce(Top2 &T) {
+template <typename R>
+__device__ __forceinline__ void top2_reduce(Top2T<R> &T) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        Top2 U;
+        Top2T<R> U;
         U.m1 = __shfl_xor_sync(0xffffffffu, T.m1, o);
         U.m2 = __shfl_xor_sync(0xffffffffu, T.m2, o);
         U.r1 = __shfl_xor_sync(0xffffffffu, T.r1, o);
@@ -466,47 +477,187 @@ struct AtomsPair {
     const int *cs;
     int64_t vb;
     float prune2;
+    // the pair, for the exact distances: frame, solute molecule, solvent
+    // molecule or slot, and for a random slot its sample
+    int f, s, v, sample;
+    bool random;
 };
+
+__device__ __forceinline__ const d4 *sq_of(const AtomsPair &A, double) { return A.sq64; }
+__device__ __forceinline__ const float4 *sq_of(const AtomsPair &A, float) { return A.sq32; }
+__device__ __forceinline__ const d4 *vq_of(const AtomsPair &A, double) { return A.vq64; }
+__device__ __forceinline__ const float4 *vq_of(const AtomsPair &A, float) { return A.vq32; }
+__device__ __forceinline__ const d4 *off_of(const AtomsPair &A, double) { return A.off64; }
+__device__ __forceinline__ const float4 *off_of(const AtomsPair &A, float) { return A.off32; }
+
+// The pair's molecules for the exact distances; a random slot's placement is
+// drawn again from its stream (the same draws as k_atoms_place).
+__device__ __noinline__ ExactMol atoms_exact_mol(const DevSys &S, const Bufs &B, const AtomsPair &A) {
+    if (!A.random) return exact_mol(S, A.f, A.s, A.v);
+    const Sample sm = B.samples[A.sample];
+    const Placement P = draw_placement(S, A.G->frame_id, sm, A.v, B.bulk + (int64_t)A.f * B.ndist * B.mv,
+                                       B.nbulk + (int64_t)A.f * B.ndist);
+    uint64_t st = P.st;
+    double R[9];
+    draw_rotation(st, R);
+    return exact_mol_placed(S, *A.G, A.f, A.s, P.jmol, P.fc, R);
+}
 
 // Exact scan of a molecule pair; STRIDE 32: lanes over the atoms of each cell
 // (the whole warp calls it, the result is reduced over the lanes); STRIDE 1:
-// one thread.  With `filter` only pairs whose FP32 squared distance is within
-// the thresholds are evaluated in FP64.  Out of line: it runs only in
-// the FP64 engine path and for records inside the guard band, and keeps its
-// registers away from the FP32 loop.
-template <int STRIDE>
-__device__ __noinline__ void atoms_exact(const DevSys &S, const AtomsPair &A, int lane, bool filter, float thr_arg,
-                                         float thr_r1, Best64 &Bst, double &rr1, long long &evals) {
+// one thread.  Only the pairs whose squared distance in the search precision
+// R is within the thresholds are evaluated exactly (exact_d2 on the input
+// coordinates).  Out of line: it runs only for records inside the guard band,
+// and keeps its registers away from the search loops.
+template <int STRIDE, typename R>
+__device__ __noinline__ void atoms_exact(const DevSys &S, const Bufs &B, const AtomsPair &A, int lane, R thr_arg, R thr_r1,
+                                         Best64 &Bst, double &rr1, long long &evals) {
+    using V = typename Vec4T<R>::type;
     best_init(Bst);
     rr1 = INFINITY;
     evals = 0;
     const int apv = S.apv, iref = S.iref;
+    const V *sq = sq_of(A, (R)0), *vq = vq_of(A, (R)0), *off = off_of(A, (R)0);
+    ExactMol X = atoms_exact_mol(S, B, A);
     for (int b = 0; b < apv; ++b) {
         const Site sb = site_of(*A.F, A.vcell[A.vb + b], A.vq32[A.vb + b]);
-        const d4 qb = A.vq64[A.vb + b];
+        const V qb = vq[A.vb + b];
+        double yb[3];
+        bool have_y = false;
         atoms_walk(*A.G, *A.F, A.cs, sb, A.prune2, [&](int beg, int end, int oi) {
-            const d4 o = A.off64[oi];
-            const double tx = sub(qb.x, o.x), ty = sub(qb.y, o.y), tz = sub(qb.z, o.z);
-            const float4 of = A.off32[oi];
-            const float fx = sb.q.x - of.x, fy = sb.q.y - of.y, fz = sb.q.z - of.z;
+            const V o = off[oi];
+            const R tx = (R)qb.x - (R)o.x, ty = (R)qb.y - (R)o.y, tz = (R)qb.z - (R)o.z;
             for (int p = beg + lane; p < end; p += STRIDE) {
-                const float4 qa32 = A.sq32[p];
-                if (filter) {
-                    const float ex = qa32.x - fx, ey = qa32.y - fy, ez = qa32.z - fz;
-                    const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                    if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1))) continue;
+                const V qa = sq[p];
+                const R d2f = sq3((R)qa.x - tx, (R)qa.y - ty, (R)qa.z - tz);
+                if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1))) continue;
+                if (!have_y) {
+                    exact_solvent_atom(B, *A.G, X, b, yb);
+                    have_y = true;
                 }
-                const d4 qa = A.sq64[p];
-                const double d2 = pair_d2_64(tx, ty, tz, qa.x, qa.y, qa.z);
+                const int a = __float_as_int(A.sq32[p].w);
+                double xa[3];
+                exact_solute_atom(B, X, a, xa);
+                const double d2 = exact_d2(*A.G, xa, yb);
                 evals++;
                 if (d2 <= S.cut2) {
                     if (b == iref) rr1 = fmin(rr1, d2);
-                    best_update<false>(Bst, d2, __float_as_int(qa32.w), b);
+                    best_update<false>(Bst, d2, a, b);
                 }
             }
         });
     }
     if (STRIDE == 32) best_reduce(Bst, rr1, evals);
+}
+
+// FP64 search of a molecule pair (the FP64 engine path): each site's stencil
+// cells, every solute atom in them, squared distances from the FP64
+// cell-relative positions; top-2 per lane, reduced over the warp for STRIDE 32.
+template <int STRIDE>
+__device__ __noinline__ Top2T<double> atoms_pass64(const DevSys &S, const AtomsPair &A, int lane, long long &evals) {
+    Top2T<double> T;
+    top2_init(T);
+    const int apv = S.apv, iref = S.iref;
+    for (int b = 0; b < apv; ++b) {
+        const Site sb = site_of(*A.F, A.vcell[A.vb + b], A.vq32[A.vb + b]);
+        const d4 qb = A.vq64[A.vb + b];
+        const bool isref = b == iref;
+        atoms_walk(*A.G, *A.F, A.cs, sb, A.prune2, [&](int beg, int end, int oi) {
+            const d4 o = A.off64[oi];
+            const double tx = qb.x - o.x, ty = qb.y - o.y, tz = qb.z - o.z;
+            for (int p = beg + lane; p < end; p += STRIDE) {
+                const d4 qa = A.sq64[p];
+                const double d2 = sq3(qa.x - tx, qa.y - ty, qa.z - tz);
+                evals++;
+                T.m2 = fmin(T.m2, fmax(T.m1, d2));
+                const bool lt = d2 < T.m1;
+                T.p1 = lt ? p : T.p1;
+                T.b1 = lt ? b : T.b1;
+                T.m1 = fmin(T.m1, d2);
+                if (isref) T.r1 = fmin(T.r1, d2);
+            }
+        });
+    }
+    if (STRIDE == 32) top2_reduce(T);
+    return T;
+}
+
+// The record of a molecule pair from its search's top-2 (precision R): taken
+// from the search where every value is farther than the band from its
+// decision boundary, otherwise from exact distances.  With STRIDE 32 every
+// lane holds the same T and takes the same branches.
+template <int STRIDE, typename R>
+__device__ __noinline__ DirRec atoms_decide(const DevSys &S, const Bufs &B, const AtomsPair &A, const GuardT<R> &g, const Top2T<R> &T,
+                               int lane, LocalStats &st) {
+    DirRec r = dir_none(S);
+    if (!(T.m1 <= g.cutp2)) return r;
+    auto from_exact = [&](Best64 &Bst, double rr1) {
+        DirRec q = dir_none(S);
+        if (Bst.d2 <= S.cut2) {
+            const double d = best_d(Bst);
+            q.within = 1;
+            q.i_local = Bst.a;
+            q.j = A.vb + Bst.b;
+            q.bin = setbin0(d, S.binstep);
+            q.bulk = inbulk64(S, true, d);
+            if (rr1 <= S.cut2) { q.ref = 1; q.rbin = setbin0(sqrt(rr1), S.binstep); }
+        }
+        return q;
+    };
+    const R d1 = r_sqrt(T.m1);
+    const bool amb = T.m1 >= g.cutm2 || (r_sqrt(T.m2) - d1) <= g.two_delta;
+    if (amb) {
+        R thr1 = (R)-1;
+        if (T.r1 <= g.cutp2) thr1 = r_sq_ru(r_sqrt(T.r1) + g.two_delta);
+        Best64 Bst;
+        double rr1;
+        long long ev;
+        atoms_exact<STRIDE, R>(S, B, A, lane, r_sq_ru(d1 + g.two_delta), thr1, Bst, rr1, ev);
+        r = from_exact(Bst, rr1);
+        if (lane == 0) {
+            st.guard++;
+            st.guard_pairs += ev;
+            if (Bst.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(Bst)));
+        }
+        return r;
+    }
+    // unambiguous: the search's minimum pair is the exact minimum pair
+    int bin = bin_of(g, d1);
+    double d64 = -1.0;
+    const int a1 = __float_as_int(A.sq32[T.p1].w);
+    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
+        ExactMol X = atoms_exact_mol(S, B, A);
+        d64 = sqrt(exact_pair_d2(B, *A.G, X, a1, T.b1));
+        bin = setbin0(d64, S.binstep);
+        if (lane == 0) {
+            st.guard++;
+            st.guard_pairs++;
+            st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
+        }
+    }
+    r.within = 1;
+    r.i_local = a1;
+    r.j = A.vb + T.b1;
+    r.bin = bin;
+    r.bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
+    if (T.r1 <= g.cutp2) {
+        const int rb = T.r1 < g.cutm2 ? bin_of(g, r_sqrt(T.r1)) : -1;
+        if (rb >= 0) {
+            r.ref = 1;
+            r.rbin = rb;
+        } else {
+            Best64 Bst;
+            double rr1;
+            long long ev;
+            atoms_exact<STRIDE, R>(S, B, A, lane, (R)-1, r_sq_ru(r_sqrt(T.r1) + g.two_delta), Bst, rr1, ev);
+            if (lane == 0) {
+                st.guard++;
+                st.guard_pairs += ev;
+            }
+            if (rr1 <= S.cut2) { r.ref = 1; r.rbin = setbin0(sqrt(rr1), S.binstep); }
+        }
+    }
+    return r;
 }
 
 // Schedules of k_atoms_eval.  CELL: one warp per queue entry, the lanes over
@@ -583,35 +734,19 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, CM_ATOMS_MIN_CTAS) k_atoms_e
         A.cs = cs;
         A.vb = vb;
         A.prune2 = prune2;
-        auto exact = [&](bool filter, float thr_arg, float thr_r1, Best64 &Bst, double &rr1, long long &evals) {
-            atoms_exact<STRIDE>(S, A, lane, filter, thr_arg, thr_r1, Bst, rr1, evals);
-        };
-        auto from_exact = [&](Best64 &Bst, double rr1) {
-            DirRec q = dir_none(S);
-            if (Bst.d2 <= S.cut2) {
-                const double d = best_d(Bst);
-                q.within = 1;
-                q.i_local = Bst.a;
-                q.j = vb + Bst.b;
-                q.bin = setbin0(d, S.binstep);
-                q.bulk = inbulk64(S, true, d);
-                if (rr1 <= S.cut2) { q.ref = 1; q.rbin = setbin0(sqrt(rr1), S.binstep); }
-            }
-            return q;
-        };
+        A.f = f;
+        A.s = s;
+        A.v = v;
+        A.sample = RANDOM ? e.z : -1;
+        A.random = RANDOM;
         DirRec r = dir_none(S);
         long long lane_evals = 0;
         if (!FP32) {
-            Best64 Bst;
-            double rr1;
-            exact(false, 0.f, 0.f, Bst, rr1, lane_evals);
-            r = from_exact(Bst, rr1);
-            if (lane != 0) lane_evals = 0;  // the reduction left the total in every lane
+            const Top2T<double> T = atoms_pass64<STRIDE>(S, A, lane, lane_evals);
+            r = atoms_decide<STRIDE, double>(S, B, A, F.g64, T, lane, st);
         } else {
             Top2 T;
-            T.m1 = T.m2 = T.r1 = INFINITY;
-            T.p1 = 0x7fffffff;
-            T.b1 = 0;
+            top2_init(T);
             // one site with its own stencil walk
             auto one_site = [&](int b) {
                 const Site sb = site_of(F, vcell[vb + b], vq32[vb + b]);
@@ -700,81 +835,7 @@ __global__ void __launch_bounds__(kAtomsWarps * 32, CM_ATOMS_MIN_CTAS) k_atoms_e
                 for (int b = 0; b < apv; ++b) one_site(b);
             }
             if (WARP) top2_reduce(T);
-            if (T.m1 <= g.cutp2) {
-                const float d1 = sqrtf(T.m1);
-                const bool amb = T.m1 >= g.cutm2 || (sqrtf(T.m2) - d1) <= g.two_delta;
-                if (amb) {
-                    const float t = d1 + g.two_delta;
-                    float thr1 = -1.f;
-                    if (T.r1 <= g.cutp2) {
-                        const float u = sqrtf(T.r1) + g.two_delta;
-                        thr1 = __fmul_ru(u, u);
-                    }
-                    Best64 Bst;
-                    double rr1;
-                    long long ev;
-                    exact(true, __fmul_ru(t, t), thr1, Bst, rr1, ev);
-                    r = from_exact(Bst, rr1);
-                    if (lane == 0) {
-                        st.guard++;
-                        st.guard_pairs += ev;
-                        if (Bst.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(Bst)));
-                    }
-                } else {
-                    int bin = bin32(g, d1);
-                    double d64 = -1.0;
-                    const float4 qa32 = sq32[T.p1];
-                    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
-                        // exact distance of the minimum pair over the stencil
-                        // images that hold its solute atom
-                        const int pk = vcell[vb + T.b1];
-                        const int cx = pk & 1023, cy = (pk >> 10) & 1023, cz = (pk >> 20) & 1023;
-                        const d4 qb = vq64[vb + T.b1];
-                        const d4 qa = sq64[T.p1];
-                        double best = INFINITY;
-                        for (int dz = -F.La[2]; dz <= F.La[2]; ++dz)
-                            for (int dy = -F.La[1]; dy <= F.La[1]; ++dy)
-                                for (int dx = -F.La[0]; dx <= F.La[0]; ++dx) {
-                                    const int cell = (wrap_cell(cz + dz, G.n[2]) * G.n[1] + wrap_cell(cy + dy, G.n[1])) * G.n[0] +
-                                                     wrap_cell(cx + dx, G.n[0]);
-                                    if (T.p1 < cs[cell] || T.p1 >= cs[cell + 1]) continue;
-                                    const d4 o = off64[off_index(dx, dy, dz)];
-                                    best = fmin(best, pair_d2_64(sub(qb.x, o.x), sub(qb.y, o.y), sub(qb.z, o.z), qa.x, qa.y,
-                                                                 qa.z));
-                                }
-                        d64 = sqrt(best);
-                        bin = setbin0(d64, S.binstep);
-                        if (lane == 0) {
-                            st.guard++;
-                            st.guard_pairs++;
-                            st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
-                        }
-                    }
-                    r.within = 1;
-                    r.i_local = __float_as_int(qa32.w);
-                    r.j = vb + T.b1;
-                    r.bin = bin;
-                    r.bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
-                    if (T.r1 <= g.cutp2) {
-                        const int rb = T.r1 < g.cutm2 ? bin32(g, sqrtf(T.r1)) : -1;
-                        if (rb >= 0) {
-                            r.ref = 1;
-                            r.rbin = rb;
-                        } else {
-                            const float u = sqrtf(T.r1) + g.two_delta;
-                            Best64 Bst;
-                            double rr1;
-                            long long ev;
-                            exact(true, -1.f, __fmul_ru(u, u), Bst, rr1, ev);
-                            if (lane == 0) {
-                                st.guard++;
-                                st.guard_pairs += ev;
-                            }
-                            if (rr1 <= S.cut2) { r.ref = 1; r.rbin = setbin0(sqrt(rr1), S.binstep); }
-                        }
-                    }
-                }
-            }
+            r = atoms_decide<STRIDE, float>(S, B, A, g, T, lane, st);
         }
         st.atompairs += (unsigned long long)lane_evals;
         if (lane == 0) {

@@ -447,13 +447,13 @@ __device__ __forceinline__ void pass32_warp(const DevSys &S, const float4 *__res
     }
 }
 
-// pairs_exact<true, SELF> with the pairs split over the lanes, merged over the
-// warp; every lane ends with the result.
+// pairs_exact with the pairs split over the lanes (FP32 filter), merged over
+// the warp; every lane ends with the result.
 template <bool SELF>
-__device__ void exact_warp(const DevSys &S, const d4 *__restrict__ off64, const float4 *__restrict__ off32, const Images &im,
-                           d4 qs64, float4 qs32, d4 qv64, float4 qv32, const d4 *os64, const float4 *os32, const d4 *ov64,
-                           const float4 *ov32, float thr_arg, float thr_r1, float thr_r2, const PairIndex &pi, int total,
-                           int lane, Exact64 &E) {
+__device__ void exact_warp(const DevSys &S, const FrameGeom &G, const Bufs &B, ExactMol &X,
+                           const float4 *__restrict__ off32, const Images &im, float4 qs32, float4 qv32,
+                           const float4 *os32, const float4 *ov32, float thr_arg, float thr_r1, float thr_r2,
+                           const PairIndex &pi, int total, int lane, Exact64 &E) {
     constexpr unsigned kFull = 0xffffffffu;
     best_init(E.B);
     E.rr1 = INFINITY;
@@ -462,7 +462,6 @@ __device__ void exact_warp(const DevSys &S, const d4 *__restrict__ off64, const 
     const int iref = S.iref;
     const double cut2 = S.cut2;
     int cur = -1;
-    double Dx = 0.0, Dy = 0.0, Dz = 0.0;
     float Fx = 0.f, Fy = 0.f, Fz = 0.f;
     for (int i = lane; i < total; i += 32) {
         int img, b, a;
@@ -470,23 +469,17 @@ __device__ void exact_warp(const DevSys &S, const d4 *__restrict__ off64, const 
         if (img != cur) {
             int dx, dy, dz;
             image_at(im, img, dx, dy, dz);
-            const int oi = off_index(dx, dy, dz);
-            const float4 of = off32[oi];
+            const float4 of = off32[off_index(dx, dy, dz)];
             Fx = (qv32.x - qs32.x) + of.x;
             Fy = (qv32.y - qs32.y) + of.y;
             Fz = (qv32.z - qs32.z) + of.z;
-            const d4 o = off64[oi];
-            Dx = add(sub(qv64.x, qs64.x), o.x);
-            Dy = add(sub(qv64.y, qs64.y), o.y);
-            Dz = add(sub(qv64.z, qs64.z), o.z);
             cur = img;
         }
         const float4 ob32 = ov32[b], oa32 = os32[a];
         const float ex = (Fx + ob32.x) - oa32.x, ey = (Fy + ob32.y) - oa32.y, ez = (Fz + ob32.z) - oa32.z;
         const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
         if (!(d2f <= thr_arg || (b == iref && d2f <= thr_r1) || (SELF && a == iref && d2f <= thr_r2))) continue;
-        const d4 ob = ov64[b], oa = os64[a];
-        const double d2 = pair_d2_64(add(Dx, ob.x), add(Dy, ob.y), add(Dz, ob.z), oa.x, oa.y, oa.z);
+        const double d2 = exact_pair_d2(B, G, X, a, b);
         E.evals++;
         if (d2 <= cut2) {
             if (b == iref) E.rr1 = fmin(E.rr1, d2);
@@ -524,10 +517,10 @@ __device__ void exact_warp(const DevSys &S, const d4 *__restrict__ off64, const 
 // pairs_decide with the warp-parallel pass and scans; the statistics are
 // counted on lane 0.
 template <bool SELF>
-__device__ void decide_warp(const DevSys &S, const Guard &g, const Pass32 &P, const d4 *__restrict__ off64,
-                            const float4 *__restrict__ off32, const Images &im, d4 qs64, float4 qs32, d4 qv64, float4 qv32,
-                            const d4 *os64, const float4 *os32, const d4 *ov64, const float4 *ov32, int s, int64_t v,
-                            const PairIndex &pi, int total, int lane, DirRec &r1, DirRec &r2, LocalStats &st) {
+__device__ void decide_warp(const DevSys &S, const FrameGeom &G, const Bufs &B, ExactMol &X, const Guard &g,
+                            const Pass32 &P, const float4 *__restrict__ off32, const Images &im, float4 qs32, float4 qv32,
+                            const float4 *os32, const float4 *ov32, int s, int64_t v, const PairIndex &pi, int total,
+                            int lane, DirRec &r1, DirRec &r2, LocalStats &st) {
     r1 = dir_none(S);
     r2 = dir_none(S);
     if (P.m1 > g.cutp2) return;
@@ -541,8 +534,7 @@ __device__ void decide_warp(const DevSys &S, const Guard &g, const Pass32 &P, co
         if (SELF && P.r2 <= g.cutp2) { const float u = sqrtf(P.r2) + g.two_delta; thr2 = __fmul_ru(u, u); }
         if (!SELF) thr2 = INFINITY;
         Exact64 E;
-        exact_warp<SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, thr, thr1, thr2, pi, total,
-                         lane, E);
+        exact_warp<SELF>(S, G, B, X, off32, im, qs32, qv32, os32, ov32, thr, thr1, thr2, pi, total, lane, E);
         records_from_exact<SELF>(S, E, s, v, r1, r2);
         if (lane == 0) {
             st.guard++;
@@ -556,11 +548,11 @@ __device__ void decide_warp(const DevSys &S, const Guard &g, const Pass32 &P, co
     int bin = bin32(g, d1);
     double d64 = -1.0;
     if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
-        d64 = sqrt(pairs_one64(off64, im, qs64, qv64, os64[a], ov64[b]));
+        d64 = sqrt(exact_pair_d2(B, G, X, a, b));
         bin = setbin0(d64, S.binstep);
         if (lane == 0) {
             st.guard++;
-            st.guard_pairs += image_count(im);
+            st.guard_pairs += 1;
             st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
         }
     }
@@ -591,8 +583,8 @@ __device__ void decide_warp(const DevSys &S, const Guard &g, const Pass32 &P, co
         const float u = sqrtf(rm) + g.two_delta;
         const float thr = __fmul_ru(u, u);
         Exact64 E;
-        exact_warp<SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, -1.f, dir == 0 ? thr : -1.f,
-                         dir == 1 ? thr : -1.f, pi, total, lane, E);
+        exact_warp<SELF>(S, G, B, X, off32, im, qs32, qv32, os32, ov32, -1.f, dir == 0 ? thr : -1.f, dir == 1 ? thr : -1.f,
+                         pi, total, lane, E);
         const double rr = dir == 0 ? E.rr1 : E.rr2;
         if (lane == 0) {
             st.guard++;
@@ -632,7 +624,6 @@ __global__ void __launch_bounds__(kGuardWarps * 32) k_pairs_guard(DevSys S, Bufs
         const Images im = images_of(*Pf.G, F, it.z);
         const int total = pi.per_img * image_count(im);
         const float4 qs32 = Pf.sq32[s], qv32 = Pf.vq32[v];
-        const d4 qs64 = Pf.sq64[s], qv64 = Pf.vq64[v];
         __syncwarp();
         if (lane < aps) s_os[warp][lane] = Pf.so32[(int64_t)s * aps + lane];
         if (lane < apv) s_ov[warp][lane] = Pf.vo32[(int64_t)v * apv + lane];
@@ -640,8 +631,9 @@ __global__ void __launch_bounds__(kGuardWarps * 32) k_pairs_guard(DevSys S, Bufs
         Pass32 P;
         pass32_warp<SELF>(S, Pf.off32, im, qs32, qv32, s_os[warp], s_ov[warp], pi, total, lane, P);
         DirRec r1, r2;
-        decide_warp<SELF>(S, F.g, P, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, Pf.so64 + (int64_t)s * aps, s_os[warp],
-                          Pf.vo64 + (int64_t)v * apv, s_ov[warp], s, v, pi, total, lane, r1, r2, st);
+        ExactMol X = exact_mol(S, f, s, v);
+        decide_warp<SELF>(S, *Pf.G, B, X, F.g, P, Pf.off32, im, qs32, qv32, s_os[warp], s_ov[warp], s, v, pi, total, lane, r1,
+                          r2, st);
         if (lane == 0) emit<SELF>(S, h, r1, r2, s, v, Pf.slot, Pf.flags, st);
     }
     stats_flush(S, st, false);
@@ -668,10 +660,9 @@ __device__ __forceinline__ float edge_d2(const PairsFrame &Pf, const Images &im,
 // (second-closest pair beyond 2 delta, cutoff and dbulk clear) but whose md
 // bin, solvent reference-atom row or solute reference-atom column (marked -2)
 // lies within the guard band of a bin edge or of the cutoff.  Each marked
-// value comes from FP64 pair distances formed as in the exact scan: the
-// closest pair for the md bin, the aps pairs of the solvent molecule's
-// reference atom for the row, the apv pairs of the solute molecule's
-// reference atom for the column.
+// value comes from exact pair distances (exact_d2): the closest pair for the
+// md bin, the aps pairs of the solvent molecule's reference atom for the row,
+// the apv pairs of the solute molecule's reference atom for the column.
 template <bool SELF>
 __global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -689,22 +680,20 @@ __global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
         const float d32 = __int_as_float(y.x);
         const PairsFrame Pf = pairs_frame(B, f, SELF);
         const Images im = images_of(*Pf.G, *Pf.F, e.z);
-        const d4 qs = Pf.sq64[s], qv = Pf.vq64[v];
-        const d4 *os = Pf.so64 + (int64_t)s * S.aps;
-        const d4 *ov = Pf.vo64 + (int64_t)v * S.apv;
-        const int nimg = image_count(im);
+        const FrameGeom &G = *Pf.G;
+        ExactMol X = exact_mol(S, f, s, v);
         st.guard++;
         int bulk = S.usecutoff ? (d32 > Pf.F->g.dbulk_hi) : 0;
         if (bin == -2) {
-            const double d64 = sqrt(pairs_one64(Pf.off64, im, qs, qv, os[a1], ov[b1]));
+            const double d64 = sqrt(exact_pair_d2(B, G, X, a1, b1));
             bin = setbin0(d64, S.binstep);
             bulk = S.usecutoff ? (d64 > S.dbulk) : 0;
-            st.guard_pairs += nimg;
+            st.guard_pairs += 1;
             st.maxerr = fmax(st.maxerr, fabs((double)d32 - d64));
         }
         // a row or column minimum in the band: its FP32 pass picks the pairs
         // within 2 delta of the FP32 minimum (the exact minimum is among them),
-        // which are then evaluated in FP64
+        // which are then evaluated exactly
         const Guard &g = Pf.F->g;
         if (rb1 == -2) {
             const float4 ob = Pf.vo32[(int64_t)v * S.apv + S.iref];
@@ -715,8 +704,8 @@ __global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
             double rr = INFINITY;
             for (int a = 0; a < S.aps; ++a) {
                 if (!(edge_d2(Pf, im, s, v, os32[a], ob) <= thr)) continue;
-                rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[a], ov[S.iref]));
-                st.guard_pairs += nimg;
+                rr = fmin(rr, exact_pair_d2(B, G, X, a, S.iref));
+                st.guard_pairs += 1;
             }
             rb1 = rr <= S.cut2 ? setbin0(sqrt(rr), S.binstep) : -1;
         }
@@ -729,8 +718,8 @@ __global__ void __launch_bounds__(128) k_pairs_edge(DevSys S, Bufs B) {
             double rr = INFINITY;
             for (int b = 0; b < S.apv; ++b) {
                 if (!(edge_d2(Pf, im, s, v, oa, ov32[b]) <= thr)) continue;
-                rr = fmin(rr, pairs_one64(Pf.off64, im, qs, qv, os[S.iref], ov[b]));
-                st.guard_pairs += nimg;
+                rr = fmin(rr, exact_pair_d2(B, G, X, S.iref, b));
+                st.guard_pairs += 1;
             }
             rb2 = rr <= S.cut2 ? setbin0(sqrt(rr), S.binstep) : -1;
         }

@@ -82,17 +82,24 @@ struct DevSys {
     int *err;
 };
 
-// FP32 decision constants of one frame.
-struct Guard {
+// Decision constants of one frame for a search in precision R (float: the
+// FP32 search; double: the FP64 search).  A value computed in R is within
+// delta of the exact distance (cm_geom.h, exact_d2), so a decision taken from
+// it is the exact decision when the value lies farther than delta from the
+// decision boundary.
+template <typename R>
+struct GuardT {
     double delta;     // Angstrom
-    float cutp2;      // (cut + delta)^2, rounded up
-    float cutm2;      // (cut - delta)^2, rounded down
-    float two_delta;
-    float inv_bs;     // 1 / binstep in FP32
-    float bin_band;   // half-width of the bin-edge band in units of bins
-    float dbulk_lo, dbulk_hi;
+    R cutp2;          // (cut + delta)^2, rounded up
+    R cutm2;          // (cut - delta)^2, rounded down
+    R two_delta;
+    R inv_bs;         // 1 / binstep in R
+    R bin_band;       // half-width of the bin-edge band in units of bins
+    R dbulk_lo, dbulk_hi;
     float cut_pre;    // cutoff + margin of the bounding-sphere tests
 };
+using Guard = GuardT<float>;
+using Guard64 = GuardT<double>;
 
 // Per-frame values found by the prep kernels and the constants derived from
 // them by k_frame_consts (one block, before the search kernels).
@@ -107,8 +114,9 @@ struct FrameScratch {
     int L[3];       // PAIRS stencil half-widths
     int multi;      // PAIRS axes with several images (bit k set for axis k)
     int La[3];      // ATOMS stencil half-widths
-    int pad;
-    Guard g;
+    float xmax;     // largest |coordinate component| of the frame's input atoms (rounded up)
+    Guard g;        // FP32 search
+    Guard64 g64;    // FP64 search
 };
 
 struct Sample {
@@ -324,343 +332,7 @@ struct DirRec {
     int bulk;      // inbulk(...) of the solvent molecule for this solute molecule (src/mddf.jl:55-57)
 };
 
-// ---------------------------------------------------------- PAIRS evaluation
-// FP32 first pass: smallest / second-smallest squared distance and the pair
-// (a, b) of the smallest, plus the reference-atom row / column minima.
-struct Pass32 {
-    float m1, m2;
-    int k1;        // a * apv + b
-    float r1, r2;
-};
-
-template <bool ROW>
-__device__ __forceinline__ void inner32(const float4 *__restrict__ os, int aps, int apv, int b, float tx, float ty, float tz,
-                                        Pass32 &P) {
-    float row = P.r1;
-    for (int a = 0; a < aps; ++a) {
-        float4 oa = os[a];
-        float dx = tx - oa.x, dy = ty - oa.y, dz = tz - oa.z;
-        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        P.m2 = fminf(P.m2, fmaxf(P.m1, d2));
-        P.k1 = d2 < P.m1 ? a * apv + b : P.k1;
-        P.m1 = fminf(P.m1, d2);
-        if (ROW) row = fminf(row, d2);
-    }
-    if (ROW) P.r1 = row;
-}
-
-template <bool SELF>
-__device__ __forceinline__ void pairs_pass32(const DevSys &S, const float4 *__restrict__ off32, const Images &im, float4 qs,
-                                             float4 qv, const float4 *__restrict__ os, const float4 *ov, Pass32 &P) {
-    P.m1 = P.m2 = P.r1 = P.r2 = INFINITY;
-    P.k1 = 0;
-    const int aps = S.aps, apv = S.apv, iref = S.iref;
-    CM_FOR_IMAGES(im, dx, dy, dz) {
-        float4 o = off32[off_index(dx, dy, dz)];
-        float Dx = (qv.x - qs.x) + o.x, Dy = (qv.y - qs.y) + o.y, Dz = (qv.z - qs.z) + o.z;
-        for (int b = 0; b < apv; ++b) {
-            float4 ob = ov[b];
-            float tx = Dx + ob.x, ty = Dy + ob.y, tz = Dz + ob.z;
-            if (b == iref) inner32<true>(os, aps, apv, b, tx, ty, tz, P);
-            else inner32<false>(os, aps, apv, b, tx, ty, tz, P);
-            if (SELF) {
-                float4 oa = os[iref];
-                float ex = tx - oa.x, ey = ty - oa.y, ez = tz - oa.z;
-                P.r2 = fminf(P.r2, fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
-            }
-        }
-    }
-}
-
-// Exact FP64 minimum search with the reference's tie rule: among equal
-// distances the pair visited last wins (src/minimum_distances.jl:33-37, the new
-// pair replaces the record unless the record is strictly closer), restated as
-// the largest (solute atom, solvent atom) index pair.  Distances are compared
-// as d = sqrt(d2) like the reference; d2 decides when it is far enough from the
-// current best that the square roots cannot tie.
-struct Best64 {
-    double d2, d, lo, hi;
-    int a, b;     // direction 1: key (a, b)
-    int a2, b2;   // direction 2 (self mode): key (b, a)
-};
-
-__device__ __forceinline__ void best_init(Best64 &B) {
-    B.d2 = INFINITY;
-    B.d = -1.0;
-    B.lo = INFINITY;
-    B.hi = INFINITY;
-    B.a = B.b = B.a2 = B.b2 = -1;
-}
-
-template <bool DIR2>
-__device__ __forceinline__ void best_update(Best64 &B, double d2, int a, int b) {
-    if (d2 < B.lo) {
-        B.d2 = d2;
-        B.d = -1.0;
-        B.lo = mul(d2, 1.0 - 0x1.0p-50);
-        B.hi = mul(d2, 1.0 + 0x1.0p-50);
-        B.a = a; B.b = b; B.a2 = a; B.b2 = b;
-    } else if (d2 <= B.hi) {
-        double d = sqrt(d2);
-        if (B.d < 0.0) B.d = sqrt(B.d2);
-        if (d < B.d) {
-            B.d2 = d2;
-            B.d = d;
-            B.lo = mul(d2, 1.0 - 0x1.0p-50);
-            B.hi = mul(d2, 1.0 + 0x1.0p-50);
-            B.a = a; B.b = b; B.a2 = a; B.b2 = b;
-        } else if (d == B.d) {
-            if (a > B.a || (a == B.a && b > B.b)) { B.a = a; B.b = b; }
-            if (DIR2 && (b > B.b2 || (b == B.b2 && a > B.a2))) { B.a2 = a; B.b2 = b; }
-        }
-    }
-}
-
-__device__ __forceinline__ double best_d(Best64 &B) {
-    if (B.d < 0.0) B.d = sqrt(B.d2);
-    return B.d;
-}
-
-__device__ __forceinline__ double pair_d2_64(double tx, double ty, double tz, double ax, double ay, double az) {
-    double dx = sub(tx, ax), dy = sub(ty, ay), dz = sub(tz, az);
-    return add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz));
-}
-
-struct Exact64 {
-    Best64 B;
-    double rr1, rr2;   // exact squared minima (within cutoff) of the row / column
-    long long evals;
-};
-
-// Exact scan of a molecule pair over its images.  With FILTER an atom pair is
-// evaluated in FP64 only if its FP32 squared distance is at most the threshold
-// of an accumulator it feeds (thr_arg: the minimum; thr_r1: row of v's
-// reference atom; thr_r2: column of s's reference atom); each threshold keeps
-// every pair that can hold the exact minimum of its accumulator.
-template <bool FILTER, bool SELF>
-__device__ void pairs_exact(const DevSys &S, const d4 *__restrict__ off64, const float4 *__restrict__ off32, const Images &im,
-                            d4 qs64, float4 qs32, d4 qv64, float4 qv32, const d4 *os64, const float4 *os32,
-                            const d4 *ov64, const float4 *ov32, float thr_arg, float thr_r1, float thr_r2, Exact64 &E) {
-    best_init(E.B);
-    E.rr1 = INFINITY;
-    E.rr2 = INFINITY;
-    E.evals = 0;
-    const int aps = S.aps, apv = S.apv, iref = S.iref;
-    const double cut2 = S.cut2;
-    CM_FOR_IMAGES(im, ix, iy, iz) {
-        int oi = off_index(ix, iy, iz);
-        d4 o = off64[oi];
-        double Dx = add(sub(qv64.x, qs64.x), o.x);
-        double Dy = add(sub(qv64.y, qs64.y), o.y);
-        double Dz = add(sub(qv64.z, qs64.z), o.z);
-        float Fx = 0.f, Fy = 0.f, Fz = 0.f;
-        if (FILTER) {
-            float4 of = off32[oi];
-            Fx = (qv32.x - qs32.x) + of.x;
-            Fy = (qv32.y - qs32.y) + of.y;
-            Fz = (qv32.z - qs32.z) + of.z;
-        }
-        for (int b = 0; b < apv; ++b) {
-            d4 ob = ov64[b];
-            double tx = add(Dx, ob.x), ty = add(Dy, ob.y), tz = add(Dz, ob.z);
-            float fx = 0.f, fy = 0.f, fz = 0.f;
-            if (FILTER) {
-                float4 of = ov32[b];
-                fx = Fx + of.x; fy = Fy + of.y; fz = Fz + of.z;
-            }
-            for (int a = 0; a < aps; ++a) {
-                if (FILTER) {
-                    float4 oa = os32[a];
-                    float ex = fx - oa.x, ey = fy - oa.y, ez = fz - oa.z;
-                    float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                    bool need = d2f <= thr_arg || (b == iref && d2f <= thr_r1) || (SELF && a == iref && d2f <= thr_r2);
-                    if (!need) continue;
-                }
-                d4 oa = os64[a];
-                double d2 = pair_d2_64(tx, ty, tz, oa.x, oa.y, oa.z);
-                E.evals++;
-                if (d2 <= cut2) {
-                    if (b == iref) E.rr1 = fmin(E.rr1, d2);
-                    if (SELF && a == iref) E.rr2 = fmin(E.rr2, d2);
-                    best_update<SELF>(E.B, d2, a, b);
-                }
-            }
-        }
-    }
-}
-
-// FP64 squared distance of one atom pair, minimum over the images.
-__device__ double pairs_one64(const d4 *__restrict__ off64, const Images &im, d4 qs64, d4 qv64, d4 oa,
-                              d4 ob) {
-    double best = INFINITY;
-    CM_FOR_IMAGES(im, ix, iy, iz) {
-        d4 o = off64[off_index(ix, iy, iz)];
-        double tx = add(add(sub(qv64.x, qs64.x), o.x), ob.x);
-        double ty = add(add(sub(qv64.y, qs64.y), o.y), ob.y);
-        double tz = add(add(sub(qv64.z, qs64.z), o.z), ob.z);
-        best = fmin(best, pair_d2_64(tx, ty, tz, oa.x, oa.y, oa.z));
-    }
-    return best;
-}
-
-// Bin from an FP32 distance, or -1 when it lies in the band around a bin edge.
-__device__ __forceinline__ int bin32(const Guard &g, float d) {
-    float k = d * g.inv_bs;
-    float r = rintf(k);
-    if (fabsf(k - r) <= g.bin_band) return -1;
-    int b = (int)ceilf(k);
-    return (b < 1 ? 1 : b) - 1;
-}
-
-__device__ __forceinline__ DirRec dir_none(const DevSys &S) {
-    DirRec r;
-    r.within = 0; r.i_local = -1; r.j = -1; r.bin = -1; r.ref = 0; r.rbin = -1;
-    r.bulk = S.usecutoff ? 0 : 1;
-    return r;
-}
-
-__device__ __forceinline__ int inbulk64(const DevSys &S, bool within, double d) {
-    return S.usecutoff ? (within && d > S.dbulk) : !within;
-}
-
-// Records from an exact scan.
-template <bool SELF>
-__device__ __forceinline__ void records_from_exact(const DevSys &S, Exact64 &E, int s, int64_t v, DirRec &r1, DirRec &r2) {
-    r1 = dir_none(S);
-    r2 = dir_none(S);
-    if (!(E.B.d2 <= S.cut2)) return;
-    double d = best_d(E.B);
-    int bin = setbin0(d, S.binstep);
-    r1.within = 1;
-    r1.i_local = E.B.a;
-    r1.j = v * S.apv + E.B.b;
-    r1.bin = bin;
-    r1.bulk = inbulk64(S, true, d);
-    if (E.rr1 <= S.cut2) { r1.ref = 1; r1.rbin = setbin0(sqrt(E.rr1), S.binstep); }
-    if (SELF) {
-        r2.within = 1;
-        r2.i_local = E.B.b2;
-        r2.j = (int64_t)s * S.aps + E.B.a2;
-        r2.bin = bin;
-        r2.bulk = r1.bulk;
-        if (E.rr2 <= S.cut2) { r2.ref = 1; r2.rbin = setbin0(sqrt(E.rr2), S.binstep); }
-    }
-}
-
-// Decide one molecule pair from its FP32 pass, falling back to FP64 inside the
-// guard band.  Produces exactly the records of pairs_exact<false, SELF>.
-template <bool SELF>
-__device__ void pairs_decide(const DevSys &S, const Guard &g, const Pass32 &P, const d4 *__restrict__ off64,
-                             const float4 *__restrict__ off32, const Images &im, d4 qs64, float4 qs32, d4 qv64,
-                             float4 qv32, const d4 *os64, const float4 *os32, const d4 *ov64, const float4 *ov32, int s,
-                             int64_t v, DirRec &r1, DirRec &r2, LocalStats &st) {
-    r1 = dir_none(S);
-    r2 = dir_none(S);
-    if (P.m1 > g.cutp2) return;  // every pair is beyond the cutoff
-    float d1 = sqrtf(P.m1);
-    bool amb = P.m1 >= g.cutm2 || (sqrtf(P.m2) - d1) <= g.two_delta;
-    if (amb) {
-        float t = d1 + g.two_delta;
-        float thr = __fmul_ru(t, t);
-        float thr1 = INFINITY, thr2 = INFINITY;
-        if (P.r1 <= g.cutp2) { float u = sqrtf(P.r1) + g.two_delta; thr1 = __fmul_ru(u, u); } else thr1 = -1.f;
-        if (SELF) { if (P.r2 <= g.cutp2) { float u = sqrtf(P.r2) + g.two_delta; thr2 = __fmul_ru(u, u); } else thr2 = -1.f; }
-        Exact64 E;
-        pairs_exact<true, SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, thr, thr1, thr2, E);
-        records_from_exact<SELF>(S, E, s, v, r1, r2);
-        st.guard++;
-        st.guard_pairs += E.evals;
-        if (E.B.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(E.B)));
-        return;
-    }
-    // unambiguous: the FP32 minimum pair is the exact minimum pair, within cutoff
-    int a = P.k1 / S.apv, b = P.k1 - a * S.apv;
-    int bin = bin32(g, d1);
-    double d64 = -1.0;
-    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
-        double q = pairs_one64(off64, im, qs64, qv64, os64[a], ov64[b]);
-        d64 = sqrt(q);
-        bin = setbin0(d64, S.binstep);
-        st.guard++;
-        st.guard_pairs += image_count(im);
-        st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
-    }
-    int bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
-    r1.within = 1;
-    r1.i_local = a;
-    r1.j = v * S.apv + b;
-    r1.bin = bin;
-    r1.bulk = bulk;
-    if (SELF) {
-        r2.within = 1;
-        r2.i_local = b;
-        r2.j = (int64_t)s * S.aps + a;
-        r2.bin = bin;
-        r2.bulk = bulk;
-    }
-    // reference-atom rows (and columns in self mode)
-    for (int dir = 0; dir < (SELF ? 2 : 1); ++dir) {
-        float rm = dir == 0 ? P.r1 : P.r2;
-        DirRec &r = dir == 0 ? r1 : r2;
-        if (rm > g.cutp2) continue;
-        int rb = -1;
-        if (rm < g.cutm2) rb = bin32(g, sqrtf(rm));
-        if (rb >= 0) {
-            r.ref = 1;
-            r.rbin = rb;
-            continue;
-        }
-        float u = sqrtf(rm) + g.two_delta;
-        float thr = __fmul_ru(u, u);
-        Exact64 E;
-        pairs_exact<true, SELF>(S, off64, off32, im, qs64, qs32, qv64, qv32, os64, os32, ov64, ov32, -1.f, dir == 0 ? thr : -1.f,
-                                dir == 1 ? thr : -1.f, E);
-        double rr = dir == 0 ? E.rr1 : E.rr2;
-        st.guard++;
-        st.guard_pairs += E.evals;
-        if (rr <= S.cut2) {
-            r.ref = 1;
-            r.rbin = setbin0(sqrt(rr), S.binstep);
-        }
-    }
-}
-
-__device__ __forceinline__ unsigned char flag_code(const DirRec &r) { return r.within ? (unsigned char)(1 + (r.bulk ? 1 : 0)) : 0; }
-
-__device__ __forceinline__ int pack_delta(int dx, int dy, int dz) { return (dx + 16) | ((dy + 16) << 5) | ((dz + 16) << 10); }
-__device__ __forceinline__ void unpack_delta(int c, int &dx, int &dy, int &dz) {
-    dx = (c & 31) - 16;
-    dy = ((c >> 5) & 31) - 16;
-    dz = ((c >> 10) & 31) - 16;
-}
-
-// ------------------------------------------------------------------ geometry
-__device__ __forceinline__ double norm3d(double x, double y, double z) { return sqrt(x * x + y * y + z * z); }
-
-// Largest |Hn v| over the 8 sign patterns of v = (+-l0, +-l1, +-l2).
-__device__ double corner_norm(const FrameGeom &G, double l0, double l1, double l2) {
-    double best = 0.0;
-    for (int m = 0; m < 8; ++m) {
-        double v[3];
-        matvec_cm(G.Hn, (m & 1) ? -l0 : l0, (m & 2) ? -l1 : l1, (m & 4) ? -l2 : l2, v);
-        best = fmax(best, norm3d(v[0], v[1], v[2]));
-    }
-    return best;
-}
-
-// Stencil half-widths for a search range; false if the offset table is too small.
-__device__ bool stencil(const FrameGeom &G, double range, int *L) {
-    bool ok = true;
-    for (int k = 0; k < 3; ++k) {
-        int l = (int)ceil(range * (1.0 + 1e-9) / G.cw[k]);
-        if (l < 1) l = 1;
-        if (l > kLT) { ok = false; l = kLT; }
-        L[k] = l;
-    }
-    return ok;
-}
-
-// ------------------------------------------------------------------- kernels
+// ------------------------------------------------------------------- buffers
 // Frames are processed in chunks.  Every per-frame buffer holds the chunk's
 // frames at a fixed stride, and each kernel finds the frame of its work item
 // (grid y, or the item's own frame tag), so one launch per stage serves all
@@ -671,6 +343,11 @@ struct Bufs {
     int64_t ms, Ns, mv, Nv;
     const FrameGeom *G;             // [nf]
     FrameScratch *FS;               // [nf]
+    // the chunk's input coordinates as the caller gave them ([nf][Ns][3] and
+    // [nf][Nv][3], FP32 or FP64; xv_raw == xs_raw in self mode): the exact
+    // distances are formed from these
+    const void *xs_raw, *xv_raw;
+    int raw64;                      // 1: FP64 input coordinates
     d4 *off64;                      // [nf][kOffEntries]
     float4 *off32;
     // PAIRS molecules; in self mode the solvent pointers alias the solute ones
@@ -721,6 +398,458 @@ struct Bufs {
     int aq_cap;
 };
 
+// ------------------------------------------------------------ exact distances
+// Input coordinates of one atom of frame f (solute or solvent selection),
+// widened to FP64 exactly.
+__device__ __forceinline__ void raw_atom(const Bufs &B, bool solvent, int f, int64_t atom, double *x) {
+    const int64_t i = ((int64_t)f * (solvent ? B.Nv : B.Ns) + atom) * 3;
+    if (B.raw64) {
+        const double *p = (const double *)(solvent ? B.xv_raw : B.xs_raw) + i;
+        x[0] = p[0]; x[1] = p[1]; x[2] = p[2];
+    } else {
+        const float *p = (const float *)(solvent ? B.xv_raw : B.xs_raw) + i;
+        x[0] = (double)p[0]; x[1] = (double)p[1]; x[2] = (double)p[2];
+    }
+}
+
+// The two molecules of one evaluated pair, for the exact distances: the
+// solute molecule's atoms and the solvent molecule's atoms from the input
+// coordinates, or, for a random-insertion slot, the source molecule placed by
+// the slot's draws exactly as the random insertion defines it
+// (exact_unwrapped / exact_placed: src/rigid_body.jl:107-137).
+struct ExactMol {
+    int f;
+    int apv, iref;
+    int placed;
+    int ready;         // placed: xr and cm computed
+    int64_t sbase;     // selection index of the solute molecule's first atom
+    int64_t vbase;     // selection index of the solvent molecule's (the placed source molecule's) first atom
+    double A[9];       // placed: rotation (row-major)
+    double ncm[3];     // placed: new centre H fc
+    double xr[3];      // placed: the source molecule's reference atom
+    double cm[3];      // placed: mean of the unwrapped source atoms
+};
+
+__device__ __forceinline__ ExactMol exact_mol(const DevSys &S, int f, int64_t s, int64_t v) {
+    ExactMol X;
+    X.f = f;
+    X.apv = S.apv;
+    X.iref = S.iref;
+    X.placed = 0;
+    X.ready = 1;
+    X.sbase = s * S.aps;
+    X.vbase = v * S.apv;
+    return X;
+}
+
+__device__ __forceinline__ ExactMol exact_mol_placed(const DevSys &S, const FrameGeom &G, int f, int64_t s, int jmol,
+                                                     const double *fc, const double *A) {
+    ExactMol X = exact_mol(S, f, s, jmol);
+    X.placed = 1;
+    X.ready = 0;
+    for (int k = 0; k < 9; ++k) X.A[k] = A[k];
+    exact_lat(G, fc, X.ncm);
+    return X;
+}
+
+__device__ __noinline__ void exact_mol_ready(const Bufs &B, const FrameGeom &G, ExactMol &X) {
+    raw_atom(B, true, X.f, X.vbase + X.iref, X.xr);
+    double cm[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < X.apv; ++b) {
+        double x[3], u[3];
+        raw_atom(B, true, X.f, X.vbase + b, x);
+        exact_unwrapped(G, x, X.xr, u);
+        for (int k = 0; k < 3; ++k) cm[k] = add(cm[k], u[k]);
+    }
+    for (int k = 0; k < 3; ++k) X.cm[k] = div(cm[k], (double)X.apv);
+    X.ready = 1;
+}
+
+__device__ __forceinline__ void exact_solute_atom(const Bufs &B, const ExactMol &X, int a, double *x) {
+    raw_atom(B, false, X.f, X.sbase + a, x);
+}
+
+__device__ __forceinline__ void exact_solvent_atom(const Bufs &B, const FrameGeom &G, ExactMol &X, int b, double *y) {
+    raw_atom(B, true, X.f, X.vbase + b, y);
+    if (!X.placed) return;
+    if (!X.ready) exact_mol_ready(B, G, X);
+    double u[3];
+    exact_unwrapped(G, y, X.xr, u);
+    exact_placed(u, X.cm, X.A, X.ncm, y);
+}
+
+// Exact squared distance of solute atom a and solvent atom b of a pair.
+__device__ __forceinline__ double exact_pair_d2(const Bufs &B, const FrameGeom &G, ExactMol &X, int a, int b) {
+    double x[3], y[3];
+    exact_solute_atom(B, X, a, x);
+    exact_solvent_atom(B, G, X, b, y);
+    return exact_d2(G, x, y);
+}
+
+// A pair's molecules as the search kernels name them (a few words, so the
+// search loops carry no ExactMol): frame, solute molecule, solvent molecule,
+// and for a random-insertion slot the placed source molecule (v), its
+// rotation and its fractional centre.
+struct ExactRef {
+    int f, s, v;
+    const double *A;    // nullptr: a real pair
+    const double *fc;
+};
+
+__device__ __forceinline__ ExactMol exact_mol_of(const DevSys &S, const FrameGeom &G, const ExactRef &r) {
+    return r.A ? exact_mol_placed(S, G, r.f, r.s, r.v, r.fc, r.A) : exact_mol(S, r.f, r.s, r.v);
+}
+
+// exact_pair_d2 out of line, for the searches' rare exact decisions.
+__device__ __noinline__ double exact_pair_ref(const DevSys &S, const Bufs &B, const FrameGeom &G, const ExactRef &r, int a,
+                                              int b) {
+    ExactMol X = exact_mol_of(S, G, r);
+    return exact_pair_d2(B, G, X, a, b);
+}
+
+// ---------------------------------------------------------- PAIRS evaluation
+// Search pass in precision R over cell-relative coordinates (float4 for the
+// FP32 search, d4 for the FP64 search): smallest / second-smallest squared
+// distance and the pair (a, b) of the smallest, plus the reference-atom row /
+// column minima.
+template <typename R>
+struct Vec4T;
+template <>
+struct Vec4T<float> {
+    using type = float4;
+};
+template <>
+struct Vec4T<double> {
+    using type = d4;
+};
+
+template <typename R>
+struct PassT {
+    R m1, m2;
+    int k1;        // a * apv + b
+    R r1, r2;
+};
+using Pass32 = PassT<float>;
+
+__device__ __forceinline__ float sq3(float x, float y, float z) { return fmaf(z, z, fmaf(y, y, x * x)); }
+__device__ __forceinline__ double sq3(double x, double y, double z) { return fma(z, z, fma(y, y, x * x)); }
+__device__ __forceinline__ float r_min(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double r_min(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float r_max(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double r_max(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float r_abs(float a) { return fabsf(a); }
+__device__ __forceinline__ double r_abs(double a) { return fabs(a); }
+
+template <bool ROW, typename R, typename V>
+__device__ __forceinline__ void inner_pass(const V *__restrict__ os, int aps, int apv, int b, R tx, R ty, R tz,
+                                           PassT<R> &P) {
+    R row = P.r1;
+    for (int a = 0; a < aps; ++a) {
+        const V oa = os[a];
+        const R d2 = sq3(tx - (R)oa.x, ty - (R)oa.y, tz - (R)oa.z);
+        P.m2 = r_min(P.m2, r_max(P.m1, d2));
+        P.k1 = d2 < P.m1 ? a * apv + b : P.k1;
+        P.m1 = r_min(P.m1, d2);
+        if (ROW) row = r_min(row, d2);
+    }
+    if (ROW) P.r1 = row;
+}
+
+template <bool SELF, typename R, typename V>
+__device__ __forceinline__ void pairs_pass(const DevSys &S, const V *__restrict__ off, const Images &im, V qs, V qv,
+                                           const V *__restrict__ os, const V *ov, PassT<R> &P) {
+    P.m1 = P.m2 = P.r1 = P.r2 = (R)INFINITY;
+    P.k1 = 0;
+    const int aps = S.aps, apv = S.apv, iref = S.iref;
+    CM_FOR_IMAGES(im, dx, dy, dz) {
+        const V o = off[off_index(dx, dy, dz)];
+        const R Dx = ((R)qv.x - (R)qs.x) + (R)o.x, Dy = ((R)qv.y - (R)qs.y) + (R)o.y, Dz = ((R)qv.z - (R)qs.z) + (R)o.z;
+        for (int b = 0; b < apv; ++b) {
+            const V ob = ov[b];
+            const R tx = Dx + (R)ob.x, ty = Dy + (R)ob.y, tz = Dz + (R)ob.z;
+            if (b == iref) inner_pass<true>(os, aps, apv, b, tx, ty, tz, P);
+            else inner_pass<false>(os, aps, apv, b, tx, ty, tz, P);
+            if (SELF) {
+                const V oa = os[iref];
+                P.r2 = r_min(P.r2, sq3(tx - (R)oa.x, ty - (R)oa.y, tz - (R)oa.z));
+            }
+        }
+    }
+}
+
+// Exact minimum search with the reference's tie rule: among equal distances
+// the pair visited last wins (src/minimum_distances.jl:33-37, the new pair
+// replaces the record unless the record is strictly closer), restated as the
+// largest (solute atom, solvent atom) index pair.  Distances are compared as
+// d = sqrt(d2) like the reference; d2 decides when it is far enough from the
+// current best that the square roots cannot tie.
+struct Best64 {
+    double d2, d, lo, hi;
+    int a, b;     // direction 1: key (a, b)
+    int a2, b2;   // direction 2 (self mode): key (b, a)
+};
+
+__device__ __forceinline__ void best_init(Best64 &B) {
+    B.d2 = INFINITY;
+    B.d = -1.0;
+    B.lo = INFINITY;
+    B.hi = INFINITY;
+    B.a = B.b = B.a2 = B.b2 = -1;
+}
+
+template <bool DIR2>
+__device__ __forceinline__ void best_update(Best64 &B, double d2, int a, int b) {
+    if (d2 < B.lo) {
+        B.d2 = d2;
+        B.d = -1.0;
+        B.lo = mul(d2, 1.0 - 0x1.0p-50);
+        B.hi = mul(d2, 1.0 + 0x1.0p-50);
+        B.a = a; B.b = b; B.a2 = a; B.b2 = b;
+    } else if (d2 <= B.hi) {
+        double d = sqrt(d2);
+        if (B.d < 0.0) B.d = sqrt(B.d2);
+        if (d < B.d) {
+            B.d2 = d2;
+            B.d = d;
+            B.lo = mul(d2, 1.0 - 0x1.0p-50);
+            B.hi = mul(d2, 1.0 + 0x1.0p-50);
+            B.a = a; B.b = b; B.a2 = a; B.b2 = b;
+        } else if (d == B.d) {
+            if (a > B.a || (a == B.a && b > B.b)) { B.a = a; B.b = b; }
+            if (DIR2 && (b > B.b2 || (b == B.b2 && a > B.a2))) { B.a2 = a; B.b2 = b; }
+        }
+    }
+}
+
+__device__ __forceinline__ double best_d(Best64 &B) {
+    if (B.d < 0.0) B.d = sqrt(B.d2);
+    return B.d;
+}
+
+struct Exact64 {
+    Best64 B;
+    double rr1, rr2;   // exact squared minima (within cutoff) of the row / column
+    long long evals;
+};
+
+// Exact scan of a molecule pair.  An atom pair is evaluated exactly
+// (exact_d2 on the input coordinates, the smallest over the images) only if
+// its squared distance in the search precision R, the smallest over the
+// images, is at most the threshold of an accumulator it feeds (thr_arg: the
+// minimum; thr_r1: row of v's reference atom; thr_r2: column of s's reference
+// atom); each threshold keeps every pair that can hold the exact minimum of
+// its accumulator.
+template <bool SELF, typename R, typename V>
+__device__ __noinline__ void pairs_exact(const DevSys &S, const FrameGeom &G, const Bufs &B, const ExactRef &xref,
+                                         const V *__restrict__ off, const Images &im, V qs, V qv, const V *os, const V *ov,
+                                         R thr_arg, R thr_r1, R thr_r2, Exact64 &E) {
+    ExactMol X = exact_mol_of(S, G, xref);
+    best_init(E.B);
+    E.rr1 = INFINITY;
+    E.rr2 = INFINITY;
+    E.evals = 0;
+    const int aps = S.aps, apv = S.apv, iref = S.iref;
+    const double cut2 = S.cut2;
+    for (int b = 0; b < apv; ++b) {
+        const V ob = ov[b];
+        double yb[3];
+        bool have_y = false;
+        for (int a = 0; a < aps; ++a) {
+            const V oa = os[a];
+            R m = (R)INFINITY;
+            CM_FOR_IMAGES(im, ix, iy, iz) {
+                const V o = off[off_index(ix, iy, iz)];
+                const R tx = (((R)qv.x - (R)qs.x) + (R)o.x) + (R)ob.x;
+                const R ty = (((R)qv.y - (R)qs.y) + (R)o.y) + (R)ob.y;
+                const R tz = (((R)qv.z - (R)qs.z) + (R)o.z) + (R)ob.z;
+                m = r_min(m, sq3(tx - (R)oa.x, ty - (R)oa.y, tz - (R)oa.z));
+            }
+            const bool need = m <= thr_arg || (b == iref && m <= thr_r1) || (SELF && a == iref && m <= thr_r2);
+            if (!need) continue;
+            if (!have_y) {
+                exact_solvent_atom(B, G, X, b, yb);
+                have_y = true;
+            }
+            double xa[3];
+            exact_solute_atom(B, X, a, xa);
+            const double d2 = exact_d2(G, xa, yb);
+            E.evals++;
+            if (d2 <= cut2) {
+                if (b == iref) E.rr1 = fmin(E.rr1, d2);
+                if (SELF && a == iref) E.rr2 = fmin(E.rr2, d2);
+                best_update<SELF>(E.B, d2, a, b);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float r_rint(float x) { return rintf(x); }
+__device__ __forceinline__ double r_rint(double x) { return rint(x); }
+__device__ __forceinline__ float r_ceil(float x) { return ceilf(x); }
+__device__ __forceinline__ double r_ceil(double x) { return ceil(x); }
+__device__ __forceinline__ float r_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double r_sqrt(double x) { return sqrt(x); }
+// a * a rounded up: thresholds that must not lose a pair to rounding
+__device__ __forceinline__ float r_sq_ru(float x) { return __fmul_ru(x, x); }
+__device__ __forceinline__ double r_sq_ru(double x) { return __dmul_ru(x, x); }
+
+// Bin from a search-precision distance, or -1 when it lies in the band
+// around a bin edge.
+template <typename R>
+__device__ __forceinline__ int bin_of(const GuardT<R> &g, R d) {
+    const R k = d * g.inv_bs;
+    const R r = r_rint(k);
+    if (r_abs(k - r) <= g.bin_band) return -1;
+    const int b = (int)r_ceil(k);
+    return (b < 1 ? 1 : b) - 1;
+}
+__device__ __forceinline__ int bin32(const Guard &g, float d) { return bin_of<float>(g, d); }
+
+__device__ __forceinline__ DirRec dir_none(const DevSys &S) {
+    DirRec r;
+    r.within = 0; r.i_local = -1; r.j = -1; r.bin = -1; r.ref = 0; r.rbin = -1;
+    r.bulk = S.usecutoff ? 0 : 1;
+    return r;
+}
+
+__device__ __forceinline__ int inbulk64(const DevSys &S, bool within, double d) {
+    return S.usecutoff ? (within && d > S.dbulk) : !within;
+}
+
+// Records from an exact scan.
+template <bool SELF>
+__device__ __forceinline__ void records_from_exact(const DevSys &S, Exact64 &E, int s, int64_t v, DirRec &r1, DirRec &r2) {
+    r1 = dir_none(S);
+    r2 = dir_none(S);
+    if (!(E.B.d2 <= S.cut2)) return;
+    double d = best_d(E.B);
+    int bin = setbin0(d, S.binstep);
+    r1.within = 1;
+    r1.i_local = E.B.a;
+    r1.j = v * S.apv + E.B.b;
+    r1.bin = bin;
+    r1.bulk = inbulk64(S, true, d);
+    if (E.rr1 <= S.cut2) { r1.ref = 1; r1.rbin = setbin0(sqrt(E.rr1), S.binstep); }
+    if (SELF) {
+        r2.within = 1;
+        r2.i_local = E.B.b2;
+        r2.j = (int64_t)s * S.aps + E.B.a2;
+        r2.bin = bin;
+        r2.bulk = r1.bulk;
+        if (E.rr2 <= S.cut2) { r2.ref = 1; r2.rbin = setbin0(sqrt(E.rr2), S.binstep); }
+    }
+}
+
+// Decide one molecule pair from its search pass (precision R), with the exact
+// rules wherever a value lies within the guard band of its decision boundary.
+// Produces exactly the records of an unfiltered exact scan.
+template <bool SELF, typename R, typename V>
+__device__ void pairs_decide(const DevSys &S, const FrameGeom &G, const Bufs &B, const ExactRef &X, const GuardT<R> &g,
+                             const PassT<R> &P, const V *__restrict__ off, const Images &im, V qs, V qv, const V *os,
+                             const V *ov, int s, int64_t v, DirRec &r1, DirRec &r2, LocalStats &st) {
+    r1 = dir_none(S);
+    r2 = dir_none(S);
+    if (P.m1 > g.cutp2) return;  // every pair is beyond the cutoff
+    const R d1 = r_sqrt(P.m1);
+    const bool amb = P.m1 >= g.cutm2 || (r_sqrt(P.m2) - d1) <= g.two_delta;
+    if (amb) {
+        const R thr = r_sq_ru(d1 + g.two_delta);
+        R thr1 = (R)-1, thr2 = (R)-1;
+        if (P.r1 <= g.cutp2) thr1 = r_sq_ru(r_sqrt(P.r1) + g.two_delta);
+        if (SELF && P.r2 <= g.cutp2) thr2 = r_sq_ru(r_sqrt(P.r2) + g.two_delta);
+        Exact64 E;
+        pairs_exact<SELF>(S, G, B, X, off, im, qs, qv, os, ov, thr, thr1, thr2, E);
+        records_from_exact<SELF>(S, E, s, v, r1, r2);
+        st.guard++;
+        st.guard_pairs += E.evals;
+        if (E.B.d2 <= S.cut2) st.maxerr = fmax(st.maxerr, fabs((double)d1 - best_d(E.B)));
+        return;
+    }
+    // unambiguous: the search's minimum pair is the exact minimum pair, within cutoff
+    const int a = P.k1 / S.apv, b = P.k1 - a * S.apv;
+    int bin = bin_of(g, d1);
+    double d64 = -1.0;
+    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
+        d64 = sqrt(exact_pair_ref(S, B, G, X, a, b));
+        bin = setbin0(d64, S.binstep);
+        st.guard++;
+        st.guard_pairs += 1;
+        st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
+    }
+    const int bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
+    r1.within = 1;
+    r1.i_local = a;
+    r1.j = v * S.apv + b;
+    r1.bin = bin;
+    r1.bulk = bulk;
+    if (SELF) {
+        r2.within = 1;
+        r2.i_local = b;
+        r2.j = (int64_t)s * S.aps + a;
+        r2.bin = bin;
+        r2.bulk = bulk;
+    }
+    // reference-atom rows (and columns in self mode)
+    for (int dir = 0; dir < (SELF ? 2 : 1); ++dir) {
+        const R rm = dir == 0 ? P.r1 : P.r2;
+        DirRec &r = dir == 0 ? r1 : r2;
+        if (rm > g.cutp2) continue;
+        int rb = -1;
+        if (rm < g.cutm2) rb = bin_of(g, r_sqrt(rm));
+        if (rb >= 0) {
+            r.ref = 1;
+            r.rbin = rb;
+            continue;
+        }
+        const R thr = r_sq_ru(r_sqrt(rm) + g.two_delta);
+        Exact64 E;
+        pairs_exact<SELF>(S, G, B, X, off, im, qs, qv, os, ov, (R)-1, dir == 0 ? thr : (R)-1, dir == 1 ? thr : (R)-1, E);
+        const double rr = dir == 0 ? E.rr1 : E.rr2;
+        st.guard++;
+        st.guard_pairs += E.evals;
+        if (rr <= S.cut2) {
+            r.ref = 1;
+            r.rbin = setbin0(sqrt(rr), S.binstep);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned char flag_code(const DirRec &r) { return r.within ? (unsigned char)(1 + (r.bulk ? 1 : 0)) : 0; }
+
+__device__ __forceinline__ int pack_delta(int dx, int dy, int dz) { return (dx + 16) | ((dy + 16) << 5) | ((dz + 16) << 10); }
+__device__ __forceinline__ void unpack_delta(int c, int &dx, int &dy, int &dz) {
+    dx = (c & 31) - 16;
+    dy = ((c >> 5) & 31) - 16;
+    dz = ((c >> 10) & 31) - 16;
+}
+
+// ------------------------------------------------------------------ geometry
+__device__ __forceinline__ double norm3d(double x, double y, double z) { return sqrt(x * x + y * y + z * z); }
+
+// Largest |Hn v| over the 8 sign patterns of v = (+-l0, +-l1, +-l2).
+__device__ double corner_norm(const FrameGeom &G, double l0, double l1, double l2) {
+    double best = 0.0;
+    for (int m = 0; m < 8; ++m) {
+        double v[3];
+        matvec_cm(G.Hn, (m & 1) ? -l0 : l0, (m & 2) ? -l1 : l1, (m & 4) ? -l2 : l2, v);
+        best = fmax(best, norm3d(v[0], v[1], v[2]));
+    }
+    return best;
+}
+
+// Stencil half-widths for a search range; false if the offset table is too small.
+__device__ bool stencil(const FrameGeom &G, double range, int *L) {
+    bool ok = true;
+    for (int k = 0; k < 3; ++k) {
+        int l = (int)ceil(range * (1.0 + 1e-9) / G.cw[k]);
+        if (l < 1) l = 1;
+        if (l > kLT) { ok = false; l = kLT; }
+        L[k] = l;
+    }
+    return ok;
+}
+
+// ------------------------------------------------------------------- kernels
 // Per-frame offset tables: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
 __global__ void k_offtable(Bufs B) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y;
@@ -740,6 +869,14 @@ __device__ __forceinline__ void load_xyz(const T *p, double *x) {
 }
 
 __device__ __forceinline__ void atomic_max_pos(float *addr, float v) { atomicMax((int *)addr, __float_as_int(v)); }
+
+// atomic_max_pos of the largest value over the calling warp's active lanes
+// (one atomic per warp).
+__device__ __forceinline__ void warp_max_pos(float *addr, float v) {
+    const unsigned mask = __activemask();
+    const int m = __reduce_max_sync(mask, __float_as_int(v));
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicMax((int *)addr, m);
+}
 
 // PAIRS prep, one thread per molecule (grid y = frame).  The molecule is made
 // whole around its first atom (minimum image of each atom's displacement), its
@@ -767,10 +904,11 @@ __global__ void k_prep_pairs(Bufs B, const T *__restrict__ xyz, int64_t xyz_stri
     double x0[3];
     load_xyz(x, x0);
     const float wlim = (float)(0.45 * fmin(G.w[0], fmin(G.w[1], G.w[2])));
-    double sx = 0.0, sy = 0.0, sz = 0.0;
+    double sx = 0.0, sy = 0.0, sz = 0.0, xm = 0.0;
     for (int a = 0; a < apm; ++a) {
         double xa[3], d[3];
         load_xyz(x + 3 * a, xa);
+        xm = fmax(xm, fmax(fabs(xa[0]), fmax(fabs(xa[1]), fabs(xa[2]))));
         for (int k = 0; k < 3; ++k) d[k] = sub(xa[k], x0[k]);
         const float fx = (float)d[0], fy = (float)d[1], fz = (float)d[2];
         if (fmaf(fz, fz, fmaf(fy, fy, fx * fx)) > wlim * wlim) unwrap(G, d);
@@ -802,7 +940,8 @@ __global__ void k_prep_pairs(Bufs B, const T *__restrict__ xyz, int64_t xyz_stri
     mq64[m] = make_d4(q[0], q[1], q[2], 0.0);
     mq32[m] = make_float4((float)q[0], (float)q[1], (float)q[2], rf);
     if (count_cells) atomicAdd(B.ccount + (int64_t)f * B.cs + cell, 1);
-    atomic_max_pos(solvent_side ? &F.rmax_v : &F.rmax_s, rf);
+    warp_max_pos(solvent_side ? &F.rmax_v : &F.rmax_s, rf);
+    warp_max_pos(&F.xmax, __double2float_ru(xm));
 }
 
 // Exclusive scans of the chunk's per-frame count arrays (one CTA of 1024
@@ -1045,7 +1184,6 @@ __global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, in
             if (lane == 0) raise_err(S, ERR_STENCIL);
             continue;
         }
-        const Guard g = F.g;
         const float4 qs32 = Pf.sq32[s];
         const d4 qs64 = Pf.sq64[s];
         __syncwarp();
@@ -1053,24 +1191,23 @@ __global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, in
         __syncwarp();
         auto process = [&](int v, int code) {
             const Images im = images_of(G, F, code);
-            const float4 qv32 = Pf.vq32[v];
-            const d4 qv64 = Pf.vq64[v];
-            const float4 *ov32 = Pf.vo32 + (int64_t)v * S.apv;
-            const d4 *ov64 = Pf.vo64 + (int64_t)v * S.apv;
-            const d4 *os64 = Pf.so64 + (int64_t)s * S.aps;
             DirRec r1, r2;
             st.molpairs++;
             st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
+            const ExactRef X{f, s, v, nullptr, nullptr};
             if (FP32) {
+                const float4 qv32 = Pf.vq32[v];
+                const float4 *ov32 = Pf.vo32 + (int64_t)v * S.apv;
                 Pass32 P;
-                pairs_pass32<SELF>(S, Pf.off32, im, qs32, qv32, os, ov32, P);
-                pairs_decide<SELF>(S, g, P, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, s, v, r1, r2,
-                                   st);
+                pairs_pass<SELF>(S, Pf.off32, im, qs32, qv32, os, ov32, P);
+                pairs_decide<SELF>(S, G, B, X, F.g, P, Pf.off32, im, qs32, qv32, (const float4 *)os, ov32, s, v, r1, r2, st);
             } else {
-                Exact64 E;
-                pairs_exact<false, SELF>(S, Pf.off64, Pf.off32, im, qs64, qs32, qv64, qv32, os64, os, ov64, ov32, 0.f, 0.f, 0.f,
-                                         E);
-                records_from_exact<SELF>(S, E, s, v, r1, r2);
+                const d4 qv64 = Pf.vq64[v];
+                const d4 *ov64 = Pf.vo64 + (int64_t)v * S.apv;
+                const d4 *os64 = Pf.so64 + (int64_t)s * S.aps;
+                PassT<double> P;
+                pairs_pass<SELF>(S, Pf.off64, im, qs64, qv64, os64, ov64, P);
+                pairs_decide<SELF>(S, G, B, X, F.g64, P, Pf.off64, im, qs64, qv64, os64, ov64, s, v, r1, r2, st);
             }
             emit<SELF>(S, h, r1, r2, s, v, Pf.slot, Pf.flags, st);
         };
@@ -1222,41 +1359,46 @@ __global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
         const PairsFrame Pf = pairs_frame(B, f, S.self);
         const FrameGeom &G = *Pf.G;
         const FrameScratch &F = *Pf.F;
-        const Guard g = F.g;
         Placement P = draw_placement(S, G.frame_id, sm, k, Pf.bulk, Pf.nbulk);
         double qp[3];
         const Images im = placed_images(G, F, Pf.scell[s], P.fc, qp);
         double A[9];
         draw_rotation(P.st, A);
-        d4 ov64[kMaxSmallMol];
-        float4 ov32[kMaxSmallMol];
+        // the search places the molecule's centroid-relative atom offsets;
+        // the exact distances use the placement of the input coordinates
+        const ExactRef X{f, s, P.jmol, A, P.fc};
         const d4 *o = Pf.vo64 + (int64_t)P.jmol * S.apv;
-        for (int b = 0; b < S.apv; ++b) {
-            const d4 w = o[b];
-            double r[3];
-            matvec_rm(A, w.x, w.y, w.z, r);
-            ov64[b] = make_d4(r[0], r[1], r[2], 0.0);
-            ov32[b] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
-        }
-        const float4 qs32 = Pf.sq32[s];
-        const d4 qs64 = Pf.sq64[s];
-        const float4 qp32 = make_float4((float)qp[0], (float)qp[1], (float)qp[2], 0.f);
-        const d4 qp64 = make_d4(qp[0], qp[1], qp[2], 0.0);
-        const float4 *os32 = Pf.so32 + (int64_t)s * S.aps;
-        const d4 *os64 = Pf.so64 + (int64_t)s * S.aps;
         DirRec r1, r2;
         st.molpairs++;
         st.atompairs += (unsigned long long)S.aps * S.apv * image_count(im);
         if (FP32) {
+            float4 ov32[kMaxSmallMol];
+            for (int b = 0; b < S.apv; ++b) {
+                const d4 w = o[b];
+                double r[3];
+                matvec_rm(A, w.x, w.y, w.z, r);
+                ov32[b] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
+            }
+            const float4 qs32 = Pf.sq32[s];
+            const float4 qp32 = make_float4((float)qp[0], (float)qp[1], (float)qp[2], 0.f);
+            const float4 *os32 = Pf.so32 + (int64_t)s * S.aps;
             Pass32 Q;
-            pairs_pass32<false>(S, Pf.off32, im, qs32, qp32, os32, ov32, Q);
-            pairs_decide<false>(S, g, Q, Pf.off64, Pf.off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, s, k, r1, r2,
-                                st);
+            pairs_pass<false>(S, Pf.off32, im, qs32, qp32, os32, (const float4 *)ov32, Q);
+            pairs_decide<false>(S, G, B, X, F.g, Q, Pf.off32, im, qs32, qp32, os32, (const float4 *)ov32, s, k, r1, r2, st);
         } else {
-            Exact64 E;
-            pairs_exact<false, false>(S, Pf.off64, Pf.off32, im, qs64, qs32, qp64, qp32, os64, os32, ov64, ov32, 0.f, 0.f, 0.f,
-                                      E);
-            records_from_exact<false>(S, E, s, k, r1, r2);
+            d4 ov64[kMaxSmallMol];
+            for (int b = 0; b < S.apv; ++b) {
+                const d4 w = o[b];
+                double r[3];
+                matvec_rm(A, w.x, w.y, w.z, r);
+                ov64[b] = make_d4(r[0], r[1], r[2], 0.0);
+            }
+            const d4 qs64 = Pf.sq64[s];
+            const d4 qp64 = make_d4(qp[0], qp[1], qp[2], 0.0);
+            const d4 *os64 = Pf.so64 + (int64_t)s * S.aps;
+            PassT<double> Q;
+            pairs_pass<false>(S, Pf.off64, im, qs64, qp64, os64, (const d4 *)ov64, Q);
+            pairs_decide<false>(S, G, B, X, F.g64, Q, Pf.off64, im, qs64, qp64, os64, (const d4 *)ov64, s, k, r1, r2, st);
         }
         if (r1.within) { apply_hit(S, h, true, r1.bin, r1.i_local, r1.j, r1.ref, r1.rbin); st.hits++; }
     }
@@ -1281,6 +1423,19 @@ __global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
 // sqrt(3) E plus 2.5 u d (three roundings of d^2, one of the square root).  The
 // atom-cell layout's displacement (q_a - (q_b - off)) is bounded by the same
 // expression with r = 0.  delta adds 25 % to the bound.
+//
+// The exact distance (exact_d2, on the input coordinates) and the FP64 values
+// the searches start from (cell-relative positions, offsets, radii, placed
+// atoms) are other roundings of the same real distance.  Each is a chain of
+// at most a few dozen FP64 operations (plus a sum over a molecule's atoms for
+// a centroid or a placement) whose operands are bounded by
+//   M = X (1 + 3 |H| |H^-1|) + 16 |H| + cutoff + 2 (r_s + r_v + r_c) + 1,
+// X the largest input coordinate, |H| and |H^-1| the largest entries of the
+// cell matrix and of its inverse, r_c the largest molecule radius of the
+// random insertion; so with u64 = 2^-53 both are within
+//   eps = u64 (512 + 4 (apv + aps in the molecule layout)) M
+// of the real distance.  The FP32 band is delta + eps; the FP64 search uses
+// eps as its band, so both decide every count from the exact distance.
 __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
     const int f = blockIdx.x;
     const FrameGeom &G = B.G[f];
@@ -1341,9 +1496,19 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
     }
     const double rs = radii[0], rv = radii[1];
     const double range = S.cut + rs + rv;
+    // eps: the exact distance against the FP64 values the searches use
+    double hmax = 0.0, himax = 0.0;
+    for (int k = 0; k < 9; ++k) {
+        hmax = fmax(hmax, fabs(G.H[k]));
+        himax = fmax(himax, fabs(G.Hi[k]));
+    }
+    const double rc = S.self ? F.rmax_s : fmax((double)F.rmax_v, (double)F.rcmax);
+    const double M = (double)F.xmax * (1.0 + 3.0 * hmax * himax) + 16.0 * hmax + S.cut +
+                     2.0 * ((double)F.rmax_s + rc + (double)F.rcmax) + 1.0;
+    const double eps = 0x1.0p-53 * (512.0 + 4.0 * (double)(S.apv + (pairs ? S.aps : 0))) * M;
     const double u = 0x1.0p-24;
     const double E = u * (5.0 * Q + 4.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
-    const double delta = 1.25 * (1.7320508075688772 * E + 2.5 * u * (S.cut + 1.0)) + 1e-9;
+    const double delta = 1.25 * (1.7320508075688772 * E + 2.5 * u * (S.cut + 1.0)) + 1e-9 + eps;
     Guard g;
     g.delta = delta;
     const double cp = S.cut + delta, cm = S.cut - delta;
@@ -1357,6 +1522,19 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
     g.dbulk_hi = __double2float_ru(S.dbulk + delta);
     g.cut_pre = __double2float_ru(S.cut + 1e-3 * (1.0 + range));
     F.g = g;
+    // the FP64 search: the same rules with band eps
+    Guard64 g64;
+    g64.delta = eps;
+    const double cp64 = __dadd_ru(S.cut, eps), cm64 = __dsub_rd(S.cut, eps);
+    g64.cutp2 = __dmul_ru(cp64, cp64);
+    g64.cutm2 = cm64 > 0.0 ? __dmul_rd(cm64, cm64) : 0.0;
+    g64.two_delta = __dmul_ru(2.0, eps);
+    g64.inv_bs = 1.0 / S.binstep;
+    g64.bin_band = __dadd_ru(__ddiv_ru(eps, S.binstep), (double)(S.nbins + 2) * 8.0 * 0x1.0p-53);
+    g64.dbulk_lo = __dsub_rd(S.dbulk, eps);
+    g64.dbulk_hi = __dadd_ru(S.dbulk, eps);
+    g64.cut_pre = g.cut_pre;
+    F.g64 = g64;
 }
 
 // Molecule-centred data for random insertion (src/rigid_body.jl:127-134):
@@ -1408,9 +1586,11 @@ __global__ void k_prep_atoms_solvent(Bufs B, const T *__restrict__ xyz, int64_t 
     const FrameGeom &G = B.G[f];
     const T *x = xyz + (int64_t)f * xyz_stride + (int64_t)m * apm * 3;
     const int64_t fo = (int64_t)f * B.Nv;
+    double xm = 0.0;
     for (int b = 0; b < apm; ++b) {
         double xb[3];
         load_xyz(x + 3 * b, xb);
+        xm = fmax(xm, fmax(fabs(xb[0]), fmax(fabs(xb[1]), fabs(xb[2]))));
         int c[3];
         double q[3];
         bin_position(G, xb[0], xb[1], xb[2], c, q);
@@ -1419,6 +1599,7 @@ __global__ void k_prep_atoms_solvent(Bufs B, const T *__restrict__ xyz, int64_t 
         B.avq32[i] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
         B.avq64[i] = make_d4(q[0], q[1], q[2], 0.0);
     }
+    warp_max_pos(&B.FS[f].xmax, __double2float_ru(xm));
     if (centroids) {
         float r;
         centroid_data(G, x, apm, iref, B.u64 + fo + (int64_t)m * apm, r);
@@ -1447,6 +1628,7 @@ __global__ void k_prep_atoms_solute(Bufs B, const T *__restrict__ xyz, int64_t x
     B.atq32[fi] = make_float4((float)q[0], (float)q[1], (float)q[2], __int_as_float(a));
     B.atq64[fi] = make_d4(q[0], q[1], q[2], 0.0);
     atomicAdd(B.acount + (int64_t)f * B.as + k, 1);
+    warp_max_pos(&B.FS[f].xmax, __double2float_ru(fmax(fabs(x[0]), fmax(fabs(x[1]), fabs(x[2])))));
 }
 
 __global__ void k_scatter_atoms(Bufs B) {

@@ -314,6 +314,8 @@ void frame_geometry(const double *H, double cs, int ncap_axis, FrameGeom &G) {
     G.w[0] = V / std::sqrt(dot3(bc, bc));
     G.w[1] = V / std::sqrt(dot3(ca, ca));
     G.w[2] = V / std::sqrt(dot3(ab, ab));
+    G.hw = 0.5 * std::fmin(G.w[0], std::fmin(G.w[1], G.w[2]));
+    G.hortho = (H[1] == 0.0 && H[2] == 0.0 && H[3] == 0.0 && H[5] == 0.0 && H[6] == 0.0 && H[7] == 0.0) ? 1 : 0;
     for (int k = 0; k < 3; ++k) {
         int n = (int)std::floor(G.w[k] / cs);
         if (n < 1) n = 1;
@@ -959,8 +961,11 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
     cudaStream_t st = h->stream;
     ensure_cells(h, c.ncell_max);
     DevSys S = devsys_full(h);
-    const Bufs B = chunk_bufs(h, c, dG, dS);
+    Bufs B = chunk_bufs(h, c, dG, dS);
     const bool self = d.autocorrelation;
+    B.xs_raw = xs;
+    B.xv_raw = self ? (const void *)xs : (const void *)xv;
+    B.raw64 = sizeof(T) == 8 ? 1 : 0;
     const bool fp32 = d.precision == CM_PRECISION_FP32_GUARD;
     const int nf = c.nf;
     const int64_t ms = d.solute_nmols, mv = d.solvent_nmols, apv = d.solvent_natomspermol;
