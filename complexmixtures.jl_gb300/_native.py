@@ -12,7 +12,7 @@ from typing import Optional
 
 import numpy as np
 
-CM_API_VERSION = 2
+CM_API_VERSION = 3
 CM_OK, CM_EINVAL, CM_ENOMEM, CM_ECUDA, CM_EDEVICE, CM_ESTATE = range(6)
 CM_MODE_MDDF, CM_MODE_COORDINATION_NUMBER = 0, 1
 CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
@@ -65,6 +65,8 @@ class cm_system_desc(C.Structure):
         ("cell_scale_pct", C.c_int32),
         ("launch", C.c_int32),
         ("atoms_schedule", C.c_int32),
+        ("guard_queue_capacity", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

@@ -194,9 +194,10 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
     bool hard = m1 >= g.cutm2 || (sqrtf(m2) - dmin) <= g.two_delta;
     if (S.usecutoff) hard = hard || (dmin >= g.dbulk_lo && dmin <= g.dbulk_hi);
     if (hard) {
+        // past the capacity the record is dropped and k_queue_check has the
+        // chunk redone without queues
         const int slot = atomicAdd(B.counters + 0, 1);
         if (slot < B.gq_cap) B.gq[slot] = make_int4(s, v, code, f);
-        else raise_err(S, ERR_QUEUE);
         return;
     }
     // otherwise each of the md bin, the solvent reference-atom row and (self)
@@ -220,8 +221,6 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
             B.eq[3 * slot] = make_int4(s, v, code, f);
             B.eq[3 * slot + 1] = make_int4(a1 | b1 << 8, rb1, rb2, bin);
             B.eq[3 * slot + 2] = make_int4(__float_as_int(dmin), 0, 0, 0);
-        } else {
-            raise_err(S, ERR_QUEUE);
         }
         return;
     }

@@ -378,7 +378,8 @@ struct Bufs {
     int rq_cap;
     int4 *eq;                       // edge queue: 3 int4 per entry (s, v, code, frame), (a | b << 8, rb1, rb2, bin), (d32 bits)
     int eq_cap;
-    int *counters;                  // [0] guard queue, [1] random queue, [2] ATOMS queue, [3] edge queue
+    int *counters;                  // [0] guard queue, [1] random queue, [2] ATOMS queue, [3] edge queue,
+                                    // [4] the chunk's real pass is redone without queues (k_queue_check)
     // ATOMS
     int *akey;                      // [nf][Ns]
     float4 *atq32, *asq32;
@@ -1149,9 +1150,10 @@ __device__ __forceinline__ void emit(const DevSys &S, const SHist &h, const DirR
 }
 
 // PAIRS real pass, generic (any molecule size, FP32 or FP64): one warp per
-// (frame, solute molecule) work item.  With only_multi set it processes only
-// the frames that need several images per molecule pair (the rest were done by
-// the specialised FP32 kernel).
+// (frame, solute molecule) work item, every record decided where it is found
+// (no queues).  only_multi 0: every frame; 1: only the frames that need
+// several images per molecule pair (the rest were done by the specialised
+// FP32 kernel); 2: every frame, if k_queue_check raised the chunk's redo flag.
 template <bool FP32, bool SELF>
 __global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, int only_multi) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1159,7 +1161,9 @@ __global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, in
     const int hw = hist_words(S);
     float4 *os_all = (float4 *)(smem_raw + (((size_t)hw * 4 + 15) & ~(size_t)15));
     int *q_all = (int *)(os_all + kWarps * kMaxSmallMol);
-    if (only_multi) {
+    if (only_multi == 2) {
+        if (B.counters[4] == 0) return;
+    } else if (only_multi) {
         // nothing to do unless a frame of the chunk needs several images
         int any = 0;
         for (int f = threadIdx.x; f < B.nf; f += blockDim.x) any |= B.FS[f].multi;
@@ -1179,7 +1183,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, in
         const PairsFrame Pf = pairs_frame(B, f, SELF);
         const FrameGeom &G = *Pf.G;
         const FrameScratch &F = *Pf.F;
-        if (only_multi && !F.multi) continue;
+        if (only_multi == 1 && !F.multi) continue;
         if (!F.ok) {
             if (lane == 0) raise_err(S, ERR_STENCIL);
             continue;
@@ -1216,6 +1220,21 @@ __global__ void __launch_bounds__(kWarps * 32) k_pairs_real(DevSys S, Bufs B, in
     stats_flush(S, st, false);
     __syncthreads();
     shist_flush(S, h, false);
+}
+
+// After the FP32 real pass, its guard and edge kernels: if a queue
+// overflowed (records past the capacity were dropped), the accumulators and
+// statistics go back to their values before the real pass and the chunk's
+// redo flag is raised, so k_pairs_real (mode 2) decides every record of the
+// chunk again without queues.  Any grid; returns at once without an overflow.
+__global__ void k_queue_check(Bufs B, unsigned long long *__restrict__ hist, const unsigned long long *__restrict__ snap,
+                              int64_t n, unsigned long long *__restrict__ stats,
+                              const unsigned long long *__restrict__ stats_snap) {
+    if (B.counters[0] <= B.gq_cap && B.counters[3] <= B.eq_cap) return;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t i = t0; i < n; i += (int64_t)gridDim.x * blockDim.x) hist[i] = snap[i];
+    if (t0 < ST_N) stats[t0] = stats_snap[t0];
+    if (t0 == 0) B.counters[4] = 1;
 }
 
 // Bulk-molecule list of each distinct sampled solute molecule of each frame,

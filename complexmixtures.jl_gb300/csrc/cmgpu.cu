@@ -180,11 +180,13 @@ struct cm_handle {
     // device memory
     int64_t device_bytes = 0;
     DevBuf geoms, samples, tabs, fscratch, off64, off32, hist, sums, stats, errflag, counters, slot, flags, bulk, nbulk;
+    DevBuf hist_snap, stats_snap;  // accumulators before a chunk's real pass (restored if its queues overflow)
     DevBuf stage_s[2], stage_v[2];
     // PAIRS
     DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, ccount, cstart, cfill, cmol, cq32, gq, rq, eq;
     int gq_cap = 0, rq_cap = 0;
     int flat_ctas = 0;  // resident CTAs per SM of k_pairs_flat32
+    int guard_ctas = 1, edge_ctas = 1, rand_ctas = 1, real_ctas = 1;  // ... of the guard, edge, random and generic kernels
     // group tables
     DevBuf g_soff, g_sidx, g_voff, g_vidx;
     // ATOMS
@@ -358,6 +360,8 @@ void check_desc(const cm_system_desc *d) {
     if (d->api_version != CM_API_VERSION) bad("api_version mismatch");
     if (d->launch < CM_LAUNCH_AUTO || d->launch > CM_LAUNCH_GRAPH) bad("unknown launch mode");
     if (d->atoms_schedule < CM_SCHED_AUTO || d->atoms_schedule > CM_SCHED_BALANCED) bad("unknown atoms_schedule");
+    if (d->guard_queue_capacity < 0) bad("guard_queue_capacity must be >= 0");
+    if (d->reserved != 0) bad("reserved must be 0");
     if (d->solute_nmols < 1 || d->solute_natomspermol < 1 || d->solvent_nmols < 1 || d->solvent_natomspermol < 1)
         bad("selections must have at least one molecule of at least one atom");
     if (d->autocorrelation && (d->solute_nmols != d->solvent_nmols || d->solute_natomspermol != d->solvent_natomspermol))
@@ -528,13 +532,27 @@ void check_smem(const cm_handle *h, size_t need) {
                                       std::to_string(optin) + " (use fewer bins)");
 }
 
-// Resident CTAs per SM of the FP32 real pass.
-int flat_setup(cm_handle *h) {
-    const size_t smem = hist_smem_bytes(h, h->smem_groups) + (size_t)kFlatWarps * flat_warp_smem();
-    const FlatKernel k = flat_kernel(h);
+// Resident CTAs per SM of a kernel at a launch shape: the persistent
+// (grid-stride) kernels launch that many per SM, so they run in one wave.
+int resident_ctas(const void *fn, int threads, size_t smem) {
     int n = 0;
-    CM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, kFlatWarps * 32, smem));
+    CM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem));
     return std::max(1, n);
+}
+
+// Resident CTAs per SM of the PAIRS kernels: the FP32 real pass (returned)
+// and the guard, edge, random-evaluation and generic kernels (kept in h).
+int flat_setup(cm_handle *h) {
+    const size_t hsm = hist_smem_bytes(h, h->smem_groups);
+    const bool self = h->d.autocorrelation, fp32 = h->d.precision == CM_PRECISION_FP32_GUARD;
+    h->guard_ctas = resident_ctas(self ? (const void *)k_pairs_guard<true> : (const void *)k_pairs_guard<false>,
+                                  kGuardWarps * 32, hsm);
+    h->edge_ctas = resident_ctas(self ? (const void *)k_pairs_edge<true> : (const void *)k_pairs_edge<false>, 128, hsm);
+    h->rand_ctas = resident_ctas(fp32 ? (const void *)k_random_eval<true> : (const void *)k_random_eval<false>, 128, hsm);
+    const void *real = fp32 ? (self ? (const void *)k_pairs_real<true, true> : (const void *)k_pairs_real<true, false>)
+                            : (self ? (const void *)k_pairs_real<false, true> : (const void *)k_pairs_real<false, false>);
+    h->real_ctas = resident_ctas(real, kWarps * 32, hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8);
+    return resident_ctas(flat_kernel(h).fn, kFlatWarps * 32, hsm + (size_t)kFlatWarps * flat_warp_smem());
 }
 
 // The ATOMS evaluation kernels of a system (precision x schedule).
@@ -714,7 +732,7 @@ void plan(cm_handle *h, const cm_frames *f) {
     dev_alloc(h, h->fscratch, sizeof(FrameScratch) * fc);
     dev_alloc(h, h->off64, sizeof(d4) * cmgeom::kOffEntries * fc);
     dev_alloc(h, h->off32, sizeof(float4) * cmgeom::kOffEntries * fc);
-    dev_alloc(h, h->counters, 16);
+    dev_alloc(h, h->counters, 8 * sizeof(int));
     if (h->mddf) {
         const int nd = h->ndist_max;
         dev_alloc(h, h->slot, (size_t)fc * ms * 4);
@@ -744,6 +762,7 @@ void plan(cm_handle *h, const cm_frames *f) {
         const int64_t bound = ms * mv * fc;
         h->gq_cap = (int)(bound <= (1LL << 24) ? std::max<int64_t>(bound, 1024)
                                                : std::min<int64_t>(std::max<int64_t>(1 << 20, 64 * ms * fc), 1LL << 25));
+        if (d.guard_queue_capacity > 0) h->gq_cap = d.guard_queue_capacity;
         dev_alloc(h, h->gq, (size_t)h->gq_cap * sizeof(int4));
         dev_alloc(h, h->eq, (size_t)h->gq_cap * 3 * sizeof(int4));
         if (h->mddf) {
@@ -975,7 +994,7 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
     const int sms = h->sms;
     int launches = 0;
     CM_CUDA(cudaMemsetAsync(B.FS, 0, sizeof(FrameScratch) * nf, st));
-    CM_CUDA(cudaMemsetAsync(B.counters, 0, 4 * sizeof(int), st));
+    CM_CUDA(cudaMemsetAsync(B.counters, 0, 8 * sizeof(int), st));
     CM_LAUNCH(CM_K_PREP, k_offtable<<<dim3(grid_for(cmgeom::kOffEntries, 256), nf), 256, 0, st>>>(B));
     if (h->regime == CM_REGIME_PAIRS) {
         if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
@@ -988,11 +1007,14 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         CM_LAUNCH(CM_K_CELLS, k_scan<<<nf, 1024, 0, st>>>(B, 0));
         CM_LAUNCH(CM_K_CELLS, k_scatter_mols<<<dim3(grid_for(mv, 256), nf), 256, 0, st>>>(B, self ? 1 : 0));
         const size_t smem = hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
-        const int grid = (int)std::min<int64_t>(((int64_t)nf * ms + kWarps - 1) / kWarps, (int64_t)sms * 8);
+        const int grid = (int)std::min<int64_t>(((int64_t)nf * ms + kWarps - 1) / kWarps, (int64_t)sms * h->real_ctas);
         // FP32: one lane per solvent atom; the frames that need several images
         // per molecule pair are left to the generic kernel below
         const bool special = fp32;
         if (fp32) {
+            // the accumulators before the real pass, for a redo after a queue overflow
+            CM_CUDA(cudaMemcpyAsync(h->hist_snap.p, h->hist.p, (size_t)h->hist_n * 8, cudaMemcpyDeviceToDevice, st));
+            CM_CUDA(cudaMemcpyAsync(h->stats_snap.p, h->stats.p, ST_N * 8, cudaMemcpyDeviceToDevice, st));
             const size_t fsm = hsm + (size_t)kFlatWarps * flat_warp_smem();
             const int fgrid = (int)std::min<int64_t>(((int64_t)nf * ms + kFlatWarps - 1) / kFlatWarps,
                                                      (int64_t)sms * h->flat_ctas);
@@ -1007,10 +1029,21 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         else if (self) CM_LAUNCH(CM_K_REAL, k_pairs_real<false, true><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
         else CM_LAUNCH(CM_K_REAL, k_pairs_real<false, false><<<grid, kWarps * 32, smem, st>>>(S, B, only_multi));
         if (special) {
-            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_guard<true><<<sms * 4, kGuardWarps * 32, hsm, st>>>(S, B));
-            else CM_LAUNCH(CM_K_GUARD, k_pairs_guard<false><<<sms * 4, kGuardWarps * 32, hsm, st>>>(S, B));
-            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_edge<true><<<sms * 4, 128, hsm, st>>>(S, B));
-            else CM_LAUNCH(CM_K_GUARD, k_pairs_edge<false><<<sms * 4, 128, hsm, st>>>(S, B));
+            const int ggrid = sms * h->guard_ctas, egrid = sms * h->edge_ctas;
+            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_guard<true><<<ggrid, kGuardWarps * 32, hsm, st>>>(S, B));
+            else CM_LAUNCH(CM_K_GUARD, k_pairs_guard<false><<<ggrid, kGuardWarps * 32, hsm, st>>>(S, B));
+            if (self) CM_LAUNCH(CM_K_GUARD, k_pairs_edge<true><<<egrid, 128, hsm, st>>>(S, B));
+            else CM_LAUNCH(CM_K_GUARD, k_pairs_edge<false><<<egrid, 128, hsm, st>>>(S, B));
+            // a guard or edge queue overflow: the accumulators go back to the
+            // snapshot and the generic kernel redoes every frame of the chunk,
+            // deciding each record where it is found (both launches return at
+            // once otherwise)
+            const int64_t nrest = std::max<int64_t>(h->hist_n, ST_N);
+            CM_LAUNCH(CM_K_GUARD, k_queue_check<<<(int)std::min<int64_t>(grid_for(nrest, 256), (int64_t)sms * 4), 256, 0, st>>>(
+                                      B, P<unsigned long long>(h->hist), P<unsigned long long>(h->hist_snap), h->hist_n,
+                                      P<unsigned long long>(h->stats), P<unsigned long long>(h->stats_snap)));
+            if (self) CM_LAUNCH(CM_K_REAL, k_pairs_real<true, true><<<grid, kWarps * 32, smem, st>>>(S, B, 2));
+            else CM_LAUNCH(CM_K_REAL, k_pairs_real<true, false><<<grid, kWarps * 32, smem, st>>>(S, B, 2));
         }
         if (rnd) {
             CM_LAUNCH(CM_K_BULK, k_bulk<<<c.ntab, 1024, 0, st>>>(S, B, dtab + c.tab0));
@@ -1020,8 +1053,8 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
                 const int ny = std::min(piece, c.nsmp - s0);
                 if (s0 > 0) CM_CUDA(cudaMemsetAsync(B.counters + 1, 0, sizeof(int), st));
                 CM_LAUNCH(CM_K_RANDOM, k_random_filter<<<grid_for((int64_t)ny * mv, 128), 128, 0, st>>>(S, B, c.smp0 + s0, ny));
-                if (fp32) CM_LAUNCH(CM_K_RANDOM, k_random_eval<true><<<sms * 4, 128, hsm, st>>>(S, B));
-                else CM_LAUNCH(CM_K_RANDOM, k_random_eval<false><<<sms * 4, 128, hsm, st>>>(S, B));
+                if (fp32) CM_LAUNCH(CM_K_RANDOM, k_random_eval<true><<<sms * h->rand_ctas, 128, hsm, st>>>(S, B));
+                else CM_LAUNCH(CM_K_RANDOM, k_random_eval<false><<<sms * h->rand_ctas, 128, hsm, st>>>(S, B));
             }
         }
     } else {
@@ -1358,7 +1391,7 @@ void check_device_error(cm_handle *h) {
         std::string m = "device-side check failed:";
         if (e & ERR_STENCIL) m += " search range wider than the offset table (box too small for the cutoff);";
         if (e & ERR_BIN) m += " histogram bin out of range;";
-        if (e & ERR_QUEUE) m += " guard or random-insertion queue overflow (rerun with FP64 precision);";
+        if (e & ERR_QUEUE) m += " random-insertion or molecule-pair queue overflow;";
         if (e & ERR_SIZE) m += " molecule too large for the PAIRS layout;";
         throw cm_error(CM_EDEVICE, m);
     }
@@ -1390,7 +1423,7 @@ void free_all(cm_handle *h) {
     // the blocks go back to the cache: nothing of this handle may still use them
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
-    DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag,
+    DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag, &h->hist_snap, &h->stats_snap,
                      &h->slot, &h->flags, &h->bulk, &h->nbulk, &h->tabs, &h->counters, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
                      &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->eq, &h->rq, &h->akey, &h->atq32,
@@ -1433,8 +1466,8 @@ void free_all(cm_handle *h) {
 //
 // Every device buffer the frame needs beyond the caller's coordinates and
 // output lives in g_noalloc_scratch, a file-scope array of
-// CM_NOALLOC_SCRATCH_BYTES.  Its address is looked up once per device, with
-// that device current, by the first call on the device.  All calls share the
+// CM_NOALLOC_SCRATCH_BYTES.  Each call looks up its address with the call's
+// device current (cudaGetSymbolAddress).  All calls share the
 // array and find the previous call's contents in it: each call clears what
 // must start at zero (frame scratch, queue counters, cell counts, bulk flags,
 // the slot table, statistics, the error flag and the output), and calls whose
@@ -1444,19 +1477,16 @@ namespace {
 __device__ __align__(256) unsigned char g_noalloc_scratch[CM_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-unsigned char *g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
-unsigned char *noalloc_scratch(int device) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            throw cm_error(CM_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-        g_noalloc_ptr[device] = (unsigned char *)p;
-    }
-    return g_noalloc_ptr[device];
+// The array's device address in the current context, looked up on every call
+// (a driver query, no stream work): a caller that runs calls in another
+// context of the same device, or after cudaDeviceReset, gets the address that
+// is valid there, never a stale one.
+unsigned char *noalloc_scratch() {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) throw cm_error(CM_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    return (unsigned char *)p;
 }
 
 // Bump allocator over the scratch array, 256-byte aligned pieces.  With a
@@ -1487,8 +1517,12 @@ void noalloc_fixed(cm_handle *h, Carve &c) {
     c.take(h->fscratch, sizeof(FrameScratch));
     c.take(h->off64, sizeof(d4) * cmgeom::kOffEntries);
     c.take(h->off32, sizeof(float4) * cmgeom::kOffEntries);
-    c.take(h->counters, 16);
+    c.take(h->counters, 8 * sizeof(int));
     c.take(h->stats, ST_N * 8);
+    if (d.precision == CM_PRECISION_FP32_GUARD) {
+        c.take(h->hist_snap, (size_t)h->hist_n * 8);
+        c.take(h->stats_snap, ST_N * 8);
+    }
     c.take(h->errflag, 8);
     if (h->mddf) {
         const int nd = h->ndist_max;
@@ -1514,6 +1548,7 @@ void noalloc_fixed(cm_handle *h, Carve &c) {
     c.take(h->cmol, mv * 4);
     c.take(h->cq32, mv * 16);
     h->gq_cap = (int)std::min<int64_t>(std::max<int64_t>(ms * mv, 1024), 1 << 17);
+    if (d.guard_queue_capacity > 0) h->gq_cap = std::min(h->gq_cap, d.guard_queue_capacity);
     c.take(h->gq, (size_t)h->gq_cap * sizeof(int4));
     c.take(h->eq, (size_t)h->gq_cap * 3 * sizeof(int4));
     if (h->mddf) {
@@ -1559,7 +1594,7 @@ thread_local int4 t_noalloc_tab[CM_NOALLOC_MAX_SAMPLES];
 template <typename T>
 void noalloc_run(cm_handle *h, const cm_frames *f, cudaStream_t stream) {
     const cm_system_desc &d = h->d;
-    Carve c{noalloc_scratch(h->device), 0};
+    Carve c{noalloc_scratch(), 0};
     noalloc_fixed(h, c);
     const T *xs = (const T *)f->solute_xyz;
     const T *xv = d.autocorrelation ? nullptr : (const T *)f->solvent_xyz;
@@ -1591,7 +1626,7 @@ void noalloc_run(cm_handle *h, const cm_frames *f, cudaStream_t stream) {
 
     // the frame on its cell grid
     memset(&G, 0, sizeof(G));
-    frame_geometry(f->cells, h->pair_cell, 1023, G);
+    frame_geometry(f->cells, target_cell(h), 1023, G);
     G.weight = 1.0;
     G.frame_id = f->frame_ids[0];
     Chunk one;
@@ -1626,7 +1661,7 @@ void noalloc_run(cm_handle *h, const cm_frames *f, cudaStream_t stream) {
         std::string m = "device-side check failed:";
         if (e & ERR_STENCIL) m += " search range wider than the offset table (box too small for the cutoff);";
         if (e & ERR_BIN) m += " histogram bin out of range;";
-        if (e & ERR_QUEUE) m += " guard queue overflow (rerun with FP64 precision);";
+        if (e & ERR_QUEUE) m += " random-insertion queue overflow;";
         if (e & ERR_SIZE) m += " molecule too large for the PAIRS layout;";
         throw cm_error(CM_EDEVICE, m);
     }
@@ -1904,6 +1939,10 @@ int cm_create(const cm_system_desc *desc, cm_handle **out) {
         dev_alloc(h, h->sums, h->hist_n * 8);
         dev_alloc(h, h->stats, ST_N * 8);
         dev_alloc(h, h->errflag, 8);
+        if (desc->precision == CM_PRECISION_FP32_GUARD) {
+            dev_alloc(h, h->hist_snap, h->hist_n * 8);
+            dev_alloc(h, h->stats_snap, ST_N * 8);
+        }
         CM_CUDA(cudaMemsetAsync(h->hist.p, 0, h->hist_n * 8, h->stream));
         CM_CUDA(cudaMemsetAsync(h->sums.p, 0, h->hist_n * 8, h->stream));
         CM_CUDA(cudaMemsetAsync(h->stats.p, 0, ST_N * 8, h->stream));

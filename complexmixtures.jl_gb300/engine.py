@@ -56,6 +56,7 @@ def system_desc(
     cell_scale_pct: int = 0,
     launch: str = "auto",
     atoms_schedule: str = "auto",
+    guard_queue_capacity: int = 0,
 ):
     """cm_system_desc of a system, and the arrays it points to (keep them
     alive while the description is in use).  ``cell_scale_pct`` scales the
@@ -63,7 +64,10 @@ def system_desc(
     or "graph") says whether each compute chunk's kernels are launched one by
     one or replayed as a captured CUDA graph; ``atoms_schedule`` ("auto",
     "cell" or "balanced") picks the ATOMS-layout evaluation schedule (both
-    speed only)."""
+    speed only); ``guard_queue_capacity`` (0 = sized by the engine) bounds the
+    FP32 real pass's guard and edge queues per compute chunk: a chunk that
+    overflows them is redone on the device without queues, so the counts do
+    not depend on it."""
     d = N.cm_system_desc()
     d.api_version = N.CM_API_VERSION
     d.solute_nmols = solute_nmols
@@ -108,6 +112,7 @@ def system_desc(
     if atoms_schedule not in SCHEDULES:
         raise ValueError(f"atoms_schedule must be one of {sorted(SCHEDULES)}")
     d.atoms_schedule = SCHEDULES[atoms_schedule]
+    d.guard_queue_capacity = guard_queue_capacity
     return d, keep
 
 

@@ -41,7 +41,7 @@
 extern "C" {
 #endif
 
-#define CM_API_VERSION 2
+#define CM_API_VERSION 3
 
 typedef enum cm_status {
     CM_OK = 0,
@@ -123,6 +123,11 @@ typedef struct cm_system_desc {
                                          the counts do not depend on it, only the speed (cm_autotune) */
     int32_t launch;                   /* CM_LAUNCH_*; the counts do not depend on it */
     int32_t atoms_schedule;           /* CM_SCHED_*; the counts do not depend on it */
+    int32_t guard_queue_capacity;     /* records per compute chunk of the FP32 real pass's guard and edge
+                                         queues; 0 = sized by the engine.  A chunk whose deferred records
+                                         do not fit is redone on the device without queues, so the counts
+                                         do not depend on it (a small value only exercises that path) */
+    int32_t reserved;                 /* must be 0 */
 } cm_system_desc;
 
 /*
@@ -515,11 +520,18 @@ const char *cm_server_last_error(const cm_server *s);
  * the PAIRS layout (at most 32 atoms per molecule), default per-atom groups,
  * frame->nframes == 1 with coordinates in device memory and weights NULL,
  * n_random_samples <= CM_NOALLOC_MAX_SAMPLES, and the frame's buffers within
- * the scratch array (the message gives the size needed).
+ * the scratch array (the message gives the size needed).  Of the tuning
+ * fields, cell_scale_pct and guard_queue_capacity are honoured; launch,
+ * atoms_schedule, max_frames_per_batch, hbm_budget_bytes and kernel_timing
+ * are ignored.  The guard and edge queues hold at most 131,072 records: a
+ * frame that defers more is redone on the device without queues (slower,
+ * the same counts).
  *
- * The first call on a device looks up the scratch array's address
- * (cudaGetSymbolAddress, with desc->device current); make that first call
- * before any stream capture.  Every call shares the array and finds the
+ * Every call looks up the scratch array's address in the current context
+ * (cudaGetSymbolAddress, with desc->device current), so calls from another
+ * context of the device, or after cudaDeviceReset, use the address valid
+ * there.  The first call in a context may load the library's device code:
+ * make it before any stream capture.  Every call shares the array and finds the
  * previous call's contents in it; each call clears what must start at zero.
  * Calls whose GPU work overlaps (several streams or host threads) race on the
  * array.  Work is ordered on `stream` (NULL: the legacy default stream) and

@@ -112,7 +112,7 @@ def make_system(rng, H, ms, aps, mv, apv, nframes, self_mode, spread=0.9):
 
 
 def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, regime, frame_ids=None, groups=None,
-            backend="cells", dtype=np.float64, cell_scale_pct=0, atoms_schedule="auto", **opt):
+            backend="cells", dtype=np.float64, cell_scale_pct=0, atoms_schedule="auto", engine_kw=None, **opt):
     nf = xs.shape[0]
     frame_ids = list(range(1, nf + 1)) if frame_ids is None else frame_ids
     kw = dict(autocorrelation=self_mode, **opt)
@@ -126,7 +126,7 @@ def compare(cm, orc, *, ms, aps, mv, apv, xs, xv, cells, self_mode, precision, r
         g = dict(solute_groups=gs, solute_ngroups=5, solvent_groups=gv, solvent_ngroups=5)
     eng = cm.Engine(solute_nmols=ms, solute_natomspermol=aps, solvent_nmols=mv, solvent_natomspermol=apv,
                     precision=precision, regime=regime, max_frames_per_batch=2, cell_scale_pct=cell_scale_pct,
-                    atoms_schedule=atoms_schedule, **kw,
+                    atoms_schedule=atoms_schedule, **kw, **(engine_kw or {}),
                     **g)
     eng.submit(xs.astype(dtype), None if self_mode else xv.astype(dtype), cells, frame_ids=frame_ids)
     got = eng.raw_counts()

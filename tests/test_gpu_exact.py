@@ -23,7 +23,7 @@ well (their placements are not on the lattice).
 import numpy as np
 import pytest
 
-from helpers import KEYS, compare, golden
+from helpers import KEYS, TRICLINIC, compare, golden, make_system
 
 pytestmark = pytest.mark.gpu
 
@@ -166,3 +166,25 @@ def test_toy_cross_every_bin(cm, orc, gpu_ready, precision, regime):
     assert ref["md"][449] == 2 * 2 and ref["md"].sum() == 2 * 2
     for k in KEYS:
         assert np.array_equal(got[k], ref[k]), k
+
+
+@pytest.mark.parametrize("lattice", [True, False], ids=["lattice", "random"])
+@pytest.mark.parametrize("self_mode", [False, True], ids=["cross", "self"])
+def test_guard_queue_overflow_finishes_on_the_gpu(cm, orc, gpu_ready, lattice, self_mode):
+    """A guard and edge queue of one record per compute chunk: nearly every
+    chunk overflows it, is redone on the device without queues, and the
+    counts are still the oracle's."""
+    rng = np.random.default_rng(105)
+    if lattice:
+        H = TRICLINIC_INT
+        xs = lattice_frames(rng, lattice_mols(rng, 40 if self_mode else 12, T5, box_of(H)), 3, 5)
+        xv = None if self_mode else lattice_frames(rng, lattice_mols(rng, 260, T3, box_of(H)), 3, 3)
+        cells = np.repeat(H[None], 3, axis=0)
+    else:
+        xs, xv, cells = make_system(rng, TRICLINIC, 40 if self_mode else 12, 5, 260, 3, 3, self_mode)
+    mv, apv = (40, 5) if self_mode else (260, 3)
+    opt = dict(OPT, dbulk=5.0, usecutoff=True, binstep=0.02, nbins=bins_for(0.02))
+    got, ref, st = compare(cm, orc, ms=40 if self_mode else 12, aps=5, mv=mv, apv=apv, xs=xs, xv=xv, cells=cells,
+                           self_mode=self_mode, precision="fp32", regime="pairs", groups="custom",
+                           engine_kw=dict(guard_queue_capacity=1), **opt)
+    assert ref["md"].sum() > 0

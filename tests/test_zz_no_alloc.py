@@ -1,10 +1,12 @@
 """Allocation-free entry point cm_frame_counts_noalloc, called through the C ABI.
 
 Its counts for one frame must equal, bit for bit, what cm_submit_frames +
-cm_read_raw_counts give for a handle that was given only that frame.  Two
-calls in a row on different frames (and then on a different system) check that
-each call clears the shared static scratch the previous call left behind.
-The file is named to be collected last, and passes alone in a fresh process.
+cm_read_raw_counts give for a handle that was given only that frame, and the
+oracle's.  Two calls in a row on different frames (and then on a different
+system) check that each call clears the shared static scratch the previous
+call left behind, and the device's free memory must not move while calls run
+(the entry point exists for callers that cannot allocate).  The file is named
+to be collected last, and passes alone in a fresh process.
 """
 import ctypes as C
 
@@ -65,16 +67,24 @@ def engine_counts(cm, *, ms, aps, mv, apv, self_mode, precision, xs, xv, cell, f
     return np.concatenate(parts)
 
 
-def noalloc_counts(cm, *, ms, aps, mv, apv, self_mode, precision, xs, xv, cell, frame_id):
+def device_inputs(xs, xv, n):
+    """The call's device buffers (made by torch, outside the entry point)."""
+    import torch
+
+    xs_d = torch.from_numpy(np.ascontiguousarray(xs[None])).cuda()
+    xv_d = None if xv is None else torch.from_numpy(np.ascontiguousarray(xv[None])).cuda()
+    out = torch.full((n,), -7, dtype=torch.int64, device="cuda")  # overwritten by the call
+    return xs_d, xv_d, out
+
+
+def noalloc_counts(cm, *, ms, aps, mv, apv, self_mode, precision, xs, xv, cell, frame_id, bufs=None):
     import torch
 
     N = cm._native
     lib = N.load()
     d = desc_of(N, ms=ms, aps=aps, mv=mv, apv=apv, self_mode=self_mode, precision=precision)
-    xs_d = torch.from_numpy(np.ascontiguousarray(xs[None])).cuda()
-    xv_d = None if xv is None else torch.from_numpy(np.ascontiguousarray(xv[None])).cuda()
     n = counts_len(aps=aps, apv=apv, self_mode=self_mode)
-    out = torch.full((n,), -7, dtype=torch.int64, device="cuda")  # overwritten by the call
+    xs_d, xv_d, out = bufs if bufs is not None else device_inputs(xs, xv, n)
     cm_cols = np.ascontiguousarray(cell.T).reshape(9)  # column-major: columns are lattice vectors
     ids = np.array([frame_id], dtype=np.int64)
     fr = N.cm_frames()
@@ -109,6 +119,47 @@ def test_noalloc_matches_engine_on_consecutive_calls(cm, gpu_ready):
         assert np.array_equal(got[k], b), k
         assert got[k][:OPT["nbins"]].sum() > 0
     assert not np.array_equal(got[0], got[1])
+
+
+@pytest.mark.gpu
+def test_noalloc_matches_oracle_bin_by_bin(cm, orc, gpu_ready):
+    """A small cross system, both precisions: every bin equals the oracle's."""
+    rng = np.random.default_rng(11)
+    xs, xv, cells = system(rng, np.diag([24.0, 25.0, 26.0]), 20, 4, 200, 3, 1, False)
+    ref = orc.run(ms=20, aps=4, mv=200, apv=3, solute_xyz=xs, solvent_xyz=xv, cells=cells, frame_ids=[5],
+                  autocorrelation=False, **OPT)
+    expect = np.concatenate([ref[k].ravel() for k in KEYS])
+    assert expect[:OPT["nbins"]].sum() > 0
+    for prec in ("fp32", "fp64"):
+        got = noalloc_counts(cm, ms=20, aps=4, mv=200, apv=3, self_mode=False, precision=prec, xs=xs[0], xv=xv[0],
+                             cell=cells[0], frame_id=5)
+        assert np.array_equal(got, expect), prec
+
+
+@pytest.mark.gpu
+def test_noalloc_allocates_no_device_memory(cm, gpu_ready):
+    """After a first call (which may load the library's kernels), further
+    calls, one of them on a larger system, leave the device's free memory
+    where it was: every input and output buffer is made before the reading."""
+    import torch
+
+    rng = np.random.default_rng(13)
+    small = system(rng, np.diag([26.0, 28.0, 27.0]), 150, 3, 150, 3, 2, True)
+    large = system(rng, np.diag([60.0, 62.0, 61.0]), 2000, 3, 2000, 3, 1, True)
+    n = counts_len(aps=3, apv=3, self_mode=True)
+    calls = [(150, small, 0), (150, small, 1), (2000, large, 0), (150, small, 0)]
+    bufs = [device_inputs(sysd[0][k], None, n) for _, sysd, k in calls]
+    out = []
+    free0 = None
+    for i, ((m, (xs, _, cells), k), b) in enumerate(zip(calls, bufs)):
+        out.append(noalloc_counts(cm, ms=m, aps=3, mv=m, apv=3, self_mode=True, precision="fp32", xs=xs[k], xv=None,
+                                  cell=cells[k], frame_id=k + 1, bufs=b))
+        torch.cuda.synchronize()
+        free = torch.cuda.mem_get_info()[0]
+        if i == 0:
+            free0 = free
+        assert free == free0, (i, free0 - free)
+    assert np.array_equal(out[0], out[3]) and out[2][:OPT["nbins"]].sum() > 0
 
 
 @pytest.mark.gpu
