@@ -247,6 +247,8 @@ EXPORTED = (
     "cm_batch_last_error",
     "cm_read_counts",
     "cm_read_raw_counts",
+    "cm_raw_counts_weight",
+    "cm_load_raw_counts",
     "cm_read_results",
     "cm_contributions",
     "cm_get_stats",
@@ -301,6 +303,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_read_counts.restype = C.c_int
     lib.cm_read_raw_counts.argtypes = [H, C.POINTER(cm_raw_counts)]
     lib.cm_read_raw_counts.restype = C.c_int
+    lib.cm_raw_counts_weight.argtypes = [H, C.POINTER(C.c_double)]
+    lib.cm_raw_counts_weight.restype = C.c_int
+    lib.cm_load_raw_counts.argtypes = [H, C.POINTER(cm_raw_counts), C.c_double, C.c_int64, C.c_double]
+    lib.cm_load_raw_counts.restype = C.c_int
     lib.cm_get_stats.argtypes = [H, C.POINTER(cm_stats)]
     lib.cm_get_stats.restype = C.c_int
     lib.cm_get_kernel_times.argtypes = [H, C.POINTER(cm_kernel_times)]

@@ -11,6 +11,7 @@
 // mddf_frame! (src/mddf.jl:361-429), coordination_number_frame!
 // (src/mddf.jl:438-471) and sum! (src/results.jl:629-649).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -27,6 +28,19 @@
 #include "cm_flat32.cuh"
 #include "cm_final.cuh"
 #include "cm_grid3d.cuh"
+
+namespace {
+// NVTX range over a host scope (header-only NVTX v3: a no-op unless a
+// profiler is attached), named after the stage of the reference's frame loop
+// it covers; the reference reports the same stages as progress
+// (src/mddf.jl:251, 279-282).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+}  // namespace
 
 using namespace cmk;
 using cmgeom::FrameGeom;
@@ -978,6 +992,7 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
                const T *xv) {
     const cm_system_desc &d = h->d;
     cudaStream_t st = h->stream;
+    NvtxRange range("cm: chunk (mddf_frame! of each frame)");
     ensure_cells(h, c.ncell_max);
     DevSys S = devsys_full(h);
     Bufs B = chunk_bufs(h, c, dG, dS);
@@ -1228,6 +1243,7 @@ void check_frames(cm_handle *h, const cm_frames *f) {
 // Host preparation (geometries, random samples, chunking) and the copies of
 // one staging batch; the copies end with ev_copied[b] on the copy stream.
 Staged stage(cm_handle *h, const cm_frames *f, int f0) {
+    NvtxRange range("cm: stage batch (geometry, samples, copies)");
     const cm_system_desc &d = h->d;
     Staged S;
     const bool dcd = f->coord_type == CM_COORD_DCD;
@@ -1668,6 +1684,7 @@ void noalloc_run(cm_handle *h, const cm_frames *f, cudaStream_t stream) {
 }
 
 int noalloc_frame(const cm_system_desc *desc, const cm_frames *f, int64_t *counts, int64_t counts_len, void *stream) {
+    NvtxRange range("cm: allocation-free frame");
     int prev = -1;
     try {
         check_desc(desc);
@@ -2043,6 +2060,7 @@ int cm_batch_create(cm_handle *const *handles, int32_t nhandles, cm_batch **out)
 }
 
 int cm_batch_submit(cm_batch *b, const cm_frames *frames) {
+    NvtxRange range("cm: batch submit (all systems)");
     return batch_guarded(b, [&] {
         if (!frames) throw cm_error(CM_EINVAL, "NULL frames");
         int rounds = 0;
@@ -2082,6 +2100,7 @@ const char *cm_batch_last_error(const cm_batch *b) {
 
 int cm_read_counts(cm_handle *h, cm_counts *out) {
     return guarded(h, [&] {
+        NvtxRange range("cm: read counts");
         if (!out) throw cm_error(CM_EINVAL, "NULL output");
         check_device_error(h);
         std::vector<unsigned long long> acc(h->hist_n);
@@ -2118,6 +2137,7 @@ int cm_read_counts(cm_handle *h, cm_counts *out) {
 // FinalVec vectors, group blocks, FinalScalar scalars); returns its length in
 // doubles.  Asynchronous on the handle's stream.
 static int64_t launch_finalize(cm_handle *h, double frame_weight_sum) {
+    NvtxRange range("cm: finalresults (k_finalize)");
     if (!(frame_weight_sum >= 0.0) || !std::isfinite(frame_weight_sum))
         throw cm_error(CM_EINVAL, "frame_weight_sum must be finite and non-negative");
     check_device_error(h);
@@ -2190,6 +2210,7 @@ int cm_read_results(cm_handle *h, double frame_weight_sum, cm_results *out) {
 
 int cm_contributions(cm_handle *h, double frame_weight_sum, int32_t nqueries, const cm_contrib_query *queries,
                      double *out) {
+    NvtxRange range("cm: contributions (k_contrib)");
     return guarded(h, [&] {
         if (nqueries < 1 || !queries || !out) throw cm_error(CM_EINVAL, "contributions need at least one query and an output");
         if (nqueries > 65535) throw cm_error(CM_EINVAL, "at most 65535 queries per call");
@@ -2336,6 +2357,54 @@ int cm_reset(cm_handle *h) {
     });
 }
 
+int cm_raw_counts_weight(cm_handle *h, double *frame_weight) {
+    return guarded(h, [&] {
+        if (!frame_weight) throw cm_error(CM_EINVAL, "NULL output");
+        if (h->folds > 0) throw cm_error(CM_ESTATE, "raw counts are defined only while all frames carry one weight");
+        *frame_weight = h->class_open ? h->class_w : 1.0;
+    });
+}
+
+int cm_load_raw_counts(cm_handle *h, const cm_raw_counts *in, double frame_weight, int64_t frames, double volume_total) {
+    return guarded(h, [&] {
+        if (!in || !in->md || !in->md_random || !in->rdf || !in->rdf_random || !in->solute_group ||
+            !in->solute_group_random)
+            throw cm_error(CM_EINVAL, "md, md_random, rdf, rdf_random, solute_group and solute_group_random are required");
+        if (!h->d.autocorrelation && (!in->solvent_group || !in->solvent_group_random))
+            throw cm_error(CM_EINVAL, "solvent_group and solvent_group_random are required unless autocorrelation");
+        if (!(frame_weight > 0.0) || !std::isfinite(frame_weight)) throw cm_error(CM_EINVAL, "frame_weight must be finite and positive");
+        if (frames < 0) throw cm_error(CM_EINVAL, "frames must be >= 0");
+        if (!std::isfinite(volume_total)) throw cm_error(CM_EINVAL, "volume_total must be finite");
+        const int64_t nb = h->d.nbins;
+        std::vector<int64_t> acc(h->hist_n, 0);
+        auto get = [&](const int64_t *src, int64_t off, int64_t n) {
+            for (int64_t i = 0; i < n; ++i) {
+                if (src[i] < 0) throw cm_error(CM_EINVAL, "counts must be non-negative");
+                acc[off + i] = src[i];
+            }
+        };
+        get(in->md, h->o_md, nb);
+        get(in->md_random, h->o_mdr, nb);
+        get(in->rdf, h->o_rdf, nb);
+        get(in->rdf_random, h->o_rdfr, nb);
+        get(in->solute_group, h->o_gs, h->Gs * nb);
+        get(in->solute_group_random, h->o_gsr, h->Gs * nb);
+        if (!h->d.autocorrelation) {
+            get(in->solvent_group, h->o_gv, h->Gv * nb);
+            get(in->solvent_group_random, h->o_gvr, h->Gv * nb);
+        }
+        check_device_error(h);  // the handle's earlier work is done (synchronised)
+        CM_CUDA(cudaMemcpy(h->hist.p, acc.data(), h->hist_n * 8, cudaMemcpyHostToDevice));
+        CM_CUDA(cudaMemset(h->sums.p, 0, h->hist_n * 8));
+        h->class_open = true;
+        h->class_w = frame_weight;
+        h->folds = 0;
+        h->frames = frames;
+        h->weight_total = frame_weight * (double)frames;
+        h->volume_total = volume_total;
+    });
+}
+
 int cm_destroy(cm_handle *h) {
     if (!h) return CM_OK;
     cudaSetDevice(h->device);
@@ -2365,6 +2434,7 @@ const char *cm_status_string(int status) {
 int64_t cm_device_bytes(const cm_handle *h) { return h ? h->device_bytes : 0; }
 
 int cm_grid3d(const cm_grid3d_desc *D, cm_grid3d_out *out) {
+    NvtxRange range("cm: grid3D (k_grid3d)");
     if (!D || !out) {
         g_create_error = "NULL argument";
         return CM_EINVAL;

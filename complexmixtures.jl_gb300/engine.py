@@ -393,6 +393,35 @@ class Engine:
         self._inflight.clear()
         return out
 
+    def snapshot(self) -> dict:
+        """Exact state of the accumulators for a later resume: the half-unit
+        counts, the frame weight they were computed with, the frames and the
+        weighted volume sum (single-weight runs, as ``raw_counts``)."""
+        snap = self.raw_counts()
+        w = C.c_double(0.0)
+        N.raise_for(self._lib.cm_raw_counts_weight(self._h, C.byref(w)), self._h)
+        c = self.counts()
+        snap.update(frame_weight=w.value, frames=int(c["frames"]), volume_total=float(c["volume_total"]))
+        return snap
+
+    def restore(self, snap: dict) -> None:
+        """Load a snapshot (``snapshot``, ``load_snapshot`` or
+        ``snapshot_from_result``) into this engine (cm_load_raw_counts):
+        frames submitted afterwards add to it, so frames 1..k, a snapshot and
+        frames k+1..n on a restored engine give the counts of one run over
+        1..n."""
+        keep = {}
+        c = N.cm_raw_counts()
+        for k in ("md", "md_random", "rdf", "rdf_random", "solute_group", "solute_group_random", "solvent_group",
+                  "solvent_group_random"):
+            if k.startswith("solvent") and self.autocorrelation:
+                continue
+            keep[k] = np.ascontiguousarray(snap[k], dtype=np.int64)
+            setattr(c, k, N.as_ptr(keep[k], C.c_int64))
+        st = self._lib.cm_load_raw_counts(self._h, C.byref(c), float(snap["frame_weight"]), int(snap["frames"]),
+                                          float(snap["volume_total"]))
+        N.raise_for(st, self._h)
+
     def stats(self) -> dict:
         s = N.cm_stats()
         st = self._lib.cm_get_stats(self._h, C.byref(s))
@@ -485,3 +514,23 @@ class Batch:
     def __exit__(self, *exc):
         self.close()
 
+
+SNAPSHOT_COUNTS = ("md", "md_random", "rdf", "rdf_random", "solute_group", "solute_group_random", "solvent_group",
+                   "solvent_group_random")
+
+
+def save_snapshot(filename: str, snap: dict) -> str:
+    """Write an engine snapshot (exact int64 half-unit counts and the frame
+    weight, frames and volume sum behind them) as a compressed .npz."""
+    np.savez_compressed(filename, **{k: np.asarray(snap[k]) for k in SNAPSHOT_COUNTS},
+                        frame_weight=np.float64(snap["frame_weight"]), frames=np.int64(snap["frames"]),
+                        volume_total=np.float64(snap["volume_total"]))
+    return filename
+
+
+def load_snapshot(filename: str) -> dict:
+    """Read a snapshot written by ``save_snapshot``."""
+    with np.load(filename, allow_pickle=False) as z:
+        snap = {k: np.array(z[k], dtype=np.int64) for k in SNAPSHOT_COUNTS}
+        snap.update(frame_weight=float(z["frame_weight"]), frames=int(z["frames"]), volume_total=float(z["volume_total"]))
+    return snap

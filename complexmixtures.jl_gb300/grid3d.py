@@ -134,10 +134,40 @@ def grid3D(result: Result, atoms: Atoms, output_file: Optional[str] = None, *, d
         raise ValueError("type must be :mddf, :coordination_number or :md_count")
     sel = result.solute
     idx = np.asarray(sel.indices, dtype=np.int64)
-    xyz = np.ascontiguousarray(atoms.xyz[idx - 1], dtype=np.float64)
-    atype = np.ascontiguousarray(((idx - idx[0]) % sel.natomspermol).astype(np.int32))
-    table = np.ascontiguousarray(atom_contribution_table(result, type), dtype=np.float64)
-    d = np.ascontiguousarray(result.d, dtype=np.float64)
+    xyz = atoms.xyz[idx - 1]
+    atype = (idx - idx[0]) % sel.natomspermol
+    point, atom, dist, val, n, origin = grid_search(xyz, atype, atom_contribution_table(result, type), result.d,
+                                                    dmin=dmin, dmax=dmax, step=step, device=device)
+    k = len(point)
+    ix, rem = np.divmod(point, n[1] * n[2])
+    iy, iz = np.divmod(rem, n[2])
+    pos = [origin[a] + step * i.astype(np.float64) for a, i in enumerate((ix, iy, iz))]
+    # beta scaled to [0, 1] over the kept points (src/tools/grid3D.jl:139-146)
+    bmin, bmax = (val.min(), val.max()) if k else (0.0, 1.0)
+    beta = (val - bmin) / (bmax - bmin) if k else val
+    gi = idx[atom] if k else np.zeros(0, dtype=np.int64)
+    g = Grid3D(pos[0], pos[1], pos[2], gi, dist, val, beta, [atoms.name[i - 1] for i in gi],
+               [atoms.resname[i - 1] for i in gi], [atoms.chain[i - 1] for i in gi], [atoms.resnum[i - 1] for i in gi],
+               [atoms.element[i - 1] for i in gi], n, origin)
+    if output_file is not None:
+        g.write_pdb(output_file)
+        if not silent:
+            print(f"Grid written to {output_file}")
+    return g
+
+
+def grid_search(xyz, atom_type, table, d, *, dmin: float, dmax: float, step: float, device: int = 0):
+    """The grid search of grid3D on the GPU (cm_grid3d): every point of the
+    grid around the atoms ``xyz`` whose closest atom lies between dmin and
+    dmax, with that atom's contribution curve ``table[atom_type[atom]]``
+    (over the distances ``d``) interpolated at the distance, kept when
+    positive.  Returns, in ascending grid order, the points' linear indices,
+    the closest atoms (0-based), the distances and the values, plus the grid
+    shape and origin."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    atype = np.ascontiguousarray(np.asarray(atom_type).astype(np.int32))
+    table = np.ascontiguousarray(table, dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
     lib = N.load()
     desc = N.cm_grid3d_desc(device=device, nbins=len(d), natoms=len(xyz), ntypes=table.shape[0], dmin=dmin,
                             dmax=dmax, step=step)
@@ -159,21 +189,4 @@ def grid3D(result: Result, atoms: Atoms, output_file: Optional[str] = None, *, d
     out.value = N.as_ptr(val, C.c_double)
     N.raise_for(lib.cm_grid3d(C.byref(desc), C.byref(out)), None)
     k = int(out.count)
-    point, atom, dist, val = point[:k], atom[:k], dist[:k], val[:k]
-    n = tuple(int(v) for v in out.n)
-    origin = np.array(list(out.origin))
-    ix, rem = np.divmod(point, n[1] * n[2])
-    iy, iz = np.divmod(rem, n[2])
-    pos = [origin[a] + step * i.astype(np.float64) for a, i in enumerate((ix, iy, iz))]
-    # beta scaled to [0, 1] over the kept points (src/tools/grid3D.jl:139-146)
-    bmin, bmax = (val.min(), val.max()) if k else (0.0, 1.0)
-    beta = (val - bmin) / (bmax - bmin) if k else val
-    gi = idx[atom] if k else np.zeros(0, dtype=np.int64)
-    g = Grid3D(pos[0], pos[1], pos[2], gi, dist, val, beta, [atoms.name[i - 1] for i in gi],
-               [atoms.resname[i - 1] for i in gi], [atoms.chain[i - 1] for i in gi], [atoms.resnum[i - 1] for i in gi],
-               [atoms.element[i - 1] for i in gi], n, origin)
-    if output_file is not None:
-        g.write_pdb(output_file)
-        if not silent:
-            print(f"Grid written to {output_file}")
-    return g
+    return point[:k], atom[:k], dist[:k], val[:k], tuple(int(v) for v in out.n), np.array(list(out.origin))

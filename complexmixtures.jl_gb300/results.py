@@ -472,6 +472,55 @@ def load(filename: str, kind=None):
         raise ValueError(f"The file {filename} does not appear to contain a Result object.") from e
 
 
+def snapshot_from_result(R: Result) -> dict:
+    """The engine snapshot behind a finalised Result (``load`` of a saved
+    JSON, src/results.jl:567-588): the normalisation of finalresults!
+    (src/results.jl:320-376, 430-469) undone -- md/rdf/group counts times
+    nmols x Q, random counts divided by density_fix and times nrandom x Q,
+    volume times Q, with Q the sum of the frame weights -- and rounded to the
+    exact half-unit integers of the frames' common weight.  ``Engine.restore``
+    then resumes the run: frames submitted afterwards add to these counts.
+    Results whose frames carry different weights cannot be resumed this way
+    (``merge`` them instead)."""
+    ws = [f.frame_weights[k - 1] for f in R.files
+          for k in range(f.options.firstframe, f.lastframe_read + 1, f.options.stride) if f.frame_weights[k - 1] != 0.0]
+    if not ws:
+        raise ValueError("the Result holds no computed frame")
+    w = float(ws[0])
+    if any(float(x) != w for x in ws):
+        raise ValueError("the Result's frames carry different weights: resume is defined for one frame weight "
+                         "(merge the Results instead)")
+    frames = len(ws)
+    Q = sum_frame_weights(R)
+    nmols = R.solute.nmols
+    _, nrandom = set_samples(R)
+    fix = np.float64(R.density.solvent_bulk) / np.float64(R.density.solvent) if R.density.solvent else 0.0
+
+    def half_units(v, scale, random=False):
+        v = np.asarray(v, dtype=np.float64)
+        if random:
+            if not np.any(v):
+                return np.zeros(v.shape, dtype=np.int64)
+            v = v / fix
+        return np.rint(2.0 * (v * scale) / w).astype(np.int64)
+
+    real, rand = nmols * Q, nrandom * Q
+    snap = {
+        "md": half_units(R.md_count, real), "md_random": half_units(R.md_count_random, rand, True),
+        "rdf": half_units(R.rdf_count, real), "rdf_random": half_units(R.rdf_count_random, rand, True),
+        "solute_group": half_units(R.solute_group_count, real),
+        "solute_group_random": half_units(R.solute_group_count_random, rand, True),
+    }
+    if R.autocorrelation:
+        snap["solvent_group"] = np.zeros_like(snap["solute_group"])
+        snap["solvent_group_random"] = np.zeros_like(snap["solute_group_random"])
+    else:
+        snap["solvent_group"] = half_units(R.solvent_group_count, real)
+        snap["solvent_group_random"] = half_units(R.solvent_group_count_random, rand, True)
+    snap.update(frame_weight=w, frames=frames, volume_total=float(np.float64(R.volume.total) * np.float64(Q)))
+    return snap
+
+
 def merge(results: List[Result]) -> Result:
     """Average of Results of the same analysis over several trajectories or
     parts of one (src/tools/merge.jl:10-150): every function and counter is

@@ -329,6 +329,22 @@ int cm_contributions(cm_handle *h, double frame_weight_sum, int32_t nqueries, co
 /* Synchronise and copy the exact half-unit counts (single-weight runs only). */
 int cm_read_raw_counts(cm_handle *h, cm_raw_counts *out);
 
+/* The weight of the frames behind cm_read_raw_counts (1.0 before any frame);
+ * CM_ESTATE once frames of different weights were submitted. */
+int cm_raw_counts_weight(cm_handle *h, double *frame_weight);
+
+/*
+ * Resume (src/results.jl:533-588 save/load, src/tools/merge.jl:10 merge):
+ * replace the handle's accumulators with saved half-unit counts -- what
+ * cm_read_raw_counts and cm_raw_counts_weight gave for `frames` frames of
+ * weight `frame_weight`, with volume_total the sum of weight x cell volume
+ * over them (cm_counts volume_total) -- so that frames submitted afterwards
+ * add to them.  With the same frame weight the handle then holds exactly the counts
+ * of one run over all the frames.  The solvent arrays may be NULL with
+ * autocorrelation.  Synchronises the handle's stream; keeps its statistics.
+ */
+int cm_load_raw_counts(cm_handle *h, const cm_raw_counts *in, double frame_weight, int64_t frames, double volume_total);
+
 /* Engine statistics (synchronises). */
 int cm_get_stats(cm_handle *h, cm_stats *out);
 

@@ -117,3 +117,59 @@ def test_contribution_table_equals_one_atom_contributions(cm, orc, kind):
     for t in range(R.solute.natomspermol):
         want = cm.contributions(R, cm.SoluteGroup([R.solute.indices[0] + t]), type=kind, _warn_zero_md_count=False)
         assert np.array_equal(table[t], want), t
+
+
+# ------------------------------------------------------- a case solved by hand
+# Two solute atoms, A at the origin (type 0) and B at (4, 0, 0) (type 1), a
+# grid of step 1 with dmin = 1.5 and dmax = 2.5.  The grid spans the atoms'
+# box widened by dmax: n = (10, 6, 6) points from (-2.5, -2.5, -2.5), so every
+# coordinate of a point is a half-integer and twice a displacement from A or B
+# is a triple of odd integers (a, b, c); the squared distance is
+# (a^2 + b^2 + c^2) / 4.  No point is as close to A as to B (that needs
+# x = 2, not a half-integer).  Sums of three odd squares
+# between 4 dmin^2 = 9 and 4 dmax^2 = 25 are 11 and 19 only, so the kept
+# points are the 24 permutations and sign patterns of (1, 1, 3) and the 24 of
+# (1, 3, 3) around each atom: 96 points, at distances sqrt(11)/2 and
+# sqrt(19)/2.  The contribution curves are c_A(d) = d and c_B(d) = 2 d, whose
+# linear interpolation is the distance itself (A) or twice it (B).
+HAND_XYZ = np.array([[0.0, 0.0, 0.0], [4.0, 0.0, 0.0]])
+HAND_TYPE = np.array([0, 1])
+HAND_D = np.arange(1, 61) * 0.05
+HAND_TABLE = np.stack([HAND_D, 2.0 * HAND_D])
+
+
+def hand_grid():
+    """The kept points of the case above from integer arithmetic, in grid order:
+    (linear index, closest atom, 4 x the squared distance)."""
+    n = (10, 6, 6)
+    out = []
+    for ix in range(n[0]):
+        for iy in range(n[1]):
+            for iz in range(n[2]):
+                b, c = 2 * iy - 5, 2 * iz - 5
+                s_a, s_b = (2 * ix - 5) ** 2 + b * b + c * c, (2 * ix - 13) ** 2 + b * b + c * c
+                atom, s = (0, s_a) if s_a < s_b else (1, s_b)
+                if 9 < s < 25:
+                    out.append(((ix * n[1] + iy) * n[2] + iz, atom, s))
+    return n, out
+
+
+def check_hand(point, atom, dist, val, n, origin):
+    n_hand, want = hand_grid()
+    assert len(want) == 96 and sorted({s for _, _, s in want}) == [11, 19]
+    assert tuple(n) == n_hand and np.array_equal(np.asarray(origin), [-2.5, -2.5, -2.5])
+    assert [int(p) for p in point] == [w[0] for w in want]
+    assert [int(a) for a in atom] == [w[1] for w in want]
+    r = np.array([math.sqrt(s) / 2.0 for _, _, s in want])
+    assert np.array_equal(np.asarray(dist), r)
+    assert np.allclose(val, r * np.array([1.0 + w[1] for w in want]), rtol=1e-14, atol=0.0)
+
+
+def test_restatement_matches_the_case_solved_by_hand(orc):
+    g = orc.grid3d(HAND_XYZ, HAND_TYPE, HAND_TABLE, HAND_D, dmin=1.5, dmax=2.5, step=1.0)
+    check_hand(g["point"], g["atom"], g["distance"], g["value"], g["n"], g["origin"])
+
+
+@pytest.mark.gpu
+def test_gpu_grid3d_matches_the_case_solved_by_hand(cm, gpu_ready):
+    check_hand(*cm.grid3d.grid_search(HAND_XYZ, HAND_TYPE, HAND_TABLE, HAND_D, dmin=1.5, dmax=2.5, step=1.0))

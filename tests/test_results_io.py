@@ -102,3 +102,28 @@ def test_load_rejects_other_json(cm, tmp_path):
     p.write_text('{"a": 1}')
     with pytest.raises(ValueError):
         cm.load(str(p))
+
+
+def test_snapshot_from_saved_result_recovers_half_units(cm, orc, tmp_path):
+    """A finalised Result, saved as JSON and loaded, gives back the exact
+    half-unit counts behind it (the resume snapshot), here against the
+    oracle's counts for the same frames."""
+    from helpers import KEYS, TRICLINIC, make_system, system_kwargs
+
+    rng = np.random.default_rng(33)
+    xs, xv, cells = make_system(rng, TRICLINIC, 10, 4, 150, 3, 3, False)
+    solute = cm.AtomSelection.from_indices(list(range(1, 41)), natomspermol=4)
+    solvent = cm.AtomSelection.from_indices(list(range(41, 491)), natomspermol=3)
+    traj = cm.ArrayTrajectory(solute, solvent, solute_frames=xs, solvent_frames=xv, cells=cells)
+    opts = cm.make_options(seed=43, silent=True, n_random_samples=6, dbulk=6.0, binstep=0.02)
+    R = oracle_mddf(cm, orc, traj, opts)
+    path = str(tmp_path / "r.json")
+    cm.save(path, R)
+    snap = cm.snapshot_from_result(cm.load(path))
+    tmeta = cm.trajectory_metadata(traj, opts)
+    kw = system_kwargs(cm.new_result(traj, opts, tmeta, None), opts, tmeta.irefatom)
+    ref = orc.run(ms=10, aps=4, mv=150, apv=3, solute_xyz=xs, solvent_xyz=xv, cells=cells, frame_ids=[1, 2, 3], **kw)
+    for k in KEYS:
+        assert np.array_equal(snap[k], ref[k]), k
+    assert snap["frames"] == 3 and snap["frame_weight"] == 1.0
+    assert math.isclose(snap["volume_total"], sum(orc.cell_volume(c) for c in cells), rel_tol=1e-14)
