@@ -52,11 +52,14 @@ NRAND = 5
 SEED = 20261203 + 3
 METRIC = "MDDF frames/s (config 3, batched FP32 + FP64 guard)"
 
-# serving leg (config-5 shapes, scaled): request pool and arrival process
-SERVE_SYSTEMS = 8            # c3-like systems, atoms log-uniform in [5,000, 500,000]
-SERVE_REQUESTS = 160
-SERVE_MAX_FRAMES = 16        # frames per request uniform in [1, 16]
+# serving (config 5): requests carved from one large c3-density system, see c5_bank
 SERVE_SEED = 20261203 + 5
+C5_REQUESTS = 2000           # the configuration's request count (--workload c5)
+C5_MAX_FRAMES = 200          # frames per request uniform in [1, 200]
+C5_ATOMS = (5000, 500000)    # atoms per request log-uniform in this range
+C5_BANK_MOLS = 36000         # 504,000 atoms: every request size is a part of this system
+SERVE_REQUESTS = 250         # requests of the serving leg of the default bench line
+SERVE_RATES = (1.0, 1.5, 2.0)  # arrival rates, multiples of the serial FP32 service rate
 
 
 def parse():
@@ -70,7 +73,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-serving", action="store_true")
-    p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4", "grid3d"],
+    p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4", "c5", "grid3d"],
                    help="c3 (default): the headline line; the others: frames/s of that configuration's system "
                         "(ATOMS layout) on device-resident frames")
     return p.parse_args()
@@ -178,102 +181,158 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def serving_pool(syn):
-    """SERVE_SYSTEMS c3-like base systems (frame 0 from the config-5 generator)
-    with SERVE_MAX_FRAMES frames each: rigid molecule translations of
-    sigma = 0.4 A per frame."""
+def c5_bank(syn, device, nframes=C5_MAX_FRAMES):
+    """Frames of every config-5 request, resident on the device, from one
+    large system at c3 density: 36,000 rigid 14-atom molecules (504,000 atoms)
+    in a triclinic cell H (a = b = c, gamma = 60), uniform positions, random
+    orientations, each frame rigid molecule translations of sigma = 0.4 A.
+    The molecules are ordered by the largest fractional coordinate of their
+    centroid, so the molecules whose centroids lie in the cell s H (s <= 1,
+    the same shape) are a prefix: a request of n atoms takes s = (n / N)^(1/3),
+    the prefix of molecules inside s H and the cell s H, i.e. a uniform c3-like
+    system of about n atoms, and its frames are slices of the shared frames
+    (frame stride N x 3), so no request copies coordinates."""
+    import math
+
+    import torch
+
     rng = np.random.default_rng(SERVE_SEED)
-    sizes = np.exp(np.linspace(np.log(5000), np.log(500000), SERVE_SYSTEMS)).astype(int)
-    pool = []
-    for i, n in enumerate(sizes):
-        sysm = syn.config5_request(int(n), SERVE_SEED + i, SERVE_MAX_FRAMES)
-        x0 = sysm.solute0.astype(np.float32).reshape(-1, 14, 3)
-        frames = np.empty((SERVE_MAX_FRAMES,) + x0.shape, np.float32)
-        for k in range(SERVE_MAX_FRAMES):
-            frames[k] = x0 + rng.normal(scale=0.4, size=(x0.shape[0], 1, 3)).astype(np.float32)
-        pool.append((frames.reshape(SERVE_MAX_FRAMES, -1, 3), sysm.cell, x0.shape[0]))
-    return pool
+    dens = 10000 / (110.0**3 * math.sin(math.radians(60)))
+    edge = (C5_BANK_MOLS / dens / math.sin(math.radians(60))) ** (1 / 3)
+    H = syn.triclinic_cell(edge, edge, edge, 90.0, 90.0, 60.0)
+    frac = rng.random((C5_BANK_MOLS, 3))
+    order = np.argsort(frac.max(axis=1), kind="stable")
+    frac = frac[order]
+    x0 = syn.place_molecules(rng, syn.ball_template(rng, 14, 4.0), frac @ H.T).astype(np.float32)
+    x0 = torch.from_numpy(x0.reshape(C5_BANK_MOLS, 14, 3)).to(device)
+    gen = torch.Generator(device=device).manual_seed(SERVE_SEED)
+    bank = torch.empty((nframes, C5_BANK_MOLS * 14, 3), dtype=torch.float32, device=device)
+    for k in range(nframes):
+        shift = torch.randn((C5_BANK_MOLS, 1, 3), generator=gen, device=device, dtype=torch.float32) * 0.4
+        bank[k] = (x0 + shift).reshape(-1, 3)
+    return bank, H, np.sort(frac.max(axis=1))
 
 
-def serving_requests(pool):
+def c5_requests(H, mmax, nreq):
+    """nreq requests: atoms log-uniform in C5_ATOMS, 1..C5_MAX_FRAMES frames,
+    cutoff uniform in [8, 14] rounded to a multiple of 0.02 (Options accepts
+    no other, src/Options.jl:167-172).  Each is (molecules, frames, cutoff, cell)."""
     rng = np.random.default_rng(SERVE_SEED + 1)
     reqs = []
-    for _ in range(SERVE_REQUESTS):
-        i = int(rng.integers(len(pool)))
-        nf = int(rng.integers(1, SERVE_MAX_FRAMES + 1))
+    for _ in range(nreq):
+        n = float(np.exp(rng.uniform(np.log(C5_ATOMS[0]), np.log(C5_ATOMS[1]))))
+        sc = (n / (C5_BANK_MOLS * 14)) ** (1 / 3)
+        nm = max(2, int(np.searchsorted(mmax, sc)))
+        nf = int(rng.integers(1, C5_MAX_FRAMES + 1))
         cutoff = float(f"{round(rng.uniform(8.0, 14.0) / 0.02) * 0.02:.2f}")
-        reqs.append((i, nf, cutoff))
+        reqs.append((nm, nf, cutoff, H * sc))
     return reqs
 
 
-def serving_leg(cm, device):
-    """Config-5 shaped serving load: Poisson arrivals of c3-like self-MDDF
-    requests into the continuous-batching server (FP32 + guard), against the
-    same requests run one at a time on the plain FP64 engine."""
+def serving_leg(cm, device, nreq=SERVE_REQUESTS, rates=SERVE_RATES, fp64_sample=12):
+    """Config-5 serving load: Poisson arrivals of c3-like self-MDDF requests
+    (c5_bank, c5_requests) into the continuous-batching server (FP32 + guard)
+    at several arrival rates, against the same requests run one at a time on
+    the FP32 engine (the serial service rate, and the counts every request
+    must reproduce) and a sample of them on the plain FP64 engine."""
+    import hashlib
+
     import torch
 
     syn = __import__("importlib").import_module("complexmixtures_gb300.synth")
-    pool = serving_pool(syn)
-    reqs = serving_requests(pool)
+    dev = f"cuda:{device}"
+    bank, H, mmax = c5_bank(syn, dev)
+    reqs = c5_requests(H, mmax, nreq)
+    frames_total = sum(nf for _, nf, _, _ in reqs)
+    atoms = [nm * 14 for nm, _, _, _ in reqs]
 
-    def kw(i, cutoff, precision):
-        nm = pool[i][2]
+    def kw(nm, cutoff, precision):
         return dict(solute_nmols=nm, solute_natomspermol=14, solvent_nmols=nm, solvent_natomspermol=14,
                     autocorrelation=True, irefatom=1, cutoff=cutoff, binstep=0.02, dbulk=cutoff, usecutoff=False,
                     nbins=cm.setbin(cutoff, 0.02), n_random_samples=5, seed=SERVE_SEED, precision=precision,
                     device=device)
 
-    def cells(i, nf):
-        return np.repeat(pool[i][1][None], nf, axis=0)
+    def frames(nm, nf):
+        return bank[:nf, : nm * 14]
 
-    frames_total = sum(nf for _, nf, _ in reqs)
+    def cells(cell, nf):
+        return np.repeat(cell[None], nf, axis=0)
 
-    def serial(precision):
-        out = []
+    def digest(raw):
+        h = hashlib.sha256()
+        for k in ("md", "md_random", "rdf", "rdf_random", "solute_group", "solute_group_random"):
+            h.update(np.ascontiguousarray(raw[k]).tobytes())
+        return h.hexdigest()
+
+    def serial(precision, which):
+        out = {}
         torch.cuda.synchronize()
         t = time.perf_counter()
-        for i, nf, cutoff in reqs:
-            eng = cm.Engine(**kw(i, cutoff, precision))
-            eng.submit(pool[i][0][:nf], None, cells(i, nf))
-            out.append(eng.raw_counts())
-            eng.close()
+        for i in which:
+            nm, nf, cutoff, cell = reqs[i]
+            with cm.Engine(**kw(nm, cutoff, precision)) as eng:
+                eng.submit(frames(nm, nf), None, cells(cell, nf))
+                out[i] = digest(eng.raw_counts())
         return time.perf_counter() - t, out
 
-    serial("fp32")  # warm-up: module load, first allocations
-    t64, ref = serial("fp64")
-    t32, _ = serial("fp32")
-    # arrivals at the serial FP32 service rate (the server's overlap is the headroom)
-    rate = len(reqs) / t32
-    gaps = np.random.default_rng(SERVE_SEED + 2).exponential(1.0 / rate, len(reqs))
-    with cm.Server(device=device, frames_per_turn=4) as srv:
-        ids = []
-        t0 = time.perf_counter()
-        due = t0
-        for (i, nf, cutoff), g in zip(reqs, gaps):
-            due += g
-            while time.perf_counter() < due:
-                time.sleep(min(1e-4, max(0.0, due - time.perf_counter())))
-            ids.append(srv.submit(pool[i][0][:nf], None, cells(i, nf), **kw(i, cutoff, "fp32")))
-        infos = [srv.wait(r, timeout=600) for r in ids]
-        span = max(x["t_done"] for x in infos) - min(x["t_submit"] for x in infos)
-        same = all(np.array_equal(srv.raw_counts(r)["md"], ref[k]["md"]) and
-                   np.array_equal(srv.raw_counts(r)["md_random"], ref[k]["md_random"]) and
-                   np.array_equal(srv.raw_counts(r)["solute_group"], ref[k]["solute_group"])
-                   for k, r in enumerate(ids))
-    pct = cm.latency_percentiles(infos)
+    serial("fp32", range(min(8, nreq)))  # warm-up: module load, first allocations
+    t32, ref = serial("fp32", range(nreq))
+    rate32 = frames_total / t32
+    sample = list(range(0, nreq, max(1, nreq // fp64_sample)))[:fp64_sample]
+    t64, ref64 = serial("fp64", sample)
+    sample_frames = sum(reqs[i][1] for i in sample)
+    runs = []
+    for mult in rates:
+        rate = mult * nreq / t32
+        gaps = np.random.default_rng(SERVE_SEED + 2).exponential(1.0 / rate, nreq)
+        with cm.Server(device=device, frames_per_turn=32, max_active=32, hbm_budget_bytes=96 << 30) as srv:
+            ids = []
+            t0 = time.perf_counter()
+            due = t0
+            for (nm, nf, cutoff, cell), g in zip(reqs, gaps):
+                due += g
+                while time.perf_counter() < due:
+                    time.sleep(min(1e-4, max(0.0, due - time.perf_counter())))
+                ids.append(srv.submit(frames(nm, nf), None, cells(cell, nf), **kw(nm, cutoff, "fp32")))
+            infos = [srv.wait(r, timeout=1800) for r in ids]
+            span = max(x["t_done"] for x in infos) - min(x["t_submit"] for x in infos)
+            same = all(x["state"] == "done" and digest(srv.raw_counts(r)) == ref[k]
+                       for k, (r, x) in enumerate(zip(ids, infos)))
+        pct = cm.latency_percentiles(infos)
+        runs.append({"arrival_rate_x_serial": mult, "arrival_rate_per_s": rate, "p50_ms": pct["p50"],
+                     "p99_ms": pct["p99"], "frames_per_s": frames_total / span,
+                     "failed": sum(1 for x in infos if x["state"] != "done"),
+                     "counts_identical_to_serial": bool(same)})
+    best = max(runs, key=lambda r: r["frames_per_s"])
     return {
-        "workload": f"{len(reqs)} Poisson-arrival self-MDDF requests over {SERVE_SYSTEMS} c3-like systems "
-                    f"(5,000-500,000 atoms, log-spaced), 1-{SERVE_MAX_FRAMES} frames each, cutoff U[8,14] "
-                    f"rounded to 0.02, 5 random samples; arrival rate = serial FP32 service rate",
-        "requests": len(reqs), "frames": frames_total,
-        "p50_ms": pct["p50"], "p99_ms": pct["p99"],
-        "frames_per_s": frames_total / span,
-        "serial_fp64_frames_per_s": frames_total / t64,
-        "serial_fp32_frames_per_s": frames_total / t32,
-        "arrival_rate_per_s": rate,
-        "failed": sum(1 for x in infos if x["state"] != "done"),
-        "counts_identical_to_serial_fp64": bool(same),
+        "workload": f"{nreq} Poisson-arrival self-MDDF requests, c3-like (14-atom molecules at c3 density, "
+                    f"triclinic gamma=60), atoms log-uniform in [{C5_ATOMS[0]:,}, {C5_ATOMS[1]:,}] "
+                    f"(drawn {min(atoms):,}-{max(atoms):,}), 1-{C5_MAX_FRAMES} frames each, cutoff U[8,14] "
+                    f"rounded to 0.02, 5 random samples; frames resident on the device",
+        "requests": nreq, "frames": frames_total,
+        "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "frames_per_s": best["frames_per_s"],
+        "serial_fp32_frames_per_s": rate32,
+        "serial_fp64_frames_per_s": sample_frames / t64,
+        "serial_fp64_sample": f"{len(sample)} of the requests ({sample_frames} frames)",
+        "fp64_sample_counts_identical": all(ref64[i] == ref[i] for i in sample),
+        "arrival_sweep": runs,
+        "failed": sum(r["failed"] for r in runs),
+        "counts_identical_to_serial": all(r["counts_identical_to_serial"] for r in runs),
     }
+
+
+def c5_workload(args, local):
+    """Config 5 at its stated load: 2,000 requests (serving_leg)."""
+    import torch
+
+    import __graft_entry__ as entry
+
+    cm = entry.load_package()
+    torch.cuda.set_device(local)
+    out = serving_leg(cm, local, nreq=C5_REQUESTS, fp64_sample=20)
+    out.update(metric="MDDF frames/s and request latency (config 5 serving load)", unit="frames/s",
+               value=out["frames_per_s"], data="synthetic (seeded generator of the configuration)")
+    print(json.dumps(out), flush=True)
 
 
 C4_FRAMES = 50              # frames per config-4 system
@@ -564,6 +623,10 @@ def main():
     if args.workload == "grid3d":
         if rank == 0:
             grid3d_workload(args, local)
+        return
+    if args.workload == "c5":
+        if rank == 0:
+            c5_workload(args, local)
         return
     if args.workload != "c3":
         if rank == 0:

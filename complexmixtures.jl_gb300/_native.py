@@ -95,6 +95,8 @@ class cm_frames(C.Structure):
         ("cells", C.POINTER(C.c_double)),
         ("weights", C.POINTER(C.c_double)),
         ("frame_ids", C.POINTER(C.c_int64)),
+        ("solute_frame_stride", C.c_int64),
+        ("solvent_frame_stride", C.c_int64),
     ]
 
 

@@ -344,9 +344,10 @@ struct Bufs {
     const FrameGeom *G;             // [nf]
     FrameScratch *FS;               // [nf]
     // the chunk's input coordinates as the caller gave them ([nf][Ns][3] and
-    // [nf][Nv][3], FP32 or FP64; xv_raw == xs_raw in self mode): the exact
-    // distances are formed from these
+    // [nf][Nv][3] at the strides below, FP32 or FP64; xv_raw == xs_raw in self
+    // mode): the exact distances are formed from these
     const void *xs_raw, *xv_raw;
+    int64_t xs_stride, xv_stride;   // coordinate values from one frame's first atom to the next frame's
     int raw64;                      // 1: FP64 input coordinates
     d4 *off64;                      // [nf][kOffEntries]
     float4 *off32;
@@ -403,7 +404,7 @@ struct Bufs {
 // Input coordinates of one atom of frame f (solute or solvent selection),
 // widened to FP64 exactly.
 __device__ __forceinline__ void raw_atom(const Bufs &B, bool solvent, int f, int64_t atom, double *x) {
-    const int64_t i = ((int64_t)f * (solvent ? B.Nv : B.Ns) + atom) * 3;
+    const int64_t i = (int64_t)f * (solvent ? B.xv_stride : B.xs_stride) + atom * 3;
     if (B.raw64) {
         const double *p = (const double *)(solvent ? B.xv_raw : B.xs_raw) + i;
         x[0] = p[0]; x[1] = p[1]; x[2] = p[2];

@@ -1,7 +1,8 @@
 // cm_server.cpp -- request server over the engine handles: continuous
 // batching of MDDF jobs on one device.
 //
-// A request is one system (cm_system_desc) with its frames in host memory.
+// A request is one system (cm_system_desc) with its frames in host or device
+// memory (the caller keeps them valid until the request is done).
 // Requests wait in arrival order until the server admits them: a request is
 // admitted when fewer than max_active requests are on the device and its
 // handle's memory fits in what is left of the server's HBM budget (the handle
@@ -133,9 +134,11 @@ int submit_turn(Request &r, int64_t n) {
     const int64_t Ns = (int64_t)r.desc.solute_nmols * r.desc.solute_natomspermol;
     const int64_t Nv = (int64_t)r.desc.solvent_nmols * r.desc.solvent_natomspermol;
     const int64_t elem = f.coord_type == CM_COORD_F32 ? 4 : 8;
+    const int64_t ss = f.solute_frame_stride > 0 ? f.solute_frame_stride : Ns * 3;
+    const int64_t vs = f.solvent_frame_stride > 0 ? f.solvent_frame_stride : Nv * 3;
     f.nframes = (int32_t)n;
-    f.solute_xyz = (const char *)r.frames.solute_xyz + k * Ns * 3 * elem;
-    f.solvent_xyz = r.frames.solvent_xyz ? (const char *)r.frames.solvent_xyz + k * Nv * 3 * elem : nullptr;
+    f.solute_xyz = (const char *)r.frames.solute_xyz + k * ss * elem;
+    f.solvent_xyz = r.frames.solvent_xyz ? (const char *)r.frames.solvent_xyz + k * vs * elem : nullptr;
     f.cells = r.cells.data() + 9 * k;
     f.weights = r.weights.empty() ? nullptr : r.weights.data() + k;
     f.frame_ids = r.ids.data() + k;
@@ -349,7 +352,10 @@ int cm_server_create(const cm_server_desc *desc, cm_server **out) {
 
 int cm_server_submit(cm_server *s, const cm_system_desc *desc, const cm_frames *frames, int64_t *request_id) {
     if (!s || !desc || !frames || !request_id) return server_fail(s, CM_EINVAL, "NULL argument");
-    if (frames->memory != CM_MEM_HOST) return server_fail(s, CM_EINVAL, "server requests take frames in host memory");
+    if (frames->memory != CM_MEM_HOST && frames->memory != CM_MEM_DEVICE)
+        return server_fail(s, CM_EINVAL, "unknown memory kind");
+    if (frames->coord_type != CM_COORD_F32 && frames->coord_type != CM_COORD_F64)
+        return server_fail(s, CM_EINVAL, "server requests take FP32 or FP64 coordinates");
     if (frames->nframes < 1 || !frames->solute_xyz || !frames->cells || !frames->frame_ids)
         return server_fail(s, CM_EINVAL, "a request needs at least one frame with coordinates, cells and frame ids");
     if (!desc->autocorrelation && !frames->solvent_xyz) return server_fail(s, CM_EINVAL, "solvent_xyz is required");

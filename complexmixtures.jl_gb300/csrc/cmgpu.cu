@@ -989,7 +989,7 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
 
 template <typename T>
 void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *dS, const int4 *dtab, const T *xs,
-               const T *xv) {
+               const T *xv, int64_t xs_stride, int64_t xv_stride) {
     const cm_system_desc &d = h->d;
     cudaStream_t st = h->stream;
     NvtxRange range("cm: chunk (mddf_frame! of each frame)");
@@ -999,6 +999,8 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
     const bool self = d.autocorrelation;
     B.xs_raw = xs;
     B.xv_raw = self ? (const void *)xs : (const void *)xv;
+    B.xs_stride = xs_stride;
+    B.xv_stride = self ? xs_stride : xv_stride;
     B.raw64 = sizeof(T) == 8 ? 1 : 0;
     const bool fp32 = d.precision == CM_PRECISION_FP32_GUARD;
     const int nf = c.nf;
@@ -1015,9 +1017,9 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
         CM_CUDA(cudaMemsetAsync(B.ccount, 0, (size_t)nf * B.cs * 4, st));
         // solute molecules (in self mode they also fill the cell counts)
-        CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<dim3(grid_for(ms, 128), nf), 128, 0, st>>>(B, xs, h->Ns * 3, 0, self ? 1 : 0));
+        CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<dim3(grid_for(ms, 128), nf), 128, 0, st>>>(B, xs, xs_stride, 0, self ? 1 : 0));
         if (!self)
-            CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<dim3(grid_for(mv, 128), nf), 128, 0, st>>>(B, xv, h->Nv * 3, 1, 1));
+            CM_LAUNCH(CM_K_PREP, k_prep_pairs<T><<<dim3(grid_for(mv, 128), nf), 128, 0, st>>>(B, xv, xv_stride, 1, 1));
         CM_LAUNCH(CM_K_PREP, k_frame_consts<<<nf, 128, 0, st>>>(S, B, 1));
         CM_LAUNCH(CM_K_CELLS, k_scan<<<nf, 1024, 0, st>>>(B, 0));
         CM_LAUNCH(CM_K_CELLS, k_scatter_mols<<<dim3(grid_for(mv, 256), nf), 256, 0, st>>>(B, self ? 1 : 0));
@@ -1074,10 +1076,10 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
         }
     } else {
         const T *xsolv = self ? xs : xv;
-        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solvent<T><<<dim3(grid_for(mv, 128), nf), 128, 0, st>>>(B, xsolv, h->Nv * 3, iref,
+        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solvent<T><<<dim3(grid_for(mv, 128), nf), 128, 0, st>>>(B, xsolv, self ? xs_stride : xv_stride, iref,
                                                                                                  h->mddf ? 1 : 0));
         CM_CUDA(cudaMemsetAsync(B.acount, 0, (size_t)nf * B.as * 4, st));
-        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solute<T><<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B, xs, h->Ns * 3));
+        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solute<T><<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B, xs, xs_stride));
         CM_LAUNCH(CM_K_PREP, k_frame_consts<<<nf, 128, 0, st>>>(S, B, 0));
         CM_LAUNCH(CM_K_CELLS, k_scan<<<nf, 1024, 0, st>>>(B, 1));
         CM_LAUNCH(CM_K_CELLS, k_scatter_atoms<<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B));
@@ -1174,7 +1176,7 @@ struct Staged {
     Sample *dS = nullptr;
     int4 *dT = nullptr;
     const char *xs_base = nullptr, *xv_base = nullptr;
-    int64_t sbytes = 0, vbytes = 0;
+    int64_t sbytes = 0, vbytes = 0;  // bytes from one frame to the next as the kernels read them
     std::vector<Chunk> chunks;
 };
 
@@ -1220,6 +1222,13 @@ void check_frames(cm_handle *h, const cm_frames *f) {
     const bool dcd = f->coord_type == CM_COORD_DCD;
     if (dcd && !h->dcd) throw cm_error(CM_ESTATE, "raw DCD frames need cm_set_dcd_layout first");
     if (dcd && f->solvent_xyz) throw cm_error(CM_EINVAL, "raw DCD frames hold both selections: solvent_xyz must be NULL");
+    if (dcd && (f->solute_frame_stride || f->solvent_frame_stride))
+        throw cm_error(CM_EINVAL, "raw DCD frames take no frame strides (the layout gives them)");
+    if (f->solute_frame_stride < 0 || (f->solute_frame_stride > 0 && f->solute_frame_stride < h->Ns * 3))
+        throw cm_error(CM_EINVAL, "solute_frame_stride must be 0 or at least solute atoms x 3");
+    if (!d.autocorrelation &&
+        (f->solvent_frame_stride < 0 || (f->solvent_frame_stride > 0 && f->solvent_frame_stride < h->Nv * 3)))
+        throw cm_error(CM_EINVAL, "solvent_frame_stride must be 0 or at least solvent atoms x 3");
     if (!dcd && !d.autocorrelation && !f->solvent_xyz) throw cm_error(CM_EINVAL, "solvent_xyz is required unless autocorrelation");
     if (!h->planned) {
         if (dcd) {
@@ -1251,6 +1260,9 @@ Staged stage(cm_handle *h, const cm_frames *f, int f0) {
     S.f0 = f0;
     S.sbytes = h->Ns * 3 * S.elem;
     S.vbytes = h->Nv * 3 * S.elem;
+    // the caller's frame strides (bytes)
+    const int64_t src_s = (f->solute_frame_stride > 0 ? f->solute_frame_stride : h->Ns * 3) * S.elem;
+    const int64_t src_v = (f->solvent_frame_stride > 0 ? f->solvent_frame_stride : h->Nv * 3) * S.elem;
     const double cs = target_cell(h);
     const int fce = chunk_frames(h);
     const int nf = S.nf = std::min(h->max_frames, f->nframes - f0);
@@ -1343,15 +1355,24 @@ Staged stage(cm_handle *h, const cm_frames *f, int f0) {
         // the staging buffers exist already unless the handle's first frames came from device memory
         dev_alloc(h, h->stage_s[b], (size_t)h->max_frames * h->Ns * 3 * h->coord_elem);
         if (!d.autocorrelation) dev_alloc(h, h->stage_v[b], (size_t)h->max_frames * h->Nv * 3 * h->coord_elem);
-        CM_CUDA(cudaMemcpyAsync(h->stage_s[b].p, (const char *)f->solute_xyz + S.sbytes * f0, (size_t)S.sbytes * nf,
-                                cudaMemcpyHostToDevice, cp));
+        // consecutive frames in one copy, frames of a larger array row by row
+        auto copy = [&](void *dst, const void *src, int64_t width, int64_t src_stride) {
+            if (src_stride == width)
+                CM_CUDA(cudaMemcpyAsync(dst, (const char *)src + width * f0, (size_t)width * nf, cudaMemcpyHostToDevice, cp));
+            else
+                CM_CUDA(cudaMemcpy2DAsync(dst, (size_t)width, (const char *)src + src_stride * f0, (size_t)src_stride,
+                                          (size_t)width, (size_t)nf, cudaMemcpyHostToDevice, cp));
+        };
+        copy(h->stage_s[b].p, f->solute_xyz, S.sbytes, src_s);
         S.xs_base = (const char *)h->stage_s[b].p;
         if (!d.autocorrelation) {
-            CM_CUDA(cudaMemcpyAsync(h->stage_v[b].p, (const char *)f->solvent_xyz + S.vbytes * f0, (size_t)S.vbytes * nf,
-                                    cudaMemcpyHostToDevice, cp));
+            copy(h->stage_v[b].p, f->solvent_xyz, S.vbytes, src_v);
             S.xv_base = (const char *)h->stage_v[b].p;
         }
     } else {
+        // device frames are read in place, at the caller's strides
+        S.sbytes = src_s;
+        S.vbytes = src_v;
         S.xs_base = (const char *)f->solute_xyz + S.sbytes * f0;
         if (!d.autocorrelation) S.xv_base = (const char *)f->solvent_xyz + S.vbytes * f0;
     }
@@ -1364,8 +1385,9 @@ Staged stage(cm_handle *h, const cm_frames *f, int f0) {
 void run_staged_chunk(cm_handle *h, const Staged &S, const Chunk &c) {
     const char *xs = S.xs_base + S.sbytes * c.c0;
     const char *xv = S.xv_base ? S.xv_base + S.vbytes * c.c0 : nullptr;
-    if (S.elem == 4) run_chunk<float>(h, c, S.dG, S.dS, S.dT, (const float *)xs, (const float *)xv);
-    else run_chunk<double>(h, c, S.dG, S.dS, S.dT, (const double *)xs, (const double *)xv);
+    const int64_t ss = S.sbytes / S.elem, vs = S.vbytes / S.elem;
+    if (S.elem == 4) run_chunk<float>(h, c, S.dG, S.dS, S.dT, (const float *)xs, (const float *)xv, ss, vs);
+    else run_chunk<double>(h, c, S.dG, S.dS, S.dT, (const double *)xs, (const double *)xv, ss, vs);
 }
 
 // Host accumulators of a chunk's frames (src/mddf.jl:352).
@@ -1669,7 +1691,7 @@ void noalloc_run(cm_handle *h, const cm_frames *f, cudaStream_t stream) {
     CM_CUDA(cudaMemsetAsync(h->stats.p, 0, ST_N * 8, stream));
     CM_CUDA(cudaMemsetAsync(h->errflag.p, 0, 8, stream));
     CM_CUDA(cudaMemsetAsync(h->hist.p, 0, h->hist_n * 8, stream));
-    run_chunk<T>(h, one, dG, P<Sample>(h->samples), P<int4>(h->tabs), xs, xv);
+    run_chunk<T>(h, one, dG, P<Sample>(h->samples), P<int4>(h->tabs), xs, xv, h->Ns * 3, h->Nv * 3);
     int e = 0;
     CM_CUDA(cudaMemcpyAsync(&e, h->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CM_CUDA(cudaStreamSynchronize(stream));

@@ -146,12 +146,14 @@ def memory_cache(device: int = 0, release: bool = False) -> dict:
 
 
 def frames_struct(solute_xyz, solvent_xyz, cells, weights, frame_ids, natoms_solute, natoms_solvent, autocorrelation):
-    """cm_frames for a batch of frames, and the arrays it points to."""
-    xs, kind_s, mem_s = _coords(solute_xyz, natoms_solute)
+    """cm_frames for a batch of frames, and the arrays it points to.  Frames
+    that are slices of a larger array (each frame's atoms contiguous, the
+    frames further apart) are passed with their frame stride, not copied."""
+    xs, kind_s, mem_s, ss = _coords(solute_xyz, natoms_solute)
     nf = int(xs.shape[0])
-    xv = None
+    xv, vs = None, 0
     if not autocorrelation:
-        xv, kind_v, mem_v = _coords(solvent_xyz, natoms_solvent)
+        xv, kind_v, mem_v, vs = _coords(solvent_xyz, natoms_solvent)
         if kind_v != kind_s or mem_v != mem_s:
             raise ValueError("solute and solvent coordinates must share dtype and device")
     cells = np.asarray(cells, dtype=np.float64).reshape(nf, 3, 3)
@@ -169,6 +171,8 @@ def frames_struct(solute_xyz, solvent_xyz, cells, weights, frame_ids, natoms_sol
     fr.cells = N.as_ptr(cm, C.c_double)
     fr.weights = N.as_ptr(w, C.c_double) if w is not None else None
     fr.frame_ids = N.as_ptr(ids, C.c_int64)
+    fr.solute_frame_stride = ss
+    fr.solvent_frame_stride = vs
     return fr, [xs, xv, cm, w, ids]
 
 
@@ -180,29 +184,45 @@ def _ptr(x):
     return C.c_void_p(x.ctypes.data)
 
 
+def _frame_stride(shape, strides, natoms):
+    """Element stride between frames when each frame's [natoms, 3] block is
+    contiguous (0 when the frames are consecutive too), else None."""
+    if strides[2] != 1 or (natoms > 1 and strides[1] != 3):
+        return None
+    if shape[0] == 1 or strides[0] == natoms * 3:
+        return 0
+    return strides[0] if strides[0] >= natoms * 3 else None
+
+
 def _coords(x, natoms):
     if _is_torch(x):
         import torch
 
         if x.dtype not in (torch.float32, torch.float64):
             raise ValueError("coordinates must be float32 or float64")
-        x = x.contiguous()
-        kind = N.CM_COORD_F32 if x.dtype == torch.float32 else N.CM_COORD_F64
-        mem = N.CM_MEM_DEVICE if x.is_cuda else N.CM_MEM_HOST
         if x.dim() == 2:
             x = x.unsqueeze(0)
         if x.shape[1] != natoms or x.shape[2] != 3:
             raise ValueError(f"coordinates must be [nframes, {natoms}, 3]")
-        return x, kind, mem
+        stride = _frame_stride(tuple(x.shape), tuple(x.stride()), natoms)
+        if stride is None:
+            x, stride = x.contiguous(), 0
+        kind = N.CM_COORD_F32 if x.dtype == torch.float32 else N.CM_COORD_F64
+        mem = N.CM_MEM_DEVICE if x.is_cuda else N.CM_MEM_HOST
+        return x, kind, mem, stride
     a = np.asarray(x)
     if a.dtype not in (np.float32, np.float64):
         a = a.astype(np.float64)
-    a = np.ascontiguousarray(a)
     if a.ndim == 2:
         a = a[None]
     if a.shape[1] != natoms or a.shape[2] != 3:
         raise ValueError(f"coordinates must be [nframes, {natoms}, 3]")
-    return a, (N.CM_COORD_F32 if a.dtype == np.float32 else N.CM_COORD_F64), N.CM_MEM_HOST
+    stride = None
+    if all(v % a.itemsize == 0 for v in a.strides):
+        stride = _frame_stride(a.shape, tuple(v // a.itemsize for v in a.strides), natoms)
+    if stride is None:
+        a, stride = np.ascontiguousarray(a), 0
+    return a, (N.CM_COORD_F32 if a.dtype == np.float32 else N.CM_COORD_F64), N.CM_MEM_HOST, stride
 
 
 def counts_arrays(nbins, ngroups_solute, ngroups_solvent):

@@ -41,14 +41,15 @@ class Server:
         self._req = {}   # id -> (arrays kept alive, nbins, ngroups solute, ngroups solvent)
 
     def submit(self, solute_xyz, solvent_xyz, cells, weights=None, frame_ids=None, **system) -> int:
-        """Queue a request; returns its id.  Coordinates are host arrays
-        [nframes, natoms, 3] (float32 or float64)."""
+        """Queue a request; returns its id.  Coordinates are [nframes, natoms,
+        3] float32 or float64 arrays: numpy, or torch tensors on the host or
+        the GPU (kept alive, and not to be changed, until the request is
+        done).  A frame may be a slice of a larger array (frames[:, :n]): the
+        frame stride is passed, the frames are not copied."""
         d, keep_d = system_desc(**system)
         Ns = d.solute_nmols * d.solute_natomspermol
         Nv = d.solvent_nmols * d.solvent_natomspermol
         fr, keep_f = frames_struct(solute_xyz, solvent_xyz, cells, weights, frame_ids, Ns, Nv, bool(d.autocorrelation))
-        if fr.memory != N.CM_MEM_HOST:
-            raise ValueError("server requests take frames in host memory")
         rid = C.c_int64()
         self._check(self._lib.cm_server_submit(self._s, C.byref(d), C.byref(fr), C.byref(rid)))
         gs = d.solute_ngroups if system.get("solute_groups") is not None else d.solute_natomspermol

@@ -145,6 +145,11 @@ typedef struct cm_frames {
     const double *weights;            /* host [nframes]; NULL = all 1.0 (frame_weights) */
     const int64_t *frame_ids;         /* host [nframes]; 1-based trajectory frame numbers,
                                          they key the random-insertion stream */
+    int64_t solute_frame_stride;      /* coordinate values from one frame's first solute atom to the next
+                                         frame's (>= solute atoms x 3); 0 = consecutive frames.  A frame
+                                         may thus be a slice of a larger array, e.g. a contiguous
+                                         selection of a trajectory's frames, with no gather */
+    int64_t solvent_frame_stride;     /* the same for solvent_xyz; ignored in self mode */
 } cm_frames;
 
 /*
@@ -489,7 +494,8 @@ typedef struct cm_server cm_server;
 /* Start a server (and its scheduler thread) on one device. */
 int cm_server_create(const cm_server_desc *desc, cm_server **out);
 
-/* Queue a request: a system and its frames in host memory. */
+/* Queue a request: a system and its frames, in host memory or in device memory
+ * that stays valid (and unchanged) until the request is done. */
 int cm_server_submit(cm_server *s, const cm_system_desc *desc, const cm_frames *frames, int64_t *request_id);
 
 /* State of a request. */

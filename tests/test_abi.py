@@ -29,7 +29,7 @@ def test_struct_sizes_match_header(cm):
     N = cm._native
     # field-by-field mirror of include/cmgpu.h on LP64
     assert C.sizeof(N.cm_system_desc) == 184
-    assert C.sizeof(N.cm_frames) == 56
+    assert C.sizeof(N.cm_frames) == 72
     assert C.sizeof(N.cm_counts) == 88
     assert C.sizeof(N.cm_raw_counts) == 64
     assert C.sizeof(N.cm_stats) == 104

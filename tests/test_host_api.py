@@ -119,3 +119,16 @@ def test_random_move_keeps_internal_distances(orc, H, shift):
         y = orc.move(whole, centre, A)
         assert np.allclose(_internal_distances(x), _internal_distances(y), rtol=1e-12, atol=1e-12)
         assert np.allclose(y.mean(axis=0), centre, atol=1e-12)
+
+
+def test_frame_slices_keep_their_stride(cm):
+    """A slice of a larger frame array is passed with its frame stride, a
+    non-contiguous frame is copied (no GPU needed)."""
+    eng = cm.engine
+    big = np.zeros((3, 10, 3), dtype=np.float32)
+    fr, keep = eng.frames_struct(big[:, :4], None, np.repeat(np.eye(3)[None], 3, 0), None, None, 4, 4, True)
+    assert fr.solute_frame_stride == 30 and keep[0].base is not None
+    fr, _ = eng.frames_struct(big[:, :4].copy(), None, np.repeat(np.eye(3)[None], 3, 0), None, None, 4, 4, True)
+    assert fr.solute_frame_stride == 0
+    fr, keep = eng.frames_struct(big[:, ::2], None, np.repeat(np.eye(3)[None], 3, 0), None, None, 5, 5, True)
+    assert fr.solute_frame_stride == 0 and keep[0].flags["C_CONTIGUOUS"]
