@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--real-pass", default="auto", choices=["auto", "warp", "tile"],
+                   help="FP32 real-pass schedule (speed only): per-molecule warps or home-cell tiles")
     p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4", "c5", "grid3d"],
                    help="c3 (default): the headline line; the others: frames/s of that configuration's system "
                         "(ATOMS layout) on device-resident frames")
@@ -648,7 +650,8 @@ def main():
         return cm.Engine(solute_nmols=NMOLS, solute_natomspermol=APM, solvent_nmols=NMOLS, solvent_natomspermol=APM,
                          autocorrelation=True, irefatom=1, cutoff=CUTOFF, binstep=BINSTEP, dbulk=CUTOFF,
                          usecutoff=False, nbins=500, n_random_samples=NRAND, seed=SEED, precision=precision,
-                         device=local, max_frames_per_batch=chunk, kernel_timing=timing)
+                         device=local, max_frames_per_batch=chunk, kernel_timing=timing,
+                         real_pass=args.real_pass)
 
     eng = engine("fp32", True)
     stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=f"cuda:{local}")
@@ -776,7 +779,8 @@ def main():
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, config-3 shapes and distributions)",
-        "config": config_dict(nf, {"parallelism": "replicas" if world > 1 else "single GPU"}),
+        "config": config_dict(nf, {"parallelism": "replicas" if world > 1 else "single GPU",
+                                   "real_pass": args.real_pass}),
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
         "plain_fp64": plain,
         "fp32_guard_speedup_vs_plain_fp64": (value / world) / plain["value"] * world if plain else None,

@@ -19,6 +19,7 @@ CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
 CM_REGIME_AUTO, CM_REGIME_PAIRS, CM_REGIME_ATOMS = 0, 1, 2
 CM_LAUNCH_AUTO, CM_LAUNCH_STREAM, CM_LAUNCH_GRAPH = 0, 1, 2
 CM_SCHED_AUTO, CM_SCHED_CELL, CM_SCHED_BALANCED = 0, 1, 2
+CM_REAL_AUTO, CM_REAL_WARP, CM_REAL_TILE = 0, 1, 2
 CM_COORD_F64, CM_COORD_F32, CM_COORD_DCD = 0, 1, 2
 CM_MEM_HOST, CM_MEM_DEVICE = 0, 1
 CM_NOALLOC_SCRATCH_BYTES = 32 << 20
@@ -66,7 +67,7 @@ class cm_system_desc(C.Structure):
         ("launch", C.c_int32),
         ("atoms_schedule", C.c_int32),
         ("guard_queue_capacity", C.c_int32),
-        ("reserved", C.c_int32),
+        ("real_pass", C.c_int32),
     ]
 
 

@@ -242,12 +242,19 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
     }
 }
 
+// skip_tile: the frames the tiled kernel took (FrameScratch::tile) are
+// skipped, and the kernel returns at once when that is every frame.
 template <bool SELF, int APS>
-__global__ void __launch_bounds__(kFlatWarps * 32, CM_FLAT_MIN_CTAS) k_pairs_flat32(DevSys S, Bufs B) {
+__global__ void __launch_bounds__(kFlatWarps * 32, CM_FLAT_MIN_CTAS) k_pairs_flat32(DevSys S, Bufs B, int skip_tile) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
     const int hw = hist_words(S);
     FlatWarpSmem *wsm = (FlatWarpSmem *)(smem_raw + (((size_t)hw * 4 + 15) & ~(size_t)15));
+    if (skip_tile) {
+        int any = 0;
+        for (int f = threadIdx.x; f < B.nf; f += blockDim.x) any |= (B.FS[f].tile == 0);
+        if (!__syncthreads_or(any)) return;
+    }
     shist_zero(S, hbase);
     __syncthreads();
     SHist h = shist_bind(S, hbase);
@@ -265,6 +272,7 @@ __global__ void __launch_bounds__(kFlatWarps * 32, CM_FLAT_MIN_CTAS) k_pairs_fla
             continue;
         }
         if (F.multi) continue;  // several images per pair: the generic kernel takes the frame
+        if (skip_tile && F.tile) continue;
         const FrameGeom &G = *Pf.G;
         const Guard g = F.g;
         const float4 qs = Pf.sq32[s];
@@ -360,6 +368,215 @@ __global__ void __launch_bounds__(kFlatWarps * 32, CM_FLAT_MIN_CTAS) k_pairs_fla
         __syncwarp();
         if (cnt > 0) flat_batch<SELF, APS>(S, B, h, W, Pf, g, f, s, sslot, rs2, lane, cnt, st);
         __syncwarp();
+    }
+    stats_flush(S, st, false);
+    __syncthreads();
+    shist_flush(S, h, false);
+}
+
+// ------------------------------------------------------------ tiled real pass
+// Self mode.  The stencil walk of k_pairs_flat32 gathers each neighbour
+// cell's molecule table from L2 once per solute molecule, one warp per
+// molecule, and was most of that kernel's time.  Here a CTA takes one home
+// cell: it stages the molecules of the cell's half stencil (the home cell,
+// its row forward, the rest of its plane forward, the planes above) in
+// shared memory once -- each as its cell-relative centroid plus the cell's
+// stencil offset, with its radius and, packed with its index, the staged
+// cell -- and its warps then claim the home cell's molecules one by one and
+// test each against the whole staged table, 32 candidates per round.  The
+// candidates then go through flat_batch exactly as in k_pairs_flat32 (the
+// displacement is formed as (q_v + off) - q_s, an order the guard band
+// covers), so the records, and the guard and edge queues, are the same.
+#ifndef CM_TILE_WARPS
+#define CM_TILE_WARPS 12
+#endif
+#ifndef CM_TILE_MIN_CTAS
+#define CM_TILE_MIN_CTAS 2
+#endif
+constexpr int kTileWarps = CM_TILE_WARPS;
+constexpr int kTileStage = 1024;  // staged neighbour molecules per pass
+
+struct TileSmem {
+    float4 w[kTileStage];       // staged molecule: centroid + stencil offset (x, y, z), radius
+    int v[kTileStage];          // molecule index | staged cell << 24
+    int nbeg[kTileCells + 1];   // first staged position of each cell (prefix of the cells' molecule counts)
+    int cbeg[kTileCells];       // the cell's first position in the cell-sorted molecule table
+    int code[kTileCells];       // the cell's packed stencil offset
+    int next;                   // next home molecule to claim
+};
+
+__host__ __device__ constexpr size_t tile_smem_extra() { return sizeof(TileSmem) + 16; }
+
+// Stencil offset of half-stencil cell k: the home cell's row forward
+// (k <= L0), the rest of its plane forward, then the planes above.
+__device__ __forceinline__ void half_stencil_cell(int k, const int *L, int &dx, int &dy, int &dz) {
+    const int wx = 2 * L[0] + 1;
+    if (k <= L[0]) {
+        dx = k; dy = 0; dz = 0;
+        return;
+    }
+    k -= L[0] + 1;
+    if (k < wx * L[1]) {
+        dy = 1 + k / wx; dx = k % wx - L[0]; dz = 0;
+        return;
+    }
+    k -= wx * L[1];
+    const int wxy = wx * (2 * L[1] + 1);
+    dz = 1 + k / wxy;
+    const int r = k % wxy;
+    dy = r / wx - L[1];
+    dx = r % wx - L[0];
+}
+
+template <int APS>
+__global__ void __launch_bounds__(kTileWarps * 32, CM_TILE_MIN_CTAS) k_pairs_tile32(DevSys S, Bufs B) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    const int hw = hist_words(S);
+    FlatWarpSmem *wsm = (FlatWarpSmem *)(smem_raw + (((size_t)hw * 4 + 15) & ~(size_t)15));
+    TileSmem &T = *(TileSmem *)(((uintptr_t)(wsm + kTileWarps) + 15) & ~(uintptr_t)15);
+    shist_zero(S, hbase);
+    __syncthreads();
+    SHist h = shist_bind(S, hbase);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
+    FlatWarpSmem &W = wsm[warp];
+    LocalStats st;
+    const int aps = S.aps;
+    const int64_t ncap = B.cs - 1;
+    const int64_t items = (int64_t)B.nf * ncap;
+    for (int64_t t = blockIdx.x; t < items; t += gridDim.x) {
+        const int f = (int)(t / ncap), H = (int)(t - (int64_t)f * ncap);
+        const PairsFrame Pf = pairs_frame(B, f, true);
+        const FrameScratch &F = *Pf.F;
+        const FrameGeom &G = *Pf.G;
+        // every thread takes the same branches: the conditions depend on the item only
+        if (!F.ok || !F.tile || H >= G.ncell) continue;
+        const int hbeg = Pf.cstart[H], nH = Pf.cstart[H + 1] - hbeg;
+        if (nH == 0) continue;
+        const int n0 = G.n[0], n1 = G.n[1], n2 = G.n[2];
+        const int cx = H % n0, cy = (H / n0) % n1, cz = H / (n0 * n1);
+        const int K = (F.L[0] + 1) + (2 * F.L[0] + 1) * F.L[1] + (2 * F.L[0] + 1) * (2 * F.L[1] + 1) * F.L[2];
+        const Guard g = F.g;
+        const float4 *cq32 = B.cq32 + (int64_t)f * B.mv;
+        __syncthreads();  // the previous item's staged table is no longer read
+        if (tid < K) {
+            int dx, dy, dz;
+            half_stencil_cell(tid, F.L, dx, dy, dz);
+            const int c = (wrap_cell(cz + dz, n2) * n1 + wrap_cell(cy + dy, n1)) * n0 + wrap_cell(cx + dx, n0);
+            T.cbeg[tid] = Pf.cstart[c];
+            T.nbeg[tid + 1] = Pf.cstart[c + 1] - Pf.cstart[c];
+            T.code[tid] = pack_delta(dx, dy, dz);
+        }
+        if (tid == 0) T.nbeg[0] = 0;
+        __syncthreads();
+        if (warp == 0) {
+            // inclusive prefix of the K <= kTileCells counts, four per lane
+            int c[4], sum = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = 4 * lane + j;
+                c[j] = k < K ? T.nbeg[k + 1] : 0;
+                sum += c[j];
+            }
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            int run = incl - sum;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = 4 * lane + j;
+                run += c[j];
+                if (k < K) T.nbeg[k + 1] = run;
+            }
+        }
+        __syncthreads();
+        const int M = T.nbeg[K];
+        for (int m0 = 0; m0 < M; m0 += kTileStage) {
+            const int n = min(kTileStage, M - m0);
+            if (m0 > 0) __syncthreads();  // the previous pass's table is no longer read
+            for (int i = tid; i < n; i += blockDim.x) {
+                const int m = m0 + i;
+                int lo = 0, hi = K;  // the cell k with nbeg[k] <= m < nbeg[k + 1]
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (T.nbeg[mid] <= m) lo = mid;
+                    else hi = mid;
+                }
+                int dx, dy, dz;
+                half_stencil_cell(lo, F.L, dx, dy, dz);
+                const float4 of = Pf.off32[off_index(dx, dy, dz)];
+                const int p = T.cbeg[lo] + (m - T.nbeg[lo]);
+                const float4 q = cq32[p];
+                T.w[i] = make_float4(q.x + of.x, q.y + of.y, q.z + of.z, q.w);
+                T.v[i] = Pf.cmol[p] | (lo << 24);
+            }
+            if (tid == 0) T.next = 0;
+            __syncthreads();
+            // the home molecules, claimed one at a time
+            const int own_end = T.nbeg[1] - m0;  // staged positions below this are the home cell (pass 0)
+            for (;;) {
+                int sl = 0;
+                if (lane == 0) sl = atomicAdd(&T.next, 1);
+                sl = __shfl_sync(0xffffffffu, sl, 0);
+                if (sl >= nH) break;
+                const int s = Pf.cmol[hbeg + sl];
+                const float4 qs = Pf.sq32[s];
+                const int sslot = Pf.slot ? Pf.slot[s] : -1;
+                __syncwarp();
+                for (int a = lane; a < aps; a += 32) W.os[a] = Pf.so32[(int64_t)s * aps + a];
+                __syncwarp();
+                const float rsc = g.cut_pre + qs.w;
+                const float rs2 = rsc * rsc;
+                int cnt = 0;
+                for (int p0 = 0; p0 < n; p0 += 32) {
+                    const int p = p0 + lane;
+                    const bool in = p < n;
+                    const int pc = in ? p : n - 1;
+                    const float4 w = T.w[pc];
+                    const int vk = T.v[pc];
+                    const int v = vk & 0xffffff;
+                    float4 Dv;
+                    Dv.x = w.x - qs.x;
+                    Dv.y = w.y - qs.y;
+                    Dv.z = w.z - qs.z;
+                    Dv.w = __int_as_float(v);
+                    const float rr = rsc + w.w;
+                    const bool cand = in && fmaf(Dv.z, Dv.z, fmaf(Dv.y, Dv.y, Dv.x * Dv.x)) <= rr * rr &&
+                                      !(p < own_end && v <= s);
+                    const unsigned mask = __ballot_sync(0xffffffffu, cand);
+                    const int pos = cnt + __popc(mask & ((1u << lane) - 1u));
+                    if (cand) {
+                        W.cq[pos] = Dv;
+                        W.cc[pos] = T.code[vk >> 24];
+                    }
+                    cnt += __popc(mask);
+                    if (cnt >= 32) {
+                        __syncwarp();
+                        flat_batch<true, APS>(S, B, h, W, Pf, g, f, s, sslot, rs2, lane, 32, st);
+                        __syncwarp();
+                        float4 rq = make_float4(0.f, 0.f, 0.f, 0.f);
+                        int rc = 0;
+                        if (lane < cnt - 32) {
+                            rq = W.cq[32 + lane];
+                            rc = W.cc[32 + lane];
+                        }
+                        __syncwarp();
+                        if (lane < cnt - 32) {
+                            W.cq[lane] = rq;
+                            W.cc[lane] = rc;
+                        }
+                        cnt -= 32;
+                        __syncwarp();
+                    }
+                }
+                __syncwarp();
+                if (cnt > 0) flat_batch<true, APS>(S, B, h, W, Pf, g, f, s, sslot, rs2, lane, cnt, st);
+                __syncwarp();
+            }
+        }
     }
     stats_flush(S, st, false);
     __syncthreads();

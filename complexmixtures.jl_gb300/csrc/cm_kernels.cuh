@@ -46,6 +46,7 @@ using namespace cmgeom;
 constexpr int kMaxSmallMol = 32;  // PAIRS regime: atoms per molecule on either side
 constexpr int kWarps = 8;         // warps per CTA of the PAIRS real-pass kernels
 constexpr int kQueue = 64;        // per-warp candidate queue
+constexpr int kTileCells = 128;   // half-stencil cells the tiled real pass stages per home cell
 
 enum : int { ERR_STENCIL = 1, ERR_BIN = 2, ERR_QUEUE = 4, ERR_SIZE = 8 };
 enum : int {
@@ -115,6 +116,7 @@ struct FrameScratch {
     int multi;      // PAIRS axes with several images (bit k set for axis k)
     int La[3];      // ATOMS stencil half-widths
     float xmax;     // largest |coordinate component| of the frame's input atoms (rounded up)
+    int tile;       // self mode, one image per pair, half stencil within kTileCells: the tiled real pass takes the frame
     Guard g;        // FP32 search
     Guard64 g64;    // FP64 search
 };
@@ -1496,6 +1498,9 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
             if (2 * L[k] + 1 > G.n[k]) multi |= 1 << k;
         }
         F.multi = multi;
+        // half-stencil cells: the home cell's row forward, the rest of its plane forward, the planes above
+        const int K = (L[0] + 1) + (2 * L[0] + 1) * L[1] + (2 * L[0] + 1) * (2 * L[1] + 1) * L[2];
+        F.tile = (pairs && S.self && multi == 0 && K <= kTileCells && S.mv < (1 << 24)) ? 1 : 0;
         F.ok = ok ? 1 : 0;
     }
     __syncthreads();

@@ -200,6 +200,7 @@ struct cm_handle {
     DevBuf scell, sq32, sq64, so32, so64, vcell, vq32, vq64, vo32, vo64, ccount, cstart, cfill, cmol, cq32, gq, rq, eq;
     int gq_cap = 0, rq_cap = 0;
     int flat_ctas = 0;  // resident CTAs per SM of k_pairs_flat32
+    int tile_ctas = 0;  // resident CTAs per SM of k_pairs_tile32 (self mode)
     int guard_ctas = 1, edge_ctas = 1, rand_ctas = 1, real_ctas = 1;  // ... of the guard, edge, random and generic kernels
     // group tables
     DevBuf g_soff, g_sidx, g_voff, g_vidx;
@@ -375,7 +376,7 @@ void check_desc(const cm_system_desc *d) {
     if (d->launch < CM_LAUNCH_AUTO || d->launch > CM_LAUNCH_GRAPH) bad("unknown launch mode");
     if (d->atoms_schedule < CM_SCHED_AUTO || d->atoms_schedule > CM_SCHED_BALANCED) bad("unknown atoms_schedule");
     if (d->guard_queue_capacity < 0) bad("guard_queue_capacity must be >= 0");
-    if (d->reserved != 0) bad("reserved must be 0");
+    if (d->real_pass < CM_REAL_AUTO || d->real_pass > CM_REAL_TILE) bad("unknown real_pass");
     if (d->solute_nmols < 1 || d->solute_natomspermol < 1 || d->solvent_nmols < 1 || d->solvent_natomspermol < 1)
         bad("selections must have at least one molecule of at least one atom");
     if (d->autocorrelation && (d->solute_nmols != d->solvent_nmols || d->solute_natomspermol != d->solvent_natomspermol))
@@ -502,31 +503,50 @@ double target_cell(const cm_handle *h) {
 size_t pairs_extra_smem() {
     const size_t real = (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8;
     const size_t flat = (size_t)kFlatWarps * flat_warp_smem();
-    return std::max(real, flat);
+    const size_t tile = (size_t)kTileWarps * flat_warp_smem() + tile_smem_extra();
+    return std::max(real, std::max(flat, tile));
 }
 
 // The FP32 real-pass kernel for a system: specialised on the solute molecule
 // size for the common sizes, generic otherwise.
-using FlatLaunch = void (*)(int, size_t, cudaStream_t, const DevSys &, const Bufs &);
+// The tiled kernel (self mode) is launched first; the per-molecule kernel then
+// takes the frames it did not (skip = 1), or every frame (skip = 0).
+using FlatLaunch = void (*)(int, size_t, cudaStream_t, const DevSys &, const Bufs &, int);
+using TileLaunch = void (*)(int, size_t, cudaStream_t, const DevSys &, const Bufs &);
 struct FlatKernel {
     const void *fn;
     FlatLaunch launch;
+    const void *tile_fn;  // nullptr in cross mode
+    TileLaunch tile_launch;
 };
 
 template <bool SELF, int APS>
-void launch_flat(int grid, size_t smem, cudaStream_t st, const DevSys &S, const Bufs &B) {
-    k_pairs_flat32<SELF, APS><<<grid, kFlatWarps * 32, smem, st>>>(S, B);
+void launch_flat(int grid, size_t smem, cudaStream_t st, const DevSys &S, const Bufs &B, int skip_tile) {
+    k_pairs_flat32<SELF, APS><<<grid, kFlatWarps * 32, smem, st>>>(S, B, skip_tile);
+}
+
+template <int APS>
+void launch_tile(int grid, size_t smem, cudaStream_t st, const DevSys &S, const Bufs &B) {
+    k_pairs_tile32<APS><<<grid, kTileWarps * 32, smem, st>>>(S, B);
+}
+
+template <bool SELF, int APS>
+FlatKernel flat_kernel_for() {
+    if (SELF)
+        return {(const void *)k_pairs_flat32<SELF, APS>, launch_flat<SELF, APS>, (const void *)k_pairs_tile32<APS>,
+                launch_tile<APS>};
+    return {(const void *)k_pairs_flat32<SELF, APS>, launch_flat<SELF, APS>, nullptr, nullptr};
 }
 
 template <bool SELF>
 FlatKernel flat_kernel_of(int aps) {
     switch (aps) {
-        case 1: return {(const void *)k_pairs_flat32<SELF, 1>, launch_flat<SELF, 1>};
-        case 3: return {(const void *)k_pairs_flat32<SELF, 3>, launch_flat<SELF, 3>};
-        case 4: return {(const void *)k_pairs_flat32<SELF, 4>, launch_flat<SELF, 4>};
-        case 5: return {(const void *)k_pairs_flat32<SELF, 5>, launch_flat<SELF, 5>};
-        case 14: return {(const void *)k_pairs_flat32<SELF, 14>, launch_flat<SELF, 14>};
-        default: return {(const void *)k_pairs_flat32<SELF, 0>, launch_flat<SELF, 0>};
+        case 1: return flat_kernel_for<SELF, 1>();
+        case 3: return flat_kernel_for<SELF, 3>();
+        case 4: return flat_kernel_for<SELF, 4>();
+        case 5: return flat_kernel_for<SELF, 5>();
+        case 14: return flat_kernel_for<SELF, 14>();
+        default: return flat_kernel_for<SELF, 0>();
     }
 }
 
@@ -566,7 +586,11 @@ int flat_setup(cm_handle *h) {
     const void *real = fp32 ? (self ? (const void *)k_pairs_real<true, true> : (const void *)k_pairs_real<true, false>)
                             : (self ? (const void *)k_pairs_real<false, true> : (const void *)k_pairs_real<false, false>);
     h->real_ctas = resident_ctas(real, kWarps * 32, hsm + (size_t)kWarps * kMaxSmallMol * 16 + (size_t)kWarps * kQueue * 8);
-    return resident_ctas(flat_kernel(h).fn, kFlatWarps * 32, hsm + (size_t)kFlatWarps * flat_warp_smem());
+    const FlatKernel fk = flat_kernel(h);
+    h->tile_ctas = fk.tile_fn ? resident_ctas(fk.tile_fn, kTileWarps * 32,
+                                              hsm + (size_t)kTileWarps * flat_warp_smem() + tile_smem_extra())
+                              : 0;
+    return resident_ctas(fk.fn, kFlatWarps * 32, hsm + (size_t)kFlatWarps * flat_warp_smem());
 }
 
 // The ATOMS evaluation kernels of a system (precision x schedule).
@@ -631,6 +655,7 @@ void kernel_smem_limits(int device) {
     raise((const void *)k_pairs_edge<false>);
     for (int aps : {0, 1, 3, 4, 5, 14}) {
         raise(flat_kernel_of<true>(aps).fn);
+        raise(flat_kernel_of<true>(aps).tile_fn);
         raise(flat_kernel_of<false>(aps).fn);
     }
     g_smem_done[device] = true;
@@ -1036,7 +1061,14 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
             const int fgrid = (int)std::min<int64_t>(((int64_t)nf * ms + kFlatWarps - 1) / kFlatWarps,
                                                      (int64_t)sms * h->flat_ctas);
             const FlatKernel fk = flat_kernel(h);
-            CM_LAUNCH(CM_K_REAL, fk.launch(fgrid, fsm, st, S, B));
+            const bool tile = fk.tile_fn && d.real_pass != CM_REAL_WARP;
+            if (tile) {
+                // one CTA per home cell; the per-molecule kernel returns at once
+                // unless a frame's stencil is beyond the tiled kernel's table
+                const size_t tsm = hsm + (size_t)kTileWarps * flat_warp_smem() + tile_smem_extra();
+                CM_LAUNCH(CM_K_REAL, fk.tile_launch(sms * h->tile_ctas, tsm, st, S, B));
+            }
+            CM_LAUNCH(CM_K_REAL, fk.launch(fgrid, fsm, st, S, B, tile ? 1 : 0));
         }
         // the generic kernel takes every frame, or after the specialised one
         // only the frames that need several images per molecule pair

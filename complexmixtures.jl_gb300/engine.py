@@ -24,6 +24,8 @@ def _is_torch(x) -> bool:
 
 SCHEDULES = {"auto": N.CM_SCHED_AUTO, "cell": N.CM_SCHED_CELL, "balanced": N.CM_SCHED_BALANCED}
 SCHEDULE_NAMES = {v: k for k, v in SCHEDULES.items()}
+REAL_PASSES = {"auto": N.CM_REAL_AUTO, "warp": N.CM_REAL_WARP, "tile": N.CM_REAL_TILE}
+REAL_PASS_NAMES = {v: k for k, v in REAL_PASSES.items()}
 
 
 def system_desc(
@@ -57,6 +59,7 @@ def system_desc(
     launch: str = "auto",
     atoms_schedule: str = "auto",
     guard_queue_capacity: int = 0,
+    real_pass: str = "auto",
 ):
     """cm_system_desc of a system, and the arrays it points to (keep them
     alive while the description is in use).  ``cell_scale_pct`` scales the
@@ -67,7 +70,8 @@ def system_desc(
     speed only); ``guard_queue_capacity`` (0 = sized by the engine) bounds the
     FP32 real pass's guard and edge queues per compute chunk: a chunk that
     overflows them is redone on the device without queues, so the counts do
-    not depend on it."""
+    not depend on it; ``real_pass`` ("auto", "warp" or "tile") picks the FP32
+    real-pass schedule of the molecule layout (speed only)."""
     d = N.cm_system_desc()
     d.api_version = N.CM_API_VERSION
     d.solute_nmols = solute_nmols
@@ -113,6 +117,9 @@ def system_desc(
         raise ValueError(f"atoms_schedule must be one of {sorted(SCHEDULES)}")
     d.atoms_schedule = SCHEDULES[atoms_schedule]
     d.guard_queue_capacity = guard_queue_capacity
+    if real_pass not in REAL_PASSES:
+        raise ValueError(f"real_pass must be one of {sorted(REAL_PASSES)}")
+    d.real_pass = REAL_PASSES[real_pass]
     return d, keep
 
 

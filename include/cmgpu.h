@@ -66,6 +66,11 @@ enum { CM_LAUNCH_AUTO = 0, CM_LAUNCH_STREAM = 1, CM_LAUNCH_GRAPH = 2 };
  * thread per pair in the FP64 path) for sparse solutes.  AUTO picks by the
  * solute atoms per occupied cell of the first frame (64 or more: CELL). */
 enum { CM_SCHED_AUTO = 0, CM_SCHED_CELL = 1, CM_SCHED_BALANCED = 2 };
+/* FP32 real pass of the PAIRS layout: WARP = one warp per solute molecule
+ * walking its stencil; TILE (self-MDDF) = one CTA per home cell, the cell's
+ * half-stencil molecules staged in shared memory and shared by its warps.
+ * AUTO takes TILE in self mode. */
+enum { CM_REAL_AUTO = 0, CM_REAL_WARP = 1, CM_REAL_TILE = 2 };
 /* CM_COORD_DCD: solute_xyz points at nframes raw DCD frames (frame_bytes each,
  * laid out as cm_set_dcd_layout declared) and solvent_xyz is NULL; the
  * engine gathers the selections on the device. */
@@ -127,7 +132,8 @@ typedef struct cm_system_desc {
                                          queues; 0 = sized by the engine.  A chunk whose deferred records
                                          do not fit is redone on the device without queues, so the counts
                                          do not depend on it (a small value only exercises that path) */
-    int32_t reserved;                 /* must be 0 */
+    int32_t real_pass;                /* CM_REAL_*: FP32 real-pass schedule of the PAIRS layout; the counts do
+                                         not depend on it */
 } cm_system_desc;
 
 /*
