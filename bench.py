@@ -501,22 +501,35 @@ def run_reference(args, world, rank):
 
 
 def other_workload(args, local):
-    """Frames/s of one ATOMS-layout configuration (FP32 + guard, frames in
-    HBM), with the per-class kernel times; the config-4 case is its median
-    system (43,000 atoms)."""
+    """Frames/s of one ATOMS-layout configuration (bench --workload)."""
     import torch
 
     import __graft_entry__ as entry
 
     cm = entry.load_package()
     torch.cuda.set_device(local)
+    print(json.dumps(atoms_leg(cm, local, args.workload, steps, args.warmup)), flush=True)
+
+
+_SYNTH_CACHE = {}
+
+
+def atoms_leg(cm, local, workload, steps, warmup):
+    """Frames/s of one ATOMS-layout configuration (FP32 + guard, frames in
+    HBM), with the per-class kernel times, the guard statistics and the plain
+    FP64 path on the same frames; the config-4 case is its median system
+    (43,000 atoms)."""
+    import torch
+
     syn = __import__("importlib").import_module("complexmixtures_gb300.synth")
     nframes, solvent = 10, 0
-    if args.workload == "c1":
+    if workload == "c1":
         sysm = syn.config1()
-    elif args.workload.startswith("c2"):
-        sysm, nframes = syn.config2(), 4
-        solvent = 0 if args.workload == "c2-water" else 1
+    elif workload.startswith("c2"):
+        if "c2" not in _SYNTH_CACHE:
+            _SYNTH_CACHE["c2"] = syn.config2()
+        sysm, nframes = _SYNTH_CACHE["c2"], 4
+        solvent = 0 if workload == "c2-water" else 1
     else:
         sysm = syn.config4_system(43000, 20261207 + 43000, nframes=16)
         nframes = 16
@@ -533,13 +546,13 @@ def other_workload(args, local):
     ids = np.arange(1, nframes + 1)
     eng = cm.Engine(precision="fp32", kernel_timing=True, **kw)
     stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=f"cuda:{local}")
-    for _ in range(max(args.warmup, 1)):
+    for _ in range(max(warmup, 1)):
         eng.submit(xd, vd, cells, frame_ids=ids)
     eng.synchronize()
     eng.reset()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         eng.submit(xd, vd, cells, frame_ids=ids)
     e1.record(stream)
     e1.synchronize()
@@ -548,13 +561,13 @@ def other_workload(args, local):
     st = eng.stats()
     raw32 = eng.raw_counts()
     eng.close()
-    frames = args.steps * nframes
+    frames = steps * nframes
     # the plain FP64 path on the same frames: its frames/s and the count comparison
     eng64 = cm.Engine(precision="fp64", **kw)
     s64 = torch.cuda.ExternalStream(eng64.stream_ptr(), device=f"cuda:{local}")
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(s64)
-    for _ in range(args.steps):
+    for _ in range(steps):
         eng64.submit(xd, vd, cells, frame_ids=ids)
     b.record(s64)
     b.synchronize()
@@ -562,9 +575,9 @@ def other_workload(args, local):
     raw64 = eng64.raw_counts()
     eng64.close()
     hits = st["hits_real"] + st["hits_random"]
-    print(json.dumps({
-        "workload": args.workload, "metric": "MDDF frames/s", "value": frames / (ms / 1e3), "unit": "frames/s",
-        "steps": args.steps, "warmup": args.warmup, "frames_per_step": nframes,
+    return {
+        "workload": workload, "metric": "MDDF frames/s", "value": frames / (ms / 1e3), "unit": "frames/s",
+        "steps": steps, "warmup": warmup, "frames_per_step": nframes,
         "atoms": {"solute": int(sysm.solute_nmols * aps), "solvent": int(sv.nmols * sv.natomspermol)},
         "layout": "ATOMS" if st["regime"] == 2 else "PAIRS",
         "kernel_ms_per_frame": {k: v[0] / frames for k, v in kt.items()},
@@ -574,7 +587,7 @@ def other_workload(args, local):
         "plain_fp64": {"value": frames / (ms64 / 1e3), "unit": "frames/s",
                        "counts_identical_to_fp32_guard": all(np.array_equal(raw32[k], raw64[k]) for k in raw32)},
         "precision": "fp32 search, fp64 guard band", "data": "synthetic (seeded generator of the configuration)",
-    }), flush=True)
+    }
 
 
 def grid3d_workload(args, local):
@@ -769,9 +782,12 @@ def main():
             pass
 
     serving = batched = None
+    atoms_configs = None
     if not args.no_serving and world == 1:
         serving = serving_leg(cm, local)
         batched = batched_c4_leg(cm, local)
+        # the other configurations' systems (ATOMS layout), a few frames each
+        atoms_configs = {w: atoms_leg(cm, local, w, steps=2, warmup=1) for w in ("c1", "c2-water", "c2-cosolvent", "c4")}
 
     launches = st["kernel_launches"] - st0["kernel_launches"]
     line = {
@@ -789,6 +805,7 @@ def main():
                   "hits_per_frame": (st["hits_real"] + st["hits_random"]) / max(1, st["frames"]),
                   "max_fp32_error_A": st["max_guard_error"]},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
+        "atoms_configs": atoms_configs,
         "serving": serving,
         "batched_c4": batched,
     }

@@ -210,7 +210,7 @@ class cm_tuning(C.Structure):
         ("ms_per_frame", C.c_double * CM_TUNE_MAX),
         ("atoms_schedule", C.c_int32),
         ("schedules", C.c_int32 * CM_TUNE_MAX),
-        ("reserved", C.c_int32),
+        ("real_pass", C.c_int32),
     ]
 
 

@@ -2697,16 +2697,19 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
                        (desc->regime == CM_REGIME_AUTO &&
                         (desc->solute_natomspermol > kMaxSmallMol || desc->solvent_natomspermol > kMaxSmallMol));
     // ATOMS: cutoff / (lcell k), each with both evaluation schedules;
-    // PAIRS: the molecule cell and smaller ones
+    // PAIRS: the molecule cell and smaller ones, in self mode each with both
+    // real-pass schedules (home-cell tiles, warps per molecule)
     const int cand_atoms[] = {100, 80, 50, 34};
     const int cand_pairs[] = {100, 75, 60, 50};
     const int *cand = atoms ? cand_atoms : cand_pairs;
-    const int ncand = atoms ? 8 : 4;
+    const bool two_real = !atoms && desc->autocorrelation && desc->precision == CM_PRECISION_FP32_GUARD;
+    const int ncand = (atoms || two_real) ? 8 : 4;
     double best = 0.0;
     for (int c = 0; c < ncand; ++c) {
         cm_system_desc d = *desc;
         d.cell_scale_pct = cand[c % 4];
         d.atoms_schedule = atoms ? (c < 4 ? CM_SCHED_CELL : CM_SCHED_BALANCED) : CM_SCHED_AUTO;
+        if (!atoms) d.real_pass = two_real ? (c < 4 ? CM_REAL_TILE : CM_REAL_WARP) : desc->real_pass;
         d.kernel_timing = 1;
         d.launch = CM_LAUNCH_STREAM;
         cm_handle *h = nullptr;
@@ -2730,12 +2733,13 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
         }
         cm_destroy(h);
         out->candidates[c] = cand[c % 4];
-        out->schedules[c] = d.atoms_schedule;
+        out->schedules[c] = atoms ? d.atoms_schedule : d.real_pass;
         out->ms_per_frame[c] = ms / std::max(1, sample->nframes);
         if (c == 0 || out->ms_per_frame[c] < best) {
             best = out->ms_per_frame[c];
             out->cell_scale_pct = cand[c % 4];
-            out->atoms_schedule = d.atoms_schedule;
+            out->atoms_schedule = atoms ? d.atoms_schedule : 0;
+            out->real_pass = atoms ? 0 : d.real_pass;
         }
     }
     out->ncandidates = ncand;

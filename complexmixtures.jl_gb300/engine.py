@@ -124,12 +124,14 @@ def system_desc(
 
 
 def autotune(solute_xyz, solvent_xyz, cells, frame_ids=None, **system) -> dict:
-    """Time the candidate search-cell sizes (and, in the ATOMS layout, both
-    evaluation schedules) on sample frames (cm_autotune).  Returns the fastest
-    as {"cell_scale_pct", "atoms_schedule"} plus "candidates", a list of
-    {"cell_scale_pct", "atoms_schedule", "ms_per_frame"}; pass the first two to
-    Engine."""
+    """Time the candidate search-cell sizes, and with each the evaluation
+    schedules (ATOMS layout: cell and balanced; self-MDDF in the molecule
+    layout: home-cell tiles and warps per molecule), on sample frames
+    (cm_autotune).  Returns the fastest as {"cell_scale_pct",
+    "atoms_schedule", "real_pass"} plus "candidates", a list of the same keys
+    with "ms_per_frame"; pass the first three to Engine."""
     lib = N.load()
+    system = {k: v for k, v in system.items() if k not in ("cell_scale_pct", "atoms_schedule", "real_pass")}
     d, keep = system_desc(**system)
     Ns = d.solute_nmols * d.solute_natomspermol
     Nv = d.solvent_nmols * d.solvent_natomspermol
@@ -137,9 +139,19 @@ def autotune(solute_xyz, solvent_xyz, cells, frame_ids=None, **system) -> dict:
     t = N.cm_tuning()
     N.raise_for(lib.cm_autotune(C.byref(d), C.byref(fr), C.byref(t)), None)
     del keep, keep_f
-    return {"cell_scale_pct": t.cell_scale_pct, "atoms_schedule": SCHEDULE_NAMES[t.atoms_schedule],
-            "candidates": [{"cell_scale_pct": t.candidates[i], "atoms_schedule": SCHEDULE_NAMES[t.schedules[i]],
-                            "ms_per_frame": t.ms_per_frame[i]} for i in range(t.ncandidates)]}
+    atoms = d.regime == N.CM_REGIME_ATOMS or (d.regime == N.CM_REGIME_AUTO and max(
+        d.solute_natomspermol, d.solvent_natomspermol) > 32)
+    out = {"cell_scale_pct": t.cell_scale_pct, "atoms_schedule": SCHEDULE_NAMES[t.atoms_schedule],
+           "real_pass": REAL_PASS_NAMES[t.real_pass], "candidates": []}
+    for i in range(t.ncandidates):
+        c = {"cell_scale_pct": t.candidates[i], "ms_per_frame": t.ms_per_frame[i]}
+        if atoms:
+            c["atoms_schedule"] = SCHEDULE_NAMES[t.schedules[i]]
+        else:
+            c["atoms_schedule"] = "auto"
+            c["real_pass"] = REAL_PASS_NAMES[t.schedules[i]]
+        out["candidates"].append(c)
+    return out
 
 
 def memory_cache(device: int = 0, release: bool = False) -> dict:

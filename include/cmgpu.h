@@ -449,8 +449,9 @@ typedef struct cm_tuning {
     int32_t candidates[CM_TUNE_MAX];  /* cell_scale_pct of each candidate */
     double ms_per_frame[CM_TUNE_MAX]; /* measured GPU time per frame of each candidate */
     int32_t atoms_schedule;           /* the fastest candidate's CM_SCHED_* (ATOMS layout; 0 otherwise) */
-    int32_t schedules[CM_TUNE_MAX];   /* CM_SCHED_* of each candidate */
-    int32_t reserved;
+    int32_t schedules[CM_TUNE_MAX];   /* each candidate's CM_SCHED_* (ATOMS layout) or CM_REAL_* (molecule
+                                         layout) */
+    int32_t real_pass;                /* the fastest candidate's CM_REAL_* (molecule layout; 0 otherwise) */
 } cm_tuning;
 
 int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *out);

@@ -233,9 +233,11 @@ def test_autotune_reports_candidates(cm, gpu_ready):
     t = cm.autotune(xs, None, cells, solute_nmols=200, solute_natomspermol=5, solvent_nmols=200,
                     solvent_natomspermol=5, autocorrelation=True, irefatom=1, cutoff=7.0, binstep=0.02, dbulk=7.0,
                     usecutoff=False, nbins=350, n_random_samples=4)
-    ms = {c["cell_scale_pct"]: c["ms_per_frame"] for c in t["candidates"]}
-    assert len(ms) == 4 and all(v > 0 for v in ms.values()) and t["atoms_schedule"] == "auto"
-    assert ms[t["cell_scale_pct"]] == min(ms.values())
+    # self-MDDF in the molecule layout: 4 cell sizes x both real-pass schedules
+    ms = {(c["cell_scale_pct"], c["real_pass"]): c["ms_per_frame"] for c in t["candidates"]}
+    assert len(ms) == 8 and all(v > 0 for v in ms.values()) and t["atoms_schedule"] == "auto"
+    assert {k[1] for k in ms} == {"tile", "warp"}
+    assert ms[(t["cell_scale_pct"], t["real_pass"])] == min(ms.values())
 
 
 def test_autotune_atoms_tries_both_schedules(cm, gpu_ready):
