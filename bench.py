@@ -75,7 +75,7 @@ def parse():
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--real-pass", default="auto", choices=["auto", "warp", "tile"],
                    help="FP32 real-pass schedule (speed only): per-molecule warps or home-cell tiles")
-    p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4", "c5", "grid3d"],
+    p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4", "c4-batch", "c5", "grid3d"],
                    help="c3 (default): the headline line; the others: frames/s of that configuration's system "
                         "(ATOMS layout) on device-resident frames")
     return p.parse_args()
@@ -366,6 +366,7 @@ def batched_c4_leg(cm, device):
     tune = cm.autotune(xs[:2], xv[:2], cells[:2], **kw)
     pct = tune["cell_scale_pct"]
     sched = tune["atoms_schedule"]
+    agrid = tune["atoms_grid"]
     frames_total = C4_FRAMES * len(systems)
 
     def serial():
@@ -373,7 +374,7 @@ def batched_c4_leg(cm, device):
         torch.cuda.synchronize()
         t = time.perf_counter()
         for xs, xv, cells, kw in systems:
-            eng = cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, **kw)
+            eng = cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, atoms_grid=agrid, **kw)
             eng.submit(xs, xv, cells)
             out.append(eng.raw_counts())
             eng.close()
@@ -383,7 +384,7 @@ def batched_c4_leg(cm, device):
         # all 64 systems in one cm_batch: one CUDA graph launch per staging round
         torch.cuda.synchronize()
         t = time.perf_counter()
-        engines = [cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, **kw) for xs, xv, cells, kw in systems]
+        engines = [cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, atoms_grid=agrid, **kw) for xs, xv, cells, kw in systems]
         with cm.Batch(engines) as b:
             b.submit([(xs, xv, cells) for xs, xv, cells, kw in systems])
             gst = b.graph_stats()
@@ -392,16 +393,17 @@ def batched_c4_leg(cm, device):
             e.close()
         return time.perf_counter() - t, out, gst
 
-    def resident_batch(steps=3):
+    def resident_batch(mode, steps=3):
         # the systems stay resident: engines and batch made once, frames on the
         # device, each step one cm_batch_submit of every system's frames
         dev = [(torch.as_tensor(xs, device=device), torch.as_tensor(xv, device=device), cells)
                for xs, xv, cells, kw in systems]
-        engines = [cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, **kw) for xs, xv, cells, kw in systems]
-        with cm.Batch(engines) as b:
+        engines = [cm.Engine(cell_scale_pct=pct, atoms_schedule=sched, atoms_grid=agrid, **kw) for xs, xv, cells, kw in systems]
+        with cm.Batch(engines, mode=mode) as b:
             b.submit(dev)  # warm-up
             for e in engines:
                 e.reset()
+            g0 = b.graph_stats()
             torch.cuda.synchronize()
             t = time.perf_counter()
             for _ in range(steps):
@@ -409,10 +411,12 @@ def batched_c4_leg(cm, device):
             for e in engines:
                 e.synchronize()
             dt = time.perf_counter() - t
+            g1 = b.graph_stats()
         out = [e.raw_counts() for e in engines]
         for e in engines:
             e.close()
-        return dt / steps, out
+        per = {k: (g1[k] - g0[k]) / steps for k in ("graph_launches", "fused_rounds", "stage_launches")}
+        return dt / steps, out, per
 
     serial()  # warm-up
     ts, ref = serial()
@@ -420,13 +424,16 @@ def batched_c4_leg(cm, device):
     tg, gout, gst = graph_batch()
     same_graph = all(all(np.array_equal(gout[i][k], ref[i][k]) for k in ("md", "md_random", "solute_group"))
                      for i in range(len(systems)))
-    tr, rout = resident_batch()
+    tr, rout, rper = resident_batch("fused")
     # three steps of the same frames: each count is three times the one-pass count
     same_resident = all(all(np.array_equal(rout[i][k], 3 * ref[i][k]) for k in ("md", "md_random", "solute_group"))
                         for i in range(len(systems)))
+    trs, rsout, rsper = resident_batch("streams")
+    same_streams = all(all(np.array_equal(rsout[i][k], 3 * ref[i][k]) for k in ("md", "md_random", "solute_group"))
+                       for i in range(len(systems)))
     with cm.Server(device=device, frames_per_turn=C4_FRAMES) as srv:
         t0 = time.perf_counter()
-        ids = [srv.submit(xs, xv, cells, cell_scale_pct=pct, atoms_schedule=sched, **kw) for xs, xv, cells, kw in systems]
+        ids = [srv.submit(xs, xv, cells, cell_scale_pct=pct, atoms_schedule=sched, atoms_grid=agrid, **kw) for xs, xv, cells, kw in systems]
         infos = [srv.wait(r, timeout=600) for r in ids]
         tb = time.perf_counter() - t0
         same = all(all(np.array_equal(srv.raw_counts(r)[k], ref[i][k]) for k in ("md", "md_random", "solute_group"))
@@ -443,10 +450,14 @@ def batched_c4_leg(cm, device):
         "graph_batch_counts_identical_to_serial": bool(same_graph),
         "graph_batch_resident_frames_per_s": frames_total / tr,
         "graph_batch_resident_counts_identical_to_serial": bool(same_resident),
+        "graph_batch_resident_launches_per_step": rper,
+        "graph_batch_resident_streams_frames_per_s": frames_total / trs,
+        "graph_batch_resident_streams_counts_identical_to_serial": bool(same_streams),
+        "graph_batch_resident_streams_launches_per_step": rsper,
         "p50_ms": pct_lat["p50"], "p99_ms": pct_lat["p99"],
-        "cell_scale_pct": pct, "atoms_schedule": sched,
-        "autotune_ms_per_frame": {f'{c["cell_scale_pct"]}/{c["atoms_schedule"]}': round(c["ms_per_frame"], 4)
-                                  for c in tune["candidates"]},
+        "cell_scale_pct": pct, "atoms_schedule": sched, "atoms_grid": agrid,
+        "autotune_ms_per_frame": {f'{c["cell_scale_pct"]}/{c["atoms_schedule"]}/grid{c["atoms_grid"]}':
+                                  round(c["ms_per_frame"], 4) for c in tune["candidates"]},
         "failed": sum(1 for x in infos if x["state"] != "done"),
         "counts_identical_to_serial": bool(same),
     }
@@ -501,14 +512,21 @@ def run_reference(args, world, rank):
 
 
 def other_workload(args, local):
-    """Frames/s of one ATOMS-layout configuration (bench --workload)."""
+    """Frames/s of one ATOMS-layout configuration (bench --workload), or the
+    config-4 load of 64 systems (c4-batch)."""
     import torch
 
     import __graft_entry__ as entry
 
     cm = entry.load_package()
     torch.cuda.set_device(local)
-    print(json.dumps(atoms_leg(cm, local, args.workload, steps, args.warmup)), flush=True)
+    if args.workload == "c4-batch":
+        out = batched_c4_leg(cm, local)
+        out.update(metric="MDDF frames/s (config 4, 64 systems)", unit="frames/s",
+                   value=out["graph_batch_resident_frames_per_s"])
+        print(json.dumps(out), flush=True)
+        return
+    print(json.dumps(atoms_leg(cm, local, args.workload, args.steps, args.warmup)), flush=True)
 
 
 _SYNTH_CACHE = {}
@@ -584,6 +602,9 @@ def atoms_leg(cm, local, workload, steps, warmup):
         "guard": {"band_A": st["guard_band"], "reevaluations": st["guard_reevaluations"],
                   "rate_per_record": st["guard_reevaluations"] / hits if hits else 0.0,
                   "max_fp32_error_A": st["max_guard_error"]},
+        "per_frame": {"molecule_pairs_evaluated": st["molecule_pairs_evaluated"] / frames,
+                      "atom_pairs_evaluated": st["atom_pairs_evaluated"] / frames,
+                      "hits": hits / frames},
         "plain_fp64": {"value": frames / (ms64 / 1e3), "unit": "frames/s",
                        "counts_identical_to_fp32_guard": all(np.array_equal(raw32[k], raw64[k]) for k in raw32)},
         "precision": "fp32 search, fp64 guard band", "data": "synthetic (seeded generator of the configuration)",

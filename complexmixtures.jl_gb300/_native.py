@@ -12,7 +12,7 @@ from typing import Optional
 
 import numpy as np
 
-CM_API_VERSION = 3
+CM_API_VERSION = 4
 CM_OK, CM_EINVAL, CM_ENOMEM, CM_ECUDA, CM_EDEVICE, CM_ESTATE = range(6)
 CM_MODE_MDDF, CM_MODE_COORDINATION_NUMBER = 0, 1
 CM_PRECISION_FP64, CM_PRECISION_FP32_GUARD = 0, 1
@@ -68,6 +68,8 @@ class cm_system_desc(C.Structure):
         ("atoms_schedule", C.c_int32),
         ("guard_queue_capacity", C.c_int32),
         ("real_pass", C.c_int32),
+        ("atoms_grid", C.c_int32),
+        ("atoms_grid_capacity", C.c_int32),
     ]
 
 
@@ -211,6 +213,8 @@ class cm_tuning(C.Structure):
         ("atoms_schedule", C.c_int32),
         ("schedules", C.c_int32 * CM_TUNE_MAX),
         ("real_pass", C.c_int32),
+        ("atoms_grid", C.c_int32),
+        ("grids", C.c_int32 * CM_TUNE_MAX),
     ]
 
 
@@ -246,6 +250,8 @@ EXPORTED = (
     "cm_batch_create",
     "cm_batch_submit",
     "cm_batch_graph_stats",
+    "cm_batch_set_mode",
+    "cm_batch_fused_stats",
     "cm_batch_destroy",
     "cm_batch_last_error",
     "cm_read_counts",
@@ -336,6 +342,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cm_batch_submit.restype = C.c_int
     lib.cm_batch_graph_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.cm_batch_graph_stats.restype = C.c_int
+    lib.cm_batch_set_mode.argtypes = [C.c_void_p, C.c_int32]
+    lib.cm_batch_set_mode.restype = C.c_int
+    lib.cm_batch_fused_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.cm_batch_fused_stats.restype = C.c_int
     lib.cm_batch_destroy.argtypes = [C.c_void_p]
     lib.cm_batch_destroy.restype = C.c_int
     lib.cm_batch_last_error.argtypes = [C.c_void_p]

@@ -1,0 +1,517 @@
+// cm_agrid.cuh -- candidate grid of the ATOMS layout for a single solute
+// molecule (a protein or a long chain: configs 1, 2 and 4), FP32 search.
+//
+// The question the ATOMS search answers per solvent molecule is, site by
+// site, "which solute atom is closest, how close is the second, and how close
+// is the closest atom to the reference site" (src/minimum_distances.jl:30-39,
+// 107-120).  With one solute molecule that is a nearest-neighbour query
+// against one fixed point set per frame, asked once per real solvent molecule
+// and n_random_samples times per slot of the random insertion
+// (src/mddf.jl:65-88, 403-423).  So per frame each search cell is split into
+// K^3 fine cells, and each fine cell g gets the list of solute atoms a with
+//
+//     dmin(a, g) <= min( min_a' dmax(a', g), cutoff ) + margin,
+//
+// dmin / dmax the smallest / largest distance from a to a point of g (exact
+// box distances for orthogonal cells, the fine cell's bounding sphere
+// otherwise) and margin = 2 delta + 1e-3 (1 + cutoff).  For a point y of g the
+// nearest atom is within min_a' dmax(a', g), so the list holds every atom
+// within (nearest distance + 2 delta) of y, and every atom within the cutoff
+// when nothing is closer.  A query (one site) reads its fine cell's list and
+// evaluates only those atoms: the smallest FP32 distance, its atom, the
+// second-smallest value (exact whenever it is within 2 delta of the smallest;
+// the guard test only asks that) and the reference site's smallest distance
+// are then the values a walk over every stencil cell gives, and every decision
+// follows the FP32 + guard rules of atoms_decide.  A query whose record lies
+// inside the guard band is queued for k_atoms_eval, which walks the stencil
+// and decides it from exact distances, so the counts stay the oracle's.
+//
+// A list entry is the atom's FP32 position from the fine cell's search-cell
+// origin, q_a + off(cell_a - cell), which is the displacement form of the
+// ATOMS walks (the guard band's error bound covers it), and the atom's index
+// in the molecule.
+//
+// Kernels: k_agrid_build<false> (list lengths), k_agrid_scan (per-frame
+// offsets; a frame whose lists do not fit loses its grid), k_agrid_build<true>
+// (entries), k_agrid_real (real pass) and k_agrid_random (random insertion:
+// placement and query fused, nothing written for slots decided at once).
+// Frames without a grid take the walk path through the same two kernels,
+// which then queue their molecule pairs for k_atoms_eval as k_atoms_filter and
+// k_atoms_place do.
+#pragma once
+#include "cm_atoms32.cuh"
+
+namespace cmk {
+
+constexpr int kAgridMaxK = 6;          // fine cells per search-cell axis
+constexpr int kAgridBuckets = 8;       // each list ordered by bucket of the atom's smallest distance to the fine cell
+constexpr int kAgridBatch = 1024;      // stencil atoms staged in shared memory per round
+constexpr int kAgridBuildThreads = 256;
+
+// The fine cells of a search cell: edge vectors and bounds, FP32.
+struct FineCells {
+    int K, K3;
+    float e[9];  // column-major edge vectors of a fine cell (column k = search-cell edge k / K)
+    float h[3];  // orthogonal cells: half sides
+    float R;     // bounding-sphere radius (half the longest diagonal), rounded up
+    int ortho;
+};
+
+__device__ __forceinline__ FineCells fine_cells(const FrameGeom &G, const FrameScratch &F, int K) {
+    FineCells fc;
+    fc.K = K;
+    fc.K3 = K * K * K;
+    fc.ortho = F.ortho;
+    for (int i = 0; i < 9; ++i) fc.e[i] = (float)(G.Hn[i] / (double)K);
+    for (int k = 0; k < 3; ++k) fc.h[k] = (float)(0.5 * fabs(G.Hn[4 * k]) / (double)K) * (1.0f + 1e-6f);
+    double R = 0.0;
+    for (int m = 0; m < 4; ++m) {
+        double v[3];
+        matvec_cm(G.Hn, 1.0, (m & 1) ? -1.0 : 1.0, (m & 2) ? -1.0 : 1.0, v);
+        R = fmax(R, 0.5 * norm3d(v[0], v[1], v[2]) / (double)K);
+    }
+    fc.R = __double2float_ru(R * (1.0 + 1e-6) + 1e-6);
+    return fc;
+}
+
+// Largest distance from p to a point of the fine cell centred at c: squared
+// for orthogonal cells, the distance to the centre squared otherwise (the
+// bound is then that distance + R).
+__device__ __forceinline__ float fine_far2(const FineCells &fc, const float *c, const float4 &p) {
+    const float dx = fabsf(p.x - c[0]), dy = fabsf(p.y - c[1]), dz = fabsf(p.z - c[2]);
+    if (fc.ortho) {
+        const float vx = dx + fc.h[0], vy = dy + fc.h[1], vz = dz + fc.h[2];
+        return fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+    }
+    return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
+
+// Smallest distance from p to the fine cell, squared (orthogonal cells), or
+// the squared distance to the centre (the bound is then that distance - R).
+__device__ __forceinline__ float fine_near2(const FineCells &fc, const float *c, const float4 &p) {
+    const float dx = fabsf(p.x - c[0]), dy = fabsf(p.y - c[1]), dz = fabsf(p.z - c[2]);
+    if (fc.ortho) {
+        const float ux = fmaxf(dx - fc.h[0], 0.f), uy = fmaxf(dy - fc.h[1], 0.f), uz = fmaxf(dz - fc.h[2], 0.f);
+        return fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+    }
+    return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
+
+// Lists of the fine cells of one search cell (grid: x = search cell, y =
+// frame; one thread per fine cell, the CTA staging the cell's stencil atoms
+// in shared memory).  FILL = false writes the list lengths to gcount,
+// FILL = true the entries at gstart.  Both passes find the same threshold
+// (the same operations in the same order).
+template <bool FILL>
+__device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
+    __shared__ float4 s_at[kAgridBatch];
+    __shared__ int s_pre[kAgridMaxStencil + 1];
+    __shared__ int s_beg[kAgridMaxStencil];
+    __shared__ short s_oi[kAgridMaxStencil];
+    const int f = blockIdx.y;
+    const int c = blockIdx.x;
+    const FrameGeom &G = B.G[f];
+    const FrameScratch &F = B.FS[f];
+    if (c >= G.ncell) return;
+    const int K = B.agk, K3 = K * K * K;
+    const int t = threadIdx.x;
+    const int64_t gbase = (int64_t)f * B.gs + (int64_t)c * K3 * kAgridBuckets;  // bucket counts / starts
+    const int64_t ebase = (int64_t)f * B.gfs + (int64_t)c * K3;                  // fine-cell bucket edges
+    const bool active = F.agrid && B.anear[(int64_t)f * B.as + c];
+    if (!active) {
+        // no solute atom within a stencil of this cell: empty lists
+        if (!FILL) {
+            for (int g = t; g < K3 * kAgridBuckets; g += blockDim.x) B.gcount[gbase + g] = 0;
+            for (int g = t; g < K3; g += blockDim.x) B.gedge[ebase + g] = make_float2(0.f, 0.f);
+        }
+        return;
+    }
+    const int La0 = F.La[0], La1 = F.La[1], La2 = F.La[2];
+    const int nx = 2 * La0 + 1, ny = 2 * La1 + 1, nst = nx * ny * (2 * La2 + 1);
+    const int cx = c % G.n[0], cy = (c / G.n[0]) % G.n[1], cz = c / (G.n[0] * G.n[1]);
+    const int *cs = B.astart + (int64_t)f * B.as;  // solute molecule 0
+    for (int i = t; i < nst; i += blockDim.x) {
+        const int dx = i % nx - La0, dy = (i / nx) % ny - La1, dz = i / (nx * ny) - La2;
+        const int cell = (wrap_cell(cz + dz, G.n[2]) * G.n[1] + wrap_cell(cy + dy, G.n[1])) * G.n[0] +
+                         wrap_cell(cx + dx, G.n[0]);
+        s_beg[i] = cs[cell];
+        s_pre[i] = cs[cell + 1] - cs[cell];
+        s_oi[i] = (short)off_index(dx, dy, dz);
+    }
+    __syncthreads();
+    if (t < 32) {
+        // exclusive scan of the stencil cells' atom counts
+        int run = 0;
+        for (int i0 = 0; i0 < nst; i0 += 32) {
+            const int i = i0 + t;
+            const int v = i < nst ? s_pre[i] : 0;
+            int incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (t >= o) incl += u;
+            }
+            if (i < nst) s_pre[i] = run + incl - v;
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (t == 0) s_pre[nst] = run;
+    }
+    __syncthreads();
+    const int N = s_pre[nst];
+    const float4 *aq = B.asq32 + (int64_t)f * B.Ns;
+    const float4 *off = B.off32 + (int64_t)f * kOffEntries;
+    // atoms [k0, k0 + nb) of the stencil, positions from this cell's origin
+    auto stage = [&](int k0) {
+        const int nb = min(kAgridBatch, N - k0);
+        for (int k = t; k < nb; k += blockDim.x) {
+            const int kk = k0 + k;
+            int lo = 0, hi = nst - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_pre[mid] <= kk) lo = mid;
+                else hi = mid - 1;
+            }
+            const float4 q = aq[s_beg[lo] + (kk - s_pre[lo])];
+            const float4 o = off[s_oi[lo]];
+            s_at[k] = make_float4(q.x + o.x, q.y + o.y, q.z + o.z, q.w);
+        }
+        return nb;
+    };
+    const FineCells fc = fine_cells(G, F, K);
+    const bool mine = t < K3;
+    float cen[3] = {0.f, 0.f, 0.f};
+    if (mine) {
+        const float u0 = ((float)(t % K) + 0.5f), u1 = ((float)((t / K) % K) + 0.5f), u2 = ((float)(t / (K * K)) + 0.5f);
+        for (int r = 0; r < 3; ++r) cen[r] = fmaf(fc.e[6 + r], u2, fmaf(fc.e[3 + r], u1, fc.e[r] * u0));
+    }
+    const float cut = (float)S.cut;
+    const float margin = F.g.two_delta + 1e-3f * (1.0f + cut);
+    float L = 0.f, T = 0.f;
+    if (!FILL) {
+        // pass 1: an upper bound of the nearest atom's distance over the fine
+        // cell, and the smallest distance of any atom to it
+        float far = INFINITY, near = INFINITY;
+        for (int k0 = 0; k0 < N; k0 += kAgridBatch) {
+            __syncthreads();
+            const int nb = stage(k0);
+            __syncthreads();
+            if (mine)
+                for (int k = 0; k < nb; ++k) {
+                    const float4 p = s_at[k];
+                    far = fminf(far, fine_far2(fc, cen, p));
+                    near = fminf(near, fine_near2(fc, cen, p));
+                }
+        }
+        T = fminf(fc.ortho ? sqrtf(far) : sqrtf(far) + fc.R, cut) + margin;
+        L = fc.ortho ? sqrtf(near) : fmaxf(sqrtf(near) - fc.R, 0.f);
+        if (mine) B.gedge[ebase + t] = make_float2(L, T);
+    } else if (mine) {
+        const float2 e = B.gedge[ebase + t];
+        L = e.x;
+        T = e.y;
+    }
+    const float lim2 = fc.ortho ? T * T : (T + fc.R) * (T + fc.R);
+    const float inv = T > L ? (float)kAgridBuckets / (T - L) : 0.f;
+    // pass 2: the atoms whose smallest distance to the fine cell is within T,
+    // by bucket of that distance; the fill pass bounds every write by the
+    // next bucket's start (the count pass found the same buckets)
+    int pos[kAgridBuckets], end[kAgridBuckets];
+#pragma unroll
+    for (int b = 0; b < kAgridBuckets; ++b) {
+        pos[b] = FILL && mine ? B.gstart[gbase + (int64_t)t * kAgridBuckets + b] : 0;
+        end[b] = FILL && mine ? B.gstart[gbase + (int64_t)t * kAgridBuckets + b + 1] : 0;
+    }
+    float4 *ent = FILL ? B.gent + (int64_t)f * B.gcap : nullptr;
+    for (int k0 = 0; k0 < N; k0 += kAgridBatch) {
+        int nb = min(kAgridBatch, N - k0);
+        if (FILL || N > kAgridBatch) {
+            __syncthreads();
+            nb = stage(k0);
+            __syncthreads();
+        }
+        if (mine)
+            for (int k = 0; k < nb; ++k) {
+                const float4 p = s_at[k];
+                const float d2 = fine_near2(fc, cen, p);
+                if (d2 <= lim2) {
+                    const float dmin = fc.ortho ? sqrtf(d2) : fmaxf(sqrtf(d2) - fc.R, 0.f);
+                    const int bk = min(kAgridBuckets - 1, max(0, (int)((dmin - L) * inv)));
+#pragma unroll
+                    for (int b = 0; b < kAgridBuckets; ++b)
+                        if (bk == b) {
+                            if (FILL && pos[b] < end[b]) ent[pos[b]] = p;
+                            ++pos[b];
+                        }
+                }
+            }
+    }
+    if (!FILL && mine)
+#pragma unroll
+        for (int b = 0; b < kAgridBuckets; ++b) B.gcount[gbase + (int64_t)t * kAgridBuckets + b] = pos[b];
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(kAgridBuildThreads) k_agrid_build(DevSys S, Bufs B) {
+    k_agrid_build_body<FILL>(blockIdx, gridDim, S, B);
+}
+
+// Per-frame exclusive scan of the list lengths (one CTA of 1024 threads per
+// frame) into gstart[0 .. n]; a frame whose entries exceed gcap loses its
+// grid (its molecule pairs take the walk path).
+__device__ __forceinline__ void k_agrid_scan_body(const uint3 blockIdx, const dim3 gridDim, Bufs B) {
+    const int f = blockIdx.x;
+    const int64_t base = (int64_t)f * B.gs;
+    const int *count = B.gcount + base;
+    int *start = B.gstart + base;
+    const int K = B.agk;
+    const int n = B.G[f].ncell * K * K * K * kAgridBuckets;
+    const int t = threadIdx.x;
+    const int per = (n + 1023) / 1024;
+    const int lo = t * per, hi = min(n, lo + per);
+    long long local = 0;
+    for (int i = lo; i < hi; ++i) local += count[i];
+    const int lane = t & 31, w = t >> 5;
+    long long v = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    __shared__ long long wtot[32];
+    if (lane == 31) wtot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        long long s = wtot[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        wtot[lane] = s;
+    }
+    __syncthreads();
+    const long long total = wtot[31];
+    if (total > B.gcap) {
+        if (t == 0) B.FS[f].agrid = 0;
+        return;
+    }
+    int excl = (int)(v - local + (w > 0 ? wtot[w - 1] : 0));
+    for (int i = lo; i < hi; ++i) {
+        start[i] = excl;
+        excl += count[i];
+    }
+    if (t == 0) start[n] = (int)total;
+}
+
+__global__ void __launch_bounds__(1024) k_agrid_scan(Bufs B) {
+    k_agrid_scan_body(blockIdx, gridDim, B);
+}
+
+// One site's query: its fine cell from its FP32 position q in search cell
+// (cx, cy, cz), then the top-2 update over the list (p1 holds the solute atom
+// index in the molecule), bucket by bucket of the entries' smallest distance to
+// the fine cell.  A bucket whose smallest distance exceeds the running minimum
+// (for the reference site, also its own minimum) by more than `band` holds no
+// atom that can be the minimum, be within the guard band of it or lower the
+// reference row, and neither do the buckets after it.
+__device__ __forceinline__ void agrid_query(const Bufs &B, const FrameGeom &G, const FrameScratch &F, int f, int packed,
+                                            float4 q, int b, bool isref, float band, Top2 &T, long long &evals) {
+    const int K = B.agk;
+    const int cx = packed & 1023, cy = (packed >> 10) & 1023, cz = packed >> 20;
+    int gi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float u = fmaf(F.hin[3 * k + 2], q.z, fmaf(F.hin[3 * k + 1], q.y, F.hin[3 * k] * q.x));
+        gi[k] = min(max((int)floorf(u * (float)K), 0), K - 1);
+    }
+    const int64_t fine = (int64_t)((cz * G.n[1] + cy) * G.n[0] + cx) * (K * K * K) + (gi[2] * K + gi[1]) * K + gi[0];
+    const float2 edge = B.gedge[(int64_t)f * B.gfs + fine];
+    const int *st = B.gstart + (int64_t)f * B.gs + fine * kAgridBuckets;
+    const float w = (edge.y - edge.x) * (1.0f / (float)kAgridBuckets);
+    const float4 *e = B.gent + (int64_t)f * B.gcap;
+    int i = st[0];
+#pragma unroll 1
+    for (int k = 0; k < kAgridBuckets; ++k) {
+        const float thr = fmaxf(sqrtf(T.m1), isref ? sqrtf(T.r1) : 0.f) + band;
+        if (fmaf(w, (float)k, edge.x) > thr) break;
+        const int end = st[k + 1];
+        evals += end - i;
+        for (; i < end; ++i) {
+            const float4 a = e[i];
+            const float ex = a.x - q.x, ey = a.y - q.y, ez = a.z - q.z;
+            const float d2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+            T.m2 = fminf(T.m2, fmaxf(T.m1, d2));
+            const bool lt = d2 < T.m1;
+            T.p1 = lt ? __float_as_int(a.w) : T.p1;
+            T.b1 = lt ? b : T.b1;
+            T.m1 = fminf(T.m1, d2);
+            if (isref) T.r1 = fminf(T.r1, d2);
+        }
+    }
+}
+
+// The record of a query's top-2 when every value is farther than the band
+// from its decision boundary (the unambiguous branch of atoms_decide):
+// 0 = no record within the cutoff, 1 = record r, 2 = inside the band (the
+// pair goes to k_atoms_eval).
+__device__ __forceinline__ int agrid_decide(const DevSys &S, const Guard &g, const Top2 &T, int64_t vb, DirRec &r) {
+    r = dir_none(S);
+    if (!(T.m1 <= g.cutp2)) return 0;
+    const float d1 = sqrtf(T.m1);
+    if (T.m1 >= g.cutm2 || (sqrtf(T.m2) - d1) <= g.two_delta) return 2;
+    const int bin = bin_of(g, d1);
+    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) return 2;
+    r.within = 1;
+    r.i_local = T.p1;
+    r.j = vb + T.b1;
+    r.bin = bin;
+    r.bulk = S.usecutoff ? (d1 > g.dbulk_hi) : 0;
+    if (T.r1 <= g.cutp2) {
+        const int rb = T.r1 < g.cutm2 ? bin_of(g, sqrtf(T.r1)) : -1;
+        if (rb < 0) return 2;
+        r.ref = 1;
+        r.rbin = rb;
+    }
+    return 1;
+}
+
+// Real pass of a single solute molecule, one thread per (frame, solvent
+// molecule), persistent grid; frames without a grid queue their near pairs
+// for k_atoms_eval (k_atoms_filter's rule).
+__device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    shist_zero(S, hbase);
+    __syncthreads();
+    const SHist h = shist_bind(S, hbase);
+    LocalStats st;
+    const int apv = S.apv, iref = S.iref;
+    const int64_t n = (int64_t)B.nf * S.mv;
+    for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n; it += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(it / S.mv), v = (int)(it - (int64_t)f * S.mv);
+        const FrameScratch &F = B.FS[f];
+        const FrameGeom &G = B.G[f];
+        const int *vc = B.avcell + (int64_t)f * B.Nv + (int64_t)v * apv;
+        if (!F.agrid) {
+            if (!F.ok) {
+                raise_err(S, ERR_STENCIL);
+                continue;
+            }
+            if (atoms_near(B, G, f, 0, vc, apv)) atoms_push(S, B, make_int4(v, 0, f, 0));
+            continue;
+        }
+        const float4 *vq = B.avq32 + (int64_t)f * B.Nv + (int64_t)v * apv;
+        Top2 T;
+        top2_init(T);
+        long long ev = 0;
+        const float band = F.g.two_delta + 1e-3f * (1.0f + (float)S.cut);
+        for (int b = 0; b < apv; ++b) agrid_query(B, G, F, f, vc[b], vq[b], b, b == iref, band, T, ev);
+        if (ev == 0) continue;
+        st.atompairs += (unsigned long long)ev;
+        DirRec r;
+        const int res = agrid_decide(S, F.g, T, (int64_t)v * apv, r);
+        if (res == 2) {
+            atoms_push(S, B, make_int4(v, 0, f, 0));
+            continue;
+        }
+        st.molpairs++;
+        if (res == 1) {
+            apply_hit(S, h, false, r.bin, r.i_local, r.j, r.ref, r.rbin);
+            st.hits++;
+            if (B.slot) {
+                const int sl = B.slot[(int64_t)f * B.ms];
+                if (sl >= 0) B.flags[((int64_t)f * B.ndist + sl) * S.mv + v] = flag_code(r);
+            }
+        }
+    }
+    stats_flush(S, st, false);
+    __syncthreads();
+    shist_flush(S, h, false);
+}
+
+__global__ void __launch_bounds__(256) k_agrid_real(DevSys S, Bufs B) {
+    k_agrid_real_body(blockIdx, gridDim, S, B);
+}
+
+// Random insertion of a single solute molecule: one thread per slot of the
+// samples sample0 .. sample0 + ny - 1, persistent grid.  The slot is drawn and
+// placed as k_atoms_place does (the same helpers); with a grid its sites are
+// queried at once and only a record inside the band is written out and
+// queued; frames without a grid write and queue every near slot.
+__device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0, int ny) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int *hbase = (unsigned int *)smem_raw;
+    shist_zero(S, hbase);
+    __syncthreads();
+    const SHist h = shist_bind(S, hbase);
+    LocalStats st;
+    const int apv = S.apv, iref = S.iref;
+    const int64_t n = (int64_t)ny * S.mv;
+    for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n; it += (int64_t)gridDim.x * blockDim.x) {
+        const int y = (int)(it / S.mv), k = (int)(it - (int64_t)y * S.mv);
+        const Sample sm = B.samples[sample0 + y];
+        const int f = sm.pad;
+        const FrameGeom &G = B.G[f];
+        const FrameScratch &F = B.FS[f];
+        const int64_t base = (int64_t)y * B.Nv + (int64_t)k * apv;
+        if (S.self && k == sm.s) continue;
+        const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
+                                           B.nbulk + (int64_t)f * B.ndist);
+        int c0[3];
+        double q0[3];
+        bin_fractional(G, P.fc, c0, q0);
+        const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
+        if (!placed_maybe_near(G, F, nm, P.fc, c0, B.rc[(int64_t)f * B.mv + P.jmol])) continue;
+        uint64_t rs = P.st;
+        double A[9];
+        draw_rotation(rs, A);
+        const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
+        const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * apv;
+        bool queue;
+        if (F.agrid) {
+            Top2 T;
+            top2_init(T);
+            long long ev = 0;
+            const float band = F.g.two_delta + 1e-3f * (1.0f + (float)S.cut);
+            for (int b = 0; b < apv; ++b) {
+                int c[3];
+                double q[3];
+                placed_atom(G, F, off64, A, u[b], c0, q0, P.fc, c, q);
+                agrid_query(B, G, F, f, pack_cell(c), make_float4((float)q[0], (float)q[1], (float)q[2], 0.f), b,
+                            b == iref, band, T, ev);
+            }
+            if (ev == 0) continue;
+            st.atompairs += (unsigned long long)ev;
+            DirRec r;
+            const int res = agrid_decide(S, F.g, T, (int64_t)k * apv, r);
+            queue = res == 2;
+            if (!queue) {
+                st.molpairs++;
+                if (res == 1) {
+                    apply_hit(S, h, true, r.bin, r.i_local, r.j, r.ref, r.rbin);
+                    st.hits++;
+                }
+            }
+        } else {
+            // the walk path: queue the slot if one of its atoms lies in a near cell
+            queue = false;
+            for (int b = 0; b < apv && !queue; ++b) {
+                int c[3];
+                double q[3];
+                placed_atom(G, F, off64, A, u[b], c0, q0, P.fc, c, q);
+                queue = nm[(c[2] * G.n[1] + c[1]) * G.n[0] + c[0]] != 0;
+            }
+        }
+        if (queue) {
+            placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
+            atoms_push(S, B, make_int4(k, y, sample0 + y, 1));
+        }
+    }
+    stats_flush(S, st, true);
+    __syncthreads();
+    shist_flush(S, h, true);
+}
+
+__global__ void __launch_bounds__(256) k_agrid_random(DevSys S, Bufs B, int sample0, int ny) {
+    k_agrid_random_body(blockIdx, gridDim, S, B, sample0, ny);
+}
+
+}  // namespace cmk

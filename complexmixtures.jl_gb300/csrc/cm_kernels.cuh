@@ -47,6 +47,7 @@ constexpr int kMaxSmallMol = 32;  // PAIRS regime: atoms per molecule on either 
 constexpr int kWarps = 8;         // warps per CTA of the PAIRS real-pass kernels
 constexpr int kQueue = 64;        // per-warp candidate queue
 constexpr int kTileCells = 128;   // half-stencil cells the tiled real pass stages per home cell
+constexpr int kAgridMaxStencil = 343;  // ATOMS stencil cells the candidate-grid build stages (half-widths up to 3)
 
 enum : int { ERR_STENCIL = 1, ERR_BIN = 2, ERR_QUEUE = 4, ERR_SIZE = 8 };
 enum : int {
@@ -117,6 +118,7 @@ struct FrameScratch {
     int La[3];      // ATOMS stencil half-widths
     float xmax;     // largest |coordinate component| of the frame's input atoms (rounded up)
     int tile;       // self mode, one image per pair, half stencil within kTileCells: the tiled real pass takes the frame
+    int agrid;      // ATOMS, one solute molecule: the frame's candidate grid is complete (k_agrid_scan clears it on overflow)
     Guard g;        // FP32 search
     Guard64 g64;    // FP64 search
 };
@@ -400,6 +402,17 @@ struct Bufs {
     unsigned char *anear;           // [nf][as] cells within a stencil of a solute molecule's atoms
     int4 *aq;                       // ATOMS work queue; count in counters[2]
     int aq_cap;
+    // ATOMS candidate grid (one solute molecule, FP32 search): each search
+    // cell split into agk^3 fine cells, each with the list of solute atoms
+    // that can be the closest (or within the guard band of it) to a point of
+    // the fine cell; agk = 0: no grid
+    int agk;
+    int64_t gs;                     // per-frame stride of gcount / gstart (ncell_cap * agk^3 * buckets + 1)
+    int64_t gfs;                    // per-frame stride of gedge (ncell_cap * agk^3)
+    int64_t gcap;                   // entries per frame
+    int *gcount, *gstart;           // [nf][gs]: entries per (fine cell, bucket) and their starts
+    float2 *gedge;                  // [nf][gfs]: smallest distance of a listed atom to the fine cell, list threshold
+    float4 *gent;                   // [nf][gcap]: position from the fine cell's search-cell origin, solute atom index
 };
 
 // ------------------------------------------------------------ exact distances
@@ -855,7 +868,7 @@ __device__ bool stencil(const FrameGeom &G, double range, int *L) {
 
 // ------------------------------------------------------------------- kernels
 // Per-frame offset tables: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
-__global__ void k_offtable(Bufs B) {
+__device__ __forceinline__ void k_offtable_body(const uint3 blockIdx, const dim3 gridDim, Bufs B) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y;
     if (i >= kOffEntries) return;
     const int dx = i % kLTW - kLT, dy = (i / kLTW) % kLTW - kLT, dz = i / (kLTW * kLTW) - kLT;
@@ -863,6 +876,10 @@ __global__ void k_offtable(Bufs B) {
     matvec_cm(B.G[f].Hn, (double)dx, (double)dy, (double)dz, v);
     B.off64[(int64_t)f * kOffEntries + i] = make_d4(v[0], v[1], v[2], 0.0);
     B.off32[(int64_t)f * kOffEntries + i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+}
+
+__global__ void k_offtable(Bufs B) {
+    k_offtable_body(blockIdx, gridDim, B);
 }
 
 template <typename T>
@@ -952,7 +969,7 @@ __global__ void k_prep_pairs(Bufs B, const T *__restrict__ xyz, int64_t xyz_stri
 // threads per frame): start[0..n] and a copy in fill for the scatter.  n is
 // the frame's cell count times `mult` (1: molecule cells, ms: per-molecule
 // atom cells).
-__global__ void __launch_bounds__(1024) k_scan(Bufs B, int atoms_layout) {
+__device__ __forceinline__ void k_scan_body(const uint3 blockIdx, const dim3 gridDim, Bufs B, int atoms_layout) {
     __shared__ int wsum[32];
     const int f = blockIdx.x;
     const int64_t stride = atoms_layout ? B.as : B.cs;
@@ -990,6 +1007,10 @@ __global__ void __launch_bounds__(1024) k_scan(Bufs B, int atoms_layout) {
     }
     if (hi == n && lo < hi) start[n] = excl;
     if (n == 0 && t == 0) start[0] = 0;
+}
+
+__global__ void __launch_bounds__(1024) k_scan(Bufs B, int atoms_layout) {
+    k_scan_body(blockIdx, gridDim, B, atoms_layout);
 }
 
 __global__ void k_scatter_mols(Bufs B, int self) {
@@ -1244,7 +1265,7 @@ __global__ void k_queue_check(Bufs B, unsigned long long *__restrict__ hist, con
 // ascending (src/mddf.jl:406-415); one CTA per (frame, sampled molecule) entry
 // of `tab` = (frame, distinct index, solute molecule).  Clears the molecule's
 // entry of the slot table when done (it was set by k_frame_consts).
-__global__ void __launch_bounds__(1024) k_bulk(const DevSys S, Bufs B, const int4 *__restrict__ tab) {
+__device__ __forceinline__ void k_bulk_body(const uint3 blockIdx, const dim3 gridDim, const DevSys S, Bufs B, const int4 *__restrict__ tab) {
     __shared__ int wsum[32];
     __shared__ int carry;
     const int4 e = tab[blockIdx.x];
@@ -1283,6 +1304,10 @@ __global__ void __launch_bounds__(1024) k_bulk(const DevSys S, Bufs B, const int
         B.nbulk[(int64_t)f * B.ndist + d] = carry;
         B.slot[(int64_t)f * B.ms + s] = -1;
     }
+}
+
+__global__ void __launch_bounds__(1024) k_bulk(const DevSys S, Bufs B, const int4 *__restrict__ tab) {
+    k_bulk_body(blockIdx, gridDim, S, B, tab);
 }
 
 // Draws of one placement slot, in stream order: bulk pick, centre, angles.
@@ -1458,7 +1483,7 @@ __global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
 //   eps = u64 (512 + 4 (apv + aps in the molecule layout)) M
 // of the real distance.  The FP32 band is delta + eps; the FP64 search uses
 // eps as its band, so both decide every count from the exact distance.
-__global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
+__device__ __forceinline__ void k_frame_consts_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int pairs) {
     const int f = blockIdx.x;
     const FrameGeom &G = B.G[f];
     FrameScratch &F = B.FS[f];
@@ -1502,6 +1527,7 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
         const int K = (L[0] + 1) + (2 * L[0] + 1) * L[1] + (2 * L[0] + 1) * (2 * L[1] + 1) * L[2];
         F.tile = (pairs && S.self && multi == 0 && K <= kTileCells && S.mv < (1 << 24)) ? 1 : 0;
         F.ok = ok ? 1 : 0;
+        F.agrid = (!pairs && B.agk > 0 && ok && (2 * La[0] + 1) * (2 * La[1] + 1) * (2 * La[2] + 1) <= kAgridMaxStencil) ? 1 : 0;
     }
     __syncthreads();
     if (lane < 16) {
@@ -1562,6 +1588,10 @@ __global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
     F.g64 = g64;
 }
 
+__global__ void k_frame_consts(DevSys S, Bufs B, int pairs) {
+    k_frame_consts_body(blockIdx, gridDim, S, B, pairs);
+}
+
 // Molecule-centred data for random insertion (src/rigid_body.jl:127-134):
 // the molecule made whole around its reference atom, relative to its mean.
 template <typename T>
@@ -1603,7 +1633,7 @@ __device__ __forceinline__ int pack_cell(const int *c) { return c[0] | (c[1] << 
 // Solvent atoms binned individually (grid y = frame); molecule-centred data
 // for random insertion.
 template <typename T>
-__global__ void k_prep_atoms_solvent(Bufs B, const T *__restrict__ xyz, int64_t xyz_stride, int iref, int centroids) {
+__device__ __forceinline__ void k_prep_atoms_solvent_body(const uint3 blockIdx, const dim3 gridDim, Bufs B, const T *__restrict__ xyz, int64_t xyz_stride, int iref, int centroids) {
     const int f = blockIdx.y;
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= B.mv) return;
@@ -1633,9 +1663,14 @@ __global__ void k_prep_atoms_solvent(Bufs B, const T *__restrict__ xyz, int64_t 
     }
 }
 
+template <typename T>
+__global__ void k_prep_atoms_solvent(Bufs B, const T *__restrict__ xyz, int64_t xyz_stride, int iref, int centroids) {
+    k_prep_atoms_solvent_body<T>(blockIdx, gridDim, B, xyz, xyz_stride, iref, centroids);
+}
+
 // Solute atoms binned into per-molecule cell lists: key = s * ncell + cell.
 template <typename T>
-__global__ void k_prep_atoms_solute(Bufs B, const T *__restrict__ xyz, int64_t xyz_stride) {
+__device__ __forceinline__ void k_prep_atoms_solute_body(const uint3 blockIdx, const dim3 gridDim, Bufs B, const T *__restrict__ xyz, int64_t xyz_stride) {
     const int f = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B.Ns) return;
@@ -1656,7 +1691,12 @@ __global__ void k_prep_atoms_solute(Bufs B, const T *__restrict__ xyz, int64_t x
     warp_max_pos(&B.FS[f].xmax, __double2float_ru(fmax(fabs(x[0]), fmax(fabs(x[1]), fabs(x[2])))));
 }
 
-__global__ void k_scatter_atoms(Bufs B) {
+template <typename T>
+__global__ void k_prep_atoms_solute(Bufs B, const T *__restrict__ xyz, int64_t xyz_stride) {
+    k_prep_atoms_solute_body<T>(blockIdx, gridDim, B, xyz, xyz_stride);
+}
+
+__device__ __forceinline__ void k_scatter_atoms_body(const uint3 blockIdx, const dim3 gridDim, Bufs B) {
     const int f = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B.Ns) return;
@@ -1666,11 +1706,86 @@ __global__ void k_scatter_atoms(Bufs B) {
     B.asq64[(int64_t)f * B.Ns + p] = B.atq64[fi];
 }
 
+__global__ void k_scatter_atoms(Bufs B) {
+    k_scatter_atoms_body(blockIdx, gridDim, B);
+}
+
 // Placed solvent for the ATOMS regime: every slot of samples sample0 ..
 // sample0 + gridDim.y - 1 of the chunk, absolute FP64 positions A u + centre,
 // binned per atom; slots that can reach the solute molecule are queued for
 // k_atoms_warp (the near mask of k_atoms_near must be built).
-__global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
+// Far-slot test of a placement: every atom lies within the molecule's radius
+// rc of the centre, so its cell is in the box of cells that sphere touches;
+// false if no cell of the box is near the solute molecule (nm: its near mask),
+// and then no atom of the slot can be within the cutoff.
+__device__ __forceinline__ bool placed_maybe_near(const FrameGeom &G, const FrameScratch &F, const unsigned char *nm,
+                                                  const double *fc, const int *c0, float rc) {
+    int lo[3], hi[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float g = (float)(fc[q] * (double)G.n[q]) - (float)c0[q];  // grid units inside the cell
+        const float reach = rc / F.cw[q] + 1e-3f;
+        lo[q] = (int)floorf(g - reach);
+        hi[q] = (int)floorf(g + reach);
+    }
+    if (hi[0] - lo[0] >= G.n[0] || hi[1] - lo[1] >= G.n[1] || hi[2] - lo[2] >= G.n[2]) return true;
+    for (int dz = lo[2]; dz <= hi[2]; ++dz)
+        for (int dy = lo[1]; dy <= hi[1]; ++dy)
+            for (int dx = lo[0]; dx <= hi[0]; ++dx)
+                if (nm[(wrap_cell(c0[2] + dz, G.n[2]) * G.n[1] + wrap_cell(c0[1] + dy, G.n[1])) * G.n[0] +
+                       wrap_cell(c0[0] + dx, G.n[0])]) return true;
+    return false;
+}
+
+// Atom w (molecule-centred, FP64) of a slot rotated by A and moved to the
+// centre (cell c0, position q0 from that cell's origin; fc its fractional
+// coordinates): its cell c and its FP64 position q from that cell's origin.
+// The cell is c0 shifted by the floor of the atom's FP32 grid coordinates;
+// the FP64 offset is taken from the shifted cell's origin, so the two stay
+// consistent.
+__device__ __forceinline__ void placed_atom(const FrameGeom &G, const FrameScratch &F, const d4 *off64, const double *A,
+                                            const d4 &w, const int *c0, const double *q0, const double *fc, int *c,
+                                            double *q) {
+    double o[3];
+    matvec_rm(A, w.x, w.y, w.z, o);
+    const double t[3] = {add(q0[0], o[0]), add(q0[1], o[1]), add(q0[2], o[2])};
+    const float tx = (float)t[0], ty = (float)t[1], tz = (float)t[2];
+    int dl[3];
+    bool in_table = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        dl[k] = (int)floorf(fmaf(F.hin[3 * k + 2], tz, fmaf(F.hin[3 * k + 1], ty, F.hin[3 * k] * tx)));
+        if (dl[k] < -kLT || dl[k] > kLT) in_table = false;
+        c[k] = wrap_cell(c0[k] + dl[k], G.n[k]);
+    }
+    if (in_table) {
+        const d4 ov = off64[off_index(dl[0], dl[1], dl[2])];
+        q[0] = sub(t[0], ov.x);
+        q[1] = sub(t[1], ov.y);
+        q[2] = sub(t[2], ov.z);
+    } else {
+        // a molecule much larger than a cell: bin its absolute position
+        double cm[3];
+        matvec_cm(G.H, fc[0], fc[1], fc[2], cm);
+        bin_position(G, add(o[0], cm[0]), add(o[1], cm[1]), add(o[2], cm[2]), c, q);
+    }
+}
+
+// Every atom of a placed slot into the placement buffers at `base`.
+__device__ __forceinline__ void placed_store(const DevSys &S, const Bufs &B, const FrameGeom &G, const FrameScratch &F,
+                                             const d4 *off64, const double *A, const d4 *u, const int *c0,
+                                             const double *q0, const double *fc, int64_t base) {
+    for (int b = 0; b < S.apv; ++b) {
+        int c[3];
+        double q[3];
+        placed_atom(G, F, off64, A, u[b], c0, q0, fc, c, q);
+        B.pcell[base + b] = pack_cell(c);
+        B.pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
+        B.pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
+    }
+}
+
+__device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= S.mv) return;
     const Sample sm = B.samples[sample0 + blockIdx.y];
@@ -1681,75 +1796,24 @@ __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
         for (int b = 0; b < S.apv; ++b) B.pcell[base + b] = -1;
         return;
     }
+    const FrameScratch &F = B.FS[f];
+    // frames with a candidate grid are placed and evaluated by k_agrid_random
+    if (F.agrid) return;
     const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
                                        B.nbulk + (int64_t)f * B.ndist);
     // the new centre's cell c0 and its position q0 from that cell's origin
     int c0[3];
     double q0[3];
     bin_fractional(G, P.fc, c0, q0);
-    const FrameScratch &F = B.FS[f];
     const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
-    {
-        // far slots: every atom lies within the molecule's radius rc of the
-        // centre, so its cell is in the box of cells that sphere touches; if no
-        // cell of the box is near the solute molecule the slot is not queued,
-        // and nothing reads its atoms
-        const float rc = B.rc[(int64_t)f * B.mv + P.jmol];
-        int lo[3], hi[3];
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            const float g = (float)(P.fc[q] * (double)G.n[q]) - (float)c0[q];  // grid units inside the cell
-            const float reach = rc / F.cw[q] + 1e-3f;
-            lo[q] = (int)floorf(g - reach);
-            hi[q] = (int)floorf(g + reach);
-        }
-        bool maybe = false;
-        if (hi[0] - lo[0] >= G.n[0] || hi[1] - lo[1] >= G.n[1] || hi[2] - lo[2] >= G.n[2]) maybe = true;
-        for (int dz = lo[2]; dz <= hi[2] && !maybe; ++dz)
-            for (int dy = lo[1]; dy <= hi[1] && !maybe; ++dy)
-                for (int dx = lo[0]; dx <= hi[0] && !maybe; ++dx)
-                    maybe = nm[(wrap_cell(c0[2] + dz, G.n[2]) * G.n[1] + wrap_cell(c0[1] + dy, G.n[1])) * G.n[0] +
-                               wrap_cell(c0[0] + dx, G.n[0])] != 0;
-        if (!maybe) return;
-    }
+    // far slots are not queued, and nothing reads their atoms
+    if (!placed_maybe_near(G, F, nm, P.fc, c0, B.rc[(int64_t)f * B.mv + P.jmol])) return;
     uint64_t rs = P.st;
     double A[9];
     draw_rotation(rs, A);
     const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
     const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
-    for (int b = 0; b < S.apv; ++b) {
-        const d4 w = u[b];
-        double o[3];
-        matvec_rm(A, w.x, w.y, w.z, o);
-        // the atom from c0's origin; its cell is c0 shifted by the floor of its
-        // grid coordinates (FP32 picks the shift; the FP64 offset is taken from
-        // the shifted cell's origin, so the two stay consistent)
-        const double t[3] = {add(q0[0], o[0]), add(q0[1], o[1]), add(q0[2], o[2])};
-        const float tx = (float)t[0], ty = (float)t[1], tz = (float)t[2];
-        int dl[3], c[3];
-        bool in_table = true;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            dl[k] = (int)floorf(fmaf(F.hin[3 * k + 2], tz, fmaf(F.hin[3 * k + 1], ty, F.hin[3 * k] * tx)));
-            if (dl[k] < -kLT || dl[k] > kLT) in_table = false;
-            c[k] = wrap_cell(c0[k] + dl[k], G.n[k]);
-        }
-        double q[3];
-        if (in_table) {
-            const d4 ov = off64[off_index(dl[0], dl[1], dl[2])];
-            q[0] = sub(t[0], ov.x);
-            q[1] = sub(t[1], ov.y);
-            q[2] = sub(t[2], ov.z);
-        } else {
-            // a molecule much larger than a cell: bin its absolute position
-            double cm[3];
-            matvec_cm(G.H, P.fc[0], P.fc[1], P.fc[2], cm);
-            bin_position(G, add(o[0], cm[0]), add(o[1], cm[1]), add(o[2], cm[2]), c, q);
-        }
-        B.pcell[base + b] = pack_cell(c);
-        B.pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
-        B.pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
-    }
+    placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
     // queue the slot if one of its atoms lies in a near cell of the solute
     // molecule: (slot, placed sample, sample, 1)
     bool near = false;
@@ -1762,6 +1826,10 @@ __global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
         if (slot < B.aq_cap) B.aq[slot] = make_int4(k, (int)blockIdx.y, sample0 + (int)blockIdx.y, 1);
         else raise_err(S, ERR_QUEUE);
     }
+}
+
+__global__ void k_atoms_place(DevSys S, Bufs B, int sample0) {
+    k_atoms_place_body(blockIdx, gridDim, S, B, sample0);
 }
 
 // DCD decode (src/trajectory_formats/NamdDCD.jl:141-169): a frame of the file

@@ -25,6 +25,8 @@
 #include "../../include/cmgpu.h"
 #include "cm_kernels.cuh"
 #include "cm_atoms32.cuh"
+#include "cm_agrid.cuh"
+#include "cm_multi.cuh"
 #include "cm_flat32.cuh"
 #include "cm_final.cuh"
 #include "cm_grid3d.cuh"
@@ -211,6 +213,12 @@ struct cm_handle {
     int atoms_ctas = 0;    // resident CTAs per SM of k_atoms_eval
     bool atoms_dense = true; // ATOMS evaluation schedule: dense solutes (many atoms per occupied cell) or sparse
     int atoms_piece = 0;   // samples placed per random-insertion launch
+    // candidate grid of a single solute molecule (FP32): agk fine cells per
+    // search-cell axis (0: none), gcap entries per frame
+    DevBuf gcount, gstart, gedge, gent;
+    int agk = 0;
+    int64_t gcap = 0;
+    int agrid_real_ctas = 1, agrid_rand_ctas = 1;  // resident CTAs per SM of k_agrid_real / k_agrid_random
     // pinned host staging
     FrameGeom *h_geoms[2] = {nullptr, nullptr};
     Sample *h_samples[2] = {nullptr, nullptr};
@@ -377,6 +385,8 @@ void check_desc(const cm_system_desc *d) {
     if (d->atoms_schedule < CM_SCHED_AUTO || d->atoms_schedule > CM_SCHED_BALANCED) bad("unknown atoms_schedule");
     if (d->guard_queue_capacity < 0) bad("guard_queue_capacity must be >= 0");
     if (d->real_pass < CM_REAL_AUTO || d->real_pass > CM_REAL_TILE) bad("unknown real_pass");
+    if (d->atoms_grid < -1 || d->atoms_grid > kAgridMaxK) bad("atoms_grid must be -1, 0 or 1-" + std::to_string(kAgridMaxK));
+    if (d->atoms_grid_capacity < 0) bad("atoms_grid_capacity must be >= 0");
     if (d->solute_nmols < 1 || d->solute_natomspermol < 1 || d->solvent_nmols < 1 || d->solvent_natomspermol < 1)
         bad("selections must have at least one molecule of at least one atom");
     if (d->autocorrelation && (d->solute_nmols != d->solvent_nmols || d->solute_natomspermol != d->solvent_natomspermol))
@@ -653,6 +663,14 @@ void kernel_smem_limits(int device) {
     raise((const void *)k_pairs_guard<false>);
     raise((const void *)k_pairs_edge<true>);
     raise((const void *)k_pairs_edge<false>);
+    raise((const void *)k_agrid_real);
+    raise((const void *)k_agrid_random);
+    raise((const void *)k_multi<MK_AGRID_REAL>);
+    raise((const void *)k_multi<MK_AGRID_RANDOM>);
+    raise((const void *)k_multi<MK_EVAL_REAL_CELL>);
+    raise((const void *)k_multi<MK_EVAL_RANDOM_CELL>);
+    raise((const void *)k_multi<MK_EVAL_REAL_BALANCED>);
+    raise((const void *)k_multi<MK_EVAL_RANDOM_BALANCED>);
     for (int aps : {0, 1, 3, 4, 5, 14}) {
         raise(flat_kernel_of<true>(aps).fn);
         raise(flat_kernel_of<true>(aps).tile_fn);
@@ -713,6 +731,13 @@ void ensure_cells(cm_handle *h, int64_t ncell) {
         dev_alloc(h, h->astart, n * 4);
         dev_alloc(h, h->afill, n * 4);
         dev_alloc(h, h->anear, n);
+        if (h->agk > 0) {
+            const int64_t k3 = (int64_t)h->agk * h->agk * h->agk;
+            const size_t g = (size_t)h->fc * (ncell * k3 * kAgridBuckets + 1) * 4;
+            dev_alloc(h, h->gcount, g);
+            dev_alloc(h, h->gstart, g);
+            dev_alloc(h, h->gedge, (size_t)h->fc * ncell * k3 * sizeof(float2));
+        }
     }
 }
 
@@ -847,8 +872,35 @@ void plan(cm_handle *h, const cm_frames *f) {
     check_smem(h, hist_smem_bytes(h, h->smem_groups) + extra);
     if (h->regime == CM_REGIME_PAIRS) h->flat_ctas = flat_setup(h);
     else {
-        h->atoms_dense = h->d.atoms_schedule == CM_SCHED_AUTO ? atoms_dense(h, f) : h->d.atoms_schedule == CM_SCHED_CELL;
+        const bool dense = atoms_dense(h, f);
+        h->atoms_dense = h->d.atoms_schedule == CM_SCHED_AUTO ? dense : h->d.atoms_schedule == CM_SCHED_CELL;
         h->atoms_ctas = atoms_setup(h);
+        // candidate grid of a single solute molecule in the FP32 search (the
+        // plain FP64 path keeps the walk): by default for dense solutes, whose
+        // stencils hold many atoms per query, with fine cells of about 2.5 A.
+        // The fallback of a frame whose lists overflow queues its near pairs,
+        // so every item of a chunk must fit the queue.
+        h->agk = 0;
+        const bool fp32 = d.precision == CM_PRECISION_FP32_GUARD;
+        const bool want = d.atoms_grid > 0 || (d.atoms_grid == 0 && dense);
+        if (want && fp32 && ms == 1 && !d.autocorrelation && (int64_t)fc * mv <= h->aq_cap) {
+            int K = d.atoms_grid > 0 ? d.atoms_grid : (int)std::ceil(target_cell(h) / 2.5);
+            K = std::max(1, std::min(K, kAgridMaxK));
+            const int64_t gcap = d.atoms_grid_capacity > 0 ? (int64_t)d.atoms_grid_capacity
+                                                           : std::min<int64_t>(h->Ns * 96 + 65536, (int64_t)INT32_MAX);
+            const int64_t bytes = (int64_t)fc * gcap * 16;
+            // under an HBM budget the grid takes at most a quarter of it
+            if (d.hbm_budget_bytes <= 0 || h->device_bytes + bytes <= d.hbm_budget_bytes / 4) {
+                h->agk = K;
+                h->gcap = gcap;
+                dev_alloc(h, h->gent, (size_t)bytes);
+            }
+        }
+        if (h->agk > 0) {
+            const size_t hsm = hist_smem_bytes(h, h->smem_groups);
+            h->agrid_real_ctas = resident_ctas((const void *)k_agrid_real, 256, hsm);
+            h->agrid_rand_ctas = resident_ctas((const void *)k_agrid_random, 256, hsm);
+        }
     }
     h->planned = true;
 }
@@ -1001,6 +1053,16 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         B.anear = P<unsigned char>(h->anear);
         B.aq = P<int4>(h->aq);
         B.aq_cap = h->aq_cap;
+        B.agk = h->agk;
+        if (h->agk > 0) {
+            B.gfs = h->ncell_cap * (int64_t)h->agk * h->agk * h->agk;
+            B.gs = B.gfs * kAgridBuckets + 1;
+            B.gcap = h->gcap;
+            B.gcount = P<int>(h->gcount);
+            B.gstart = P<int>(h->gstart);
+            B.gedge = P<float2>(h->gedge);
+            B.gent = P<float4>(h->gent);
+        }
         if (h->mddf) {
             B.u64 = P<d4>(h->u64);
             B.rc = P<float>(h->rc);
@@ -1010,6 +1072,186 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         }
     }
     return B;
+}
+
+// One launch of a chain stage with its arguments, as a stand-alone kernel.
+void launch_one(int kid, dim3 g, size_t smem, cudaStream_t st, const MArgs &a) {
+    const int t = mk_threads(kid);
+    switch (kid) {
+    case MK_OFFTABLE: k_offtable<<<g, t, smem, st>>>(a.B); break;
+    case MK_PREP_SOLVENT_F32:
+        k_prep_atoms_solvent<float><<<g, t, smem, st>>>(a.B, (const float *)a.p, a.i0, a.a0, a.a1);
+        break;
+    case MK_PREP_SOLVENT_F64:
+        k_prep_atoms_solvent<double><<<g, t, smem, st>>>(a.B, (const double *)a.p, a.i0, a.a0, a.a1);
+        break;
+    case MK_PREP_SOLUTE_F32: k_prep_atoms_solute<float><<<g, t, smem, st>>>(a.B, (const float *)a.p, a.i0); break;
+    case MK_PREP_SOLUTE_F64: k_prep_atoms_solute<double><<<g, t, smem, st>>>(a.B, (const double *)a.p, a.i0); break;
+    case MK_FRAME_CONSTS: k_frame_consts<<<g, t, smem, st>>>(a.S, a.B, a.a0); break;
+    case MK_SCAN: k_scan<<<g, t, smem, st>>>(a.B, a.a0); break;
+    case MK_SCATTER_ATOMS: k_scatter_atoms<<<g, t, smem, st>>>(a.B); break;
+    case MK_ATOMS_NEAR: k_atoms_near<<<g, t, smem, st>>>(a.B); break;
+    case MK_AGRID_COUNT: k_agrid_build<false><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_AGRID_SCAN: k_agrid_scan<<<g, t, smem, st>>>(a.B); break;
+    case MK_AGRID_FILL: k_agrid_build<true><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_AGRID_REAL: k_agrid_real<<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_AGRID_RANDOM: k_agrid_random<<<g, t, smem, st>>>(a.S, a.B, a.a0, a.a1); break;
+    case MK_ATOMS_FILTER: k_atoms_filter<<<g, t, smem, st>>>(a.S, a.B, a.i0, a.i1); break;
+    case MK_ATOMS_PLACE: k_atoms_place<<<g, t, smem, st>>>(a.S, a.B, a.a0); break;
+    case MK_BULK: k_bulk<<<g, t, smem, st>>>(a.S, a.B, (const int4 *)a.p); break;
+    case MK_EVAL_REAL_CELL: k_atoms_eval<true, false, kSchedCell><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_EVAL_RANDOM_CELL: k_atoms_eval<true, true, kSchedCell><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_EVAL_REAL_BALANCED: k_atoms_eval<true, false, kSchedBalanced><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_EVAL_RANDOM_BALANCED: k_atoms_eval<true, true, kSchedBalanced><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_EVAL64_REAL_CELL: k_atoms_eval<false, false, kSchedCell><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_EVAL64_RANDOM_CELL: k_atoms_eval<false, true, kSchedCell><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_EVAL64_REAL_THREAD: k_atoms_eval<false, false, kSchedThread><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_EVAL64_RANDOM_THREAD: k_atoms_eval<false, true, kSchedThread><<<g, t, smem, st>>>(a.S, a.B); break;
+    default: throw cm_error(CM_ECUDA, "unknown chain stage");
+    }
+}
+
+// A stage of a compute chunk's chain: a zero-fill or a kernel with its grid
+// and arguments.
+struct Step {
+    int kernel = 0;  // 0: zero-fill of (zp, zbytes); 1: kernel kid
+    int kid = 0;
+    dim3 grid;
+    size_t smem = 0;
+    int cls = 0;
+    MArgs a{};
+    void *zp = nullptr;
+    size_t zbytes = 0;
+};
+
+// Where a chain goes: launched on the handle's stream (rec == nullptr), or
+// recorded for cm_batch, which launches each stage once for all its systems.
+struct Emitter {
+    cm_handle *h;
+    std::vector<Step> *rec;
+    int launches = 0;
+    void zero(void *p, size_t bytes) {
+        if (rec) {
+            Step s;
+            s.zp = p;
+            s.zbytes = bytes;
+            rec->push_back(s);
+            return;
+        }
+        CM_CUDA(cudaMemsetAsync(p, 0, bytes, h->stream));
+    }
+    void kernel(int kid, dim3 grid, size_t smem, int cls, const MArgs &a) {
+        if (rec) {
+            Step s;
+            s.kernel = 1;
+            s.kid = kid;
+            s.grid = grid;
+            s.smem = smem;
+            s.cls = cls;
+            s.a = a;
+            rec->push_back(s);
+            return;
+        }
+        kbegin(h, cls);
+        launch_one(kid, grid, smem, h->stream, a);
+        kend(h);
+        launches++;
+    }
+};
+
+// The ATOMS-layout evaluation stage of a handle (precision x schedule).
+int eval_kid(const cm_handle *h, bool random) {
+    if (h->d.precision == CM_PRECISION_FP32_GUARD)
+        return h->atoms_dense ? (random ? MK_EVAL_RANDOM_CELL : MK_EVAL_REAL_CELL)
+                              : (random ? MK_EVAL_RANDOM_BALANCED : MK_EVAL_REAL_BALANCED);
+    return h->atoms_dense ? (random ? MK_EVAL64_RANDOM_CELL : MK_EVAL64_REAL_CELL)
+                          : (random ? MK_EVAL64_RANDOM_THREAD : MK_EVAL64_REAL_THREAD);
+}
+
+// The chain of one ATOMS-layout compute chunk (solute atoms binned per
+// molecule; see cm_atoms32.cuh and cm_agrid.cuh).
+template <typename T>
+void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, const int4 *dtab, const T *xs,
+                 const T *xv, int64_t xs_stride, int64_t xv_stride, Emitter &em) {
+    const cm_system_desc &d = h->d;
+    const bool self = d.autocorrelation;
+    const int nf = c.nf;
+    const int64_t ms = d.solute_nmols, mv = d.solvent_nmols;
+    const int iref = d.irefatom - 1;
+    const bool rnd = h->mddf && c.nsmp > 0;
+    const size_t hsm = hist_smem_bytes(h, h->smem_groups);
+    const int sms = h->sms;
+    const bool f32 = sizeof(T) == 4;
+    MArgs base{};
+    base.S = S;
+    base.B = B;
+    auto args = [&](const void *p, int64_t i0, int64_t i1, int a0, int a1) {
+        MArgs a = base;
+        a.p = p;
+        a.i0 = i0;
+        a.i1 = i1;
+        a.a0 = a0;
+        a.a1 = a1;
+        return a;
+    };
+    em.zero(B.FS, sizeof(FrameScratch) * nf);
+    em.zero(B.counters, 8 * sizeof(int));
+    em.kernel(MK_OFFTABLE, dim3(grid_for(cmgeom::kOffEntries, 256), nf), 0, CM_K_PREP, base);
+    const T *xsolv = self ? xs : xv;
+    em.kernel(f32 ? MK_PREP_SOLVENT_F32 : MK_PREP_SOLVENT_F64, dim3(grid_for(mv, 128), nf), 0, CM_K_PREP,
+              args(xsolv, self ? xs_stride : xv_stride, 0, iref, h->mddf ? 1 : 0));
+    em.zero(B.acount, (size_t)nf * B.as * 4);
+    em.kernel(f32 ? MK_PREP_SOLUTE_F32 : MK_PREP_SOLUTE_F64, dim3(grid_for(h->Ns, 256), nf), 0, CM_K_PREP,
+              args(xs, xs_stride, 0, 0, 0));
+    em.kernel(MK_FRAME_CONSTS, dim3(nf), 0, CM_K_PREP, args(nullptr, 0, 0, 0, 0));
+    em.kernel(MK_SCAN, dim3(nf), 0, CM_K_CELLS, args(nullptr, 0, 0, 1, 0));
+    em.kernel(MK_SCATTER_ATOMS, dim3(grid_for(h->Ns, 256), nf), 0, CM_K_CELLS, base);
+    if (rnd) em.zero(B.flags, (size_t)nf * B.ndist * mv);
+    em.kernel(MK_ATOMS_NEAR, dim3(grid_for(ms * h->ncell_cap, 256), nf), 0, CM_K_CELLS, base);
+    // the evaluation's persistent grid: one wave, or fewer CTAs when its
+    // queue (at most `items` entries, one per warp at a time) cannot fill them
+    auto wgrid_for = [&](int64_t items) {
+        return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * h->atoms_ctas, grid_for(items, kAtomsWarps)));
+    };
+    const bool agrid = h->agk > 0;
+    auto agrid_grid = [&](int64_t n, int ctas) {
+        return (int)std::min<int64_t>(grid_for(n, 256), (int64_t)sms * ctas);
+    };
+    if (agrid) {
+        // the single solute molecule's candidate lists of every frame
+        const dim3 gb(c.ncell_max, nf);
+        em.kernel(MK_AGRID_COUNT, gb, 0, CM_K_CELLS, base);
+        em.kernel(MK_AGRID_SCAN, dim3(nf), 0, CM_K_CELLS, base);
+        em.kernel(MK_AGRID_FILL, gb, 0, CM_K_CELLS, base);
+        // real pass: every solvent molecule queried; records inside the band
+        // (and frames without a grid) go to the evaluation queue
+        em.zero(B.counters + 2, sizeof(int));
+        em.kernel(MK_AGRID_REAL, dim3(agrid_grid((int64_t)nf * mv, h->agrid_real_ctas)), hsm, CM_K_REAL, base);
+        em.kernel(eval_kid(h, false), dim3(wgrid_for((int64_t)nf * mv)), hsm, CM_K_REAL, base);
+    } else {
+        // real pass: molecule pairs that can hold a pair within the cutoff,
+        // in pieces of the queue's capacity
+        const int64_t items = (int64_t)nf * ms * mv;
+        for (int64_t i0 = 0; i0 < items; i0 += h->aq_cap) {
+            const int64_t n = std::min<int64_t>(h->aq_cap, items - i0);
+            em.zero(B.counters + 2, sizeof(int));
+            em.kernel(MK_ATOMS_FILTER, dim3(grid_for(n, 256)), 0, CM_K_REAL, args(nullptr, i0, n, 0, 0));
+            em.kernel(eval_kid(h, false), dim3(wgrid_for(n)), hsm, CM_K_REAL, base);
+        }
+    }
+    if (rnd) {
+        em.kernel(MK_BULK, dim3(c.ntab), 0, CM_K_BULK, args(dtab + c.tab0, 0, 0, 0, 0));
+        for (int s0 = 0; s0 < c.nsmp; s0 += h->atoms_piece) {
+            const int ny = std::min(h->atoms_piece, c.nsmp - s0);
+            em.zero(B.counters + 2, sizeof(int));
+            if (agrid)
+                em.kernel(MK_AGRID_RANDOM, dim3(agrid_grid((int64_t)ny * mv, h->agrid_rand_ctas)), hsm, CM_K_RANDOM,
+                          args(nullptr, 0, 0, c.smp0 + s0, ny));
+            else
+                em.kernel(MK_ATOMS_PLACE, dim3(grid_for(mv, 128), ny), 0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
+            em.kernel(eval_kid(h, true), dim3(wgrid_for((int64_t)ny * mv)), hsm, CM_K_RANDOM, base);
+        }
+    }
 }
 
 template <typename T>
@@ -1035,10 +1277,10 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
     const size_t hsm = hist_smem_bytes(h, h->smem_groups);
     const int sms = h->sms;
     int launches = 0;
-    CM_CUDA(cudaMemsetAsync(B.FS, 0, sizeof(FrameScratch) * nf, st));
-    CM_CUDA(cudaMemsetAsync(B.counters, 0, 8 * sizeof(int), st));
-    CM_LAUNCH(CM_K_PREP, k_offtable<<<dim3(grid_for(cmgeom::kOffEntries, 256), nf), 256, 0, st>>>(B));
     if (h->regime == CM_REGIME_PAIRS) {
+        CM_CUDA(cudaMemsetAsync(B.FS, 0, sizeof(FrameScratch) * nf, st));
+        CM_CUDA(cudaMemsetAsync(B.counters, 0, 8 * sizeof(int), st));
+        CM_LAUNCH(CM_K_PREP, k_offtable<<<dim3(grid_for(cmgeom::kOffEntries, 256), nf), 256, 0, st>>>(B));
         if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
         CM_CUDA(cudaMemsetAsync(B.ccount, 0, (size_t)nf * B.cs * 4, st));
         // solute molecules (in self mode they also fill the cell counts)
@@ -1107,37 +1349,9 @@ void run_chunk(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample *
             }
         }
     } else {
-        const T *xsolv = self ? xs : xv;
-        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solvent<T><<<dim3(grid_for(mv, 128), nf), 128, 0, st>>>(B, xsolv, self ? xs_stride : xv_stride, iref,
-                                                                                                 h->mddf ? 1 : 0));
-        CM_CUDA(cudaMemsetAsync(B.acount, 0, (size_t)nf * B.as * 4, st));
-        CM_LAUNCH(CM_K_PREP, k_prep_atoms_solute<T><<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B, xs, xs_stride));
-        CM_LAUNCH(CM_K_PREP, k_frame_consts<<<nf, 128, 0, st>>>(S, B, 0));
-        CM_LAUNCH(CM_K_CELLS, k_scan<<<nf, 1024, 0, st>>>(B, 1));
-        CM_LAUNCH(CM_K_CELLS, k_scatter_atoms<<<dim3(grid_for(h->Ns, 256), nf), 256, 0, st>>>(B));
-        if (rnd) CM_CUDA(cudaMemsetAsync(B.flags, 0, (size_t)nf * B.ndist * mv, st));
-        CM_LAUNCH(CM_K_CELLS, k_atoms_near<<<dim3(grid_for(ms * h->ncell_cap, 256), nf), 256, 0, st>>>(B));
-        const int wgrid = sms * h->atoms_ctas;
-        const AtomsKernels ak = atoms_kernels(h);
-        // real pass: molecule pairs that can hold a pair within the cutoff,
-        // in pieces of the queue's capacity
-        const int64_t items = (int64_t)nf * ms * mv;
-        for (int64_t i0 = 0; i0 < items; i0 += h->aq_cap) {
-            const int64_t n = std::min<int64_t>(h->aq_cap, items - i0);
-            CM_CUDA(cudaMemsetAsync(B.counters + 2, 0, sizeof(int), st));
-            CM_LAUNCH(CM_K_REAL, k_atoms_filter<<<grid_for(n, 256), 256, 0, st>>>(S, B, i0, n));
-            CM_LAUNCH(CM_K_REAL, ak.real(wgrid, hsm, st, S, B));
-        }
-        if (rnd) {
-            CM_LAUNCH(CM_K_BULK, k_bulk<<<c.ntab, 1024, 0, st>>>(S, B, dtab + c.tab0));
-            for (int s0 = 0; s0 < c.nsmp; s0 += h->atoms_piece) {
-                const int ny = std::min(h->atoms_piece, c.nsmp - s0);
-                const dim3 gp(grid_for(mv, 128), ny);
-                CM_CUDA(cudaMemsetAsync(B.counters + 2, 0, sizeof(int), st));
-                CM_LAUNCH(CM_K_RANDOM, k_atoms_place<<<gp, 128, 0, st>>>(S, B, c.smp0 + s0));
-                CM_LAUNCH(CM_K_RANDOM, ak.random(wgrid, hsm, st, S, B));
-            }
-        }
+        Emitter em{h, nullptr};
+        atoms_chain<T>(h, c, S, B, dtab, xs, xv, xs_stride, xv_stride, em);
+        launches += em.launches;
     }
     CM_CUDA(cudaGetLastError());
     h->kernels_per_frame = (launches + nf - 1) / nf;
@@ -1821,11 +2035,18 @@ int noalloc_frame(const cm_system_desc *desc, const cm_frames *f, int64_t *count
 struct cm_batch {
     std::vector<cm_handle *> hs;
     int device = 0;
+    int mode = CM_BATCH_FUSED;
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr, after = nullptr;
     std::vector<cudaEvent_t> pre, join;
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec = nullptr, gexec_fused = nullptr;
     int64_t launches = 0, instantiations = 0;
+    // fused rounds: one launch per stage for every system, from work tables
+    // staged in pinned host memory and copied to the device before the graph
+    int64_t fused_rounds = 0, stage_launches = 0, fused_systems = 0;
+    void *h_tab = nullptr, *d_tab = nullptr;
+    size_t tab_cap = 0;
+    cudaEvent_t tab_copied = nullptr;
     std::string err;
 };
 
@@ -1834,11 +2055,234 @@ namespace {
 void batch_free(cm_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->gexec_fused) cudaGraphExecDestroy(b->gexec_fused);
+    if (b->tab_copied) cudaEventDestroy(b->tab_copied);
+    if (b->h_tab) cudaFreeHost(b->h_tab);
+    if (b->d_tab) cudaFree(b->d_tab);
     for (cudaEvent_t e : b->pre) cudaEventDestroy(e);
     for (cudaEvent_t e : b->join) cudaEventDestroy(e);
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->after) cudaEventDestroy(b->after);
     if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// One fused launch of a chain stage: k_multi<kid> over every system's work-table
+// entry.
+void launch_multi(int kid, unsigned grid, size_t smem, cudaStream_t st, const MTask *t, int n, long long nb) {
+    const int th = mk_threads(kid);
+    switch (kid) {
+#define CM_MK(K)                                          \
+    case K:                                               \
+        k_multi<K><<<grid, th, smem, st>>>(t, n, nb); \
+        break;
+        CM_MK(MK_OFFTABLE)
+        CM_MK(MK_PREP_SOLVENT_F32)
+        CM_MK(MK_PREP_SOLVENT_F64)
+        CM_MK(MK_PREP_SOLUTE_F32)
+        CM_MK(MK_PREP_SOLUTE_F64)
+        CM_MK(MK_FRAME_CONSTS)
+        CM_MK(MK_SCAN)
+        CM_MK(MK_SCATTER_ATOMS)
+        CM_MK(MK_ATOMS_NEAR)
+        CM_MK(MK_AGRID_COUNT)
+        CM_MK(MK_AGRID_SCAN)
+        CM_MK(MK_AGRID_FILL)
+        CM_MK(MK_AGRID_REAL)
+        CM_MK(MK_AGRID_RANDOM)
+        CM_MK(MK_ATOMS_FILTER)
+        CM_MK(MK_ATOMS_PLACE)
+        CM_MK(MK_BULK)
+        CM_MK(MK_EVAL_REAL_CELL)
+        CM_MK(MK_EVAL_RANDOM_CELL)
+        CM_MK(MK_EVAL_REAL_BALANCED)
+        CM_MK(MK_EVAL_RANDOM_BALANCED)
+#undef CM_MK
+    default: throw cm_error(CM_ECUDA, "stage without a fused kernel");
+    }
+}
+
+// Systems whose chains a batch fuses: the ATOMS layout in FP32 (the plain FP64
+// path keeps one launch per system), stream launches without per-launch timing.
+bool fusable(const cm_handle *h) {
+    return h->regime == CM_REGIME_ATOMS && h->d.precision == CM_PRECISION_FP32_GUARD && !h->timing;
+}
+
+// The stages of one staged chunk, recorded instead of launched.
+void record_chunk(cm_handle *h, const Staged &S, const Chunk &c, std::vector<Step> &out) {
+    Emitter em{h, &out};
+    const char *xs = S.xs_base + S.sbytes * c.c0;
+    const char *xv = S.xv_base ? S.xv_base + S.vbytes * c.c0 : nullptr;
+    const int64_t ss = S.sbytes / S.elem, vs = S.vbytes / S.elem;
+    DevSys D = devsys_full(h);
+    Bufs B = chunk_bufs(h, c, S.dG, S.dS);
+    const bool self = h->d.autocorrelation;
+    B.xs_raw = xs;
+    B.xv_raw = self ? (const void *)xs : (const void *)xv;
+    B.xs_stride = ss;
+    B.xv_stride = self ? ss : vs;
+    B.raw64 = S.elem == 8 ? 1 : 0;
+    if (S.elem == 4) atoms_chain<float>(h, c, D, B, S.dT, (const float *)xs, (const float *)xv, ss, vs, em);
+    else atoms_chain<double>(h, c, D, B, S.dT, (const double *)xs, (const double *)xv, ss, vs, em);
+}
+
+// A fused staging round: every system's chunk j goes through the same chain
+// of stages, and each stage runs once for all of them (k_multi, k_multi_zero)
+// in one captured graph on the batch stream.  False (nothing launched) when
+// the systems cannot share the launches: another layout or precision, a
+// weight class change inside the round, or chains of different shapes.
+bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<char> &active) {
+    const size_t n = bt->hs.size();
+    size_t nchunks = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (!active[i]) continue;
+        cm_handle *h = bt->hs[i];
+        if (!fusable(h)) return false;
+        for (const Chunk &c : st[i].chunks)
+            if ((h->class_open && c.weight != h->class_w) || c.weight != st[i].chunks[0].weight) return false;
+        nchunks = std::max(nchunks, st[i].chunks.size());
+    }
+    // rec[j][i]: the stages of system i's chunk j
+    std::vector<std::vector<std::vector<Step>>> rec(nchunks, std::vector<std::vector<Step>>(n));
+    for (size_t j = 0; j < nchunks; ++j) {
+        const std::vector<Step> *shape = nullptr;
+        for (size_t i = 0; i < n; ++i) {
+            if (!active[i] || j >= st[i].chunks.size()) continue;
+            record_chunk(bt->hs[i], st[i], st[i].chunks[j], rec[j][i]);
+            const std::vector<Step> &r = rec[j][i];
+            if (!shape) shape = &r;
+            else {
+                if (r.size() != shape->size()) return false;
+                for (size_t k = 0; k < r.size(); ++k)
+                    if (r[k].kernel != (*shape)[k].kernel || r[k].kid != (*shape)[k].kid) return false;
+            }
+        }
+    }
+    // the work tables of the round, laid out in one pinned buffer
+    struct Launch {
+        int kernel, kid;
+        size_t off;
+        int n;
+        long long blocks;
+        size_t smem;
+    };
+    std::vector<Launch> plan;
+    std::vector<unsigned char> host;
+    auto put = [&](const void *p, size_t bytes) {
+        const size_t off = (host.size() + 255) & ~(size_t)255;
+        host.resize(off + bytes);
+        memcpy(host.data() + off, p, bytes);
+        return off;
+    };
+    for (size_t j = 0; j < nchunks; ++j) {
+        size_t nsteps = 0;
+        for (size_t i = 0; i < n; ++i) nsteps = std::max(nsteps, rec[j][i].size());
+        for (size_t k = 0; k < nsteps; ++k) {
+            Launch L{};
+            std::vector<MZero> zs;
+            std::vector<MTask> ts;
+            long long blocks = 0;
+            for (size_t i = 0; i < n; ++i) {
+                if (rec[j][i].size() <= k) continue;
+                const Step &s = rec[j][i][k];
+                L.kernel = s.kernel;
+                L.kid = s.kid;
+                if (!s.kernel) {
+                    zs.push_back({s.zp, (long long)s.zbytes});
+                } else {
+                    MTask t;
+                    t.a = s.a;
+                    t.grid = make_uint3(s.grid.x, s.grid.y, s.grid.z);
+                    t.first = blocks;
+                    blocks += (long long)s.grid.x * s.grid.y * s.grid.z;
+                    ts.push_back(t);
+                    L.smem = std::max(L.smem, s.smem);
+                }
+            }
+            if (L.kernel) {
+                L.n = (int)ts.size();
+                L.blocks = blocks;
+                L.off = put(ts.data(), ts.size() * sizeof(MTask));
+            } else {
+                L.n = (int)zs.size();
+                L.off = put(zs.data(), zs.size() * sizeof(MZero));
+            }
+            plan.push_back(L);
+        }
+    }
+    // the tables to the device, ahead of the graph on the batch stream
+    if (host.size() > bt->tab_cap) {
+        CM_CUDA(cudaStreamSynchronize(bt->stream));
+        if (bt->h_tab) cudaFreeHost(bt->h_tab);
+        if (bt->d_tab) cudaFree(bt->d_tab);
+        bt->h_tab = bt->d_tab = nullptr;
+        bt->tab_cap = 0;
+        const size_t cap = host.size() * 3 / 2 + 4096;
+        CM_CUDA(cudaMallocHost(&bt->h_tab, cap));
+        CM_CUDA(cudaMalloc(&bt->d_tab, cap));
+        bt->tab_cap = cap;
+    }
+    CM_CUDA(cudaEventSynchronize(bt->tab_copied));  // the previous round's copy has read the host table
+    memcpy(bt->h_tab, host.data(), host.size());
+    CM_CUDA(cudaMemcpyAsync(bt->d_tab, bt->h_tab, host.size(), cudaMemcpyHostToDevice, bt->stream));
+    CM_CUDA(cudaEventRecord(bt->tab_copied, bt->stream));
+    for (size_t i = 0; i < n; ++i)
+        if (active[i])
+            for (const Chunk &c : st[i].chunks) open_class(bt->hs[i], c.weight);
+    CM_CUDA(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t g = nullptr;
+    try {
+        unsigned char *base = (unsigned char *)bt->d_tab;
+        for (const Launch &L : plan) {
+            if (L.kernel && L.blocks == 0) continue;
+            if (!L.kernel) {
+                k_multi_zero<<<(unsigned)std::min(L.n, 4096), 256, 0, bt->stream>>>((const MZero *)(base + L.off), L.n);
+            } else {
+                const unsigned grid = (unsigned)std::min<long long>(L.blocks, (1LL << 31) - 1);
+                launch_multi(L.kid, grid, L.smem, bt->stream, (const MTask *)(base + L.off), L.n, L.blocks);
+            }
+            CM_CUDA(cudaGetLastError());
+        }
+    } catch (...) {
+        cudaStreamEndCapture(bt->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        throw;
+    }
+    CM_CUDA(cudaStreamEndCapture(bt->stream, &g));
+    bool updated = false;
+    if (bt->gexec_fused) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(bt->gexec_fused, g, &info) == cudaSuccess;
+        if (!updated) {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(bt->gexec_fused);
+            bt->gexec_fused = nullptr;
+        }
+    }
+    if (!updated) {
+        const cudaError_t e = cudaGraphInstantiate(&bt->gexec_fused, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            bt->gexec_fused = nullptr;
+            throw cm_error(CM_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+        bt->instantiations++;
+    }
+    cudaGraphDestroy(g);
+    CM_CUDA(cudaGraphLaunch(bt->gexec_fused, bt->stream));
+    bt->launches++;
+    bt->fused_rounds++;
+    bt->stage_launches += (int64_t)plan.size();
+    int64_t nsys = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (!active[i]) continue;
+        ++nsys;
+        cm_handle *h = bt->hs[i];
+        for (const Chunk &c : st[i].chunks) account_chunk(h, st[i], c);
+        h->launches_total += (int64_t)rec[0][i].size();
+    }
+    bt->fused_systems = nsys;
+    return true;
 }
 
 // One staging round: frames [r * max_frames, ...) of every system that has
@@ -1862,6 +2306,16 @@ void batch_round(cm_batch *bt, const cm_frames *frames, int r) {
         CM_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copied[st[i].b], 0));
         CM_CUDA(cudaEventRecord(bt->pre[i], h->stream));
         CM_CUDA(cudaStreamWaitEvent(bt->stream, bt->pre[i], 0));
+    }
+    if (bt->mode == CM_BATCH_FUSED && batch_round_fused(bt, st, active)) {
+        CM_CUDA(cudaEventRecord(bt->after, bt->stream));
+        for (size_t i = 0; i < n; ++i) {
+            if (!active[i]) continue;
+            cm_handle *h = bt->hs[i];
+            CM_CUDA(cudaStreamWaitEvent(h->stream, bt->after, 0));
+            CM_CUDA(cudaEventRecord(h->ev_done[st[i].b], h->stream));
+        }
+        return;
     }
     CM_CUDA(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
     cudaGraph_t g = nullptr;
@@ -2094,6 +2548,7 @@ int cm_batch_create(cm_handle *const *handles, int32_t nhandles, cm_batch **out)
         CM_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
         CM_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
         CM_CUDA(cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming));
+        CM_CUDA(cudaEventCreateWithFlags(&b->tab_copied, cudaEventDisableTiming));
         b->pre.assign(nhandles, nullptr);
         b->join.assign(nhandles, nullptr);
         for (int i = 0; i < nhandles; ++i) {
@@ -2130,6 +2585,24 @@ int cm_batch_submit(cm_batch *b, const cm_frames *frames) {
         }
         for (int r = 0; r < rounds; ++r) batch_round(b, frames, r);
     });
+}
+
+int cm_batch_set_mode(cm_batch *b, int32_t mode) {
+    if (!b) return CM_EINVAL;
+    if (mode != CM_BATCH_FUSED && mode != CM_BATCH_STREAMS) {
+        b->err = "unknown batch mode";
+        return CM_EINVAL;
+    }
+    b->mode = mode;
+    return CM_OK;
+}
+
+int cm_batch_fused_stats(const cm_batch *b, int64_t *fused_rounds, int64_t *stage_launches, int64_t *systems) {
+    if (!b) return CM_EINVAL;
+    if (fused_rounds) *fused_rounds = b->fused_rounds;
+    if (stage_launches) *stage_launches = b->stage_launches;
+    if (systems) *systems = b->fused_systems;
+    return CM_OK;
 }
 
 int cm_batch_graph_stats(const cm_batch *b, int64_t *graph_launches, int64_t *graph_instantiations) {
@@ -2703,12 +3176,22 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
     const int cand_pairs[] = {100, 75, 60, 50};
     const int *cand = atoms ? cand_atoms : cand_pairs;
     const bool two_real = !atoms && desc->autocorrelation && desc->precision == CM_PRECISION_FP32_GUARD;
+    // a single solute molecule in the FP32 search: the walk with both
+    // schedules at two cell sizes, and the candidate grid at several fine-cell
+    // counts (the walk schedule then only serves the records inside the band)
+    const bool grid = atoms && desc->solute_nmols == 1 && !desc->autocorrelation &&
+                      desc->precision == CM_PRECISION_FP32_GUARD && desc->atoms_grid >= 0;
+    const int cand_grid_pct[] = {100, 100, 80, 80, 100, 100, 100, 70};
+    const int cand_grid_k[] = {-1, -1, -1, -1, 3, 4, 5, 4};
     const int ncand = (atoms || two_real) ? 8 : 4;
     double best = 0.0;
     for (int c = 0; c < ncand; ++c) {
         cm_system_desc d = *desc;
-        d.cell_scale_pct = cand[c % 4];
-        d.atoms_schedule = atoms ? (c < 4 ? CM_SCHED_CELL : CM_SCHED_BALANCED) : CM_SCHED_AUTO;
+        d.cell_scale_pct = grid ? cand_grid_pct[c] : cand[c % 4];
+        d.atoms_schedule = atoms ? (grid ? (c < 4 ? (c % 2 == 0 ? CM_SCHED_CELL : CM_SCHED_BALANCED) : desc->atoms_schedule)
+                                         : (c < 4 ? CM_SCHED_CELL : CM_SCHED_BALANCED))
+                                 : CM_SCHED_AUTO;
+        if (grid) d.atoms_grid = cand_grid_k[c];
         if (!atoms) d.real_pass = two_real ? (c < 4 ? CM_REAL_TILE : CM_REAL_WARP) : desc->real_pass;
         d.kernel_timing = 1;
         d.launch = CM_LAUNCH_STREAM;
@@ -2732,14 +3215,16 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
             return st;
         }
         cm_destroy(h);
-        out->candidates[c] = cand[c % 4];
+        out->candidates[c] = d.cell_scale_pct;
         out->schedules[c] = atoms ? d.atoms_schedule : d.real_pass;
+        out->grids[c] = grid ? d.atoms_grid : 0;
         out->ms_per_frame[c] = ms / std::max(1, sample->nframes);
         if (c == 0 || out->ms_per_frame[c] < best) {
             best = out->ms_per_frame[c];
-            out->cell_scale_pct = cand[c % 4];
+            out->cell_scale_pct = d.cell_scale_pct;
             out->atoms_schedule = atoms ? d.atoms_schedule : 0;
             out->real_pass = atoms ? 0 : d.real_pass;
+            out->atoms_grid = grid ? d.atoms_grid : 0;
         }
     }
     out->ncandidates = ncand;

@@ -60,6 +60,8 @@ def system_desc(
     atoms_schedule: str = "auto",
     guard_queue_capacity: int = 0,
     real_pass: str = "auto",
+    atoms_grid: int = 0,
+    atoms_grid_capacity: int = 0,
 ):
     """cm_system_desc of a system, and the arrays it points to (keep them
     alive while the description is in use).  ``cell_scale_pct`` scales the
@@ -71,7 +73,13 @@ def system_desc(
     FP32 real pass's guard and edge queues per compute chunk: a chunk that
     overflows them is redone on the device without queues, so the counts do
     not depend on it; ``real_pass`` ("auto", "warp" or "tile") picks the FP32
-    real-pass schedule of the molecule layout (speed only)."""
+    real-pass schedule of the molecule layout (speed only); ``atoms_grid``
+    (ATOMS layout, one solute molecule, FP32) sets the fine cells per
+    search-cell axis of the per-frame candidate grid (1-6; 0 = fine cells of
+    about 2.5 A for dense solutes, the walk for sparse ones; -1 = no grid,
+    every query walks the stencil; speed only) and
+    ``atoms_grid_capacity`` its list entries per frame (0 = sized by the
+    engine; a frame whose lists do not fit walks the stencil)."""
     d = N.cm_system_desc()
     d.api_version = N.CM_API_VERSION
     d.solute_nmols = solute_nmols
@@ -120,6 +128,12 @@ def system_desc(
     if real_pass not in REAL_PASSES:
         raise ValueError(f"real_pass must be one of {sorted(REAL_PASSES)}")
     d.real_pass = REAL_PASSES[real_pass]
+    if not -1 <= int(atoms_grid) <= 6:
+        raise ValueError("atoms_grid must be -1, 0 or 1-6")
+    d.atoms_grid = int(atoms_grid)
+    if atoms_grid_capacity < 0:
+        raise ValueError("atoms_grid_capacity must be >= 0")
+    d.atoms_grid_capacity = int(atoms_grid_capacity)
     return d, keep
 
 
@@ -127,11 +141,15 @@ def autotune(solute_xyz, solvent_xyz, cells, frame_ids=None, **system) -> dict:
     """Time the candidate search-cell sizes, and with each the evaluation
     schedules (ATOMS layout: cell and balanced; self-MDDF in the molecule
     layout: home-cell tiles and warps per molecule), on sample frames
-    (cm_autotune).  Returns the fastest as {"cell_scale_pct",
-    "atoms_schedule", "real_pass"} plus "candidates", a list of the same keys
-    with "ms_per_frame"; pass the first three to Engine."""
+    (cm_autotune); a single solute molecule in the ATOMS layout (FP32) also
+    tries the candidate grid at several fine-cell counts (atoms_grid=-1 keeps
+    it out).
+    Returns the fastest as {"cell_scale_pct", "atoms_schedule", "real_pass",
+    "atoms_grid"} plus "candidates", a list of the same keys with
+    "ms_per_frame"; pass the first four to Engine."""
     lib = N.load()
-    system = {k: v for k, v in system.items() if k not in ("cell_scale_pct", "atoms_schedule", "real_pass")}
+    system = {k: v for k, v in system.items()
+              if k not in ("cell_scale_pct", "atoms_schedule", "real_pass") and not (k == "atoms_grid" and v >= 0)}
     d, keep = system_desc(**system)
     Ns = d.solute_nmols * d.solute_natomspermol
     Nv = d.solvent_nmols * d.solvent_natomspermol
@@ -142,9 +160,9 @@ def autotune(solute_xyz, solvent_xyz, cells, frame_ids=None, **system) -> dict:
     atoms = d.regime == N.CM_REGIME_ATOMS or (d.regime == N.CM_REGIME_AUTO and max(
         d.solute_natomspermol, d.solvent_natomspermol) > 32)
     out = {"cell_scale_pct": t.cell_scale_pct, "atoms_schedule": SCHEDULE_NAMES[t.atoms_schedule],
-           "real_pass": REAL_PASS_NAMES[t.real_pass], "candidates": []}
+           "real_pass": REAL_PASS_NAMES[t.real_pass], "atoms_grid": t.atoms_grid, "candidates": []}
     for i in range(t.ncandidates):
-        c = {"cell_scale_pct": t.candidates[i], "ms_per_frame": t.ms_per_frame[i]}
+        c = {"cell_scale_pct": t.candidates[i], "ms_per_frame": t.ms_per_frame[i], "atoms_grid": t.grids[i]}
         if atoms:
             c["atoms_schedule"] = SCHEDULE_NAMES[t.schedules[i]]
         else:
@@ -508,16 +526,24 @@ class Engine:
 
 class Batch:
     """Several engines whose frames run as one CUDA graph per staging round
-    (cm_batch_*): each system's kernels on its own stream, forked from and
-    joined to one capture, launched once.  Counts are those of submitting to
-    each engine alone.  Close the batch before its engines."""
+    (cm_batch_*).  ``mode`` "fused" (default): when every system is in the
+    ATOMS layout with the FP32 search, each stage of the chain is one kernel
+    launch for all systems, draining a device work table of (system, block)
+    entries; otherwise, or with "streams", each system's kernels run on its own
+    stream, forked from and joined to one capture.  Counts are those of
+    submitting to each engine alone.  Close the batch before its engines."""
 
-    def __init__(self, engines):
+    MODES = {"fused": 0, "streams": 1}
+
+    def __init__(self, engines, mode: str = "fused"):
         self._lib = N.load()
         self.engines = list(engines)
+        if mode not in self.MODES:
+            raise ValueError(f"mode must be one of {sorted(self.MODES)}")
         arr = (C.c_void_p * len(self.engines))(*[e._h.value for e in self.engines])
         self._b = C.c_void_p()
         N.raise_for(self._lib.cm_batch_create(arr, len(self.engines), C.byref(self._b)), None)
+        N.raise_for(self._lib.cm_batch_set_mode(self._b, self.MODES[mode]), None, batch=self._b)
 
     def submit(self, items) -> None:
         """``items[i]`` = (solute_xyz, solvent_xyz, cells[, frame_ids]) for
@@ -540,7 +566,10 @@ class Batch:
     def graph_stats(self) -> dict:
         a, b = C.c_int64(0), C.c_int64(0)
         N.raise_for(self._lib.cm_batch_graph_stats(self._b, C.byref(a), C.byref(b)), None, batch=self._b)
-        return {"graph_launches": a.value, "graph_instantiations": b.value}
+        r, l, n = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        N.raise_for(self._lib.cm_batch_fused_stats(self._b, C.byref(r), C.byref(l), C.byref(n)), None, batch=self._b)
+        return {"graph_launches": a.value, "graph_instantiations": b.value, "fused_rounds": r.value,
+                "stage_launches": l.value, "fused_systems": n.value}
 
     def close(self) -> None:
         if self._b:

@@ -41,7 +41,7 @@
 extern "C" {
 #endif
 
-#define CM_API_VERSION 3
+#define CM_API_VERSION 4
 
 typedef enum cm_status {
     CM_OK = 0,
@@ -134,6 +134,14 @@ typedef struct cm_system_desc {
                                          do not depend on it (a small value only exercises that path) */
     int32_t real_pass;                /* CM_REAL_*: FP32 real-pass schedule of the PAIRS layout; the counts do
                                          not depend on it */
+    int32_t atoms_grid;               /* ATOMS layout with one solute molecule, FP32 search: fine cells per
+                                         search-cell axis of the per-frame candidate grid (1-6; 0 = a grid of
+                                         fine cells of about 2.5 A for dense solutes, the stencil walk for
+                                         sparse ones; -1 = no grid, every query walks the stencil).  The
+                                         counts do not depend on it */
+    int32_t atoms_grid_capacity;      /* list entries per frame of that grid; 0 = sized by the engine.  A frame
+                                         whose lists do not fit walks the stencil instead, so the counts do
+                                         not depend on it (a small value only exercises that path) */
 } cm_system_desc;
 
 /*
@@ -276,6 +284,19 @@ typedef struct cm_batch cm_batch;
 int cm_batch_create(cm_handle *const *handles, int32_t nhandles, cm_batch **out);
 int cm_batch_submit(cm_batch *b, const cm_frames *frames);  /* frames[nhandles]; nframes 0 skips a system */
 int cm_batch_graph_stats(const cm_batch *b, int64_t *graph_launches, int64_t *graph_instantiations);
+
+/* How a staging round runs (the counts do not depend on it).  FUSED (the
+ * default): when every system of the round is in the ATOMS layout with the
+ * FP32 search and their chunks have the same chain of stages, each stage runs
+ * once for all systems -- one kernel launch drains a device work table of
+ * (system, block) entries, each entry the system's own arguments and grid --
+ * so a round is one graph of about 15 launches plus 3 per random-insertion
+ * piece whatever the number of systems; other rounds fall back to STREAMS.
+ * STREAMS: each system's chain on its own stream of the graph, as above. */
+enum { CM_BATCH_FUSED = 0, CM_BATCH_STREAMS = 1 };
+int cm_batch_set_mode(cm_batch *b, int32_t mode);
+/* Rounds run fused, their stage launches in total, and the systems of the last fused round. */
+int cm_batch_fused_stats(const cm_batch *b, int64_t *fused_rounds, int64_t *stage_launches, int64_t *systems);
 int cm_batch_destroy(cm_batch *b);
 const char *cm_batch_last_error(const cm_batch *b);
 
@@ -452,6 +473,9 @@ typedef struct cm_tuning {
     int32_t schedules[CM_TUNE_MAX];   /* each candidate's CM_SCHED_* (ATOMS layout) or CM_REAL_* (molecule
                                          layout) */
     int32_t real_pass;                /* the fastest candidate's CM_REAL_* (molecule layout; 0 otherwise) */
+    int32_t atoms_grid;               /* the fastest candidate's atoms_grid (one solute molecule in the ATOMS
+                                         layout, FP32; 0 otherwise) */
+    int32_t grids[CM_TUNE_MAX];       /* each candidate's atoms_grid */
 } cm_tuning;
 
 int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *out);

@@ -28,7 +28,7 @@ def test_library_exports_header_symbols(cm):
 def test_struct_sizes_match_header(cm):
     N = cm._native
     # field-by-field mirror of include/cmgpu.h on LP64
-    assert C.sizeof(N.cm_system_desc) == 184
+    assert C.sizeof(N.cm_system_desc) == 192
     assert C.sizeof(N.cm_frames) == 72
     assert C.sizeof(N.cm_counts) == 88
     assert C.sizeof(N.cm_raw_counts) == 64
@@ -36,7 +36,7 @@ def test_struct_sizes_match_header(cm):
     assert C.sizeof(N.cm_kernel_times) == 112
     assert C.sizeof(N.cm_server_desc) == 24
     assert C.sizeof(N.cm_request_info) == 48
-    assert C.sizeof(N.cm_tuning) == 144
+    assert C.sizeof(N.cm_tuning) == 184
     assert C.sizeof(N.cm_dcd_layout) == 64
     assert C.sizeof(N.cm_contrib_query) == 24
 

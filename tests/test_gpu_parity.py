@@ -241,12 +241,28 @@ def test_autotune_reports_candidates(cm, gpu_ready):
 
 
 def test_autotune_atoms_tries_both_schedules(cm, gpu_ready):
+    # the walk for every query (no candidate grid): both evaluation schedules
     rng = np.random.default_rng(24)
     xs, xv, cells = make_system(rng, ORTHO, 1, 120, 400, 3, 2, False, spread=3.0)
     t = cm.autotune(xs, xv, cells, solute_nmols=1, solute_natomspermol=120, solvent_nmols=400, solvent_natomspermol=3,
                     autocorrelation=False, irefatom=1, cutoff=7.0, binstep=0.02, dbulk=7.0, usecutoff=False,
-                    nbins=350, n_random_samples=4)
+                    nbins=350, n_random_samples=4, atoms_grid=-1)
     assert len(t["candidates"]) == 8
     assert {c["atoms_schedule"] for c in t["candidates"]} == {"cell", "balanced"}
     best = min(t["candidates"], key=lambda c: c["ms_per_frame"])
     assert (best["cell_scale_pct"], best["atoms_schedule"]) == (t["cell_scale_pct"], t["atoms_schedule"])
+
+
+def test_autotune_atoms_grid_subdivisions(cm, gpu_ready):
+    # one solute molecule in FP32: the walk (both schedules, two cell sizes) and the candidate grid
+    rng = np.random.default_rng(25)
+    xs, xv, cells = make_system(rng, ORTHO, 1, 120, 400, 3, 2, False, spread=3.0)
+    t = cm.autotune(xs, xv, cells, solute_nmols=1, solute_natomspermol=120, solvent_nmols=400, solvent_natomspermol=3,
+                    autocorrelation=False, irefatom=1, cutoff=7.0, binstep=0.02, dbulk=7.0, usecutoff=False,
+                    nbins=350, n_random_samples=4, precision="fp32")
+    assert len(t["candidates"]) == 8
+    assert [(c["cell_scale_pct"], c["atoms_grid"]) for c in t["candidates"]] == [
+        (100, -1), (100, -1), (80, -1), (80, -1), (100, 3), (100, 4), (100, 5), (70, 4)]
+    assert {c["atoms_schedule"] for c in t["candidates"][:4]} == {"cell", "balanced"}
+    best = min(t["candidates"], key=lambda c: c["ms_per_frame"])
+    assert (best["cell_scale_pct"], best["atoms_grid"]) == (t["cell_scale_pct"], t["atoms_grid"])
