@@ -160,22 +160,17 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
     const int N = s_pre[nst];
     const float4 *aq = B.asq32 + (int64_t)f * B.Ns;
     const float4 *off = B.off32 + (int64_t)f * kOffEntries;
-    // atoms [k0, k0 + nb) of the stencil, positions from this cell's origin
-    auto stage = [&](int k0) {
-        const int nb = min(kAgridBatch, N - k0);
-        for (int k = t; k < nb; k += blockDim.x) {
-            const int kk = k0 + k;
-            int lo = 0, hi = nst - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (s_pre[mid] <= kk) lo = mid;
-                else hi = mid - 1;
-            }
-            const float4 q = aq[s_beg[lo] + (kk - s_pre[lo])];
-            const float4 o = off[s_oi[lo]];
-            s_at[k] = make_float4(q.x + o.x, q.y + o.y, q.z + o.z, q.w);
+    // stencil atom kk: its position from this cell's origin
+    auto atom_at = [&](int kk) {
+        int lo = 0, hi = nst - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_pre[mid] <= kk) lo = mid;
+            else hi = mid - 1;
         }
-        return nb;
+        const float4 q = aq[s_beg[lo] + (kk - s_pre[lo])];
+        const float4 o = off[s_oi[lo]];
+        return make_float4(q.x + o.x, q.y + o.y, q.z + o.z, q.w);
     };
     const FineCells fc = fine_cells(G, F, K);
     const bool mine = t < K3;
@@ -184,23 +179,100 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         const float u0 = ((float)(t % K) + 0.5f), u1 = ((float)((t / K) % K) + 0.5f), u2 = ((float)(t / (K * K)) + 0.5f);
         for (int r = 0; r < 3; ++r) cen[r] = fmaf(fc.e[6 + r], u2, fmaf(fc.e[3 + r], u1, fc.e[r] * u0));
     }
+    // a lower bound of the distance from p to this search cell: its box for
+    // orthogonal cells, its bounding sphere otherwise
+    float blo[3], bhi[3], cc[3];
+    const float Rc = fc.R * (float)K;
+    for (int r = 0; r < 3; ++r) {
+        const float e = fc.e[4 * r] * (float)K;
+        blo[r] = fminf(0.f, e);
+        bhi[r] = fmaxf(0.f, e);
+        cc[r] = 0.5f * (float)K * (fc.e[r] + fc.e[3 + r] + fc.e[6 + r]);
+    }
+    auto cell_near = [&](const float4 &p) {
+        if (fc.ortho) {
+            const float dx = fmaxf(fmaxf(blo[0] - p.x, p.x - bhi[0]), 0.f);
+            const float dy = fmaxf(fmaxf(blo[1] - p.y, p.y - bhi[1]), 0.f);
+            const float dz = fmaxf(fmaxf(blo[2] - p.z, p.z - bhi[2]), 0.f);
+            return sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+        }
+        const float dx = p.x - cc[0], dy = p.y - cc[1], dz = p.z - cc[2];
+        return fmaxf(sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))) - Rc, 0.f);
+    };
+    // the next stencil atoms within `thr` of this cell, from atom `cursor` on,
+    // compacted into s_at in stencil order; returns how many
+    __shared__ int s_wsum[kAgridBuildThreads / 32];
+    __shared__ float s_tmax;
+    const int lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
+    auto stage_kept = [&](int &cursor, float thr) {
+        int n = 0;
+        while (cursor < N && n + (int)blockDim.x <= kAgridBatch) {
+            const int kk = cursor + t;
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+            bool keep = false;
+            if (kk < N) {
+                p = atom_at(kk);
+                keep = cell_near(p) <= thr;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) s_wsum[warp] = __popc(m);
+            __syncthreads();
+            int before = 0, total = 0;
+            for (int w = 0; w < nwarps; ++w) {
+                const int cw = s_wsum[w];
+                before += w < warp ? cw : 0;
+                total += cw;
+            }
+            if (keep) s_at[n + before + __popc(m & ((1u << lane) - 1u))] = p;
+            n += total;
+            cursor += blockDim.x;
+            __syncthreads();
+        }
+        return n;
+    };
+    // the largest of the fine cells' values v (non-negative), to every thread
+    auto block_max = [&](float v) {
+        if (t == 0) s_tmax = 0.f;
+        __syncthreads();
+        if (mine) atomicMax((int *)&s_tmax, __float_as_int(v));
+        __syncthreads();
+        const float r = s_tmax;
+        __syncthreads();
+        return r;
+    };
     const float cut = (float)S.cut;
-    const float margin = F.g.two_delta + 1e-3f * (1.0f + cut);
+    const float slack = 1e-3f * (1.0f + cut);
+    const float margin = F.g.two_delta + slack;
     float L = 0.f, T = 0.f;
     if (!FILL) {
+        // the search cell's own atoms first: each fine cell's bound from them
+        // limits the stencil atoms that can matter to those within the
+        // largest bound of the cell (dense solutes: a few Angstrom)
+        float far = INFINITY, near = INFINITY;
+        const int own = (La2 * ny + La1) * nx + La0;
+        const int own_beg = s_pre[own], own_n = s_pre[own + 1] - s_pre[own];
+        for (int k0 = 0; k0 < own_n; k0 += kAgridBatch) {
+            const int nb = min(kAgridBatch, own_n - k0);
+            __syncthreads();
+            for (int k = t; k < nb; k += blockDim.x) s_at[k] = atom_at(own_beg + k0 + k);
+            __syncthreads();
+            if (mine)
+                for (int k = 0; k < nb; ++k) far = fminf(far, fine_far2(fc, cen, s_at[k]));
+        }
+        const float T_own = fminf(fc.ortho ? sqrtf(far) : sqrtf(far) + fc.R, cut) + margin;
+        const float thr1 = block_max(T_own) + slack;
         // pass 1: an upper bound of the nearest atom's distance over the fine
         // cell, and the smallest distance of any atom to it
-        float far = INFINITY, near = INFINITY;
-        for (int k0 = 0; k0 < N; k0 += kAgridBatch) {
-            __syncthreads();
-            const int nb = stage(k0);
-            __syncthreads();
+        int cursor = 0;
+        while (cursor < N) {
+            const int nb = stage_kept(cursor, thr1);
             if (mine)
                 for (int k = 0; k < nb; ++k) {
                     const float4 p = s_at[k];
                     far = fminf(far, fine_far2(fc, cen, p));
                     near = fminf(near, fine_near2(fc, cen, p));
                 }
+            __syncthreads();
         }
         T = fminf(fc.ortho ? sqrtf(far) : sqrtf(far) + fc.R, cut) + margin;
         L = fc.ortho ? sqrtf(near) : fmaxf(sqrtf(near) - fc.R, 0.f);
@@ -210,11 +282,13 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         L = e.x;
         T = e.y;
     }
+    // pass 2: the atoms whose smallest distance to the fine cell is within T,
+    // by bucket of that distance; the count and fill passes stage the same
+    // atoms in the same order and find the same buckets, and the fill pass
+    // bounds every write by the next bucket's start
+    const float thr2 = block_max(mine ? T : 0.f) + slack;
     const float lim2 = fc.ortho ? T * T : (T + fc.R) * (T + fc.R);
     const float inv = T > L ? (float)kAgridBuckets / (T - L) : 0.f;
-    // pass 2: the atoms whose smallest distance to the fine cell is within T,
-    // by bucket of that distance; the fill pass bounds every write by the
-    // next bucket's start (the count pass found the same buckets)
     int pos[kAgridBuckets], end[kAgridBuckets];
 #pragma unroll
     for (int b = 0; b < kAgridBuckets; ++b) {
@@ -222,13 +296,9 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         end[b] = FILL && mine ? B.gstart[gbase + (int64_t)t * kAgridBuckets + b + 1] : 0;
     }
     float4 *ent = FILL ? B.gent + (int64_t)f * B.gcap : nullptr;
-    for (int k0 = 0; k0 < N; k0 += kAgridBatch) {
-        int nb = min(kAgridBatch, N - k0);
-        if (FILL || N > kAgridBatch) {
-            __syncthreads();
-            nb = stage(k0);
-            __syncthreads();
-        }
+    int cursor = 0;
+    while (cursor < N) {
+        const int nb = stage_kept(cursor, thr2);
         if (mine)
             for (int k = 0; k < nb; ++k) {
                 const float4 p = s_at[k];
@@ -244,6 +314,7 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
                         }
                 }
             }
+        __syncthreads();
     }
     if (!FILL && mine)
 #pragma unroll
@@ -431,11 +502,12 @@ __global__ void __launch_bounds__(256) k_agrid_real(DevSys S, Bufs B) {
     k_agrid_real_body(blockIdx, gridDim, S, B);
 }
 
-// Random insertion of a single solute molecule: one thread per slot of the
-// samples sample0 .. sample0 + ny - 1, persistent grid.  The slot is drawn and
-// placed as k_atoms_place does (the same helpers); with a grid its sites are
-// queried at once and only a record inside the band is written out and
-// queued; frames without a grid write and queue every near slot.
+// Random insertion of a single solute molecule, second pass: one thread per
+// slot of the list k_slot_filter made (slots of samples sample0 .. that can
+// reach the solute), persistent grid.  The slot is drawn and placed as
+// k_atoms_place does (the same helpers); with a grid its sites are queried at
+// once and only a record inside the band is written out and queued; frames
+// without a grid write and queue every slot with an atom in a near cell.
 __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0, int ny) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
@@ -444,22 +516,22 @@ __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const 
     const SHist h = shist_bind(S, hbase);
     LocalStats st;
     const int apv = S.apv, iref = S.iref;
-    const int64_t n = (int64_t)ny * S.mv;
-    for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n; it += (int64_t)gridDim.x * blockDim.x) {
-        const int y = (int)(it / S.mv), k = (int)(it - (int64_t)y * S.mv);
+    (void)ny;
+    const int n = min(B.counters[5], B.aslot_cap);
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
+        const int e = B.aslot[it];
+        const int y = e / S.mv, k = e - y * S.mv;
         const Sample sm = B.samples[sample0 + y];
         const int f = sm.pad;
         const FrameGeom &G = B.G[f];
         const FrameScratch &F = B.FS[f];
         const int64_t base = (int64_t)y * B.Nv + (int64_t)k * apv;
-        if (S.self && k == sm.s) continue;
         const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
                                            B.nbulk + (int64_t)f * B.ndist);
         int c0[3];
         double q0[3];
         bin_fractional(G, P.fc, c0, q0);
         const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
-        if (!placed_maybe_near(G, F, nm, P.fc, c0, B.rc[(int64_t)f * B.mv + P.jmol])) continue;
         uint64_t rs = P.st;
         double A[9];
         draw_rotation(rs, A);

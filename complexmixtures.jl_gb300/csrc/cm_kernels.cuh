@@ -402,6 +402,8 @@ struct Bufs {
     unsigned char *anear;           // [nf][as] cells within a stencil of a solute molecule's atoms
     int4 *aq;                       // ATOMS work queue; count in counters[2]
     int aq_cap;
+    int *aslot;                     // random-insertion slots that can reach the solute (y * mv + slot); count in counters[5]
+    int aslot_cap;
     // ATOMS candidate grid (one solute molecule, FP32 search): each search
     // cell split into agk^3 fine cells, each with the list of solute atoms
     // that can be the closest (or within the guard band of it) to a point of
@@ -1710,10 +1712,6 @@ __global__ void k_scatter_atoms(Bufs B) {
     k_scatter_atoms_body(blockIdx, gridDim, B);
 }
 
-// Placed solvent for the ATOMS regime: every slot of samples sample0 ..
-// sample0 + gridDim.y - 1 of the chunk, absolute FP64 positions A u + centre,
-// binned per atom; slots that can reach the solute molecule are queued for
-// k_atoms_warp (the near mask of k_atoms_near must be built).
 // Far-slot test of a placement: every atom lies within the molecule's radius
 // rc of the centre, so its cell is in the box of cells that sphere touches;
 // false if no cell of the box is near the solute molecule (nm: its near mask),
@@ -1785,46 +1783,88 @@ __device__ __forceinline__ void placed_store(const DevSys &S, const Bufs &B, con
     }
 }
 
-__device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0) {
+// Random-insertion slots of the ATOMS regime, first pass: one thread per
+// slot of samples sample0 .. sample0 + gridDim.y - 1 of the chunk.  Only the
+// slot's draws are taken (the bulk pick and the centre; integer and FP32
+// work): a slot whose molecule cannot reach a cell near its solute molecule
+// (placed_maybe_near on a box widened to cover the FP32 rounding of the
+// centre's cell) can hold no pair within the cutoff and is dropped; the others
+// go to the slot list (y * mv + slot, count in counters[5]), so that the FP64
+// placement runs on full warps.
+__device__ __forceinline__ void k_slot_filter_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= S.mv) return;
-    const Sample sm = B.samples[sample0 + blockIdx.y];
+    const int y = blockIdx.y;
+    const Sample sm = B.samples[sample0 + y];
+    if (S.self && k == sm.s) return;
     const int f = sm.pad;
     const FrameGeom &G = B.G[f];
-    const int64_t base = (int64_t)blockIdx.y * B.Nv + (int64_t)k * S.apv;
-    if (S.self && k == sm.s) {
-        for (int b = 0; b < S.apv; ++b) B.pcell[base + b] = -1;
-        return;
-    }
     const FrameScratch &F = B.FS[f];
-    // frames with a candidate grid are placed and evaluated by k_agrid_random
-    if (F.agrid) return;
     const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
                                        B.nbulk + (int64_t)f * B.ndist);
-    // the new centre's cell c0 and its position q0 from that cell's origin
-    int c0[3];
-    double q0[3];
-    bin_fractional(G, P.fc, c0, q0);
     const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
-    // far slots are not queued, and nothing reads their atoms
-    if (!placed_maybe_near(G, F, nm, P.fc, c0, B.rc[(int64_t)f * B.mv + P.jmol])) return;
-    uint64_t rs = P.st;
-    double A[9];
-    draw_rotation(rs, A);
-    const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
-    const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
-    placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
-    // queue the slot if one of its atoms lies in a near cell of the solute
-    // molecule: (slot, placed sample, sample, 1)
-    bool near = false;
-    for (int b = 0; b < S.apv && !near; ++b) {
-        const int pc = B.pcell[base + b];
-        near = nm[((pc >> 20) * G.n[1] + ((pc >> 10) & 1023)) * G.n[0] + (pc & 1023)] != 0;
+    const float rc = B.rc[(int64_t)f * B.mv + P.jmol];
+    int lo[3], hi[3];
+    bool maybe = false;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float g = (float)(P.fc[q] * (double)G.n[q]);  // grid units from the cell's origin
+        const float reach = rc / F.cw[q] + 2e-3f;
+        lo[q] = (int)floorf(g - reach);
+        hi[q] = (int)floorf(g + reach);
+        if (hi[q] - lo[q] >= G.n[q]) maybe = true;
     }
-    if (near) {
-        const int slot = atomicAdd(B.counters + 2, 1);
-        if (slot < B.aq_cap) B.aq[slot] = make_int4(k, (int)blockIdx.y, sample0 + (int)blockIdx.y, 1);
-        else raise_err(S, ERR_QUEUE);
+    for (int dz = lo[2]; dz <= hi[2] && !maybe; ++dz)
+        for (int dy = lo[1]; dy <= hi[1] && !maybe; ++dy)
+            for (int dx = lo[0]; dx <= hi[0] && !maybe; ++dx)
+                maybe = nm[(wrap_cell(dz, G.n[2]) * G.n[1] + wrap_cell(dy, G.n[1])) * G.n[0] + wrap_cell(dx, G.n[0])] != 0;
+    if (!maybe) return;
+    const int at = atomicAdd(B.counters + 5, 1);
+    if (at < B.aslot_cap) B.aslot[at] = y * S.mv + k;
+    else raise_err(S, ERR_QUEUE);
+}
+
+__global__ void k_slot_filter(DevSys S, Bufs B, int sample0) {
+    k_slot_filter_body(blockIdx, gridDim, S, B, sample0);
+}
+
+// Second pass of the walk path: the listed slots placed (FP64, the same draws),
+// written to the placement buffers, and queued for k_atoms_eval when one of
+// their atoms lies in a near cell of the solute molecule: (slot, placed
+// sample, sample, 1).  Persistent grid over the list.
+__device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0) {
+    const int n = min(B.counters[5], B.aslot_cap);
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
+        const int e = B.aslot[it];
+        const int y = e / S.mv, k = e - y * S.mv;
+        const Sample sm = B.samples[sample0 + y];
+        const int f = sm.pad;
+        const FrameGeom &G = B.G[f];
+        const FrameScratch &F = B.FS[f];
+        const int64_t base = (int64_t)y * B.Nv + (int64_t)k * S.apv;
+        const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
+                                           B.nbulk + (int64_t)f * B.ndist);
+        // the new centre's cell c0 and its position q0 from that cell's origin
+        int c0[3];
+        double q0[3];
+        bin_fractional(G, P.fc, c0, q0);
+        const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
+        uint64_t rs = P.st;
+        double A[9];
+        draw_rotation(rs, A);
+        const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
+        const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
+        placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
+        bool near = false;
+        for (int b = 0; b < S.apv && !near; ++b) {
+            const int pc = B.pcell[base + b];
+            near = nm[((pc >> 20) * G.n[1] + ((pc >> 10) & 1023)) * G.n[0] + (pc & 1023)] != 0;
+        }
+        if (near) {
+            const int slot = atomicAdd(B.counters + 2, 1);
+            if (slot < B.aq_cap) B.aq[slot] = make_int4(k, y, sample0 + y, 1);
+            else raise_err(S, ERR_QUEUE);
+        }
     }
 }
 

@@ -51,6 +51,7 @@ enum MKid : int {
     MK_AGRID_RANDOM,
     MK_ATOMS_FILTER,
     MK_ATOMS_PLACE,
+    MK_SLOT_FILTER,
     MK_BULK,
     MK_EVAL_REAL_CELL,
     MK_EVAL_RANDOM_CELL,
@@ -75,7 +76,7 @@ __host__ __device__ constexpr int mk_threads(int kid) {
          : (kid == MK_AGRID_COUNT || kid == MK_AGRID_FILL) ? kAgridBuildThreads
          : kid == MK_AGRID_SCAN ? 1024
          : (kid == MK_AGRID_REAL || kid == MK_AGRID_RANDOM || kid == MK_ATOMS_FILTER) ? 256
-         : kid == MK_ATOMS_PLACE ? 128
+         : (kid == MK_ATOMS_PLACE || kid == MK_SLOT_FILTER) ? 128
          : kid == MK_BULK ? 1024
          : kAtomsWarps * 32;
 }
@@ -100,6 +101,7 @@ __device__ __forceinline__ void mk_body(const uint3 vb, const dim3 vg, const MAr
     else if constexpr (KID == MK_AGRID_RANDOM) k_agrid_random_body(vb, vg, a.S, a.B, a.a0, a.a1);
     else if constexpr (KID == MK_ATOMS_FILTER) k_atoms_filter_body(vb, vg, a.S, a.B, a.i0, a.i1);
     else if constexpr (KID == MK_ATOMS_PLACE) k_atoms_place_body(vb, vg, a.S, a.B, a.a0);
+    else if constexpr (KID == MK_SLOT_FILTER) k_slot_filter_body(vb, vg, a.S, a.B, a.a0);
     else if constexpr (KID == MK_BULK) k_bulk_body(vb, vg, a.S, a.B, (const int4 *)a.p);
     else if constexpr (KID == MK_EVAL_REAL_CELL) k_atoms_eval_body<true, false, kSchedCell>(vb, vg, a.S, a.B);
     else if constexpr (KID == MK_EVAL_RANDOM_CELL) k_atoms_eval_body<true, true, kSchedCell>(vb, vg, a.S, a.B);

@@ -208,8 +208,9 @@ struct cm_handle {
     DevBuf g_soff, g_sidx, g_voff, g_vidx;
     // ATOMS
     DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, u64, rc, pcell, pq32, pq64,
-        anear, aq;
+        anear, aq, aslot;
     int aq_cap = 0;
+    int aslot_cap = 0;     // random-insertion slot list (slots of one placement piece)
     int atoms_ctas = 0;    // resident CTAs per SM of k_atoms_eval
     bool atoms_dense = true; // ATOMS evaluation schedule: dense solutes (many atoms per occupied cell) or sparse
     int atoms_piece = 0;   // samples placed per random-insertion launch
@@ -852,6 +853,8 @@ void plan(cm_handle *h, const cm_frames *f) {
             h->atoms_piece = (int)std::max<int64_t>(1, std::min<int64_t>(kChunkSamples, want / mv));
             const int chunk = std::min(h->atoms_piece, std::max(1, fc * d.n_random_samples));
             dev_alloc(h, h->pcell, (size_t)chunk * h->Nv * 4);
+            h->aslot_cap = (int)std::min<int64_t>((int64_t)chunk * mv, (int64_t)INT32_MAX);
+            dev_alloc(h, h->aslot, (size_t)h->aslot_cap * 4);
             dev_alloc(h, h->pq32, (size_t)chunk * h->Nv * 16);
             dev_alloc(h, h->pq64, (size_t)chunk * h->Nv * 32);
         }
@@ -1053,6 +1056,10 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         B.anear = P<unsigned char>(h->anear);
         B.aq = P<int4>(h->aq);
         B.aq_cap = h->aq_cap;
+        if (h->mddf) {
+            B.aslot = P<int>(h->aslot);
+            B.aslot_cap = h->aslot_cap;
+        }
         B.agk = h->agk;
         if (h->agk > 0) {
             B.gfs = h->ncell_cap * (int64_t)h->agk * h->agk * h->agk;
@@ -1098,6 +1105,7 @@ void launch_one(int kid, dim3 g, size_t smem, cudaStream_t st, const MArgs &a) {
     case MK_AGRID_RANDOM: k_agrid_random<<<g, t, smem, st>>>(a.S, a.B, a.a0, a.a1); break;
     case MK_ATOMS_FILTER: k_atoms_filter<<<g, t, smem, st>>>(a.S, a.B, a.i0, a.i1); break;
     case MK_ATOMS_PLACE: k_atoms_place<<<g, t, smem, st>>>(a.S, a.B, a.a0); break;
+    case MK_SLOT_FILTER: k_slot_filter<<<g, t, smem, st>>>(a.S, a.B, a.a0); break;
     case MK_BULK: k_bulk<<<g, t, smem, st>>>(a.S, a.B, (const int4 *)a.p); break;
     case MK_EVAL_REAL_CELL: k_atoms_eval<true, false, kSchedCell><<<g, t, smem, st>>>(a.S, a.B); break;
     case MK_EVAL_RANDOM_CELL: k_atoms_eval<true, true, kSchedCell><<<g, t, smem, st>>>(a.S, a.B); break;
@@ -1243,12 +1251,16 @@ void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, c
         em.kernel(MK_BULK, dim3(c.ntab), 0, CM_K_BULK, args(dtab + c.tab0, 0, 0, 0, 0));
         for (int s0 = 0; s0 < c.nsmp; s0 += h->atoms_piece) {
             const int ny = std::min(h->atoms_piece, c.nsmp - s0);
-            em.zero(B.counters + 2, sizeof(int));
+            // the evaluation queue and the slot list (counters 2 .. 5)
+            em.zero(B.counters + 2, 4 * sizeof(int));
+            // slots that can reach the solute, then their FP64 placement on full warps
+            em.kernel(MK_SLOT_FILTER, dim3(grid_for(mv, 128), ny), 0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
             if (agrid)
                 em.kernel(MK_AGRID_RANDOM, dim3(agrid_grid((int64_t)ny * mv, h->agrid_rand_ctas)), hsm, CM_K_RANDOM,
                           args(nullptr, 0, 0, c.smp0 + s0, ny));
             else
-                em.kernel(MK_ATOMS_PLACE, dim3(grid_for(mv, 128), ny), 0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
+                em.kernel(MK_ATOMS_PLACE, dim3((unsigned)std::min<int64_t>(grid_for((int64_t)ny * mv, 128), (int64_t)sms * 16)),
+                          0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
             em.kernel(eval_kid(h, true), dim3(wgrid_for((int64_t)ny * mv)), hsm, CM_K_RANDOM, base);
         }
     }
@@ -2091,6 +2103,7 @@ void launch_multi(int kid, unsigned grid, size_t smem, cudaStream_t st, const MT
         CM_MK(MK_AGRID_RANDOM)
         CM_MK(MK_ATOMS_FILTER)
         CM_MK(MK_ATOMS_PLACE)
+        CM_MK(MK_SLOT_FILTER)
         CM_MK(MK_BULK)
         CM_MK(MK_EVAL_REAL_CELL)
         CM_MK(MK_EVAL_RANDOM_CELL)
