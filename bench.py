@@ -73,6 +73,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--atoms-grid", type=int, default=0,
+                   help="ATOMS layout, one solute molecule: fine cells per search-cell axis of the candidate grid "
+                        "(0 = engine default, -1 = stencil walk; speed only)")
     p.add_argument("--real-pass", default="auto", choices=["auto", "warp", "tile"],
                    help="FP32 real-pass schedule (speed only): per-molecule warps or home-cell tiles")
     p.add_argument("--workload", default="c3", choices=["c3", "c1", "c2-water", "c2-cosolvent", "c4", "c4-batch", "c5", "grid3d"],
@@ -526,13 +529,14 @@ def other_workload(args, local):
                    value=out["graph_batch_resident_frames_per_s"])
         print(json.dumps(out), flush=True)
         return
-    print(json.dumps(atoms_leg(cm, local, args.workload, args.steps, args.warmup)), flush=True)
+    print(json.dumps(atoms_leg(cm, local, args.workload, args.steps, args.warmup, atoms_grid=args.atoms_grid)),
+          flush=True)
 
 
 _SYNTH_CACHE = {}
 
 
-def atoms_leg(cm, local, workload, steps, warmup):
+def atoms_leg(cm, local, workload, steps, warmup, atoms_grid=0):
     """Frames/s of one ATOMS-layout configuration (FP32 + guard, frames in
     HBM), with the per-class kernel times, the guard statistics and the plain
     FP64 path on the same frames; the config-4 case is its median system
@@ -562,7 +566,7 @@ def atoms_leg(cm, local, workload, steps, warmup):
     xd = torch.from_numpy(xs).to(f"cuda:{local}")
     vd = torch.from_numpy(xv).to(f"cuda:{local}")
     ids = np.arange(1, nframes + 1)
-    eng = cm.Engine(precision="fp32", kernel_timing=True, **kw)
+    eng = cm.Engine(precision="fp32", kernel_timing=True, atoms_grid=atoms_grid, **kw)
     stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=f"cuda:{local}")
     for _ in range(max(warmup, 1)):
         eng.submit(xd, vd, cells, frame_ids=ids)
@@ -597,7 +601,7 @@ def atoms_leg(cm, local, workload, steps, warmup):
         "workload": workload, "metric": "MDDF frames/s", "value": frames / (ms / 1e3), "unit": "frames/s",
         "steps": steps, "warmup": warmup, "frames_per_step": nframes,
         "atoms": {"solute": int(sysm.solute_nmols * aps), "solvent": int(sv.nmols * sv.natomspermol)},
-        "layout": "ATOMS" if st["regime"] == 2 else "PAIRS",
+        "layout": "ATOMS" if st["regime"] == 2 else "PAIRS", "atoms_grid": atoms_grid,
         "kernel_ms_per_frame": {k: v[0] / frames for k, v in kt.items()},
         "guard": {"band_A": st["guard_band"], "reevaluations": st["guard_reevaluations"],
                   "rate_per_record": st["guard_reevaluations"] / hits if hits else 0.0,

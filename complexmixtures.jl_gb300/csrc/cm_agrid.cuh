@@ -45,7 +45,8 @@ namespace cmk {
 
 constexpr int kAgridMaxK = 6;          // fine cells per search-cell axis
 constexpr int kAgridBuckets = 8;       // each list ordered by bucket of the atom's smallest distance to the fine cell
-constexpr int kAgridBatch = 1024;      // stencil atoms staged in shared memory per round
+constexpr int kAgridStage = 3072;      // stencil atoms staged in shared memory at a time (48 KB, dynamic)
+constexpr int kAgridRound = 4;         // stencil atoms each thread loads per staging round
 constexpr int kAgridBuildThreads = 256;
 
 // The fine cells of a search cell: edge vectors and bounds, FP32.
@@ -98,16 +99,22 @@ __device__ __forceinline__ float fine_near2(const FineCells &fc, const float *c,
 }
 
 // Lists of the fine cells of one search cell (grid: x = search cell, y =
-// frame; one thread per fine cell, the CTA staging the cell's stencil atoms
-// in shared memory).  FILL = false writes the list lengths to gcount,
-// FILL = true the entries at gstart.  Both passes find the same threshold
-// (the same operations in the same order).
+// frame).  The CTA stages the cell's stencil atoms in shared memory; each warp
+// takes fine cells in turn and its lanes split the staged atoms (warp
+// reductions, and ballots for the compacted writes).  FILL = false writes the
+// bucket lengths to gcount and the bucket edges to gedge, FILL = true the
+// entries at gstart: both passes stage the same atoms in the same order and
+// find the same buckets.
 template <bool FILL>
 __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
-    __shared__ float4 s_at[kAgridBatch];
+    extern __shared__ float4 s_at[];  // kAgridStage entries
     __shared__ int s_pre[kAgridMaxStencil + 1];
     __shared__ int s_beg[kAgridMaxStencil];
     __shared__ short s_oi[kAgridMaxStencil];
+    __shared__ float s_far[kAgridMaxK * kAgridMaxK * kAgridMaxK], s_near[kAgridMaxK * kAgridMaxK * kAgridMaxK];
+    __shared__ int s_pos[kAgridMaxK * kAgridMaxK * kAgridMaxK][kAgridBuckets];
+    __shared__ int s_wsum[kAgridBuildThreads / 32];
+    __shared__ float s_tmax;
     const int f = blockIdx.y;
     const int c = blockIdx.x;
     const FrameGeom &G = B.G[f];
@@ -115,6 +122,8 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
     if (c >= G.ncell) return;
     const int K = B.agk, K3 = K * K * K;
     const int t = threadIdx.x;
+    const int lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
     const int64_t gbase = (int64_t)f * B.gs + (int64_t)c * K3 * kAgridBuckets;  // bucket counts / starts
     const int64_t ebase = (int64_t)f * B.gfs + (int64_t)c * K3;                  // fine-cell bucket edges
     const bool active = F.agrid && B.anear[(int64_t)f * B.as + c];
@@ -173,12 +182,10 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         return make_float4(q.x + o.x, q.y + o.y, q.z + o.z, q.w);
     };
     const FineCells fc = fine_cells(G, F, K);
-    const bool mine = t < K3;
-    float cen[3] = {0.f, 0.f, 0.f};
-    if (mine) {
-        const float u0 = ((float)(t % K) + 0.5f), u1 = ((float)((t / K) % K) + 0.5f), u2 = ((float)(t / (K * K)) + 0.5f);
+    auto centre = [&](int g, float *cen) {
+        const float u0 = ((float)(g % K) + 0.5f), u1 = ((float)((g / K) % K) + 0.5f), u2 = ((float)(g / (K * K)) + 0.5f);
         for (int r = 0; r < 3; ++r) cen[r] = fmaf(fc.e[6 + r], u2, fmaf(fc.e[3 + r], u1, fc.e[r] * u0));
-    }
+    };
     // a lower bound of the distance from p to this search cell: its box for
     // orthogonal cells, its bounding sphere otherwise
     float blo[3], bhi[3], cc[3];
@@ -200,22 +207,28 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         return fmaxf(sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))) - Rc, 0.f);
     };
     // the next stencil atoms within `thr` of this cell, from atom `cursor` on,
-    // compacted into s_at in stencil order; returns how many
-    __shared__ int s_wsum[kAgridBuildThreads / 32];
-    __shared__ float s_tmax;
-    const int lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
+    // compacted into s_at in stencil order (kAgridRound atoms per thread and
+    // two barriers per round); returns how many
     auto stage_kept = [&](int &cursor, float thr) {
         int n = 0;
-        while (cursor < N && n + (int)blockDim.x <= kAgridBatch) {
-            const int kk = cursor + t;
-            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-            bool keep = false;
-            if (kk < N) {
-                p = atom_at(kk);
-                keep = cell_near(p) <= thr;
+        const int round = kAgridRound * (int)blockDim.x;
+        while (cursor < N && n + round <= kAgridStage) {
+            float4 p[kAgridRound];
+            unsigned m[kAgridRound];
+            int mine_n = 0;
+#pragma unroll
+            for (int j = 0; j < kAgridRound; ++j) {
+                const int kk = cursor + j * (int)blockDim.x + t;
+                bool keep = false;
+                p[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (kk < N) {
+                    p[j] = atom_at(kk);
+                    keep = cell_near(p[j]) <= thr;
+                }
+                m[j] = __ballot_sync(0xffffffffu, keep);
+                mine_n += __popc(m[j]);
             }
-            const unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (lane == 0) s_wsum[warp] = __popc(m);
+            if (lane == 0) s_wsum[warp] = mine_n;
             __syncthreads();
             int before = 0, total = 0;
             for (int w = 0; w < nwarps; ++w) {
@@ -223,102 +236,173 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
                 before += w < warp ? cw : 0;
                 total += cw;
             }
-            if (keep) s_at[n + before + __popc(m & ((1u << lane) - 1u))] = p;
+            int at = n + before;
+#pragma unroll
+            for (int j = 0; j < kAgridRound; ++j) {
+                if ((m[j] >> lane) & 1u) s_at[at + __popc(m[j] & below)] = p[j];
+                at += __popc(m[j]);
+            }
             n += total;
-            cursor += blockDim.x;
+            cursor += round;
             __syncthreads();
         }
         return n;
     };
-    // the largest of the fine cells' values v (non-negative), to every thread
-    auto block_max = [&](float v) {
-        if (t == 0) s_tmax = 0.f;
-        __syncthreads();
-        if (mine) atomicMax((int *)&s_tmax, __float_as_int(v));
-        __syncthreads();
-        const float r = s_tmax;
-        __syncthreads();
-        return r;
+    auto warp_min = [&](float v) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        return v;
     };
     const float cut = (float)S.cut;
     const float slack = 1e-3f * (1.0f + cut);
     const float margin = F.g.two_delta + slack;
-    float L = 0.f, T = 0.f;
+    // the list threshold and bucket edges of fine cell g from its bounds
+    auto thresh = [&](int g) { return fminf(fc.ortho ? sqrtf(s_far[g]) : sqrtf(s_far[g]) + fc.R, cut) + margin; };
+    auto lowest = [&](int g) { return fc.ortho ? sqrtf(s_near[g]) : fmaxf(sqrtf(s_near[g]) - fc.R, 0.f); };
+    if (t == 0) s_tmax = 0.f;
+    int kept = -1;  // count pass: atoms of pass 1 still staged (-1 none yet, -2 several stages)
     if (!FILL) {
+        for (int g = t; g < K3; g += blockDim.x) {
+            s_far[g] = INFINITY;
+            s_near[g] = INFINITY;
+        }
         // the search cell's own atoms first: each fine cell's bound from them
         // limits the stencil atoms that can matter to those within the
         // largest bound of the cell (dense solutes: a few Angstrom)
-        float far = INFINITY, near = INFINITY;
         const int own = (La2 * ny + La1) * nx + La0;
         const int own_beg = s_pre[own], own_n = s_pre[own + 1] - s_pre[own];
-        for (int k0 = 0; k0 < own_n; k0 += kAgridBatch) {
-            const int nb = min(kAgridBatch, own_n - k0);
+        for (int k0 = 0; k0 < own_n; k0 += kAgridStage) {
+            const int nb = min(kAgridStage, own_n - k0);
             __syncthreads();
             for (int k = t; k < nb; k += blockDim.x) s_at[k] = atom_at(own_beg + k0 + k);
             __syncthreads();
-            if (mine)
-                for (int k = 0; k < nb; ++k) far = fminf(far, fine_far2(fc, cen, s_at[k]));
+            for (int g = warp; g < K3; g += nwarps) {
+                float cen[3];
+                centre(g, cen);
+                float far = INFINITY;
+                for (int k = lane; k < nb; k += 32) far = fminf(far, fine_far2(fc, cen, s_at[k]));
+                far = warp_min(far);
+                if (lane == 0) s_far[g] = fminf(s_far[g], far);
+            }
         }
-        const float T_own = fminf(fc.ortho ? sqrtf(far) : sqrtf(far) + fc.R, cut) + margin;
-        const float thr1 = block_max(T_own) + slack;
-        // pass 1: an upper bound of the nearest atom's distance over the fine
+        __syncthreads();
+        for (int g = t; g < K3; g += blockDim.x) atomicMax((int *)&s_tmax, __float_as_int(thresh(g)));
+        __syncthreads();
+        const float thr1 = s_tmax + slack;
+        // pass 1: an upper bound of the nearest atom's distance over each fine
         // cell, and the smallest distance of any atom to it
         int cursor = 0;
         while (cursor < N) {
             const int nb = stage_kept(cursor, thr1);
-            if (mine)
-                for (int k = 0; k < nb; ++k) {
+            kept = kept == -1 && cursor >= N ? nb : -2;  // one stage held every atom that passed
+            for (int g = warp; g < K3; g += nwarps) {
+                float cen[3];
+                centre(g, cen);
+                float far = INFINITY, near = INFINITY;
+                for (int k = lane; k < nb; k += 32) {
                     const float4 p = s_at[k];
                     far = fminf(far, fine_far2(fc, cen, p));
                     near = fminf(near, fine_near2(fc, cen, p));
                 }
-            __syncthreads();
-        }
-        T = fminf(fc.ortho ? sqrtf(far) : sqrtf(far) + fc.R, cut) + margin;
-        L = fc.ortho ? sqrtf(near) : fmaxf(sqrtf(near) - fc.R, 0.f);
-        if (mine) B.gedge[ebase + t] = make_float2(L, T);
-    } else if (mine) {
-        const float2 e = B.gedge[ebase + t];
-        L = e.x;
-        T = e.y;
-    }
-    // pass 2: the atoms whose smallest distance to the fine cell is within T,
-    // by bucket of that distance; the count and fill passes stage the same
-    // atoms in the same order and find the same buckets, and the fill pass
-    // bounds every write by the next bucket's start
-    const float thr2 = block_max(mine ? T : 0.f) + slack;
-    const float lim2 = fc.ortho ? T * T : (T + fc.R) * (T + fc.R);
-    const float inv = T > L ? (float)kAgridBuckets / (T - L) : 0.f;
-    int pos[kAgridBuckets], end[kAgridBuckets];
-#pragma unroll
-    for (int b = 0; b < kAgridBuckets; ++b) {
-        pos[b] = FILL && mine ? B.gstart[gbase + (int64_t)t * kAgridBuckets + b] : 0;
-        end[b] = FILL && mine ? B.gstart[gbase + (int64_t)t * kAgridBuckets + b + 1] : 0;
-    }
-    float4 *ent = FILL ? B.gent + (int64_t)f * B.gcap : nullptr;
-    int cursor = 0;
-    while (cursor < N) {
-        const int nb = stage_kept(cursor, thr2);
-        if (mine)
-            for (int k = 0; k < nb; ++k) {
-                const float4 p = s_at[k];
-                const float d2 = fine_near2(fc, cen, p);
-                if (d2 <= lim2) {
-                    const float dmin = fc.ortho ? sqrtf(d2) : fmaxf(sqrtf(d2) - fc.R, 0.f);
-                    const int bk = min(kAgridBuckets - 1, max(0, (int)((dmin - L) * inv)));
-#pragma unroll
-                    for (int b = 0; b < kAgridBuckets; ++b)
-                        if (bk == b) {
-                            if (FILL && pos[b] < end[b]) ent[pos[b]] = p;
-                            ++pos[b];
-                        }
+                far = warp_min(far);
+                near = warp_min(near);
+                if (lane == 0) {
+                    s_far[g] = fminf(s_far[g], far);
+                    s_near[g] = fminf(s_near[g], near);
                 }
             }
+            __syncthreads();
+        }
+        for (int g = t; g < K3; g += blockDim.x) B.gedge[ebase + g] = make_float2(lowest(g), thresh(g));
+        __syncthreads();
+        if (t == 0) s_tmax = 0.f;
+        __syncthreads();
+    } else {
+        // the fill pass: thresholds and edges from the count pass
+        for (int g = t; g < K3; g += blockDim.x) {
+            const float2 e = B.gedge[ebase + g];
+            s_near[g] = e.x;  // holds L itself here
+            s_far[g] = e.y;   // holds T itself here
+        }
         __syncthreads();
     }
-    if (!FILL && mine)
+    // pass 2: the atoms whose smallest distance to the fine cell is within T,
+    // by bucket of that distance
+    auto LT = [&](int g, float &L, float &T) {
+        if (FILL) {
+            L = s_near[g];
+            T = s_far[g];
+        } else {
+            L = lowest(g);
+            T = thresh(g);
+        }
+    };
+    for (int g = t; g < K3; g += blockDim.x) {
+        float L, T;
+        LT(g, L, T);
+        atomicMax((int *)&s_tmax, __float_as_int(T));
 #pragma unroll
-        for (int b = 0; b < kAgridBuckets; ++b) B.gcount[gbase + (int64_t)t * kAgridBuckets + b] = pos[b];
+        for (int b = 0; b < kAgridBuckets; ++b) s_pos[g][b] = FILL ? B.gstart[gbase + (int64_t)g * kAgridBuckets + b] : 0;
+    }
+    __syncthreads();
+    const float thr2 = s_tmax + slack;
+    float4 *ent = FILL ? B.gent + (int64_t)f * B.gcap : nullptr;
+    // one stage of atoms through every fine cell: lane k of a group of 32
+    // tests atom k; the count pass sums the buckets, the fill pass writes each
+    // bucket's atoms in stage order after its start (bounded by the next start)
+    auto pass2 = [&](int nb) {
+        for (int g = warp; g < K3; g += nwarps) {
+            float cen[3];
+            centre(g, cen);
+            float L, T;
+            LT(g, L, T);
+            const float lim2 = fc.ortho ? T * T : (T + fc.R) * (T + fc.R);
+            const float inv = T > L ? (float)kAgridBuckets / (T - L) : 0.f;
+            const int64_t nextb = gbase + (int64_t)g * kAgridBuckets;
+            for (int k0 = 0; k0 < nb; k0 += 32) {
+                const int k = k0 + lane;
+                int bk = -1;
+                float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k < nb) {
+                    p = s_at[k];
+                    const float d2 = fine_near2(fc, cen, p);
+                    if (d2 <= lim2) {
+                        const float dmin = fc.ortho ? sqrtf(d2) : fmaxf(sqrtf(d2) - fc.R, 0.f);
+                        bk = min(kAgridBuckets - 1, max(0, (int)((dmin - L) * inv)));
+                    }
+                }
+#pragma unroll
+                for (int b = 0; b < kAgridBuckets; ++b) {
+                    const unsigned m = __ballot_sync(0xffffffffu, bk == b);
+                    if (!m) continue;
+                    if (FILL && bk == b) {
+                        const int at = s_pos[g][b] + __popc(m & below);
+                        if (at < B.gstart[nextb + b + 1]) ent[at] = p;
+                    }
+                    __syncwarp();
+                    if (lane == 0) s_pos[g][b] += __popc(m);
+                    __syncwarp();
+                }
+            }
+        }
+    };
+    int cursor = 0;
+    if (!FILL && kept >= 0) {
+        // the count pass reuses pass 1's single stage: it holds every atom that
+        // passes thr2 (thr2 <= thr1), and the others fail the bucket test
+        pass2(kept);
+        cursor = N;
+    }
+    while (cursor < N) {
+        const int nb = stage_kept(cursor, thr2);
+        pass2(nb);
+        __syncthreads();
+    }
+    __syncthreads();
+    if (!FILL)
+        for (int g = t; g < K3; g += blockDim.x)
+#pragma unroll
+            for (int b = 0; b < kAgridBuckets; ++b) B.gcount[gbase + (int64_t)g * kAgridBuckets + b] = s_pos[g][b];
 }
 
 template <bool FILL>
@@ -329,7 +413,7 @@ __global__ void __launch_bounds__(kAgridBuildThreads) k_agrid_build(DevSys S, Bu
 // Per-frame exclusive scan of the list lengths (one CTA of 1024 threads per
 // frame) into gstart[0 .. n]; a frame whose entries exceed gcap loses its
 // grid (its molecule pairs take the walk path).
-__device__ __forceinline__ void k_agrid_scan_body(const uint3 blockIdx, const dim3 gridDim, Bufs B) {
+__device__ __forceinline__ void k_agrid_scan_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
     const int f = blockIdx.x;
     const int64_t base = (int64_t)f * B.gs;
     const int *count = B.gcount + base;
@@ -361,7 +445,11 @@ __device__ __forceinline__ void k_agrid_scan_body(const uint3 blockIdx, const di
     __syncthreads();
     const long long total = wtot[31];
     if (total > B.gcap) {
-        if (t == 0) B.FS[f].agrid = 0;
+        if (t == 0) {
+            B.FS[f].agrid = 0;
+            atomicAdd(S.stats + ST_AGRID_OVF, 1ull);
+            atomicMax(S.stats + ST_AGRID_NEED, (unsigned long long)total);
+        }
         return;
     }
     int excl = (int)(v - local + (w > 0 ? wtot[w - 1] : 0));
@@ -372,8 +460,8 @@ __device__ __forceinline__ void k_agrid_scan_body(const uint3 blockIdx, const di
     if (t == 0) start[n] = (int)total;
 }
 
-__global__ void __launch_bounds__(1024) k_agrid_scan(Bufs B) {
-    k_agrid_scan_body(blockIdx, gridDim, B);
+__global__ void __launch_bounds__(1024) k_agrid_scan(DevSys S, Bufs B) {
+    k_agrid_scan_body(blockIdx, gridDim, S, B);
 }
 
 // One site's query: its fine cell from its FP32 position q in search cell

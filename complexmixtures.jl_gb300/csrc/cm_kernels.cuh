@@ -58,6 +58,8 @@ enum : int {
     ST_GUARD,
     ST_GUARD_PAIRS,
     ST_MAXERR,  // bits of a non-negative double
+    ST_AGRID_OVF,   // frames whose candidate-grid lists did not fit (they took the walk)
+    ST_AGRID_NEED,  // the largest list entries of such a frame
     ST_N
 };
 

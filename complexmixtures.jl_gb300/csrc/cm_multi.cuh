@@ -95,7 +95,7 @@ __device__ __forceinline__ void mk_body(const uint3 vb, const dim3 vg, const MAr
     else if constexpr (KID == MK_SCATTER_ATOMS) k_scatter_atoms_body(vb, vg, a.B);
     else if constexpr (KID == MK_ATOMS_NEAR) k_atoms_near_body(vb, vg, a.B);
     else if constexpr (KID == MK_AGRID_COUNT) k_agrid_build_body<false>(vb, vg, a.S, a.B);
-    else if constexpr (KID == MK_AGRID_SCAN) k_agrid_scan_body(vb, vg, a.B);
+    else if constexpr (KID == MK_AGRID_SCAN) k_agrid_scan_body(vb, vg, a.S, a.B);
     else if constexpr (KID == MK_AGRID_FILL) k_agrid_build_body<true>(vb, vg, a.S, a.B);
     else if constexpr (KID == MK_AGRID_REAL) k_agrid_real_body(vb, vg, a.S, a.B);
     else if constexpr (KID == MK_AGRID_RANDOM) k_agrid_random_body(vb, vg, a.S, a.B, a.a0, a.a1);

@@ -666,6 +666,10 @@ void kernel_smem_limits(int device) {
     raise((const void *)k_pairs_edge<false>);
     raise((const void *)k_agrid_real);
     raise((const void *)k_agrid_random);
+    raise((const void *)k_agrid_build<false>);
+    raise((const void *)k_agrid_build<true>);
+    raise((const void *)k_multi<MK_AGRID_COUNT>);
+    raise((const void *)k_multi<MK_AGRID_FILL>);
     raise((const void *)k_multi<MK_AGRID_REAL>);
     raise((const void *)k_multi<MK_AGRID_RANDOM>);
     raise((const void *)k_multi<MK_EVAL_REAL_CELL>);
@@ -885,12 +889,18 @@ void plan(cm_handle *h, const cm_frames *f) {
         // so every item of a chunk must fit the queue.
         h->agk = 0;
         const bool fp32 = d.precision == CM_PRECISION_FP32_GUARD;
-        const bool want = d.atoms_grid > 0 || (d.atoms_grid == 0 && dense);
+        // a query is one thread per solvent molecule over its sites, so the
+        // grid pays off for small solvent molecules queried many times per
+        // frame (each real molecule and every random-insertion slot)
+        const bool pays = d.solvent_natomspermol <= 4 &&
+                          mv * (1 + (h->mddf ? (int64_t)d.n_random_samples : 0)) >= 4 * h->Ns;
+        (void)dense;
+        const bool want = d.atoms_grid > 0 || (d.atoms_grid == 0 && pays);
         if (want && fp32 && ms == 1 && !d.autocorrelation && (int64_t)fc * mv <= h->aq_cap) {
-            int K = d.atoms_grid > 0 ? d.atoms_grid : (int)std::ceil(target_cell(h) / 2.5);
+            int K = d.atoms_grid > 0 ? d.atoms_grid : (int)std::ceil(target_cell(h) / 4.5);
             K = std::max(1, std::min(K, kAgridMaxK));
             const int64_t gcap = d.atoms_grid_capacity > 0 ? (int64_t)d.atoms_grid_capacity
-                                                           : std::min<int64_t>(h->Ns * 96 + 65536, (int64_t)INT32_MAX);
+                                                           : std::min<int64_t>(h->Ns * 128 + 131072, (int64_t)INT32_MAX);
             const int64_t bytes = (int64_t)fc * gcap * 16;
             // under an HBM budget the grid takes at most a quarter of it
             if (d.hbm_budget_bytes <= 0 || h->device_bytes + bytes <= d.hbm_budget_bytes / 4) {
@@ -1099,7 +1109,7 @@ void launch_one(int kid, dim3 g, size_t smem, cudaStream_t st, const MArgs &a) {
     case MK_SCATTER_ATOMS: k_scatter_atoms<<<g, t, smem, st>>>(a.B); break;
     case MK_ATOMS_NEAR: k_atoms_near<<<g, t, smem, st>>>(a.B); break;
     case MK_AGRID_COUNT: k_agrid_build<false><<<g, t, smem, st>>>(a.S, a.B); break;
-    case MK_AGRID_SCAN: k_agrid_scan<<<g, t, smem, st>>>(a.B); break;
+    case MK_AGRID_SCAN: k_agrid_scan<<<g, t, smem, st>>>(a.S, a.B); break;
     case MK_AGRID_FILL: k_agrid_build<true><<<g, t, smem, st>>>(a.S, a.B); break;
     case MK_AGRID_REAL: k_agrid_real<<<g, t, smem, st>>>(a.S, a.B); break;
     case MK_AGRID_RANDOM: k_agrid_random<<<g, t, smem, st>>>(a.S, a.B, a.a0, a.a1); break;
@@ -1228,9 +1238,10 @@ void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, c
     if (agrid) {
         // the single solute molecule's candidate lists of every frame
         const dim3 gb(c.ncell_max, nf);
-        em.kernel(MK_AGRID_COUNT, gb, 0, CM_K_CELLS, base);
+        const size_t bsm = (size_t)kAgridStage * sizeof(float4);
+        em.kernel(MK_AGRID_COUNT, gb, bsm, CM_K_CELLS, base);
         em.kernel(MK_AGRID_SCAN, dim3(nf), 0, CM_K_CELLS, base);
-        em.kernel(MK_AGRID_FILL, gb, 0, CM_K_CELLS, base);
+        em.kernel(MK_AGRID_FILL, gb, bsm, CM_K_CELLS, base);
         // real pass: every solvent molecule queried; records inside the band
         // (and frames without a grid) go to the evaluation queue
         em.zero(B.counters + 2, sizeof(int));
@@ -1664,8 +1675,31 @@ void open_class(cm_handle *h, double w) {
     h->class_w = w;
 }
 
+// Candidate-grid lists that did not fit in earlier submits (those frames took
+// the walk): once the handle's queued work is done, grow the entries per
+// frame to a quarter above the largest frame's need, at least doubling them
+// (within the HBM budget), so that later chunks use the grid.
+void agrid_grow(cm_handle *h) {
+    if (h->agk <= 0 || h->d.atoms_grid_capacity > 0 || h->gcap >= INT32_MAX) return;
+    if (cudaStreamQuery(h->stream) != cudaSuccess) {
+        (void)cudaGetLastError();  // still running (cudaErrorNotReady): look again at the next submit
+        return;
+    }
+    unsigned long long ovf[2] = {0, 0};
+    CM_CUDA(cudaMemcpy(ovf, P<unsigned long long>(h->stats) + ST_AGRID_OVF, sizeof(ovf), cudaMemcpyDeviceToHost));
+    if (ovf[0] == 0) return;
+    const int64_t gcap = std::min<int64_t>(std::max<int64_t>(h->gcap * 2, (int64_t)(ovf[1] + ovf[1] / 4)), (int64_t)INT32_MAX);
+    const int64_t bytes = (int64_t)h->fc * gcap * 16;
+    const int64_t now = (int64_t)h->gent.charged;
+    if (h->d.hbm_budget_bytes > 0 && h->device_bytes - now + bytes > h->d.hbm_budget_bytes / 4) return;
+    dev_alloc(h, h->gent, (size_t)bytes);
+    h->gcap = gcap;
+    CM_CUDA(cudaMemsetAsync(P<unsigned long long>(h->stats) + ST_AGRID_OVF, 0, sizeof(ovf), h->stream));
+}
+
 void submit(cm_handle *h, const cm_frames *f) {
     check_frames(h, f);
+    if (h->planned) agrid_grow(h);
     for (int f0 = 0; f0 < f->nframes; f0 += h->max_frames) {
         const Staged S = stage(h, f, f0);
         CM_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copied[S.b], 0));
@@ -2308,6 +2342,7 @@ void batch_round(cm_batch *bt, const cm_frames *frames, int r) {
         cm_handle *h = bt->hs[i];
         const int64_t f0 = (int64_t)r * h->max_frames;
         if (frames[i].nframes == 0 || f0 >= frames[i].nframes) continue;
+        if (h->planned) agrid_grow(h);
         st[i] = stage(h, &frames[i], (int)f0);
         active[i] = 1;
     }
@@ -3194,8 +3229,8 @@ int cm_autotune(const cm_system_desc *desc, const cm_frames *sample, cm_tuning *
     // counts (the walk schedule then only serves the records inside the band)
     const bool grid = atoms && desc->solute_nmols == 1 && !desc->autocorrelation &&
                       desc->precision == CM_PRECISION_FP32_GUARD && desc->atoms_grid >= 0;
-    const int cand_grid_pct[] = {100, 100, 80, 80, 100, 100, 100, 70};
-    const int cand_grid_k[] = {-1, -1, -1, -1, 3, 4, 5, 4};
+    const int cand_grid_pct[] = {100, 100, 80, 80, 100, 100, 100, 100};
+    const int cand_grid_k[] = {-1, -1, -1, -1, 2, 3, 4, 5};
     const int ncand = (atoms || two_real) ? 8 : 4;
     double best = 0.0;
     for (int c = 0; c < ncand; ++c) {

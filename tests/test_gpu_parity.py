@@ -262,7 +262,7 @@ def test_autotune_atoms_grid_subdivisions(cm, gpu_ready):
                     nbins=350, n_random_samples=4, precision="fp32")
     assert len(t["candidates"]) == 8
     assert [(c["cell_scale_pct"], c["atoms_grid"]) for c in t["candidates"]] == [
-        (100, -1), (100, -1), (80, -1), (80, -1), (100, 3), (100, 4), (100, 5), (70, 4)]
+        (100, -1), (100, -1), (80, -1), (80, -1), (100, 2), (100, 3), (100, 4), (100, 5)]
     assert {c["atoms_schedule"] for c in t["candidates"][:4]} == {"cell", "balanced"}
     best = min(t["candidates"], key=lambda c: c["ms_per_frame"])
     assert (best["cell_scale_pct"], best["atoms_grid"]) == (t["cell_scale_pct"], t["atoms_grid"])
