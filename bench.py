@@ -60,6 +60,7 @@ C5_ATOMS = (5000, 500000)    # atoms per request log-uniform in this range
 C5_BANK_MOLS = 36000         # 504,000 atoms: every request size is a part of this system
 SERVE_REQUESTS = 250         # requests of the serving leg of the default bench line
 SERVE_RATES = (1.0, 1.5, 2.0)  # arrival rates, multiples of the serial FP32 service rate
+SERVE_MAX_ACTIVE = 4           # requests on the device at once (4 gave the highest aggregate rate of 4, 8 and 32)
 
 
 def parse():
@@ -73,6 +74,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--serve-max-active", type=int, default=SERVE_MAX_ACTIVE,
+                   help="serving: requests on the device at once (--workload c5 and the serving leg)")
+    p.add_argument("--serve-requests", type=int, default=0, help="--workload c5: requests (0 = the configuration's 2,000)")
+    p.add_argument("--serve-rates", default="", help="--workload c5: comma-separated arrival rates (x serial FP32)")
     p.add_argument("--atoms-grid", type=int, default=0,
                    help="ATOMS layout, one solute molecule: fine cells per search-cell axis of the candidate grid "
                         "(0 = engine default, -1 = stencil walk; speed only)")
@@ -234,7 +239,8 @@ def c5_requests(H, mmax, nreq):
     return reqs
 
 
-def serving_leg(cm, device, nreq=SERVE_REQUESTS, rates=SERVE_RATES, fp64_sample=12):
+def serving_leg(cm, device, nreq=SERVE_REQUESTS, rates=SERVE_RATES, fp64_sample=12, max_active=SERVE_MAX_ACTIVE,
+                frames_per_turn=32):
     """Config-5 serving load: Poisson arrivals of c3-like self-MDDF requests
     (c5_bank, c5_requests) into the continuous-batching server (FP32 + guard)
     at several arrival rates, against the same requests run one at a time on
@@ -290,7 +296,8 @@ def serving_leg(cm, device, nreq=SERVE_REQUESTS, rates=SERVE_RATES, fp64_sample=
     for mult in rates:
         rate = mult * nreq / t32
         gaps = np.random.default_rng(SERVE_SEED + 2).exponential(1.0 / rate, nreq)
-        with cm.Server(device=device, frames_per_turn=32, max_active=32, hbm_budget_bytes=96 << 30) as srv:
+        with cm.Server(device=device, frames_per_turn=frames_per_turn, max_active=max_active,
+                       hbm_budget_bytes=96 << 30) as srv:
             ids = []
             t0 = time.perf_counter()
             due = t0
@@ -334,7 +341,10 @@ def c5_workload(args, local):
 
     cm = entry.load_package()
     torch.cuda.set_device(local)
-    out = serving_leg(cm, local, nreq=C5_REQUESTS, fp64_sample=20)
+    rates = tuple(float(x) for x in args.serve_rates.split(",")) if args.serve_rates else SERVE_RATES
+    out = serving_leg(cm, local, nreq=args.serve_requests or C5_REQUESTS, fp64_sample=20, rates=rates,
+                      max_active=args.serve_max_active)
+    out["max_active"] = args.serve_max_active
     out.update(metric="MDDF frames/s and request latency (config 5 serving load)", unit="frames/s",
                value=out["frames_per_s"], data="synthetic (seeded generator of the configuration)")
     print(json.dumps(out), flush=True)
@@ -366,7 +376,7 @@ def batched_c4_leg(cm, device):
         systems.append((xs, xv, cells, kw))
     med = int(np.argsort(sizes)[len(sizes) // 2])
     xs, xv, cells, kw = systems[med]
-    tune = cm.autotune(xs[:2], xv[:2], cells[:2], **kw)
+    tune = cm.autotune(xs[:8], xv[:8], cells[:8], **kw)
     pct = tune["cell_scale_pct"]
     sched = tune["atoms_schedule"]
     agrid = tune["atoms_grid"]

@@ -42,9 +42,11 @@ namespace cmk {
 constexpr int kFlatWarps = CM_FLAT_WARPS;  // warps per CTA
 constexpr int kAtomQueue = 64;   // per-warp atom queue (float4: t, tag)
 
-struct CandSlot {
-    unsigned long long k1;
-    unsigned int m2, r1, r2, pad;
+// The 32 candidates' fold slots, one array per field: the lanes of a flush
+// hold different candidates, and their atomics then fall on distinct banks.
+struct CandSlots {
+    unsigned long long k1[32];
+    unsigned int m2[32], r1[32], r2[32];
 };
 
 constexpr unsigned long long kNoPair = (0x7f800000ull << 32) | 0xffffffffull;  // +inf, largest index
@@ -55,7 +57,7 @@ struct FlatWarpSmem {
     float4 aq[kAtomQueue];        // atom queue: t = position relative to the solute centroid, w = tag c << 8 | b
     float4 cq[kQueue];            // candidate queue: D = centroid displacement, w = molecule index
     int cc[kQueue];               // candidate queue: packed cell offset
-    CandSlot cand[32];
+    CandSlots cand;
 };
 
 __host__ __device__ constexpr size_t flat_warp_smem() { return sizeof(FlatWarpSmem); }
@@ -104,16 +106,16 @@ __device__ __forceinline__ void flat_flush(const DevSys &S, FlatWarpSmem &W, int
         const float m2 = fminf(fmaxf(m1a, m1b), fminf(m2a, m2b));
         const int k1 = m1b < m1a ? k1b : k1a;
         st.atompairs += (unsigned long long)aps;
-        CandSlot &C = W.cand[c];
+        CandSlots &C = W.cand;
         const unsigned long long key = ((unsigned long long)__float_as_uint(m1) << 32) | (unsigned)(k1 << 8 | b);
-        const unsigned long long old = atomicMin(&C.k1, key);
+        const unsigned long long old = atomicMin(&C.k1[c], key);
         const float displaced = fmaxf(m1, __uint_as_float((unsigned)(old >> 32)));
-        atomicMin(&C.m2, __float_as_uint(fminf(displaced, m2)));
-        if (b == S.iref) C.r1 = __float_as_uint(m1);
+        atomicMin(&C.m2[c], __float_as_uint(fminf(displaced, m2)));
+        if (b == S.iref) C.r1[c] = __float_as_uint(m1);
         if (SELF) {
             const float4 oi = W.os[S.iref];
             const float dx = e.x - oi.x, dy = e.y - oi.y, dz = e.z - oi.z;
-            atomicMin(&C.r2, __float_as_uint(fmaf(dz, dz, fmaf(dy, dy, dx * dx))));
+            atomicMin(&C.r2[c], __float_as_uint(fmaf(dz, dz, fmaf(dy, dy, dx * dx))));
         }
     }
     __syncwarp();
@@ -129,11 +131,11 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
                                            const PairsFrame &Pf, const Guard &g, int f, int s, int sslot, float rs2,
                                            int lane, int nc, LocalStats &st) {
     if (lane < nc) {
-        CandSlot &C = W.cand[lane];
-        C.k1 = kNoPair;
-        C.m2 = 0x7f800000u;
-        C.r1 = 0x7f800000u;
-        C.r2 = 0x7f800000u;
+        CandSlots &C = W.cand;
+        C.k1[lane] = kNoPair;
+        C.m2[lane] = 0x7f800000u;
+        C.r1[lane] = 0x7f800000u;
+        C.r2[lane] = 0x7f800000u;
     }
     __syncwarp();
     const int apv = S.apv;
@@ -180,14 +182,14 @@ __device__ __forceinline__ void flat_batch(const DevSys &S, const Bufs &B, const
     if (nq > 0) flat_flush<SELF, APS>(S, W, nq, lane, st);
     if (lane >= nc) return;
     st.molpairs++;
-    const CandSlot &C = W.cand[lane];
-    const unsigned long long k1 = C.k1;
+    const CandSlots &C = W.cand;
+    const unsigned long long k1 = C.k1[lane];
     if (k1 == kNoPair) return;
     const float m1 = __uint_as_float((unsigned)(k1 >> 32));
     if (m1 > g.cutp2) return;  // no atom pair within the cutoff
     const int v = __float_as_int(W.cq[lane].w), code = W.cc[lane];
     const int a1 = (int)((unsigned)k1 >> 8) & 0xff, b1 = (int)(k1 & 0xff);
-    const float m2 = __uint_as_float(C.m2), r1 = __uint_as_float(C.r1), r2 = __uint_as_float(C.r2);
+    const float m2 = __uint_as_float(C.m2[lane]), r1 = __uint_as_float(C.r1[lane]), r2 = __uint_as_float(C.r2[lane]);
     const float dmin = sqrtf(m1);
     // hard: the closest pair, or the cutoff or dbulk decision, needs the full
     // FP64 rules (guard queue)

@@ -2174,9 +2174,11 @@ void record_chunk(cm_handle *h, const Staged &S, const Chunk &c, std::vector<Ste
 
 // A fused staging round: every system's chunk j goes through the same chain
 // of stages, and each stage runs once for all of them (k_multi, k_multi_zero)
-// in one captured graph on the batch stream.  False (nothing launched) when
-// the systems cannot share the launches: another layout or precision, a
-// weight class change inside the round, or chains of different shapes.
+// in one captured graph on the batch stream; where the systems' kernels of a
+// stage differ (the ATOMS evaluation schedule follows each solute's density)
+// the stage takes one launch per kernel.  False (nothing launched) when the
+// systems cannot share the launches: another layout or precision, a weight
+// class change inside the round, or chains of different lengths.
 bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<char> &active) {
     const size_t n = bt->hs.size();
     size_t nchunks = 0;
@@ -2200,7 +2202,7 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
             else {
                 if (r.size() != shape->size()) return false;
                 for (size_t k = 0; k < r.size(); ++k)
-                    if (r[k].kernel != (*shape)[k].kernel || r[k].kid != (*shape)[k].kid) return false;
+                    if (r[k].kernel != (*shape)[k].kernel) return false;
             }
         }
     }
@@ -2224,18 +2226,34 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
         size_t nsteps = 0;
         for (size_t i = 0; i < n; ++i) nsteps = std::max(nsteps, rec[j][i].size());
         for (size_t k = 0; k < nsteps; ++k) {
-            Launch L{};
-            std::vector<MZero> zs;
-            std::vector<MTask> ts;
-            long long blocks = 0;
+            // the kernels of this stage across the systems, in order of first appearance
+            std::vector<int> kids;
+            bool zero = false;
             for (size_t i = 0; i < n; ++i) {
                 if (rec[j][i].size() <= k) continue;
                 const Step &s = rec[j][i][k];
-                L.kernel = s.kernel;
-                L.kid = s.kid;
-                if (!s.kernel) {
-                    zs.push_back({s.zp, (long long)s.zbytes});
-                } else {
+                if (!s.kernel) zero = true;
+                else if (std::find(kids.begin(), kids.end(), s.kid) == kids.end()) kids.push_back(s.kid);
+            }
+            if (zero) {
+                std::vector<MZero> zs;
+                for (size_t i = 0; i < n; ++i)
+                    if (rec[j][i].size() > k) zs.push_back({rec[j][i][k].zp, (long long)rec[j][i][k].zbytes});
+                Launch L{};
+                L.n = (int)zs.size();
+                L.off = put(zs.data(), zs.size() * sizeof(MZero));
+                plan.push_back(L);
+                continue;
+            }
+            for (int kid : kids) {
+                Launch L{};
+                L.kernel = 1;
+                L.kid = kid;
+                std::vector<MTask> ts;
+                long long blocks = 0;
+                for (size_t i = 0; i < n; ++i) {
+                    if (rec[j][i].size() <= k || rec[j][i][k].kid != kid) continue;
+                    const Step &s = rec[j][i][k];
                     MTask t;
                     t.a = s.a;
                     t.grid = make_uint3(s.grid.x, s.grid.y, s.grid.z);
@@ -2244,16 +2262,11 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
                     ts.push_back(t);
                     L.smem = std::max(L.smem, s.smem);
                 }
-            }
-            if (L.kernel) {
                 L.n = (int)ts.size();
                 L.blocks = blocks;
                 L.off = put(ts.data(), ts.size() * sizeof(MTask));
-            } else {
-                L.n = (int)zs.size();
-                L.off = put(zs.data(), zs.size() * sizeof(MZero));
+                plan.push_back(L);
             }
-            plan.push_back(L);
         }
     }
     // the tables to the device, ahead of the graph on the batch stream

@@ -26,10 +26,11 @@ def chain_system(rng, n_solute, n_water, nframes, box):
 
 
 def engine_kw(n_solute, n_water, **extra):
-    return dict(solute_nmols=1, solute_natomspermol=n_solute, solvent_nmols=n_water, solvent_natomspermol=3,
-                autocorrelation=False, precision="fp32", regime="atoms", max_frames_per_batch=4, atoms_schedule="balanced",
-                solute_groups=[[i // 10] for i in range(n_solute)], solute_ngroups=(n_solute + 9) // 10,
-                **OPT, **extra)
+    kw = dict(solute_nmols=1, solute_natomspermol=n_solute, solvent_nmols=n_water, solvent_natomspermol=3,
+              autocorrelation=False, precision="fp32", regime="atoms", max_frames_per_batch=4, atoms_schedule="balanced",
+              solute_groups=[[i // 10] for i in range(n_solute)], solute_ngroups=(n_solute + 9) // 10, **OPT)
+    kw.update(extra)
+    return kw
 
 
 def alone(cm, xs, xv, cells, **kw):
@@ -90,9 +91,11 @@ def test_fused_batch_equals_each_system_alone(cm, orc, gpu_ready, grid):
         assert np.array_equal(np.asarray(got[0][key]).ravel(), np.asarray(ref[key]).ravel()), key
 
 
-def test_fused_and_streams_modes_agree(cm, gpu_ready):
+@pytest.mark.parametrize("grid", [-1, 3], ids=["walk", "grid"])
+def test_fused_and_streams_modes_agree(cm, gpu_ready, grid):
     """The same systems through a fused batch and a per-system-streams batch,
-    resident frames, three rounds: identical counts."""
+    resident frames, three rounds, the systems' evaluation schedules differing
+    (a stage then takes one launch per kernel): identical counts."""
     import torch
 
     rng = np.random.default_rng(62)
@@ -102,7 +105,8 @@ def test_fused_and_streams_modes_agree(cm, gpu_ready):
            for xs, xv, cells in data]
     out = {}
     for mode in ("fused", "streams"):
-        engines = [cm.Engine(**engine_kw(n_s, n_w)) for n_s, n_w, _ in specs]
+        engines = [cm.Engine(**engine_kw(n_s, n_w, atoms_grid=grid, atoms_schedule=("cell", "balanced")[k % 2]))
+                   for k, (n_s, n_w, _) in enumerate(specs)]
         with cm.Batch(engines, mode=mode) as b:
             for _ in range(3):
                 b.submit(dev)
