@@ -60,7 +60,7 @@ C5_ATOMS = (5000, 500000)    # atoms per request log-uniform in this range
 C5_BANK_MOLS = 36000         # 504,000 atoms: every request size is a part of this system
 SERVE_REQUESTS = 250         # requests of the serving leg of the default bench line
 SERVE_RATES = (1.0, 1.5, 2.0)  # arrival rates, multiples of the serial FP32 service rate
-SERVE_MAX_ACTIVE = 4           # requests on the device at once (4 gave the highest aggregate rate of 4, 8 and 32)
+SERVE_MAX_ACTIVE = 2           # requests on the device at once (2 gave the highest aggregate rate of 2, 3, 4, 8 and 32)
 
 
 def parse():

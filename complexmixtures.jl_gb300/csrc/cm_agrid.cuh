@@ -31,13 +31,13 @@
 // ATOMS walks (the guard band's error bound covers it), and the atom's index
 // in the molecule.
 //
-// Kernels: k_agrid_build<false> (list lengths), k_agrid_scan (per-frame
-// offsets; a frame whose lists do not fit loses its grid), k_agrid_build<true>
-// (entries), k_agrid_real (real pass) and k_agrid_random (random insertion:
-// placement and query fused, nothing written for slots decided at once).
-// Frames without a grid take the walk path through the same two kernels,
-// which then queue their molecule pairs for k_atoms_eval as k_atoms_filter and
-// k_atoms_place do.
+// Kernels: k_agrid_build (the lists of every frame, one CTA per search cell,
+// space reserved in a per-frame pool; a frame whose pool runs out loses its
+// grid), k_agrid_real (real pass) and k_agrid_random (random insertion:
+// placement and query of the slots k_slot_filter listed, nothing written for
+// slots decided at once).  Frames without a grid take the walk path through
+// the same two kernels, which then queue their molecule pairs for
+// k_atoms_eval as k_atoms_filter and k_atoms_place do.
 #pragma once
 #include "cm_atoms32.cuh"
 
@@ -99,14 +99,14 @@ __device__ __forceinline__ float fine_near2(const FineCells &fc, const float *c,
 }
 
 // Lists of the fine cells of one search cell (grid: x = search cell, y =
-// frame).  The CTA stages the cell's stencil atoms in shared memory; each warp
-// takes fine cells in turn and its lanes split the staged atoms (warp
-// reductions, and ballots for the compacted writes).  FILL = false writes the
-// bucket lengths to gcount and the bucket edges to gedge, FILL = true the
-// entries at gstart: both passes stage the same atoms in the same order and
-// find the same buckets.
-template <bool FILL>
-__device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
+// frame), in one pass.  The CTA stages the cell's stencil atoms in shared
+// memory; each warp takes fine cells in turn and its lanes split the staged
+// atoms (warp reductions, and ballots for the compacted writes).  The CTA
+// counts its lists by bucket, reserves their room in the frame's entry pool
+// with one atomic, writes each fine cell's bucket starts and end to gstart and
+// its bucket edges to gedge, then the entries.  A frame whose pool runs out
+// loses its grid (its queries take the walk).
+__device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B) {
     extern __shared__ float4 s_at[];  // kAgridStage entries
     __shared__ int s_pre[kAgridMaxStencil + 1];
     __shared__ int s_beg[kAgridMaxStencil];
@@ -114,6 +114,7 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
     __shared__ float s_far[kAgridMaxK * kAgridMaxK * kAgridMaxK], s_near[kAgridMaxK * kAgridMaxK * kAgridMaxK];
     __shared__ int s_pos[kAgridMaxK * kAgridMaxK * kAgridMaxK][kAgridBuckets];
     __shared__ int s_wsum[kAgridBuildThreads / 32];
+    __shared__ int s_base;
     __shared__ float s_tmax;
     const int f = blockIdx.y;
     const int c = blockIdx.x;
@@ -124,15 +125,13 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
     const unsigned below = (1u << lane) - 1u;
-    const int64_t gbase = (int64_t)f * B.gs + (int64_t)c * K3 * kAgridBuckets;  // bucket counts / starts
-    const int64_t ebase = (int64_t)f * B.gfs + (int64_t)c * K3;                  // fine-cell bucket edges
+    const int64_t gbase = ((int64_t)f * B.gfs + (int64_t)c * K3) * (kAgridBuckets + 1);  // bucket starts and end
+    const int64_t ebase = (int64_t)f * B.gfs + (int64_t)c * K3;                            // fine-cell bucket edges
     const bool active = F.agrid && B.anear[(int64_t)f * B.as + c];
     if (!active) {
         // no solute atom within a stencil of this cell: empty lists
-        if (!FILL) {
-            for (int g = t; g < K3 * kAgridBuckets; g += blockDim.x) B.gcount[gbase + g] = 0;
-            for (int g = t; g < K3; g += blockDim.x) B.gedge[ebase + g] = make_float2(0.f, 0.f);
-        }
+        for (int g = t; g < K3 * (kAgridBuckets + 1); g += blockDim.x) B.gstart[gbase + g] = 0;
+        for (int g = t; g < K3; g += blockDim.x) B.gedge[ebase + g] = make_float2(0.f, 0.f);
         return;
     }
     const int La0 = F.La[0], La1 = F.La[1], La2 = F.La[2];
@@ -260,8 +259,8 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
     auto thresh = [&](int g) { return fminf(fc.ortho ? sqrtf(s_far[g]) : sqrtf(s_far[g]) + fc.R, cut) + margin; };
     auto lowest = [&](int g) { return fc.ortho ? sqrtf(s_near[g]) : fmaxf(sqrtf(s_near[g]) - fc.R, 0.f); };
     if (t == 0) s_tmax = 0.f;
-    int kept = -1;  // count pass: atoms of pass 1 still staged (-1 none yet, -2 several stages)
-    if (!FILL) {
+    int kept = -1;  // atoms of pass 1 still staged (-1 none yet, -2 several stages)
+    {
         for (int g = t; g < K3; g += blockDim.x) {
             s_far[g] = INFINITY;
             s_near[g] = INFINITY;
@@ -317,40 +316,27 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         __syncthreads();
         if (t == 0) s_tmax = 0.f;
         __syncthreads();
-    } else {
-        // the fill pass: thresholds and edges from the count pass
-        for (int g = t; g < K3; g += blockDim.x) {
-            const float2 e = B.gedge[ebase + g];
-            s_near[g] = e.x;  // holds L itself here
-            s_far[g] = e.y;   // holds T itself here
-        }
-        __syncthreads();
     }
     // pass 2: the atoms whose smallest distance to the fine cell is within T,
-    // by bucket of that distance
+    // by bucket of that distance: counted, then written
     auto LT = [&](int g, float &L, float &T) {
-        if (FILL) {
-            L = s_near[g];
-            T = s_far[g];
-        } else {
-            L = lowest(g);
-            T = thresh(g);
-        }
+        L = lowest(g);
+        T = thresh(g);
     };
     for (int g = t; g < K3; g += blockDim.x) {
         float L, T;
         LT(g, L, T);
         atomicMax((int *)&s_tmax, __float_as_int(T));
 #pragma unroll
-        for (int b = 0; b < kAgridBuckets; ++b) s_pos[g][b] = FILL ? B.gstart[gbase + (int64_t)g * kAgridBuckets + b] : 0;
+        for (int b = 0; b < kAgridBuckets; ++b) s_pos[g][b] = 0;
     }
     __syncthreads();
     const float thr2 = s_tmax + slack;
-    float4 *ent = FILL ? B.gent + (int64_t)f * B.gcap : nullptr;
+    float4 *ent = B.gent + (int64_t)f * B.gcap;
     // one stage of atoms through every fine cell: lane k of a group of 32
-    // tests atom k; the count pass sums the buckets, the fill pass writes each
-    // bucket's atoms in stage order after its start (bounded by the next start)
-    auto pass2 = [&](int nb) {
+    // tests atom k; counting sums the buckets, filling writes each bucket's
+    // atoms in stage order after its start
+    auto pass2 = [&](int nb, bool fill) {
         for (int g = warp; g < K3; g += nwarps) {
             float cen[3];
             centre(g, cen);
@@ -358,7 +344,6 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
             LT(g, L, T);
             const float lim2 = fc.ortho ? T * T : (T + fc.R) * (T + fc.R);
             const float inv = T > L ? (float)kAgridBuckets / (T - L) : 0.f;
-            const int64_t nextb = gbase + (int64_t)g * kAgridBuckets;
             for (int k0 = 0; k0 < nb; k0 += 32) {
                 const int k = k0 + lane;
                 int bk = -1;
@@ -375,10 +360,7 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
                 for (int b = 0; b < kAgridBuckets; ++b) {
                     const unsigned m = __ballot_sync(0xffffffffu, bk == b);
                     if (!m) continue;
-                    if (FILL && bk == b) {
-                        const int at = s_pos[g][b] + __popc(m & below);
-                        if (at < B.gstart[nextb + b + 1]) ent[at] = p;
-                    }
+                    if (fill && bk == b) ent[s_pos[g][b] + __popc(m & below)] = p;
                     __syncwarp();
                     if (lane == 0) s_pos[g][b] += __popc(m);
                     __syncwarp();
@@ -386,82 +368,75 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
             }
         }
     };
-    int cursor = 0;
-    if (!FILL && kept >= 0) {
-        // the count pass reuses pass 1's single stage: it holds every atom that
-        // passes thr2 (thr2 <= thr1), and the others fail the bucket test
-        pass2(kept);
-        cursor = N;
-    }
-    while (cursor < N) {
-        const int nb = stage_kept(cursor, thr2);
-        pass2(nb);
+    // pass 1's single stage holds every atom that passes thr2 (thr2 <= thr1),
+    // and the others fail the bucket test: counting and filling reuse it
+    auto sweep = [&](bool fill) {
+        int cursor = 0;
+        if (kept >= 0) {
+            pass2(kept, fill);
+            cursor = N;
+        }
+        while (cursor < N) {
+            const int nb = stage_kept(cursor, thr2);
+            pass2(nb, fill);
+            __syncthreads();
+        }
         __syncthreads();
-    }
-    __syncthreads();
-    if (!FILL)
-        for (int g = t; g < K3; g += blockDim.x)
+    };
+    sweep(false);
+    // the CTA's lists: offsets by (fine cell, bucket), one reservation in the
+    // frame's pool, the starts and each fine cell's end
+    int tot = 0;
+    if (t < K3) {
 #pragma unroll
-            for (int b = 0; b < kAgridBuckets; ++b) B.gcount[gbase + (int64_t)g * kAgridBuckets + b] = s_pos[g][b];
-}
-
-template <bool FILL>
-__global__ void __launch_bounds__(kAgridBuildThreads) k_agrid_build(DevSys S, Bufs B) {
-    k_agrid_build_body<FILL>(blockIdx, gridDim, S, B);
-}
-
-// Per-frame exclusive scan of the list lengths (one CTA of 1024 threads per
-// frame) into gstart[0 .. n]; a frame whose entries exceed gcap loses its
-// grid (its molecule pairs take the walk path).
-__device__ __forceinline__ void k_agrid_scan_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
-    const int f = blockIdx.x;
-    const int64_t base = (int64_t)f * B.gs;
-    const int *count = B.gcount + base;
-    int *start = B.gstart + base;
-    const int K = B.agk;
-    const int n = B.G[f].ncell * K * K * K * kAgridBuckets;
-    const int t = threadIdx.x;
-    const int per = (n + 1023) / 1024;
-    const int lo = t * per, hi = min(n, lo + per);
-    long long local = 0;
-    for (int i = lo; i < hi; ++i) local += count[i];
-    const int lane = t & 31, w = t >> 5;
-    long long v = local;
+        for (int b = 0; b < kAgridBuckets; ++b) {
+            const int n = s_pos[t][b];
+            s_pos[t][b] = tot;
+            tot += n;
+        }
+    }
+    int incl = tot;
+#pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const long long y = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += y;
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
     }
-    __shared__ long long wtot[32];
-    if (lane == 31) wtot[w] = v;
+    if (lane == 31) s_wsum[warp] = incl;
     __syncthreads();
-    if (w == 0) {
-        long long s = wtot[lane];
-        for (int o = 1; o < 32; o <<= 1) {
-            const long long y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-        }
-        wtot[lane] = s;
+    int wbefore = 0, all = 0;
+    for (int w = 0; w < nwarps; ++w) {
+        wbefore += w < warp ? s_wsum[w] : 0;
+        all += s_wsum[w];
     }
-    __syncthreads();
-    const long long total = wtot[31];
-    if (total > B.gcap) {
-        if (t == 0) {
-            B.FS[f].agrid = 0;
+    if (t == 0) {
+        const int base = atomicAdd(B.gpool + f, all);
+        if ((int64_t)base + all > B.gcap) {
+            B.FS[f].agrid = 0;  // this frame's queries take the walk
             atomicAdd(S.stats + ST_AGRID_OVF, 1ull);
-            atomicMax(S.stats + ST_AGRID_NEED, (unsigned long long)total);
+            atomicMax(S.stats + ST_AGRID_NEED, (unsigned long long)((int64_t)base + all));
+            s_base = -1;
+        } else {
+            s_base = base;
         }
-        return;
     }
-    int excl = (int)(v - local + (w > 0 ? wtot[w - 1] : 0));
-    for (int i = lo; i < hi; ++i) {
-        start[i] = excl;
-        excl += count[i];
+    __syncthreads();
+    if (s_base < 0) return;
+    if (t < K3) {
+        const int start = s_base + wbefore + incl - tot;
+        int *st = B.gstart + gbase + (int64_t)t * (kAgridBuckets + 1);
+#pragma unroll
+        for (int b = 0; b < kAgridBuckets; ++b) {
+            s_pos[t][b] += start;
+            st[b] = s_pos[t][b];
+        }
+        st[kAgridBuckets] = start + tot;
     }
-    if (t == 0) start[n] = (int)total;
+    __syncthreads();
+    sweep(true);
 }
 
-__global__ void __launch_bounds__(1024) k_agrid_scan(DevSys S, Bufs B) {
-    k_agrid_scan_body(blockIdx, gridDim, S, B);
+__global__ void __launch_bounds__(kAgridBuildThreads) k_agrid_build(DevSys S, Bufs B) {
+    k_agrid_build_body(blockIdx, gridDim, S, B);
 }
 
 // One site's query: its fine cell from its FP32 position q in search cell
@@ -483,7 +458,7 @@ __device__ __forceinline__ void agrid_query(const Bufs &B, const FrameGeom &G, c
     }
     const int64_t fine = (int64_t)((cz * G.n[1] + cy) * G.n[0] + cx) * (K * K * K) + (gi[2] * K + gi[1]) * K + gi[0];
     const float2 edge = B.gedge[(int64_t)f * B.gfs + fine];
-    const int *st = B.gstart + (int64_t)f * B.gs + fine * kAgridBuckets;
+    const int *st = B.gstart + ((int64_t)f * B.gfs + fine) * (kAgridBuckets + 1);
     const float w = (edge.y - edge.x) * (1.0f / (float)kAgridBuckets);
     const float4 *e = B.gent + (int64_t)f * B.gcap;
     int i = st[0];
@@ -535,7 +510,7 @@ __device__ __forceinline__ int agrid_decide(const DevSys &S, const Guard &g, con
 // Real pass of a single solute molecule, one thread per (frame, solvent
 // molecule), persistent grid; frames without a grid queue their near pairs
 // for k_atoms_eval (k_atoms_filter's rule).
-__device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
+__device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);
@@ -596,7 +571,7 @@ __global__ void __launch_bounds__(256) k_agrid_real(DevSys S, Bufs B) {
 // k_atoms_place does (the same helpers); with a grid its sites are queried at
 // once and only a record inside the band is written out and queued; frames
 // without a grid write and queue every slot with an atom in a near cell.
-__device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0, int ny) {
+__device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int sample0, int ny) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);

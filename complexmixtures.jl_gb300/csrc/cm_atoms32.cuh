@@ -38,7 +38,7 @@ constexpr int kAtomsWarps = CM_ATOMS_WARPS;  // warps per CTA of k_atoms_eval
 // Dilated occupancy of each solute molecule's cell list: near = some cell
 // within the ATOMS stencil half-widths La holds an atom of the molecule.
 // Grid: x over ms * ncell, y = frame.
-__device__ __forceinline__ void k_atoms_near_body(const uint3 blockIdx, const dim3 gridDim, Bufs B) {
+__device__ __forceinline__ void k_atoms_near_body(const uint3 blockIdx, const dim3 gridDim, const Bufs &B) {
     const int f = blockIdx.y;
     const FrameGeom &G = B.G[f];
     const FrameScratch &F = B.FS[f];
@@ -86,7 +86,7 @@ __device__ __forceinline__ void atoms_push(const DevSys &S, const Bufs &B, int4 
 
 // Real pass filter, thread per (frame, solute molecule, solvent molecule)
 // item in [i0, i0 + n): queue entry (v, s, frame, 0).
-__device__ __forceinline__ void k_atoms_filter_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int64_t i0, int64_t n) {
+__device__ __forceinline__ void k_atoms_filter_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int64_t i0, int64_t n) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int64_t it = i0 + t;
@@ -677,7 +677,7 @@ enum AtomsSched { kSchedThread = 0, kSchedCell = 1, kSchedBalanced = 2 };
 
 // ATOMS evaluation of the queue (persistent grid).
 template <bool FP32, bool RANDOM, int SCHED>
-__device__ __forceinline__ void k_atoms_eval_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B) {
+__device__ __forceinline__ void k_atoms_eval_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B) {
     constexpr bool WARP = SCHED != kSchedThread;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float4 s_win[kAtomsWarps][32];  // atoms_walk_flat's window table, one per warp

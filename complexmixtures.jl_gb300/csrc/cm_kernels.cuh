@@ -411,10 +411,10 @@ struct Bufs {
     // that can be the closest (or within the guard band of it) to a point of
     // the fine cell; agk = 0: no grid
     int agk;
-    int64_t gs;                     // per-frame stride of gcount / gstart (ncell_cap * agk^3 * buckets + 1)
-    int64_t gfs;                    // per-frame stride of gedge (ncell_cap * agk^3)
+    int64_t gfs;                    // fine cells per frame (ncell_cap * agk^3)
     int64_t gcap;                   // entries per frame
-    int *gcount, *gstart;           // [nf][gs]: entries per (fine cell, bucket) and their starts
+    int *gstart;                    // [nf][gfs][buckets + 1]: each fine cell's bucket starts and its end
+    int *gpool;                     // [nf]: entries reserved in the frame's pool
     float2 *gedge;                  // [nf][gfs]: smallest distance of a listed atom to the fine cell, list threshold
     float4 *gent;                   // [nf][gcap]: position from the fine cell's search-cell origin, solute atom index
 };
@@ -872,7 +872,7 @@ __device__ bool stencil(const FrameGeom &G, double range, int *L) {
 
 // ------------------------------------------------------------------- kernels
 // Per-frame offset tables: off(Delta) = Hn Delta for Delta in [-kLT, kLT]^3.
-__device__ __forceinline__ void k_offtable_body(const uint3 blockIdx, const dim3 gridDim, Bufs B) {
+__device__ __forceinline__ void k_offtable_body(const uint3 blockIdx, const dim3 gridDim, const Bufs &B) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y;
     if (i >= kOffEntries) return;
     const int dx = i % kLTW - kLT, dy = (i / kLTW) % kLTW - kLT, dz = i / (kLTW * kLTW) - kLT;
@@ -973,7 +973,7 @@ __global__ void k_prep_pairs(Bufs B, const T *__restrict__ xyz, int64_t xyz_stri
 // threads per frame): start[0..n] and a copy in fill for the scatter.  n is
 // the frame's cell count times `mult` (1: molecule cells, ms: per-molecule
 // atom cells).
-__device__ __forceinline__ void k_scan_body(const uint3 blockIdx, const dim3 gridDim, Bufs B, int atoms_layout) {
+__device__ __forceinline__ void k_scan_body(const uint3 blockIdx, const dim3 gridDim, const Bufs &B, int atoms_layout) {
     __shared__ int wsum[32];
     const int f = blockIdx.x;
     const int64_t stride = atoms_layout ? B.as : B.cs;
@@ -1269,7 +1269,7 @@ __global__ void k_queue_check(Bufs B, unsigned long long *__restrict__ hist, con
 // ascending (src/mddf.jl:406-415); one CTA per (frame, sampled molecule) entry
 // of `tab` = (frame, distinct index, solute molecule).  Clears the molecule's
 // entry of the slot table when done (it was set by k_frame_consts).
-__device__ __forceinline__ void k_bulk_body(const uint3 blockIdx, const dim3 gridDim, const DevSys S, Bufs B, const int4 *__restrict__ tab) {
+__device__ __forceinline__ void k_bulk_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, const int4 *__restrict__ tab) {
     __shared__ int wsum[32];
     __shared__ int carry;
     const int4 e = tab[blockIdx.x];
@@ -1487,7 +1487,7 @@ __global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
 //   eps = u64 (512 + 4 (apv + aps in the molecule layout)) M
 // of the real distance.  The FP32 band is delta + eps; the FP64 search uses
 // eps as its band, so both decide every count from the exact distance.
-__device__ __forceinline__ void k_frame_consts_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int pairs) {
+__device__ __forceinline__ void k_frame_consts_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int pairs) {
     const int f = blockIdx.x;
     const FrameGeom &G = B.G[f];
     FrameScratch &F = B.FS[f];
@@ -1637,7 +1637,7 @@ __device__ __forceinline__ int pack_cell(const int *c) { return c[0] | (c[1] << 
 // Solvent atoms binned individually (grid y = frame); molecule-centred data
 // for random insertion.
 template <typename T>
-__device__ __forceinline__ void k_prep_atoms_solvent_body(const uint3 blockIdx, const dim3 gridDim, Bufs B, const T *__restrict__ xyz, int64_t xyz_stride, int iref, int centroids) {
+__device__ __forceinline__ void k_prep_atoms_solvent_body(const uint3 blockIdx, const dim3 gridDim, const Bufs &B, const T *__restrict__ xyz, int64_t xyz_stride, int iref, int centroids) {
     const int f = blockIdx.y;
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= B.mv) return;
@@ -1674,7 +1674,7 @@ __global__ void k_prep_atoms_solvent(Bufs B, const T *__restrict__ xyz, int64_t 
 
 // Solute atoms binned into per-molecule cell lists: key = s * ncell + cell.
 template <typename T>
-__device__ __forceinline__ void k_prep_atoms_solute_body(const uint3 blockIdx, const dim3 gridDim, Bufs B, const T *__restrict__ xyz, int64_t xyz_stride) {
+__device__ __forceinline__ void k_prep_atoms_solute_body(const uint3 blockIdx, const dim3 gridDim, const Bufs &B, const T *__restrict__ xyz, int64_t xyz_stride) {
     const int f = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B.Ns) return;
@@ -1700,7 +1700,7 @@ __global__ void k_prep_atoms_solute(Bufs B, const T *__restrict__ xyz, int64_t x
     k_prep_atoms_solute_body<T>(blockIdx, gridDim, B, xyz, xyz_stride);
 }
 
-__device__ __forceinline__ void k_scatter_atoms_body(const uint3 blockIdx, const dim3 gridDim, Bufs B) {
+__device__ __forceinline__ void k_scatter_atoms_body(const uint3 blockIdx, const dim3 gridDim, const Bufs &B) {
     const int f = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B.Ns) return;
@@ -1793,7 +1793,7 @@ __device__ __forceinline__ void placed_store(const DevSys &S, const Bufs &B, con
 // centre's cell) can hold no pair within the cutoff and is dropped; the others
 // go to the slot list (y * mv + slot, count in counters[5]), so that the FP64
 // placement runs on full warps.
-__device__ __forceinline__ void k_slot_filter_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0) {
+__device__ __forceinline__ void k_slot_filter_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int sample0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= S.mv) return;
     const int y = blockIdx.y;
@@ -1834,7 +1834,7 @@ __global__ void k_slot_filter(DevSys S, Bufs B, int sample0) {
 // written to the placement buffers, and queued for k_atoms_eval when one of
 // their atoms lies in a near cell of the solute molecule: (slot, placed
 // sample, sample, 1).  Persistent grid over the list.
-__device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const dim3 gridDim, DevSys S, Bufs B, int sample0) {
+__device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int sample0) {
     const int n = min(B.counters[5], B.aslot_cap);
     for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
         const int e = B.aslot[it];

@@ -20,7 +20,7 @@
 namespace cmk {
 
 // Arguments of one system's stage (the union of what the stage bodies take).
-struct MArgs {
+struct __align__(16) MArgs {
     DevSys S;
     Bufs B;
     const void *p;   // coordinates (prep), bulk table (k_bulk)
@@ -44,9 +44,7 @@ enum MKid : int {
     MK_SCAN,
     MK_SCATTER_ATOMS,
     MK_ATOMS_NEAR,
-    MK_AGRID_COUNT,
-    MK_AGRID_SCAN,
-    MK_AGRID_FILL,
+    MK_AGRID_BUILD,
     MK_AGRID_REAL,
     MK_AGRID_RANDOM,
     MK_ATOMS_FILTER,
@@ -73,8 +71,7 @@ __host__ __device__ constexpr int mk_threads(int kid) {
          : kid == MK_FRAME_CONSTS ? 128
          : kid == MK_SCAN ? 1024
          : (kid == MK_SCATTER_ATOMS || kid == MK_ATOMS_NEAR) ? 256
-         : (kid == MK_AGRID_COUNT || kid == MK_AGRID_FILL) ? kAgridBuildThreads
-         : kid == MK_AGRID_SCAN ? 1024
+         : kid == MK_AGRID_BUILD ? kAgridBuildThreads
          : (kid == MK_AGRID_REAL || kid == MK_AGRID_RANDOM || kid == MK_ATOMS_FILTER) ? 256
          : (kid == MK_ATOMS_PLACE || kid == MK_SLOT_FILTER) ? 128
          : kid == MK_BULK ? 1024
@@ -94,9 +91,7 @@ __device__ __forceinline__ void mk_body(const uint3 vb, const dim3 vg, const MAr
     else if constexpr (KID == MK_SCAN) k_scan_body(vb, vg, a.B, a.a0);
     else if constexpr (KID == MK_SCATTER_ATOMS) k_scatter_atoms_body(vb, vg, a.B);
     else if constexpr (KID == MK_ATOMS_NEAR) k_atoms_near_body(vb, vg, a.B);
-    else if constexpr (KID == MK_AGRID_COUNT) k_agrid_build_body<false>(vb, vg, a.S, a.B);
-    else if constexpr (KID == MK_AGRID_SCAN) k_agrid_scan_body(vb, vg, a.S, a.B);
-    else if constexpr (KID == MK_AGRID_FILL) k_agrid_build_body<true>(vb, vg, a.S, a.B);
+    else if constexpr (KID == MK_AGRID_BUILD) k_agrid_build_body(vb, vg, a.S, a.B);
     else if constexpr (KID == MK_AGRID_REAL) k_agrid_real_body(vb, vg, a.S, a.B);
     else if constexpr (KID == MK_AGRID_RANDOM) k_agrid_random_body(vb, vg, a.S, a.B, a.a0, a.a1);
     else if constexpr (KID == MK_ATOMS_FILTER) k_atoms_filter_body(vb, vg, a.S, a.B, a.i0, a.i1);
@@ -117,6 +112,10 @@ __host__ __device__ constexpr int mk_min_ctas(int kid) { return mk_threads(kid) 
 template <int KID>
 __global__ void __launch_bounds__(mk_threads(KID), mk_min_ctas(KID))
     k_multi(const MTask *__restrict__ tasks, int ntasks, long long nblocks) {
+    // the entry's arguments in shared memory: the bodies read them from there
+    // as they need them instead of holding copies in registers
+    __shared__ __align__(16) MArgs s_args;
+    static_assert(sizeof(MArgs) % 16 == 0, "MArgs is copied as 16-byte words");
     for (long long vbk = blockIdx.x; vbk < nblocks; vbk += gridDim.x) {
         int lo = 0, hi = ntasks - 1;
         while (lo < hi) {
@@ -125,10 +124,14 @@ __global__ void __launch_bounds__(mk_threads(KID), mk_min_ctas(KID))
             else hi = mid - 1;
         }
         const MTask &t = tasks[lo];
+        for (int w = threadIdx.x; w < (int)(sizeof(MArgs) / 16); w += blockDim.x)
+            reinterpret_cast<int4 *>(&s_args)[w] = reinterpret_cast<const int4 *>(&t.a)[w];
         const long long local = vbk - t.first;
-        const uint3 vb = make_uint3((unsigned)(local % t.grid.x), (unsigned)((local / t.grid.x) % t.grid.y),
-                                    (unsigned)(local / ((long long)t.grid.x * t.grid.y)));
-        mk_body<KID>(vb, dim3(t.grid.x, t.grid.y, t.grid.z), t.a);
+        const uint3 g = t.grid;
+        const uint3 vb = make_uint3((unsigned)(local % g.x), (unsigned)((local / g.x) % g.y),
+                                    (unsigned)(local / ((long long)g.x * g.y)));
+        __syncthreads();
+        mk_body<KID>(vb, dim3(g.x, g.y, g.z), s_args);
         __syncthreads();  // the next block of this CTA reuses its shared memory
     }
 }

@@ -216,7 +216,7 @@ struct cm_handle {
     int atoms_piece = 0;   // samples placed per random-insertion launch
     // candidate grid of a single solute molecule (FP32): agk fine cells per
     // search-cell axis (0: none), gcap entries per frame
-    DevBuf gcount, gstart, gedge, gent;
+    DevBuf gstart, gedge, gpool, gent;
     int agk = 0;
     int64_t gcap = 0;
     int agrid_real_ctas = 1, agrid_rand_ctas = 1;  // resident CTAs per SM of k_agrid_real / k_agrid_random
@@ -666,10 +666,8 @@ void kernel_smem_limits(int device) {
     raise((const void *)k_pairs_edge<false>);
     raise((const void *)k_agrid_real);
     raise((const void *)k_agrid_random);
-    raise((const void *)k_agrid_build<false>);
-    raise((const void *)k_agrid_build<true>);
-    raise((const void *)k_multi<MK_AGRID_COUNT>);
-    raise((const void *)k_multi<MK_AGRID_FILL>);
+    raise((const void *)k_agrid_build);
+    raise((const void *)k_multi<MK_AGRID_BUILD>);
     raise((const void *)k_multi<MK_AGRID_REAL>);
     raise((const void *)k_multi<MK_AGRID_RANDOM>);
     raise((const void *)k_multi<MK_EVAL_REAL_CELL>);
@@ -738,10 +736,9 @@ void ensure_cells(cm_handle *h, int64_t ncell) {
         dev_alloc(h, h->anear, n);
         if (h->agk > 0) {
             const int64_t k3 = (int64_t)h->agk * h->agk * h->agk;
-            const size_t g = (size_t)h->fc * (ncell * k3 * kAgridBuckets + 1) * 4;
-            dev_alloc(h, h->gcount, g);
-            dev_alloc(h, h->gstart, g);
+            dev_alloc(h, h->gstart, (size_t)h->fc * ncell * k3 * (kAgridBuckets + 1) * 4);
             dev_alloc(h, h->gedge, (size_t)h->fc * ncell * k3 * sizeof(float2));
+            dev_alloc(h, h->gpool, (size_t)h->fc * 4);
         }
     }
 }
@@ -1073,10 +1070,9 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         B.agk = h->agk;
         if (h->agk > 0) {
             B.gfs = h->ncell_cap * (int64_t)h->agk * h->agk * h->agk;
-            B.gs = B.gfs * kAgridBuckets + 1;
             B.gcap = h->gcap;
-            B.gcount = P<int>(h->gcount);
             B.gstart = P<int>(h->gstart);
+            B.gpool = P<int>(h->gpool);
             B.gedge = P<float2>(h->gedge);
             B.gent = P<float4>(h->gent);
         }
@@ -1108,9 +1104,7 @@ void launch_one(int kid, dim3 g, size_t smem, cudaStream_t st, const MArgs &a) {
     case MK_SCAN: k_scan<<<g, t, smem, st>>>(a.B, a.a0); break;
     case MK_SCATTER_ATOMS: k_scatter_atoms<<<g, t, smem, st>>>(a.B); break;
     case MK_ATOMS_NEAR: k_atoms_near<<<g, t, smem, st>>>(a.B); break;
-    case MK_AGRID_COUNT: k_agrid_build<false><<<g, t, smem, st>>>(a.S, a.B); break;
-    case MK_AGRID_SCAN: k_agrid_scan<<<g, t, smem, st>>>(a.S, a.B); break;
-    case MK_AGRID_FILL: k_agrid_build<true><<<g, t, smem, st>>>(a.S, a.B); break;
+    case MK_AGRID_BUILD: k_agrid_build<<<g, t, smem, st>>>(a.S, a.B); break;
     case MK_AGRID_REAL: k_agrid_real<<<g, t, smem, st>>>(a.S, a.B); break;
     case MK_AGRID_RANDOM: k_agrid_random<<<g, t, smem, st>>>(a.S, a.B, a.a0, a.a1); break;
     case MK_ATOMS_FILTER: k_atoms_filter<<<g, t, smem, st>>>(a.S, a.B, a.i0, a.i1); break;
@@ -1237,16 +1231,15 @@ void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, c
     };
     if (agrid) {
         // the single solute molecule's candidate lists of every frame
-        const dim3 gb(c.ncell_max, nf);
-        const size_t bsm = (size_t)kAgridStage * sizeof(float4);
-        em.kernel(MK_AGRID_COUNT, gb, bsm, CM_K_CELLS, base);
-        em.kernel(MK_AGRID_SCAN, dim3(nf), 0, CM_K_CELLS, base);
-        em.kernel(MK_AGRID_FILL, gb, bsm, CM_K_CELLS, base);
+        em.zero(B.gpool, (size_t)nf * sizeof(int));
+        em.kernel(MK_AGRID_BUILD, dim3(c.ncell_max, nf), (size_t)kAgridStage * sizeof(float4), CM_K_CELLS, base);
         // real pass: every solvent molecule queried; records inside the band
         // (and frames without a grid) go to the evaluation queue
         em.zero(B.counters + 2, sizeof(int));
         em.kernel(MK_AGRID_REAL, dim3(agrid_grid((int64_t)nf * mv, h->agrid_real_ctas)), hsm, CM_K_REAL, base);
-        em.kernel(eval_kid(h, false), dim3(wgrid_for((int64_t)nf * mv)), hsm, CM_K_REAL, base);
+        // the queue holds the records inside the band (about 1 %) unless a
+        // frame lost its grid: a grid for one entry per 32 molecules
+        em.kernel(eval_kid(h, false), dim3(wgrid_for((int64_t)nf * mv / 32)), hsm, CM_K_REAL, base);
     } else {
         // real pass: molecule pairs that can hold a pair within the cutoff,
         // in pieces of the queue's capacity
@@ -1272,7 +1265,7 @@ void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, c
             else
                 em.kernel(MK_ATOMS_PLACE, dim3((unsigned)std::min<int64_t>(grid_for((int64_t)ny * mv, 128), (int64_t)sms * 16)),
                           0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
-            em.kernel(eval_kid(h, true), dim3(wgrid_for((int64_t)ny * mv)), hsm, CM_K_RANDOM, base);
+            em.kernel(eval_kid(h, true), dim3(wgrid_for((int64_t)ny * mv / (agrid ? 32 : 1))), hsm, CM_K_RANDOM, base);
         }
     }
 }
@@ -2130,9 +2123,7 @@ void launch_multi(int kid, unsigned grid, size_t smem, cudaStream_t st, const MT
         CM_MK(MK_SCAN)
         CM_MK(MK_SCATTER_ATOMS)
         CM_MK(MK_ATOMS_NEAR)
-        CM_MK(MK_AGRID_COUNT)
-        CM_MK(MK_AGRID_SCAN)
-        CM_MK(MK_AGRID_FILL)
+        CM_MK(MK_AGRID_BUILD)
         CM_MK(MK_AGRID_REAL)
         CM_MK(MK_AGRID_RANDOM)
         CM_MK(MK_ATOMS_FILTER)
@@ -2226,14 +2217,21 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
         size_t nsteps = 0;
         for (size_t i = 0; i < n; ++i) nsteps = std::max(nsteps, rec[j][i].size());
         for (size_t k = 0; k < nsteps; ++k) {
-            // the kernels of this stage across the systems, in order of first appearance
-            std::vector<int> kids;
+            // the kernels of this stage across the systems, in order of first
+            // appearance, each with the systems' shared memory in 32 KB classes:
+            // a launch asks for its largest class, and a system with a small
+            // histogram does not lower the occupancy of those with none
+            auto smem_class = [](size_t b) { return (int)((b + 32767) / 32768); };
+            std::vector<std::pair<int, int>> kids;
             bool zero = false;
             for (size_t i = 0; i < n; ++i) {
                 if (rec[j][i].size() <= k) continue;
                 const Step &s = rec[j][i][k];
                 if (!s.kernel) zero = true;
-                else if (std::find(kids.begin(), kids.end(), s.kid) == kids.end()) kids.push_back(s.kid);
+                else {
+                    const std::pair<int, int> key(s.kid, smem_class(s.smem));
+                    if (std::find(kids.begin(), kids.end(), key) == kids.end()) kids.push_back(key);
+                }
             }
             if (zero) {
                 std::vector<MZero> zs;
@@ -2245,14 +2243,16 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
                 plan.push_back(L);
                 continue;
             }
-            for (int kid : kids) {
+            for (const auto &key : kids) {
                 Launch L{};
                 L.kernel = 1;
-                L.kid = kid;
+                L.kid = key.first;
                 std::vector<MTask> ts;
                 long long blocks = 0;
                 for (size_t i = 0; i < n; ++i) {
-                    if (rec[j][i].size() <= k || rec[j][i][k].kid != kid) continue;
+                    if (rec[j][i].size() <= k || rec[j][i][k].kid != key.first ||
+                        smem_class(rec[j][i][k].smem) != key.second)
+                        continue;
                     const Step &s = rec[j][i][k];
                     MTask t;
                     t.a = s.a;
