@@ -33,11 +33,11 @@
 //
 // Kernels: k_agrid_build (the lists of every frame, one CTA per search cell,
 // space reserved in a per-frame pool; a frame whose pool runs out loses its
-// grid), k_agrid_real (real pass) and k_agrid_random (random insertion:
-// placement and query of the slots k_slot_filter listed, nothing written for
-// slots decided at once).  Frames without a grid take the walk path through
-// the same two kernels, which then queue their molecule pairs for
-// k_atoms_eval as k_atoms_filter and k_atoms_place do.
+// grid), k_agrid_real (real pass) and k_agrid_random (random insertion: the
+// queries of the slots k_slot_filter listed and k_atoms_place placed).
+// Frames without a grid take the walk path: k_agrid_real queues their
+// molecule pairs for k_atoms_eval as k_atoms_filter does, and k_atoms_place
+// queues their slots.
 #pragma once
 #include "cm_atoms32.cuh"
 
@@ -180,7 +180,11 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         const float4 o = off[s_oi[lo]];
         return make_float4(q.x + o.x, q.y + o.y, q.z + o.z, q.w);
     };
-    const FineCells fc = fine_cells(G, F, K);
+    // the fine-cell geometry once per CTA (FP64 work), shared
+    __shared__ FineCells s_fc;
+    if (t == 0) s_fc = fine_cells(G, F, K);
+    __syncthreads();
+    const FineCells fc = s_fc;
     auto centre = [&](int g, float *cen) {
         const float u0 = ((float)(g % K) + 0.5f), u1 = ((float)((g / K) % K) + 0.5f), u2 = ((float)(g / (K * K)) + 0.5f);
         for (int r = 0; r < 3; ++r) cen[r] = fmaf(fc.e[6 + r], u2, fmaf(fc.e[3 + r], u1, fc.e[r] * u0));
@@ -565,12 +569,13 @@ __global__ void __launch_bounds__(256) k_agrid_real(DevSys S, Bufs B) {
     k_agrid_real_body(blockIdx, gridDim, S, B);
 }
 
-// Random insertion of a single solute molecule, second pass: one thread per
-// slot of the list k_slot_filter made (slots of samples sample0 .. that can
-// reach the solute), persistent grid.  The slot is drawn and placed as
-// k_atoms_place does (the same helpers); with a grid its sites are queried at
-// once and only a record inside the band is written out and queued; frames
-// without a grid write and queue every slot with an atom in a near cell.
+// Random insertion of a single solute molecule, third pass: one thread per
+// slot of the list k_slot_filter made, after k_atoms_place has placed them
+// (FP64, on full warps) into the placement buffers; persistent grid.  In a
+// frame with a grid the slot's sites are queried and the record is decided at
+// once, or queued for k_atoms_eval when it lies inside the band (its placement
+// is in the buffers); k_atoms_place has queued the near slots of the other
+// frames.
 __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int sample0, int ny) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
@@ -584,60 +589,29 @@ __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const 
     for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
         const int e = B.aslot[it];
         const int y = e / S.mv, k = e - y * S.mv;
-        const Sample sm = B.samples[sample0 + y];
-        const int f = sm.pad;
-        const FrameGeom &G = B.G[f];
+        const int f = B.samples[sample0 + y].pad;
         const FrameScratch &F = B.FS[f];
+        if (!F.agrid) continue;
+        const FrameGeom &G = B.G[f];
         const int64_t base = (int64_t)y * B.Nv + (int64_t)k * apv;
-        const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
-                                           B.nbulk + (int64_t)f * B.ndist);
-        int c0[3];
-        double q0[3];
-        bin_fractional(G, P.fc, c0, q0);
-        const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
-        uint64_t rs = P.st;
-        double A[9];
-        draw_rotation(rs, A);
-        const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
-        const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * apv;
-        bool queue;
-        if (F.agrid) {
-            Top2 T;
-            top2_init(T);
-            long long ev = 0;
-            const float band = F.g.two_delta + 1e-3f * (1.0f + (float)S.cut);
-            for (int b = 0; b < apv; ++b) {
-                int c[3];
-                double q[3];
-                placed_atom(G, F, off64, A, u[b], c0, q0, P.fc, c, q);
-                agrid_query(B, G, F, f, pack_cell(c), make_float4((float)q[0], (float)q[1], (float)q[2], 0.f), b,
-                            b == iref, band, T, ev);
-            }
-            if (ev == 0) continue;
-            st.atompairs += (unsigned long long)ev;
-            DirRec r;
-            const int res = agrid_decide(S, F.g, T, (int64_t)k * apv, r);
-            queue = res == 2;
-            if (!queue) {
-                st.molpairs++;
-                if (res == 1) {
-                    apply_hit(S, h, true, r.bin, r.i_local, r.j, r.ref, r.rbin);
-                    st.hits++;
-                }
-            }
-        } else {
-            // the walk path: queue the slot if one of its atoms lies in a near cell
-            queue = false;
-            for (int b = 0; b < apv && !queue; ++b) {
-                int c[3];
-                double q[3];
-                placed_atom(G, F, off64, A, u[b], c0, q0, P.fc, c, q);
-                queue = nm[(c[2] * G.n[1] + c[1]) * G.n[0] + c[0]] != 0;
-            }
-        }
-        if (queue) {
-            placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
+        Top2 T;
+        top2_init(T);
+        long long ev = 0;
+        const float band = F.g.two_delta + 1e-3f * (1.0f + (float)S.cut);
+        for (int b = 0; b < apv; ++b)
+            agrid_query(B, G, F, f, B.pcell[base + b], B.pq32[base + b], b, b == iref, band, T, ev);
+        if (ev == 0) continue;
+        st.atompairs += (unsigned long long)ev;
+        DirRec r;
+        const int res = agrid_decide(S, F.g, T, (int64_t)k * apv, r);
+        if (res == 2) {
             atoms_push(S, B, make_int4(k, y, sample0 + y, 1));
+            continue;
+        }
+        st.molpairs++;
+        if (res == 1) {
+            apply_hit(S, h, true, r.bin, r.i_local, r.j, r.ref, r.rbin);
+            st.hits++;
         }
     }
     stats_flush(S, st, true);

@@ -1771,7 +1771,9 @@ __device__ __forceinline__ void placed_atom(const FrameGeom &G, const FrameScrat
     }
 }
 
-// Every atom of a placed slot into the placement buffers at `base`.
+// Every atom of a placed slot into the placement buffers at `base` (the FP64
+// positions only for the FP64 search: the FP32 search and its exact scans
+// read the FP32 ones and draw the exact placement again).
 __device__ __forceinline__ void placed_store(const DevSys &S, const Bufs &B, const FrameGeom &G, const FrameScratch &F,
                                              const d4 *off64, const double *A, const d4 *u, const int *c0,
                                              const double *q0, const double *fc, int64_t base) {
@@ -1781,7 +1783,7 @@ __device__ __forceinline__ void placed_store(const DevSys &S, const Bufs &B, con
         placed_atom(G, F, off64, A, u[b], c0, q0, fc, c, q);
         B.pcell[base + b] = pack_cell(c);
         B.pq32[base + b] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
-        B.pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
+        if (!S.fp32) B.pq64[base + b] = make_d4(q[0], q[1], q[2], 0.0);
     }
 }
 
@@ -1830,10 +1832,12 @@ __global__ void k_slot_filter(DevSys S, Bufs B, int sample0) {
     k_slot_filter_body(blockIdx, gridDim, S, B, sample0);
 }
 
-// Second pass of the walk path: the listed slots placed (FP64, the same draws),
-// written to the placement buffers, and queued for k_atoms_eval when one of
-// their atoms lies in a near cell of the solute molecule: (slot, placed
-// sample, sample, 1).  Persistent grid over the list.
+// Second pass: the listed slots placed (FP64, the same draws, on full warps),
+// written to the placement buffers, and -- in frames without a candidate grid
+// -- queued for k_atoms_eval when one of their atoms lies in a near cell of
+// the solute molecule: (slot, placed sample, sample, 1).  The grid's frames
+// are queried by k_agrid_random, which reads these positions.  Persistent
+// grid over the list.
 __device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int sample0) {
     const int n = min(B.counters[5], B.aslot_cap);
     for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
@@ -1857,6 +1861,7 @@ __device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const d
         const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
         const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
         placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
+        if (F.agrid) continue;
         bool near = false;
         for (int b = 0; b < S.apv && !near; ++b) {
             const int pc = B.pcell[base + b];

@@ -1257,14 +1257,14 @@ void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, c
             const int ny = std::min(h->atoms_piece, c.nsmp - s0);
             // the evaluation queue and the slot list (counters 2 .. 5)
             em.zero(B.counters + 2, 4 * sizeof(int));
-            // slots that can reach the solute, then their FP64 placement on full warps
+            // slots that can reach the solute, their FP64 placement on full
+            // warps, then (candidate grid) their queries
             em.kernel(MK_SLOT_FILTER, dim3(grid_for(mv, 128), ny), 0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
+            em.kernel(MK_ATOMS_PLACE, dim3((unsigned)std::min<int64_t>(grid_for((int64_t)ny * mv, 128), (int64_t)sms * 16)),
+                      0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
             if (agrid)
                 em.kernel(MK_AGRID_RANDOM, dim3(agrid_grid((int64_t)ny * mv, h->agrid_rand_ctas)), hsm, CM_K_RANDOM,
                           args(nullptr, 0, 0, c.smp0 + s0, ny));
-            else
-                em.kernel(MK_ATOMS_PLACE, dim3((unsigned)std::min<int64_t>(grid_for((int64_t)ny * mv, 128), (int64_t)sms * 16)),
-                          0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
             em.kernel(eval_kid(h, true), dim3(wgrid_for((int64_t)ny * mv / (agrid ? 32 : 1))), hsm, CM_K_RANDOM, base);
         }
     }
