@@ -2181,6 +2181,12 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
             if ((h->class_open && c.weight != h->class_w) || c.weight != st[i].chunks[0].weight) return false;
         nchunks = std::max(nchunks, st[i].chunks.size());
     }
+    // one shared-memory size for every system's stage: the group histograms go
+    // to global memory (their credits are a few per record), the privatised
+    // MDDF and RDF rows stay in shared memory, so the systems' launches of a
+    // stage need not be split by shared-memory class
+    for (size_t i = 0; i < n; ++i)
+        if (active[i]) bt->hs[i]->smem_groups = 0;
     // rec[j][i]: the stages of system i's chunk j
     std::vector<std::vector<std::vector<Step>>> rec(nchunks, std::vector<std::vector<Step>>(n));
     for (size_t j = 0; j < nchunks; ++j) {
