@@ -2203,6 +2203,15 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
             }
         }
     }
+    // the systems in order of decreasing size: a fused launch dispatches its
+    // blocks roughly in table order, so the largest systems' work starts
+    // first and the smaller ones fill the SMs as it drains
+    std::vector<size_t> order;
+    for (size_t i = 0; i < n; ++i)
+        if (active[i]) order.push_back(i);
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return bt->hs[a]->Ns + bt->hs[a]->Nv > bt->hs[b]->Ns + bt->hs[b]->Nv;
+    });
     // the work tables of the round, laid out in one pinned buffer
     struct Launch {
         int kernel, kid;
@@ -2241,7 +2250,7 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
             }
             if (zero) {
                 std::vector<MZero> zs;
-                for (size_t i = 0; i < n; ++i)
+                for (size_t i : order)
                     if (rec[j][i].size() > k) zs.push_back({rec[j][i][k].zp, (long long)rec[j][i][k].zbytes});
                 Launch L{};
                 L.n = (int)zs.size();
@@ -2255,7 +2264,7 @@ bool batch_round_fused(cm_batch *bt, std::vector<Staged> &st, const std::vector<
                 L.kid = key.first;
                 std::vector<MTask> ts;
                 long long blocks = 0;
-                for (size_t i = 0; i < n; ++i) {
+                for (size_t i : order) {
                     if (rec[j][i].size() <= k || rec[j][i][k].kid != key.first ||
                         smem_class(rec[j][i][k].smem) != key.second)
                         continue;
