@@ -795,8 +795,11 @@ def main():
     # algorithmic bytes of the real pass per frame: the FP32 molecule table
     # (centroid float4) and atom offsets (float4) it reads
     bytes_frame = 16.0 * NMOLS + 16.0 * NMOLS * APM
+    # the self-MDDF real pass: home-cell tiles unless --real-pass warp
+    tiled = args.real_pass != "warp"
     roofline = {
-        "bound": "fp32", "kernel": "k_pairs_flat32<self, 14> (one launch per chunk of 32 frames)",
+        "bound": "fp32",
+        "kernel": ("k_pairs_tile32<14>" if tiled else "k_pairs_flat32<self, 14>") + " (one launch per chunk of 32 frames)",
         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
         "peak_source": "FP32 FMA throughput measured by cm_measure_fp32_peak on this GPU (of measured)",
         "traffic": None,
@@ -809,7 +812,7 @@ def main():
     }
     # DRAM bytes per launch from the committed ncu capture of this kernel on
     # this workload (first number of the file)
-    traffic_file = os.path.join(ROOT, "profiles", "pairs_flat32_c3_traffic.txt")
+    traffic_file = os.path.join(ROOT, "profiles", "pairs_tile32_c3_traffic.txt" if tiled else "pairs_flat32_c3_traffic.txt")
     if os.path.exists(traffic_file):
         try:
             roofline["traffic"] = float(open(traffic_file).read().split()[0])
