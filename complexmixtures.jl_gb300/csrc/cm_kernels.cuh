@@ -121,6 +121,7 @@ struct FrameScratch {
     float xmax;     // largest |coordinate component| of the frame's input atoms (rounded up)
     int tile;       // self mode, one image per pair, half stencil within kTileCells: the tiled real pass takes the frame
     int agrid;      // ATOMS, one solute molecule: the frame's candidate grid is complete (k_agrid_scan clears it on overflow)
+    int place32;    // ATOMS, FP32 search: random-insertion slots placed in FP32 (placed_store32), the band widened to match
     Guard g;        // FP32 search
     Guard64 g64;    // FP64 search
 };
@@ -1342,6 +1343,48 @@ __device__ __forceinline__ void draw_rotation(uint64_t &st, double *A) {
     cmfeed::eulermat(cb, sb, cg, sg, ct, stt, A);
 }
 
+// cmfeed::angle for the FP32 search: the same draws and the same FP64
+// acceptance test of the point in the unit disk, so the stream advances as
+// there; cos and sin are the FP32 quotients of the same FP64 numerators and
+// r^2, each within 3.01 u (u = 2^-24) of cmfeed::angle's.  2 U - 1 is formed
+// exactly from U's 53-bit integer (the same value as cmfeed's sub(mul(2, U), 1)).
+__device__ __forceinline__ void angle32(uint64_t &st, float &c, float &sn) {
+    for (int t = 0; t < 64; ++t) {
+        const double u = (double)((int64_t)(cmfeed::next(st) >> 11) * 2 - (1LL << 53)) * 0x1.0p-53;
+        const double v = (double)((int64_t)(cmfeed::next(st) >> 11) * 2 - (1LL << 53)) * 0x1.0p-53;
+        const double uu = __dmul_rn(u, u), vv = __dmul_rn(v, v);
+        const double r2 = __dadd_rn(uu, vv);
+        if (r2 > 0.0 && r2 < 1.0) {
+            const double uv = __dmul_rn(u, v);
+            const float rf = (float)r2;
+            c = __fdiv_rn((float)__dsub_rn(uu, vv), rf);
+            sn = __fdiv_rn((float)__dadd_rn(uv, uv), rf);
+            return;
+        }
+    }
+    c = 1.f;
+    sn = 0.f;
+}
+
+// draw_rotation with angle32 and eulermat's products in FP32: every entry
+// within 20 u of the FP64 matrix's (two-factor products 7.01 u, the
+// three-factor sums 19.1 u, from the 3.01 u of the cosines and sines).
+__device__ __forceinline__ void draw_rotation32(uint64_t &st, float *A) {
+    float c1, s1, c2, s2, c3, s3;
+    angle32(st, c1, s1);
+    angle32(st, c2, s2);
+    angle32(st, c3, s3);
+    A[0] = c2 * c3;
+    A[1] = -(c2 * s3);
+    A[2] = s2;
+    A[3] = c1 * s3 + (c3 * s1) * s2;
+    A[4] = c1 * c3 - (s1 * s2) * s3;
+    A[5] = -(c2 * s1);
+    A[6] = s1 * s3 - (c1 * c3) * s2;
+    A[7] = (c1 * s2) * s3 + c3 * s1;
+    A[8] = c1 * c2;
+}
+
 // Images of a placed molecule (centre in fractional coordinates fc) relative
 // to solute molecule s, and its cell-relative position.
 __device__ __forceinline__ Images placed_images(const FrameGeom &G, const FrameScratch &F, int sc, const double *fc,
@@ -1470,7 +1513,11 @@ __global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
 //   |o| <= r (molecule radii), |q_v - q_s| <= Q, |off - q_s| <= Q + OFF,
 //   |D| <= Q + OFF, |t| <= Q + OFF + r_v, |dx| <= cutoff,
 // and D formed either as (q_v - q_s) + off or as q_v + (off - q_s), giving
-// E = u (5Q + 4 OFF + 2 r_v + r_s + cutoff).  The distance is within
+// E = u (5Q + 4 OFF + 2 r_v + r_s + cutoff).  In the ATOMS layout a placed
+// atom of the random insertion is no rounding of an FP64 value: placed_store32
+// forms it in FP32 within u (5Q + 41 r_c) of the FP64 placement (r_c the
+// largest centroid radius), and E adds u (5Q + 44 r_c) in the frames that
+// place in FP32 (F.place32).  The distance is within
 // sqrt(3) E plus 2.5 u d (three roundings of d^2, one of the square root).  The
 // atom-cell layout's displacement (q_a - (q_b - off)) is bounded by the same
 // expression with r = 0.  delta adds 25 % to the bound.
@@ -1562,7 +1609,14 @@ __device__ __forceinline__ void k_frame_consts_body(const uint3 blockIdx, const 
                      2.0 * ((double)F.rmax_s + rc + (double)F.rcmax) + 1.0;
     const double eps = 0x1.0p-53 * (512.0 + 4.0 * (double)(S.apv + (pairs ? S.aps : 0))) * M;
     const double u = 0x1.0p-24;
-    const double E = u * (5.0 * Q + 4.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
+    const double E0 = u * (5.0 * Q + 4.0 * OFF + 2.0 * rv + rs + S.cut + 1.0);
+    // ATOMS frames: the random insertion's slots are placed in FP32 (placed_store32) when
+    // that widens the band by at most 60 % (small molecules); larger molecules have few
+    // slots per atom and more records per slot in a wider band, and keep the FP64 placement
+    const double P = u * (5.0 * Q + 44.0 * (double)F.rcmax);
+    const bool place32 = !pairs && S.fp32 && P <= 0.6 * E0;
+    F.place32 = place32 ? 1 : 0;
+    const double E = E0 + (place32 ? P : 0.0);
     const double delta = 1.25 * (1.7320508075688772 * E + 2.5 * u * (S.cut + 1.0)) + 1e-9 + eps;
     Guard g;
     g.delta = delta;
@@ -1787,6 +1841,39 @@ __device__ __forceinline__ void placed_store(const DevSys &S, const Bufs &B, con
     }
 }
 
+// The FP32 search's placement of a slot: atom offsets rotated by the FP32
+// matrix of draw_rotation32 and moved to the centre (q0 rounded to FP32), the
+// cell chosen as in placed_atom and the FP32 offset of the shift taken off.
+// Each coordinate is within P = u (5 Q + 41 r_c) of placed_atom's FP64 one
+// (the guard band of k_frame_consts adds u (5 Q + 44 r_c)): u Q for q0, 39 u r_c
+// for the rotated offset (entries of A within 20 u, the offsets' rounding, three
+// roundings of the dot product), u (Q + r_c) for the sum t, u (2 Q + r_c) for
+// the shift's offset and u Q for the difference.  False (nothing to trust)
+// when an atom lands beyond the offset table; the caller then places the slot in FP64.
+__device__ __forceinline__ bool placed_store32(const Bufs &B, const FrameScratch &F, const FrameGeom &G,
+                                               const float4 *off32, const float *A, const d4 *u, const int *c0,
+                                               const double *q0, int64_t base, int apv) {
+    const float q0x = (float)q0[0], q0y = (float)q0[1], q0z = (float)q0[2];
+    for (int b = 0; b < apv; ++b) {
+        const d4 w = u[b];
+        const float wx = (float)w.x, wy = (float)w.y, wz = (float)w.z;
+        const float tx = q0x + fmaf(A[2], wz, fmaf(A[1], wy, A[0] * wx));
+        const float ty = q0y + fmaf(A[5], wz, fmaf(A[4], wy, A[3] * wx));
+        const float tz = q0z + fmaf(A[8], wz, fmaf(A[7], wy, A[6] * wx));
+        int dl[3], c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            dl[k] = (int)floorf(fmaf(F.hin[3 * k + 2], tz, fmaf(F.hin[3 * k + 1], ty, F.hin[3 * k] * tx)));
+            if (dl[k] < -kLT || dl[k] > kLT) return false;
+            c[k] = wrap_cell(c0[k] + dl[k], G.n[k]);
+        }
+        const float4 ov = off32[off_index(dl[0], dl[1], dl[2])];
+        B.pcell[base + b] = pack_cell(c);
+        B.pq32[base + b] = make_float4(tx - ov.x, ty - ov.y, tz - ov.z, 0.f);
+    }
+    return true;
+}
+
 // Random-insertion slots of the ATOMS regime, first pass: one thread per
 // slot of samples sample0 .. sample0 + gridDim.y - 1 of the chunk.  Only the
 // slot's draws are taken (the bulk pick and the centre; integer and FP32
@@ -1855,12 +1942,21 @@ __device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const d
         double q0[3];
         bin_fractional(G, P.fc, c0, q0);
         const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
-        uint64_t rs = P.st;
-        double A[9];
-        draw_rotation(rs, A);
         const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
         const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
-        placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
+        bool placed = false;
+        if (F.place32) {
+            uint64_t rs = P.st;
+            float A32[9];
+            draw_rotation32(rs, A32);
+            placed = placed_store32(B, F, G, B.off32 + (int64_t)f * kOffEntries, A32, u, c0, q0, base, S.apv);
+        }
+        if (!placed) {
+            uint64_t rs = P.st;
+            double A[9];
+            draw_rotation(rs, A);
+            placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
+        }
         if (F.agrid) continue;
         bool near = false;
         for (int b = 0; b < S.apv && !near; ++b) {

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 COMMON = dict(binstep=0.02, nbins=350, seed=91)
 
 
-def chain_system(rng, H, n=400, nframes=2, mv=350, apv=3, confined=None):
+def chain_system(rng, H, n=400, nframes=2, mv=350, apv=3, confined=None, spread=0.9):
     steps = rng.normal(size=(n, 3))
     chain = np.cumsum(steps / np.linalg.norm(steps, axis=1, keepdims=True) * 1.53, axis=0)
     if confined is not None:
@@ -26,7 +26,7 @@ def chain_system(rng, H, n=400, nframes=2, mv=350, apv=3, confined=None):
         chain = (chain - chain.mean(axis=0)) * np.minimum(1.0, confined / np.maximum(r, 1e-9))
     chain = chain - chain.mean(axis=0) + H @ np.full(3, 0.5)
     xs = np.stack([chain + rng.normal(scale=0.2, size=chain.shape) for _ in range(nframes)])
-    _, xv, cells = make_system(rng, H, 1, 1, mv, apv, nframes, False)
+    _, xv, cells = make_system(rng, H, 1, 1, mv, apv, nframes, False, spread=spread)
     return xs, xv, cells
 
 
@@ -108,3 +108,21 @@ def test_grid_and_walk_agree_with_stats(cm, orc, gpu_ready):
     for k in KEYS:
         assert np.array_equal(g1[k], g2[k]), k
     assert s1["atom_pairs_evaluated"] < s2["atom_pairs_evaluated"]
+
+
+@pytest.mark.parametrize("apv,grid", [(3, 3), (3, -1), (14, 3)], ids=["water-grid", "water-walk", "large-grid"])
+def test_random_insertion_placement_many_samples(cm, orc, gpu_ready, apv, grid):
+    """Many random samples on fine bins: the random insertion's slots are
+    placed in FP32 for small molecules (the band widened to match) and in FP64
+    for large ones; the counts equal the oracle's bin by bin either way."""
+    rng = np.random.default_rng(17)
+    H = np.diag([32.0, 32.0, 32.0])
+    mv = 1200 // apv
+    # three-site molecules of water's size (centroid radius under 1 A), fourteen-site ones of about 3 A
+    xs, xv, cells = chain_system(rng, H, n=300, nframes=2, mv=mv, apv=apv, spread=0.3 if apv == 3 else 0.9)
+    opt = dict(irefatom=1, cutoff=7.0, dbulk=7.0, usecutoff=False, n_random_samples=24, binstep=0.01, nbins=700,
+               seed=93)
+    got, ref, st = compare(cm, orc, ms=1, aps=300, mv=mv, apv=apv, xs=xs, xv=xv, cells=cells, self_mode=False,
+                           precision="fp32", regime="atoms", groups="custom", dtype=np.float32,
+                           engine_kw=dict(atoms_grid=grid), **opt)
+    assert ref["md_random"].sum() > 0 and st["guard_reevaluations"] > 0
