@@ -23,8 +23,9 @@
 // the guard test only asks that) and the reference site's smallest distance
 // are then the values a walk over every stencil cell gives, and every decision
 // follows the FP32 + guard rules of atoms_decide.  A query whose record lies
-// inside the guard band is queued for k_atoms_eval, which walks the stencil
-// and decides it from exact distances, so the counts stay the oracle's.
+// inside the guard band is decided in place from exact distances
+// (agrid_record), its exact scans reading the same lists, so the counts stay
+// the oracle's.
 //
 // A list entry is the atom's FP32 position from the fine cell's search-cell
 // origin, q_a + off(cell_a - cell), which is the displacement form of the
@@ -443,15 +444,15 @@ __global__ void __launch_bounds__(kAgridBuildThreads) k_agrid_build(DevSys S, Bu
     k_agrid_build_body(blockIdx, gridDim, S, B);
 }
 
-// One site's query: its fine cell from its FP32 position q in search cell
-// (cx, cy, cz), then the top-2 update over the list (p1 holds the solute atom
-// index in the molecule), bucket by bucket of the entries' smallest distance to
-// the fine cell.  A bucket whose smallest distance exceeds the running minimum
-// (for the reference site, also its own minimum) by more than `band` holds no
-// atom that can be the minimum, be within the guard band of it or lower the
-// reference row, and neither do the buckets after it.
-__device__ __forceinline__ void agrid_query(const Bufs &B, const FrameGeom &G, const FrameScratch &F, int f, int packed,
-                                            float4 q, int b, bool isref, float band, Top2 &T, long long &evals) {
+// A site's fine cell (FP32 position q in search cell (cx, cy, cz)): its list's
+// bucket starts and the smallest distance and width of its buckets.
+struct AgridCell {
+    const int *st;  // kAgridBuckets + 1 starts in the frame's entries
+    float lo, w;
+};
+
+__device__ __forceinline__ AgridCell agrid_cell(const Bufs &B, const FrameGeom &G, const FrameScratch &F, int f, int packed,
+                                                float4 q) {
     const int K = B.agk;
     const int cx = packed & 1023, cy = (packed >> 10) & 1023, cz = packed >> 20;
     int gi[3];
@@ -462,15 +463,30 @@ __device__ __forceinline__ void agrid_query(const Bufs &B, const FrameGeom &G, c
     }
     const int64_t fine = (int64_t)((cz * G.n[1] + cy) * G.n[0] + cx) * (K * K * K) + (gi[2] * K + gi[1]) * K + gi[0];
     const float2 edge = B.gedge[(int64_t)f * B.gfs + fine];
-    const int *st = B.gstart + ((int64_t)f * B.gfs + fine) * (kAgridBuckets + 1);
-    const float w = (edge.y - edge.x) * (1.0f / (float)kAgridBuckets);
+    AgridCell c;
+    c.st = B.gstart + ((int64_t)f * B.gfs + fine) * (kAgridBuckets + 1);
+    c.lo = edge.x;
+    c.w = (edge.y - edge.x) * (1.0f / (float)kAgridBuckets);
+    return c;
+}
+
+// One site's query: the top-2 update over its fine cell's list (p1 holds the
+// solute atom index in the molecule), bucket by bucket of the entries'
+// smallest distance to the fine cell.  A bucket whose smallest distance
+// exceeds the running minimum (for the reference site, also its own minimum)
+// by more than `band` holds no atom that can be the minimum, be within the
+// guard band of it or lower the reference row, and neither do the buckets
+// after it.
+__device__ __forceinline__ void agrid_query(const Bufs &B, const FrameGeom &G, const FrameScratch &F, int f, int packed,
+                                            float4 q, int b, bool isref, float band, Top2 &T, long long &evals) {
+    const AgridCell c = agrid_cell(B, G, F, f, packed, q);
     const float4 *e = B.gent + (int64_t)f * B.gcap;
-    int i = st[0];
+    int i = c.st[0];
 #pragma unroll 1
     for (int k = 0; k < kAgridBuckets; ++k) {
         const float thr = fmaxf(sqrtf(T.m1), isref ? sqrtf(T.r1) : 0.f) + band;
-        if (fmaf(w, (float)k, edge.x) > thr) break;
-        const int end = st[k + 1];
+        if (fmaf(c.w, (float)k, c.lo) > thr) break;
+        const int end = c.st[k + 1];
         evals += end - i;
         for (; i < end; ++i) {
             const float4 a = e[i];
@@ -486,10 +502,61 @@ __device__ __forceinline__ void agrid_query(const Bufs &B, const FrameGeom &G, c
     }
 }
 
+// Exact scan of a slot's or molecule's sites over their lists: every list
+// entry whose FP32 squared distance is within thr_arg (or, for the reference
+// site, thr_r1) is evaluated exactly (exact_d2 on the input coordinates) and
+// kept by the reference's tie rule -- the pairs of atoms_exact's stencil walk
+// for the same thresholds.  The thresholds come from the query's minima plus
+// 2 delta, so each such atom lies within (nearest distance + 3 delta) of its
+// site, which the list's margin covers, and the buckets past sqrt(thr) + band
+// hold none of them.
+__device__ __noinline__ void agrid_exact(const DevSys &S, const Bufs &B, const FrameGeom &G, const FrameScratch &F, int f,
+                                         ExactMol &X, const int *vc, const float4 *vq, float band, float thr_arg,
+                                         float thr_r1, Best64 &Bst, double &rr1, long long &evals) {
+    best_init(Bst);
+    rr1 = INFINITY;
+    evals = 0;
+    const float4 *e = B.gent + (int64_t)f * B.gcap;
+    for (int b = 0; b < S.apv; ++b) {
+        const bool isref = b == S.iref;
+        const float thr = isref ? fmaxf(thr_arg, thr_r1) : thr_arg;
+        if (!(thr >= 0.f)) continue;
+        const float4 q = vq[b];
+        const AgridCell c = agrid_cell(B, G, F, f, vc[b], q);
+        const float lim = sqrtf(thr) + band;
+        double yb[3];
+        bool have_y = false;
+        int i = c.st[0];
+        for (int k = 0; k < kAgridBuckets; ++k) {
+            if (fmaf(c.w, (float)k, c.lo) > lim) break;
+            const int end = c.st[k + 1];
+            for (; i < end; ++i) {
+                const float4 a = e[i];
+                const float ex = a.x - q.x, ey = a.y - q.y, ez = a.z - q.z;
+                const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                if (!(d2f <= thr_arg || (isref && d2f <= thr_r1))) continue;
+                if (!have_y) {
+                    exact_solvent_atom(B, G, X, b, yb);
+                    have_y = true;
+                }
+                const int ai = __float_as_int(a.w);
+                double xa[3];
+                exact_solute_atom(B, X, ai, xa);
+                const double d2 = exact_d2(G, xa, yb);
+                evals++;
+                if (d2 <= S.cut2) {
+                    if (isref) rr1 = fmin(rr1, d2);
+                    best_update<false>(Bst, d2, ai, b);
+                }
+            }
+        }
+    }
+}
+
 // The record of a query's top-2 when every value is farther than the band
 // from its decision boundary (the unambiguous branch of atoms_decide):
 // 0 = no record within the cutoff, 1 = record r, 2 = inside the band (the
-// pair goes to k_atoms_eval).
+// record is then agrid_record's).
 __device__ __forceinline__ int agrid_decide(const DevSys &S, const Guard &g, const Top2 &T, int64_t vb, DirRec &r) {
     r = dir_none(S);
     if (!(T.m1 <= g.cutp2)) return 0;
@@ -509,6 +576,90 @@ __device__ __forceinline__ int agrid_decide(const DevSys &S, const Guard &g, con
         r.rbin = rb;
     }
     return 1;
+}
+
+// The record of a query inside the band (agrid_decide's 2), decided by
+// atoms_decide's rules with the exact scans over the sites' lists (agrid_exact)
+// instead of the stencil walk: v the solvent molecule (sample < 0) or the
+// slot of sample `sample`, whose placement is drawn again in FP64.
+__device__ __noinline__ DirRec agrid_record(const DevSys &S, const Bufs &B, const FrameGeom &G, const FrameScratch &F,
+                                            int f, int v, int sample, const int *vc, const float4 *vq, const Top2 &T,
+                                            LocalStats &st) {
+    const Guard &g = F.g;
+    const float band = g.two_delta + 1e-3f * (1.0f + (float)S.cut);
+    const int64_t vb = (int64_t)v * S.apv;
+    ExactMol X;
+    if (sample < 0) {
+        X = exact_mol(S, f, 0, v);
+    } else {
+        const Sample sm = B.samples[sample];
+        const Placement P = draw_placement(S, G.frame_id, sm, v, B.bulk + (int64_t)f * B.ndist * B.mv,
+                                           B.nbulk + (int64_t)f * B.ndist);
+        uint64_t rs = P.st;
+        double R[9];
+        draw_rotation(rs, R);
+        X = exact_mol_placed(S, G, f, sm.s, P.jmol, P.fc, R);
+    }
+    DirRec r = dir_none(S);
+    if (!(T.m1 <= g.cutp2)) return r;
+    const float d1 = sqrtf(T.m1);
+    if (T.m1 >= g.cutm2 || (sqrtf(T.m2) - d1) <= g.two_delta) {
+        const float thr1 = T.r1 <= g.cutp2 ? r_sq_ru(sqrtf(T.r1) + g.two_delta) : -1.f;
+        Best64 Bst;
+        double rr1;
+        long long ev;
+        agrid_exact(S, B, G, F, f, X, vc, vq, band, r_sq_ru(d1 + g.two_delta), thr1, Bst, rr1, ev);
+        st.guard++;
+        st.guard_pairs += ev;
+        if (Bst.d2 <= S.cut2) {
+            const double d = best_d(Bst);
+            st.maxerr = fmax(st.maxerr, fabs((double)d1 - d));
+            r.within = 1;
+            r.i_local = Bst.a;
+            r.j = vb + Bst.b;
+            r.bin = setbin0(d, S.binstep);
+            r.bulk = inbulk64(S, true, d);
+            if (rr1 <= S.cut2) {
+                r.ref = 1;
+                r.rbin = setbin0(sqrt(rr1), S.binstep);
+            }
+        }
+        return r;
+    }
+    // the search's minimum pair is the exact minimum pair
+    int bin = bin_of(g, d1);
+    double d64 = -1.0;
+    if (bin < 0 || (S.usecutoff && d1 >= g.dbulk_lo && d1 <= g.dbulk_hi)) {
+        d64 = sqrt(exact_pair_d2(B, G, X, T.p1, T.b1));
+        bin = setbin0(d64, S.binstep);
+        st.guard++;
+        st.guard_pairs++;
+        st.maxerr = fmax(st.maxerr, fabs((double)d1 - d64));
+    }
+    r.within = 1;
+    r.i_local = T.p1;
+    r.j = vb + T.b1;
+    r.bin = bin;
+    r.bulk = S.usecutoff ? (d64 >= 0.0 ? (d64 > S.dbulk) : (d1 > g.dbulk_hi)) : 0;
+    if (T.r1 <= g.cutp2) {
+        const int rb = T.r1 < g.cutm2 ? bin_of(g, sqrtf(T.r1)) : -1;
+        if (rb >= 0) {
+            r.ref = 1;
+            r.rbin = rb;
+        } else {
+            Best64 Bst;
+            double rr1;
+            long long ev;
+            agrid_exact(S, B, G, F, f, X, vc, vq, band, -1.f, r_sq_ru(sqrtf(T.r1) + g.two_delta), Bst, rr1, ev);
+            st.guard++;
+            st.guard_pairs += ev;
+            if (rr1 <= S.cut2) {
+                r.ref = 1;
+                r.rbin = setbin0(sqrt(rr1), S.binstep);
+            }
+        }
+    }
+    return r;
 }
 
 // Real pass of a single solute molecule, one thread per (frame, solvent
@@ -545,13 +696,9 @@ __device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const di
         if (ev == 0) continue;
         st.atompairs += (unsigned long long)ev;
         DirRec r;
-        const int res = agrid_decide(S, F.g, T, (int64_t)v * apv, r);
-        if (res == 2) {
-            atoms_push(S, B, make_int4(v, 0, f, 0));
-            continue;
-        }
+        if (agrid_decide(S, F.g, T, (int64_t)v * apv, r) == 2) r = agrid_record(S, B, G, F, f, v, -1, vc, vq, T, st);
         st.molpairs++;
-        if (res == 1) {
+        if (r.within) {
             apply_hit(S, h, false, r.bin, r.i_local, r.j, r.ref, r.rbin);
             st.hits++;
             if (B.slot) {
@@ -571,11 +718,10 @@ __global__ void __launch_bounds__(256) k_agrid_real(DevSys S, Bufs B) {
 
 // Random insertion of a single solute molecule, third pass: one thread per
 // slot of the list k_slot_filter made, after k_atoms_place has placed them
-// (FP64, on full warps) into the placement buffers; persistent grid.  In a
-// frame with a grid the slot's sites are queried and the record is decided at
-// once, or queued for k_atoms_eval when it lies inside the band (its placement
-// is in the buffers); k_atoms_place has queued the near slots of the other
-// frames.
+// into the placement buffers; persistent grid.  In a frame with a grid the
+// slot's sites are queried and the record is decided at once (agrid_record
+// inside the band); k_atoms_place has queued the near slots of the other
+// frames for k_atoms_eval.
 __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const dim3 gridDim, const DevSys &S, const Bufs &B, int sample0, int ny) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hbase = (unsigned int *)smem_raw;
@@ -603,13 +749,10 @@ __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const 
         if (ev == 0) continue;
         st.atompairs += (unsigned long long)ev;
         DirRec r;
-        const int res = agrid_decide(S, F.g, T, (int64_t)k * apv, r);
-        if (res == 2) {
-            atoms_push(S, B, make_int4(k, y, sample0 + y, 1));
-            continue;
-        }
+        if (agrid_decide(S, F.g, T, (int64_t)k * apv, r) == 2)
+            r = agrid_record(S, B, G, F, f, k, sample0 + y, B.pcell + base, B.pq32 + base, T, st);
         st.molpairs++;
-        if (res == 1) {
+        if (r.within) {
             apply_hit(S, h, true, r.bin, r.i_local, r.j, r.ref, r.rbin);
             st.hits++;
         }
