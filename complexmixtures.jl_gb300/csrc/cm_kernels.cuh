@@ -398,6 +398,7 @@ struct Bufs {
     float4 *avq32;
     d4 *avq64;
     d4 *u64;                        // [nf][Nv]
+    float4 *u32;                    // [nf][Nv] FP32 copies of u64 (the FP32 placement)
     float *rc;                      // [nf][mv]
     int *pcell;                     // [placed samples][Nv]
     float4 *pq32;
@@ -1343,37 +1344,15 @@ __device__ __forceinline__ void draw_rotation(uint64_t &st, double *A) {
     cmfeed::eulermat(cb, sb, cg, sg, ct, stt, A);
 }
 
-// cmfeed::angle for the FP32 search: the same draws and the same FP64
-// acceptance test of the point in the unit disk, so the stream advances as
-// there; cos and sin are the FP32 quotients of the same FP64 numerators and
-// r^2, each within 3.01 u (u = 2^-24) of cmfeed::angle's.  2 U - 1 is formed
-// exactly from U's 53-bit integer (the same value as cmfeed's sub(mul(2, U), 1)).
-__device__ __forceinline__ void angle32(uint64_t &st, float &c, float &sn) {
-    for (int t = 0; t < 64; ++t) {
-        const double u = (double)((int64_t)(cmfeed::next(st) >> 11) * 2 - (1LL << 53)) * 0x1.0p-53;
-        const double v = (double)((int64_t)(cmfeed::next(st) >> 11) * 2 - (1LL << 53)) * 0x1.0p-53;
-        const double uu = __dmul_rn(u, u), vv = __dmul_rn(v, v);
-        const double r2 = __dadd_rn(uu, vv);
-        if (r2 > 0.0 && r2 < 1.0) {
-            const double uv = __dmul_rn(u, v);
-            const float rf = (float)r2;
-            c = __fdiv_rn((float)__dsub_rn(uu, vv), rf);
-            sn = __fdiv_rn((float)__dadd_rn(uv, uv), rf);
-            return;
-        }
-    }
-    c = 1.f;
-    sn = 0.f;
-}
-
-// draw_rotation with angle32 and eulermat's products in FP32: every entry
-// within 20 u of the FP64 matrix's (two-factor products 7.01 u, the
-// three-factor sums 19.1 u, from the 3.01 u of the cosines and sines).
+// draw_rotation for the FP32 search: cmfeed::angle32's (cos, sin) (the same
+// draws and acceptance as cmfeed::angle, within 3.01 u of its values, u =
+// 2^-24) and eulermat's products in FP32: every entry within 20 u of the FP64
+// matrix's (two-factor products 7.01 u, the three-factor sums 19.1 u).
 __device__ __forceinline__ void draw_rotation32(uint64_t &st, float *A) {
     float c1, s1, c2, s2, c3, s3;
-    angle32(st, c1, s1);
-    angle32(st, c2, s2);
-    angle32(st, c3, s3);
+    cmfeed::angle32(st, c1, s1);
+    cmfeed::angle32(st, c2, s2);
+    cmfeed::angle32(st, c3, s3);
     A[0] = c2 * c3;
     A[1] = -(c2 * s3);
     A[2] = s2;
@@ -1383,6 +1362,38 @@ __device__ __forceinline__ void draw_rotation32(uint64_t &st, float *A) {
     A[6] = s1 * s3 - (c1 * c3) * s2;
     A[7] = (c1 * s2) * s3 + c3 * s1;
     A[8] = c1 * c2;
+}
+
+// draw_placement's draws as integers: the bulk pick and the centre's three
+// 53-bit uniforms U_q = fk[q] 2^-53; returns the stream state after them
+// (the angles follow).
+__device__ __forceinline__ uint64_t draw_slot_bits(const DevSys &S, int64_t frame_id, const Sample &sm, int k,
+                                                   const int *bulk, const int *nbulk, int &jmol, uint64_t *fk) {
+    uint64_t st = cmfeed::key(S.seed, cmfeed::kTagSlot, (uint64_t)frame_id, (uint64_t)sm.s,
+                              ((uint64_t)(uint32_t)sm.rep << 32) | (uint64_t)(uint32_t)k);
+    const int nb = nbulk[sm.d];
+    if (nb > 0) jmol = bulk[(int64_t)sm.d * S.mv + (int64_t)cmfeed::below(st, (uint64_t)nb)];
+    else jmol = (int)cmfeed::below(st, (uint64_t)S.mv);
+    for (int q = 0; q < 3; ++q) fk[q] = cmfeed::next(st) >> 11;
+    return st;
+}
+
+// The centre's cell and its FP32 position from that cell's origin, from the
+// 53-bit uniforms: c = floor(U n) and g = U n - c exactly (integer product
+// fk n < 2^63), q0 = Hn g in FP64, rounded to FP32.
+__device__ __forceinline__ void centre32(const FrameGeom &G, const uint64_t *fk, int *c0, float *q0) {
+    double g[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const uint64_t kn = fk[q] * (uint64_t)G.n[q];
+        c0[q] = (int)(kn >> 53);
+        g[q] = (double)(kn & ((1ull << 53) - 1)) * 0x1.0p-53;
+    }
+    double v[3];
+    matvec_cm(G.Hn, g[0], g[1], g[2], v);
+    q0[0] = (float)v[0];
+    q0[1] = (float)v[1];
+    q0[2] = (float)v[2];
 }
 
 // Images of a placed molecule (centre in fractional coordinates fc) relative
@@ -1716,6 +1727,10 @@ __device__ __forceinline__ void k_prep_atoms_solvent_body(const uint3 blockIdx, 
     if (centroids) {
         float r;
         centroid_data(G, x, apm, iref, B.u64 + fo + (int64_t)m * apm, r);
+        for (int b = 0; b < apm; ++b) {
+            const d4 w = B.u64[fo + (int64_t)m * apm + b];
+            B.u32[fo + (int64_t)m * apm + b] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
+        }
         B.rc[(int64_t)f * B.mv + m] = r;
         atomic_max_pos(&B.FS[f].rcmax, r);
     }
@@ -1841,25 +1856,24 @@ __device__ __forceinline__ void placed_store(const DevSys &S, const Bufs &B, con
     }
 }
 
-// The FP32 search's placement of a slot: atom offsets rotated by the FP32
-// matrix of draw_rotation32 and moved to the centre (q0 rounded to FP32), the
-// cell chosen as in placed_atom and the FP32 offset of the shift taken off.
-// Each coordinate is within P = u (5 Q + 41 r_c) of placed_atom's FP64 one
-// (the guard band of k_frame_consts adds u (5 Q + 44 r_c)): u Q for q0, 39 u r_c
-// for the rotated offset (entries of A within 20 u, the offsets' rounding, three
-// roundings of the dot product), u (Q + r_c) for the sum t, u (2 Q + r_c) for
-// the shift's offset and u Q for the difference.  False (nothing to trust)
-// when an atom lands beyond the offset table; the caller then places the slot in FP64.
+// The FP32 search's placement of a slot: the molecule-centred atom offsets
+// (FP32 copies u32) rotated by the FP32 matrix of draw_rotation32 and moved to
+// the centre (centre32), the cell chosen as in placed_atom and the FP32
+// offset of the shift taken off.  Each coordinate is within P = u (5 Q + 41 r_c)
+// of placed_atom's FP64 one (the guard band of k_frame_consts adds
+// u (5 Q + 44 r_c)): u Q for q0, 39 u r_c for the rotated offset (entries of A
+// within 20 u, the offsets' rounding, three roundings of the dot product),
+// u (Q + r_c) for the sum t, u (2 Q + r_c) for the shift's offset and u Q for
+// the difference.  False when an atom lands beyond the offset table; the
+// caller then places the slot in FP64.
 __device__ __forceinline__ bool placed_store32(const Bufs &B, const FrameScratch &F, const FrameGeom &G,
-                                               const float4 *off32, const float *A, const d4 *u, const int *c0,
-                                               const double *q0, int64_t base, int apv) {
-    const float q0x = (float)q0[0], q0y = (float)q0[1], q0z = (float)q0[2];
+                                               const float4 *off32, const float *A, const float4 *u, const int *c0,
+                                               const float *q0, int64_t base, int apv) {
     for (int b = 0; b < apv; ++b) {
-        const d4 w = u[b];
-        const float wx = (float)w.x, wy = (float)w.y, wz = (float)w.z;
-        const float tx = q0x + fmaf(A[2], wz, fmaf(A[1], wy, A[0] * wx));
-        const float ty = q0y + fmaf(A[5], wz, fmaf(A[4], wy, A[3] * wx));
-        const float tz = q0z + fmaf(A[8], wz, fmaf(A[7], wy, A[6] * wx));
+        const float4 w = u[b];
+        const float tx = q0[0] + fmaf(A[2], w.z, fmaf(A[1], w.y, A[0] * w.x));
+        const float ty = q0[1] + fmaf(A[5], w.z, fmaf(A[4], w.y, A[3] * w.x));
+        const float tz = q0[2] + fmaf(A[8], w.z, fmaf(A[7], w.y, A[6] * w.x));
         int dl[3], c[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -1891,15 +1905,17 @@ __device__ __forceinline__ void k_slot_filter_body(const uint3 blockIdx, const d
     const int f = sm.pad;
     const FrameGeom &G = B.G[f];
     const FrameScratch &F = B.FS[f];
-    const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
-                                       B.nbulk + (int64_t)f * B.ndist);
+    int jmol;
+    uint64_t fk[3];
+    draw_slot_bits(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv, B.nbulk + (int64_t)f * B.ndist, jmol, fk);
     const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
-    const float rc = B.rc[(int64_t)f * B.mv + P.jmol];
+    const float rc = B.rc[(int64_t)f * B.mv + jmol];
     int lo[3], hi[3];
     bool maybe = false;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-        const float g = (float)(P.fc[q] * (double)G.n[q]);  // grid units from the cell's origin
+        // U n in grid units from the grid's origin (FP32 of the exact product fk n 2^-53)
+        const float g = cmfeed::u128_to_f32(0, fk[q] * (uint64_t)G.n[q]) * 0x1.0p-53f;
         const float reach = rc / F.cw[q] + 2e-3f;
         lo[q] = (int)floorf(g - reach);
         hi[q] = (int)floorf(g + reach);
@@ -1935,27 +1951,32 @@ __device__ __forceinline__ void k_atoms_place_body(const uint3 blockIdx, const d
         const FrameGeom &G = B.G[f];
         const FrameScratch &F = B.FS[f];
         const int64_t base = (int64_t)y * B.Nv + (int64_t)k * S.apv;
-        const Placement P = draw_placement(S, G.frame_id, sm, k, B.bulk + (int64_t)f * B.ndist * B.mv,
-                                           B.nbulk + (int64_t)f * B.ndist);
-        // the new centre's cell c0 and its position q0 from that cell's origin
-        int c0[3];
-        double q0[3];
-        bin_fractional(G, P.fc, c0, q0);
+        const int *bulk = B.bulk + (int64_t)f * B.ndist * B.mv, *nbulk = B.nbulk + (int64_t)f * B.ndist;
         const unsigned char *nm = B.anear + (int64_t)f * B.as + (int64_t)sm.s * G.ncell;
-        const d4 *off64 = B.off64 + (int64_t)f * kOffEntries;
-        const d4 *u = B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv;
         bool placed = false;
         if (F.place32) {
-            uint64_t rs = P.st;
+            int jmol;
+            uint64_t fk[3];
+            uint64_t rs = draw_slot_bits(S, G.frame_id, sm, k, bulk, nbulk, jmol, fk);
+            int c0[3];
+            float q0[3];
+            centre32(G, fk, c0, q0);
             float A32[9];
             draw_rotation32(rs, A32);
-            placed = placed_store32(B, F, G, B.off32 + (int64_t)f * kOffEntries, A32, u, c0, q0, base, S.apv);
+            placed = placed_store32(B, F, G, B.off32 + (int64_t)f * kOffEntries, A32,
+                                    B.u32 + (int64_t)f * B.Nv + (int64_t)jmol * S.apv, c0, q0, base, S.apv);
         }
         if (!placed) {
+            const Placement P = draw_placement(S, G.frame_id, sm, k, bulk, nbulk);
+            // the new centre's cell c0 and its position q0 from that cell's origin
+            int c0[3];
+            double q0[3];
+            bin_fractional(G, P.fc, c0, q0);
             uint64_t rs = P.st;
             double A[9];
             draw_rotation(rs, A);
-            placed_store(S, B, G, F, off64, A, u, c0, q0, P.fc, base);
+            placed_store(S, B, G, F, B.off64 + (int64_t)f * kOffEntries, A, B.u64 + (int64_t)f * B.Nv + (int64_t)P.jmol * S.apv,
+                         c0, q0, P.fc, base);
         }
         if (F.agrid) continue;
         bool near = false;

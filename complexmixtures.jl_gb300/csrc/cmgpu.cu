@@ -207,7 +207,7 @@ struct cm_handle {
     // group tables
     DevBuf g_soff, g_sidx, g_voff, g_vidx;
     // ATOMS
-    DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, u64, rc, pcell, pq32, pq64,
+    DevBuf akey, atq32, atq64, asq32, asq64, acount, astart, afill, avcell, avq32, avq64, u64, u32, rc, pcell, pq32, pq64,
         anear, aq, aslot;
     int aq_cap = 0;
     int aslot_cap = 0;     // random-insertion slot list (slots of one placement piece)
@@ -848,6 +848,7 @@ void plan(cm_handle *h, const cm_frames *f) {
         dev_alloc(h, h->avq64, fc * h->Nv * 32);
         if (h->mddf) {
             dev_alloc(h, h->u64, fc * h->Nv * 32);
+            dev_alloc(h, h->u32, fc * h->Nv * 16);
             dev_alloc(h, h->rc, fc * mv * 4);
             // the work queue holds every slot of the samples placed in one launch
             const int64_t want = std::min<int64_t>((int64_t)kChunkSamples * mv, std::max<int64_t>(1 << 22, mv));
@@ -1078,6 +1079,7 @@ Bufs chunk_bufs(cm_handle *h, const Chunk &c, const FrameGeom *dG, const Sample 
         }
         if (h->mddf) {
             B.u64 = P<d4>(h->u64);
+            B.u32 = P<float4>(h->u32);
             B.rc = P<float>(h->rc);
             B.pcell = P<int>(h->pcell);
             B.pq32 = P<float4>(h->pq32);
@@ -1749,7 +1751,7 @@ void free_all(cm_handle *h) {
     DevBuf *all[] = {&h->geoms, &h->samples, &h->fscratch, &h->off64, &h->off32, &h->hist, &h->sums, &h->stats, &h->errflag, &h->hist_snap, &h->stats_snap,
                      &h->slot, &h->flags, &h->bulk, &h->nbulk, &h->tabs, &h->counters, &h->stage_s[0], &h->stage_s[1], &h->stage_v[0],
                      &h->stage_v[1], &h->scell, &h->sq32, &h->sq64, &h->so32, &h->so64, &h->vcell, &h->vq32, &h->vq64,
-                     &h->vo32, &h->vo64, &h->u64, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->eq, &h->rq, &h->akey, &h->atq32,
+                     &h->vo32, &h->vo64, &h->u64, &h->u32, &h->rc, &h->ccount, &h->cstart, &h->cfill, &h->cmol, &h->cq32, &h->gq, &h->eq, &h->rq, &h->akey, &h->atq32,
                      &h->atq64, &h->asq32, &h->asq64, &h->acount, &h->astart, &h->afill, &h->avcell, &h->avq32, &h->avq64,
                      &h->pcell, &h->pq32, &h->pq64, &h->anear, &h->aq, &h->g_soff, &h->g_sidx, &h->g_voff, &h->g_vidx,
                      &h->dcd_sidx, &h->dcd_vidx, &h->dcd_raw[0], &h->dcd_raw[1], &h->final_out, &h->final_job,
