@@ -682,6 +682,8 @@ __device__ __forceinline__ void k_atoms_eval_body(const uint3 blockIdx, const di
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float4 s_win[kAtomsWarps][32];  // atoms_walk_flat's window table, one per warp
     __shared__ float4 s_site[kAtomsWarps][kSiteGroup];  // site_group's table, one per warp
+    // an empty queue (every frame of the chunk decided on its candidate grid): nothing to add
+    if (B.counters[2] == 0) return;
     unsigned int *hbase = (unsigned int *)smem_raw;
     shist_zero(S, hbase);
     __syncthreads();
