@@ -712,8 +712,8 @@ __device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const di
     shist_flush(S, h, false);
 }
 
-// three resident CTAs per SM: the queries' registers (agrid_record is out of line)
-__global__ void __launch_bounds__(256, 3) k_agrid_real(DevSys S, Bufs B) {
+// four resident CTAs per SM: the queries wait on their list entries (agrid_record is out of line)
+__global__ void __launch_bounds__(256, 4) k_agrid_real(DevSys S, Bufs B) {
     k_agrid_real_body(blockIdx, gridDim, S, B);
 }
 
@@ -763,7 +763,7 @@ __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const 
     shist_flush(S, h, true);
 }
 
-__global__ void __launch_bounds__(256, 3) k_agrid_random(DevSys S, Bufs B, int sample0, int ny) {
+__global__ void __launch_bounds__(256, 4) k_agrid_random(DevSys S, Bufs B, int sample0, int ny) {
     k_agrid_random_body(blockIdx, gridDim, S, B, sample0, ny);
 }
 

@@ -104,12 +104,12 @@ __device__ __forceinline__ void mk_body(const uint3 vb, const dim3 vg, const MAr
     else if constexpr (KID == MK_EVAL_RANDOM_BALANCED) k_atoms_eval_body<true, true, kSchedBalanced>(vb, vg, a.S, a.B);
 }
 
-// Two resident CTAs per SM for the stages of up to 256 threads (three for the
+// Two resident CTAs per SM for the stages of up to 256 threads (four for the
 // candidate-grid queries, as their stand-alone kernels): the arguments now
 // come from the work table instead of the parameter space, and the register
 // budget of the stand-alone kernels is kept.
 __host__ __device__ constexpr int mk_min_ctas(int kid) {
-    return (kid == MK_AGRID_REAL || kid == MK_AGRID_RANDOM) ? 3 : mk_threads(kid) <= 256 ? 2 : 1;
+    return (kid == MK_AGRID_REAL || kid == MK_AGRID_RANDOM) ? 4 : mk_threads(kid) <= 256 ? 2 : 1;
 }
 
 template <int KID>
