@@ -733,12 +733,12 @@ __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const 
     const int apv = S.apv, iref = S.iref;
     (void)ny;
     const int n = min(B.counters[5], B.aslot_cap);
-    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
+    auto one_slot = [&](int it) {
         const int e = B.aslot[it];
         const int y = e / S.mv, k = e - y * S.mv;
         const int f = B.samples[sample0 + y].pad;
         const FrameScratch &F = B.FS[f];
-        if (!F.agrid) continue;
+        if (!F.agrid) return;
         const FrameGeom &G = B.G[f];
         const int64_t base = (int64_t)y * B.Nv + (int64_t)k * apv;
         Top2 T;
@@ -747,7 +747,7 @@ __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const 
         const float band = F.g.two_delta + 1e-3f * (1.0f + (float)S.cut);
         for (int b = 0; b < apv; ++b)
             agrid_query(B, G, F, f, B.pcell[base + b], B.pq32[base + b], b, b == iref, band, T, ev);
-        if (ev == 0) continue;
+        if (ev == 0) return;
         st.atompairs += (unsigned long long)ev;
         DirRec r;
         if (agrid_decide(S, F.g, T, (int64_t)k * apv, r) == 2)
@@ -757,6 +757,18 @@ __device__ __forceinline__ void k_agrid_random_body(const uint3 blockIdx, const 
             apply_hit(S, h, true, r.bin, r.i_local, r.j, r.ref, r.rbin);
             st.hits++;
         }
+    };
+    // warps take 32 listed slots at a time from counters[6] (zeroed with the
+    // slot list): the slots' costs vary with their lists, and a fixed share per
+    // thread left the CTAs' warps waiting for their slowest one
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int at = 0;
+        if (lane == 0) at = atomicAdd(B.counters + 6, 32);
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (at >= n) break;
+        if (at + lane < n) one_slot(at + lane);
+        __syncwarp();
     }
     stats_flush(S, st, true);
     __syncthreads();

@@ -1257,8 +1257,8 @@ void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, c
         em.kernel(MK_BULK, dim3(c.ntab), 0, CM_K_BULK, args(dtab + c.tab0, 0, 0, 0, 0));
         for (int s0 = 0; s0 < c.nsmp; s0 += h->atoms_piece) {
             const int ny = std::min(h->atoms_piece, c.nsmp - s0);
-            // the evaluation queue and the slot list (counters 2 .. 5)
-            em.zero(B.counters + 2, 4 * sizeof(int));
+            // the evaluation queue, the slot list and the queries' next slot (counters 2 .. 6)
+            em.zero(B.counters + 2, 5 * sizeof(int));
             // slots that can reach the solute, their FP64 placement on full
             // warps, then (candidate grid) their queries
             em.kernel(MK_SLOT_FILTER, dim3(grid_for(mv, 128), ny), 0, CM_K_RANDOM, args(nullptr, 0, 0, c.smp0 + s0, 0));
