@@ -361,15 +361,19 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
                         bk = min(kAgridBuckets - 1, max(0, (int)((dmin - L) * inv)));
                     }
                 }
-#pragma unroll
-                for (int b = 0; b < kAgridBuckets; ++b) {
-                    const unsigned m = __ballot_sync(0xffffffffu, bk == b);
-                    if (!m) continue;
-                    if (fill && bk == b) ent[s_pos[g][b] + __popc(m & below)] = p;
-                    __syncwarp();
-                    if (lane == 0) s_pos[g][b] += __popc(m);
-                    __syncwarp();
+                if (!__any_sync(0xffffffffu, bk >= 0)) continue;
+                // the lanes of each bucket: the lowest one advances the
+                // bucket's position, the others write after it in lane order
+                const unsigned m = __match_any_sync(0xffffffffu, bk);
+                const int leader = __ffs(m) - 1;
+                int at = 0;
+                if (bk >= 0 && lane == leader) {
+                    at = s_pos[g][bk];
+                    s_pos[g][bk] = at + __popc(m);
                 }
+                at = __shfl_sync(0xffffffffu, at, leader);
+                if (fill && bk >= 0) ent[at + __popc(m & below)] = p;
+                __syncwarp();
             }
         }
     };
@@ -674,7 +678,7 @@ __device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const di
     LocalStats st;
     const int apv = S.apv, iref = S.iref;
     const int64_t n = (int64_t)B.nf * S.mv;
-    for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n; it += (int64_t)gridDim.x * blockDim.x) {
+    auto one_molecule = [&](int64_t it) {
         const int f = (int)(it / S.mv), v = (int)(it - (int64_t)f * S.mv);
         const FrameScratch &F = B.FS[f];
         const FrameGeom &G = B.G[f];
@@ -682,10 +686,10 @@ __device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const di
         if (!F.agrid) {
             if (!F.ok) {
                 raise_err(S, ERR_STENCIL);
-                continue;
+                return;
             }
             if (atoms_near(B, G, f, 0, vc, apv)) atoms_push(S, B, make_int4(v, 0, f, 0));
-            continue;
+            return;
         }
         const float4 *vq = B.avq32 + (int64_t)f * B.Nv + (int64_t)v * apv;
         Top2 T;
@@ -693,7 +697,7 @@ __device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const di
         long long ev = 0;
         const float band = F.g.two_delta + 1e-3f * (1.0f + (float)S.cut);
         for (int b = 0; b < apv; ++b) agrid_query(B, G, F, f, vc[b], vq[b], b, b == iref, band, T, ev);
-        if (ev == 0) continue;
+        if (ev == 0) return;
         st.atompairs += (unsigned long long)ev;
         DirRec r;
         if (agrid_decide(S, F.g, T, (int64_t)v * apv, r) == 2) r = agrid_record(S, B, G, F, f, v, -1, vc, vq, T, st);
@@ -706,6 +710,17 @@ __device__ __forceinline__ void k_agrid_real_body(const uint3 blockIdx, const di
                 if (sl >= 0) B.flags[((int64_t)f * B.ndist + sl) * S.mv + v] = flag_code(r);
             }
         }
+    };
+    // warps take 32 molecules at a time from counters[6] (zeroed with the
+    // chunk's counters), as k_agrid_random takes its slots
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        long long at = 0;
+        if (lane == 0) at = (long long)atomicAdd((unsigned long long *)(B.counters + 6), 32ull);
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (at >= n) break;
+        if (at + lane < n) one_molecule(at + lane);
+        __syncwarp();
     }
     stats_flush(S, st, false);
     __syncthreads();

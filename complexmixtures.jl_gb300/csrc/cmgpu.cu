@@ -1235,12 +1235,13 @@ void atoms_chain(cm_handle *h, const Chunk &c, const DevSys &S, const Bufs &B, c
         // the single solute molecule's candidate lists of every frame
         em.zero(B.gpool, (size_t)nf * sizeof(int));
         em.kernel(MK_AGRID_BUILD, dim3(c.ncell_max, nf), (size_t)kAgridStage * sizeof(float4), CM_K_CELLS, base);
-        // real pass: every solvent molecule queried; records inside the band
-        // (and frames without a grid) go to the evaluation queue
+        // real pass: every solvent molecule queried (records inside the band
+        // decided in place); frames without a grid go to the evaluation queue.
+        // counters[6 .. 7]: the queries' next molecule (zeroed with the chunk's counters)
         em.zero(B.counters + 2, sizeof(int));
         em.kernel(MK_AGRID_REAL, dim3(agrid_grid((int64_t)nf * mv, h->agrid_real_ctas)), hsm, CM_K_REAL, base);
-        // the queue holds the records inside the band (about 1 %) unless a
-        // frame lost its grid: a grid for one entry per 32 molecules
+        // the queue is empty unless a frame lost its grid: a grid for one
+        // entry per 32 molecules
         em.kernel(eval_kid(h, false), dim3(wgrid_for((int64_t)nf * mv / 32)), hsm, CM_K_REAL, base);
     } else {
         // real pass: molecule pairs that can hold a pair within the cutoff,
