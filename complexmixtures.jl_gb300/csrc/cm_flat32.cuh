@@ -405,6 +405,7 @@ struct TileSmem {
     int cbeg[kTileCells];       // the cell's first position in the cell-sorted molecule table
     int code[kTileCells];       // the cell's packed stencil offset
     int next;                   // next home molecule to claim
+    int item;                   // the CTA's current (frame, home cell) item
 };
 
 __host__ __device__ constexpr size_t tile_smem_extra() { return sizeof(TileSmem) + 16; }
@@ -446,7 +447,14 @@ __global__ void __launch_bounds__(kTileWarps * 32, CM_TILE_MIN_CTAS) k_pairs_til
     const int aps = S.aps;
     const int64_t ncap = B.cs - 1;
     const int64_t items = (int64_t)B.nf * ncap;
-    for (int64_t t = blockIdx.x; t < items; t += gridDim.x) {
+    // CTAs claim (frame, home cell) items from counters[6] (zeroed with the
+    // chunk's counters): the items' costs vary with the cells' occupancy
+    for (;;) {
+        __syncthreads();  // the previous item's staged table and claim are no longer read
+        if (tid == 0) T.item = atomicAdd(B.counters + 6, 1);
+        __syncthreads();
+        const int64_t t = T.item;
+        if (t >= items) break;
         const int f = (int)(t / ncap), H = (int)(t - (int64_t)f * ncap);
         const PairsFrame Pf = pairs_frame(B, f, true);
         const FrameScratch &F = *Pf.F;
@@ -460,7 +468,6 @@ __global__ void __launch_bounds__(kTileWarps * 32, CM_TILE_MIN_CTAS) k_pairs_til
         const int K = (F.L[0] + 1) + (2 * F.L[0] + 1) * F.L[1] + (2 * F.L[0] + 1) * (2 * F.L[1] + 1) * F.L[2];
         const Guard g = F.g;
         const float4 *cq32 = B.cq32 + (int64_t)f * B.mv;
-        __syncthreads();  // the previous item's staged table is no longer read
         if (tid < K) {
             int dx, dy, dz;
             half_stencil_cell(tid, F.L, dx, dy, dz);
