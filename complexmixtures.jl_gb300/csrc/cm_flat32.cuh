@@ -841,7 +841,13 @@ __global__ void __launch_bounds__(kGuardWarps * 32) k_pairs_guard(DevSys S, Bufs
     pi.inv_pi = 1.0f / (float)pi.per_img;
     pi.inv_aps = 1.0f / (float)aps;
     const int n = min(B.counters[0], B.gq_cap);
-    for (int i = blockIdx.x * kGuardWarps + warp; i < n; i += gridDim.x * kGuardWarps) {
+    // warps claim records from counters[7] (zeroed with the chunk's
+    // counters): a record's cost varies with its exact scan
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(B.counters + 7, 1);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= n) break;
         const int4 it = B.gq[i];
         const int s = it.x, v = it.y, f = it.w;
         const PairsFrame Pf = pairs_frame(B, f, SELF);
