@@ -51,31 +51,6 @@ constexpr int kAgridRound = 4;         // stencil atoms each thread loads per st
 constexpr int kAgridBuildThreads = 256;
 
 // The fine cells of a search cell: edge vectors and bounds, FP32.
-struct FineCells {
-    int K, K3;
-    float e[9];  // column-major edge vectors of a fine cell (column k = search-cell edge k / K)
-    float h[3];  // orthogonal cells: half sides
-    float R;     // bounding-sphere radius (half the longest diagonal), rounded up
-    int ortho;
-};
-
-__device__ __forceinline__ FineCells fine_cells(const FrameGeom &G, const FrameScratch &F, int K) {
-    FineCells fc;
-    fc.K = K;
-    fc.K3 = K * K * K;
-    fc.ortho = F.ortho;
-    for (int i = 0; i < 9; ++i) fc.e[i] = (float)(G.Hn[i] / (double)K);
-    for (int k = 0; k < 3; ++k) fc.h[k] = (float)(0.5 * fabs(G.Hn[4 * k]) / (double)K) * (1.0f + 1e-6f);
-    double R = 0.0;
-    for (int m = 0; m < 4; ++m) {
-        double v[3];
-        matvec_cm(G.Hn, 1.0, (m & 1) ? -1.0 : 1.0, (m & 2) ? -1.0 : 1.0, v);
-        R = fmax(R, 0.5 * norm3d(v[0], v[1], v[2]) / (double)K);
-    }
-    fc.R = __double2float_ru(R * (1.0 + 1e-6) + 1e-6);
-    return fc;
-}
-
 // Largest distance from p to a point of the fine cell centred at c: squared
 // for orthogonal cells, the distance to the centre squared otherwise (the
 // bound is then that distance + R).
@@ -181,9 +156,9 @@ __device__ __forceinline__ void k_agrid_build_body(const uint3 blockIdx, const d
         const float4 o = off[s_oi[lo]];
         return make_float4(q.x + o.x, q.y + o.y, q.z + o.z, q.w);
     };
-    // the fine-cell geometry once per CTA (FP64 work), shared
+    // the frame's fine-cell geometry (k_frame_consts), shared
     __shared__ FineCells s_fc;
-    if (t == 0) s_fc = fine_cells(G, F, K);
+    if (t == 0) s_fc = F.fcells;
     __syncthreads();
     const FineCells fc = s_fc;
     auto centre = [&](int g, float *cen) {

@@ -105,6 +105,15 @@ struct GuardT {
 using Guard = GuardT<float>;
 using Guard64 = GuardT<double>;
 
+// Geometry of the candidate grid's fine cells (K^3 per search cell) of a frame.
+struct FineCells {
+    int K, K3;
+    float e[9];  // column-major edge vectors of a fine cell (column k = search-cell edge k / K)
+    float h[3];  // orthogonal cells: half sides
+    float R;     // bounding-sphere radius (half the longest diagonal), rounded up
+    int ortho;
+};
+
 // Per-frame values found by the prep kernels and the constants derived from
 // them by k_frame_consts (one block, before the search kernels).
 struct FrameScratch {
@@ -121,6 +130,7 @@ struct FrameScratch {
     float xmax;     // largest |coordinate component| of the frame's input atoms (rounded up)
     int tile;       // self mode, one image per pair, half stencil within kTileCells: the tiled real pass takes the frame
     int agrid;      // ATOMS, one solute molecule: the frame's candidate grid is complete (k_agrid_scan clears it on overflow)
+    FineCells fcells;  // the candidate grid's fine cells (when agrid)
     int place32;    // ATOMS, FP32 search: random-insertion slots placed in FP32 (placed_store32), the band widened to match
     Guard g;        // FP32 search
     Guard64 g64;    // FP64 search
@@ -1512,6 +1522,24 @@ __global__ void __launch_bounds__(128) k_random_eval(DevSys S, Bufs B) {
     shist_flush(S, h, true);
 }
 
+// The fine cells of a frame's candidate grid (FP64, once per frame).
+__device__ __forceinline__ FineCells fine_cells(const FrameGeom &G, const FrameScratch &F, int K) {
+    FineCells fc;
+    fc.K = K;
+    fc.K3 = K * K * K;
+    fc.ortho = F.ortho;
+    for (int i = 0; i < 9; ++i) fc.e[i] = (float)(G.Hn[i] / (double)K);
+    for (int k = 0; k < 3; ++k) fc.h[k] = (float)(0.5 * fabs(G.Hn[4 * k]) / (double)K) * (1.0f + 1e-6f);
+    double R = 0.0;
+    for (int m = 0; m < 4; ++m) {
+        double v[3];
+        matvec_cm(G.Hn, 1.0, (m & 1) ? -1.0 : 1.0, (m & 2) ? -1.0 : 1.0, v);
+        R = fmax(R, 0.5 * norm3d(v[0], v[1], v[2]) / (double)K);
+    }
+    fc.R = __double2float_ru(R * (1.0 + 1e-6) + 1e-6);
+    return fc;
+}
+
 // One block per frame computes the frame constants: stencils, the FP32 guard
 // band, and the slot table of the frame's sampled solute molecules.
 //
@@ -1590,6 +1618,7 @@ __device__ __forceinline__ void k_frame_consts_body(const uint3 blockIdx, const 
         F.tile = (pairs && S.self && multi == 0 && K <= kTileCells && S.mv < (1 << 24)) ? 1 : 0;
         F.ok = ok ? 1 : 0;
         F.agrid = (!pairs && B.agk > 0 && ok && (2 * La[0] + 1) * (2 * La[1] + 1) * (2 * La[2] + 1) <= kAgridMaxStencil) ? 1 : 0;
+        if (F.agrid) F.fcells = fine_cells(G, F, B.agk);
     }
     __syncthreads();
     if (lane < 16) {
