@@ -220,8 +220,9 @@ CM_HD bool disk_accept(int64_t a, int64_t b, uint64_t *sq) {
 // angle() for the FP32 search: the same draws and the same acceptance
 // (disk_accept), and (cos, sin) in FP32 within 3.01 u32 (u32 = 2^-24) of
 // angle()'s: cos = (a^2 - b^2) / X and sin = 2ab / X are the FP32 quotients of
-// the exact integers rounded to FP32 (3 u32 of the exact quotients), and
-// angle()'s FP64 values are within 6 2^-53 of the same quotients.
+// the integers (shifted right together below 2^64) rounded to FP32 (3 u32 of
+// the exact quotients, plus 2^-62), and angle()'s FP64 values are within
+// 6 2^-53 of the same quotients.
 CM_HD void angle32(uint64_t &s, float &c, float &sn) {
     for (int t = 0; t < 64; ++t) {
         const int64_t a = (int64_t)(next(s) >> 11) * 2 - (int64_t(1) << 53);
@@ -242,9 +243,16 @@ CM_HD void angle32(uint64_t &s, float &c, float &sn) {
         const uint64_t ma = a < 0 ? (uint64_t)(-a) : (uint64_t)a;
         const uint64_t mb = b < 0 ? (uint64_t)(-b) : (uint64_t)b;
         const uint64_t pl = ma * mb, ph = mulhi64(ma, mb);
-        const float d = u128_to_f32(xh, xl);
-        const float n = u128_to_f32(nh, nl);
-        const float m = u128_to_f32((ph << 1) | (pl >> 63), pl << 1);
+        const uint64_t mh = (ph << 1) | (pl >> 63), ml = pl << 1;
+        // |N|, M <= X: one right shift by k brings all three below 2^64; the
+        // bits shifted out move N / X and M / X by less than 2^-63
+        const int k = xh ? 64 - clz64(xh) : 0;
+        const uint64_t d64 = k ? (xl >> k) | (xh << (64 - k)) : xl;
+        const uint64_t n64 = k ? (nl >> k) | (nh << (64 - k)) : nl;
+        const uint64_t m64 = k ? (ml >> k) | (mh << (64 - k)) : ml;
+        const float d = u128_to_f32(0, d64);
+        const float n = u128_to_f32(0, n64);
+        const float m = u128_to_f32(0, m64);
         c = div32(nneg ? -n : n, d);
         sn = div32((a < 0) != (b < 0) ? -m : m, d);
         return;

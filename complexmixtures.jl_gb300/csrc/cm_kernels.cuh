@@ -905,10 +905,8 @@ __device__ __forceinline__ void load_xyz(const T *p, double *x) {
     x[2] = (double)p[2];
 }
 
-__device__ __forceinline__ void atomic_max_pos(float *addr, float v) { atomicMax((int *)addr, __float_as_int(v)); }
-
-// atomic_max_pos of the largest value over the calling warp's active lanes
-// (one atomic per warp).
+// Atomic maximum of a nonnegative float (its bits order as int) of the largest
+// value over the calling warp's active lanes (one atomic per warp).
 __device__ __forceinline__ void warp_max_pos(float *addr, float v) {
     const unsigned mask = __activemask();
     const int m = __reduce_max_sync(mask, __float_as_int(v));
@@ -1761,7 +1759,7 @@ __device__ __forceinline__ void k_prep_atoms_solvent_body(const uint3 blockIdx, 
             B.u32[fo + (int64_t)m * apm + b] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
         }
         B.rc[(int64_t)f * B.mv + m] = r;
-        atomic_max_pos(&B.FS[f].rcmax, r);
+        warp_max_pos(&B.FS[f].rcmax, r);
     }
 }
 
